@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Benchmark of the q-LSKUM primal iteration on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision mixed|fp64] [--workload transonic|subsonic]
+
+Workload (default "transonic"): a seeded NACA 0012 point cloud, 1024 wall
+points x 1000 rings = 1,024,000 points (first spacing 2e-3 chord, far field
+20 chords, 10% jitter, 10 neighbours), M 0.85, AoA 1, CFL 0.2, VL_CONST 50,
+limiter on, 3 inner iterations.  A step is one pseudo-time iteration of the
+whole cloud (4 SSPRK stages).  Metric: point-iterations per second.
+
+Our arm prints one JSON line with the mixed-precision solve as `value` (or
+FP64 with --precision fp64) and, beside it, the FP64 drop-in's rate and the
+Cl / Cd difference between the two forms after the same iterations, the
+end-to-end rate through the C ABI with host buffers, the roofline of the
+dominant kernel and the CPU baseline (the C restatement oracle on the host
+cores).  `--impl reference` times the reference algorithm on the host cores
+(the oracle restatement: the reference's own sources are not on this
+machine) and prints the same metric.
+
+Multi-GPU: the path does not shard (one cloud per solve); with --gpus N every
+rank runs an independent replica and `value` is the sum over ranks
+("replicas only", weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(REPO, "c-_serial_gb300"), os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "transonic": dict(cloud=dict(n_wall=1024, n_layers=1000, first_spacing=2e-3, radius=20.0, seed=2),
+                      solver=dict(mach=0.85, aoa=1.0, cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=3)),
+    "subsonic": dict(cloud=dict(n_wall=160, n_layers=60, first_spacing=2e-3, radius=20.0, seed=1),
+                     solver=dict(mach=0.63, aoa=2.0, cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=0)),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                for line in out.stdout.strip().splitlines():
+                    self.rows.append([v.strip() for v in line.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in self.rows for j in range(4) if len(r) > 5 + j and r[5 + j] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_cloud(workload):
+    from qlskum import cloudgen
+    return cloudgen.make_cloud(**WORKLOADS[workload]["cloud"])
+
+
+def flux_update_bytes(cloud, precision: str) -> float:
+    """Compulsory bytes one fused flux + update launch moves (each array once).
+
+    Per point: own q / dq / qm, normal, limiter eps^2, delta, flag, nbhs,
+    four directional LSQ moment sets (4 x double4), prim in, prim out, q out,
+    prim_old on 1 stage of 4 (averaged), slice base; per edge: neighbour index,
+    edge vector / weights, rotated weights, membership byte.  Neighbour
+    gathers are served from cache (counted once, as the point's own rows).
+    """
+    n = cloud.n
+    e = int(cloud.nbhs.sum())
+    if precision == "mixed":
+        per_pt = 16 + 32 + 32 + 16 + 4 + 8 + 1 + 4 + 128 + 32 + 32 + 16 + 32 / 4 + 8 / 32
+        per_edge = 4 + 16 + 8 + 1
+    else:
+        per_pt = 32 + 64 + 64 + 16 + 8 + 8 + 1 + 4 + 128 + 32 + 32 + 32 + 32 / 4 + 8 / 32
+        per_edge = 4 + 32 + 16 + 1
+    return n * per_pt + e * per_edge
+
+
+def time_solver(qlskum, torch, solver, steps):
+    """Device time of `steps` iterations on the solver's own stream (CUDA events)."""
+    stream = torch.cuda.ExternalStream(solver.stream)
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    solver.synchronize()
+    l0 = solver.launches
+    start.record(stream)
+    solver.q_lskum(steps)
+    end.record(stream)
+    end.synchronize()
+    solver.synchronize()
+    return start.elapsed_time(end) / 1e3, solver.launches - l0
+
+
+def e2e_rate(qlskum, solver, n, steps):
+    """Point-iter/s through the C ABI with host buffers: per step, upload prim
+    from pinned host memory, one fpi_solver iteration, read back prim and the
+    residual."""
+    import torch
+    host = torch.empty((n, 4), dtype=torch.float64).pin_memory()
+    host.copy_(torch.from_numpy(solver.prim))
+    out = torch.empty((n, 4), dtype=torch.float64).pin_memory()
+    arr_in = host.numpy()
+    arr_out = out.numpy()
+    import ctypes as C
+    it0 = solver.iteration
+    solver.synchronize()
+    t0 = time.perf_counter()
+    for s in range(steps):
+        solver.set_prim(arr_in)
+        solver.fpi_solver(it0 + s + 1)
+        solver._ck(solver._L.qlskum_get_prim(solver._h, arr_out.ctypes.data_as(C.POINTER(C.c_double))))
+        res = solver.residual_history()[-1]
+        arr_in = arr_out
+    dt = time.perf_counter() - t0
+    _ = res
+    return n * steps / dt, 32 * n, 32 * n + 24 * (it0 + steps)
+
+
+def cpu_baseline(workload, cloud, threads, iters):
+    import qlskum_oracle
+    qlskum_oracle.build()
+    kw = WORKLOADS[workload]["solver"]
+    o = qlskum_oracle.Oracle(cloud, mach=kw["mach"], aoa=kw["aoa"], cfl=kw["cfl"], vl_const=kw["vl_const"],
+                             power=kw["power"], inner_iterations=kw["inner_iterations"], threads=threads)
+    t0 = time.perf_counter()
+    o.run(iters)
+    dt = time.perf_counter() - t0
+    return cloud.n * iters / dt, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import qlskum_oracle
+    qlskum_oracle.build()
+    threads = os.cpu_count() or 1
+    workload = args.workload
+    sample = workload
+    if args.steps + args.warmup > 30 and workload == "transonic":
+        sample = "subsonic"  # bounded: the 9,600-point cloud of the same recipe
+    cloud = make_cloud(sample)
+    kw = WORKLOADS[sample]["solver"]
+    o = qlskum_oracle.Oracle(cloud, mach=kw["mach"], aoa=kw["aoa"], cfl=kw["cfl"], vl_const=kw["vl_const"],
+                             power=kw["power"], inner_iterations=kw["inner_iterations"], threads=threads)
+    o.run(args.warmup)
+    t0 = time.perf_counter()
+    o.run(args.steps)
+    dt = time.perf_counter() - t0
+    v = cloud.n * args.steps / dt
+    line = {
+        "impl": "reference", "metric": "point-iter/s", "value": v, "unit": "point-iter/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(workload, cloud if sample == workload else None),
+        "cpu_baseline": {"value": v, "unit": "point-iter/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} cloud ({cloud.n} points), {args.steps} iterations, C restatement "
+                                   f"of the reference's serial FP64 path with OpenMP over points"},
+        "e2e": {"value": v, "unit": "point-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(workload, cloud=None):
+    w = WORKLOADS[workload]
+    c = dict(workload=f"naca0012_{w['cloud']['n_wall']}x{w['cloud']['n_layers']}", **w["solver"])
+    c["points"] = w["cloud"]["n_wall"] * w["cloud"]["n_layers"]
+    c["l2"] = "inputs larger than L2 (edge arrays alone > 129 MB); no flush" if workload == "transonic" else \
+        "inputs smaller than L2"
+    return c
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--workload", default="transonic", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import qlskum
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+    qlskum.load()
+    t_gen = time.perf_counter()
+    cloud = make_cloud(args.workload)
+    log(f"cloud {cloud.n} points generated in {time.perf_counter() - t_gen:.1f}s")
+    kw = WORKLOADS[args.workload]["solver"]
+    prec = qlskum.MIXED if args.precision == "mixed" else qlskum.FP64
+    solver = qlskum.Solver(cloud, precision=prec, **kw)
+    solver.q_lskum(args.warmup)
+    solver.synchronize()
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    with ClockSampler(local) as clocks:
+        dt, launches = time_solver(qlskum, torch, solver, args.steps)
+    barrier()
+    if pg:
+        t = torch.tensor([dt], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        dt = float(t.item())
+    value = cloud.n * args.steps * world / dt
+    cl, cd, cm, ent = solver.objective()
+
+    # per-kernel device time of the dominant kernel (events around each launch)
+    solver.set_kernel_timing(True)
+    solver.q_lskum(2)
+    kt = solver.kernel_timing()
+    solver.set_kernel_timing(False)
+    fl_ms, fl_n = kt["flux_update"]
+    total_ms = sum(v[0] for v in kt.values())
+    peak, peak_kind = measured_peaks()
+    nbytes = flux_update_bytes(cloud, args.precision)
+    achieved = nbytes / (fl_ms / fl_n / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": f"k_flux_update ({args.precision})",
+                "algorithmic_bytes_per_launch": nbytes, "avg_launch_ms": fl_ms / fl_n,
+                "kernel_share": fl_ms / total_ms, "peak_source": f"{peak_kind} hbm_gbs"}
+
+    # the other form on the same cloud and iteration count, for the ratio and the Cl / Cd gap
+    other = qlskum.FP64 if prec == qlskum.MIXED else qlskum.MIXED
+    s2 = qlskum.Solver(cloud, precision=other, **kw)
+    s2.q_lskum(args.warmup)
+    dt2, _ = time_solver(qlskum, torch, s2, args.fp64_steps if other == qlskum.FP64 else args.steps)
+    n2 = args.fp64_steps if other == qlskum.FP64 else args.steps
+    v2 = cloud.n * n2 * world / dt2
+    s2.q_lskum(args.steps - n2) if args.steps > n2 else None
+    cl2, cd2, cm2, ent2 = s2.objective()
+    fp64_value, mixed_value = (v2, value) if other == qlskum.FP64 else (value, v2)
+    compare = {"fp64_point_iter_s": fp64_value, "mixed_point_iter_s": mixed_value,
+               "mixed_over_fp64": mixed_value / fp64_value,
+               "after_iterations": args.warmup + args.steps,
+               "cl": cl, "cd": cd, "abs_dcl": abs(cl - cl2), "abs_dcd": abs(cd - cd2)}
+    del s2
+
+    # end to end through the C ABI with host buffers
+    e2e_steps = max(3, min(args.steps, 10))
+    e2e_v, h2d, d2h = e2e_rate(qlskum, solver, cloud.n, e2e_steps)
+    e2e_v *= world
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        thr = os.cpu_count() or 1
+        cv, cdt = cpu_baseline(args.workload, cloud, thr, 1)
+        cpu = {"value": cv, "unit": "point-iter/s", "cores": thr, "kind": "port",
+               "sample": f"1 iteration of the same {cloud.n}-point cloud ({cdt:.1f}s), C restatement of the "
+                         f"reference's serial FP64 path, OpenMP over points"}
+
+    if rank == 0:
+        line = {
+            "metric": "point-iter/s", "value": value, "unit": "point-iter/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": dict(workload_config(args.workload), precision=args.precision,
+                           parallelism="replicas" if world > 1 else "single"),
+            "clocks": clocks.summary(), "gpu_launches": launches,
+            "e2e": {"value": e2e_v, "unit": "point-iter/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": roofline, "cpu_baseline": cpu, "fp64_vs_mixed": compare,
+            "kernel_ms_per_iteration": {k: v[0] / max(1, 2) for k, v in kt.items()},
+        }
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,490 @@
+// FP64 kernels: the drop-in form of the q-LSKUM primal iteration.
+//
+// Built with -fmad=false so that no multiply-add is contracted: every
+// expression keeps the reference's rounding sequence and the results differ
+// from the serial reference only through the device's exp / log / erf.
+//
+// One thread per point; the point's edges are walked in the reference's
+// neighbour order from the sliced-ELL edge arrays (coalesced across the warp),
+// neighbour state is gathered through L1/L2 (points are Morton ordered, so
+// most neighbours of a block's points are cache-resident).  All geometry that
+// does not change between iterations (edge vectors, least-squares moments,
+// 1/det, limiter epsilon) is precomputed on the host in the reference's
+// operation order, which on this chip trades a few bytes per edge for FP64
+// instructions, its scarce resource.
+#include "qlskum_math.cuh"
+
+namespace qlskum {
+namespace fp64 {
+
+static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
+
+// ----------------------------------------------------------------- q, c
+
+// q_variables_mod.h:9-34
+__global__ void k_q_variables(int n, const double4_32a *__restrict__ prim, double4_32a *__restrict__ q)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double P[4], Q[4];
+    ld4(prim[i], P);
+    prim_to_q(P[0], P[1], P[2], P[3], Q);
+    q[i] = mk4(Q);
+}
+
+// q and the wave speed of the current state (both read by the next stage's
+// gradient kernel).
+__global__ void k_derived(int n, const double4_32a *__restrict__ prim, double4_32a *__restrict__ q, double *__restrict__ cs)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double P[4], Q[4];
+    ld4(prim[i], P);
+    prim_to_q(P[0], P[1], P[2], P[3], Q);
+    q[i] = mk4(Q);
+    cs[i] = wave_speed(P);
+}
+
+// ----------------------------------------------------------- gradients
+
+// q_variables_mod.h:36-118 (+ state_update_mod.h:448-496 when delta != null):
+// qm = neighbour max/min, dq = least-squares gradient with the precomputed
+// moments {sxx, syy, sxy, 1/det}.
+__global__ void k_q_derivatives(DevCloud c, const double4_32a *__restrict__ q, double4_32a *__restrict__ dq,
+                                double4_32a *__restrict__ qm, const double *__restrict__ cs, double *__restrict__ delta,
+                                double cfl)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    double qi[4], qmax[4], qmin[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    ld4(q[i], qi);
+#pragma unroll
+    for (int r = 0; r < 4; r++) { qmax[r] = qi[r]; qmin[r] = qi[r]; }
+    double min_delt = 1.0;
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const double4_32a g = c.e_geo[e];
+        double qk[4];
+        ld4(q[k], qk);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            if (qk[r] > qmax[r]) qmax[r] = qk[r];
+            if (qk[r] < qmin[r]) qmin[r] = qk[r];
+            sdx[r] = sdx[r] + g.z * (qk[r] - qi[r]);
+            sdy[r] = sdy[r] + g.w * (qk[r] - qi[r]);
+        }
+        if (delta) {
+            double delta_t = c.e_dist[e] / cs[k];
+            delta_t = cfl * delta_t;
+            if (min_delt > delta_t) min_delt = delta_t;
+        }
+    }
+    const double4_32a m = c.ggeo[i];  // sxx, syy, sxy, 1/det
+    double dx[4], dy[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        dx[r] = (sdx[r] * m.y - sdy[r] * m.z) * m.w;
+        dy[r] = (sdy[r] * m.x - sdx[r] * m.z) * m.w;
+    }
+    dq[2 * i] = mk4(dx);
+    dq[2 * i + 1] = mk4(dy);
+    qm[2 * i] = mk4(qmax);
+    qm[2 * i + 1] = mk4(qmin);
+    if (delta) delta[i] = min_delt;
+}
+
+// q_variables_mod.h:120-213: defect-corrected gradient from q shifted half an
+// edge on both ends; writes to dq_out (ping-pong replaces the copy-back of
+// eval_update_innerloop).
+__global__ void k_q_inner(DevCloud c, const double4_32a *__restrict__ q, const double4_32a *__restrict__ dq_in,
+                          double4_32a *__restrict__ dq_out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    double qi[4], dxi[4], dyi[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    ld4(q[i], qi);
+    ld4(dq_in[2 * i], dxi);
+    ld4(dq_in[2 * i + 1], dyi);
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const double4_32a g = c.e_geo[e];
+        double qk[4], dxk[4], dyk[4];
+        ld4(q[k], qk);
+        ld4(dq_in[2 * k], dxk);
+        ld4(dq_in[2 * k + 1], dyk);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            double temp1 = qi[r] - 0.5 * (g.x * dxi[r] + g.y * dyi[r]);
+            double temp2 = qk[r] - 0.5 * (g.x * dxk[r] + g.y * dyk[r]);
+            sdx[r] = sdx[r] + (g.z * (temp2 - temp1));
+            sdy[r] = sdy[r] + (g.w * (temp2 - temp1));
+        }
+    }
+    const double4_32a m = c.ggeo[i];
+    double dx[4], dy[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        dx[r] = m.w * (sdx[r] * m.y - sdy[r] * m.z);
+        dy[r] = m.w * (sdy[r] * m.x - sdx[r] * m.z);
+    }
+    dq_out[2 * i] = mk4(dx);
+    dq_out[2 * i + 1] = mk4(dy);
+}
+
+// state_update_mod.h:448-496, wave speed evaluated per edge as the reference does.
+__global__ void k_func_delta(DevCloud c, const double4_32a *__restrict__ prim, double *__restrict__ delta, double cfl)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    double min_delt = 1.0;
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        double P[4];
+        ld4(prim[c.e_nbr[e]], P);
+        double delta_t = c.e_dist[e] / wave_speed(P);
+        delta_t = cfl * delta_t;
+        if (min_delt > delta_t) min_delt = delta_t;
+    }
+    delta[i] = min_delt;
+}
+
+// ------------------------------------------------------------- flux
+
+// The four directional flux derivatives of point i (interior_/wall_/
+// outer_fluxes_mod.h), walked edge by edge: each edge's limited end states
+// are reconstructed once and feed every sub-stencil the edge belongs to,
+// in the reference's neighbour order, so the sums are the reference's.
+// G[d] returns the solved derivative of sub-stencil d (xpos, xneg, ypos,
+// yneg); unused directions are left at 0.
+__device__ __forceinline__ void point_flux(const DevCloud &c, int i, int f, double nx, double ny,
+                                           const double4_32a *__restrict__ q, const double4_32a *__restrict__ dq,
+                                           const double4_32a *__restrict__ qm, double G[4][4])
+{
+    double qi[4], dxi[4], dyi[4], mxi[4], mni[4];
+    ld4(q[i], qi);
+    ld4(dq[2 * i], dxi);
+    ld4(dq[2 * i + 1], dyi);
+    ld4(qm[2 * i], mxi);
+    ld4(qm[2 * i + 1], mni);
+    const double e2i = c.eps2[i];
+    double sx[4][4], sy[4][4];
+#pragma unroll
+    for (int d = 0; d < 4; d++)
+#pragma unroll
+        for (int r = 0; r < 4; r++) { sx[d][r] = 0.0; sy[d][r] = 0.0; }
+
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const double4_32a g = c.e_geo[e];
+        const double2 sw = c.e_sn[e];
+        const unsigned dir = c.e_dir[e];
+        double qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
+        ld4(q[k], qk);
+        ld4(dq[2 * k], dxk);
+        ld4(dq[2 * k + 1], dyk);
+        ld4(qm[2 * k], mxk);
+        ld4(qm[2 * k + 1], mnk);
+        double Pi[4], Pk[4];
+        edge_states<double>(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, c.eps2[k], Pi, Pk);
+        Kin<double> ki, kk;
+        kin_prep<double>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
+        kin_prep<double>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
+#define QLSKUM_ACC(D)                                                         \
+        if (dir & (1u << D)) {                                                \
+            double Gi[4], Gk[4];                                              \
+            dir_flux<double, D>(f, ki, Gi);                                   \
+            dir_flux<double, D>(f, kk, Gk);                                   \
+            _Pragma("unroll") for (int r = 0; r < 4; r++) {                   \
+                sx[D][r] = sx[D][r] + (Gk[r] - Gi[r]) * sw.x;                 \
+                sy[D][r] = sy[D][r] + (Gk[r] - Gi[r]) * sw.y;                 \
+            }                                                                 \
+        }
+        QLSKUM_ACC(0)
+        QLSKUM_ACC(1)
+        QLSKUM_ACC(2)
+        QLSKUM_ACC(3)
+#undef QLSKUM_ACC
+    }
+#pragma unroll
+    for (int d = 0; d < 4; d++) {
+        const double4_32a m = c.fgeo[4 * i + d];  // sxx, syy, sxy, 1/det
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+            G[d][r] = (d < 2) ? (sx[d][r] * m.y - sy[d][r] * m.z) * m.w
+                              : (sy[d][r] * m.x - sx[d][r] * m.z) * m.w;
+    }
+}
+
+// flux_residual_mod.h:18-87
+__device__ __forceinline__ void combine(int f, double delta, const double G[4][4], double F[4])
+{
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        if (f == kWall) F[j] = (2.0 * delta) * (G[0][j] + G[1][j] + G[3][j]);
+        else if (f == kInterior) F[j] = delta * (G[0][j] + G[1][j] + G[2][j] + G[3][j]);
+        else F[j] = delta * (G[0][j] + G[1][j] + G[2][j]);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_flux_residual(DevCloud c, const double4_32a *__restrict__ q,
+                                                       const double4_32a *__restrict__ dq, const double4_32a *__restrict__ qm,
+                                                       const double *__restrict__ delta, double4_32a *__restrict__ flux_res)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const int f = c.flag[i];
+    const double2 nn = c.nrm[i];
+    double G[4][4], F[4];
+    point_flux(c, i, f, nn.x, nn.y, q, dq, qm, G);
+    combine(f, delta[i], G, F);
+    flux_res[i] = mk4(F);
+}
+
+// state_update_mod.h:92-283 over all points, prim in place, with the
+// residual partial sums of each block.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_state_update(DevCloud c, CaseConst K, double4_32a *__restrict__ prim,
+                                                        const double4_32a *__restrict__ prim_old,
+                                                        const double4_32a *__restrict__ flux_res, int rk,
+                                                        double *__restrict__ psum, double *__restrict__ pmax)
+{
+    int i = blockIdx.x * BLOCK + threadIdx.x;
+    double r2 = 0.0;
+    if (i < c.n) {
+        const int f = c.flag[i];
+        const double2 nn = c.nrm[i];
+        double P[4], F[4];
+        ld4(prim[i], P);
+        ld4(flux_res[i], F);
+        r2 = stage_update(K, f, nn.x, nn.y, P, prim_old + i, F, rk);
+        prim[i] = mk4(P);
+    }
+    block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
+}
+
+// Fused stage: flux residual + SSPRK update of point i, then q and (after the
+// last stage) the wave speed of the new state for the next stage's kernels.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_flux_update(DevCloud c, CaseConst K, const double4_32a *__restrict__ q,
+                                                       const double4_32a *__restrict__ dq,
+                                                       const double4_32a *__restrict__ qm,
+                                                       const double *__restrict__ delta,
+                                                       const double4_32a *__restrict__ prim,
+                                                       const double4_32a *__restrict__ prim_old,
+                                                       double4_32a *__restrict__ prim_next, double4_32a *__restrict__ q_next,
+                                                       double *__restrict__ cs_next, int rk,
+                                                       double *__restrict__ psum, double *__restrict__ pmax)
+{
+    int i = blockIdx.x * BLOCK + threadIdx.x;
+    double r2 = 0.0;
+    if (i < c.n) {
+        const int f = c.flag[i];
+        const double2 nn = c.nrm[i];
+        double G[4][4], F[4], P[4], Q[4];
+        point_flux(c, i, f, nn.x, nn.y, q, dq, qm, G);
+        combine(f, delta[i], G, F);
+        ld4(prim[i], P);
+        r2 = stage_update(K, f, nn.x, nn.y, P, prim_old + i, F, rk);
+        prim_next[i] = mk4(P);
+        prim_to_q(P[0], P[1], P[2], P[3], Q);
+        q_next[i] = mk4(Q);
+        if (cs_next) cs_next[i] = wave_speed(P);
+    }
+    if (psum) block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
+}
+
+// fpi_solver_mod.h:138-147: res_new = sqrt(sum)/n, residue against res_old
+// latched at iterations 1 and 2; one block, fixed summation order.
+__global__ void k_reduce_residual(int nblocks, const double *__restrict__ psum, const double *__restrict__ pmax,
+                                  int n, int it_arg, double *hist, int capacity, double *res_old, int *iter,
+                                  int *status)
+{
+    __shared__ double ss[256], sm[256];
+    double v = 0.0, m = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += 256) {
+        v += psum[b];
+        m = pmax[b] > m ? pmax[b] : m;
+    }
+    ss[threadIdx.x] = v;
+    sm[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            ss[threadIdx.x] += ss[threadIdx.x + s];
+            sm[threadIdx.x] = sm[threadIdx.x + s] > sm[threadIdx.x] ? sm[threadIdx.x + s] : sm[threadIdx.x];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int it = it_arg > 0 ? it_arg : *iter + 1;
+        double res_new = sqrt(ss[0]) / n;
+        double residue;
+        if (it <= 2) {
+            *res_old = res_new;
+            residue = 0;
+        } else {
+            residue = log10(res_new / *res_old);
+        }
+        if (it - 1 < capacity && it >= 1) {
+            hist[3 * (it - 1)] = res_new;
+            hist[3 * (it - 1) + 1] = residue;
+            hist[3 * (it - 1) + 2] = sm[0];
+        }
+        *iter = it;
+        if (!isfinite(res_new)) *status = 1;
+    }
+}
+
+__global__ void k_copy(int n, const double4_32a *__restrict__ src, double4_32a *__restrict__ dst)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+
+// compute_force_coeffs_mod.h:37-72 per wall point and compute_entropy_mod.h:
+// 17-21 per point, then ordered tree sums in one block.
+// wall_geo: {ds, nx, ny, ...} is precomputed per shape point: x = ds,
+// y = mx - 0.25, z = my; normals come from the cloud.
+__global__ void k_objective(DevCloud c, const double4_32a *__restrict__ prim, const int *__restrict__ wall_perm,
+                            const double4_32a *__restrict__ wall_geo, int n_wall, double cp_scale, double pr_inf,
+                            double gamma, double *__restrict__ entropy, double *__restrict__ out4)
+{
+    __shared__ double sh[3][256], se[256];
+    double H = 0, V = 0, Mo = 0, E = 0;
+    for (int j = threadIdx.x; j < n_wall; j += 256) {
+        const int m = wall_perm[j];
+        const double4_32a w = wall_geo[j];
+        const double2 nn = c.nrm[m];
+        double cp = prim[m].w - pr_inf;
+        cp = -cp / cp_scale;
+        H = H + cp * nn.x * w.x;
+        V = V + cp * nn.y * w.x;
+        Mo = Mo + (-cp * nn.y * w.x * w.y + cp * nn.x * w.x * w.z);
+    }
+    const double temp2 = log(pr_inf);
+    for (int k = threadIdx.x; k < c.n; k += 256) {
+        const double4_32a P = prim[k];
+        double temp1 = pow(P.x, gamma);
+        temp1 = P.w / temp1;
+        temp1 = log(temp1);
+        const double s = fabs(temp1 - temp2);
+        entropy[k] = s;
+        E = E + s;
+    }
+    sh[0][threadIdx.x] = H;
+    sh[1][threadIdx.x] = V;
+    sh[2][threadIdx.x] = Mo;
+    se[threadIdx.x] = E;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + s];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + s];
+            sh[2][threadIdx.x] += sh[2][threadIdx.x + s];
+            se[threadIdx.x] += se[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out4[0] = sh[0][0];
+        out4[1] = sh[1][0];
+        out4[2] = sh[2][0];
+        out4[3] = se[0];
+    }
+}
+
+// ------------------------------------------------------------- launchers
+
+#define QLSKUM_LAUNCHED(L) \
+    do { if ((L).launches) ++*(L).launches; } while (0)
+
+void q_variables(const Launch &L, const DevCloud &c, const double4_32a *prim, double4_32a *q)
+{
+    k_q_variables<<<grid_for(c.n, 256), 256, 0, L.stream>>>(c.n, prim, q);
+    QLSKUM_LAUNCHED(L);
+}
+
+void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, double4_32a *q, double *cspeed)
+{
+    k_derived<<<grid_for(c.n, 256), 256, 0, L.stream>>>(c.n, prim, q, cspeed);
+    QLSKUM_LAUNCHED(L);
+}
+
+void q_derivatives(const Launch &L, const DevCloud &c, const double4_32a *q, double4_32a *dq, double4_32a *qm,
+                   const double *cspeed, double *delta, double cfl)
+{
+    k_q_derivatives<<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
+    QLSKUM_LAUNCHED(L);
+}
+
+void q_inner(const Launch &L, const DevCloud &c, const double4_32a *q, const double4_32a *dq_in, double4_32a *dq_out)
+{
+    k_q_inner<<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq_in, dq_out);
+    QLSKUM_LAUNCHED(L);
+}
+
+void func_delta(const Launch &L, const DevCloud &c, const double4_32a *prim, double *delta, double cfl)
+{
+    k_func_delta<<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, prim, delta, cfl);
+    QLSKUM_LAUNCHED(L);
+}
+
+void flux_residual(const Launch &L, const DevCloud &c, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
+                   const double *delta, double4_32a *flux_res)
+{
+    k_flux_residual<<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq, qm, delta, flux_res);
+    QLSKUM_LAUNCHED(L);
+}
+
+void state_update(const Launch &L, const DevCloud &c, const CaseConst &k, double4_32a *prim, const double4_32a *prim_old,
+                  const double4_32a *flux_res, int rk, const Reduce &R)
+{
+    k_state_update<128><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, k, prim, prim_old, flux_res, rk,
+                                                                   R.partial_sum, R.partial_max);
+    QLSKUM_LAUNCHED(L);
+}
+
+void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const double4_32a *q, const double4_32a *dq,
+                 const double4_32a *qm, const double *delta, const double4_32a *prim, const double4_32a *prim_old,
+                 double4_32a *prim_next, double4_32a *q_next, double *cspeed_next, int rk, const Reduce &R)
+{
+    k_flux_update<128><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, k, q, dq, qm, delta, prim, prim_old, prim_next,
+                                                                  q_next, cspeed_next, rk, R.partial_sum,
+                                                                  R.partial_max);
+    QLSKUM_LAUNCHED(L);
+}
+
+void reduce_residual(const Launch &L, const Reduce &R, int n, int it)
+{
+    k_reduce_residual<<<1, 256, 0, L.stream>>>(R.blocks, R.partial_sum, R.partial_max, n, it, R.hist, R.capacity,
+                                               R.res_old, R.iter, R.status);
+    QLSKUM_LAUNCHED(L);
+}
+
+void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
+{
+    k_copy<<<grid_for(n, 256), 256, 0, L.stream>>>(n, src, dst);
+    QLSKUM_LAUNCHED(L);
+}
+
+void objective(const Launch &L, const DevCloud &c, const double4_32a *prim, const int *wall_perm, const double4_32a *wall_geo,
+               int n_wall, double cp_scale, double pr_inf, double gamma, double *entropy, double *out4, double *)
+{
+    k_objective<<<1, 256, 0, L.stream>>>(c, prim, wall_perm, wall_geo, n_wall, cp_scale, pr_inf, gamma, entropy,
+                                         out4);
+    QLSKUM_LAUNCHED(L);
+}
+
+}  // namespace fp64
+}  // namespace qlskum

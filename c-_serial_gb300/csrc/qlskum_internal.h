@@ -1,0 +1,125 @@
+// Internal layout shared by the host layer (qlskum_host.cpp) and the CUDA
+// translation units.  Plain structs of device pointers; no torch types.
+//
+// Device layout (all arrays in the permuted point order, np = n rounded up to
+// a multiple of 32):
+//   * per point: flag (int8), nbhs (int32), normal (double2), eps^2 of the
+//     Venkatakrishnan limiter (double), gradient LSQ moments
+//     {sxx, syy, sxy, 1/det} (double4_32a) and the same for the four flux
+//     sub-stencils (double4_32a [np][4]);
+//   * per edge, in a sliced-ELL ("warp-padded CSR") layout: slice s holds 32
+//     consecutive points; edge j of lane l of slice s sits at
+//     slice_base[s] + 32*j + l, so the 32 threads of a warp read edge j of
+//     their points with one coalesced access.  Per edge: neighbour (int32),
+//     {delx, dely, w*delx, w*dely} (double4_32a), {dels*w, deln*w} of the rotated
+//     frame (double2), |r_k - r_i| (double), sub-stencil membership bits
+//     (uint8: 1 xpos, 2 xneg, 4 ypos, 8 yneg);
+//   * state, point-major AoS per field: prim / q (double4_32a), dq and qm
+//     (2 x double4_32a per point: d/dx then d/dy, max then min).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace qlskum {
+
+enum : int { kWall = 0, kInterior = 1, kOuter = 2 };
+enum : unsigned { kXpos = 1u, kXneg = 2u, kYpos = 4u, kYneg = 8u };
+
+struct DevCloud {
+    int n = 0;
+    int np = 0;
+    const int8_t *flag = nullptr;
+    const int *nbhs = nullptr;
+    const long long *slice_base = nullptr;   // [np/32]
+    const int *e_nbr = nullptr;
+    const double4_32a *e_geo = nullptr;          // delx, dely, w*delx, w*dely
+    const double2 *e_sn = nullptr;           // dels*w, deln*w
+    const double *e_dist = nullptr;          // |r_k - r_i|
+    const uint8_t *e_dir = nullptr;
+    const double2 *nrm = nullptr;
+    const double *eps2 = nullptr;
+    const double4_32a *ggeo = nullptr;           // [np]
+    const double4_32a *fgeo = nullptr;           // [np][4]
+    // mixed-precision copies of the per-edge geometry (FP32)
+    const float4 *e_geo32 = nullptr;         // delx, dely, w*delx, w*dely
+    const float2 *e_sn32 = nullptr;          // dels*w, deln*w
+    const float *eps2_32 = nullptr;
+};
+
+// Free-stream constants of one case (parameter_mod.h:4-30).
+struct CaseConst {
+    double mach, theta, rho_inf, pr_inf, gamma, pi;
+    double u1_inf, u2_inf;
+    double cfl;
+};
+
+// FP64 state buffers of one handle.
+struct State64 {
+    double4_32a *prim[3] = {nullptr, nullptr, nullptr};
+    double4_32a *q[2] = {nullptr, nullptr};
+    double4_32a *dq[2] = {nullptr, nullptr};     // [np][2] each
+    double4_32a *qm = nullptr;                   // [np][2]
+    double4_32a *flux_res = nullptr;
+    double *delta = nullptr;
+    double *cspeed = nullptr;                // |u| + 3 sqrt(p/rho) of the current prim
+};
+
+// Mixed-precision state: q, dq, qm in FP32, prim in FP64.
+struct State32 {
+    float4 *q[2] = {nullptr, nullptr};
+    float4 *dq[2] = {nullptr, nullptr};      // [np][2]
+    float4 *qm = nullptr;                    // [np][2]
+};
+
+// Residual reduction scratch.
+struct Reduce {
+    double *partial_sum = nullptr;           // [blocks]
+    double *partial_max = nullptr;           // [blocks]
+    double *hist = nullptr;                  // [capacity][3]: res_new, residue, max_res
+    double *res_old = nullptr;               // [1]
+    int *iter = nullptr;                     // [1] iterations completed
+    int *status = nullptr;                   // [1] 0 ok, 1 non-finite residual
+    int capacity = 0;
+    int blocks = 0;
+};
+
+struct Launch {
+    cudaStream_t stream = nullptr;
+    int block = 128;
+    long long *launches = nullptr;           // host counter
+};
+
+// ---------------------------------------------------------- FP64 kernels (qlskum_fp64.cu)
+namespace fp64 {
+void q_variables(const Launch &L, const DevCloud &c, const double4_32a *prim, double4_32a *q);
+void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, double4_32a *q, double *cspeed);
+void q_derivatives(const Launch &L, const DevCloud &c, const double4_32a *q, double4_32a *dq, double4_32a *qm,
+                   const double *cspeed, double *delta, double cfl);
+void q_inner(const Launch &L, const DevCloud &c, const double4_32a *q, const double4_32a *dq_in, double4_32a *dq_out);
+void func_delta(const Launch &L, const DevCloud &c, const double4_32a *prim, double *delta, double cfl);
+void flux_residual(const Launch &L, const DevCloud &c, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
+                   const double *delta, double4_32a *flux_res);
+void state_update(const Launch &L, const DevCloud &c, const CaseConst &k, double4_32a *prim, const double4_32a *prim_old,
+                  const double4_32a *flux_res, int rk, const Reduce &R);
+void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const double4_32a *q, const double4_32a *dq,
+                 const double4_32a *qm, const double *delta, const double4_32a *prim, const double4_32a *prim_old,
+                 double4_32a *prim_next, double4_32a *q_next, double *cspeed_next, int rk, const Reduce &R);
+void reduce_residual(const Launch &L, const Reduce &R, int n, int it);
+void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
+// objectives: per-wall-point contributions then ordered tree sums
+void objective(const Launch &L, const DevCloud &c, const double4_32a *prim, const int *wall_perm, const double4_32a *wall_geo,
+               int n_wall, double cp_scale, double pr_inf, double gamma, double *entropy, double *out4, double *scratch);
+}  // namespace fp64
+
+// ---------------------------------------------------------- mixed kernels (qlskum_mixed.cu)
+namespace mixed {
+void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, float4 *q, double *cspeed);
+void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *dq, float4 *qm,
+                   const double *cspeed, double *delta, double cfl);
+void q_inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, float4 *dq_out);
+void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const float4 *q, const float4 *dq,
+                 const float4 *qm, const double *delta, const double4_32a *prim, const double4_32a *prim_old,
+                 double4_32a *prim_next, float4 *q_next, double *cspeed_next, int rk, const Reduce &R);
+}  // namespace mixed
+
+}  // namespace qlskum

@@ -1,0 +1,328 @@
+// Per-point and per-edge arithmetic of the q-LSKUM scheme, templated on the
+// real type R so the FP64 translation unit (built with -fmad=false, every
+// expression in the reference's own operation order) and the mixed-precision
+// unit (FP32 with FMA contraction) share one source.
+//
+// Each function names the reference lines it restates.  Where the reference
+// writes `a - b` for the negative half-range we write `a + s*b` with s = -1:
+// IEEE subtraction is addition of the negation and s*b is exact, so the FP64
+// results are the reference's bit for bit apart from the device libm.
+#pragma once
+#include <cuda_runtime.h>
+#include "qlskum_internal.h"
+
+namespace qlskum {
+
+template <typename R> struct M;
+template <> struct M<double> {
+    static __device__ __forceinline__ double ex(double x) { return exp(x); }
+    static __device__ __forceinline__ double lg(double x) { return log(x); }
+    static __device__ __forceinline__ double ef(double x) { return erf(x); }
+    static __device__ __forceinline__ double sq(double x) { return sqrt(x); }
+    static __device__ __forceinline__ double ab(double x) { return fabs(x); }
+};
+template <> struct M<float> {
+    static __device__ __forceinline__ float ex(float x) { return expf(x); }
+    static __device__ __forceinline__ float lg(float x) { return logf(x); }
+    static __device__ __forceinline__ float ef(float x) { return erff(x); }
+    static __device__ __forceinline__ float sq(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ float ab(float x) { return fabsf(x); }
+};
+
+// 4 * atan(1.0) of parameter_mod.h:10, as a literal.
+#define QLSKUM_PI 3.141592653589793
+
+template <typename R> struct V4 { R v[4]; };
+
+__device__ __forceinline__ void ld4(const double4_32a &a, double o[4]) { o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; }
+__device__ __forceinline__ void ld4(const float4 &a, float o[4]) { o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; }
+__device__ __forceinline__ double4_32a mk4(const double o[4]) { return make_double4_32a(o[0], o[1], o[2], o[3]); }
+__device__ __forceinline__ float4 mk4(const float o[4]) { return make_float4(o[0], o[1], o[2], o[3]); }
+
+// q_variables_mod.h:19-33: q from (rho, u1, u2, p).
+template <typename R>
+__device__ __forceinline__ void prim_to_q(R rho, R u1, R u2, R pr, R q[4])
+{
+    R beta = R(0.5) * rho / pr;
+    q[0] = M<R>::lg(rho) + (M<R>::lg(beta) * R(2.5)) - beta * (u1 * u1 + u2 * u2);
+    R two_times_beta = R(2.0) * beta;
+    q[1] = two_times_beta * u1;
+    q[2] = two_times_beta * u2;
+    q[3] = -two_times_beta;
+}
+
+// limiters_mod.h:64-104: Venkatakrishnan limiter of one component.
+// `eps2` is (pow(VL_CONST * min_dist, 3))^2 of the point the state belongs to.
+template <typename R>
+__device__ __forceinline__ R venkat(R qt, R q, R qmax, R qmin, R eps2)
+{
+    R del_neg = qt - q;
+    if (M<R>::ab(del_neg) <= R(10e-6)) return R(1.0);
+    R del_pos = (del_neg > R(0)) ? qmax - q : qmin - q;
+    R num = (del_pos * del_pos) + eps2;
+    num = num * del_neg + R(2.0) * del_neg * del_neg * del_pos;
+    R den = del_pos * del_pos + R(2.0) * del_neg * del_neg;
+    den = den + del_neg * del_pos + eps2;
+    den = den * del_neg;
+    R temp = num / den;
+    return temp < R(1) ? temp : R(1);
+}
+
+// q_variables_mod.h:230-253
+template <typename R>
+__device__ __forceinline__ void qtilde_to_prim(const R qt[4], R &u1, R &u2, R &rho, R &pr)
+{
+    R beta = -qt[3] * R(0.5);
+    R temp = R(0.5) / beta;
+    u1 = qt[1] * temp;
+    u2 = qt[2] * temp;
+    R temp1 = qt[0] + beta * (u1 * u1 + u2 * u2);
+    R temp2 = temp1 - (M<R>::lg(beta) / (R(1.4) - R(1)));
+    rho = M<R>::ex(temp2);
+    pr = rho * temp;
+}
+
+// Half-range moments of one state in the point's (t, n) frame, shared by all
+// split and quadrant fluxes that state enters (split_fluxes_mod.h:14-26,
+// quadrant_fluxes_mod.h:14-29).
+template <typename R> struct Kin {
+    R rho, ut, un, pbr, usq, B1, B2, E1, E2;
+};
+
+template <typename R>
+__device__ __forceinline__ void kin_prep(R nx, R ny, R u1, R u2, R rho, R pr, Kin<R> &k)
+{
+    R tx = ny, ty = -nx;
+    k.ut = u1 * tx + u2 * ty;
+    k.un = u1 * nx + u2 * ny;
+    R beta = R(0.5) * rho / pr;
+    R sb = M<R>::sq(beta);
+    R spb = M<R>::sq(R(QLSKUM_PI) * beta);
+    R S1 = k.ut * sb;
+    R S2 = k.un * sb;
+    k.B1 = R(0.5) * M<R>::ex(-S1 * S1) / spb;
+    k.B2 = R(0.5) * M<R>::ex(-S2 * S2) / spb;
+    k.E1 = M<R>::ef(S1);
+    k.E2 = M<R>::ef(S2);
+    k.pbr = pr / rho;
+    k.usq = k.ut * k.ut + k.un * k.un;
+    k.rho = rho;
+}
+
+// flux_Gxp (s1 = +1) / flux_Gxn (s1 = -1): split_fluxes_mod.h:6-84
+template <typename R>
+__device__ __forceinline__ void flux_x(const Kin<R> &k, R s1, R G[4])
+{
+    R A1 = R(0.5) * (R(1.0) + s1 * k.E1);
+    R B1 = s1 * k.B1;
+    G[0] = k.rho * (k.ut * A1 + B1);
+    R temp1 = k.pbr + k.ut * k.ut;
+    R temp2 = temp1 * A1 + k.ut * B1;
+    G[1] = k.rho * temp2;
+    temp1 = k.ut * k.un * A1 + k.un * B1;
+    G[2] = k.rho * temp1;
+    temp1 = (R(7.0) * k.pbr) + k.usq;
+    temp2 = R(0.5) * k.ut * temp1 * A1;
+    temp1 = (R(6.0) * k.pbr) + k.usq;
+    G[3] = k.rho * (temp2 + R(0.5) * temp1 * B1);
+}
+
+// flux_Gyp (s2 = +1) / flux_Gyn (s2 = -1): split_fluxes_mod.h:86-164
+template <typename R>
+__device__ __forceinline__ void flux_y(const Kin<R> &k, R s2, R G[4])
+{
+    R A2 = R(0.5) * (R(1.0) + s2 * k.E2);
+    R B2 = s2 * k.B2;
+    G[0] = k.rho * (k.un * A2 + B2);
+    R temp1 = k.pbr + k.un * k.un;
+    R temp2 = temp1 * A2 + k.un * B2;
+    G[2] = k.rho * temp2;
+    temp1 = k.ut * k.un * A2 + k.ut * B2;
+    G[1] = k.rho * temp1;
+    temp1 = (R(7.0) * k.pbr) + k.usq;
+    temp2 = R(0.5) * k.un * temp1 * A2;
+    temp1 = (R(6.0) * k.pbr) + k.usq;
+    G[3] = k.rho * (temp2 + R(0.5) * temp1 * B2);
+}
+
+// flux_quad_GxI (-,-), GxII (+,-), GxIII (+,+), GxIV (-,+):
+// quadrant_fluxes_mod.h:6-211, s1 the t half-range sign, s2 the n one.
+template <typename R>
+__device__ __forceinline__ void flux_quad(const Kin<R> &k, R s1, R s2, R G[4])
+{
+    R A1 = R(0.5) * (R(1.0) + s1 * k.E1);
+    R A2 = R(0.5) * (R(1.0) + s2 * k.E2);
+    R B1 = s1 * k.B1;
+    R f1 = k.ut * A1 + B1;
+    G[0] = k.rho * A2 * f1;
+    R temp1 = k.pbr + k.ut * k.ut;
+    R temp2 = temp1 * A1 + k.ut * B1;
+    G[1] = k.rho * A2 * temp2;
+    temp2 = k.un * A2 + s2 * k.B2;
+    G[2] = k.rho * f1 * temp2;
+    temp1 = (R(7.0) * k.pbr) + k.usq;
+    temp2 = R(0.5) * k.ut * temp1 * A1;
+    temp1 = (R(6.0) * k.pbr) + k.usq;
+    R temp3 = R(0.5) * k.B1 * temp1;
+    R temp4 = R(0.5) * k.rho * k.un * k.B2 * f1;
+    G[3] = k.rho * A2 * (temp2 + s1 * temp3) + s2 * temp4;
+}
+
+// Flux at one end of an edge for sub-stencil d of a point of class f
+// (flux_residual_mod.h:18-87 picks the function per class and direction).
+template <typename R, int D>
+__device__ __forceinline__ void dir_flux(int f, const Kin<R> &k, R G[4])
+{
+    if (D <= 1) {
+        const R s1 = (D == 0) ? R(1) : R(-1);
+        if (f == kInterior) flux_x(k, s1, G);
+        else flux_quad(k, s1, (f == kOuter) ? R(1) : R(-1), G);
+    } else {
+        flux_y(k, (D == 2) ? R(1) : R(-1), G);
+    }
+}
+
+// Limited reconstruction of both ends of edge (i, k) and their primitive
+// states (interior_fluxes_mod.h:50-89 and the identical blocks of the wall
+// and outer modules).  g = (delx, dely).
+template <typename R>
+__device__ __forceinline__ void edge_states(R delx, R dely, const R qi[4], const R dxi[4], const R dyi[4],
+                                            const R mxi[4], const R mni[4], R e2i, const R qk[4],
+                                            const R dxk[4], const R dyk[4], const R mxk[4], const R mnk[4],
+                                            R e2k, R pi_[4], R pk_[4])
+{
+    R ti[4], tk[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        R gi = delx * dxi[r] + dely * dyi[r];
+        R gk = delx * dxk[r] + dely * dyk[r];
+        R phi_i = venkat(qi[r] - R(0.5) * gi, qi[r], mxi[r], mni[r], e2i);
+        R phi_k = venkat(qk[r] - R(0.5) * gk, qk[r], mxk[r], mnk[r], e2k);
+        ti[r] = qi[r] - R(0.5) * phi_i * gi;
+        tk[r] = qk[r] - R(0.5) * phi_k * gk;
+    }
+    qtilde_to_prim(ti, pi_[1], pi_[2], pi_[0], pi_[3]);
+    qtilde_to_prim(tk, pk_[1], pk_[2], pk_[0], pk_[3]);
+}
+
+// state_update_mod.h:18-33
+__device__ __forceinline__ void primitive_to_conserved(const double P[4], double nx, double ny, double U[4])
+{
+    double rho = P[0];
+    U[0] = rho;
+    double temp1 = rho * P[1];
+    double temp2 = rho * P[2];
+    U[3] = 2.5 * P[3] + 0.5 * (temp1 * temp1 + temp2 * temp2) / rho;
+    U[1] = temp1 * ny - temp2 * nx;
+    U[2] = temp1 * nx + temp2 * ny;
+}
+
+// state_update_mod.h:35-90
+__device__ __forceinline__ void conserved_vector_Ubar(const CaseConst &K, const double P[4], double nx, double ny,
+                                                      double Ubar[4])
+{
+    const double gamma_new = K.gamma, rho_inf = K.rho_inf, pr_inf = K.pr_inf, pi = K.pi;
+    double tx = ny, ty = -nx;
+    double u1_inf_rot = K.u1_inf * tx + K.u2_inf * ty;
+    double u2_inf_rot = K.u1_inf * nx + K.u2_inf * ny;
+    double temp1 = (u1_inf_rot * u1_inf_rot + u2_inf_rot * u2_inf_rot);
+    double e_inf = pr_inf / (rho_inf * (gamma_new - 1.0)) + 0.5 * (temp1);
+    double beta = (0.5 * rho_inf) / pr_inf;
+    double S2 = u2_inf_rot * sqrt(beta);
+    double B2_inf = exp(-S2 * S2) / (2.0 * sqrt(pi * beta));
+    double A2n_inf = 0.5 * (1.0 - erf(S2));
+    double rho = P[0], u1 = P[1], u2 = P[2], pr = P[3];
+    double u1_rot = u1 * tx + u2 * ty;
+    double u2_rot = u1 * nx + u2 * ny;
+    temp1 = (u1_rot * u1_rot + u2_rot * u2_rot);
+    double e = pr / (rho * (gamma_new - 1.0)) + 0.5 * (temp1);
+    beta = (rho) / (2.0 * pr);
+    S2 = u2_rot * sqrt(beta);
+    double B2 = exp(-S2 * S2) / (2.0 * sqrt(pi * beta));
+    double A2p = 0.5 * (1.0 + erf(S2));
+    Ubar[0] = (rho_inf * A2n_inf) + (rho * A2p);
+    Ubar[1] = (rho_inf * u1_inf_rot * A2n_inf) + (rho * u1_rot * A2p);
+    temp1 = rho_inf * (u2_inf_rot * A2n_inf - B2_inf);
+    double temp2 = rho * (u2_rot * A2p + B2);
+    Ubar[2] = temp1 + temp2;
+    temp1 = (rho_inf * A2n_inf * e_inf - 0.5 * rho_inf * u2_inf_rot * B2_inf);
+    temp2 = (rho * A2p * e + 0.5 * rho * u2_rot * B2);
+    Ubar[3] = temp1 + temp2;
+}
+
+// One SSPRK stage of one point (state_update_mod.h:111-282).  P is updated in
+// place; returns the point's res_sqr (0 on outer points, which the reference
+// leaves out of the residual).
+__device__ __forceinline__ double stage_update(const CaseConst &K, int f, double nx, double ny, double P[4],
+                                               const double4_32a *prim_old_i, const double F[4], int rk)
+{
+    const double obt = 1.0 / 3.0, tbt = 2.0 / 3.0, euler = 1.0;
+    double U[4], U_old[4];
+    if (f == kOuter) conserved_vector_Ubar(K, P, nx, ny, U);
+    else primitive_to_conserved(P, nx, ny, U);
+    double temp = U[0];
+    if (rk != 3) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) U[j] = U[j] - (0.5 * euler * F[j]);
+    } else {
+        double Po[4];
+        ld4(*prim_old_i, Po);
+        if (f == kOuter) conserved_vector_Ubar(K, Po, nx, ny, U_old);
+        else primitive_to_conserved(Po, nx, ny, U_old);
+#pragma unroll
+        for (int j = 0; j < 4; j++) U[j] = tbt * U_old[j] + obt * (U[j] - 0.5 * F[j]);
+    }
+    if (f == kWall) U[2] = 0.;
+    double U2_rot = U[1], U3_rot = U[2];
+    U[1] = U2_rot * ny + U3_rot * nx;
+    U[2] = U3_rot * ny - U2_rot * nx;
+    double res_sqr = (f == kOuter) ? 0.0 : (U[0] - temp) * (U[0] - temp);
+    P[0] = U[0];
+    temp = 1.0 / U[0];
+    P[1] = U[1] * temp;
+    P[2] = U[2] * temp;
+    P[3] = 0.4 * U[3] - (0.2 * temp) * (U[1] * U[1] + U[2] * U[2]);
+    return res_sqr;
+}
+
+// |u| + 3 sqrt(p / rho) of state_update_mod.h:483-485, the denominator of the
+// local time step a neighbour contributes.
+__device__ __forceinline__ double wave_speed(const double P[4])
+{
+    double mod_u = sqrt(P[1] * P[1] + P[2] * P[2]);
+    return mod_u + 3.0 * sqrt(P[3] / P[0]);
+}
+
+// Deterministic block reduction (sum and max) of one value per thread.
+template <int BLOCK>
+__device__ __forceinline__ void block_sum_max(double v, double m, double *out_sum, double *out_max)
+{
+    __shared__ double ss[BLOCK / 32], sm[BLOCK / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v += __shfl_down_sync(0xffffffffu, v, o);
+        double t = __shfl_down_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { ss[w] = v; sm[w] = m; }
+    __syncthreads();
+    if (w == 0) {
+        v = (l < BLOCK / 32) ? ss[l] : 0.0;
+        m = (l < BLOCK / 32) ? sm[l] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            v += __shfl_down_sync(0xffffffffu, v, o);
+            double t = __shfl_down_sync(0xffffffffu, m, o);
+            m = t > m ? t : m;
+        }
+        if (l == 0) { *out_sum = v; *out_max = m; }
+    }
+}
+
+__device__ __forceinline__ long long ell(const DevCloud &c, int i, int j)
+{
+    return c.slice_base[i >> 5] + 32LL * j + (i & 31);
+}
+
+}  // namespace qlskum

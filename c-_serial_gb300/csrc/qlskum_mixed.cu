@@ -1,0 +1,243 @@
+// Mixed-precision kernels: q variables, the Venkatakrishnan limiter, the
+// reconstruction and the kinetic split fluxes in FP32; the 2x2
+// least-squares solves (their determinants are near-singular on anisotropic
+// wall stencils), the flux residual, the SSPRK update and the residual sum in
+// FP64.  Same algorithm, edge order and data layout as the FP64 kernels
+// (qlskum_fp64.cu); q, dq and qm are stored in FP32, which halves the bytes
+// gathered per neighbour, and FP32 runs at many times the FP64 rate on this
+// chip.  Built with FMA contraction on.
+#include "qlskum_math.cuh"
+
+namespace qlskum {
+namespace mixed {
+
+static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
+
+__device__ __forceinline__ void q_of(const double P[4], float Q[4])
+{
+    prim_to_q<float>((float)P[0], (float)P[1], (float)P[2], (float)P[3], Q);
+}
+
+__global__ void k_derived(int n, const double4_32a *__restrict__ prim, float4 *__restrict__ q, double *__restrict__ cs)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double P[4];
+    float Q[4];
+    ld4(prim[i], P);
+    q_of(P, Q);
+    q[i] = mk4(Q);
+    cs[i] = wave_speed(P);
+}
+
+// q_variables_mod.h:36-118: FP32 differences and sums, FP64 solve.
+__global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4 *__restrict__ dq,
+                                float4 *__restrict__ qm, const double *__restrict__ cs, double *__restrict__ delta,
+                                double cfl)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    float qi[4], qmax[4], qmin[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    ld4(q[i], qi);
+#pragma unroll
+    for (int r = 0; r < 4; r++) { qmax[r] = qi[r]; qmin[r] = qi[r]; }
+    double min_delt = 1.0;
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const float4 g = c.e_geo32[e];
+        float qk[4];
+        ld4(q[k], qk);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            qmax[r] = fmaxf(qmax[r], qk[r]);
+            qmin[r] = fminf(qmin[r], qk[r]);
+            sdx[r] += g.z * (qk[r] - qi[r]);
+            sdy[r] += g.w * (qk[r] - qi[r]);
+        }
+        if (delta) {
+            double delta_t = cfl * (c.e_dist[e] / cs[k]);
+            min_delt = delta_t < min_delt ? delta_t : min_delt;
+        }
+    }
+    const double4_32a m = c.ggeo[i];
+    float dx[4], dy[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        dx[r] = (float)(((double)sdx[r] * m.y - (double)sdy[r] * m.z) * m.w);
+        dy[r] = (float)(((double)sdy[r] * m.x - (double)sdx[r] * m.z) * m.w);
+    }
+    dq[2 * i] = mk4(dx);
+    dq[2 * i + 1] = mk4(dy);
+    qm[2 * i] = mk4(qmax);
+    qm[2 * i + 1] = mk4(qmin);
+    if (delta) delta[i] = min_delt;
+}
+
+// q_variables_mod.h:120-213
+__global__ void k_q_inner(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ dq_in,
+                          float4 *__restrict__ dq_out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    float qi[4], dxi[4], dyi[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    ld4(q[i], qi);
+    ld4(dq_in[2 * i], dxi);
+    ld4(dq_in[2 * i + 1], dyi);
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const float4 g = c.e_geo32[e];
+        float qk[4], dxk[4], dyk[4];
+        ld4(q[k], qk);
+        ld4(dq_in[2 * k], dxk);
+        ld4(dq_in[2 * k + 1], dyk);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            float t1 = qi[r] - 0.5f * (g.x * dxi[r] + g.y * dyi[r]);
+            float t2 = qk[r] - 0.5f * (g.x * dxk[r] + g.y * dyk[r]);
+            sdx[r] += g.z * (t2 - t1);
+            sdy[r] += g.w * (t2 - t1);
+        }
+    }
+    const double4_32a m = c.ggeo[i];
+    float dx[4], dy[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        dx[r] = (float)(m.w * ((double)sdx[r] * m.y - (double)sdy[r] * m.z));
+        dy[r] = (float)(m.w * ((double)sdy[r] * m.x - (double)sdx[r] * m.z));
+    }
+    dq_out[2 * i] = mk4(dx);
+    dq_out[2 * i + 1] = mk4(dy);
+}
+
+// Fused stage: FP32 edge work, FP64 solve / residual / update.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_flux_update(DevCloud c, CaseConst K, const float4 *__restrict__ q,
+                                                       const float4 *__restrict__ dq, const float4 *__restrict__ qm,
+                                                       const double *__restrict__ delta,
+                                                       const double4_32a *__restrict__ prim,
+                                                       const double4_32a *__restrict__ prim_old,
+                                                       double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
+                                                       double *__restrict__ cs_next, int rk,
+                                                       double *__restrict__ psum, double *__restrict__ pmax)
+{
+    int i = blockIdx.x * BLOCK + threadIdx.x;
+    double r2 = 0.0;
+    if (i < c.n) {
+        const int f = c.flag[i];
+        const double2 nn = c.nrm[i];
+        const float nx = (float)nn.x, ny = (float)nn.y;
+        float qi[4], dxi[4], dyi[4], mxi[4], mni[4];
+        ld4(q[i], qi);
+        ld4(dq[2 * i], dxi);
+        ld4(dq[2 * i + 1], dyi);
+        ld4(qm[2 * i], mxi);
+        ld4(qm[2 * i + 1], mni);
+        const float e2i = c.eps2_32[i];
+        float sx[4][4], sy[4][4];
+#pragma unroll
+        for (int d = 0; d < 4; d++)
+#pragma unroll
+            for (int r = 0; r < 4; r++) { sx[d][r] = 0.f; sy[d][r] = 0.f; }
+        const int nb = c.nbhs[i];
+        const long long base = c.slice_base[i >> 5] + (i & 31);
+        for (int j = 0; j < nb; j++) {
+            const long long e = base + 32LL * j;
+            const int k = c.e_nbr[e];
+            const float4 g = c.e_geo32[e];
+            const float2 sw = c.e_sn32[e];
+            const unsigned dir = c.e_dir[e];
+            float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
+            ld4(q[k], qk);
+            ld4(dq[2 * k], dxk);
+            ld4(dq[2 * k + 1], dyk);
+            ld4(qm[2 * k], mxk);
+            ld4(qm[2 * k + 1], mnk);
+            float Pi[4], Pk[4];
+            edge_states<float>(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, c.eps2_32[k], Pi, Pk);
+            Kin<float> ki, kk;
+            kin_prep<float>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
+            kin_prep<float>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
+#define QLSKUM_ACC32(D)                                                       \
+            if (dir & (1u << D)) {                                            \
+                float Gi[4], Gk[4];                                           \
+                dir_flux<float, D>(f, ki, Gi);                                \
+                dir_flux<float, D>(f, kk, Gk);                                \
+                _Pragma("unroll") for (int r = 0; r < 4; r++) {               \
+                    sx[D][r] += (Gk[r] - Gi[r]) * sw.x;                       \
+                    sy[D][r] += (Gk[r] - Gi[r]) * sw.y;                       \
+                }                                                             \
+            }
+            QLSKUM_ACC32(0)
+            QLSKUM_ACC32(1)
+            QLSKUM_ACC32(2)
+            QLSKUM_ACC32(3)
+#undef QLSKUM_ACC32
+        }
+        double G[4][4];
+#pragma unroll
+        for (int d = 0; d < 4; d++) {
+            const double4_32a m = c.fgeo[4 * i + d];
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+                G[d][r] = (d < 2) ? ((double)sx[d][r] * m.y - (double)sy[d][r] * m.z) * m.w
+                                  : ((double)sy[d][r] * m.x - (double)sx[d][r] * m.z) * m.w;
+        }
+        const double dl = delta[i];
+        double F[4], P[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (f == kWall) F[j] = (2.0 * dl) * (G[0][j] + G[1][j] + G[3][j]);
+            else if (f == kInterior) F[j] = dl * (G[0][j] + G[1][j] + G[2][j] + G[3][j]);
+            else F[j] = dl * (G[0][j] + G[1][j] + G[2][j]);
+        }
+        ld4(prim[i], P);
+        r2 = stage_update(K, f, nn.x, nn.y, P, prim_old + i, F, rk);
+        prim_next[i] = mk4(P);
+        float Q[4];
+        q_of(P, Q);
+        q_next[i] = mk4(Q);
+        if (cs_next) cs_next[i] = wave_speed(P);
+    }
+    if (psum) block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
+}
+
+#define QLSKUM_LAUNCHED(L) \
+    do { if ((L).launches) ++*(L).launches; } while (0)
+
+void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, float4 *q, double *cspeed)
+{
+    k_derived<<<grid_for(c.n, 256), 256, 0, L.stream>>>(c.n, prim, q, cspeed);
+    QLSKUM_LAUNCHED(L);
+}
+
+void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *dq, float4 *qm, const double *cspeed,
+                   double *delta, double cfl)
+{
+    k_q_derivatives<<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
+    QLSKUM_LAUNCHED(L);
+}
+
+void q_inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, float4 *dq_out)
+{
+    k_q_inner<<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq_in, dq_out);
+    QLSKUM_LAUNCHED(L);
+}
+
+void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const float4 *q, const float4 *dq,
+                 const float4 *qm, const double *delta, const double4_32a *prim, const double4_32a *prim_old,
+                 double4_32a *prim_next, float4 *q_next, double *cspeed_next, int rk, const Reduce &R)
+{
+    k_flux_update<128><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, k, q, dq, qm, delta, prim, prim_old, prim_next,
+                                                                  q_next, cspeed_next, rk, R.partial_sum,
+                                                                  R.partial_max);
+    QLSKUM_LAUNCHED(L);
+}
+
+}  // namespace mixed
+}  // namespace qlskum

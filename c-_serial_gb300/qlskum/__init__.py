@@ -1,0 +1,249 @@
+"""Python front end of the GB300 q-LSKUM library (ctypes over include/qlskum.h).
+
+`Solver` mirrors the reference's module API (Pathlessbark8/C-_serial): one
+method per module function, with the state resident on the GPU.  The CUDA
+library is built in-tree (qlskum.build) and loaded from
+c-_serial_gb300/_build/libqlskum.so; there is no CPU fallback -- importing a
+missing or unbuildable library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+FP64 = 0
+MIXED = 1
+
+FIELD_PRIM, FIELD_PRIM_OLD, FIELD_Q, FIELD_DQ, FIELD_QM, FIELD_FLUX_RES, FIELD_DELTA, FIELD_NORMALS, FIELD_ENTROPY = range(9)
+_FIELD_SHAPE = {FIELD_PRIM: (4,), FIELD_PRIM_OLD: (4,), FIELD_Q: (4,), FIELD_DQ: (2, 4), FIELD_QM: (2, 4),
+                FIELD_FLUX_RES: (4,), FIELD_DELTA: (), FIELD_NORMALS: (2,), FIELD_ENTROPY: ()}
+
+STATUS = {0: "ok", 1: "invalid", 2: "degenerate stencil", 3: "non-finite state", 4: "CUDA error", 5: "unsupported"}
+
+
+class QlskumError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"qlskum {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class CloudStruct(C.Structure):
+    _fields_ = [("n", C.c_int),
+                ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),
+                ("left", C.POINTER(C.c_int)), ("right", C.POINTER(C.c_int)),
+                ("flag_1", C.POINTER(C.c_int)), ("flag_2", C.POINTER(C.c_int)),
+                ("min_dist", C.POINTER(C.c_double)),
+                ("nbhs", C.POINTER(C.c_int)), ("conn", C.POINTER(C.c_int))]
+
+
+class ParamsStruct(C.Structure):
+    _fields_ = [("mach", C.c_double), ("aoa", C.c_double), ("cfl", C.c_double), ("vl_const", C.c_double),
+                ("power", C.c_double), ("inner_iterations", C.c_int), ("precision", C.c_int),
+                ("block_size", C.c_int), ("reorder", C.c_int), ("verbose", C.c_int)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_needed: bool = True):
+    """Load libqlskum.so (building it first if missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build_if_needed else _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"libqlskum.so not found at {path}; run qlskum.build.build()")
+    L = C.CDLL(path)
+    H = C.c_void_p
+    i = C.c_int
+    dp = C.POINTER(C.c_double)
+    ip = C.POINTER(C.c_int)
+    sig = {
+        "qlskum_abi_version": (i, []),
+        "qlskum_default_params": (None, [C.POINTER(ParamsStruct)]),
+        "qlskum_create": (i, [C.POINTER(CloudStruct), C.POINTER(ParamsStruct), C.POINTER(H)]),
+        "qlskum_destroy": (i, [H]),
+        "qlskum_last_error": (C.c_char_p, [H]),
+        "qlskum_func_delta": (i, [H]),
+        "qlskum_eval_q_variables": (i, [H]),
+        "qlskum_eval_q_derivatives": (i, [H]),
+        "qlskum_eval_q_inner_loop": (i, [H]),
+        "qlskum_eval_update_innerloop": (i, [H]),
+        "qlskum_cal_flux_residual": (i, [H]),
+        "qlskum_state_update": (i, [H, i]),
+        "qlskum_snapshot_prim_old": (i, [H]),
+        "qlskum_fpi_solver": (i, [H, i]),
+        "qlskum_q_lskum": (i, [H, i]),
+        "qlskum_objective": (i, [H, dp, dp, dp, dp]),
+        "qlskum_get_field": (i, [H, i, dp]),
+        "qlskum_set_prim": (i, [H, dp]),
+        "qlskum_get_prim": (i, [H, dp]),
+        "qlskum_get_connectivity": (i, [H, ip, ip]),
+        "qlskum_get_residual_history": (i, [H, dp, i, ip]),
+        "qlskum_get_iteration": (i, [H, ip]),
+        "qlskum_synchronize": (i, [H]),
+        "qlskum_stream": (C.c_void_p, [H]),
+        "qlskum_launch_count": (C.c_longlong, [H]),
+        "qlskum_set_kernel_timing": (i, [H, i]),
+        "qlskum_get_kernel_timing": (i, [H, i, dp, C.POINTER(C.c_longlong)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def cloud_struct(cloud):
+    """ctypes view of a cloudgen.Cloud (keeps the backing arrays alive)."""
+    keep = dict(
+        x=np.ascontiguousarray(cloud.x, np.float64), y=np.ascontiguousarray(cloud.y, np.float64),
+        left=np.ascontiguousarray(cloud.left, np.int32), right=np.ascontiguousarray(cloud.right, np.int32),
+        f1=np.ascontiguousarray(cloud.flag_1, np.int32), f2=np.ascontiguousarray(cloud.flag_2, np.int32),
+        md=np.ascontiguousarray(cloud.min_dist, np.float64), nb=np.ascontiguousarray(cloud.nbhs, np.int32),
+        conn=np.ascontiguousarray(cloud.conn, np.int32))
+    if keep["conn"].shape != (cloud.n, 20):
+        raise ValueError("conn must be [n, 20]")
+    s = CloudStruct(cloud.n, _dp(keep["x"]), _dp(keep["y"]), _ip(keep["left"]), _ip(keep["right"]),
+                    _ip(keep["f1"]), _ip(keep["f2"]), _dp(keep["md"]), _ip(keep["nb"]), _ip(keep["conn"]))
+    return s, keep
+
+
+class Solver:
+    """The q-LSKUM solver on one GPU, with the reference's module functions as methods.
+
+    Parameters follow the reference's globals: mach, aoa (degrees), cfl,
+    vl_const (VL_CONST), power, inner_iterations; precision FP64 (drop-in) or
+    MIXED.  Fields come back in the cloud's original point order.
+    """
+
+    def __init__(self, cloud, mach=0.63, aoa=2.0, cfl=0.1, vl_const=150.0, power=0.0, inner_iterations=3,
+                 precision=FP64, block_size=0, reorder=True, verbose=False):
+        L = load()
+        self._L = L
+        s, self._keep = cloud_struct(cloud)
+        p = ParamsStruct(mach, aoa, cfl, vl_const, power, inner_iterations, precision, block_size,
+                         1 if reorder else 0, 1 if verbose else 0)
+        h = C.c_void_p()
+        st = L.qlskum_create(C.byref(s), C.byref(p), C.byref(h))
+        if st != 0:
+            raise QlskumError(st, L.qlskum_last_error(None).decode())
+        self._h = h
+        self.n = cloud.n
+        self.params = p
+
+    # ---------------------------------------------------------------- plumbing
+    def _ck(self, st):
+        if st != 0:
+            raise QlskumError(st, self._L.qlskum_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.qlskum_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------- module functions
+    def func_delta(self): self._ck(self._L.qlskum_func_delta(self._h))
+    def eval_q_variables(self): self._ck(self._L.qlskum_eval_q_variables(self._h))
+    def eval_q_derivatives(self): self._ck(self._L.qlskum_eval_q_derivatives(self._h))
+    def eval_q_inner_loop(self): self._ck(self._L.qlskum_eval_q_inner_loop(self._h))
+    def eval_update_innerloop(self): self._ck(self._L.qlskum_eval_update_innerloop(self._h))
+    def cal_flux_residual(self): self._ck(self._L.qlskum_cal_flux_residual(self._h))
+    def state_update(self, rk): self._ck(self._L.qlskum_state_update(self._h, int(rk)))
+    def snapshot_prim_old(self): self._ck(self._L.qlskum_snapshot_prim_old(self._h))
+    def fpi_solver(self, it): self._ck(self._L.qlskum_fpi_solver(self._h, int(it)))
+    def q_lskum(self, iters): self._ck(self._L.qlskum_q_lskum(self._h, int(iters)))
+    def synchronize(self): self._ck(self._L.qlskum_synchronize(self._h))
+
+    def objective(self):
+        """(Cl, Cd, Cm, total entropy)."""
+        v = [C.c_double() for _ in range(4)]
+        self._ck(self._L.qlskum_objective(self._h, *[C.byref(t) for t in v]))
+        return tuple(t.value for t in v)
+
+    # ------------------------------------------------------------- state I/O
+    def field(self, which: int) -> np.ndarray:
+        out = np.empty((self.n,) + _FIELD_SHAPE[which])
+        self._ck(self._L.qlskum_get_field(self._h, which, _dp(out)))
+        return out
+
+    @property
+    def prim(self): return self.field(FIELD_PRIM)
+
+    def set_prim(self, prim):
+        a = np.ascontiguousarray(prim, np.float64)
+        if a.shape != (self.n, 4):
+            raise ValueError("prim must be [n, 4]")
+        self._ck(self._L.qlskum_set_prim(self._h, _dp(a)))
+
+    def connectivity(self):
+        counts = np.empty((self.n, 4), np.int32)
+        lists = np.empty((self.n, 4, 20), np.int32)
+        self._ck(self._L.qlskum_get_connectivity(self._h, _ip(counts), _ip(lists)))
+        return counts, lists
+
+    def residual_history(self) -> np.ndarray:
+        rows = C.c_int()
+        self._ck(self._L.qlskum_get_residual_history(self._h, None, 0, C.byref(rows)))
+        out = np.empty((rows.value, 3))
+        if rows.value:
+            self._ck(self._L.qlskum_get_residual_history(self._h, _dp(out), rows.value, C.byref(rows)))
+        return out
+
+    @property
+    def iteration(self) -> int:
+        it = C.c_int()
+        self._ck(self._L.qlskum_get_iteration(self._h, C.byref(it)))
+        return it.value
+
+    @property
+    def launches(self) -> int:
+        return int(self._L.qlskum_launch_count(self._h))
+
+    KERNELS = ("gradient", "inner", "flux_update", "reduce")
+
+    def set_kernel_timing(self, enable: bool):
+        self._ck(self._L.qlskum_set_kernel_timing(self._h, 1 if enable else 0))
+
+    def kernel_timing(self) -> dict:
+        """{kernel name: (total ms, launches)} recorded while kernel timing was on."""
+        out = {}
+        for k, name in enumerate(self.KERNELS):
+            ms = C.c_double()
+            n = C.c_longlong()
+            self._ck(self._L.qlskum_get_kernel_timing(self._h, k, C.byref(ms), C.byref(n)))
+            out[name] = (ms.value, n.value)
+        return out
+
+    @property
+    def stream(self) -> int:
+        return int(self._L.qlskum_stream(self._h) or 0)

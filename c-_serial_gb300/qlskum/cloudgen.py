@@ -1,0 +1,535 @@
+"""Seeded point-cloud generator and `partGrid` text I/O for q-LSKUM.
+
+The file format is the one the reference reads (main.cpp:16-58): a header line
+holding the number of points, then one line per point
+
+    x y left right flag_1 flag_2 min_dist nbhs conn[1..nbhs]
+
+1-based indices, flag_1 = 0 wall / 1 interior / 2 outer, flag_2 > 0 marks a
+shape (surface) point, at most 20 neighbours (main.cpp:27).  Wall points come
+first because compute_cl_cd_cm walks points 1..shape_points
+(compute_force_coeffs_mod.h:25-27).
+
+Layout of a generated cloud
+---------------------------
+* Body: NACA 4-digit section of chord 1 with a closed trailing edge, wall
+  points cosine-spaced in the surface parameter theta (x = (1 + cos theta)/2).
+  Point 1 is the trailing edge; theta runs counter-clockwise (upper surface
+  first).  `left` is the next point counter-clockwise and `right` the previous
+  one, so the reference's normal formula (point_normals_mod.h:17-49,
+  n = rot90(r - l)) points into the fluid on the wall and away from the body
+  on the far-field circle.
+* Layers: `n_layers` rings; ring 0 is the wall, the last ring is the far-field
+  circle of radius `radius` centred at mid-chord.  Ring offsets grow
+  geometrically from `first_spacing`; the growth ratio is solved so that the
+  rings reach the circle (with the literal 2e-3 / 1.1 / 60-layer recipe the
+  rings would stop near 6 chords).  Near the wall a ring point sits on the
+  wall normal; further out it blends to the straight line towards the circle.
+* Jitter: interior points move by a seeded uniform offset of up to `jitter`
+  of the local tangential / normal spacing.
+* Neighbours: the `n_nbrs` nearest candidates within `nbr_radius` x the local
+  spacing, "nearest" being measured in the local (tangential, normal) spacing
+  units so that anisotropic near-wall rings still give every directional
+  sub-stencil points on both sides.  Points whose sub-stencils (split the way
+  generate_connectivity_mod.h:5-219 splits them) are empty or nearly
+  collinear get further candidates, up to 20 neighbours.  This is the job of
+  the empty `check_condition_number` stub at generate_connectivity_mod.h:84-89.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+MAX_NBHS = 20
+
+
+@dataclasses.dataclass
+class Cloud:
+    """A point cloud in the reference's layout (1-based indices in left/right/conn)."""
+
+    x: np.ndarray          # float64 [N]
+    y: np.ndarray          # float64 [N]
+    left: np.ndarray       # int32 [N] (1-based, 0 for interior points)
+    right: np.ndarray      # int32 [N]
+    flag_1: np.ndarray     # int32 [N]: 0 wall, 1 interior, 2 outer
+    flag_2: np.ndarray     # int32 [N]: shape id (>0) on wall points, else 0
+    min_dist: np.ndarray   # float64 [N]
+    nbhs: np.ndarray       # int32 [N]
+    conn: np.ndarray       # int32 [N, 20] (1-based; unused slots 0)
+
+    @property
+    def n(self) -> int:
+        return int(self.x.shape[0])
+
+    def counts(self) -> dict:
+        return {
+            "points": self.n,
+            "wall": int((self.flag_1 == 0).sum()),
+            "interior": int((self.flag_1 == 1).sum()),
+            "outer": int((self.flag_1 == 2).sum()),
+            "shape": int((self.flag_2 > 0).sum()),
+        }
+
+
+# ---------------------------------------------------------------------------
+# partGrid text I/O
+# ---------------------------------------------------------------------------
+
+def write_partgrid(cloud: Cloud, path: str) -> None:
+    """Write `cloud` in the reference's partGrid text format (main.cpp:18,32-36).
+
+    Coordinates and min_dist are written with 17 significant digits so the
+    file reads back to the identical doubles.
+    """
+    n = cloud.n
+    lines = [f"{n}\n"]
+    xs = [repr(float(v)) for v in cloud.x]
+    ys = [repr(float(v)) for v in cloud.y]
+    md = [repr(float(v)) for v in cloud.min_dist]
+    for i in range(n):
+        k = int(cloud.nbhs[i])
+        c = " ".join(str(int(v)) for v in cloud.conn[i, :k])
+        lines.append(
+            f"{xs[i]} {ys[i]} {int(cloud.left[i])} {int(cloud.right[i])} "
+            f"{int(cloud.flag_1[i])} {int(cloud.flag_2[i])} {md[i]} {k} {c}\n"
+        )
+    with open(path, "w") as f:
+        f.writelines(lines)
+
+
+def read_partgrid(path: str) -> Cloud:
+    """Read a partGrid text file (main.cpp:16-58).  Rejects nbhs outside 0..20."""
+    with open(path) as f:
+        tok = f.read().split()
+    n = int(tok[0])
+    x = np.empty(n)
+    y = np.empty(n)
+    left = np.empty(n, np.int32)
+    right = np.empty(n, np.int32)
+    f1 = np.empty(n, np.int32)
+    f2 = np.empty(n, np.int32)
+    md = np.empty(n)
+    nb = np.empty(n, np.int32)
+    conn = np.zeros((n, MAX_NBHS), np.int32)
+    p = 1
+    for i in range(n):
+        x[i] = float(tok[p]); y[i] = float(tok[p + 1])
+        left[i] = int(tok[p + 2]); right[i] = int(tok[p + 3])
+        f1[i] = int(tok[p + 4]); f2[i] = int(tok[p + 5])
+        md[i] = float(tok[p + 6]); k = int(tok[p + 7])
+        if k < 0 or k > MAX_NBHS:
+            raise ValueError(f"point {i + 1}: nbhs={k} outside 0..{MAX_NBHS}")
+        nb[i] = k
+        conn[i, :k] = [int(t) for t in tok[p + 8:p + 8 + k]]
+        p += 8 + k
+    return Cloud(x, y, left, right, f1, f2, md, nb, conn)
+
+
+# ---------------------------------------------------------------------------
+# Geometry
+# ---------------------------------------------------------------------------
+
+def naca4_surface(theta: np.ndarray, m: float = 0.0, p: float = 0.4, t: float = 0.12):
+    """NACA 4-digit surface at parameter theta in [0, 2 pi).
+
+    x_c = (1 + cos theta)/2; theta in [0, pi] is the upper surface (trailing
+    edge to leading edge), (pi, 2 pi) the lower one.  Closed trailing edge
+    (-0.1036 x^4 coefficient).  m = max camber, p = its chord position,
+    t = thickness, all as fractions of the chord.
+    """
+    xc = 0.5 * (1.0 + np.cos(theta))
+    yt = 5.0 * t * (0.2969 * np.sqrt(xc) - 0.1260 * xc - 0.3516 * xc**2 + 0.2843 * xc**3 - 0.1036 * xc**4)
+    if m > 0.0:
+        fore = xc < p
+        yc = np.where(fore, m / p**2 * (2 * p * xc - xc**2), m / (1 - p) ** 2 * ((1 - 2 * p) + 2 * p * xc - xc**2))
+        dyc = np.where(fore, 2 * m / p**2 * (p - xc), 2 * m / (1 - p) ** 2 * (p - xc))
+    else:
+        yc = np.zeros_like(xc)
+        dyc = np.zeros_like(xc)
+    th = np.arctan(dyc)
+    upper = np.sin(theta) >= 0.0
+    sgn = np.where(upper, 1.0, -1.0)
+    x = xc - sgn * yt * np.sin(th)
+    y = yc + sgn * yt * np.cos(th)
+    return x, y
+
+
+def _rot_normals(px: np.ndarray, py: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Normals of a closed ring ordered counter-clockwise: rot90(prev - next)/|.|.
+
+    The same construction as point_normals_mod.h:34-46 with l = next, r = prev.
+    """
+    lx, ly = np.roll(px, -1), np.roll(py, -1)
+    rx, ry = np.roll(px, 1), np.roll(py, 1)
+    nx = -0.5 * (ry - ly)
+    ny = 0.5 * (rx - lx)
+    d = np.sqrt(nx * nx + ny * ny)
+    return nx / d, ny / d
+
+
+def solve_growth(first: float, steps: int, total: float) -> float:
+    """Ratio r with first*(r^steps - 1)/(r - 1) == total (bisection)."""
+    if first * steps >= total:
+        return 1.0
+    lo, hi = 1.0 + 1e-12, 2.0
+    while first * (hi**steps - 1.0) / (hi - 1.0) < total:
+        hi *= 1.5
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if first * (mid**steps - 1.0) / (mid - 1.0) < total:
+            lo = mid
+        else:
+            hi = mid
+    return 0.5 * (lo + hi)
+
+
+def make_layers(n_wall: int, n_layers: int, first_spacing: float, radius: float,
+                m: float = 0.0, p: float = 0.4, t: float = 0.12,
+                center=(0.5, 0.0), blend_len: float = 1.0, smooth: int = 0):
+    """Ring points [n_layers, n_wall] (x, y) and the ring offsets d_j."""
+    theta = 2.0 * np.pi * np.arange(n_wall) / n_wall
+    wx, wy = naca4_surface(theta, m, p, t)
+    nx, ny = _rot_normals(wx, wy)
+    # Spread the ray fan at the sharp trailing edge: smooth the ray directions
+    # along the ring so that the wake behind the edge is not left empty.
+    for _ in range(smooth):
+        sx = np.roll(nx, 1) + 2.0 * nx + np.roll(nx, -1)
+        sy = np.roll(ny, 1) + 2.0 * ny + np.roll(ny, -1)
+        ln = np.sqrt(sx * sx + sy * sy)
+        nx, ny = sx / ln, sy / ln
+    cx = center[0] + radius * np.cos(theta)
+    cy = center[1] + radius * np.sin(theta)
+    span = np.sqrt((cx - wx) ** 2 + (cy - wy) ** 2)       # wall -> circle distance per ray
+    steps = n_layers - 1
+    g = solve_growth(first_spacing, steps, float(span.min()))
+    j = np.arange(n_layers, dtype=np.float64)
+    d = first_spacing * j if g == 1.0 else first_spacing * (g**j - 1.0) / (g - 1.0)
+    f = d / d[-1]                                          # 0 at wall, 1 at circle
+    beta = np.clip(d / blend_len, 0.0, 1.0) ** 2
+    beta[-1] = 1.0
+    X = np.empty((n_layers, n_wall))
+    Y = np.empty((n_layers, n_wall))
+    for jj in range(n_layers):
+        ox = wx + d[jj] * nx
+        oy = wy + d[jj] * ny
+        lx = (1.0 - f[jj]) * wx + f[jj] * cx
+        ly = (1.0 - f[jj]) * wy + f[jj] * cy
+        X[jj] = (1.0 - beta[jj]) * ox + beta[jj] * lx
+        Y[jj] = (1.0 - beta[jj]) * oy + beta[jj] * ly
+    X[-1], Y[-1] = cx, cy
+    return X, Y, g
+
+
+# ---------------------------------------------------------------------------
+# Connectivity
+# ---------------------------------------------------------------------------
+
+def _classify_masks(dels: np.ndarray, deln: np.ndarray, flag: np.ndarray):
+    """Sub-stencil membership as generate_connectivity_mod.h:5-219 decides it.
+
+    Returns four bool arrays (xpos, xneg, ypos, yneg) shaped like dels.
+    Interior: by sign of dels / deln, ties in both.  Wall: x by dels, yneg all.
+    Outer: x by dels, ypos all.
+    """
+    f = flag[:, None]
+    xpos = dels <= 0.0
+    xneg = dels >= 0.0
+    ypos = np.where(f == 1, deln <= 0.0, f == 2)
+    yneg = np.where(f == 1, deln >= 0.0, f == 0)
+    return xpos, xneg, ypos, yneg
+
+
+def _stencil_ok(dels, deln, valid, flag, min_count=2, min_rcond=1e-3):
+    """Per point: every sub-stencil the point's class uses is well posed.
+
+    A sub-stencil passes when it has >= min_count members and the reciprocal
+    condition number of its 2x2 least-squares matrix is >= min_rcond.
+    """
+    masks = _classify_masks(dels, deln, flag)
+    need = [np.ones_like(flag, bool), np.ones_like(flag, bool), flag != 0, flag != 2]
+    ok = np.ones(flag.shape[0], bool)
+    for mk, nd in zip(masks, need):
+        w = mk & valid
+        cnt = w.sum(1)
+        sxx = np.where(w, dels * dels, 0.0).sum(1)
+        syy = np.where(w, deln * deln, 0.0).sum(1)
+        sxy = np.where(w, dels * deln, 0.0).sum(1)
+        tr = sxx + syy
+        det = sxx * syy - sxy * sxy
+        disc = np.sqrt(np.maximum(tr * tr * 0.25 - det, 0.0))
+        lmax = tr * 0.5 + disc
+        lmin = tr * 0.5 - disc
+        rc = np.where(lmax > 0, lmin / np.where(lmax > 0, lmax, 1.0), 0.0)
+        good = (cnt >= min_count) & (rc >= min_rcond)
+        ok &= np.where(nd, good, True)
+    return ok
+
+
+def _visible(x, y, nx, ny, flag, rows, idx, dx, dy, dist, wall):
+    """Mask of candidate neighbours that see the point through the fluid.
+
+    `wall` is a list of closed polygons (0-based point indices, in ring order).
+    A candidate is rejected when the segment to it crosses a wall edge not
+    touching either end, and, for a wall point, when it lies behind the wall's
+    tangent line by more than a quarter of its distance (a point on the far
+    side of a thin trailing edge).
+    """
+    from scipy.spatial import cKDTree
+
+    rows = np.atleast_1d(np.arange(x.shape[0]) if rows is None else rows)
+    n, k = idx.shape
+    ok = np.ones((n, k), bool)
+    wmask = flag[rows] == 0
+    deln = dx * nx[rows][:, None] + dy * ny[rows][:, None]
+    ok &= ~(wmask[:, None] & (deln < -0.25 * dist))
+    ea = np.concatenate([np.asarray(w) for w in wall])
+    eb = np.concatenate([np.roll(np.asarray(w), -1) for w in wall])
+    mids = np.stack([(x[ea] + x[eb]) * 0.5, (y[ea] + y[eb]) * 0.5], 1)
+    etree = cKDTree(mids)
+    wpts = np.unique(ea)
+    dw, _ = cKDTree(np.stack([x[wpts], y[wpts]], 1)).query(np.stack([x, y], 1), workers=-1)
+    need = (np.minimum(dw[rows][:, None], dw[idx]) <= dist) & np.isfinite(dist)
+    rr, jj = np.nonzero(need)
+    if rr.size == 0:
+        return ok
+    ii = rows[rr]
+    kk = idx[rr, jj]
+    ax, ay, bx, by = x[ii], y[ii], x[kk], y[kk]
+    _, near = etree.query(np.stack([(ax + bx) * 0.5, (ay + by) * 0.5], 1), k=min(8, len(mids)), workers=-1)
+    cross = np.zeros(ii.size, bool)
+
+    def orient(px, py, qx, qy, rx, ry):
+        return (qx - px) * (ry - py) - (qy - py) * (rx - px)
+
+    for c in range(near.shape[1]):
+        e0 = ea[near[:, c]]
+        e1 = eb[near[:, c]]
+        touch = (e0 == ii) | (e0 == kk) | (e1 == ii) | (e1 == kk)
+        cx0, cy0, cx1, cy1 = x[e0], y[e0], x[e1], y[e1]
+        o1 = orient(ax, ay, bx, by, cx0, cy0)
+        o2 = orient(ax, ay, bx, by, cx1, cy1)
+        o3 = orient(cx0, cy0, cx1, cy1, ax, ay)
+        o4 = orient(cx0, cy0, cx1, cy1, bx, by)
+        cross |= (~touch) & (o1 * o2 < 0) & (o3 * o4 < 0)
+    ok[rr[cross], jj[cross]] = False
+    return ok
+
+
+def build_connectivity(x, y, nx, ny, flag, ht, hn, tx_, ty_, n_nbrs=10, nbr_radius=2.5,
+                       n_cand=32, min_rcond=1e-3, wall=None):
+    """conn [N, 20] (0-based, -1 padded) and counts.
+
+    Candidates come from a k-d tree; they are ranked by distance in the local
+    spacing frame (tangent (tx_, ty_) scaled by ht, normal scaled by hn), kept
+    within nbr_radius * max(ht, hn), and the first n_nbrs are taken.  Points
+    whose sub-stencils fail `_stencil_ok` take further candidates one by one.
+    """
+    from scipy.spatial import cKDTree
+
+    n = x.shape[0]
+    pts = np.stack([x, y], 1)
+    tree = cKDTree(pts)
+    hmax = np.maximum(ht, hn)
+    k = min(n_cand + 1, n)
+    _, idx = tree.query(pts, k=k, workers=-1)
+    idx = idx[:, 1:]                                       # drop self
+    dx = x[idx] - x[:, None]
+    dy = y[idx] - y[:, None]
+    dist = np.sqrt(dx * dx + dy * dy)
+    st = (dx * tx_[:, None] + dy * ty_[:, None]) / ht[:, None]
+    sn = (dx * (-ty_)[:, None] + dy * tx_[:, None]) / hn[:, None]
+    sd = np.sqrt(st * st + sn * sn)
+    inside = dist <= nbr_radius * hmax[:, None]
+    if wall is not None:
+        inside &= _visible(x, y, nx, ny, flag, None, idx, dx, dy, dist, wall)
+    sd = np.where(inside, sd, np.inf)
+    order = np.argsort(sd, axis=1, kind="stable")
+    idx = np.take_along_axis(idx, order, 1)
+    sd = np.take_along_axis(sd, order, 1)
+    dx = np.take_along_axis(dx, order, 1)
+    dy = np.take_along_axis(dy, order, 1)
+    finite = np.isfinite(sd)
+    # reference split frame: t = (ny, -nx), n = (nx, ny)
+    dels_all = dx * ny[:, None] - dy * nx[:, None]
+    deln_all = dx * nx[:, None] + dy * ny[:, None]
+    take = np.minimum(n_nbrs, finite.sum(1))
+    kk = np.arange(idx.shape[1])[None, :]
+    valid = (kk < take[:, None]) & finite
+    ok = _stencil_ok(dels_all, deln_all, valid, flag, min_rcond=min_rcond)
+    bad = np.nonzero(~ok)[0]
+    # grow failing stencils one candidate at a time, up to MAX_NBHS
+    for extra in range(MAX_NBHS - n_nbrs):
+        if bad.size == 0:
+            break
+        take[bad] = np.minimum(take[bad] + 1, np.minimum(MAX_NBHS, finite[bad].sum(1)))
+        vb = (kk < take[bad][:, None]) & finite[bad]
+        okb = _stencil_ok(dels_all[bad], deln_all[bad], vb, flag[bad], min_rcond=min_rcond)
+        bad = bad[~okb]
+    valid = (kk < take[:, None]) & finite
+    conn = np.where(valid, idx, -1)[:, :MAX_NBHS].astype(np.int64)
+    cnt = valid.sum(1)
+    if bad.size:
+        conn, cnt, bad = _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, wall)
+    return conn, cnt, bad
+
+
+def _rcond(dels, deln):
+    """Reciprocal condition number of the 2x2 LSQ matrix of one sub-stencil."""
+    sxx = float((dels * dels).sum())
+    syy = float((deln * deln).sum())
+    sxy = float((dels * deln).sum())
+    tr = sxx + syy
+    det = sxx * syy - sxy * sxy
+    disc = math.sqrt(max(tr * tr * 0.25 - det, 0.0))
+    lmax = tr * 0.5 + disc
+    return (tr * 0.5 - disc) / lmax if lmax > 0 else 0.0
+
+
+def _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, wall=None):
+    """Fix the few stencils the ranked selection leaves ill-posed.
+
+    For each such point: restart from its n_nbrs nearest (Euclidean) points
+    and, while some sub-stencil its class uses is ill-posed, add the point in
+    that sub-stencil's half-plane (among the 256 nearest) that raises the
+    sub-stencil's reciprocal condition number the most.
+    """
+    still = []
+    for i in bad:
+        _, cand = tree.query([x[i], y[i]], k=min(257, x.shape[0]))
+        cand = np.array([int(c) for c in cand if c != i])
+        dx = x[cand] - x[i]
+        dy = y[cand] - y[i]
+        if wall is not None:
+            vis = _visible(x, y, nx, ny, flag, i, cand[None, :], dx[None, :], dy[None, :],
+                           np.sqrt(dx * dx + dy * dy)[None, :], wall)[0]
+            cand, dx, dy = cand[vis], dx[vis], dy[vis]
+        dels = dx * ny[i] - dy * nx[i]
+        deln = dx * nx[i] + dy * ny[i]
+        allm = np.ones(len(cand), bool)
+        want = [dels <= 0.0, dels >= 0.0,
+                (deln <= 0.0) if flag[i] == 1 else (allm if flag[i] == 2 else None),
+                (deln >= 0.0) if flag[i] == 1 else (allm if flag[i] == 0 else None)]
+        sel = np.zeros(len(cand), bool)
+        sel[:n_nbrs] = True
+        while sel.sum() < MAX_NBHS:
+            worst = None
+            for d in range(4):
+                if want[d] is None:
+                    continue
+                w = sel & want[d]
+                if w.sum() < 2 or _rcond(dels[w], deln[w]) < min_rcond:
+                    worst = d
+                    break
+            if worst is None:
+                break
+            best, best_rc = None, -1.0
+            for c in np.nonzero(want[worst] & ~sel)[0]:
+                w = sel & want[worst]
+                w[c] = True
+                rc = _rcond(dels[w], deln[w]) if w.sum() >= 2 else 0.0
+                if rc > best_rc + 1e-12:
+                    best, best_rc = c, rc
+            if best is None:
+                break
+            sel[best] = True
+        chosen = np.nonzero(sel)[0]
+        ok = all(want[d] is None or ((sel & want[d]).sum() >= 2 and _rcond(dels[sel & want[d]], deln[sel & want[d]]) >= min_rcond)
+                 for d in range(4))
+        if not ok:
+            still.append(i)
+        conn[i, :] = -1
+        conn[i, :len(chosen)] = cand[chosen]
+        cnt[i] = len(chosen)
+    return conn, cnt, np.array(still, dtype=np.int64)
+
+
+def make_cloud(n_wall: int = 160, n_layers: int = 60, first_spacing: float = 2e-3,
+               radius: float = 20.0, seed: int = 0, jitter: float = 0.1,
+               n_nbrs: int = 10, nbr_radius: float = 2.5,
+               m: float = 0.0, p: float = 0.4, t: float = 0.12,
+               min_rcond: float = 1e-3, smooth: int = 30) -> Cloud:
+    """Generate a seeded NACA 4-digit O-type point cloud (see module docstring).
+
+    Point order: wall ring (flag_1 0, flag_2 1), interior rings (flag_1 1),
+    far-field ring (flag_1 2); inside a ring, counter-clockwise from the
+    trailing edge.
+    """
+    X, Y, _ = make_layers(n_wall, n_layers, first_spacing, radius, m, p, t, smooth=smooth)
+    L, W = X.shape
+    # local spacing: half the central difference along / across rings
+    Xp, Xm = np.roll(X, -1, 1), np.roll(X, 1, 1)
+    Yp, Ym = np.roll(Y, -1, 1), np.roll(Y, 1, 1)
+    tx = Xp - Xm
+    ty = Yp - Ym
+    ht = 0.5 * np.sqrt(tx * tx + ty * ty)
+    tl = np.sqrt(tx * tx + ty * ty)
+    tx, ty = tx / tl, ty / tl
+    dxn = np.empty_like(X)
+    dyn = np.empty_like(Y)
+    dxn[1:-1] = X[2:] - X[:-2]; dyn[1:-1] = Y[2:] - Y[:-2]
+    dxn[0] = 2 * (X[1] - X[0]); dyn[0] = 2 * (Y[1] - Y[0])
+    dxn[-1] = 2 * (X[-1] - X[-2]); dyn[-1] = 2 * (Y[-1] - Y[-2])
+    hn = 0.5 * np.sqrt(dxn * dxn + dyn * dyn)
+
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(-1.0, 1.0, size=(2, L, W))
+    jx = jitter * (u[0] * ht * tx + u[1] * hn * (-ty))
+    jy = jitter * (u[0] * ht * ty + u[1] * hn * tx)
+    jx[0] = jx[-1] = 0.0
+    jy[0] = jy[-1] = 0.0
+    X = X + jx
+    Y = Y + jy
+
+    n = L * W
+    x = X.reshape(-1).copy()
+    y = Y.reshape(-1).copy()
+    flag = np.ones(n, np.int32)
+    flag[:W] = 0
+    flag[-W:] = 2
+    ring = np.arange(W)
+    left = np.zeros(n, np.int32)
+    right = np.zeros(n, np.int32)
+    # 1-based; left = next CCW, right = previous CCW (normals into the fluid)
+    left[:W] = (ring + 1) % W + 1
+    right[:W] = (ring - 1) % W + 1
+    left[-W:] = (n - W) + (ring + 1) % W + 1
+    right[-W:] = (n - W) + (ring - 1) % W + 1
+    f2 = np.zeros(n, np.int32)
+    f2[:W] = 1
+
+    # normals exactly as the reference computes them (for the split checks)
+    nx = np.zeros(n)
+    ny = np.ones(n)
+    for sl, lo in ((slice(0, W), 0), (slice(n - W, n), n - W)):
+        li = left[sl] - 1
+        ri = right[sl] - 1
+        nxx = 0.5 * ((y[sl] - y[li]) + (y[ri] - y[sl]))
+        nyy = 0.5 * ((x[sl] - x[li]) + (x[ri] - x[sl]))
+        d = np.sqrt(nxx * nxx + nyy * nyy)
+        nx[sl] = -nxx / d
+        ny[sl] = nyy / d
+
+    conn0, cnt, bad = build_connectivity(
+        x, y, nx, ny, flag, ht.reshape(-1), hn.reshape(-1), tx.reshape(-1), ty.reshape(-1),
+        n_nbrs=n_nbrs, nbr_radius=nbr_radius, min_rcond=min_rcond, wall=[np.arange(W)])
+    if bad.size:
+        raise RuntimeError(f"{bad.size} points have degenerate sub-stencils even with {MAX_NBHS} neighbours")
+    conn = np.zeros((n, MAX_NBHS), np.int32)
+    valid = conn0 >= 0
+    conn[valid] = (conn0[valid] + 1).astype(np.int32)
+    dxs = np.where(valid, x[np.maximum(conn0, 0)] - x[:, None], np.inf)
+    dys = np.where(valid, y[np.maximum(conn0, 0)] - y[:, None], np.inf)
+    md = np.sqrt(dxs * dxs + dys * dys).min(1)
+    return Cloud(x, y, left, right, flag, f2, md, cnt.astype(np.int32), conn)
+
+
+def config1_cloud(seed: int = 1) -> Cloud:
+    """NACA 0012, 160 cosine-spaced wall points x 60 rings = 9,600 points."""
+    return make_cloud(n_wall=160, n_layers=60, first_spacing=2e-3, radius=20.0, seed=seed)
+
+
+def config2_cloud(seed: int = 2) -> Cloud:
+    """NACA 0012, 1024 wall points x 1000 rings = 1,024,000 points."""
+    return make_cloud(n_wall=1024, n_layers=1000, first_spacing=2e-3, radius=20.0, seed=seed)

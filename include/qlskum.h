@@ -1,0 +1,173 @@
+/* qlskum.h -- C ABI of the GB300 (sm_103a) q-LSKUM solver core.
+ *
+ * Drop-in for the serial reference solver's module API (Pathlessbark8/C-_serial).
+ * The reference exposes argument-less void functions over the global `point`
+ * struct (data_structure_mod.h:10-49) and global knobs (data_structure_mod.h:
+ * 57-121, parameter_mod.h:4-11); here the same modules are entry points on a
+ * handle that owns the device-resident state.
+ *
+ * Conventions
+ *   - Input cloud arrays are host arrays in the reference's grid-file layout
+ *     (main.cpp:30-58): 1-based `left`, `right` and `conn` ([n][20], row i
+ *     holding the nbhs[i] neighbours of point i+1), flag_1 0 wall / 1 interior
+ *     / 2 outer, flag_2 > 0 on shape points, which must come first
+ *     (compute_force_coeffs_mod.h:25-27).
+ *   - Every point-valued output is in the ORIGINAL point order, 0-based rows,
+ *     point-major: [n][4] for prim / q / flux_res, [n][2][4] for dq and qm
+ *     (dq[i][0] = d/dx, dq[i][1] = d/dy; qm[i][0] = max, qm[i][1] = min).
+ *   - All calls on one handle are stream-ordered on the handle's CUDA stream;
+ *     functions that return host data synchronise that stream.  A handle is
+ *     not thread-safe; distinct handles are independent.
+ *   - Errors: every function returns a qlskum_status; qlskum_last_error()
+ *     gives the message of the last failure on a handle (or of the last
+ *     failed qlskum_create when passed NULL).
+ */
+#ifndef QLSKUM_H
+#define QLSKUM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QLSKUM_MAX_NBHS 20
+#define QLSKUM_ABI_VERSION 1
+
+typedef enum {
+    QLSKUM_OK = 0,
+    QLSKUM_ERR_INVALID = 1,      /* bad argument or malformed cloud */
+    QLSKUM_ERR_DEGENERATE = 2,   /* a sub-stencil has a singular 2x2 least-squares matrix */
+    QLSKUM_ERR_NONFINITE = 3,    /* the state or the residual became NaN / Inf */
+    QLSKUM_ERR_CUDA = 4,         /* a CUDA call failed */
+    QLSKUM_ERR_UNSUPPORTED = 5   /* option not available in this build / precision */
+} qlskum_status;
+
+typedef enum {
+    QLSKUM_FP64 = 0,             /* FP64 end to end: the drop-in form */
+    QLSKUM_MIXED = 1             /* FP32 q / limiter / split fluxes, FP64 solve + accumulate + update */
+} qlskum_precision;
+
+/* The grid file's columns (main.cpp:32-36), host memory, 1-based indices. */
+typedef struct {
+    int n;
+    const double *x, *y;
+    const int *left, *right;
+    const int *flag_1, *flag_2;
+    const double *min_dist;
+    const int *nbhs;
+    const int *conn;              /* [n][QLSKUM_MAX_NBHS] */
+} qlskum_cloud;
+
+/* Case and solver knobs: parameter_mod.h:4-8 (mach, aoa) and
+ * data_structure_mod.h:72,90,96,118 (CFL, power, VL_CONST, inner_iterations). */
+typedef struct {
+    double mach;
+    double aoa;                   /* degrees */
+    double cfl;
+    double vl_const;
+    double power;                 /* least-squares weights dist^power */
+    int inner_iterations;
+    int precision;                /* qlskum_precision */
+    int block_size;               /* threads per block for the point kernels; 0 = default */
+    int reorder;                  /* 1 = Morton/class reorder of points on the device (default), 0 = file order */
+    int verbose;                  /* 1 = print "iterations <it> residue : <r>" per iteration like fpi_solver_mod.h:150 */
+} qlskum_params;
+
+typedef struct qlskum_handle qlskum_handle;
+
+/* Fill `p` with the reference's defaults (parameter_mod.h / data_structure_mod.h:
+ * mach 0.63, aoa 2, CFL 0.1, VL_CONST 150, power 0, inner_iterations 3), FP64. */
+void qlskum_default_params(qlskum_params *p);
+
+/* ---------------------------------------------------------------- lifetime */
+
+/* Copies the cloud, computes normals (point_normals_mod.h:5-55) and the four
+ * directional sub-stencils (generate_connectivity_mod.h:221-249) on the host
+ * in FP64 with the reference's operation order (bit-exact), reorders the
+ * points, uploads everything and sets the free-stream initial state
+ * (initial_conditions_mod.h:23-37).  Replaces main.cpp:59-65. */
+qlskum_status qlskum_create(const qlskum_cloud *cloud, const qlskum_params *params, qlskum_handle **out);
+qlskum_status qlskum_destroy(qlskum_handle *h);
+const char *qlskum_last_error(const qlskum_handle *h);
+int qlskum_abi_version(void);
+
+/* ------------------------------------------------ module-mirroring entry points */
+
+/* state_update_mod.h:448-496 */
+qlskum_status qlskum_func_delta(qlskum_handle *h);
+/* q_variables_mod.h:9-34 */
+qlskum_status qlskum_eval_q_variables(qlskum_handle *h);
+/* q_variables_mod.h:36-118 */
+qlskum_status qlskum_eval_q_derivatives(qlskum_handle *h);
+/* q_variables_mod.h:120-213 */
+qlskum_status qlskum_eval_q_inner_loop(qlskum_handle *h);
+/* q_variables_mod.h:215-228 */
+qlskum_status qlskum_eval_update_innerloop(qlskum_handle *h);
+/* flux_residual_mod.h:10-89 with interior_/wall_/outer_fluxes_mod.h, the
+ * split and quadrant fluxes and the Venkatakrishnan limiter (limiters_mod.h:55-104) */
+qlskum_status qlskum_cal_flux_residual(qlskum_handle *h);
+/* state_update_mod.h:92-283, rk in 1..4 */
+qlskum_status qlskum_state_update(qlskum_handle *h, int rk);
+/* prim_old <- prim (fpi_solver_mod.h:19-25) */
+qlskum_status qlskum_snapshot_prim_old(qlskum_handle *h);
+/* One pseudo-time iteration (fpi_solver_mod.h:14-151) with fused kernels.
+ * `it` is the reference's iteration number (res_old latches at it <= 2). */
+qlskum_status qlskum_fpi_solver(qlskum_handle *h, int it);
+/* `iters` iterations continuing from the handle's iteration counter
+ * (q_lskum_mod.h:13-38); replayed from a CUDA graph per iteration. */
+qlskum_status qlskum_q_lskum(qlskum_handle *h, int iters);
+
+/* compute_force_coeffs_mod.h:7-69 and compute_entropy_mod.h:5-24 (the
+ * entropy total summed over all points, which the reference computes but
+ * loses in a shadowing local).  Any pointer may be NULL. */
+qlskum_status qlskum_objective(qlskum_handle *h, double *cl, double *cd, double *cm, double *total_entropy);
+
+/* --------------------------------------------------------------- state I/O */
+
+enum {
+    QLSKUM_FIELD_PRIM = 0,        /* [n][4] */
+    QLSKUM_FIELD_PRIM_OLD = 1,    /* [n][4] */
+    QLSKUM_FIELD_Q = 2,           /* [n][4] */
+    QLSKUM_FIELD_DQ = 3,          /* [n][2][4] */
+    QLSKUM_FIELD_QM = 4,          /* [n][2][4] */
+    QLSKUM_FIELD_FLUX_RES = 5,    /* [n][4] */
+    QLSKUM_FIELD_DELTA = 6,       /* [n] */
+    QLSKUM_FIELD_NORMALS = 7,     /* [n][2] */
+    QLSKUM_FIELD_ENTROPY = 8      /* [n], filled by qlskum_objective */
+};
+
+/* Copy a field to host memory `out` (original point order, FP64). */
+qlskum_status qlskum_get_field(qlskum_handle *h, int field, double *out);
+/* Overwrite prim ([n][4], original order), e.g. from restart.dat
+ * (initial_conditions_mod.h:7-21). */
+qlskum_status qlskum_set_prim(qlskum_handle *h, const double *prim);
+qlskum_status qlskum_get_prim(qlskum_handle *h, double *out);
+/* Sub-stencils in original order: counts [n][4] (xpos, xneg, ypos, yneg) and
+ * lists [n][4][20] (1-based, unused slots 0), as generate_connectivity builds them. */
+qlskum_status qlskum_get_connectivity(qlskum_handle *h, int *counts, int *lists);
+/* Residual history: for each completed iteration (res_new, residue, max_res)
+ * as fpi_solver_mod.h:138-147 and state_update_mod.h:157-165 define them.
+ * Writes min(count, max_rows) rows to out ([max_rows][3]); returns count via *rows. */
+qlskum_status qlskum_get_residual_history(qlskum_handle *h, double *out, int max_rows, int *rows);
+/* Iterations completed so far. */
+qlskum_status qlskum_get_iteration(qlskum_handle *h, int *it);
+qlskum_status qlskum_synchronize(qlskum_handle *h);
+/* The CUDA stream (cudaStream_t) the handle launches on, as an opaque pointer. */
+void *qlskum_stream(qlskum_handle *h);
+/* Kernel launches issued by this handle so far (the benchmark's launch count). */
+long long qlskum_launch_count(const qlskum_handle *h);
+
+/* Per-kernel device time from CUDA events recorded on the handle's stream.
+ * While enabled, qlskum_q_lskum launches each iteration's kernels one by one
+ * (no CUDA graph) so that every launch is bracketed by events.
+ * kernel: 0 gradient + min/max (q_derivatives), 1 inner loop, 2 fused flux +
+ * state update, 3 residual reduction.  Enabling resets the totals. */
+enum { QLSKUM_KERNEL_GRADIENT = 0, QLSKUM_KERNEL_INNER = 1, QLSKUM_KERNEL_FLUX_UPDATE = 2, QLSKUM_KERNEL_REDUCE = 3 };
+qlskum_status qlskum_set_kernel_timing(qlskum_handle *h, int enable);
+qlskum_status qlskum_get_kernel_timing(qlskum_handle *h, int kernel, double *ms_total, long long *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
