@@ -1,11 +1,13 @@
 """Build recipe of the in-tree CUDA library (libqlskum.so) for sm_103a.
 
-Three translation units compiled in parallel and linked into one shared
+Four translation units compiled in parallel and linked into one shared
 library with a C ABI (include/qlskum.h):
 
 * csrc/qlskum_fp64.cu  -- FP64 drop-in kernels, -fmad=false (no FMA
   contraction, the reference's rounding sequence);
 * csrc/qlskum_mixed.cu -- mixed-precision kernels (FP32 edge work, FMA on);
+* csrc/qlskum_noalloc.cu -- the stage update over caller buffers that
+  allocates nothing (static device scratch), -fmad=false like the FP64 unit;
 * csrc/qlskum_host.cpp -- host layer, g++ -ffp-contract=off (bit-exact
   sub-stencil classification on x86-64 and aarch64 alike).
 
@@ -45,6 +47,7 @@ def sources():
     return {
         "qlskum_fp64.cu": ["-fmad=false"],
         "qlskum_mixed.cu": ["-fmad=true"],
+        "qlskum_noalloc.cu": ["-fmad=false"],
         "qlskum_host.cpp": [],
     }
 

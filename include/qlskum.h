@@ -167,6 +167,30 @@ enum { QLSKUM_KERNEL_GRADIENT = 0, QLSKUM_KERNEL_INNER = 1, QLSKUM_KERNEL_FLUX_U
 qlskum_status qlskum_set_kernel_timing(qlskum_handle *h, int enable);
 qlskum_status qlskum_get_kernel_timing(qlskum_handle *h, int kernel, double *ms_total, long long *launches);
 
+/* ------------------------------------------- stage update without allocation */
+
+/* One SSPRK stage update (the arithmetic of qlskum_state_update) over device
+ * buffers the caller owns, allocating nothing.  No counterpart in the
+ * reference.  It is for callers that cannot allocate device memory while they
+ * run: a host code that hands out every device buffer from its own
+ * pre-allocated arena, or a time-stepping loop that must not take the device
+ * synchronisation of cudaMalloc / cudaFree between its stages.
+ *   flag_1 int32 [n], normals double [n][2] (16-byte aligned), prim (updated
+ *   in place), prim_old and flux_res double [n][4] (32-byte aligned), all in
+ *   the caller's point order; residual_out: device double[2] receiving the
+ *   sum and the maximum of res_sqr over wall and interior points
+ *   (state_update_mod.h:157-165).  stream: a cudaStream_t or NULL.
+ * At most QLSKUM_NOALLOC_MAX_POINTS points; larger n returns
+ * QLSKUM_ERR_INVALID.  The per-block partial sums live in one 128 KiB static
+ * device array that every GPU loading the library keeps until the process
+ * exits.  The first call on a device looks up that array's address; make it
+ * before any stream capture.  Every call reuses the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
+#define QLSKUM_NOALLOC_MAX_POINTS 2097152
+qlskum_status qlskum_state_update_noalloc(int n, int rk, double mach, double aoa, const int *flag_1,
+                                          const double *normals, double *prim, const double *prim_old,
+                                          const double *flux_res, double *residual_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
