@@ -105,6 +105,16 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def max_over_ranks(value: float, dist=None, device="cpu") -> float:
+    """The slowest rank's time (the whole job's time under weak scaling)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peaks():
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -122,19 +132,20 @@ def make_cloud(workload):
 def flux_update_bytes(cloud, precision: str) -> float:
     """Compulsory bytes one fused flux + update launch moves (each array once).
 
-    Per point: own q / dq / qm, normal, limiter eps^2, delta, flag, nbhs,
-    four directional LSQ moment sets (4 x double4), prim in, prim out, q out,
-    prim_old on 1 stage of 4 (averaged), slice base; per edge: neighbour index,
+    Per point: own q / dq / qm, normal, limiter eps^2, delta, flag, nbhs, the
+    directional solve data (mixed: 4 coefficient pairs, 64 B; FP64: 4 LSQ
+    moment sets, 128 B), prim in, prim out, q out, prim_old on 1 stage of 4 and
+    the wave speed on 1 of 4 (averaged), slice base; per edge: neighbour index,
     edge vector / weights, rotated weights, membership byte.  Neighbour
     gathers are served from cache (counted once, as the point's own rows).
     """
     n = cloud.n
     e = int(cloud.nbhs.sum())
     if precision == "mixed":
-        per_pt = 16 + 32 + 32 + 16 + 4 + 8 + 1 + 4 + 128 + 32 + 32 + 16 + 32 / 4 + 8 / 32
+        per_pt = 16 + 32 + 32 + 16 + 4 + 4 + 1 + 4 + 64 + 32 + 32 + 16 + 32 / 4 + 4 / 4 + 8 / 32
         per_edge = 4 + 16 + 8 + 1
     else:
-        per_pt = 32 + 64 + 64 + 16 + 8 + 8 + 1 + 4 + 128 + 32 + 32 + 32 + 32 / 4 + 8 / 32
+        per_pt = 32 + 64 + 64 + 16 + 8 + 8 + 1 + 4 + 128 + 32 + 32 + 32 + 32 / 4 + 8 / 4 + 8 / 32
         per_edge = 4 + 32 + 16 + 1
     return n * per_pt + e * per_edge
 
@@ -277,10 +288,7 @@ def main():
     with ClockSampler(local) as clocks:
         dt, launches = time_solver(qlskum, torch, solver, args.steps)
     barrier()
-    if pg:
-        t = torch.tensor([dt], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        dt = float(t.item())
+    dt = max_over_ranks(dt, pg, "cuda")
     value = cloud.n * args.steps * world / dt
     cl, cd, cm, ent = solver.objective()
 
@@ -341,6 +349,7 @@ def main():
                     "d2h_bytes_per_step": d2h},
             "roofline": roofline, "cpu_baseline": cpu, "fp64_vs_mixed": compare,
             "kernel_ms_per_iteration": {k: v[0] / max(1, 2) for k, v in kt.items()},
+            "launch_config": solver.launch_config(),
         }
         print(json.dumps(line), flush=True)
     if pg:

@@ -352,56 +352,65 @@ __global__ void k_copy(int n, const double4_32a *__restrict__ src, double4_32a *
     if (i < n) dst[i] = src[i];
 }
 
-// compute_force_coeffs_mod.h:37-72 per wall point and compute_entropy_mod.h:
-// 17-21 per point, then ordered tree sums in one block.
-// wall_geo: {ds, nx, ny, ...} is precomputed per shape point: x = ds,
-// y = mx - 0.25, z = my; normals come from the cloud.
-__global__ void k_objective(DevCloud c, const double4_32a *__restrict__ prim, const int *__restrict__ wall_perm,
-                            const double4_32a *__restrict__ wall_geo, int n_wall, double cp_scale, double pr_inf,
-                            double gamma, double *__restrict__ entropy, double *__restrict__ out4)
+// compute_force_coeffs_mod.h:37-72 per shape point and compute_entropy_mod.h:
+// 17-21 per point; each block writes its partial sums of H, V, pitching
+// moment and entropy, k_objective_finish adds the partials in a fixed order.
+// wall_geo per shape point: x = ds, y = mx - 0.25, z = my.
+__global__ void __launch_bounds__(256) k_objective(DevCloud c, const double4_32a *__restrict__ prim,
+                                                   const int *__restrict__ wall_perm,
+                                                   const double4_32a *__restrict__ wall_geo, int n_wall,
+                                                   double cp_scale, double pr_inf, double gamma,
+                                                   double *__restrict__ entropy, double *__restrict__ partial)
 {
-    __shared__ double sh[3][256], se[256];
+    __shared__ double sh[4][256];
+    const int t = blockIdx.x * 256 + threadIdx.x;
     double H = 0, V = 0, Mo = 0, E = 0;
-    for (int j = threadIdx.x; j < n_wall; j += 256) {
-        const int m = wall_perm[j];
-        const double4_32a w = wall_geo[j];
+    if (t < n_wall) {
+        const int m = wall_perm[t];
+        const double4_32a w = wall_geo[t];
         const double2 nn = c.nrm[m];
         double cp = prim[m].w - pr_inf;
         cp = -cp / cp_scale;
-        H = H + cp * nn.x * w.x;
-        V = V + cp * nn.y * w.x;
-        Mo = Mo + (-cp * nn.y * w.x * w.y + cp * nn.x * w.x * w.z);
+        H = cp * nn.x * w.x;
+        V = cp * nn.y * w.x;
+        Mo = (-cp * nn.y * w.x * w.y + cp * nn.x * w.x * w.z);
     }
-    const double temp2 = log(pr_inf);
-    for (int k = threadIdx.x; k < c.n; k += 256) {
-        const double4_32a P = prim[k];
+    if (t < c.n) {
+        const double4_32a P = prim[t];
         double temp1 = pow(P.x, gamma);
         temp1 = P.w / temp1;
         temp1 = log(temp1);
-        const double s = fabs(temp1 - temp2);
-        entropy[k] = s;
-        E = E + s;
+        const double s = fabs(temp1 - log(pr_inf));
+        entropy[t] = s;
+        E = s;
     }
     sh[0][threadIdx.x] = H;
     sh[1][threadIdx.x] = V;
     sh[2][threadIdx.x] = Mo;
-    se[threadIdx.x] = E;
+    sh[3][threadIdx.x] = E;
     __syncthreads();
-    for (int s = 128; s > 0; s >>= 1) {
-        if (threadIdx.x < s) {
-            sh[0][threadIdx.x] += sh[0][threadIdx.x + s];
-            sh[1][threadIdx.x] += sh[1][threadIdx.x + s];
-            sh[2][threadIdx.x] += sh[2][threadIdx.x + s];
-            se[threadIdx.x] += se[threadIdx.x + s];
-        }
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st)
+            for (int q = 0; q < 4; q++) sh[q][threadIdx.x] += sh[q][threadIdx.x + st];
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        out4[0] = sh[0][0];
-        out4[1] = sh[1][0];
-        out4[2] = sh[2][0];
-        out4[3] = se[0];
+    if (threadIdx.x < 4) partial[4 * blockIdx.x + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void k_objective_finish(int nblocks, const double *__restrict__ partial, double *__restrict__ out4)
+{
+    __shared__ double sh[4][256];
+    double v[4] = {0, 0, 0, 0};
+    for (int b = threadIdx.x; b < nblocks; b += 256)
+        for (int q = 0; q < 4; q++) v[q] += partial[4 * b + q];
+    for (int q = 0; q < 4; q++) sh[q][threadIdx.x] = v[q];
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st)
+            for (int q = 0; q < 4; q++) sh[q][threadIdx.x] += sh[q][threadIdx.x + st];
+        __syncthreads();
     }
+    if (threadIdx.x < 4) out4[threadIdx.x] = sh[threadIdx.x][0];
 }
 
 // ------------------------------------------------------------- launchers
@@ -478,12 +487,16 @@ void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
     QLSKUM_LAUNCHED(L);
 }
 
-void objective(const Launch &L, const DevCloud &c, const double4_32a *prim, const int *wall_perm, const double4_32a *wall_geo,
-               int n_wall, double cp_scale, double pr_inf, double gamma, double *entropy, double *out4, double *)
+void objective(const Launch &L, const DevCloud &c, const double4_32a *prim, const int *wall_perm,
+               const double4_32a *wall_geo, int n_wall, double cp_scale, double pr_inf, double gamma, double *entropy,
+               double *out4, double *scratch)
 {
-    k_objective<<<1, 256, 0, L.stream>>>(c, prim, wall_perm, wall_geo, n_wall, cp_scale, pr_inf, gamma, entropy,
-                                         out4);
-    QLSKUM_LAUNCHED(L);
+    const int items = c.n > n_wall ? c.n : n_wall;
+    const int blocks = grid_for(items, 256);
+    k_objective<<<blocks, 256, 0, L.stream>>>(c, prim, wall_perm, wall_geo, n_wall, cp_scale, pr_inf, gamma, entropy,
+                                              scratch);
+    k_objective_finish<<<1, 256, 0, L.stream>>>(blocks, scratch, out4);
+    if (L.launches) *L.launches += 2;
 }
 
 }  // namespace fp64

@@ -108,11 +108,16 @@ struct qlskum_handle {
     bool derived_valid = false;  // q[0] and cspeed match prim[pcur] for the fused solver
     int it = 0;
     double *d_obj = nullptr;
+    double *d_obj_partial = nullptr;
     double *d_entropy = nullptr;
     double *d_last = nullptr;
     int *d_wall_perm = nullptr;
     double4_32a *d_wall_geo = nullptr;
     cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+    // launch shape of the mixed fused kernel and of the point kernels, set by
+    // tune() on the first fused iteration unless params.block_size fixes it
+    int flux_variant = 0;
+    bool tuned = false;
     // per-kernel event timing (qlskum_set_kernel_timing)
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -353,15 +358,19 @@ qlskum_status ensure_hist(qlskum_handle *h, int needed)
     return QLSKUM_OK;
 }
 
+qlskum_status tune(qlskum_handle *h);
+
 qlskum_status ensure_derived(qlskum_handle *h)
 {
     if (h->derived_valid) return QLSKUM_OK;
     if (h->prm.precision == QLSKUM_MIXED)
-        mixed::derived(h->L, h->dc, h->s64.prim[h->pcur], h->s32.q[0], h->s64.cspeed);
+        mixed::derived(h->L, h->dc, h->s64.prim[h->pcur], h->s32.q[0], h->s32.cspeed);
     else
         fp64::derived(h->L, h->dc, h->s64.prim[h->pcur], h->s64.q[0], h->s64.cspeed);
     h->derived_valid = true;
-    return check_launch(h, "derived");
+    qlskum_status st = check_launch(h, "derived");
+    if (st) return st;
+    return tune(h);
 }
 
 cudaEvent_t take_event(qlskum_handle *h)
@@ -406,6 +415,56 @@ qlskum_status collect_timing(qlskum_handle *h)
     return QLSKUM_OK;
 }
 
+// Autotuner of the mixed form: times each launch shape of the fused flux +
+// update kernel (threads per block x register cap) and each block size of the
+// gradient / inner-loop kernels on this cloud, three launches each after one
+// warm-up, and keeps the fastest.  The trial launches write only buffers the
+// next iteration overwrites before reading (stage-1 targets, dq, qm, delta).
+qlskum_status tune(qlskum_handle *h)
+{
+    if (h->tuned || h->prm.precision != QLSKUM_MIXED) return QLSKUM_OK;
+    h->tuned = true;
+    if (h->prm.block_size != 0) return QLSKUM_OK;
+    const DevCloud &c = h->dc;
+    State32 &S = h->s32;
+    const int o = h->pcur, x = (o + 1) % 3;
+    cudaEvent_t a = take_event(h), b = take_event(h);
+    auto time3 = [&](auto &&launch) -> float {
+        launch();
+        cudaEventRecord(a, h->L.stream);
+        for (int r = 0; r < 3; r++) launch();
+        cudaEventRecord(b, h->L.stream);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        return ms;
+    };
+    long long launches0 = h->launches;
+    static const int blocks[4] = {64, 128, 256, 512};
+    float best = 1e30f;
+    int best_block = h->L.block;
+    for (int bs : blocks) {
+        Launch L = h->L;
+        L.block = bs;
+        float ms = time3([&] { mixed::q_inner(L, c, S.q[0], S.dq[0], S.dq[1]); });
+        if (ms < best) { best = ms; best_block = bs; }
+    }
+    h->L.block = best_block;
+    mixed::q_derivatives(h->L, c, S.q[0], S.dq[0], S.qm, S.cspeed, S.delta, (float)h->K.cfl);
+    best = 1e30f;
+    for (int v = 0; v < mixed::flux_variants(); v++) {
+        float ms = time3([&] {
+            mixed::flux_update(h->L, c, h->K, S.q[0], S.dq[0], S.qm, S.delta, h->s64.prim[o], h->s64.prim[o],
+                               h->s64.prim[x], S.q[1], nullptr, 1, h->R, v);
+        });
+        if (ms < best) { best = ms; h->flux_variant = v; }
+    }
+    h->launches = launches0;
+    h->ev_pool.push_back(a);
+    h->ev_pool.push_back(b);
+    return check_launch(h, "tune");
+}
+
 // The kernels of one fused iteration from prim buffer o (fpi_solver_mod.h:
 // 14-151).  Stage buffers: o -> x -> y -> x -> y, prim_old = o throughout;
 // q ping-pongs q0 -> q1 -> q0 -> q1 -> q0.
@@ -425,14 +484,16 @@ void enqueue_iteration(qlskum_handle *h, int o, int it_arg)
         double4_32a *pout = h->s64.prim[dst[rk - 1]];
         if (h->prm.precision == QLSKUM_MIXED) {
             State32 &S = h->s32;
+            float *dl32 = rk == 1 ? S.delta : nullptr;
+            float *cs32 = rk == 4 ? S.cspeed : nullptr;
             timed(h, QLSKUM_KERNEL_GRADIENT, [&] {
-                mixed::q_derivatives(L, c, S.q[qa], S.dq[0], S.qm, h->s64.cspeed, dl, h->K.cfl);
+                mixed::q_derivatives(L, c, S.q[qa], S.dq[0], S.qm, S.cspeed, dl32, (float)h->K.cfl);
             });
             for (int j = 0; j < ni; j++)
                 timed(h, QLSKUM_KERNEL_INNER, [&] { mixed::q_inner(L, c, S.q[qa], S.dq[j & 1], S.dq[(j + 1) & 1]); });
             timed(h, QLSKUM_KERNEL_FLUX_UPDATE, [&] {
-                mixed::flux_update(L, c, h->K, S.q[qa], S.dq[ni & 1], S.qm, h->s64.delta, pin, pold, pout, S.q[qb],
-                                   cs, rk, h->R);
+                mixed::flux_update(L, c, h->K, S.q[qa], S.dq[ni & 1], S.qm, S.delta, pin, pold, pout, S.q[qb], cs32,
+                                   rk, h->R, h->flux_variant);
             });
         } else {
             State64 &S = h->s64;
@@ -447,7 +508,10 @@ void enqueue_iteration(qlskum_handle *h, int o, int it_arg)
             });
         }
     }
-    timed(h, QLSKUM_KERNEL_REDUCE, [&] { fp64::reduce_residual(L, h->R, h->n, it_arg); });
+    Reduce R = h->R;
+    R.blocks = (h->n + (h->prm.precision == QLSKUM_MIXED ? mixed::flux_block(h->flux_variant) : 128) - 1) /
+               (h->prm.precision == QLSKUM_MIXED ? mixed::flux_block(h->flux_variant) : 128);
+    timed(h, QLSKUM_KERNEL_REDUCE, [&] { fp64::reduce_residual(L, R, h->n, it_arg); });
 }
 
 void after_iteration(qlskum_handle *h, int o)
@@ -585,6 +649,8 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
     std::vector<float> eps2_32(h->np, 0.0f);
     std::vector<double4_32a> ggeo(h->np, make_double4_32a(0, 0, 0, 0));
     std::vector<double4_32a> fgeo((size_t)h->np * 4, make_double4_32a(0, 0, 0, 0));
+    std::vector<double2> fcoef((size_t)h->np * 4, make_double2(0, 0));
+    std::vector<float> e_dist32(ne, 1.0f);
     const Precomp &P = h->pc;
     for (int pp = 0; pp < n; pp++) {
         const int i = h->iperm[pp];
@@ -595,9 +661,19 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
         eps2_32[pp] = (float)P.eps2[i];
         ggeo[pp] = make_double4_32a(P.ggeo[4 * (size_t)i], P.ggeo[4 * (size_t)i + 1], P.ggeo[4 * (size_t)i + 2],
                                 P.ggeo[4 * (size_t)i + 3]);
+        static const bool used[3][4] = {{true, true, false, true}, {true, true, true, true}, {true, true, true, false}};
+        const int fl = c->flag_1[i];
+        const double scale = fl == kWall ? 2.0 : 1.0;  // flux_residual_mod.h:29
         for (int d = 0; d < 4; d++) {
             const double *F = &P.fgeo[((size_t)i * 4 + d) * 4];
             fgeo[(size_t)pp * 4 + d] = make_double4_32a(F[0], F[1], F[2], F[3]);
+            // x rows (d < 2): G = (Sx syy - Sy sxy) / det;  y rows: G = (Sy sxx - Sx sxy) / det
+            double a = 0.0, b = 0.0;
+            if (used[fl][d]) {
+                if (d < 2) { a = scale * F[1] * F[3]; b = -scale * F[2] * F[3]; }
+                else { a = -scale * F[2] * F[3]; b = scale * F[0] * F[3]; }
+            }
+            fcoef[(size_t)pp * 4 + d] = make_double2(a, b);
         }
         for (int r = 0; r < c->nbhs[i]; r++) {
             const size_t e = (size_t)(sbase[pp >> 5] + 32LL * r + (pp & 31));
@@ -606,6 +682,7 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
             e_geo[e] = make_double4_32a(P.geo[4 * src], P.geo[4 * src + 1], P.geo[4 * src + 2], P.geo[4 * src + 3]);
             e_sn[e] = make_double2(P.sn[2 * src], P.sn[2 * src + 1]);
             e_dist[e] = P.dist[src];
+            e_dist32[e] = (float)P.dist[src];
             e_dir[e] = P.edge_dir[src];
             e_geo32[e] = make_float4((float)P.geo[4 * src], (float)P.geo[4 * src + 1], (float)P.geo[4 * src + 2],
                                      (float)P.geo[4 * src + 3]);
@@ -641,19 +718,23 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
     double4_32a *d_fgeo = A.alloc<double4_32a>((size_t)h->np * 4);
     float4 *d_egeo32 = nullptr;
     float2 *d_esn32 = nullptr;
-    float *d_eps32 = nullptr;
+    float *d_eps32 = nullptr, *d_edist32 = nullptr;
+    double2 *d_fcoef = nullptr;
     if (p->precision == QLSKUM_MIXED) {
         d_egeo32 = A.alloc<float4>(ne);
         d_esn32 = A.alloc<float2>(ne);
         d_eps32 = A.alloc<float>(h->np);
+        d_edist32 = A.alloc<float>(ne);
+        d_fcoef = A.alloc<double2>((size_t)h->np * 4);
     }
     up(d_flag, flag); up(d_nb, nbh); up(d_sb, sbase); up(d_enbr, e_nbr); up(d_egeo, e_geo); up(d_esn, e_sn);
     up(d_edist, e_dist); up(d_edir, e_dir); up(d_nrm, nrm); up(d_eps2, eps2); up(d_ggeo, ggeo); up(d_fgeo, fgeo);
-    up(d_egeo32, e_geo32); up(d_esn32, e_sn32); up(d_eps32, eps2_32);
+    up(d_egeo32, e_geo32); up(d_esn32, e_sn32); up(d_eps32, eps2_32); up(d_edist32, e_dist32); up(d_fcoef, fcoef);
     DevCloud &dc = h->dc;
     dc.n = n; dc.np = h->np; dc.flag = d_flag; dc.nbhs = d_nb; dc.slice_base = d_sb; dc.e_nbr = d_enbr;
     dc.e_geo = d_egeo; dc.e_sn = d_esn; dc.e_dist = d_edist; dc.e_dir = d_edir; dc.nrm = d_nrm; dc.eps2 = d_eps2;
     dc.ggeo = d_ggeo; dc.fgeo = d_fgeo; dc.e_geo32 = d_egeo32; dc.e_sn32 = d_esn32; dc.eps2_32 = d_eps32;
+    dc.e_dist32 = d_edist32; dc.fcoef = d_fcoef;
 
     for (int b = 0; b < 3; b++) h->s64.prim[b] = A.alloc<double4_32a>(h->np);
     for (int b = 0; b < 2; b++) {
@@ -670,14 +751,18 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
             h->s32.dq[b] = A.alloc<float4>((size_t)h->np * 2);
         }
         h->s32.qm = A.alloc<float4>((size_t)h->np * 2);
+        h->s32.delta = A.alloc<float>(h->np);
+        h->s32.cspeed = A.alloc<float>(h->np);
     }
     h->R.blocks = (n + 127) / 128;
-    h->R.partial_sum = A.alloc<double>(h->R.blocks);
-    h->R.partial_max = A.alloc<double>(h->R.blocks);
+    h->R.max_blocks = (n + 63) / 64;
+    h->R.partial_sum = A.alloc<double>(h->R.max_blocks);
+    h->R.partial_max = A.alloc<double>(h->R.max_blocks);
     h->R.res_old = A.alloc<double>(1);
     h->R.iter = A.alloc<int>(1);
     h->R.status = A.alloc<int>(1);
     h->d_obj = A.alloc<double>(8);
+    h->d_obj_partial = A.alloc<double>(4 * (size_t)((std::max(n, sp) + 255) / 256));
     h->d_entropy = A.alloc<double>(h->np);
     h->d_last = A.alloc<double>(2);
     h->d_wall_perm = A.alloc<int>(std::max(sp, 1));
@@ -898,7 +983,7 @@ qlskum_status qlskum_objective(qlskum_handle *h, double *cl, double *cd, double 
     NEED(h);
     const double cp_scale = 0.5 * h->K.rho_inf * h->K.mach * h->K.mach;
     fp64::objective(h->L, h->dc, h->s64.prim[h->pcur], h->d_wall_perm, h->d_wall_geo, h->shape_points, cp_scale,
-                    h->K.pr_inf, h->K.gamma, h->d_entropy, h->d_obj, nullptr);
+                    h->K.pr_inf, h->K.gamma, h->d_entropy, h->d_obj, h->d_obj_partial);
     qlskum_status st = check_launch(h, "objective");
     if (st) return st;
     double o[4];
@@ -976,6 +1061,8 @@ qlskum_status qlskum_set_prim(qlskum_handle *h, const double *prim)
     }
     CK(h, cudaMemcpyAsync(h->s64.prim[h->pcur], dev.data(), sizeof(double4_32a) * h->np, cudaMemcpyHostToDevice,
                           h->L.stream));
+    // a new state clears a non-finite flag raised by the old one
+    CK(h, cudaMemsetAsync(h->R.status, 0, sizeof(int), h->L.stream));
     CK(h, cudaStreamSynchronize(h->L.stream));
     h->derived_valid = false;
     return QLSKUM_OK;
@@ -1019,6 +1106,16 @@ qlskum_status qlskum_synchronize(qlskum_handle *h)
 void *qlskum_stream(qlskum_handle *h) { return h ? (void *)h->L.stream : nullptr; }
 
 long long qlskum_launch_count(const qlskum_handle *h) { return h ? h->launches : 0; }
+
+qlskum_status qlskum_get_launch_config(qlskum_handle *h, int *flux_block, int *flux_min_blocks, int *point_block)
+{
+    NEED(h);
+    static const int minb[4] = {4, 5, 8, 2};
+    if (flux_block) *flux_block = h->prm.precision == QLSKUM_MIXED ? mixed::flux_block(h->flux_variant) : 128;
+    if (flux_min_blocks) *flux_min_blocks = h->prm.precision == QLSKUM_MIXED ? minb[h->flux_variant] : 1;
+    if (point_block) *point_block = h->L.block;
+    return QLSKUM_OK;
+}
 
 qlskum_status qlskum_set_kernel_timing(qlskum_handle *h, int enable)
 {

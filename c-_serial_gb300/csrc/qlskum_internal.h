@@ -43,7 +43,15 @@ struct DevCloud {
     // mixed-precision copies of the per-edge geometry (FP32)
     const float4 *e_geo32 = nullptr;         // delx, dely, w*delx, w*dely
     const float2 *e_sn32 = nullptr;          // dels*w, deln*w
+    const float *e_dist32 = nullptr;         // |r_k - r_i|
     const float *eps2_32 = nullptr;
+    // Mixed form: the four directional 2x2 solves and their combination into
+    // the flux residual folded into one coefficient pair per direction,
+    // F = delta * sum_d (a_d * Sx_d + b_d * Sy_d) with Sx_d = sum dG dels w,
+    // Sy_d = sum dG deln w; a_d, b_d carry 1/det, the x / y row of the
+    // inverse, the wall's factor 2 and zero for directions a class does not
+    // use.  FP64, [np][4].
+    const double2 *fcoef = nullptr;
 };
 
 // Free-stream constants of one case (parameter_mod.h:4-30).
@@ -64,11 +72,15 @@ struct State64 {
     double *cspeed = nullptr;                // |u| + 3 sqrt(p/rho) of the current prim
 };
 
-// Mixed-precision state: q, dq, qm in FP32, prim in FP64.
+// Mixed-precision state: q, dq, qm in FP32, prim in FP64; the local time step
+// and the wave speed it is built from in FP32 (a pseudo-time step size: its
+// rounding does not move the steady state).
 struct State32 {
     float4 *q[2] = {nullptr, nullptr};
     float4 *dq[2] = {nullptr, nullptr};      // [np][2]
     float4 *qm = nullptr;                    // [np][2]
+    float *delta = nullptr;
+    float *cspeed = nullptr;
 };
 
 // Residual reduction scratch.
@@ -80,7 +92,8 @@ struct Reduce {
     int *iter = nullptr;                     // [1] iterations completed
     int *status = nullptr;                   // [1] 0 ok, 1 non-finite residual
     int capacity = 0;
-    int blocks = 0;
+    int blocks = 0;                          // partials written by the last stage kernel
+    int max_blocks = 0;                      // partials allocated (n / 64 rounded up)
 };
 
 struct Launch {
@@ -106,20 +119,22 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const d
                  double4_32a *prim_next, double4_32a *q_next, double *cspeed_next, int rk, const Reduce &R);
 void reduce_residual(const Launch &L, const Reduce &R, int n, int it);
 void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
-// objectives: per-wall-point contributions then ordered tree sums
+// objectives: per-block partial sums into scratch ([4][ceil(max(n, n_wall)/256)]), then one ordered sum
 void objective(const Launch &L, const DevCloud &c, const double4_32a *prim, const int *wall_perm, const double4_32a *wall_geo,
                int n_wall, double cp_scale, double pr_inf, double gamma, double *entropy, double *out4, double *scratch);
 }  // namespace fp64
 
 // ---------------------------------------------------------- mixed kernels (qlskum_mixed.cu)
 namespace mixed {
-void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, float4 *q, double *cspeed);
+void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, float4 *q, float *cspeed);
 void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *dq, float4 *qm,
-                   const double *cspeed, double *delta, double cfl);
+                   const float *cspeed, float *delta, float cfl);
 void q_inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, float4 *dq_out);
 void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const float4 *q, const float4 *dq,
-                 const float4 *qm, const double *delta, const double4_32a *prim, const double4_32a *prim_old,
-                 double4_32a *prim_next, float4 *q_next, double *cspeed_next, int rk, const Reduce &R);
+                 const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
+                 double4_32a *prim_next, float4 *q_next, float *cspeed_next, int rk, const Reduce &R, int variant);
+int flux_variants();
+int flux_block(int variant);
 }  // namespace mixed
 
 }  // namespace qlskum

@@ -13,6 +13,11 @@
 
 namespace qlskum {
 
+// Elementary operations per real type.  For double they are exactly the
+// reference's: IEEE division and square root, libm-style exp / log / erf.
+// For float (mixed form only) divisions and square roots use the
+// reciprocal / reciprocal-square-root units (2 ulp), exp / log / erf stay the
+// accurate single-precision functions.
 template <typename R> struct M;
 template <> struct M<double> {
     static __device__ __forceinline__ double ex(double x) { return exp(x); }
@@ -20,13 +25,18 @@ template <> struct M<double> {
     static __device__ __forceinline__ double ef(double x) { return erf(x); }
     static __device__ __forceinline__ double sq(double x) { return sqrt(x); }
     static __device__ __forceinline__ double ab(double x) { return fabs(x); }
+    static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+    // a / sqrt(x)
+    static __device__ __forceinline__ double rdsq(double a, double x) { return a / sqrt(x); }
 };
 template <> struct M<float> {
     static __device__ __forceinline__ float ex(float x) { return expf(x); }
     static __device__ __forceinline__ float lg(float x) { return logf(x); }
     static __device__ __forceinline__ float ef(float x) { return erff(x); }
-    static __device__ __forceinline__ float sq(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ float sq(float x) { return x * rsqrtf(x); }
     static __device__ __forceinline__ float ab(float x) { return fabsf(x); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+    static __device__ __forceinline__ float rdsq(float a, float x) { return a * rsqrtf(x); }
 };
 
 // 4 * atan(1.0) of parameter_mod.h:10, as a literal.
@@ -43,7 +53,7 @@ __device__ __forceinline__ float4 mk4(const float o[4]) { return make_float4(o[0
 template <typename R>
 __device__ __forceinline__ void prim_to_q(R rho, R u1, R u2, R pr, R q[4])
 {
-    R beta = R(0.5) * rho / pr;
+    R beta = M<R>::div(R(0.5) * rho, pr);
     q[0] = M<R>::lg(rho) + (M<R>::lg(beta) * R(2.5)) - beta * (u1 * u1 + u2 * u2);
     R two_times_beta = R(2.0) * beta;
     q[1] = two_times_beta * u1;
@@ -64,7 +74,7 @@ __device__ __forceinline__ R venkat(R qt, R q, R qmax, R qmin, R eps2)
     R den = del_pos * del_pos + R(2.0) * del_neg * del_neg;
     den = den + del_neg * del_pos + eps2;
     den = den * del_neg;
-    R temp = num / den;
+    R temp = M<R>::div(num, den);
     return temp < R(1) ? temp : R(1);
 }
 
@@ -73,11 +83,11 @@ template <typename R>
 __device__ __forceinline__ void qtilde_to_prim(const R qt[4], R &u1, R &u2, R &rho, R &pr)
 {
     R beta = -qt[3] * R(0.5);
-    R temp = R(0.5) / beta;
+    R temp = M<R>::div(R(0.5), beta);
     u1 = qt[1] * temp;
     u2 = qt[2] * temp;
     R temp1 = qt[0] + beta * (u1 * u1 + u2 * u2);
-    R temp2 = temp1 - (M<R>::lg(beta) / (R(1.4) - R(1)));
+    R temp2 = temp1 - M<R>::div(M<R>::lg(beta), R(1.4) - R(1));
     rho = M<R>::ex(temp2);
     pr = rho * temp;
 }
@@ -95,16 +105,15 @@ __device__ __forceinline__ void kin_prep(R nx, R ny, R u1, R u2, R rho, R pr, Ki
     R tx = ny, ty = -nx;
     k.ut = u1 * tx + u2 * ty;
     k.un = u1 * nx + u2 * ny;
-    R beta = R(0.5) * rho / pr;
+    R beta = M<R>::div(R(0.5) * rho, pr);
     R sb = M<R>::sq(beta);
-    R spb = M<R>::sq(R(QLSKUM_PI) * beta);
     R S1 = k.ut * sb;
     R S2 = k.un * sb;
-    k.B1 = R(0.5) * M<R>::ex(-S1 * S1) / spb;
-    k.B2 = R(0.5) * M<R>::ex(-S2 * S2) / spb;
+    k.B1 = M<R>::rdsq(R(0.5) * M<R>::ex(-S1 * S1), R(QLSKUM_PI) * beta);
+    k.B2 = M<R>::rdsq(R(0.5) * M<R>::ex(-S2 * S2), R(QLSKUM_PI) * beta);
     k.E1 = M<R>::ef(S1);
     k.E2 = M<R>::ef(S2);
-    k.pbr = pr / rho;
+    k.pbr = M<R>::div(pr, rho);
     k.usq = k.ut * k.ut + k.un * k.un;
     k.rho = rho;
 }

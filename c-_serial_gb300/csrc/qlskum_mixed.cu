@@ -4,8 +4,14 @@
 // wall stencils), the flux residual, the SSPRK update and the residual sum in
 // FP64.  Same algorithm, edge order and data layout as the FP64 kernels
 // (qlskum_fp64.cu); q, dq and qm are stored in FP32, which halves the bytes
-// gathered per neighbour, and FP32 runs at many times the FP64 rate on this
-// chip.  Built with FMA contraction on.
+// gathered per neighbour.  Built with FMA contraction on.
+//
+// On GB300 FP64 runs at about 1/64 of the FP32 rate, so the O(points) FP64
+// work is kept to a minimum: the four directional solves and their sum are
+// one FMA chain over precomputed coefficient pairs (DevCloud::fcoef), the
+// conserved-variable update has no FP64 division (one reciprocal from an FP32
+// seed and two Newton steps), and the local time step and its wave speed are
+// FP32 (they only set the pseudo-time step, not the steady state).
 #include "qlskum_math.cuh"
 
 namespace qlskum {
@@ -18,7 +24,68 @@ __device__ __forceinline__ void q_of(const double P[4], float Q[4])
     prim_to_q<float>((float)P[0], (float)P[1], (float)P[2], (float)P[3], Q);
 }
 
-__global__ void k_derived(int n, const double4_32a *__restrict__ prim, float4 *__restrict__ q, double *__restrict__ cs)
+// |u| + 3 sqrt(p / rho) in FP32 (state_update_mod.h:483-485)
+__device__ __forceinline__ float wave_speed32(const double P[4])
+{
+    const float rho = (float)P[0], u1 = (float)P[1], u2 = (float)P[2], p = (float)P[3];
+    return sqrtf(u1 * u1 + u2 * u2) + 3.0f * sqrtf(__fdividef(p, rho));
+}
+
+// 1 / x in FP64 without a division: FP32 seed, two Newton steps.
+__device__ __forceinline__ double recip64(double x)
+{
+    double r = (double)__frcp_rn((float)x);
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+
+// primitive_to_conserved (state_update_mod.h:18-33) rearranged for FMA and
+// without the division: 0.5 (t1^2 + t2^2) / rho == 0.5 rho |u|^2.
+__device__ __forceinline__ void p2c_fast(const double P[4], double nx, double ny, double U[4])
+{
+    const double t1 = P[0] * P[1], t2 = P[0] * P[2];
+    U[0] = P[0];
+    U[3] = fma(0.5, fma(t1, P[1], t2 * P[2]), 2.5 * P[3]);
+    U[1] = fma(t1, ny, -t2 * nx);
+    U[2] = fma(t1, nx, t2 * ny);
+}
+
+// One SSPRK stage of one point (state_update_mod.h:111-282), FP64.
+__device__ __forceinline__ double stage_update_fast(const CaseConst &K, int f, double nx, double ny, double P[4],
+                                                    const double4_32a *prim_old_i, const double F[4], int rk)
+{
+    double U[4];
+    if (f == kOuter) conserved_vector_Ubar(K, P, nx, ny, U);
+    else p2c_fast(P, nx, ny, U);
+    const double rho0 = U[0];
+    if (rk != 3) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) U[j] = fma(-0.5, F[j], U[j]);
+    } else {
+        double Po[4], Uo[4];
+        ld4(*prim_old_i, Po);
+        if (f == kOuter) conserved_vector_Ubar(K, Po, nx, ny, Uo);
+        else p2c_fast(Po, nx, ny, Uo);
+#pragma unroll
+        for (int j = 0; j < 4; j++) U[j] = fma(2.0 / 3.0, Uo[j], (1.0 / 3.0) * fma(-0.5, F[j], U[j]));
+    }
+    if (f == kWall) U[2] = 0.;
+    const double U2r = U[1], U3r = U[2];
+    U[1] = fma(U2r, ny, U3r * nx);
+    U[2] = fma(U3r, ny, -U2r * nx);
+    const double d = U[0] - rho0;
+    const double res_sqr = (f == kOuter) ? 0.0 : d * d;
+    const double inv = recip64(U[0]);
+    P[0] = U[0];
+    P[1] = U[1] * inv;
+    P[2] = U[2] * inv;
+    P[3] = fma(-0.2 * inv, fma(U[1], U[1], U[2] * U[2]), 0.4 * U[3]);
+    return res_sqr;
+}
+
+__global__ void k_derived(int n, const double4_32a *__restrict__ prim, float4 *__restrict__ q, float *__restrict__ cs)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -27,13 +94,14 @@ __global__ void k_derived(int n, const double4_32a *__restrict__ prim, float4 *_
     ld4(prim[i], P);
     q_of(P, Q);
     q[i] = mk4(Q);
-    cs[i] = wave_speed(P);
+    cs[i] = wave_speed32(P);
 }
 
-// q_variables_mod.h:36-118: FP32 differences and sums, FP64 solve.
+// q_variables_mod.h:36-118: FP32 differences and sums, FP64 solve; in the
+// first stage also the local time step (state_update_mod.h:448-496) in FP32.
 __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4 *__restrict__ dq,
-                                float4 *__restrict__ qm, const double *__restrict__ cs, double *__restrict__ delta,
-                                double cfl)
+                                float4 *__restrict__ qm, const float *__restrict__ cs, float *__restrict__ delta,
+                                float cfl)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
@@ -41,7 +109,7 @@ __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4
     ld4(q[i], qi);
 #pragma unroll
     for (int r = 0; r < 4; r++) { qmax[r] = qi[r]; qmin[r] = qi[r]; }
-    double min_delt = 1.0;
+    float min_dt = 1.0f;
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
     for (int j = 0; j < nb; j++) {
@@ -57,10 +125,7 @@ __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4
             sdx[r] += g.z * (qk[r] - qi[r]);
             sdy[r] += g.w * (qk[r] - qi[r]);
         }
-        if (delta) {
-            double delta_t = cfl * (c.e_dist[e] / cs[k]);
-            min_delt = delta_t < min_delt ? delta_t : min_delt;
-        }
+        if (delta) min_dt = fminf(min_dt, cfl * __fdividef(c.e_dist32[e], cs[k]));
     }
     const double4_32a m = c.ggeo[i];
     float dx[4], dy[4];
@@ -73,7 +138,7 @@ __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4
     dq[2 * i + 1] = mk4(dy);
     qm[2 * i] = mk4(qmax);
     qm[2 * i + 1] = mk4(qmin);
-    if (delta) delta[i] = min_delt;
+    if (delta) delta[i] = min_dt;
 }
 
 // q_variables_mod.h:120-213
@@ -116,14 +181,14 @@ __global__ void k_q_inner(DevCloud c, const float4 *__restrict__ q, const float4
 }
 
 // Fused stage: FP32 edge work, FP64 solve / residual / update.
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_flux_update(DevCloud c, CaseConst K, const float4 *__restrict__ q,
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseConst K, const float4 *__restrict__ q,
                                                        const float4 *__restrict__ dq, const float4 *__restrict__ qm,
-                                                       const double *__restrict__ delta,
+                                                       const float *__restrict__ delta,
                                                        const double4_32a *__restrict__ prim,
                                                        const double4_32a *__restrict__ prim_old,
                                                        double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
-                                                       double *__restrict__ cs_next, int rk,
+                                                       float *__restrict__ cs_next, int rk,
                                                        double *__restrict__ psum, double *__restrict__ pmax)
 {
     int i = blockIdx.x * BLOCK + threadIdx.x;
@@ -179,30 +244,30 @@ __global__ void __launch_bounds__(BLOCK) k_flux_update(DevCloud c, CaseConst K, 
             QLSKUM_ACC32(3)
 #undef QLSKUM_ACC32
         }
-        double G[4][4];
+        // F = delta * sum_d (a_d Sx_d + b_d Sy_d): the four solves and
+        // flux_residual_mod.h's sum (with the wall's 2 delta) in FP64.
+        double2 cf[4];
 #pragma unroll
-        for (int d = 0; d < 4; d++) {
-            const double4_32a m = c.fgeo[4 * i + d];
-#pragma unroll
-            for (int r = 0; r < 4; r++)
-                G[d][r] = (d < 2) ? ((double)sx[d][r] * m.y - (double)sy[d][r] * m.z) * m.w
-                                  : ((double)sy[d][r] * m.x - (double)sx[d][r] * m.z) * m.w;
-        }
-        const double dl = delta[i];
+        for (int d = 0; d < 4; d++) cf[d] = c.fcoef[4 * i + d];
+        const double dl = (double)delta[i];
         double F[4], P[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            if (f == kWall) F[j] = (2.0 * dl) * (G[0][j] + G[1][j] + G[3][j]);
-            else if (f == kInterior) F[j] = dl * (G[0][j] + G[1][j] + G[2][j] + G[3][j]);
-            else F[j] = dl * (G[0][j] + G[1][j] + G[2][j]);
+        for (int r = 0; r < 4; r++) {
+            double acc = 0.0;
+#pragma unroll
+            for (int d = 0; d < 4; d++) {
+                acc = fma(cf[d].x, (double)sx[d][r], acc);
+                acc = fma(cf[d].y, (double)sy[d][r], acc);
+            }
+            F[r] = dl * acc;
         }
         ld4(prim[i], P);
-        r2 = stage_update(K, f, nn.x, nn.y, P, prim_old + i, F, rk);
+        r2 = stage_update_fast(K, f, nn.x, nn.y, P, prim_old + i, F, rk);
         prim_next[i] = mk4(P);
         float Q[4];
         q_of(P, Q);
         q_next[i] = mk4(Q);
-        if (cs_next) cs_next[i] = wave_speed(P);
+        if (cs_next) cs_next[i] = wave_speed32(P);
     }
     if (psum) block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
 }
@@ -210,14 +275,14 @@ __global__ void __launch_bounds__(BLOCK) k_flux_update(DevCloud c, CaseConst K, 
 #define QLSKUM_LAUNCHED(L) \
     do { if ((L).launches) ++*(L).launches; } while (0)
 
-void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, float4 *q, double *cspeed)
+void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, float4 *q, float *cspeed)
 {
     k_derived<<<grid_for(c.n, 256), 256, 0, L.stream>>>(c.n, prim, q, cspeed);
     QLSKUM_LAUNCHED(L);
 }
 
-void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *dq, float4 *qm, const double *cspeed,
-                   double *delta, double cfl)
+void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *dq, float4 *qm, const float *cspeed,
+                   float *delta, float cfl)
 {
     k_q_derivatives<<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
     QLSKUM_LAUNCHED(L);
@@ -229,13 +294,29 @@ void q_inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *
     QLSKUM_LAUNCHED(L);
 }
 
+// Launch-shape variants of the fused kernel (threads per block, minimum
+// resident blocks per SM -> register cap), picked by the host's autotuner.
+const int kFluxVariants = 4;
+static const int kFluxBlock[kFluxVariants] = {128, 128, 64, 256};
+
+int flux_variants() { return kFluxVariants; }
+int flux_block(int v) { return kFluxBlock[v]; }
+
 void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const float4 *q, const float4 *dq,
-                 const float4 *qm, const double *delta, const double4_32a *prim, const double4_32a *prim_old,
-                 double4_32a *prim_next, float4 *q_next, double *cspeed_next, int rk, const Reduce &R)
+                 const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
+                 double4_32a *prim_next, float4 *q_next, float *cspeed_next, int rk, const Reduce &R, int variant)
 {
-    k_flux_update<128><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, k, q, dq, qm, delta, prim, prim_old, prim_next,
-                                                                  q_next, cspeed_next, rk, R.partial_sum,
-                                                                  R.partial_max);
+#define QLSKUM_FLUX(B, MB)                                                                                  \
+    k_flux_update<B, MB><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim, prim_old,      \
+                                                                prim_next, q_next, cspeed_next, rk,        \
+                                                                R.partial_sum, R.partial_max)
+    switch (variant) {
+    case 1: QLSKUM_FLUX(128, 5); break;
+    case 2: QLSKUM_FLUX(64, 8); break;
+    case 3: QLSKUM_FLUX(256, 2); break;
+    default: QLSKUM_FLUX(128, 4); break;
+    }
+#undef QLSKUM_FLUX
     QLSKUM_LAUNCHED(L);
 }
 

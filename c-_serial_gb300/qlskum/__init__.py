@@ -92,6 +92,7 @@ def load(build_if_needed: bool = True):
         "qlskum_synchronize": (i, [H]),
         "qlskum_stream": (C.c_void_p, [H]),
         "qlskum_launch_count": (C.c_longlong, [H]),
+        "qlskum_get_launch_config": (i, [H, ip, ip, ip]),
         "qlskum_set_kernel_timing": (i, [H, i]),
         "qlskum_get_kernel_timing": (i, [H, i, dp, C.POINTER(C.c_longlong)]),
     }
@@ -228,6 +229,11 @@ class Solver:
     @property
     def launches(self) -> int:
         return int(self._L.qlskum_launch_count(self._h))
+
+    def launch_config(self) -> dict:
+        v = [C.c_int() for _ in range(3)]
+        self._ck(self._L.qlskum_get_launch_config(self._h, *[C.byref(t) for t in v]))
+        return {"flux_block": v[0].value, "flux_min_blocks": v[1].value, "point_block": v[2].value}
 
     KERNELS = ("gradient", "inner", "flux_update", "reduce")
 

@@ -158,6 +158,13 @@ void *qlskum_stream(qlskum_handle *h);
 /* Kernel launches issued by this handle so far (the benchmark's launch count). */
 long long qlskum_launch_count(const qlskum_handle *h);
 
+/* Launch shape in use: threads per block and minimum resident blocks per SM
+ * (register cap) of the fused flux + update kernel, and threads per block of
+ * the gradient / inner-loop kernels.  With params.block_size == 0 the mixed
+ * form picks them on its first fused iteration by timing the candidates on
+ * the handle's own cloud (the autotuner). */
+qlskum_status qlskum_get_launch_config(qlskum_handle *h, int *flux_block, int *flux_min_blocks, int *point_block);
+
 /* Per-kernel device time from CUDA events recorded on the handle's stream.
  * While enabled, qlskum_q_lskum launches each iteration's kernels one by one
  * (no CUDA graph) so that every launch is bracketed by events.

@@ -43,8 +43,8 @@ def small_cloud(n_wall=40, n_layers=12, seed=7, **kw):
     from qlskum import cloudgen
     key = (n_wall, n_layers, seed, tuple(sorted(kw.items())))
     if key not in _clouds:
-        _clouds[key] = cloudgen.make_cloud(n_wall=n_wall, n_layers=n_layers, first_spacing=kw.pop("first_spacing", 2e-3),
-                                           radius=kw.pop("radius", 20.0), seed=seed, **kw)
+        _clouds[key] = cloudgen.make_cloud(n_wall=n_wall, n_layers=n_layers, first_spacing=kw.pop("first_spacing", 1e-2),
+                                           radius=kw.pop("radius", 5.0), seed=seed, **kw)
     return _clouds[key]
 
 
