@@ -478,6 +478,9 @@ void enqueue_iteration(qlskum_handle *h, int o, int it_arg)
     const Launch &L = h->L;
     for (int rk = 1; rk <= 4; rk++) {
         const int qa = (rk - 1) & 1, qb = rk & 1;
+        // only the last stage's residual is reported (fpi_solver_mod.h:138)
+        Reduce Rk = h->R;
+        if (rk != 4) Rk.partial_sum = Rk.partial_max = nullptr;
         double *dl = rk == 1 ? h->s64.delta : nullptr;
         double *cs = rk == 4 ? h->s64.cspeed : nullptr;
         const double4_32a *pin = h->s64.prim[src[rk - 1]], *pold = h->s64.prim[o];
@@ -493,7 +496,7 @@ void enqueue_iteration(qlskum_handle *h, int o, int it_arg)
                 timed(h, QLSKUM_KERNEL_INNER, [&] { mixed::q_inner(L, c, S.q[qa], S.dq[j & 1], S.dq[(j + 1) & 1]); });
             timed(h, QLSKUM_KERNEL_FLUX_UPDATE, [&] {
                 mixed::flux_update(L, c, h->K, S.q[qa], S.dq[ni & 1], S.qm, S.delta, pin, pold, pout, S.q[qb], cs32,
-                                   rk, h->R, h->flux_variant);
+                                   rk, Rk, h->flux_variant);
             });
         } else {
             State64 &S = h->s64;
@@ -504,7 +507,7 @@ void enqueue_iteration(qlskum_handle *h, int o, int it_arg)
                 timed(h, QLSKUM_KERNEL_INNER, [&] { fp64::q_inner(L, c, S.q[qa], S.dq[j & 1], S.dq[(j + 1) & 1]); });
             timed(h, QLSKUM_KERNEL_FLUX_UPDATE, [&] {
                 fp64::flux_update(L, c, h->K, S.q[qa], S.dq[ni & 1], S.qm, S.delta, pin, pold, pout, S.q[qb], cs, rk,
-                                  h->R);
+                                  Rk);
             });
         }
     }
@@ -650,6 +653,9 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
     std::vector<double4_32a> ggeo(h->np, make_double4_32a(0, 0, 0, 0));
     std::vector<double4_32a> fgeo((size_t)h->np * 4, make_double4_32a(0, 0, 0, 0));
     std::vector<double2> fcoef((size_t)h->np * 4, make_double2(0, 0));
+    std::vector<double4_32a> gcoef(h->np, make_double4_32a(0, 0, 0, 0));
+    std::vector<float2> e_xy32(ne, make_float2(0, 0));
+    const bool unit_w = p->power == 0.0;
     std::vector<float> e_dist32(ne, 1.0f);
     const Precomp &P = h->pc;
     for (int pp = 0; pp < n; pp++) {
@@ -661,6 +667,10 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
         eps2_32[pp] = (float)P.eps2[i];
         ggeo[pp] = make_double4_32a(P.ggeo[4 * (size_t)i], P.ggeo[4 * (size_t)i + 1], P.ggeo[4 * (size_t)i + 2],
                                 P.ggeo[4 * (size_t)i + 3]);
+        // q_variables_mod.h:112-116 as coefficients: dq_x = Sx syy/det - Sy sxy/det, dq_y = Sy sxx/det - Sx sxy/det
+        gcoef[pp] = make_double4_32a(P.ggeo[4 * (size_t)i + 1] * P.ggeo[4 * (size_t)i + 3],
+                                     P.ggeo[4 * (size_t)i + 2] * P.ggeo[4 * (size_t)i + 3],
+                                     P.ggeo[4 * (size_t)i + 0] * P.ggeo[4 * (size_t)i + 3], 0.0);
         static const bool used[3][4] = {{true, true, false, true}, {true, true, true, true}, {true, true, true, false}};
         const int fl = c->flag_1[i];
         const double scale = fl == kWall ? 2.0 : 1.0;  // flux_residual_mod.h:29
@@ -683,6 +693,7 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
             e_sn[e] = make_double2(P.sn[2 * src], P.sn[2 * src + 1]);
             e_dist[e] = P.dist[src];
             e_dist32[e] = (float)P.dist[src];
+            e_xy32[e] = make_float2((float)P.geo[4 * src], (float)P.geo[4 * src + 1]);
             e_dir[e] = P.edge_dir[src];
             e_geo32[e] = make_float4((float)P.geo[4 * src], (float)P.geo[4 * src + 1], (float)P.geo[4 * src + 2],
                                      (float)P.geo[4 * src + 3]);
@@ -720,21 +731,29 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
     float2 *d_esn32 = nullptr;
     float *d_eps32 = nullptr, *d_edist32 = nullptr;
     double2 *d_fcoef = nullptr;
+    double4_32a *d_gcoef = nullptr;
+    float2 *d_exy32 = nullptr;
     if (p->precision == QLSKUM_MIXED) {
-        d_egeo32 = A.alloc<float4>(ne);
-        d_esn32 = A.alloc<float2>(ne);
+        if (unit_w) {
+            d_exy32 = A.alloc<float2>(ne);
+        } else {
+            d_egeo32 = A.alloc<float4>(ne);
+            d_esn32 = A.alloc<float2>(ne);
+        }
         d_eps32 = A.alloc<float>(h->np);
         d_edist32 = A.alloc<float>(ne);
         d_fcoef = A.alloc<double2>((size_t)h->np * 4);
+        d_gcoef = A.alloc<double4_32a>(h->np);
     }
     up(d_flag, flag); up(d_nb, nbh); up(d_sb, sbase); up(d_enbr, e_nbr); up(d_egeo, e_geo); up(d_esn, e_sn);
     up(d_edist, e_dist); up(d_edir, e_dir); up(d_nrm, nrm); up(d_eps2, eps2); up(d_ggeo, ggeo); up(d_fgeo, fgeo);
     up(d_egeo32, e_geo32); up(d_esn32, e_sn32); up(d_eps32, eps2_32); up(d_edist32, e_dist32); up(d_fcoef, fcoef);
+    up(d_gcoef, gcoef); up(d_exy32, e_xy32);
     DevCloud &dc = h->dc;
     dc.n = n; dc.np = h->np; dc.flag = d_flag; dc.nbhs = d_nb; dc.slice_base = d_sb; dc.e_nbr = d_enbr;
     dc.e_geo = d_egeo; dc.e_sn = d_esn; dc.e_dist = d_edist; dc.e_dir = d_edir; dc.nrm = d_nrm; dc.eps2 = d_eps2;
     dc.ggeo = d_ggeo; dc.fgeo = d_fgeo; dc.e_geo32 = d_egeo32; dc.e_sn32 = d_esn32; dc.eps2_32 = d_eps32;
-    dc.e_dist32 = d_edist32; dc.fcoef = d_fcoef;
+    dc.e_dist32 = d_edist32; dc.fcoef = d_fcoef; dc.gcoef = d_gcoef; dc.unit_w = unit_w ? 1 : 0; dc.e_xy32 = d_exy32;
 
     for (int b = 0; b < 3; b++) h->s64.prim[b] = A.alloc<double4_32a>(h->np);
     for (int b = 0; b < 2; b++) {
@@ -942,6 +961,20 @@ qlskum_status qlskum_q_lskum(qlskum_handle *h, int iters)
     // the device counter continues from the host's
     CK(h, cudaMemcpyAsync(h->R.iter, &h->it, sizeof(int), cudaMemcpyHostToDevice, h->L.stream));
     CK(h, cudaStreamSynchronize(h->L.stream));
+    // one graph per buffer-rotation phase, all three captured up front
+    for (int o = 0; o < 3 && !h->timing && iters > 0; o++) {
+        if (h->graph[o]) continue;
+        cudaGraph_t g = nullptr;
+        CK(h, cudaStreamBeginCapture(h->L.stream, cudaStreamCaptureModeThreadLocal));
+        long long before = h->launches;
+        enqueue_iteration(h, o, 0);
+        h->launches = before;  // counted when replayed
+        cudaError_t e = cudaStreamEndCapture(h->L.stream, &g);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&h->graph[o], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+    }
     for (int t = 0; t < iters; t++) {
         const int o = h->pcur;
         if (h->timing) {
@@ -951,18 +984,6 @@ qlskum_status qlskum_q_lskum(qlskum_handle *h, int iters)
             after_iteration(h, o);
             h->it += 1;
             continue;
-        }
-        if (!h->graph[o]) {
-            cudaGraph_t g = nullptr;
-            CK(h, cudaStreamBeginCapture(h->L.stream, cudaStreamCaptureModeThreadLocal));
-            long long before = h->launches;
-            enqueue_iteration(h, o, 0);
-            h->launches = before;  // counted when replayed
-            cudaError_t e = cudaStreamEndCapture(h->L.stream, &g);
-            if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
-            e = cudaGraphInstantiate(&h->graph[o], g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
         }
         CK(h, cudaGraphLaunch(h->graph[o], h->L.stream));
         h->launches += 4 * (2 + h->prm.inner_iterations) + 1;

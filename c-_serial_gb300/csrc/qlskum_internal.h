@@ -52,6 +52,13 @@ struct DevCloud {
     // inverse, the wall's factor 2 and zero for directions a class does not
     // use.  FP64, [np][4].
     const double2 *fcoef = nullptr;
+    // Mixed form, gradient and inner loop: the 2x2 solve as coefficients
+    // {syy/det, sxy/det, sxx/det} (FP64), dq_x = Sx a - Sy b, dq_y = Sy c - Sx b.
+    const double4_32a *gcoef = nullptr;
+    // power == 0 (all weights 1): the mixed kernels read only {delx, dely}
+    // per edge (FP32) and rotate it by the point normal themselves.
+    int unit_w = 0;
+    const float2 *e_xy32 = nullptr;
 };
 
 // Free-stream constants of one case (parameter_mod.h:4-30).

@@ -19,22 +19,52 @@ namespace mixed {
 
 static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
 
+// float -> double on the integer pipe.  The hardware conversion issues on the
+// FP64 pipe, which on this chip is the scarce one; this is exact for normal
+// numbers and zero, flushes subnormals to zero and keeps Inf / NaN.
+__device__ __forceinline__ double f2d(float x)
+{
+    const unsigned b = __float_as_uint(x);
+    const unsigned mag = b & 0x7fffffffu;
+    const unsigned sign = b & 0x80000000u;
+    unsigned hi = sign | (((mag >> 23) + 896u) << 20) | ((mag & 0x7fffffu) >> 3);
+    unsigned lo = b << 29;
+    if (mag < 0x00800000u) { hi = sign; lo = 0u; }
+    if (mag >= 0x7f800000u) hi = sign | 0x7ff00000u | ((mag & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// double -> float on the integer pipe, truncating the mantissa (< 1 ulp);
+// underflow goes to zero, overflow and Inf to Inf, NaN stays NaN.
+__device__ __forceinline__ float d2f(double x)
+{
+    const unsigned h = (unsigned)__double2hiint(x), l = (unsigned)__double2loint(x);
+    const unsigned mag = h & 0x7fffffffu;
+    const unsigned sign = h & 0x80000000u;
+    const int e = (int)(mag >> 20) - 896;
+    const unsigned m = ((mag & 0xfffffu) << 3) | (l >> 29);
+    unsigned b = sign | ((unsigned)e << 23) | m;
+    if (e <= 0) b = sign;
+    if (e >= 255) b = sign | 0x7f800000u | ((mag >= 0x7ff00000u && (m | (mag & 0xfffffu) | l)) ? 0x400000u : 0u);
+    return __uint_as_float(b);
+}
+
 __device__ __forceinline__ void q_of(const double P[4], float Q[4])
 {
-    prim_to_q<float>((float)P[0], (float)P[1], (float)P[2], (float)P[3], Q);
+    prim_to_q<float>(d2f(P[0]), d2f(P[1]), d2f(P[2]), d2f(P[3]), Q);
 }
 
 // |u| + 3 sqrt(p / rho) in FP32 (state_update_mod.h:483-485)
 __device__ __forceinline__ float wave_speed32(const double P[4])
 {
-    const float rho = (float)P[0], u1 = (float)P[1], u2 = (float)P[2], p = (float)P[3];
+    const float rho = d2f(P[0]), u1 = d2f(P[1]), u2 = d2f(P[2]), p = d2f(P[3]);
     return sqrtf(u1 * u1 + u2 * u2) + 3.0f * sqrtf(__fdividef(p, rho));
 }
 
 // 1 / x in FP64 without a division: FP32 seed, two Newton steps.
 __device__ __forceinline__ double recip64(double x)
 {
-    double r = (double)__frcp_rn((float)x);
+    double r = f2d(__frcp_rn(d2f(x)));
     double e = fma(-x, r, 1.0);
     r = fma(r, e, r);
     e = fma(-x, r, 1.0);
@@ -97,8 +127,32 @@ __global__ void k_derived(int n, const double4_32a *__restrict__ prim, float4 *_
     cs[i] = wave_speed32(P);
 }
 
+// Edge vector and least-squares weights of edge e: {delx, dely, w delx, w dely}.
+template <bool UW>
+__device__ __forceinline__ float4 edge_w(const DevCloud &c, long long e)
+{
+    if (UW) {
+        const float2 d = c.e_xy32[e];
+        return make_float4(d.x, d.y, d.x, d.y);
+    }
+    return c.e_geo32[e];
+}
+
+// dq = the 2x2 solve of the sums (Sx, Sy), FP64 (dq_x = Sx a - Sy b, dq_y = Sy c - Sx b).
+__device__ __forceinline__ void solve_grad(const double4_32a &m, const float sdx[4], const float sdy[4], float dx[4],
+                                           float dy[4])
+{
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const double X = f2d(sdx[r]), Y = f2d(sdy[r]);
+        dx[r] = d2f(fma(X, m.x, -Y * m.y));
+        dy[r] = d2f(fma(Y, m.z, -X * m.y));
+    }
+}
+
 // q_variables_mod.h:36-118: FP32 differences and sums, FP64 solve; in the
 // first stage also the local time step (state_update_mod.h:448-496) in FP32.
+template <bool UW>
 __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4 *__restrict__ dq,
                                 float4 *__restrict__ qm, const float *__restrict__ cs, float *__restrict__ delta,
                                 float cfl)
@@ -115,7 +169,7 @@ __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
-        const float4 g = c.e_geo32[e];
+        const float4 g = edge_w<UW>(c, e);
         float qk[4];
         ld4(q[k], qk);
 #pragma unroll
@@ -127,13 +181,8 @@ __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4
         }
         if (delta) min_dt = fminf(min_dt, cfl * __fdividef(c.e_dist32[e], cs[k]));
     }
-    const double4_32a m = c.ggeo[i];
     float dx[4], dy[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        dx[r] = (float)(((double)sdx[r] * m.y - (double)sdy[r] * m.z) * m.w);
-        dy[r] = (float)(((double)sdy[r] * m.x - (double)sdx[r] * m.z) * m.w);
-    }
+    solve_grad(c.gcoef[i], sdx, sdy, dx, dy);
     dq[2 * i] = mk4(dx);
     dq[2 * i + 1] = mk4(dy);
     qm[2 * i] = mk4(qmax);
@@ -142,6 +191,7 @@ __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4
 }
 
 // q_variables_mod.h:120-213
+template <bool UW>
 __global__ void k_q_inner(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ dq_in,
                           float4 *__restrict__ dq_out)
 {
@@ -156,7 +206,7 @@ __global__ void k_q_inner(DevCloud c, const float4 *__restrict__ q, const float4
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
-        const float4 g = c.e_geo32[e];
+        const float4 g = edge_w<UW>(c, e);
         float qk[4], dxk[4], dyk[4];
         ld4(q[k], qk);
         ld4(dq_in[2 * k], dxk);
@@ -169,19 +219,14 @@ __global__ void k_q_inner(DevCloud c, const float4 *__restrict__ q, const float4
             sdy[r] += g.w * (t2 - t1);
         }
     }
-    const double4_32a m = c.ggeo[i];
     float dx[4], dy[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        dx[r] = (float)(m.w * ((double)sdx[r] * m.y - (double)sdy[r] * m.z));
-        dy[r] = (float)(m.w * ((double)sdy[r] * m.x - (double)sdx[r] * m.z));
-    }
+    solve_grad(c.gcoef[i], sdx, sdy, dx, dy);
     dq_out[2 * i] = mk4(dx);
     dq_out[2 * i + 1] = mk4(dy);
 }
 
 // Fused stage: FP32 edge work, FP64 solve / residual / update.
-template <int BLOCK, int MINB>
+template <int BLOCK, int MINB, bool UW>
 __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseConst K, const float4 *__restrict__ q,
                                                        const float4 *__restrict__ dq, const float4 *__restrict__ qm,
                                                        const float *__restrict__ delta,
@@ -196,7 +241,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseCon
     if (i < c.n) {
         const int f = c.flag[i];
         const double2 nn = c.nrm[i];
-        const float nx = (float)nn.x, ny = (float)nn.y;
+        const float nx = d2f(nn.x), ny = d2f(nn.y);
         float qi[4], dxi[4], dyi[4], mxi[4], mni[4];
         ld4(q[i], qi);
         ld4(dq[2 * i], dxi);
@@ -214,8 +259,17 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseCon
         for (int j = 0; j < nb; j++) {
             const long long e = base + 32LL * j;
             const int k = c.e_nbr[e];
-            const float4 g = c.e_geo32[e];
-            const float2 sw = c.e_sn32[e];
+            float4 g;
+            float2 sw;
+            if (UW) {
+                // dels, deln of the point's (t, n) frame (interior_fluxes_mod.h:53-54), weight 1
+                const float2 d = c.e_xy32[e];
+                g = make_float4(d.x, d.y, 0.f, 0.f);
+                sw = make_float2(d.x * ny - d.y * nx, d.x * nx + d.y * ny);
+            } else {
+                g = c.e_geo32[e];
+                sw = c.e_sn32[e];
+            }
             const unsigned dir = c.e_dir[e];
             float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
             ld4(q[k], qk);
@@ -249,15 +303,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseCon
         double2 cf[4];
 #pragma unroll
         for (int d = 0; d < 4; d++) cf[d] = c.fcoef[4 * i + d];
-        const double dl = (double)delta[i];
+        const double dl = f2d(delta[i]);
         double F[4], P[4];
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             double acc = 0.0;
 #pragma unroll
             for (int d = 0; d < 4; d++) {
-                acc = fma(cf[d].x, (double)sx[d][r], acc);
-                acc = fma(cf[d].y, (double)sy[d][r], acc);
+                acc = fma(cf[d].x, f2d(sx[d][r]), acc);
+                acc = fma(cf[d].y, f2d(sy[d][r]), acc);
             }
             F[r] = dl * acc;
         }
@@ -284,13 +338,19 @@ void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, float4
 void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *dq, float4 *qm, const float *cspeed,
                    float *delta, float cfl)
 {
-    k_q_derivatives<<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
+    if (c.unit_w)
+        k_q_derivatives<true><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
+    else
+        k_q_derivatives<false><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
     QLSKUM_LAUNCHED(L);
 }
 
 void q_inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, float4 *dq_out)
 {
-    k_q_inner<<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq_in, dq_out);
+    if (c.unit_w)
+        k_q_inner<true><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq_in, dq_out);
+    else
+        k_q_inner<false><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq_in, dq_out);
     QLSKUM_LAUNCHED(L);
 }
 
@@ -307,9 +367,16 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
                  double4_32a *prim_next, float4 *q_next, float *cspeed_next, int rk, const Reduce &R, int variant)
 {
 #define QLSKUM_FLUX(B, MB)                                                                                  \
-    k_flux_update<B, MB><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim, prim_old,      \
-                                                                prim_next, q_next, cspeed_next, rk,        \
-                                                                R.partial_sum, R.partial_max)
+    if (c.unit_w)                                                                                           \
+        k_flux_update<B, MB, true><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,      \
+                                                                      prim_old, prim_next, q_next,         \
+                                                                      cspeed_next, rk, R.partial_sum,      \
+                                                                      R.partial_max);                      \
+    else                                                                                                    \
+        k_flux_update<B, MB, false><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,     \
+                                                                       prim_old, prim_next, q_next,        \
+                                                                       cspeed_next, rk, R.partial_sum,     \
+                                                                       R.partial_max)
     switch (variant) {
     case 1: QLSKUM_FLUX(128, 5); break;
     case 2: QLSKUM_FLUX(64, 8); break;
