@@ -129,7 +129,7 @@ def make_cloud(workload):
     return cloudgen.make_cloud(**WORKLOADS[workload]["cloud"])
 
 
-def flux_update_bytes(cloud, precision: str) -> float:
+def flux_update_bytes(cloud, precision: str, unit_weights: bool = True) -> float:
     """Compulsory bytes one fused flux + update launch moves (each array once).
 
     Per point: own q / dq / qm, normal, limiter eps^2, delta, flag, nbhs, the
@@ -143,7 +143,8 @@ def flux_update_bytes(cloud, precision: str) -> float:
     e = int(cloud.nbhs.sum())
     if precision == "mixed":
         per_pt = 16 + 32 + 32 + 16 + 4 + 4 + 1 + 4 + 64 + 32 + 32 + 16 + 32 / 4 + 4 / 4 + 8 / 32
-        per_edge = 4 + 16 + 8 + 1
+        # power 0: {delx, dely} FP32 per edge, rotated in the kernel; else + {w delx, w dely, dels w, deln w}
+        per_edge = 4 + 8 + 1 if unit_weights else 4 + 16 + 8 + 1
     else:
         per_pt = 32 + 64 + 64 + 16 + 8 + 8 + 1 + 4 + 128 + 32 + 32 + 32 + 32 / 4 + 8 / 4 + 8 / 32
         per_edge = 4 + 32 + 16 + 1
@@ -203,6 +204,72 @@ def cpu_baseline(workload, cloud, threads, iters):
     return cloud.n * iters / dt, dt
 
 
+def batch_workload(seed=3, n_clouds=32, n_cases=64):
+    """Seeded NACA 4-digit clouds (thickness 8-16%, camber 0-4%, camber
+    position 0.3-0.5) of 20k-500k points, and flight conditions M 0.5-0.85,
+    AoA -2..4 deg; case j solves cloud j mod n_clouds."""
+    from qlskum import cloudgen
+    rng = np.random.default_rng(seed)
+    clouds = []
+    for k in range(n_clouds):
+        size = int(rng.uniform(20_000, 500_000))
+        n_wall = max(64, int(round(np.sqrt(size) / 8)) * 8)
+        n_layers = max(12, size // n_wall)
+        t = rng.uniform(0.08, 0.16)
+        m = rng.uniform(0.0, 0.04)
+        pc = rng.uniform(0.3, 0.5)
+        clouds.append(cloudgen.make_cloud(n_wall=n_wall, n_layers=n_layers, first_spacing=2e-3, radius=20.0,
+                                          seed=100 + k, m=m, p=pc, t=t))
+    cases = [(j % n_clouds, rng.uniform(0.5, 0.85), rng.uniform(-2.0, 4.0)) for j in range(n_cases)]
+    return clouds, cases
+
+
+def run_batch(args):
+    """Batched launch: 64 flight conditions over 32 uneven clouds, mixed precision."""
+    import torch
+    import qlskum
+    qlskum.load()
+    t0 = time.perf_counter()
+    clouds, cases = batch_workload()
+    log(f"batch: {len(clouds)} clouds, {sum(c.n for c in clouds)} cloud points, generated in "
+        f"{time.perf_counter() - t0:.1f}s")
+    kw = dict(cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=3)
+    b = qlskum.Batch(clouds, cases, **kw)
+    b.run(args.warmup)
+    stream = torch.cuda.ExternalStream(b.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    l0 = b.launches
+    with ClockSampler(0) as clocks:
+        e0.record(stream)
+        b.run(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    dt = e0.elapsed_time(e1) / 1e3
+    value = b.total_points * args.steps / dt
+    cl, cd, _, _ = b.objective()
+    # per-case Cl / Cd against the FP64 form of the same case and iterations (first 4 cases)
+    errs = []
+    for k in range(min(4, len(cases))):
+        ci, mach, aoa = cases[k]
+        s = qlskum.Solver(clouds[ci], mach=mach, aoa=aoa, precision=qlskum.FP64, **kw)
+        s.q_lskum(args.warmup + args.steps)
+        c64 = s.objective()
+        errs.append({"case": k, "points": clouds[ci].n, "mach": mach, "aoa": aoa, "cl": cl[k],
+                     "abs_dcl": abs(cl[k] - c64[0]), "abs_dcd": abs(cd[k] - c64[1])})
+        del s
+    line = {"metric": "point-iter/s", "value": value, "unit": "point-iter/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "batch_64_conditions_32_clouds", "cases": len(cases),
+                       "points": b.total_points, "cloud_sizes": [c.n for c in clouds], **kw,
+                       "precision": "mixed"},
+            "clocks": clocks.summary(), "gpu_launches": b.launches - l0, "tuning": b.tuning(),
+            "cl_vs_fp64": errs}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -251,7 +318,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="transonic", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="transonic", choices=sorted(WORKLOADS) + ["batch"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=3)
     args = ap.parse_args()
@@ -259,6 +326,10 @@ def main():
 
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "batch":
+        if rank == 0:
+            run_batch(args)
         return
 
     import torch
@@ -300,7 +371,7 @@ def main():
     fl_ms, fl_n = kt["flux_update"]
     total_ms = sum(v[0] for v in kt.values())
     peak, peak_kind = measured_peaks()
-    nbytes = flux_update_bytes(cloud, args.precision)
+    nbytes = flux_update_bytes(cloud, args.precision, kw["power"] == 0.0)
     achieved = nbytes / (fl_ms / fl_n / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": None, "kernel": f"k_flux_update ({args.precision})",

@@ -37,6 +37,12 @@ struct Precomp {
     std::vector<double> ggeo;      // [n][4]
     std::vector<double> fgeo;      // [n][4][4]
     std::vector<double> eps2;      // [n]
+    // drop what only the device upload needs (keeps normals and sub-stencils)
+    void release_upload_data()
+    {
+        for (auto *v : {&geo, &sn, &dist, &ggeo, &fgeo, &eps2}) std::vector<double>().swap(*v);
+        std::vector<uint8_t>().swap(edge_dir);
+    }
 };
 
 std::string fmt(const char *f, ...)
@@ -558,6 +564,204 @@ qlskum_status check_status(qlskum_handle *h)
 
 }  // namespace
 
+struct Geometry {
+    int n = 0, np = 0, nslices = 0, shape_points = 0;
+    std::vector<int> perm, iperm;
+    Precomp pc;
+    DevCloud dc;
+    int *d_wall_perm = nullptr;
+    double4_32a *d_wall_geo = nullptr;
+};
+
+namespace {
+
+// The device geometry of one cloud: point order (class, then Morton code),
+// sliced-ELL edge arrays and every per-point / per-edge quantity the kernels
+// read, uploaded on `stream` into `A`.  G.pc must already hold precompute()'s
+// result (done first, on the host only, so malformed clouds are reported
+// before any device work).  need_fp64 / need_mixed select the arrays of the
+// FP64 and the mixed kernels.  Synchronises the stream.
+qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int sp, bool need_fp64, bool need_mixed,
+                             DeviceArena &A, cudaStream_t stream, Geometry &G)
+{
+    G.n = c->n;
+    G.shape_points = sp;
+    const int n = c->n, NB = QLSKUM_MAX_NBHS;
+    // ---- point order: class (wall, outer, interior), then Morton code
+    G.iperm.resize(n);
+    std::iota(G.iperm.begin(), G.iperm.end(), 0);
+    if (p->reorder) {
+        double x0 = c->x[0], x1 = c->x[0], y0 = c->y[0], y1 = c->y[0];
+        for (int i = 0; i < n; i++) {
+            x0 = std::min(x0, c->x[i]); x1 = std::max(x1, c->x[i]);
+            y0 = std::min(y0, c->y[i]); y1 = std::max(y1, c->y[i]);
+        }
+        const double span = std::max(x1 - x0, y1 - y0) + 1e-300;
+        std::vector<uint64_t> key(n);
+        for (int i = 0; i < n; i++) {
+            uint32_t qx = (uint32_t)std::min(2097151.0, std::floor((c->x[i] - x0) / span * 2097151.0));
+            uint32_t qy = (uint32_t)std::min(2097151.0, std::floor((c->y[i] - y0) / span * 2097151.0));
+            static const int rank[3] = {0, 2, 1};
+            key[i] = ((uint64_t)rank[c->flag_1[i]] << 62) | morton2(qx, qy);
+        }
+        std::stable_sort(G.iperm.begin(), G.iperm.end(), [&](int a, int b) { return key[a] < key[b]; });
+    }
+    G.perm.resize(n);
+    for (int p2 = 0; p2 < n; p2++) G.perm[G.iperm[p2]] = p2;
+
+    // ---- sliced ELL
+    G.np = (n + 31) / 32 * 32;
+    G.nslices = G.np / 32;
+    std::vector<long long> sbase(G.nslices);
+    long long tot = 0;
+    for (int s = 0; s < G.nslices; s++) {
+        int w = 0;
+        for (int l = 0; l < 32; l++) {
+            int pp = s * 32 + l;
+            if (pp < n) w = std::max(w, c->nbhs[G.iperm[pp]]);
+        }
+        sbase[s] = tot;
+        tot += 32LL * w;
+    }
+    const size_t ne = (size_t)std::max(tot, 32LL);
+    std::vector<int> e_nbr(ne, 0);
+    std::vector<double4_32a> e_geo(ne, make_double4_32a(0, 0, 0, 0));
+    std::vector<double2> e_sn(ne, make_double2(0, 0));
+    std::vector<double> e_dist(ne, 1.0);
+    std::vector<uint8_t> e_dir(ne, 0);
+    std::vector<float4> e_geo32(ne, make_float4(0, 0, 0, 0));
+    std::vector<float2> e_sn32(ne, make_float2(0, 0));
+    std::vector<int8_t> flag(G.np, 1);
+    std::vector<int> nbh(G.np, 0);
+    std::vector<double2> nrm(G.np, make_double2(0, 1));
+    std::vector<double> eps2(G.np, 0.0);
+    std::vector<float> eps2_32(G.np, 0.0f);
+    std::vector<double4_32a> ggeo(G.np, make_double4_32a(0, 0, 0, 0));
+    std::vector<double4_32a> fgeo((size_t)G.np * 4, make_double4_32a(0, 0, 0, 0));
+    std::vector<double2> fcoef((size_t)G.np * 4, make_double2(0, 0));
+    std::vector<double4_32a> gcoef(G.np, make_double4_32a(0, 0, 0, 0));
+    std::vector<float2> e_xy32(ne, make_float2(0, 0));
+    const bool unit_w = p->power == 0.0;
+    std::vector<float> e_dist32(ne, 1.0f);
+    const Precomp &P = G.pc;
+    for (int pp = 0; pp < n; pp++) {
+        const int i = G.iperm[pp];
+        flag[pp] = (int8_t)c->flag_1[i];
+        nbh[pp] = c->nbhs[i];
+        nrm[pp] = make_double2(P.nx[i], P.ny[i]);
+        eps2[pp] = P.eps2[i];
+        eps2_32[pp] = (float)P.eps2[i];
+        ggeo[pp] = make_double4_32a(P.ggeo[4 * (size_t)i], P.ggeo[4 * (size_t)i + 1], P.ggeo[4 * (size_t)i + 2],
+                                P.ggeo[4 * (size_t)i + 3]);
+        // q_variables_mod.h:112-116 as coefficients: dq_x = Sx syy/det - Sy sxy/det, dq_y = Sy sxx/det - Sx sxy/det
+        gcoef[pp] = make_double4_32a(P.ggeo[4 * (size_t)i + 1] * P.ggeo[4 * (size_t)i + 3],
+                                     P.ggeo[4 * (size_t)i + 2] * P.ggeo[4 * (size_t)i + 3],
+                                     P.ggeo[4 * (size_t)i + 0] * P.ggeo[4 * (size_t)i + 3], 0.0);
+        static const bool used[3][4] = {{true, true, false, true}, {true, true, true, true}, {true, true, true, false}};
+        const int fl = c->flag_1[i];
+        const double scale = fl == kWall ? 2.0 : 1.0;  // flux_residual_mod.h:29
+        for (int d = 0; d < 4; d++) {
+            const double *F = &P.fgeo[((size_t)i * 4 + d) * 4];
+            fgeo[(size_t)pp * 4 + d] = make_double4_32a(F[0], F[1], F[2], F[3]);
+            // x rows (d < 2): G = (Sx syy - Sy sxy) / det;  y rows: G = (Sy sxx - Sx sxy) / det
+            double a = 0.0, b = 0.0;
+            if (used[fl][d]) {
+                if (d < 2) { a = scale * F[1] * F[3]; b = -scale * F[2] * F[3]; }
+                else { a = -scale * F[2] * F[3]; b = scale * F[0] * F[3]; }
+            }
+            fcoef[(size_t)pp * 4 + d] = make_double2(a, b);
+        }
+        for (int r = 0; r < c->nbhs[i]; r++) {
+            const size_t e = (size_t)(sbase[pp >> 5] + 32LL * r + (pp & 31));
+            const size_t src = (size_t)i * NB + r;
+            e_nbr[e] = G.perm[c->conn[src] - 1];
+            e_geo[e] = make_double4_32a(P.geo[4 * src], P.geo[4 * src + 1], P.geo[4 * src + 2], P.geo[4 * src + 3]);
+            e_sn[e] = make_double2(P.sn[2 * src], P.sn[2 * src + 1]);
+            e_dist[e] = P.dist[src];
+            e_dist32[e] = (float)P.dist[src];
+            e_xy32[e] = make_float2((float)P.geo[4 * src], (float)P.geo[4 * src + 1]);
+            e_dir[e] = P.edge_dir[src];
+            e_geo32[e] = make_float4((float)P.geo[4 * src], (float)P.geo[4 * src + 1], (float)P.geo[4 * src + 2],
+                                     (float)P.geo[4 * src + 3]);
+            e_sn32[e] = make_float2((float)P.sn[2 * src], (float)P.sn[2 * src + 1]);
+        }
+    }
+
+    // ---- device
+    // Host vectors must outlive the asynchronous uploads: keep them until the
+    // stream is synchronised at the end of this function.
+    auto up = [&](auto *dptr, const auto &vec) {
+        if (dptr && !vec.empty())
+            cudaMemcpyAsync(dptr, vec.data(), vec.size() * sizeof(vec[0]), cudaMemcpyHostToDevice, stream);
+    };
+    int8_t *d_flag = A.alloc<int8_t>(G.np);
+    int *d_nb = A.alloc<int>(G.np);
+    long long *d_sb = A.alloc<long long>(G.nslices);
+    int *d_enbr = A.alloc<int>(ne);
+    double4_32a *d_egeo = need_fp64 ? A.alloc<double4_32a>(ne) : nullptr;
+    double2 *d_esn = need_fp64 ? A.alloc<double2>(ne) : nullptr;
+    double *d_edist = need_fp64 ? A.alloc<double>(ne) : nullptr;
+    uint8_t *d_edir = A.alloc<uint8_t>(ne);
+    double2 *d_nrm = A.alloc<double2>(G.np);
+    double *d_eps2 = A.alloc<double>(G.np);
+    double4_32a *d_ggeo = need_fp64 ? A.alloc<double4_32a>(G.np) : nullptr;
+    double4_32a *d_fgeo = need_fp64 ? A.alloc<double4_32a>((size_t)G.np * 4) : nullptr;
+    float4 *d_egeo32 = nullptr;
+    float2 *d_esn32 = nullptr;
+    float *d_eps32 = nullptr, *d_edist32 = nullptr;
+    double2 *d_fcoef = nullptr;
+    double4_32a *d_gcoef = nullptr;
+    float2 *d_exy32 = nullptr;
+    if (need_mixed) {
+        if (unit_w) {
+            d_exy32 = A.alloc<float2>(ne);
+        } else {
+            d_egeo32 = A.alloc<float4>(ne);
+            d_esn32 = A.alloc<float2>(ne);
+        }
+        d_eps32 = A.alloc<float>(G.np);
+        d_edist32 = A.alloc<float>(ne);
+        d_fcoef = A.alloc<double2>((size_t)G.np * 4);
+        d_gcoef = A.alloc<double4_32a>(G.np);
+    }
+    up(d_flag, flag); up(d_nb, nbh); up(d_sb, sbase); up(d_enbr, e_nbr); up(d_egeo, e_geo); up(d_esn, e_sn);
+    up(d_edist, e_dist); up(d_edir, e_dir); up(d_nrm, nrm); up(d_eps2, eps2); up(d_ggeo, ggeo); up(d_fgeo, fgeo);
+    up(d_egeo32, e_geo32); up(d_esn32, e_sn32); up(d_eps32, eps2_32); up(d_edist32, e_dist32); up(d_fcoef, fcoef);
+    up(d_gcoef, gcoef); up(d_exy32, e_xy32);
+    DevCloud &dc = G.dc;
+    dc.n = n; dc.np = G.np; dc.flag = d_flag; dc.nbhs = d_nb; dc.slice_base = d_sb; dc.e_nbr = d_enbr;
+    dc.e_geo = d_egeo; dc.e_sn = d_esn; dc.e_dist = d_edist; dc.e_dir = d_edir; dc.nrm = d_nrm; dc.eps2 = d_eps2;
+    dc.ggeo = d_ggeo; dc.fgeo = d_fgeo; dc.e_geo32 = d_egeo32; dc.e_sn32 = d_esn32; dc.eps2_32 = d_eps32;
+    dc.e_dist32 = d_edist32; dc.fcoef = d_fcoef; dc.gcoef = d_gcoef; dc.unit_w = unit_w ? 1 : 0; dc.e_xy32 = d_exy32;
+
+    G.d_wall_perm = A.alloc<int>(std::max(sp, 1));
+    G.d_wall_geo = A.alloc<double4_32a>(std::max(sp, 1));
+    if (A.err != cudaSuccess) return fail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(A.err)));
+    // compute_force_coeffs_mod.h:37-59 geometry of the first shape_points points
+    std::vector<int> wperm(std::max(sp, 1), 0);
+    std::vector<double4_32a> wgeo(std::max(sp, 1), make_double4_32a(0, 0, 0, 0));
+    for (int m = 0; m < sp; m++) {
+        int r = c->right[m] - 1, l = c->left[m] - 1;
+        double lx = c->x[l], ly = c->y[l], mx = c->x[m], my = c->y[m], rx = c->x[r], ry = c->y[r];
+        double ds1 = std::pow((mx - lx), 2) + std::pow((my - ly), 2);
+        ds1 = std::sqrt(ds1);
+        double ds2 = std::pow((rx - mx), 2) + std::pow((ry - my), 2);
+        ds2 = std::sqrt(ds2);
+        double ds = 0.5 * (ds1 + ds2);
+        wperm[m] = G.perm[m];
+        wgeo[m] = make_double4_32a(ds, mx - 0.25, my, 0.0);
+    }
+    up(G.d_wall_perm, wperm);
+    up(G.d_wall_geo, wgeo);
+    cudaError_t ce = cudaStreamSynchronize(stream);
+    if (ce == cudaSuccess) ce = cudaGetLastError();
+    if (ce != cudaSuccess) return fail(nullptr, QLSKUM_ERR_CUDA, fmt("geometry upload: %s", cudaGetErrorString(ce)));
+    if (A.err != cudaSuccess) return fail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(A.err)));
+    return QLSKUM_OK;
+}
+
+}  // namespace
+
 // ======================================================================= C ABI
 
 extern "C" {
@@ -589,119 +793,14 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
     int sp = 0;
     qlskum_status st = validate(c, p, &sp);
     if (st) return st;
+    Geometry G;
+    st = precompute(c, p, G.pc);
+    if (st) return st;
     qlskum_handle *h = new qlskum_handle();
     h->prm = *p;
     h->n = c->n;
     h->shape_points = sp;
-    st = precompute(c, p, h->pc);
-    if (st) {
-        delete h;
-        return st;
-    }
     set_case(h);
-    const int n = c->n, NB = QLSKUM_MAX_NBHS;
-
-    // ---- point order: class (wall, outer, interior), then Morton code
-    h->iperm.resize(n);
-    std::iota(h->iperm.begin(), h->iperm.end(), 0);
-    if (p->reorder) {
-        double x0 = c->x[0], x1 = c->x[0], y0 = c->y[0], y1 = c->y[0];
-        for (int i = 0; i < n; i++) {
-            x0 = std::min(x0, c->x[i]); x1 = std::max(x1, c->x[i]);
-            y0 = std::min(y0, c->y[i]); y1 = std::max(y1, c->y[i]);
-        }
-        const double span = std::max(x1 - x0, y1 - y0) + 1e-300;
-        std::vector<uint64_t> key(n);
-        for (int i = 0; i < n; i++) {
-            uint32_t qx = (uint32_t)std::min(2097151.0, std::floor((c->x[i] - x0) / span * 2097151.0));
-            uint32_t qy = (uint32_t)std::min(2097151.0, std::floor((c->y[i] - y0) / span * 2097151.0));
-            static const int rank[3] = {0, 2, 1};
-            key[i] = ((uint64_t)rank[c->flag_1[i]] << 62) | morton2(qx, qy);
-        }
-        std::stable_sort(h->iperm.begin(), h->iperm.end(), [&](int a, int b) { return key[a] < key[b]; });
-    }
-    h->perm.resize(n);
-    for (int p2 = 0; p2 < n; p2++) h->perm[h->iperm[p2]] = p2;
-
-    // ---- sliced ELL
-    h->np = (n + 31) / 32 * 32;
-    h->nslices = h->np / 32;
-    std::vector<long long> sbase(h->nslices);
-    long long tot = 0;
-    for (int s = 0; s < h->nslices; s++) {
-        int w = 0;
-        for (int l = 0; l < 32; l++) {
-            int pp = s * 32 + l;
-            if (pp < n) w = std::max(w, c->nbhs[h->iperm[pp]]);
-        }
-        sbase[s] = tot;
-        tot += 32LL * w;
-    }
-    const size_t ne = (size_t)std::max(tot, 32LL);
-    std::vector<int> e_nbr(ne, 0);
-    std::vector<double4_32a> e_geo(ne, make_double4_32a(0, 0, 0, 0));
-    std::vector<double2> e_sn(ne, make_double2(0, 0));
-    std::vector<double> e_dist(ne, 1.0);
-    std::vector<uint8_t> e_dir(ne, 0);
-    std::vector<float4> e_geo32(ne, make_float4(0, 0, 0, 0));
-    std::vector<float2> e_sn32(ne, make_float2(0, 0));
-    std::vector<int8_t> flag(h->np, 1);
-    std::vector<int> nbh(h->np, 0);
-    std::vector<double2> nrm(h->np, make_double2(0, 1));
-    std::vector<double> eps2(h->np, 0.0);
-    std::vector<float> eps2_32(h->np, 0.0f);
-    std::vector<double4_32a> ggeo(h->np, make_double4_32a(0, 0, 0, 0));
-    std::vector<double4_32a> fgeo((size_t)h->np * 4, make_double4_32a(0, 0, 0, 0));
-    std::vector<double2> fcoef((size_t)h->np * 4, make_double2(0, 0));
-    std::vector<double4_32a> gcoef(h->np, make_double4_32a(0, 0, 0, 0));
-    std::vector<float2> e_xy32(ne, make_float2(0, 0));
-    const bool unit_w = p->power == 0.0;
-    std::vector<float> e_dist32(ne, 1.0f);
-    const Precomp &P = h->pc;
-    for (int pp = 0; pp < n; pp++) {
-        const int i = h->iperm[pp];
-        flag[pp] = (int8_t)c->flag_1[i];
-        nbh[pp] = c->nbhs[i];
-        nrm[pp] = make_double2(P.nx[i], P.ny[i]);
-        eps2[pp] = P.eps2[i];
-        eps2_32[pp] = (float)P.eps2[i];
-        ggeo[pp] = make_double4_32a(P.ggeo[4 * (size_t)i], P.ggeo[4 * (size_t)i + 1], P.ggeo[4 * (size_t)i + 2],
-                                P.ggeo[4 * (size_t)i + 3]);
-        // q_variables_mod.h:112-116 as coefficients: dq_x = Sx syy/det - Sy sxy/det, dq_y = Sy sxx/det - Sx sxy/det
-        gcoef[pp] = make_double4_32a(P.ggeo[4 * (size_t)i + 1] * P.ggeo[4 * (size_t)i + 3],
-                                     P.ggeo[4 * (size_t)i + 2] * P.ggeo[4 * (size_t)i + 3],
-                                     P.ggeo[4 * (size_t)i + 0] * P.ggeo[4 * (size_t)i + 3], 0.0);
-        static const bool used[3][4] = {{true, true, false, true}, {true, true, true, true}, {true, true, true, false}};
-        const int fl = c->flag_1[i];
-        const double scale = fl == kWall ? 2.0 : 1.0;  // flux_residual_mod.h:29
-        for (int d = 0; d < 4; d++) {
-            const double *F = &P.fgeo[((size_t)i * 4 + d) * 4];
-            fgeo[(size_t)pp * 4 + d] = make_double4_32a(F[0], F[1], F[2], F[3]);
-            // x rows (d < 2): G = (Sx syy - Sy sxy) / det;  y rows: G = (Sy sxx - Sx sxy) / det
-            double a = 0.0, b = 0.0;
-            if (used[fl][d]) {
-                if (d < 2) { a = scale * F[1] * F[3]; b = -scale * F[2] * F[3]; }
-                else { a = -scale * F[2] * F[3]; b = scale * F[0] * F[3]; }
-            }
-            fcoef[(size_t)pp * 4 + d] = make_double2(a, b);
-        }
-        for (int r = 0; r < c->nbhs[i]; r++) {
-            const size_t e = (size_t)(sbase[pp >> 5] + 32LL * r + (pp & 31));
-            const size_t src = (size_t)i * NB + r;
-            e_nbr[e] = h->perm[c->conn[src] - 1];
-            e_geo[e] = make_double4_32a(P.geo[4 * src], P.geo[4 * src + 1], P.geo[4 * src + 2], P.geo[4 * src + 3]);
-            e_sn[e] = make_double2(P.sn[2 * src], P.sn[2 * src + 1]);
-            e_dist[e] = P.dist[src];
-            e_dist32[e] = (float)P.dist[src];
-            e_xy32[e] = make_float2((float)P.geo[4 * src], (float)P.geo[4 * src + 1]);
-            e_dir[e] = P.edge_dir[src];
-            e_geo32[e] = make_float4((float)P.geo[4 * src], (float)P.geo[4 * src + 1], (float)P.geo[4 * src + 2],
-                                     (float)P.geo[4 * src + 3]);
-            e_sn32[e] = make_float2((float)P.sn[2 * src], (float)P.sn[2 * src + 1]);
-        }
-    }
-
-    // ---- device
     cudaError_t ce = cudaStreamCreateWithFlags(&h->L.stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) {
         qlskum_status s2 = fail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaStreamCreate: %s", cudaGetErrorString(ce)));
@@ -711,50 +810,29 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
     h->L.block = p->block_size ? p->block_size : 128;
     h->L.launches = &h->launches;
     DeviceArena &A = h->arena;
+    {
+        st = build_geometry(c, p, sp, true, p->precision == QLSKUM_MIXED, A, h->L.stream, G);
+        if (st) {
+            A.release();
+            cudaStreamDestroy(h->L.stream);
+            delete h;
+            return st;
+        }
+        h->np = G.np;
+        h->nslices = G.nslices;
+        h->perm = std::move(G.perm);
+        h->iperm = std::move(G.iperm);
+        h->pc = std::move(G.pc);
+        h->pc.release_upload_data();
+        h->dc = G.dc;
+        h->d_wall_perm = G.d_wall_perm;
+        h->d_wall_geo = G.d_wall_geo;
+    }
     auto up = [&](auto *dptr, const auto &vec) {
         if (dptr && !vec.empty())
             cudaMemcpyAsync(dptr, vec.data(), vec.size() * sizeof(vec[0]), cudaMemcpyHostToDevice, h->L.stream);
     };
-    int8_t *d_flag = A.alloc<int8_t>(h->np);
-    int *d_nb = A.alloc<int>(h->np);
-    long long *d_sb = A.alloc<long long>(h->nslices);
-    int *d_enbr = A.alloc<int>(ne);
-    double4_32a *d_egeo = A.alloc<double4_32a>(ne);
-    double2 *d_esn = A.alloc<double2>(ne);
-    double *d_edist = A.alloc<double>(ne);
-    uint8_t *d_edir = A.alloc<uint8_t>(ne);
-    double2 *d_nrm = A.alloc<double2>(h->np);
-    double *d_eps2 = A.alloc<double>(h->np);
-    double4_32a *d_ggeo = A.alloc<double4_32a>(h->np);
-    double4_32a *d_fgeo = A.alloc<double4_32a>((size_t)h->np * 4);
-    float4 *d_egeo32 = nullptr;
-    float2 *d_esn32 = nullptr;
-    float *d_eps32 = nullptr, *d_edist32 = nullptr;
-    double2 *d_fcoef = nullptr;
-    double4_32a *d_gcoef = nullptr;
-    float2 *d_exy32 = nullptr;
-    if (p->precision == QLSKUM_MIXED) {
-        if (unit_w) {
-            d_exy32 = A.alloc<float2>(ne);
-        } else {
-            d_egeo32 = A.alloc<float4>(ne);
-            d_esn32 = A.alloc<float2>(ne);
-        }
-        d_eps32 = A.alloc<float>(h->np);
-        d_edist32 = A.alloc<float>(ne);
-        d_fcoef = A.alloc<double2>((size_t)h->np * 4);
-        d_gcoef = A.alloc<double4_32a>(h->np);
-    }
-    up(d_flag, flag); up(d_nb, nbh); up(d_sb, sbase); up(d_enbr, e_nbr); up(d_egeo, e_geo); up(d_esn, e_sn);
-    up(d_edist, e_dist); up(d_edir, e_dir); up(d_nrm, nrm); up(d_eps2, eps2); up(d_ggeo, ggeo); up(d_fgeo, fgeo);
-    up(d_egeo32, e_geo32); up(d_esn32, e_sn32); up(d_eps32, eps2_32); up(d_edist32, e_dist32); up(d_fcoef, fcoef);
-    up(d_gcoef, gcoef); up(d_exy32, e_xy32);
-    DevCloud &dc = h->dc;
-    dc.n = n; dc.np = h->np; dc.flag = d_flag; dc.nbhs = d_nb; dc.slice_base = d_sb; dc.e_nbr = d_enbr;
-    dc.e_geo = d_egeo; dc.e_sn = d_esn; dc.e_dist = d_edist; dc.e_dir = d_edir; dc.nrm = d_nrm; dc.eps2 = d_eps2;
-    dc.ggeo = d_ggeo; dc.fgeo = d_fgeo; dc.e_geo32 = d_egeo32; dc.e_sn32 = d_esn32; dc.eps2_32 = d_eps32;
-    dc.e_dist32 = d_edist32; dc.fcoef = d_fcoef; dc.gcoef = d_gcoef; dc.unit_w = unit_w ? 1 : 0; dc.e_xy32 = d_exy32;
-
+    const int n = c->n;
     for (int b = 0; b < 3; b++) h->s64.prim[b] = A.alloc<double4_32a>(h->np);
     for (int b = 0; b < 2; b++) {
         h->s64.q[b] = A.alloc<double4_32a>(h->np);
@@ -784,8 +862,6 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
     h->d_obj_partial = A.alloc<double>(4 * (size_t)((std::max(n, sp) + 255) / 256));
     h->d_entropy = A.alloc<double>(h->np);
     h->d_last = A.alloc<double>(2);
-    h->d_wall_perm = A.alloc<int>(std::max(sp, 1));
-    h->d_wall_geo = A.alloc<double4_32a>(std::max(sp, 1));
     if (A.err != cudaSuccess) {
         qlskum_status s2 = fail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(A.err)));
         A.release();
@@ -793,22 +869,6 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
         delete h;
         return s2;
     }
-    // compute_force_coeffs_mod.h:37-59 geometry of the first shape_points points
-    std::vector<int> wperm(std::max(sp, 1), 0);
-    std::vector<double4_32a> wgeo(std::max(sp, 1), make_double4_32a(0, 0, 0, 0));
-    for (int m = 0; m < sp; m++) {
-        int r = c->right[m] - 1, l = c->left[m] - 1;
-        double lx = c->x[l], ly = c->y[l], mx = c->x[m], my = c->y[m], rx = c->x[r], ry = c->y[r];
-        double ds1 = std::pow((mx - lx), 2) + std::pow((my - ly), 2);
-        ds1 = std::sqrt(ds1);
-        double ds2 = std::pow((rx - mx), 2) + std::pow((ry - my), 2);
-        ds2 = std::sqrt(ds2);
-        double ds = 0.5 * (ds1 + ds2);
-        wperm[m] = h->perm[m];
-        wgeo[m] = make_double4_32a(ds, mx - 0.25, my, 0.0);
-    }
-    up(h->d_wall_perm, wperm);
-    up(h->d_wall_geo, wgeo);
     // initial_conditions_mod.h:23-37
     std::vector<double4_32a> prim0(h->np, make_double4_32a(h->K.rho_inf, h->K.u1_inf, h->K.u2_inf, h->K.pr_inf));
     for (int b = 0; b < 3; b++) up(h->s64.prim[b], prim0);
@@ -1159,6 +1219,419 @@ qlskum_status qlskum_get_kernel_timing(qlskum_handle *h, int kernel, double *ms_
     if (st) return st;
     if (ms_total) *ms_total = h->kt_ms[kernel];
     if (launches) *launches = h->kt_n[kernel];
+    return QLSKUM_OK;
+}
+
+}  // extern "C"
+
+// =================================================================== batches
+
+struct qlskum_batch {
+    qlskum_params prm{};
+    std::vector<Geometry> geo;                 // per cloud
+    std::vector<BatchCase> cases;
+    std::vector<BatchTile> tiles[3];
+    DeviceArena arena;
+    BatchView view;
+    Launch L;
+    long long launches = 0;
+    long long total = 0;                       // state points over all cases
+    double4_32a *prim[3] = {nullptr, nullptr, nullptr};
+    float4 *q[2] = {nullptr, nullptr};
+    float4 *dq[2] = {nullptr, nullptr};
+    float4 *qm = nullptr;
+    float *delta = nullptr, *cspeed = nullptr;
+    double *psum = nullptr, *pmax = nullptr;   // per flux tile
+    int *d_iter = nullptr, *d_status = nullptr;
+    double *res_old = nullptr, *res_new = nullptr, *hist = nullptr;
+    int capacity = 0;
+    double *d_obj = nullptr, *d_obj_scratch = nullptr, *d_entropy = nullptr;
+    int pcur = 0;
+    int tile = 128, flux_variant = 0;
+    bool tuned = false, derived_valid = false;
+    int it = 0;
+    float cfl = 0.f;
+    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+    std::string err;
+};
+
+namespace {
+
+qlskum_status bfail(qlskum_batch *b, qlskum_status s, const std::string &msg)
+{
+    if (b) b->err = msg;
+    else g_create_error = msg;
+    return s;
+}
+
+#define BCK(b, call)                                                                                    \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) return bfail(b, QLSKUM_ERR_CUDA, fmt("%s: %s", #call, cudaGetErrorString(e_))); \
+    } while (0)
+
+static const int kFluxTile[4] = {128, 128, 64, 256};
+static const int kFluxMinB[4] = {4, 5, 8, 2};
+
+void batch_enqueue_iteration(qlskum_batch *b, int o)
+{
+    const int x = (o + 1) % 3, y = (o + 2) % 3;
+    const int dst[4] = {x, y, x, y};
+    const int src[4] = {o, x, y, x};
+    const int ni = b->prm.inner_iterations;
+    for (int rk = 1; rk <= 4; rk++) {
+        const int qa = (rk - 1) & 1, qb = rk & 1;
+        mixed::batch_q_derivatives(b->L, b->view, b->tile, b->q[qa], b->dq[0], b->qm, b->cspeed,
+                                   rk == 1 ? b->delta : nullptr, b->cfl);
+        for (int j = 0; j < ni; j++) mixed::batch_q_inner(b->L, b->view, b->tile, b->q[qa], b->dq[j & 1], b->dq[(j + 1) & 1]);
+        mixed::batch_flux_update(b->L, b->view, b->flux_variant, b->q[qa], b->dq[ni & 1], b->qm, b->delta,
+                                 b->prim[src[rk - 1]], b->prim[o], b->prim[dst[rk - 1]], b->q[qb],
+                                 rk == 4 ? b->cspeed : nullptr, rk, rk == 4 ? b->psum : nullptr,
+                                 rk == 4 ? b->pmax : nullptr);
+    }
+    mixed::batch_reduce(b->L, b->view, kFluxTile[b->flux_variant], b->psum, b->pmax, b->d_iter, b->res_old,
+                        b->res_new, b->hist, b->capacity, b->d_status);
+}
+
+qlskum_status batch_ensure_hist(qlskum_batch *b, int needed)
+{
+    if (needed <= b->capacity) return QLSKUM_OK;
+    int cap = std::max(256, b->capacity);
+    while (cap < needed) cap *= 2;
+    const size_t nc = b->cases.size();
+    double *nh = nullptr;
+    BCK(b, cudaMalloc(&nh, sizeof(double) * nc * (size_t)cap));
+    BCK(b, cudaMemsetAsync(nh, 0, sizeof(double) * nc * (size_t)cap, b->L.stream));
+    if (b->hist) {
+        BCK(b, cudaMemcpyAsync(nh, b->hist, sizeof(double) * nc * (size_t)b->capacity, cudaMemcpyDeviceToDevice,
+                               b->L.stream));
+        BCK(b, cudaStreamSynchronize(b->L.stream));
+        cudaFree(b->hist);
+    }
+    b->hist = nh;
+    b->capacity = cap;
+    for (auto &g : b->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    return QLSKUM_OK;
+}
+
+// Batch autotuner: points per tile of the gradient / inner-loop kernels and
+// the shape of the flux kernel, each timed over three launches on the batch.
+qlskum_status batch_tune(qlskum_batch *b)
+{
+    if (b->tuned) return QLSKUM_OK;
+    b->tuned = true;
+    if (b->prm.block_size != 0) {
+        b->tile = b->prm.block_size == 64 || b->prm.block_size == 256 ? b->prm.block_size : 128;
+        return QLSKUM_OK;
+    }
+    cudaEvent_t e0, e1;
+    BCK(b, cudaEventCreate(&e0));
+    BCK(b, cudaEventCreate(&e1));
+    auto time3 = [&](auto &&launch) -> float {
+        launch();
+        cudaEventRecord(e0, b->L.stream);
+        for (int r = 0; r < 3; r++) launch();
+        cudaEventRecord(e1, b->L.stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms;
+    };
+    const long long l0 = b->launches;
+    float best = 1e30f;
+    for (int t : {64, 128, 256}) {
+        float ms = time3([&] { mixed::batch_q_inner(b->L, b->view, t, b->q[0], b->dq[0], b->dq[1]); });
+        if (ms < best) { best = ms; b->tile = t; }
+    }
+    const int o = b->pcur, x = (o + 1) % 3;
+    mixed::batch_q_derivatives(b->L, b->view, b->tile, b->q[0], b->dq[0], b->qm, b->cspeed, b->delta, b->cfl);
+    best = 1e30f;
+    for (int v = 0; v < 4; v++) {
+        float ms = time3([&] {
+            mixed::batch_flux_update(b->L, b->view, v, b->q[0], b->dq[0], b->qm, b->delta, b->prim[o], b->prim[o],
+                                     b->prim[x], b->q[1], nullptr, 1, nullptr, nullptr);
+        });
+        if (ms < best) { best = ms; b->flux_variant = v; }
+    }
+    b->launches = l0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return bfail(b, QLSKUM_ERR_CUDA, fmt("batch tune: %s", cudaGetErrorString(e)));
+    return QLSKUM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+qlskum_status qlskum_batch_create(const qlskum_cloud *clouds, int n_clouds, const int *case_cloud,
+                                  const double *case_mach, const double *case_aoa, int n_cases,
+                                  const qlskum_params *params, qlskum_batch **out)
+{
+    if (!out) return bfail(nullptr, QLSKUM_ERR_INVALID, "null output batch pointer");
+    *out = nullptr;
+    if (!clouds || n_clouds < 1 || !case_cloud || !case_mach || !case_aoa || n_cases < 1 || !params)
+        return bfail(nullptr, QLSKUM_ERR_INVALID, "batch needs >= 1 cloud, >= 1 case and non-null arrays");
+    if (params->precision != QLSKUM_MIXED)
+        return bfail(nullptr, QLSKUM_ERR_UNSUPPORTED, "batched launches run the mixed-precision form only");
+    for (int c = 0; c < n_cases; c++)
+        if (case_cloud[c] < 0 || case_cloud[c] >= n_clouds)
+            return bfail(nullptr, QLSKUM_ERR_INVALID, fmt("case %d: cloud index %d out of range", c, case_cloud[c]));
+    std::vector<int> sp(n_clouds);
+    std::vector<Geometry> geo(n_clouds);
+    for (int k = 0; k < n_clouds; k++) {
+        qlskum_status st = validate(&clouds[k], params, &sp[k]);
+        if (st) return bfail(nullptr, st, fmt("cloud %d: %s", k, g_create_error.c_str()));
+        st = precompute(&clouds[k], params, geo[k].pc);
+        if (st) return bfail(nullptr, st, fmt("cloud %d: %s", k, g_create_error.c_str()));
+    }
+    qlskum_batch *b = new qlskum_batch();
+    b->prm = *params;
+    b->cfl = (float)params->cfl;
+    b->geo = std::move(geo);
+    cudaError_t ce = cudaStreamCreateWithFlags(&b->L.stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) {
+        delete b;
+        return bfail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaStreamCreate: %s", cudaGetErrorString(ce)));
+    }
+    b->L.launches = &b->launches;
+    DeviceArena &A = b->arena;
+    auto cleanup = [&](qlskum_status st, const std::string &m) {
+        A.release();
+        cudaStreamDestroy(b->L.stream);
+        delete b;
+        return bfail(nullptr, st, m);
+    };
+    for (int k = 0; k < n_clouds; k++) {
+        qlskum_status st = build_geometry(&clouds[k], params, sp[k], false, true, A, b->L.stream, b->geo[k]);
+        if (st) return cleanup(st, fmt("cloud %d: %s", k, g_create_error.c_str()));
+        b->geo[k].pc = Precomp();
+        std::vector<int>().swap(b->geo[k].perm);
+    }
+    // cases, state offsets and the tile tables of the three tile sizes
+    long long off = 0;
+    b->cases.resize(n_cases);
+    for (int c = 0; c < n_cases; c++) {
+        BatchCase &C = b->cases[c];
+        C.cloud = case_cloud[c];
+        C.n = clouds[C.cloud].n;
+        C.off = off;
+        off += (C.n + 31) / 32 * 32;
+        CaseConst &K = C.K;
+        K.pi = 4 * std::atan(1.0);
+        K.rho_inf = 1.0;
+        K.pr_inf = 1.0 / 1.4;
+        K.gamma = 1.4;
+        K.mach = case_mach[c];
+        K.theta = case_aoa[c] * K.pi / 180;
+        K.u1_inf = case_mach[c] * std::cos(K.theta);
+        K.u2_inf = case_mach[c] * std::sin(K.theta);
+        K.cfl = params->cfl;
+    }
+    b->total = off;
+    const int tsz[3] = {64, 128, 256};
+    for (int ti = 0; ti < 3; ti++) {
+        for (int c = 0; c < n_cases; c++) {
+            BatchCase &C = b->cases[c];
+            C.tile0[ti] = (int)b->tiles[ti].size();
+            for (int f = 0; f < C.n; f += tsz[ti]) b->tiles[ti].push_back(BatchTile{c, f});
+            C.ntl[ti] = (int)b->tiles[ti].size() - C.tile0[ti];
+        }
+    }
+    std::vector<DevCloud> dcs(n_clouds);
+    for (int k = 0; k < n_clouds; k++) dcs[k] = b->geo[k].dc;
+    DevCloud *d_clouds = A.alloc<DevCloud>(n_clouds);
+    BatchCase *d_cases = A.alloc<BatchCase>(n_cases);
+    BatchTile *d_tiles[3];
+    for (int ti = 0; ti < 3; ti++) d_tiles[ti] = A.alloc<BatchTile>(b->tiles[ti].size());
+    const size_t T = (size_t)b->total;
+    for (int k = 0; k < 3; k++) b->prim[k] = A.alloc<double4_32a>(T);
+    for (int k = 0; k < 2; k++) {
+        b->q[k] = A.alloc<float4>(T);
+        b->dq[k] = A.alloc<float4>(2 * T);
+    }
+    b->qm = A.alloc<float4>(2 * T);
+    b->delta = A.alloc<float>(T);
+    b->cspeed = A.alloc<float>(T);
+    b->psum = A.alloc<double>(b->tiles[0].size());
+    b->pmax = A.alloc<double>(b->tiles[0].size());
+    b->d_iter = A.alloc<int>(1);
+    b->d_status = A.alloc<int>(1);
+    b->res_old = A.alloc<double>(n_cases);
+    b->res_new = A.alloc<double>(n_cases);
+    b->d_obj = A.alloc<double>(4 * (size_t)n_cases);
+    size_t maxn = 1;
+    for (int k = 0; k < n_clouds; k++) maxn = std::max(maxn, (size_t)std::max(clouds[k].n, sp[k]));
+    b->d_obj_scratch = A.alloc<double>(4 * ((maxn + 255) / 256));
+    b->d_entropy = A.alloc<double>(T);
+    if (A.err != cudaSuccess) return cleanup(QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(A.err)));
+    cudaStream_t s = b->L.stream;
+    cudaMemcpyAsync(d_clouds, dcs.data(), sizeof(DevCloud) * n_clouds, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_cases, b->cases.data(), sizeof(BatchCase) * n_cases, cudaMemcpyHostToDevice, s);
+    for (int ti = 0; ti < 3; ti++)
+        cudaMemcpyAsync(d_tiles[ti], b->tiles[ti].data(), sizeof(BatchTile) * b->tiles[ti].size(),
+                        cudaMemcpyHostToDevice, s);
+    // initial_conditions_mod.h:23-37 per case
+    std::vector<double4_32a> prim0(T, make_double4_32a(1.0, 0.0, 0.0, 1.0 / 1.4));
+    for (const BatchCase &C : b->cases)
+        for (int i = 0; i < C.n; i++)
+            prim0[C.off + i] = make_double4_32a(C.K.rho_inf, C.K.u1_inf, C.K.u2_inf, C.K.pr_inf);
+    for (int k = 0; k < 3; k++)
+        cudaMemcpyAsync(b->prim[k], prim0.data(), sizeof(double4_32a) * T, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(b->d_iter, 0, sizeof(int), s);
+    cudaMemsetAsync(b->d_status, 0, sizeof(int), s);
+    cudaMemsetAsync(b->res_old, 0, sizeof(double) * n_cases, s);
+    cudaMemsetAsync(b->res_new, 0, sizeof(double) * n_cases, s);
+    cudaMemsetAsync(b->dq[0], 0, sizeof(float4) * 2 * T, s);
+    cudaMemsetAsync(b->dq[1], 0, sizeof(float4) * 2 * T, s);
+    ce = cudaStreamSynchronize(s);
+    if (ce == cudaSuccess) ce = cudaGetLastError();
+    if (ce != cudaSuccess) return cleanup(QLSKUM_ERR_CUDA, fmt("batch upload: %s", cudaGetErrorString(ce)));
+    b->view.clouds = d_clouds;
+    b->view.cases = d_cases;
+    b->view.ncases = n_cases;
+    for (int ti = 0; ti < 3; ti++) {
+        b->view.tiles[ti] = d_tiles[ti];
+        b->view.ntiles[ti] = (int)b->tiles[ti].size();
+    }
+    b->view.unit_w = params->power == 0.0 ? 1 : 0;
+    if (batch_ensure_hist(b, 256) != QLSKUM_OK) return cleanup(QLSKUM_ERR_CUDA, b->err);
+    *out = b;
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_batch_destroy(qlskum_batch *b)
+{
+    if (!b) return QLSKUM_OK;
+    if (b->L.stream) cudaStreamSynchronize(b->L.stream);
+    for (auto &g : b->graph)
+        if (g) cudaGraphExecDestroy(g);
+    if (b->hist) cudaFree(b->hist);
+    b->arena.release();
+    if (b->L.stream) cudaStreamDestroy(b->L.stream);
+    delete b;
+    return QLSKUM_OK;
+}
+
+const char *qlskum_batch_last_error(const qlskum_batch *b) { return b ? b->err.c_str() : g_create_error.c_str(); }
+
+qlskum_status qlskum_batch_run(qlskum_batch *b, int iters)
+{
+    if (!b) return bfail(nullptr, QLSKUM_ERR_INVALID, "null batch");
+    if (iters < 0) return bfail(b, QLSKUM_ERR_INVALID, "iters < 0");
+    qlskum_status st = batch_ensure_hist(b, b->it + iters);
+    if (st) return st;
+    if (!b->derived_valid) {
+        mixed::batch_derived(b->L, b->view, 128, b->prim[b->pcur], b->q[0], b->cspeed);
+        b->derived_valid = true;
+        st = batch_tune(b);
+        if (st) return st;
+    }
+    for (int o = 0; o < 3 && iters > 0; o++) {
+        if (b->graph[o]) continue;
+        cudaGraph_t g = nullptr;
+        BCK(b, cudaStreamBeginCapture(b->L.stream, cudaStreamCaptureModeThreadLocal));
+        const long long l0 = b->launches;
+        batch_enqueue_iteration(b, o);
+        b->launches = l0;
+        cudaError_t e = cudaStreamEndCapture(b->L.stream, &g);
+        if (e != cudaSuccess) return bfail(b, QLSKUM_ERR_CUDA, fmt("batch capture: %s", cudaGetErrorString(e)));
+        e = cudaGraphInstantiate(&b->graph[o], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return bfail(b, QLSKUM_ERR_CUDA, fmt("batch instantiate: %s", cudaGetErrorString(e)));
+    }
+    for (int t = 0; t < iters; t++) {
+        const int o = b->pcur;
+        BCK(b, cudaGraphLaunch(b->graph[o], b->L.stream));
+        b->launches += 4 * (2 + b->prm.inner_iterations) + 2;
+        b->pcur = (o + 2) % 3;
+        b->it += 1;
+    }
+    int status = 0;
+    BCK(b, cudaMemcpyAsync(&status, b->d_status, sizeof(int), cudaMemcpyDeviceToHost, b->L.stream));
+    BCK(b, cudaStreamSynchronize(b->L.stream));
+    if (status) return bfail(b, QLSKUM_ERR_NONFINITE, "a case's residual became non-finite");
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_batch_objective(qlskum_batch *b, double *cl, double *cd, double *cm, double *entropy)
+{
+    if (!b) return bfail(nullptr, QLSKUM_ERR_INVALID, "null batch");
+    const int nc = (int)b->cases.size();
+    for (int c = 0; c < nc; c++) {
+        const BatchCase &C = b->cases[c];
+        const Geometry &G = b->geo[C.cloud];
+        const double cp_scale = 0.5 * C.K.rho_inf * C.K.mach * C.K.mach;
+        fp64::objective(b->L, G.dc, b->prim[b->pcur] + C.off, G.d_wall_perm, G.d_wall_geo, G.shape_points, cp_scale,
+                        C.K.pr_inf, C.K.gamma, b->d_entropy + C.off, b->d_obj + 4 * c, b->d_obj_scratch);
+    }
+    std::vector<double> o(4 * (size_t)nc);
+    BCK(b, cudaMemcpyAsync(o.data(), b->d_obj, sizeof(double) * o.size(), cudaMemcpyDeviceToHost, b->L.stream));
+    BCK(b, cudaStreamSynchronize(b->L.stream));
+    for (int c = 0; c < nc; c++) {
+        const double H = o[4 * c], V = o[4 * c + 1], th = b->cases[c].K.theta;
+        if (cl) cl[c] = V * std::cos(th) - H * std::sin(th);
+        if (cd) cd[c] = H * std::cos(th) + V * std::sin(th);
+        if (cm) cm[c] = o[4 * c + 2];
+        if (entropy) entropy[c] = o[4 * c + 3];
+    }
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_batch_get_prim(qlskum_batch *b, int case_index, double *out)
+{
+    if (!b) return bfail(nullptr, QLSKUM_ERR_INVALID, "null batch");
+    if (case_index < 0 || case_index >= (int)b->cases.size() || !out)
+        return bfail(b, QLSKUM_ERR_INVALID, "case index out of range or null output");
+    const BatchCase &C = b->cases[case_index];
+    const Geometry &G = b->geo[C.cloud];
+    std::vector<double> dev(4 * (size_t)C.n);
+    BCK(b, cudaMemcpyAsync(dev.data(), b->prim[b->pcur] + C.off, sizeof(double) * dev.size(), cudaMemcpyDeviceToHost,
+                           b->L.stream));
+    BCK(b, cudaStreamSynchronize(b->L.stream));
+    for (int p = 0; p < C.n; p++) std::memcpy(out + 4 * (size_t)G.iperm[p], dev.data() + 4 * (size_t)p, 32);
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_batch_residual_history(qlskum_batch *b, double *out, int max_rows, int *rows)
+{
+    if (!b) return bfail(nullptr, QLSKUM_ERR_INVALID, "null batch");
+    const int cnt = std::min(b->it, b->capacity);
+    if (rows) *rows = cnt;
+    const int m = std::min(cnt, std::max(0, max_rows));
+    if (out && m > 0) {
+        BCK(b, cudaMemcpyAsync(out, b->hist, sizeof(double) * b->cases.size() * (size_t)m, cudaMemcpyDeviceToHost,
+                               b->L.stream));
+        BCK(b, cudaStreamSynchronize(b->L.stream));
+    }
+    return QLSKUM_OK;
+}
+
+long long qlskum_batch_total_points(const qlskum_batch *b)
+{
+    if (!b) return 0;
+    long long t = 0;
+    for (const BatchCase &C : b->cases) t += C.n;
+    return t;
+}
+
+long long qlskum_batch_launch_count(const qlskum_batch *b) { return b ? b->launches : 0; }
+
+void *qlskum_batch_stream(qlskum_batch *b) { return b ? (void *)b->L.stream : nullptr; }
+
+qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_tile, int *flux_min_blocks,
+                                  int *points_per_warp)
+{
+    if (!b) return QLSKUM_ERR_INVALID;
+    if (tile) *tile = b->tile;
+    if (flux_tile) *flux_tile = kFluxTile[b->flux_variant];
+    if (flux_min_blocks) *flux_min_blocks = kFluxMinB[b->flux_variant];
+    if (points_per_warp) *points_per_warp = 32;
     return QLSKUM_OK;
 }
 

@@ -68,6 +68,35 @@ struct CaseConst {
     double cfl;
 };
 
+// ----------------------------------------------------------------- batches
+// A batch runs many cases (a cloud and a flight condition each) through the
+// same kernels: the state of case c occupies points [off, off + n) of the
+// batch arrays; its geometry is its cloud's DevCloud.  Work is cut into tiles
+// of 64, 128 or 256 points of one case (one thread per point).
+constexpr int tile_index(int tile) { return tile == 64 ? 0 : (tile == 256 ? 2 : 1); }
+
+struct BatchCase {
+    int cloud;
+    int n;
+    long long off;
+    int tile0[3], ntl[3];                    // first tile and tile count per tile size
+    CaseConst K;
+};
+
+struct BatchTile {
+    int cas;
+    int first;                               // first cloud-local point (a multiple of 32)
+};
+
+struct BatchView {
+    const DevCloud *clouds = nullptr;        // device array [n_clouds]
+    const BatchCase *cases = nullptr;        // device array [ncases]
+    int ncases = 0;
+    const BatchTile *tiles[3] = {nullptr, nullptr, nullptr};
+    int ntiles[3] = {0, 0, 0};
+    int unit_w = 0;
+};
+
 // FP64 state buffers of one handle.
 struct State64 {
     double4_32a *prim[3] = {nullptr, nullptr, nullptr};
@@ -142,6 +171,17 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
                  double4_32a *prim_next, float4 *q_next, float *cspeed_next, int rk, const Reduce &R, int variant);
 int flux_variants();
 int flux_block(int variant);
+// batched (persistent) forms
+void batch_derived(const Launch &L, const BatchView &B, int tile, const double4_32a *prim, float4 *q, float *cs);
+void batch_q_derivatives(const Launch &L, const BatchView &B, int tile, const float4 *q, float4 *dq, float4 *qm,
+                         const float *cs, float *delta, float cfl);
+void batch_q_inner(const Launch &L, const BatchView &B, int tile, const float4 *q, const float4 *dq_in,
+                   float4 *dq_out);
+void batch_flux_update(const Launch &L, const BatchView &B, int variant, const float4 *q, const float4 *dq,
+                       const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
+                       double4_32a *prim_next, float4 *q_next, float *cs_next, int rk, double *psum, double *pmax);
+void batch_reduce(const Launch &L, const BatchView &B, int flux_tile, const double *psum, const double *pmax,
+                  int *iter, double *res_old, double *res_new, double *hist, int capacity, int *status);
 }  // namespace mixed
 
 }  // namespace qlskum

@@ -150,15 +150,19 @@ __device__ __forceinline__ void solve_grad(const double4_32a &m, const float sdx
     }
 }
 
+// ----------------------------------------------------------- point bodies
+// One point's work, shared by the single-case kernels and the batched
+// persistent kernels.  Geometry (c) is indexed by the cloud-local point i;
+// the state pointers are already offset to the case's first point, so
+// neighbour indices from the edge list address them directly.
+
 // q_variables_mod.h:36-118: FP32 differences and sums, FP64 solve; in the
 // first stage also the local time step (state_update_mod.h:448-496) in FP32.
 template <bool UW>
-__global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4 *__restrict__ dq,
-                                float4 *__restrict__ qm, const float *__restrict__ cs, float *__restrict__ delta,
-                                float cfl)
+__device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float4 *__restrict__ q,
+                                           float4 *__restrict__ dq, float4 *__restrict__ qm,
+                                           const float *__restrict__ cs, float *__restrict__ delta, float cfl)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
     float qi[4], qmax[4], qmin[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
     ld4(q[i], qi);
 #pragma unroll
@@ -192,11 +196,9 @@ __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4
 
 // q_variables_mod.h:120-213
 template <bool UW>
-__global__ void k_q_inner(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ dq_in,
-                          float4 *__restrict__ dq_out)
+__device__ __forceinline__ void inner_point(const DevCloud &c, int i, const float4 *__restrict__ q,
+                                            const float4 *__restrict__ dq_in, float4 *__restrict__ dq_out)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
     float qi[4], dxi[4], dyi[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
     ld4(q[i], qi);
     ld4(dq_in[2 * i], dxi);
@@ -225,7 +227,122 @@ __global__ void k_q_inner(DevCloud c, const float4 *__restrict__ q, const float4
     dq_out[2 * i + 1] = mk4(dy);
 }
 
-// Fused stage: FP32 edge work, FP64 solve / residual / update.
+// Fused stage of one point: FP32 edge work, FP64 solve / residual / update.
+// Returns the point's res_sqr.
+template <bool UW>
+__device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst &K, int i,
+                                             const float4 *__restrict__ q, const float4 *__restrict__ dq,
+                                             const float4 *__restrict__ qm, const float *__restrict__ delta,
+                                             const double4_32a *__restrict__ prim,
+                                             const double4_32a *__restrict__ prim_old,
+                                             double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
+                                             float *__restrict__ cs_next, int rk)
+{
+    const int f = c.flag[i];
+    const double2 nn = c.nrm[i];
+    const float nx = d2f(nn.x), ny = d2f(nn.y);
+    float qi[4], dxi[4], dyi[4], mxi[4], mni[4];
+    ld4(q[i], qi);
+    ld4(dq[2 * i], dxi);
+    ld4(dq[2 * i + 1], dyi);
+    ld4(qm[2 * i], mxi);
+    ld4(qm[2 * i + 1], mni);
+    const float e2i = c.eps2_32[i];
+    float sx[4][4], sy[4][4];
+#pragma unroll
+    for (int d = 0; d < 4; d++)
+#pragma unroll
+        for (int r = 0; r < 4; r++) { sx[d][r] = 0.f; sy[d][r] = 0.f; }
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        float4 g;
+        float2 sw;
+        if (UW) {
+            // dels, deln of the point's (t, n) frame (interior_fluxes_mod.h:53-54), weight 1
+            const float2 d = c.e_xy32[e];
+            g = make_float4(d.x, d.y, 0.f, 0.f);
+            sw = make_float2(d.x * ny - d.y * nx, d.x * nx + d.y * ny);
+        } else {
+            g = c.e_geo32[e];
+            sw = c.e_sn32[e];
+        }
+        const unsigned dir = c.e_dir[e];
+        float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
+        ld4(q[k], qk);
+        ld4(dq[2 * k], dxk);
+        ld4(dq[2 * k + 1], dyk);
+        ld4(qm[2 * k], mxk);
+        ld4(qm[2 * k + 1], mnk);
+        float Pi[4], Pk[4];
+        edge_states<float>(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, c.eps2_32[k], Pi, Pk);
+        Kin<float> ki, kk;
+        kin_prep<float>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
+        kin_prep<float>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
+#define QLSKUM_ACC32(D)                                                       \
+        if (dir & (1u << D)) {                                                \
+            float Gi[4], Gk[4];                                               \
+            dir_flux<float, D>(f, ki, Gi);                                    \
+            dir_flux<float, D>(f, kk, Gk);                                    \
+            _Pragma("unroll") for (int r = 0; r < 4; r++) {                   \
+                sx[D][r] += (Gk[r] - Gi[r]) * sw.x;                           \
+                sy[D][r] += (Gk[r] - Gi[r]) * sw.y;                           \
+            }                                                                 \
+        }
+        QLSKUM_ACC32(0)
+        QLSKUM_ACC32(1)
+        QLSKUM_ACC32(2)
+        QLSKUM_ACC32(3)
+#undef QLSKUM_ACC32
+    }
+    // F = delta * sum_d (a_d Sx_d + b_d Sy_d): the four solves and
+    // flux_residual_mod.h's sum (with the wall's 2 delta) in FP64.
+    double2 cf[4];
+#pragma unroll
+    for (int d = 0; d < 4; d++) cf[d] = c.fcoef[4 * i + d];
+    const double dl = f2d(delta[i]);
+    double F[4], P[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        double acc = 0.0;
+#pragma unroll
+        for (int d = 0; d < 4; d++) {
+            acc = fma(cf[d].x, f2d(sx[d][r]), acc);
+            acc = fma(cf[d].y, f2d(sy[d][r]), acc);
+        }
+        F[r] = dl * acc;
+    }
+    ld4(prim[i], P);
+    const double r2 = stage_update_fast(K, f, nn.x, nn.y, P, prim_old + i, F, rk);
+    prim_next[i] = mk4(P);
+    float Q[4];
+    q_of(P, Q);
+    q_next[i] = mk4(Q);
+    if (cs_next) cs_next[i] = wave_speed32(P);
+    return r2;
+}
+
+// ---------------------------------------------------- single-case kernels
+
+template <bool UW>
+__global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4 *__restrict__ dq,
+                                float4 *__restrict__ qm, const float *__restrict__ cs, float *__restrict__ delta,
+                                float cfl)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < c.n) grad_point<UW>(c, i, q, dq, qm, cs, delta, cfl);
+}
+
+template <bool UW>
+__global__ void k_q_inner(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ dq_in,
+                          float4 *__restrict__ dq_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < c.n) inner_point<UW>(c, i, q, dq_in, dq_out);
+}
+
 template <int BLOCK, int MINB, bool UW>
 __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseConst K, const float4 *__restrict__ q,
                                                        const float4 *__restrict__ dq, const float4 *__restrict__ qm,
@@ -236,95 +353,130 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseCon
                                                        float *__restrict__ cs_next, int rk,
                                                        double *__restrict__ psum, double *__restrict__ pmax)
 {
-    int i = blockIdx.x * BLOCK + threadIdx.x;
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
     double r2 = 0.0;
-    if (i < c.n) {
-        const int f = c.flag[i];
-        const double2 nn = c.nrm[i];
-        const float nx = d2f(nn.x), ny = d2f(nn.y);
-        float qi[4], dxi[4], dyi[4], mxi[4], mni[4];
-        ld4(q[i], qi);
-        ld4(dq[2 * i], dxi);
-        ld4(dq[2 * i + 1], dyi);
-        ld4(qm[2 * i], mxi);
-        ld4(qm[2 * i + 1], mni);
-        const float e2i = c.eps2_32[i];
-        float sx[4][4], sy[4][4];
-#pragma unroll
-        for (int d = 0; d < 4; d++)
-#pragma unroll
-            for (int r = 0; r < 4; r++) { sx[d][r] = 0.f; sy[d][r] = 0.f; }
-        const int nb = c.nbhs[i];
-        const long long base = c.slice_base[i >> 5] + (i & 31);
-        for (int j = 0; j < nb; j++) {
-            const long long e = base + 32LL * j;
-            const int k = c.e_nbr[e];
-            float4 g;
-            float2 sw;
-            if (UW) {
-                // dels, deln of the point's (t, n) frame (interior_fluxes_mod.h:53-54), weight 1
-                const float2 d = c.e_xy32[e];
-                g = make_float4(d.x, d.y, 0.f, 0.f);
-                sw = make_float2(d.x * ny - d.y * nx, d.x * nx + d.y * ny);
-            } else {
-                g = c.e_geo32[e];
-                sw = c.e_sn32[e];
-            }
-            const unsigned dir = c.e_dir[e];
-            float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
-            ld4(q[k], qk);
-            ld4(dq[2 * k], dxk);
-            ld4(dq[2 * k + 1], dyk);
-            ld4(qm[2 * k], mxk);
-            ld4(qm[2 * k + 1], mnk);
-            float Pi[4], Pk[4];
-            edge_states<float>(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, c.eps2_32[k], Pi, Pk);
-            Kin<float> ki, kk;
-            kin_prep<float>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
-            kin_prep<float>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
-#define QLSKUM_ACC32(D)                                                       \
-            if (dir & (1u << D)) {                                            \
-                float Gi[4], Gk[4];                                           \
-                dir_flux<float, D>(f, ki, Gi);                                \
-                dir_flux<float, D>(f, kk, Gk);                                \
-                _Pragma("unroll") for (int r = 0; r < 4; r++) {               \
-                    sx[D][r] += (Gk[r] - Gi[r]) * sw.x;                       \
-                    sy[D][r] += (Gk[r] - Gi[r]) * sw.y;                       \
-                }                                                             \
-            }
-            QLSKUM_ACC32(0)
-            QLSKUM_ACC32(1)
-            QLSKUM_ACC32(2)
-            QLSKUM_ACC32(3)
-#undef QLSKUM_ACC32
-        }
-        // F = delta * sum_d (a_d Sx_d + b_d Sy_d): the four solves and
-        // flux_residual_mod.h's sum (with the wall's 2 delta) in FP64.
-        double2 cf[4];
-#pragma unroll
-        for (int d = 0; d < 4; d++) cf[d] = c.fcoef[4 * i + d];
-        const double dl = f2d(delta[i]);
-        double F[4], P[4];
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            double acc = 0.0;
-#pragma unroll
-            for (int d = 0; d < 4; d++) {
-                acc = fma(cf[d].x, f2d(sx[d][r]), acc);
-                acc = fma(cf[d].y, f2d(sy[d][r]), acc);
-            }
-            F[r] = dl * acc;
-        }
-        ld4(prim[i], P);
-        r2 = stage_update_fast(K, f, nn.x, nn.y, P, prim_old + i, F, rk);
-        prim_next[i] = mk4(P);
-        float Q[4];
-        q_of(P, Q);
-        q_next[i] = mk4(Q);
-        if (cs_next) cs_next[i] = wave_speed32(P);
-    }
+    if (i < c.n) r2 = flux_point<UW>(c, K, i, q, dq, qm, delta, prim, prim_old, prim_next, q_next, cs_next, rk);
     if (psum) block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
 }
+
+// ------------------------------------------------------- batched kernels
+// Persistent grids: block b walks tiles b, b + gridDim.x, ...; a tile is
+// TILE consecutive points of one case (one thread per point), so every case
+// of every cloud runs in the same launch.
+
+template <int TILE>
+__global__ void __launch_bounds__(TILE) kb_derived(const BatchCase *__restrict__ cases,
+                                                   const BatchTile *__restrict__ tiles, int ntiles,
+                                                   const double4_32a *__restrict__ prim, float4 *__restrict__ q,
+                                                   float *__restrict__ cs)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BatchTile T = tiles[t];
+        const BatchCase &C = cases[T.cas];
+        const int i = T.first + threadIdx.x;
+        if (i < C.n) {
+            const long long g = C.off + i;
+            double P[4];
+            float Q[4];
+            ld4(prim[g], P);
+            q_of(P, Q);
+            q[g] = mk4(Q);
+            cs[g] = wave_speed32(P);
+        }
+    }
+}
+
+template <int TILE, bool UW>
+__global__ void __launch_bounds__(TILE) kb_q_derivatives(const DevCloud *__restrict__ clouds,
+                                                         const BatchCase *__restrict__ cases,
+                                                         const BatchTile *__restrict__ tiles, int ntiles,
+                                                         const float4 *__restrict__ q, float4 *__restrict__ dq,
+                                                         float4 *__restrict__ qm, const float *__restrict__ cs,
+                                                         float *__restrict__ delta, float cfl)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BatchTile T = tiles[t];
+        const BatchCase &C = cases[T.cas];
+        const int i = T.first + threadIdx.x;
+        if (i < C.n)
+            grad_point<UW>(clouds[C.cloud], i, q + C.off, dq + 2 * C.off, qm + 2 * C.off, cs + C.off,
+                           delta ? delta + C.off : nullptr, cfl);
+    }
+}
+
+template <int TILE, bool UW>
+__global__ void __launch_bounds__(TILE) kb_q_inner(const DevCloud *__restrict__ clouds,
+                                                   const BatchCase *__restrict__ cases,
+                                                   const BatchTile *__restrict__ tiles, int ntiles,
+                                                   const float4 *__restrict__ q, const float4 *__restrict__ dq_in,
+                                                   float4 *__restrict__ dq_out)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BatchTile T = tiles[t];
+        const BatchCase &C = cases[T.cas];
+        const int i = T.first + threadIdx.x;
+        if (i < C.n) inner_point<UW>(clouds[C.cloud], i, q + C.off, dq_in + 2 * C.off, dq_out + 2 * C.off);
+    }
+}
+
+template <int TILE, int MINB, bool UW>
+__global__ void __launch_bounds__(TILE, MINB) kb_flux_update(const DevCloud *__restrict__ clouds,
+                                                             const BatchCase *__restrict__ cases,
+                                                             const BatchTile *__restrict__ tiles, int ntiles,
+                                                             const float4 *__restrict__ q,
+                                                             const float4 *__restrict__ dq,
+                                                             const float4 *__restrict__ qm,
+                                                             const float *__restrict__ delta,
+                                                             const double4_32a *__restrict__ prim,
+                                                             const double4_32a *__restrict__ prim_old,
+                                                             double4_32a *__restrict__ prim_next,
+                                                             float4 *__restrict__ q_next, float *__restrict__ cs_next,
+                                                             int rk, double *__restrict__ psum,
+                                                             double *__restrict__ pmax)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BatchTile T = tiles[t];
+        const BatchCase &C = cases[T.cas];
+        const int i = T.first + threadIdx.x;
+        double r2 = 0.0;
+        if (i < C.n) {
+            const long long o = C.off;
+            r2 = flux_point<UW>(clouds[C.cloud], C.K, i, q + o, dq + 2 * o, qm + 2 * o, delta + o, prim + o,
+                                prim_old + o, prim_next + o, q_next + o, cs_next ? cs_next + o : nullptr, rk);
+        }
+        if (psum) block_sum_max<TILE>(r2, r2, psum + t, pmax + t);
+    }
+}
+
+// Per case: res_new = sqrt(sum of its tiles' partials) / n, residue against
+// res_old latched at iterations 1 and 2 (fpi_solver_mod.h:138-147).
+__global__ void kb_reduce(const BatchCase *__restrict__ cases, int ncases, int ti, const double *__restrict__ psum,
+                          const double *__restrict__ pmax, int *iter, double *res_old, double *res_new,
+                          double *hist, int capacity, int *status)
+{
+    __shared__ double ss[256];
+    const int c = blockIdx.x;
+    if (c >= ncases) return;
+    const BatchCase &C = cases[c];
+    double v = 0.0;
+    for (int t = threadIdx.x; t < C.ntl[ti]; t += 256) v += psum[C.tile0[ti] + t];
+    ss[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) ss[threadIdx.x] += ss[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int it = *iter + 1;
+        const double r = sqrt(ss[0]) / C.n;
+        if (it <= 2) res_old[c] = r;
+        res_new[c] = r;
+        if (it - 1 < capacity) hist[(size_t)(it - 1) * ncases + c] = r;
+        if (!isfinite(r)) atomicOr(status, 1);
+    }
+}
+
+__global__ void kb_count(int *iter) { *iter += 1; }
 
 #define QLSKUM_LAUNCHED(L) \
     do { if ((L).launches) ++*(L).launches; } while (0)
@@ -385,6 +537,108 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
     }
 #undef QLSKUM_FLUX
     QLSKUM_LAUNCHED(L);
+}
+
+// ---------------------------------------------------- batched launchers
+
+template <typename K> static int persistent_grid(K kernel, int block, int ntiles)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    const int g = sms * (per_sm > 0 ? per_sm : 1);
+    return g < ntiles ? g : (ntiles > 0 ? ntiles : 1);
+}
+
+#define QLSKUM_TILE_SWITCH(TS, ...)                                                            \
+    switch (TS) {                                                                              \
+    case 64: { constexpr int T_ = 64; __VA_ARGS__; } break;                                    \
+    case 256: { constexpr int T_ = 256; __VA_ARGS__; } break;                                  \
+    default: { constexpr int T_ = 128; __VA_ARGS__; } break;                                   \
+    }
+
+void batch_derived(const Launch &L, const BatchView &B, int tile, const double4_32a *prim, float4 *q, float *cs)
+{
+    QLSKUM_TILE_SWITCH(tile, {
+        const int g = persistent_grid(kb_derived<T_>, T_, B.ntiles[tile_index(T_)]);
+        kb_derived<T_><<<g, T_, 0, L.stream>>>(B.cases, B.tiles[tile_index(T_)], B.ntiles[tile_index(T_)], prim, q, cs);
+    })
+    QLSKUM_LAUNCHED(L);
+}
+
+void batch_q_derivatives(const Launch &L, const BatchView &B, int tile, const float4 *q, float4 *dq, float4 *qm,
+                         const float *cs, float *delta, float cfl)
+{
+    QLSKUM_TILE_SWITCH(tile, {
+        const int ti = tile_index(T_);
+        if (B.unit_w) {
+            const int g = persistent_grid(kb_q_derivatives<T_, true>, T_, B.ntiles[ti]);
+            kb_q_derivatives<T_, true><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq, qm,
+                                                               cs, delta, cfl);
+        } else {
+            const int g = persistent_grid(kb_q_derivatives<T_, false>, T_, B.ntiles[ti]);
+            kb_q_derivatives<T_, false><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq,
+                                                                qm, cs, delta, cfl);
+        }
+    })
+    QLSKUM_LAUNCHED(L);
+}
+
+void batch_q_inner(const Launch &L, const BatchView &B, int tile, const float4 *q, const float4 *dq_in,
+                   float4 *dq_out)
+{
+    QLSKUM_TILE_SWITCH(tile, {
+        const int ti = tile_index(T_);
+        if (B.unit_w) {
+            const int g = persistent_grid(kb_q_inner<T_, true>, T_, B.ntiles[ti]);
+            kb_q_inner<T_, true><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq_in, dq_out);
+        } else {
+            const int g = persistent_grid(kb_q_inner<T_, false>, T_, B.ntiles[ti]);
+            kb_q_inner<T_, false><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq_in,
+                                                          dq_out);
+        }
+    })
+    QLSKUM_LAUNCHED(L);
+}
+
+// flux variants as for the single case: (tile, min blocks) = (128,4) (128,5) (64,8) (256,2)
+void batch_flux_update(const Launch &L, const BatchView &B, int variant, const float4 *q, const float4 *dq,
+                       const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
+                       double4_32a *prim_next, float4 *q_next, float *cs_next, int rk, double *psum, double *pmax)
+{
+#define QLSKUM_BFLUX(T_, MB)                                                                                     \
+    {                                                                                                            \
+        const int ti = tile_index(T_);                                                                           \
+        if (B.unit_w) {                                                                                          \
+            const int g = persistent_grid(kb_flux_update<T_, MB, true>, T_, B.ntiles[ti]);                      \
+            kb_flux_update<T_, MB, true><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, \
+                                                                 dq, qm, delta, prim, prim_old, prim_next,        \
+                                                                 q_next, cs_next, rk, psum, pmax);                \
+        } else {                                                                                                 \
+            const int g = persistent_grid(kb_flux_update<T_, MB, false>, T_, B.ntiles[ti]);                     \
+            kb_flux_update<T_, MB, false><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti],  \
+                                                                  q, dq, qm, delta, prim, prim_old, prim_next,    \
+                                                                  q_next, cs_next, rk, psum, pmax);               \
+        }                                                                                                        \
+    }
+    switch (variant) {
+    case 1: QLSKUM_BFLUX(128, 5); break;
+    case 2: QLSKUM_BFLUX(64, 8); break;
+    case 3: QLSKUM_BFLUX(256, 2); break;
+    default: QLSKUM_BFLUX(128, 4); break;
+    }
+#undef QLSKUM_BFLUX
+    QLSKUM_LAUNCHED(L);
+}
+
+void batch_reduce(const Launch &L, const BatchView &B, int flux_tile, const double *psum, const double *pmax,
+                  int *iter, double *res_old, double *res_new, double *hist, int capacity, int *status)
+{
+    kb_reduce<<<B.ncases, 256, 0, L.stream>>>(B.cases, B.ncases, tile_index(flux_tile), psum, pmax, iter, res_old,
+                                              res_new, hist, capacity, status);
+    kb_count<<<1, 1, 0, L.stream>>>(iter);
+    if (L.launches) *L.launches += 2;
 }
 
 }  // namespace mixed

@@ -93,6 +93,18 @@ def load(build_if_needed: bool = True):
         "qlskum_stream": (C.c_void_p, [H]),
         "qlskum_launch_count": (C.c_longlong, [H]),
         "qlskum_get_launch_config": (i, [H, ip, ip, ip]),
+        "qlskum_batch_create": (i, [C.POINTER(CloudStruct), i, ip, dp, dp, i, C.POINTER(ParamsStruct), C.POINTER(H)]),
+        "qlskum_batch_destroy": (i, [H]),
+        "qlskum_batch_last_error": (C.c_char_p, [H]),
+        "qlskum_batch_run": (i, [H, i]),
+        "qlskum_batch_objective": (i, [H, dp, dp, dp, dp]),
+        "qlskum_batch_get_prim": (i, [H, i, dp]),
+        "qlskum_batch_residual_history": (i, [H, dp, i, ip]),
+        "qlskum_batch_total_points": (C.c_longlong, [H]),
+        "qlskum_batch_launch_count": (C.c_longlong, [H]),
+        "qlskum_batch_stream": (C.c_void_p, [H]),
+        "qlskum_batch_tuning": (i, [H, ip, ip, ip, ip]),
+        "qlskum_state_update_noalloc": (i, [i, i, C.c_double, C.c_double] + [C.c_void_p] * 7),
         "qlskum_set_kernel_timing": (i, [H, i]),
         "qlskum_get_kernel_timing": (i, [H, i, dp, C.POINTER(C.c_longlong)]),
     }
@@ -253,3 +265,87 @@ class Solver:
     @property
     def stream(self) -> int:
         return int(self._L.qlskum_stream(self._h) or 0)
+
+
+class Batch:
+    """Many flight conditions over many clouds in one set of persistent,
+    graph-captured launches (mixed precision).  cases: list of
+    (cloud index, mach, aoa)."""
+
+    def __init__(self, clouds, cases, cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=3, block_size=0):
+        L = load()
+        self._L = L
+        structs, self._keep = [], []
+        for c in clouds:
+            s, keep = cloud_struct(c)
+            structs.append(s)
+            self._keep.append(keep)
+        arr = (CloudStruct * len(structs))(*structs)
+        self._arr = arr
+        cc = np.ascontiguousarray([int(c[0]) for c in cases], np.int32)
+        mm = np.ascontiguousarray([float(c[1]) for c in cases], np.float64)
+        aa = np.ascontiguousarray([float(c[2]) for c in cases], np.float64)
+        p = ParamsStruct(0.0, 0.0, cfl, vl_const, power, inner_iterations, MIXED, block_size, 1, 0)
+        h = C.c_void_p()
+        st = L.qlskum_batch_create(arr, len(structs), _ip(cc), _dp(mm), _dp(aa), len(cases), C.byref(p),
+                                   C.byref(h))
+        if st != 0:
+            raise QlskumError(st, L.qlskum_batch_last_error(None).decode())
+        self._h = h
+        self.cases = list(cases)
+        self.sizes = [clouds[int(c[0])].n for c in cases]
+
+    def _ck(self, st):
+        if st != 0:
+            raise QlskumError(st, self._L.qlskum_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.qlskum_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, iters):
+        self._ck(self._L.qlskum_batch_run(self._h, int(iters)))
+
+    def objective(self):
+        n = len(self.cases)
+        out = [np.empty(n) for _ in range(4)]
+        self._ck(self._L.qlskum_batch_objective(self._h, *[_dp(o) for o in out]))
+        return out
+
+    def prim(self, case):
+        out = np.empty((self.sizes[case], 4))
+        self._ck(self._L.qlskum_batch_get_prim(self._h, int(case), _dp(out)))
+        return out
+
+    def residual_history(self):
+        rows = C.c_int()
+        self._ck(self._L.qlskum_batch_residual_history(self._h, None, 0, C.byref(rows)))
+        out = np.empty((rows.value, len(self.cases)))
+        if rows.value:
+            self._ck(self._L.qlskum_batch_residual_history(self._h, _dp(out), rows.value, C.byref(rows)))
+        return out
+
+    @property
+    def total_points(self) -> int:
+        return int(self._L.qlskum_batch_total_points(self._h))
+
+    @property
+    def launches(self) -> int:
+        return int(self._L.qlskum_batch_launch_count(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(self._L.qlskum_batch_stream(self._h) or 0)
+
+    def tuning(self) -> dict:
+        v = [C.c_int() for _ in range(4)]
+        self._ck(self._L.qlskum_batch_tuning(self._h, *[C.byref(t) for t in v]))
+        return {"tile": v[0].value, "flux_tile": v[1].value, "flux_min_blocks": v[2].value,
+                "points_per_warp": v[3].value}

@@ -174,6 +174,41 @@ enum { QLSKUM_KERNEL_GRADIENT = 0, QLSKUM_KERNEL_INNER = 1, QLSKUM_KERNEL_FLUX_U
 qlskum_status qlskum_set_kernel_timing(qlskum_handle *h, int enable);
 qlskum_status qlskum_get_kernel_timing(qlskum_handle *h, int kernel, double *ms_total, long long *launches);
 
+/* ------------------------------------------------------- batched launches */
+
+/* Many flight conditions over many clouds of uneven size, solved together:
+ * every kernel of an iteration is one persistent launch over all cases
+ * (tiles of one case, walked by a grid sized to the GPU), each iteration's
+ * four SSPRK stages are captured once per buffer phase as a CUDA graph and
+ * replayed, and the tile size and the register / occupancy shape of the flux
+ * kernel are picked by timing the candidates on the batch (autotuner).  The
+ * q-LSKUM iteration per case is fpi_solver_mod.h:14-151 in the mixed
+ * precision form (params->precision must be QLSKUM_MIXED).
+ * Case c solves cloud case_cloud[c] at Mach case_mach[c], AoA case_aoa[c]
+ * (degrees); cfl, vl_const, power and inner_iterations come from params. */
+typedef struct qlskum_batch qlskum_batch;
+qlskum_status qlskum_batch_create(const qlskum_cloud *clouds, int n_clouds, const int *case_cloud,
+                                  const double *case_mach, const double *case_aoa, int n_cases,
+                                  const qlskum_params *params, qlskum_batch **out);
+qlskum_status qlskum_batch_destroy(qlskum_batch *b);
+const char *qlskum_batch_last_error(const qlskum_batch *b);
+/* `iters` iterations of every case. */
+qlskum_status qlskum_batch_run(qlskum_batch *b, int iters);
+/* Per-case Cl, Cd, Cm and total entropy ([n_cases] each; any may be NULL). */
+qlskum_status qlskum_batch_objective(qlskum_batch *b, double *cl, double *cd, double *cm, double *entropy);
+/* prim of one case, [n][4] in its cloud's original point order. */
+qlskum_status qlskum_batch_get_prim(qlskum_batch *b, int case_index, double *out);
+/* res_new of every case per completed iteration: out [rows][n_cases]. */
+qlskum_status qlskum_batch_residual_history(qlskum_batch *b, double *out, int max_rows, int *rows);
+long long qlskum_batch_total_points(const qlskum_batch *b);
+long long qlskum_batch_launch_count(const qlskum_batch *b);
+void *qlskum_batch_stream(qlskum_batch *b);
+/* The autotuned launch shape: points per tile of the gradient / inner-loop
+ * kernels, points per tile and minimum resident blocks per SM of the flux
+ * kernel, points per warp (one thread per point: 32). */
+qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_tile, int *flux_min_blocks,
+                                  int *points_per_warp);
+
 /* ------------------------------------------- stage update without allocation */
 
 /* One SSPRK stage update (the arithmetic of qlskum_state_update) over device

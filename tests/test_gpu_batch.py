@@ -1,0 +1,79 @@
+"""Batched launches: several flight conditions over clouds of different size
+in one set of persistent, graph-captured kernels.  Each case must give what a
+single-case mixed-precision solve of the same cloud and condition gives: the
+per-point arithmetic is the same code, so the state is bit-identical; only
+the order of the residual sums differs."""
+import numpy as np
+import pytest
+
+from conftest import golden_cloud, small_cloud
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def qlskum():
+    import qlskum as q
+    q.load()
+    return q
+
+
+def _clouds():
+    return [golden_cloud("cloud_trans"),
+            small_cloud(n_wall=48, n_layers=24, first_spacing=5e-3, radius=3.0, seed=5, m=0.03, p=0.4, t=0.14)]
+
+
+CASES = [(0, 0.63, 2.0), (1, 0.70, 3.0), (0, 0.80, -1.0), (1, 0.55, 0.5), (0, 0.85, 1.0)]
+KW = dict(cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=1)
+
+
+def test_batch_matches_single_case_solves(qlskum):
+    clouds = _clouds()
+    b = qlskum.Batch(clouds, CASES, **KW)
+    assert b.total_points == sum(clouds[c].n for c, _, _ in CASES)
+    b.run(8)
+    cl, cd, cm, ent = b.objective()
+    hist = b.residual_history()
+    assert hist.shape == (8, len(CASES))
+    for k, (ci, mach, aoa) in enumerate(CASES):
+        s = qlskum.Solver(clouds[ci], mach=mach, aoa=aoa, precision=qlskum.MIXED, **KW)
+        s.q_lskum(8)
+        assert np.array_equal(b.prim(k), s.prim), k
+        np.testing.assert_allclose(hist[:, k], s.residual_history()[:, 0], rtol=1e-12)
+        np.testing.assert_allclose([cl[k], cd[k], cm[k], ent[k]], s.objective(), rtol=1e-12)
+
+
+def test_batch_tuning_and_graph_replay(qlskum):
+    clouds = _clouds()
+    b = qlskum.Batch(clouds, CASES[:3], **KW)
+    b.run(2)
+    t = b.tuning()
+    assert t["tile"] in (64, 128, 256) and t["flux_tile"] in (64, 128, 256) and t["points_per_warp"] == 32
+    l0 = b.launches
+    b.run(3)
+    # per iteration: 4 x (gradient + 1 inner + flux) + reduce + counter
+    assert b.launches - l0 == 3 * (4 * 3 + 2)
+    fixed = qlskum.Batch(clouds, CASES[:3], block_size=128, **KW)
+    fixed.run(5)
+    for k in range(3):
+        assert np.array_equal(b.prim(k), fixed.prim(k))
+
+
+def test_batch_rejects_fp64_and_bad_case(qlskum):
+    import ctypes as C
+    L = qlskum.load()
+    clouds = _clouds()
+    s, keep = qlskum.cloud_struct(clouds[0])
+    arr = (qlskum.CloudStruct * 1)(s)
+    cc = np.array([1], np.int32)
+    mm = np.array([0.6])
+    aa = np.array([1.0])
+    p = qlskum.ParamsStruct(0, 0, 0.2, 50, 0, 1, qlskum.MIXED, 0, 1, 0)
+    h = C.c_void_p()
+    assert L.qlskum_batch_create(arr, 1, qlskum._ip(cc), qlskum._dp(mm), qlskum._dp(aa), 1, C.byref(p),
+                                 C.byref(h)) == 1
+    cc[0] = 0
+    p.precision = qlskum.FP64
+    assert L.qlskum_batch_create(arr, 1, qlskum._ip(cc), qlskum._dp(mm), qlskum._dp(aa), 1, C.byref(p),
+                                 C.byref(h)) == 5
+    _ = keep
