@@ -321,6 +321,8 @@ def main():
     ap.add_argument("--workload", default="transonic", choices=sorted(WORKLOADS) + ["batch"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--adjoint-iters", type=int, default=3,
+                    help="iterations differentiated by the adjoint timing on the FP64 handle (0: skip)")
     args = ap.parse_args()
     rank, world, local = dist_env()
 
@@ -392,6 +394,25 @@ def main():
                "mixed_over_fp64": mixed_value / fp64_value,
                "after_iterations": args.warmup + args.steps,
                "cl": cl, "cd": cd, "abs_dcl": abs(cl - cl2), "abs_dcd": abs(cd - cd2)}
+
+    # discrete adjoint on the FP64 handle: dCl/dMach, dCl/dAoA through K
+    # iterations from the free stream (checkpointed primal + reverse sweep),
+    # against the same K primal iterations; host-synchronous calls, wall clock
+    adjoint = None
+    if args.adjoint_iters > 0:
+        sf = s2 if other == qlskum.FP64 else solver
+        k = args.adjoint_iters
+        sf.adjoint_gradient("cl", iters=k)          # first call allocates
+        t0 = time.perf_counter()
+        g = sf.adjoint_gradient("cl", iters=k)
+        t_adj = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        sf.q_lskum(k)
+        sf.synchronize()
+        t_pr = time.perf_counter() - t0
+        adjoint = {"objective": "cl", "iterations": k, "points": cloud.n, "seconds": t_adj,
+                   "primal_seconds": t_pr, "adjoint_over_primal": t_adj / t_pr,
+                   "point_iter_s": cloud.n * k / t_adj, "dcl_dmach": g["dmach"], "dcl_daoa_per_deg": g["daoa"]}
     del s2
 
     # end to end through the C ABI with host buffers
@@ -418,7 +439,7 @@ def main():
             "clocks": clocks.summary(), "gpu_launches": launches,
             "e2e": {"value": e2e_v, "unit": "point-iter/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "roofline": roofline, "cpu_baseline": cpu, "fp64_vs_mixed": compare,
+            "roofline": roofline, "cpu_baseline": cpu, "fp64_vs_mixed": compare, "adjoint": adjoint,
             "kernel_ms_per_iteration": {k: v[0] / max(1, 2) for k, v in kt.items()},
             "launch_config": solver.launch_config(),
         }

@@ -1,0 +1,588 @@
+// Discrete adjoint (reverse mode) of the FP64 q-LSKUM iteration.
+//
+// The reverse of one pseudo-time iteration (fpi_solver_mod.h:14-151) runs
+// stage by stage from the last: the SSPRK update, the flux residual (limiter,
+// reconstruction, split fluxes, least-squares solves), the inner-loop
+// gradients, the least-squares gradient and neighbour min / max, the q
+// variables, and finally the local time step.  The forward stage states it
+// needs are recomputed by the FP64 forward kernels from the iteration's
+// checkpointed state.  One thread per point; a point's contributions to its
+// neighbours' adjoints are scattered with FP64 atomics (the bar of a
+// neighbour's q, dq, qm, or wave speed).
+//
+// With GEO the kernels also accumulate the adjoints of the geometry each
+// launch reads (edge vectors, rotated edge vectors, edge lengths, normals,
+// least-squares moments) for the wall-displacement gradient, which the host
+// finishes (qlskum_host.cpp).
+#include "qlskum_adjoint.cuh"
+
+namespace qlskum {
+namespace adjk {
+
+using adj::KinBar;
+
+static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
+
+__device__ __forceinline__ void atomic_add4(double4_32a *p, const double v[4])
+{
+    double *d = reinterpret_cast<double *>(p);
+    atomicAdd(d + 0, v[0]);
+    atomicAdd(d + 1, v[1]);
+    atomicAdd(d + 2, v[2]);
+    atomicAdd(d + 3, v[3]);
+}
+
+// Reverse of the SSPRK update of every point (stage rk).  bP holds the bar of
+// the stage output on entry and is overwritten with the bar of the stage
+// input; bPold (stage 3) and bF receive their bars; bn / buinf the normal's
+// and the free stream's (GEO / parameters).
+__global__ void k_update(AdjView a, CaseConst K, const double4_32a *__restrict__ Pin,
+                         const double4_32a *__restrict__ Pold, const double4_32a *__restrict__ Pout, int rk,
+                         double4_32a *__restrict__ bP, double4_32a *__restrict__ bPold, double4_32a *__restrict__ bF,
+                         double *__restrict__ buinf)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double bu1 = 0.0, bu2 = 0.0;
+    if (i < a.c.n) {
+        const int f = a.c.flag[i];
+        const double2 nn = a.c.nrm[i];
+        double pin[4], pold[4], pout[4], bout[4], bin[4] = {0, 0, 0, 0}, bo[4] = {0, 0, 0, 0}, bf[4] = {0, 0, 0, 0};
+        ld4(Pin[i], pin);
+        ld4(Pold[i], pold);
+        ld4(Pout[i], pout);
+        ld4(bP[i], bout);
+        double bnx = 0.0, bny = 0.0;
+        adj::stage_update_vjp(K, f, nn.x, nn.y, pin, pold, pout, rk, bout, bin, bo, bf, bnx, bny, bu1, bu2);
+        bP[i] = mk4(bin);
+        bF[i] = mk4(bf);
+        if (rk == 3) {
+            double acc[4];
+            ld4(bPold[i], acc);
+            for (int r = 0; r < 4; r++) acc[r] += bo[r];
+            bPold[i] = mk4(acc);
+        }
+        if (a.bnrm) {
+            a.bnrm[i].x += bnx;
+            a.bnrm[i].y += bny;
+        }
+    }
+    // free-stream bars: warp sums, one atomic per warp
+    for (int o = 16; o > 0; o >>= 1) {
+        bu1 += __shfl_down_sync(0xffffffffu, bu1, o);
+        bu2 += __shfl_down_sync(0xffffffffu, bu2, o);
+    }
+    if ((threadIdx.x & 31) == 0 && (bu1 != 0.0 || bu2 != 0.0)) {
+        atomicAdd(buinf, bu1);
+        atomicAdd(buinf + 1, bu2);
+    }
+}
+
+// Reverse of the flux residual of every point: F_i = s delta_i sum_d G_d.
+// Adds the bars of q, dq, qm (own and neighbours'), of delta, and (GEO) of the
+// edge geometry, the normal and the directional moments.
+template <bool GEO>
+__global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__restrict__ q,
+                                               const double4_32a *__restrict__ dq, const double4_32a *__restrict__ qm,
+                                               const double *__restrict__ delta, const double4_32a *__restrict__ bF,
+                                               double4_32a *__restrict__ bq, double4_32a *__restrict__ bdq,
+                                               double4_32a *__restrict__ bqm, double *__restrict__ bdelta)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.c.n) return;
+    const DevCloud &c = a.c;
+    const int f = c.flag[i];
+    const double2 nn = c.nrm[i];
+    const double nx = nn.x, ny = nn.y;
+    double qi[4], dxi[4], dyi[4], mxi[4], mni[4];
+    ld4(q[i], qi);
+    ld4(dq[2 * i], dxi);
+    ld4(dq[2 * i + 1], dyi);
+    ld4(qm[2 * i], mxi);
+    ld4(qm[2 * i + 1], mni);
+    const double e2i = c.eps2[i];
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    const double scale = (f == kWall) ? 2.0 : 1.0;
+    const bool used[4] = {true, true, f != kWall, f != kOuter};
+
+    // forward: the directional sums (for the bars of delta and of the moments)
+    double sx[4][4], sy[4][4];
+    for (int d = 0; d < 4; d++)
+        for (int r = 0; r < 4; r++) sx[d][r] = sy[d][r] = 0.0;
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const double4_32a g = c.e_geo[e];
+        const double2 sw = c.e_sn[e];
+        const unsigned dir = c.e_dir[e];
+        double qk[4], dxk[4], dyk[4], mxk[4], mnk[4], Pi[4], Pk[4];
+        ld4(q[k], qk);
+        ld4(dq[2 * k], dxk);
+        ld4(dq[2 * k + 1], dyk);
+        ld4(qm[2 * k], mxk);
+        ld4(qm[2 * k + 1], mnk);
+        edge_states<double>(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, c.eps2[k], Pi, Pk);
+        Kin<double> ki, kk;
+        kin_prep<double>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
+        kin_prep<double>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
+#define QLSKUM_FWD(D)                                                                \
+        if (dir & (1u << D)) {                                                       \
+            double Gi[4], Gk[4];                                                     \
+            dir_flux<double, D>(f, ki, Gi);                                          \
+            dir_flux<double, D>(f, kk, Gk);                                          \
+            for (int r = 0; r < 4; r++) {                                            \
+                sx[D][r] += (Gk[r] - Gi[r]) * sw.x;                                  \
+                sy[D][r] += (Gk[r] - Gi[r]) * sw.y;                                  \
+            }                                                                        \
+        }
+        QLSKUM_FWD(0)
+        QLSKUM_FWD(1)
+        QLSKUM_FWD(2)
+        QLSKUM_FWD(3)
+#undef QLSKUM_FWD
+    }
+    double bFi[4];
+    ld4(bF[i], bFi);
+    const double dl = delta[i];
+    // bars of the directional sums
+    double bsx[4][4], bsy[4][4];
+    double bdl = 0.0;
+    for (int d = 0; d < 4; d++) {
+        const double4_32a m = c.fgeo[4 * i + d];
+        double bm[4] = {0, 0, 0, 0};
+        for (int r = 0; r < 4; r++) {
+            bsx[d][r] = bsy[d][r] = 0.0;
+            if (!used[d]) continue;
+            const double bG = scale * dl * bFi[r];
+            if (d < 2) {
+                const double G = (sx[d][r] * m.y - sy[d][r] * m.z) * m.w;
+                bdl += scale * bFi[r] * G;
+                bsx[d][r] = bG * m.y * m.w;
+                bsy[d][r] = -bG * m.z * m.w;
+                bm[1] += bG * sx[d][r] * m.w;
+                bm[2] -= bG * sy[d][r] * m.w;
+                bm[3] += bG * (sx[d][r] * m.y - sy[d][r] * m.z);
+            } else {
+                const double G = (sy[d][r] * m.x - sx[d][r] * m.z) * m.w;
+                bdl += scale * bFi[r] * G;
+                bsy[d][r] = bG * m.x * m.w;
+                bsx[d][r] = -bG * m.z * m.w;
+                bm[0] += bG * sy[d][r] * m.w;
+                bm[2] -= bG * sx[d][r] * m.w;
+                bm[3] += bG * (sy[d][r] * m.x - sx[d][r] * m.z);
+            }
+        }
+        if (GEO) {
+            double4_32a &acc = a.bfmom[4 * i + d];
+            acc.x += bm[0];
+            acc.y += bm[1];
+            acc.z += bm[2];
+            acc.w += bm[3];
+        }
+    }
+    bdelta[i] += bdl;
+
+    // reverse over the edges
+    double bqi[4] = {0, 0, 0, 0}, bdxi[4] = {0, 0, 0, 0}, bdyi[4] = {0, 0, 0, 0}, bmxi[4] = {0, 0, 0, 0},
+           bmni[4] = {0, 0, 0, 0};
+    double bnx = 0.0, bny = 0.0;
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const double4_32a g = c.e_geo[e];
+        const double2 sw = c.e_sn[e];
+        const unsigned dir = c.e_dir[e];
+        double qk[4], dxk[4], dyk[4], mxk[4], mnk[4], Pi[4], Pk[4];
+        ld4(q[k], qk);
+        ld4(dq[2 * k], dxk);
+        ld4(dq[2 * k + 1], dyk);
+        ld4(qm[2 * k], mxk);
+        ld4(qm[2 * k + 1], mnk);
+        edge_states<double>(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, c.eps2[k], Pi, Pk);
+        Kin<double> ki, kk;
+        kin_prep<double>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
+        kin_prep<double>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
+        KinBar kbi, kbk;
+        double bsw_x = 0.0, bsw_y = 0.0;
+#define QLSKUM_REV(D)                                                                \
+        if (dir & (1u << D)) {                                                       \
+            double bGk[4], bGi[4];                                                   \
+            for (int r = 0; r < 4; r++) {                                            \
+                bGk[r] = bsx[D][r] * sw.x + bsy[D][r] * sw.y;                        \
+                bGi[r] = -bGk[r];                                                    \
+            }                                                                        \
+            adj::dir_flux_vjp<D>(f, kk, bGk, kbk);                                   \
+            adj::dir_flux_vjp<D>(f, ki, bGi, kbi);                                   \
+            if (GEO) {                                                               \
+                double Gi[4], Gk[4];                                                 \
+                dir_flux<double, D>(f, ki, Gi);                                      \
+                dir_flux<double, D>(f, kk, Gk);                                      \
+                for (int r = 0; r < 4; r++) {                                        \
+                    bsw_x += bsx[D][r] * (Gk[r] - Gi[r]);                            \
+                    bsw_y += bsy[D][r] * (Gk[r] - Gi[r]);                            \
+                }                                                                    \
+            }                                                                        \
+        }
+        QLSKUM_REV(0)
+        QLSKUM_REV(1)
+        QLSKUM_REV(2)
+        QLSKUM_REV(3)
+#undef QLSKUM_REV
+        double bPi[4] = {0, 0, 0, 0}, bPk[4] = {0, 0, 0, 0};
+        adj::kin_vjp(nx, ny, Pi, ki, kbi, bPi, bnx, bny);
+        adj::kin_vjp(nx, ny, Pk, kk, kbk, bPk, bnx, bny);
+        // qtilde_to_prim outputs are (u1, u2, rho, p) in the edge_states order P = (rho, u1, u2, p)
+        double ti[4], tk[4];
+        for (int r = 0; r < 4; r++) {
+            const double gi = g.x * dxi[r] + g.y * dyi[r];
+            const double gk = g.x * dxk[r] + g.y * dyk[r];
+            const double phi_i = venkat(qi[r] - 0.5 * gi, qi[r], mxi[r], mni[r], e2i);
+            const double phi_k = venkat(qk[r] - 0.5 * gk, qk[r], mxk[r], mnk[r], c.eps2[k]);
+            ti[r] = qi[r] - 0.5 * phi_i * gi;
+            tk[r] = qk[r] - 0.5 * phi_k * gk;
+        }
+        double bti[4] = {0, 0, 0, 0}, btk[4] = {0, 0, 0, 0};
+        adj::qtilde_to_prim_vjp(ti, bPi, bti);
+        adj::qtilde_to_prim_vjp(tk, bPk, btk);
+        double bdelx = 0.0, bdely = 0.0;
+        adj::edge_end_vjp(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, bti, bqi, bdxi, bdyi, bmxi, bmni, bdelx, bdely);
+        double bqk[4] = {0, 0, 0, 0}, bdxk[4] = {0, 0, 0, 0}, bdyk[4] = {0, 0, 0, 0}, bmxk[4] = {0, 0, 0, 0},
+               bmnk[4] = {0, 0, 0, 0};
+        adj::edge_end_vjp(g.x, g.y, qk, dxk, dyk, mxk, mnk, c.eps2[k], btk, bqk, bdxk, bdyk, bmxk, bmnk, bdelx,
+                          bdely);
+        atomic_add4(bq + k, bqk);
+        atomic_add4(bdq + 2 * k, bdxk);
+        atomic_add4(bdq + 2 * k + 1, bdyk);
+        atomic_add4(bqm + 2 * k, bmxk);
+        atomic_add4(bqm + 2 * k + 1, bmnk);
+        if (GEO) {
+            double4_32a &ge = a.bedge[e];
+            ge.x += bdelx;
+            ge.y += bdely;
+            ge.z += bsw_x;
+            ge.w += bsw_y;
+        }
+    }
+    atomic_add4(bq + i, bqi);
+    atomic_add4(bdq + 2 * i, bdxi);
+    atomic_add4(bdq + 2 * i + 1, bdyi);
+    atomic_add4(bqm + 2 * i, bmxi);
+    atomic_add4(bqm + 2 * i + 1, bmni);
+    if (GEO && a.bnrm) {
+        a.bnrm[i].x += bnx;
+        a.bnrm[i].y += bny;
+    }
+}
+
+// Reverse of one inner iteration (q_variables_mod.h:120-213): bdq_out is the
+// bar of its output; adds bars of q and of its input dq.
+template <bool GEO>
+__global__ void k_inner(AdjView a, const double4_32a *__restrict__ q, const double4_32a *__restrict__ dq_in,
+                        const double4_32a *__restrict__ bdq_out, double4_32a *__restrict__ bq,
+                        double4_32a *__restrict__ bdq_in)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.c.n) return;
+    const DevCloud &c = a.c;
+    const double4_32a m = c.ggeo[i];
+    double bx[4], by[4];
+    ld4(bdq_out[2 * i], bx);
+    ld4(bdq_out[2 * i + 1], by);
+    double bsdx[4], bsdy[4];
+    for (int r = 0; r < 4; r++) {
+        bsdx[r] = m.w * (bx[r] * m.y - by[r] * m.z);
+        bsdy[r] = m.w * (by[r] * m.x - bx[r] * m.z);
+    }
+    double qi[4], dxi[4], dyi[4];
+    ld4(q[i], qi);
+    ld4(dq_in[2 * i], dxi);
+    ld4(dq_in[2 * i + 1], dyi);
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    double sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    double bqi[4] = {0, 0, 0, 0}, bdxi[4] = {0, 0, 0, 0}, bdyi[4] = {0, 0, 0, 0};
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const double4_32a g = c.e_geo[e];
+        double qk[4], dxk[4], dyk[4];
+        ld4(q[k], qk);
+        ld4(dq_in[2 * k], dxk);
+        ld4(dq_in[2 * k + 1], dyk);
+        double bqk[4], bdxk[4], bdyk[4];
+        double bgx = 0.0, bgy = 0.0, bwx = 0.0, bwy = 0.0;
+        for (int r = 0; r < 4; r++) {
+            const double t1 = qi[r] - 0.5 * (g.x * dxi[r] + g.y * dyi[r]);
+            const double t2 = qk[r] - 0.5 * (g.x * dxk[r] + g.y * dyk[r]);
+            sdx[r] += g.z * (t2 - t1);
+            sdy[r] += g.w * (t2 - t1);
+            const double bt = g.z * bsdx[r] + g.w * bsdy[r];
+            bqk[r] = bt;
+            bdxk[r] = -0.5 * g.x * bt;
+            bdyk[r] = -0.5 * g.y * bt;
+            bqi[r] -= bt;
+            bdxi[r] += 0.5 * g.x * bt;
+            bdyi[r] += 0.5 * g.y * bt;
+            if (GEO) {
+                bwx += bsdx[r] * (t2 - t1);
+                bwy += bsdy[r] * (t2 - t1);
+                bgx += -0.5 * bt * (dxk[r] - dxi[r]);
+                bgy += -0.5 * bt * (dyk[r] - dyi[r]);
+            }
+        }
+        atomic_add4(bq + k, bqk);
+        atomic_add4(bdq_in + 2 * k, bdxk);
+        atomic_add4(bdq_in + 2 * k + 1, bdyk);
+        if (GEO) {
+            // unit weights: w delx == delx
+            double4_32a &ge = a.bedge[e];
+            ge.x += bgx + bwx;
+            ge.y += bgy + bwy;
+        }
+    }
+    atomic_add4(bq + i, bqi);
+    atomic_add4(bdq_in + 2 * i, bdxi);
+    atomic_add4(bdq_in + 2 * i + 1, bdyi);
+    if (GEO) {
+        double bm[4] = {0, 0, 0, 0};
+        for (int r = 0; r < 4; r++) {
+            // dx = ood (Sx syy - Sy sxy), dy = ood (Sy sxx - Sx sxy)
+            bm[1] += m.w * bx[r] * sdx[r];
+            bm[2] += -m.w * (bx[r] * sdy[r] + by[r] * sdx[r]);
+            bm[0] += m.w * by[r] * sdy[r];
+            bm[3] += bx[r] * (sdx[r] * m.y - sdy[r] * m.z) + by[r] * (sdy[r] * m.x - sdx[r] * m.z);
+        }
+        double4_32a &acc = a.bgmom[i];
+        acc.x += bm[0];
+        acc.y += bm[1];
+        acc.z += bm[2];
+        acc.w += bm[3];
+    }
+}
+
+// Reverse of the least-squares gradient and of the neighbour max / min
+// (q_variables_mod.h:36-118).
+template <bool GEO>
+__global__ void k_grad(AdjView a, const double4_32a *__restrict__ q, const double4_32a *__restrict__ bdq,
+                       const double4_32a *__restrict__ bqm, double4_32a *__restrict__ bq)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.c.n) return;
+    const DevCloud &c = a.c;
+    const double4_32a m = c.ggeo[i];
+    double bx[4], by[4], bmax[4], bmin[4];
+    ld4(bdq[2 * i], bx);
+    ld4(bdq[2 * i + 1], by);
+    ld4(bqm[2 * i], bmax);
+    ld4(bqm[2 * i + 1], bmin);
+    double bsdx[4], bsdy[4];
+    for (int r = 0; r < 4; r++) {
+        bsdx[r] = (bx[r] * m.y - by[r] * m.z) * m.w;
+        bsdy[r] = (by[r] * m.x - bx[r] * m.z) * m.w;
+    }
+    double qi[4];
+    ld4(q[i], qi);
+    double qmax[4], qmin[4];
+    int amax[4], amin[4];
+    for (int r = 0; r < 4; r++) {
+        qmax[r] = qmin[r] = qi[r];
+        amax[r] = amin[r] = i;
+    }
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    double sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    double bqi[4] = {0, 0, 0, 0};
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const double4_32a g = c.e_geo[e];
+        double qk[4], bqk[4];
+        ld4(q[k], qk);
+        double bwx = 0.0, bwy = 0.0;
+        for (int r = 0; r < 4; r++) {
+            if (qk[r] > qmax[r]) { qmax[r] = qk[r]; amax[r] = k; }
+            if (qk[r] < qmin[r]) { qmin[r] = qk[r]; amin[r] = k; }
+            sdx[r] += g.z * (qk[r] - qi[r]);
+            sdy[r] += g.w * (qk[r] - qi[r]);
+            const double bt = g.z * bsdx[r] + g.w * bsdy[r];
+            bqk[r] = bt;
+            bqi[r] -= bt;
+            if (GEO) {
+                bwx += bsdx[r] * (qk[r] - qi[r]);
+                bwy += bsdy[r] * (qk[r] - qi[r]);
+            }
+        }
+        atomic_add4(bq + k, bqk);
+        if (GEO) {
+            double4_32a &ge = a.bedge[e];
+            ge.x += bwx;
+            ge.y += bwy;
+        }
+    }
+    atomic_add4(bq + i, bqi);
+    double *bqd = reinterpret_cast<double *>(bq);
+    for (int r = 0; r < 4; r++) {
+        if (bmax[r] != 0.0) atomicAdd(bqd + 4 * (size_t)amax[r] + r, bmax[r]);
+        if (bmin[r] != 0.0) atomicAdd(bqd + 4 * (size_t)amin[r] + r, bmin[r]);
+    }
+    if (GEO) {
+        double bm[4] = {0, 0, 0, 0};
+        for (int r = 0; r < 4; r++) {
+            bm[1] += m.w * bx[r] * sdx[r];
+            bm[2] += -m.w * (bx[r] * sdy[r] + by[r] * sdx[r]);
+            bm[0] += m.w * by[r] * sdy[r];
+            bm[3] += bx[r] * (sdx[r] * m.y - sdy[r] * m.z) + by[r] * (sdy[r] * m.x - sdx[r] * m.z);
+        }
+        double4_32a &acc = a.bgmom[i];
+        acc.x += bm[0];
+        acc.y += bm[1];
+        acc.z += bm[2];
+        acc.w += bm[3];
+    }
+}
+
+// bP += (dq/dP)^T bq  (q_variables_mod.h:19-33)
+__global__ void k_q(int n, const double4_32a *__restrict__ P, const double4_32a *__restrict__ bq,
+                    double4_32a *__restrict__ bP)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double p[4], b[4], acc[4];
+    ld4(P[i], p);
+    ld4(bq[i], b);
+    ld4(bP[i], acc);
+    adj::prim_to_q_vjp(p, b, acc);
+    bP[i] = mk4(acc);
+}
+
+// Reverse of the local time step (state_update_mod.h:448-496): the bar of
+// delta_i goes to the wave speed of the neighbour that set the minimum.
+template <bool GEO>
+__global__ void k_delta(AdjView a, const double4_32a *__restrict__ P, const double *__restrict__ bdelta,
+                        double cfl, double *__restrict__ bc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.c.n) return;
+    const DevCloud &c = a.c;
+    double min_delt = 1.0;
+    int arg = -1;
+    long long earg = -1;
+    double carg = 0.0;
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        double p[4];
+        ld4(P[k], p);
+        const double ck = wave_speed(p);
+        double dt = c.e_dist[e] / ck;
+        dt = cfl * dt;
+        if (min_delt > dt) {
+            min_delt = dt;
+            arg = k;
+            earg = e;
+            carg = ck;
+        }
+    }
+    if (arg >= 0 && bdelta[i] != 0.0) {
+        atomicAdd(bc + arg, -bdelta[i] * cfl * c.e_dist[earg] / (carg * carg));
+        if (GEO) a.bdist[earg] += bdelta[i] * cfl / carg;
+    }
+}
+
+__global__ void k_wave(int n, const double4_32a *__restrict__ P, const double *__restrict__ bc,
+                       double4_32a *__restrict__ bP)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || bc[i] == 0.0) return;
+    double p[4], acc[4];
+    ld4(P[i], p);
+    ld4(bP[i], acc);
+    adj::wave_speed_vjp(p, bc[i], acc);
+    bP[i] = mk4(acc);
+}
+
+// bP = the bar of Cl (which = 0) or Cd (which = 1) w.r.t. the wall pressures
+// (compute_force_coeffs_mod.h:37-67), added to the shape points' entries.
+__global__ void k_objective(AdjView a, const int *__restrict__ wall_perm, const double4_32a *__restrict__ wall_geo,
+                            int n_wall, double cp_scale, double theta, int which, double4_32a *__restrict__ bP)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_wall) return;
+    const int m = wall_perm[t];
+    const double ds = wall_geo[t].x;
+    const double2 nn = a.c.nrm[m];
+    // Cl = V cos - H sin, Cd = H cos + V sin; H = sum cp nx ds, V = sum cp ny ds, cp = -(p - p_inf) / cp_scale
+    const double bH = which == 0 ? -sin(theta) : cos(theta);
+    const double bV = which == 0 ? cos(theta) : sin(theta);
+    bP[m].w += -(bH * nn.x + bV * nn.y) * ds / cp_scale;
+}
+
+}  // namespace adjk
+
+// ------------------------------------------------------------- launchers
+
+namespace adjl {
+
+void update(const Launch &L, const AdjView &a, const CaseConst &K, const double4_32a *Pin, const double4_32a *Pold,
+            const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, double4_32a *bF, double *buinf)
+{
+    adjk::k_update<<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, K, Pin, Pold, Pout, rk, bP, bPold, bF, buinf);
+}
+
+void flux(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
+          const double *delta, const double4_32a *bF, double4_32a *bq, double4_32a *bdq, double4_32a *bqm,
+          double *bdelta)
+{
+    if (a.bedge)
+        adjk::k_flux<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, bF, bq, bdq, bqm,
+                                                                             bdelta);
+    else
+        adjk::k_flux<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, bF, bq, bdq, bqm,
+                                                                              bdelta);
+}
+
+void inner(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq_in,
+           const double4_32a *bdq_out, double4_32a *bq, double4_32a *bdq_in)
+{
+    if (a.bedge)
+        adjk::k_inner<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq_in, bdq_out, bq, bdq_in);
+    else
+        adjk::k_inner<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq_in, bdq_out, bq, bdq_in);
+}
+
+void grad(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *bdq, const double4_32a *bqm,
+          double4_32a *bq)
+{
+    if (a.bedge)
+        adjk::k_grad<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, bdq, bqm, bq);
+    else
+        adjk::k_grad<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, bdq, bqm, bq);
+}
+
+void qvars(const Launch &L, int n, const double4_32a *P, const double4_32a *bq, double4_32a *bP)
+{
+    adjk::k_q<<<adjk::grid_for(n, 256), 256, 0, L.stream>>>(n, P, bq, bP);
+}
+
+void delta(const Launch &L, const AdjView &a, const double4_32a *P, const double *bdelta, double cfl, double *bc,
+           double4_32a *bP)
+{
+    if (a.bdist)
+        adjk::k_delta<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, P, bdelta, cfl, bc);
+    else
+        adjk::k_delta<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, P, bdelta, cfl, bc);
+    adjk::k_wave<<<adjk::grid_for(a.c.n, 256), 256, 0, L.stream>>>(a.c.n, P, bc, bP);
+}
+
+void objective(const Launch &L, const AdjView &a, const int *wall_perm, const double4_32a *wall_geo, int n_wall,
+               double cp_scale, double theta, int which, double4_32a *bP)
+{
+    if (n_wall > 0)
+        adjk::k_objective<<<adjk::grid_for(n_wall, 128), 128, 0, L.stream>>>(a, wall_perm, wall_geo, n_wall, cp_scale,
+                                                                            theta, which, bP);
+}
+
+}  // namespace adjl
+}  // namespace qlskum

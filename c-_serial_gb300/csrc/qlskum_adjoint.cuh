@@ -1,0 +1,340 @@
+// Reverse mode (vector-Jacobian products) of the per-point and per-edge
+// arithmetic of qlskum_math.cuh, FP64, host + device.
+//
+// Each *_vjp function takes the forward inputs (it recomputes what it needs)
+// and the bar (adjoint) of the forward outputs, and ADDS the bars of the
+// inputs into the caller's accumulators.  Non-smooth points follow the
+// branch the forward pass took: the limiter's |dq-| <= 1e-5 and phi >= 1
+// cases have zero derivative, neighbour max / min and the local time step's
+// min pass the bar to the selected entry.  The derivatives are written out
+// by hand from the formulas of the reference (split_fluxes_mod.h,
+// quadrant_fluxes_mod.h, limiters_mod.h, q_variables_mod.h,
+// state_update_mod.h) and each is checked against central differences
+// (tests/test_adjoint_math.py).
+#pragma once
+#include "qlskum_math.cuh"
+
+namespace qlskum {
+namespace adj {
+
+// q_variables_mod.h:19-33
+QLSKUM_HD void prim_to_q_vjp(const double P[4], const double bq[4], double bP[4])
+{
+    const double rho = P[0], u1 = P[1], u2 = P[2], p = P[3];
+    const double beta = 0.5 * rho / p;
+    const double usq = u1 * u1 + u2 * u2;
+    const double bbeta = bq[0] * (2.5 / beta - usq) + bq[1] * 2.0 * u1 + bq[2] * 2.0 * u2 - 2.0 * bq[3];
+    bP[0] += bq[0] / rho + bbeta * 0.5 / p;
+    bP[1] += -bq[0] * 2.0 * beta * u1 + bq[1] * 2.0 * beta;
+    bP[2] += -bq[0] * 2.0 * beta * u2 + bq[2] * 2.0 * beta;
+    bP[3] += -bbeta * beta / p;
+}
+
+// limiters_mod.h:64-104 for one component.
+QLSKUM_HD void venkat_vjp(double qt, double q, double qmax, double qmin, double eps2, double bphi, double &bqt,
+                          double &bq, double &bqmax, double &bqmin)
+{
+    const double dn = qt - q;
+    if (fabs(dn) <= 10e-6) return;
+    const bool up = dn > 0;
+    const double dp = (up ? qmax : qmin) - q;
+    const double num = (dp * dp + eps2) * dn + 2.0 * dn * dn * dp;
+    const double den = (dp * dp + 2.0 * dn * dn + dn * dp + eps2) * dn;
+    const double t = num / den;
+    if (!(t < 1.0)) return;
+    const double bnum = bphi / den, bden = -bphi * t / den;
+    const double bdn = bnum * (dp * dp + eps2 + 4.0 * dn * dp) +
+                       bden * ((dp * dp + 2.0 * dn * dn + dn * dp + eps2) + dn * (4.0 * dn + dp));
+    const double bdp = bnum * (2.0 * dp * dn + 2.0 * dn * dn) + bden * (dn * (2.0 * dp + dn));
+    bqt += bdn;
+    bq -= bdn + bdp;
+    if (up) bqmax += bdp;
+    else bqmin += bdp;
+}
+
+// q_variables_mod.h:230-253; P = (rho, u1, u2, p).
+QLSKUM_HD void qtilde_to_prim_vjp(const double qt[4], const double bP[4], double bqt[4])
+{
+    const double gm1 = 1.4 - 1.0;
+    const double beta = -qt[3] * 0.5;
+    const double t = 0.5 / beta;
+    const double u1 = qt[1] * t, u2 = qt[2] * t;
+    const double T1 = qt[0] + beta * (u1 * u1 + u2 * u2);
+    const double rho = exp(T1 - log(beta) / gm1);
+    const double brho = bP[0] + bP[3] * t;
+    const double bT2 = brho * rho, bT1 = bT2;
+    const double bu1 = bP[1] + bT1 * 2.0 * beta * u1;
+    const double bu2 = bP[2] + bT1 * 2.0 * beta * u2;
+    const double bt = bP[3] * rho + bu1 * qt[1] + bu2 * qt[2];
+    const double bbeta = bT1 * (u1 * u1 + u2 * u2) - bT2 / (gm1 * beta) - bt * 0.5 / (beta * beta);
+    bqt[0] += bT1;
+    bqt[1] += bu1 * t;
+    bqt[2] += bu2 * t;
+    bqt[3] += -0.5 * bbeta;
+}
+
+// Bars of the fields of Kin<double>.
+struct KinBar {
+    double rho = 0, ut = 0, un = 0, pbr = 0, usq = 0, B1 = 0, B2 = 0, E1 = 0, E2 = 0;
+};
+
+// kin_prep (split_fluxes_mod.h:14-26): bars of (u1, u2, rho, p) and of the normal.
+QLSKUM_HD void kin_vjp(double nx, double ny, const double P[4], const Kin<double> &k, const KinBar &kb, double bP[4],
+                       double &bnx, double &bny)
+{
+    const double rho = P[0], u1 = P[1], u2 = P[2], p = P[3];
+    const double beta = 0.5 * rho / p;
+    const double sb = sqrt(beta);
+    const double S1 = k.ut * sb, S2 = k.un * sb;
+    const double two_over_sqrtpi = 1.1283791670955126;
+    double but = kb.ut + 2.0 * k.ut * kb.usq;
+    double bun = kb.un + 2.0 * k.un * kb.usq;
+    const double bS1 = kb.E1 * two_over_sqrtpi * exp(-S1 * S1) + kb.B1 * k.B1 * (-2.0 * S1);
+    const double bS2 = kb.E2 * two_over_sqrtpi * exp(-S2 * S2) + kb.B2 * k.B2 * (-2.0 * S2);
+    but += bS1 * sb;
+    bun += bS2 * sb;
+    const double bsb = bS1 * k.ut + bS2 * k.un;
+    const double bbeta = bsb * 0.5 / sb - (kb.B1 * k.B1 + kb.B2 * k.B2) * 0.5 / beta;
+    bP[0] += kb.rho + bbeta * 0.5 / p - kb.pbr * p / (rho * rho);
+    bP[3] += -bbeta * beta / p + kb.pbr / rho;
+    bP[1] += but * ny + bun * nx;
+    bP[2] += -but * nx + bun * ny;
+    bnx += -but * u2 + bun * u1;
+    bny += but * u1 + bun * u2;
+}
+
+// flux_Gxp / flux_Gxn
+QLSKUM_HD void flux_x_vjp(const Kin<double> &k, double s1, const double bG[4], KinBar &kb)
+{
+    const double A1 = 0.5 * (1.0 + s1 * k.E1), B1s = s1 * k.B1;
+    const double ut = k.ut, un = k.un, pbr = k.pbr, usq = k.usq, rho = k.rho;
+    const double a0 = ut * A1 + B1s, a1 = (pbr + ut * ut) * A1 + ut * B1s, a2 = ut * un * A1 + un * B1s;
+    const double a3 = 0.5 * ut * (7.0 * pbr + usq) * A1 + 0.5 * (6.0 * pbr + usq) * B1s;
+    kb.rho += bG[0] * a0 + bG[1] * a1 + bG[2] * a2 + bG[3] * a3;
+    const double b0 = rho * bG[0], b1 = rho * bG[1], b2 = rho * bG[2], b3 = rho * bG[3];
+    const double bA1 = b0 * ut + b1 * (pbr + ut * ut) + b2 * ut * un + b3 * 0.5 * ut * (7.0 * pbr + usq);
+    const double bB1s = b0 + b1 * ut + b2 * un + b3 * 0.5 * (6.0 * pbr + usq);
+    kb.ut += b0 * A1 + b1 * (2.0 * ut * A1 + B1s) + b2 * un * A1 + b3 * 0.5 * (7.0 * pbr + usq) * A1;
+    kb.un += b2 * (ut * A1 + B1s);
+    kb.pbr += b1 * A1 + b3 * (3.5 * ut * A1 + 3.0 * B1s);
+    kb.usq += b3 * (0.5 * ut * A1 + 0.5 * B1s);
+    kb.E1 += 0.5 * s1 * bA1;
+    kb.B1 += s1 * bB1s;
+}
+
+// flux_Gyp / flux_Gyn
+QLSKUM_HD void flux_y_vjp(const Kin<double> &k, double s2, const double bG[4], KinBar &kb)
+{
+    const double A2 = 0.5 * (1.0 + s2 * k.E2), B2s = s2 * k.B2;
+    const double ut = k.ut, un = k.un, pbr = k.pbr, usq = k.usq, rho = k.rho;
+    const double a0 = un * A2 + B2s, a2 = (pbr + un * un) * A2 + un * B2s, a1 = ut * un * A2 + ut * B2s;
+    const double a3 = 0.5 * un * (7.0 * pbr + usq) * A2 + 0.5 * (6.0 * pbr + usq) * B2s;
+    kb.rho += bG[0] * a0 + bG[1] * a1 + bG[2] * a2 + bG[3] * a3;
+    const double b0 = rho * bG[0], b1 = rho * bG[1], b2 = rho * bG[2], b3 = rho * bG[3];
+    const double bA2 = b0 * un + b2 * (pbr + un * un) + b1 * ut * un + b3 * 0.5 * un * (7.0 * pbr + usq);
+    const double bB2s = b0 + b2 * un + b1 * ut + b3 * 0.5 * (6.0 * pbr + usq);
+    kb.un += b0 * A2 + b2 * (2.0 * un * A2 + B2s) + b1 * ut * A2 + b3 * 0.5 * (7.0 * pbr + usq) * A2;
+    kb.ut += b1 * (un * A2 + B2s);
+    kb.pbr += b2 * A2 + b3 * (3.5 * un * A2 + 3.0 * B2s);
+    kb.usq += b3 * (0.5 * un * A2 + 0.5 * B2s);
+    kb.E2 += 0.5 * s2 * bA2;
+    kb.B2 += s2 * bB2s;
+}
+
+// flux_quad_GxI..IV
+QLSKUM_HD void flux_quad_vjp(const Kin<double> &k, double s1, double s2, const double bG[4], KinBar &kb)
+{
+    const double ut = k.ut, un = k.un, pbr = k.pbr, usq = k.usq, rho = k.rho;
+    const double A1 = 0.5 * (1.0 + s1 * k.E1), A2 = 0.5 * (1.0 + s2 * k.E2), B1s = s1 * k.B1;
+    const double f1 = ut * A1 + B1s;
+    const double h = (pbr + ut * ut) * A1 + ut * B1s;
+    const double m = un * A2 + s2 * k.B2;
+    const double t2 = 0.5 * ut * (7.0 * pbr + usq) * A1, t3 = 0.5 * k.B1 * (6.0 * pbr + usq);
+    const double bt4 = s2 * bG[3];
+    kb.rho += bG[0] * A2 * f1 + bG[1] * A2 * h + bG[2] * f1 * m + bG[3] * A2 * (t2 + s1 * t3) +
+              bt4 * 0.5 * un * k.B2 * f1;
+    double bA2 = rho * (bG[0] * f1 + bG[1] * h + bG[3] * (t2 + s1 * t3));
+    double bf1 = rho * (bG[0] * A2 + bG[2] * m) + bt4 * 0.5 * rho * un * k.B2;
+    const double bh = rho * A2 * bG[1];
+    const double bm = rho * f1 * bG[2];
+    const double bt2 = rho * A2 * bG[3], bt3 = rho * A2 * s1 * bG[3];
+    kb.un += bt4 * 0.5 * rho * k.B2 * f1 + bm * A2;
+    kb.B2 += bt4 * 0.5 * rho * un * f1 + bm * s2;
+    bA2 += bm * un;
+    kb.pbr += bh * A1 + bt2 * 3.5 * ut * A1 + bt3 * 3.0 * k.B1;
+    kb.ut += bh * (2.0 * ut * A1 + B1s) + bf1 * A1 + bt2 * 0.5 * (7.0 * pbr + usq) * A1;
+    double bA1 = bh * (pbr + ut * ut) + bf1 * ut + bt2 * 0.5 * ut * (7.0 * pbr + usq);
+    const double bB1s = bh * ut + bf1;
+    kb.usq += bt2 * 0.5 * ut * A1 + bt3 * 0.5 * k.B1;
+    kb.B1 += bt3 * 0.5 * (6.0 * pbr + usq) + s1 * bB1s;
+    kb.E1 += 0.5 * s1 * bA1;
+    kb.E2 += 0.5 * s2 * bA2;
+}
+
+template <int D> QLSKUM_HD void dir_flux_vjp(int f, const Kin<double> &k, const double bG[4], KinBar &kb)
+{
+    if (D <= 1) {
+        const double s1 = (D == 0) ? 1.0 : -1.0;
+        if (f == kInterior) flux_x_vjp(k, s1, bG, kb);
+        else flux_quad_vjp(k, s1, (f == kOuter) ? 1.0 : -1.0, bG, kb);
+    } else {
+        flux_y_vjp(k, (D == 2) ? 1.0 : -1.0, bG, kb);
+    }
+}
+
+// Reconstruction of one edge end (interior_fluxes_mod.h:72-83) for all four
+// components: q~ = q - 0.5 phi(q - 0.5 g) g with g = delx dqx + dely dqy.
+// Adds bars of q, dq (x, y), qm (max, min) and of the edge vector.
+QLSKUM_HD void edge_end_vjp(double delx, double dely, const double q[4], const double dx[4], const double dy[4],
+                            const double mx[4], const double mn[4], double e2, const double bqt[4], double bq[4],
+                            double bdx[4], double bdy[4], double bmx[4], double bmn[4], double &bdelx, double &bdely)
+{
+    for (int r = 0; r < 4; r++) {
+        const double g = delx * dx[r] + dely * dy[r];
+        const double qtu = q[r] - 0.5 * g;
+        const double phi = venkat(qtu, q[r], mx[r], mn[r], e2);
+        bq[r] += bqt[r];
+        const double bphi = -0.5 * g * bqt[r];
+        double bg = -0.5 * phi * bqt[r];
+        double bqtu = 0.0;
+        venkat_vjp(qtu, q[r], mx[r], mn[r], e2, bphi, bqtu, bq[r], bmx[r], bmn[r]);
+        bq[r] += bqtu;
+        bg += -0.5 * bqtu;
+        bdx[r] += bg * delx;
+        bdy[r] += bg * dely;
+        bdelx += bg * dx[r];
+        bdely += bg * dy[r];
+    }
+}
+
+// primitive_to_conserved (state_update_mod.h:18-33)
+QLSKUM_HD void p2c_vjp(const double P[4], double nx, double ny, const double bU[4], double bP[4], double &bnx,
+                       double &bny)
+{
+    const double rho = P[0], t1 = rho * P[1], t2 = rho * P[2];
+    const double bt1 = bU[3] * t1 / rho + bU[1] * ny + bU[2] * nx;
+    const double bt2 = bU[3] * t2 / rho - bU[1] * nx + bU[2] * ny;
+    bP[0] += bU[0] - bU[3] * 0.5 * (t1 * t1 + t2 * t2) / (rho * rho) + bt1 * P[1] + bt2 * P[2];
+    bP[1] += bt1 * rho;
+    bP[2] += bt2 * rho;
+    bP[3] += 2.5 * bU[3];
+    bnx += -bU[1] * t2 + bU[2] * t1;
+    bny += bU[1] * t1 + bU[2] * t2;
+}
+
+// conserved_vector_Ubar (state_update_mod.h:35-90): bars of the point's
+// state, of the normal and of the free-stream velocity (u1_inf, u2_inf).
+QLSKUM_HD void ubar_vjp(const CaseConst &K, const double P[4], double nx, double ny, const double bU[4], double bP[4],
+                        double &bnx, double &bny, double &bu1i, double &bu2i)
+{
+    const double g1 = K.gamma - 1.0, pi = K.pi, rhoi = K.rho_inf, pri = K.pr_inf;
+    const double tx = ny, ty = -nx;
+    const double inv_sqrtpi = 0.5641895835477563;
+    // free-stream half
+    const double u1ri = K.u1_inf * tx + K.u2_inf * ty, u2ri = K.u1_inf * nx + K.u2_inf * ny;
+    const double einf = pri / (rhoi * g1) + 0.5 * (u1ri * u1ri + u2ri * u2ri);
+    const double bi = (0.5 * rhoi) / pri, sbi = sqrt(bi);
+    const double Si = u2ri * sbi;
+    const double Bi = exp(-Si * Si) / (2.0 * sqrt(pi * bi));
+    const double Ai = 0.5 * (1.0 - erf(Si));
+    const double bAi = bU[0] * rhoi + bU[1] * rhoi * u1ri + bU[2] * rhoi * u2ri + bU[3] * rhoi * einf;
+    const double bBi = -bU[2] * rhoi - bU[3] * 0.5 * rhoi * u2ri;
+    const double bei = bU[3] * rhoi * Ai;
+    const double bSi = -bAi * inv_sqrtpi * exp(-Si * Si) + bBi * Bi * (-2.0 * Si);
+    const double bu1ri = bU[1] * rhoi * Ai + bei * u1ri;
+    const double bu2ri = bU[2] * rhoi * Ai - bU[3] * 0.5 * rhoi * Bi + bei * u2ri + bSi * sbi;
+    bu1i += bu1ri * tx + bu2ri * nx;
+    bu2i += bu1ri * ty + bu2ri * ny;
+    bnx += -bu1ri * K.u2_inf + bu2ri * K.u1_inf;
+    bny += bu1ri * K.u1_inf + bu2ri * K.u2_inf;
+    // the point's half
+    const double rho = P[0], u1 = P[1], u2 = P[2], p = P[3];
+    const double u1r = u1 * tx + u2 * ty, u2r = u1 * nx + u2 * ny;
+    const double e = p / (rho * g1) + 0.5 * (u1r * u1r + u2r * u2r);
+    const double beta = rho / (2.0 * p), sb = sqrt(beta);
+    const double S = u2r * sb;
+    const double B = exp(-S * S) / (2.0 * sqrt(pi * beta));
+    const double A = 0.5 * (1.0 + erf(S));
+    const double bA = bU[0] * rho + bU[1] * rho * u1r + bU[2] * rho * u2r + bU[3] * rho * e;
+    const double bB = bU[2] * rho + bU[3] * 0.5 * rho * u2r;
+    const double be = bU[3] * rho * A;
+    double brho = bU[0] * A + bU[1] * u1r * A + bU[2] * (u2r * A + B) + bU[3] * (A * e + 0.5 * u2r * B);
+    const double bS = bA * inv_sqrtpi * exp(-S * S) + bB * B * (-2.0 * S);
+    const double bu1r = bU[1] * rho * A + be * u1r;
+    const double bu2r = bU[2] * rho * A + bU[3] * 0.5 * rho * B + be * u2r + bS * sb;
+    const double bbeta = bS * u2r * 0.5 / sb - bB * B * 0.5 / beta;
+    double bp = be / (rho * g1);
+    brho += -be * p / (rho * rho * g1);
+    brho += bbeta / (2.0 * p);
+    bp += -bbeta * beta / p;
+    bP[0] += brho;
+    bP[1] += bu1r * tx + bu2r * nx;
+    bP[2] += bu1r * ty + bu2r * ny;
+    bP[3] += bp;
+    bnx += -bu1r * u2 + bu2r * u1;
+    bny += bu1r * u1 + bu2r * u2;
+}
+
+// One SSPRK stage of one point (state_update_mod.h:111-282) in reverse.
+// Pout is the stage's output state (it carries U' and 1/U'0).  Adds the bars
+// of the input state, of prim_old (stage 3), of the flux residual, of the
+// normal and of the free-stream velocity (outer points).
+QLSKUM_HD void stage_update_vjp(const CaseConst &K, int f, double nx, double ny, const double Pin[4],
+                                const double Pold[4], const double Pout[4], int rk, const double bPout[4],
+                                double bPin[4], double bPold[4], double bF[4], double &bnx, double &bny,
+                                double &bu1i, double &bu2i)
+{
+    const double obt = 1.0 / 3.0, tbt = 2.0 / 3.0;
+    const double U0 = Pout[0], inv = 1.0 / U0;
+    const double V1 = Pout[1] * U0, V2 = Pout[2] * U0;  // rotated-back momentum
+    double bU[4];
+    double binv = bPout[1] * V1 + bPout[2] * V2 - 0.2 * bPout[3] * (V1 * V1 + V2 * V2);
+    const double bV1 = bPout[1] * inv - 0.4 * bPout[3] * inv * V1;
+    const double bV2 = bPout[2] * inv - 0.4 * bPout[3] * inv * V2;
+    bU[0] = bPout[0] - binv * inv * inv;
+    bU[3] = 0.4 * bPout[3];
+    // V1 = U1 ny + U2 nx, V2 = U2 ny - U1 nx (U in the (t, n) frame)
+    bU[1] = bV1 * ny - bV2 * nx;
+    bU[2] = bV1 * nx + bV2 * ny;
+    // the frame of the output: U1 = V1 ny - V2 nx, U2 = V1 nx + V2 ny
+    const double U1 = V1 * ny - V2 * nx, U2 = V1 * nx + V2 * ny;
+    bny += bV1 * U1 + bV2 * U2;
+    bnx += bV1 * U2 - bV2 * U1;
+    if (f == kWall) bU[2] = 0.0;
+    double bUin[4], bUold[4];
+    for (int j = 0; j < 4; j++) {
+        if (rk != 3) {
+            bUin[j] = bU[j];
+            bF[j] += -0.5 * bU[j];
+            bUold[j] = 0.0;
+        } else {
+            bUold[j] = tbt * bU[j];
+            bUin[j] = obt * bU[j];
+            bF[j] += -0.5 * obt * bU[j];
+        }
+    }
+    if (f == kOuter) {
+        ubar_vjp(K, Pin, nx, ny, bUin, bPin, bnx, bny, bu1i, bu2i);
+        if (rk == 3) ubar_vjp(K, Pold, nx, ny, bUold, bPold, bnx, bny, bu1i, bu2i);
+    } else {
+        p2c_vjp(Pin, nx, ny, bUin, bPin, bnx, bny);
+        if (rk == 3) p2c_vjp(Pold, nx, ny, bUold, bPold, bnx, bny);
+    }
+}
+
+// |u| + 3 sqrt(p / rho) (state_update_mod.h:483-485)
+QLSKUM_HD void wave_speed_vjp(const double P[4], double bc, double bP[4])
+{
+    const double mod_u = sqrt(P[1] * P[1] + P[2] * P[2]);
+    if (mod_u > 0.0) {
+        bP[1] += bc * P[1] / mod_u;
+        bP[2] += bc * P[2] / mod_u;
+    }
+    const double a = P[3] / P[0], sa = sqrt(a);
+    const double ba = bc * 1.5 / sa;
+    bP[3] += ba / P[0];
+    bP[0] += -ba * P[3] / (P[0] * P[0]);
+}
+
+}  // namespace adj
+}  // namespace qlskum

@@ -352,6 +352,15 @@ __global__ void k_copy(int n, const double4_32a *__restrict__ src, double4_32a *
     if (i < n) dst[i] = src[i];
 }
 
+__global__ void k_add(int n, const double4_32a *__restrict__ src, double4_32a *__restrict__ dst)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const double4_32a a = src[i], b = dst[i];
+        dst[i] = make_double4_32a(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+    }
+}
+
 // compute_force_coeffs_mod.h:37-72 per shape point and compute_entropy_mod.h:
 // 17-21 per point; each block writes its partial sums of H, V, pitching
 // moment and entropy, k_objective_finish adds the partials in a fixed order.
@@ -484,6 +493,12 @@ void reduce_residual(const Launch &L, const Reduce &R, int n, int it)
 void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
 {
     k_copy<<<grid_for(n, 256), 256, 0, L.stream>>>(n, src, dst);
+    QLSKUM_LAUNCHED(L);
+}
+
+void add_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
+{
+    k_add<<<grid_for(n, 256), 256, 0, L.stream>>>(n, src, dst);
     QLSKUM_LAUNCHED(L);
 }
 

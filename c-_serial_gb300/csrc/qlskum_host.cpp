@@ -37,11 +37,11 @@ struct Precomp {
     std::vector<double> ggeo;      // [n][4]
     std::vector<double> fgeo;      // [n][4][4]
     std::vector<double> eps2;      // [n]
-    // drop what only the device upload needs (keeps normals and sub-stencils)
+    // drop what only the device upload needs (keeps normals, sub-stencils and
+    // their membership bits)
     void release_upload_data()
     {
         for (auto *v : {&geo, &sn, &dist, &ggeo, &fgeo, &eps2}) std::vector<double>().swap(*v);
-        std::vector<uint8_t>().swap(edge_dir);
     }
 };
 
@@ -124,6 +124,11 @@ struct qlskum_handle {
     // tune() on the first fused iteration unless params.block_size fixes it
     int flux_variant = 0;
     bool tuned = false;
+    // the cloud as given (original order), for the geometry part of the adjoint
+    std::vector<double> hx, hy;
+    std::vector<int> hleft, hright, hflag, hnbhs, hconn;
+    // discrete adjoint buffers, allocated on first use
+    struct AdjBuf *adj = nullptr;
     // per-kernel event timing (qlskum_set_kernel_timing)
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -762,6 +767,8 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
 
 }  // namespace
 
+void adj_free(qlskum_handle *h);
+
 // ======================================================================= C ABI
 
 extern "C" {
@@ -828,6 +835,13 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
         h->d_wall_perm = G.d_wall_perm;
         h->d_wall_geo = G.d_wall_geo;
     }
+    h->hx.assign(c->x, c->x + c->n);
+    h->hy.assign(c->y, c->y + c->n);
+    h->hleft.assign(c->left, c->left + c->n);
+    h->hright.assign(c->right, c->right + c->n);
+    h->hflag.assign(c->flag_1, c->flag_1 + c->n);
+    h->hnbhs.assign(c->nbhs, c->nbhs + c->n);
+    h->hconn.assign(c->conn, c->conn + (size_t)c->n * QLSKUM_MAX_NBHS);
     auto up = [&](auto *dptr, const auto &vec) {
         if (dptr && !vec.empty())
             cudaMemcpyAsync(dptr, vec.data(), vec.size() * sizeof(vec[0]), cudaMemcpyHostToDevice, h->L.stream);
@@ -913,6 +927,7 @@ qlskum_status qlskum_destroy(qlskum_handle *h)
     }
     for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
     if (h->R.hist) cudaFree(h->R.hist);
+    adj_free(h);
     h->arena.release();
     if (h->L.stream) cudaStreamDestroy(h->L.stream);
     delete h;
@@ -1632,6 +1647,582 @@ qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_ti
     if (flux_tile) *flux_tile = kFluxTile[b->flux_variant];
     if (flux_min_blocks) *flux_min_blocks = kFluxMinB[b->flux_variant];
     if (points_per_warp) *points_per_warp = 32;
+    return QLSKUM_OK;
+}
+
+}  // extern "C"
+
+
+// ============================================================ discrete adjoint
+//
+// Reverse mode of the FP64 iteration (qlskum_adjoint.cu holds the kernels).
+// The stage states of an iteration are recomputed from its checkpointed
+// state by the FP64 module kernels, whose results equal the fused solver's
+// bit for bit; the reverse sweep then runs stage by stage from the last.
+
+struct AdjBuf {
+    DeviceArena arena;
+    int ni = 0;
+    bool geo = false;
+    size_t ne = 0;
+    double4_32a *P[5] = {};            // stage states of one iteration
+    double4_32a *q[4] = {};            // q of P[0 .. 3]
+    std::vector<double4_32a *> dq;     // [stage][inner step 0 .. ni], each [np][2]
+    double4_32a *qm[4] = {};
+    double *delta = nullptr;
+    double4_32a *flux = nullptr;
+    double4_32a *bP = nullptr, *bPacc = nullptr, *bF = nullptr, *bq = nullptr, *bdqA = nullptr, *bdqB = nullptr,
+                *bqm = nullptr, *lam = nullptr, *lam_prev = nullptr, *seed = nullptr;
+    double *bdelta = nullptr, *bc = nullptr, *buinf = nullptr;
+    // geometry adjoints (wall-displacement gradients only)
+    double4_32a *bedge = nullptr;
+    double *bdist = nullptr;
+    double2 *bnrm = nullptr;
+    double4_32a *bgmom = nullptr, *bfmom = nullptr;
+    // one state per iteration of the checkpointed primal
+    double4_32a *ckpt = nullptr;
+    int ckpt_cap = 0;
+};
+
+void adj_free(qlskum_handle *h)
+{
+    if (!h->adj) return;
+    if (h->adj->ckpt) cudaFree(h->adj->ckpt);
+    h->adj->arena.release();
+    delete h->adj;
+    h->adj = nullptr;
+}
+
+namespace {
+
+// Sliced-ELL slice bases of the handle's point order (as build_geometry lays
+// them out) and the edge-slot count.
+std::vector<long long> slice_bases(const qlskum_handle *h, size_t *ne)
+{
+    std::vector<long long> sb(h->nslices);
+    long long tot = 0;
+    for (int s2 = 0; s2 < h->nslices; s2++) {
+        int w = 0;
+        for (int l = 0; l < 32; l++) {
+            const int pp = s2 * 32 + l;
+            if (pp < h->n) w = std::max(w, h->hnbhs[h->iperm[pp]]);
+        }
+        sb[s2] = tot;
+        tot += 32LL * w;
+    }
+    if (ne) *ne = (size_t)std::max(tot, 32LL);
+    return sb;
+}
+
+qlskum_status d2h(qlskum_handle *h, void *dst, const void *src, size_t bytes)
+{
+    CK(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->L.stream));
+    CK(h, cudaStreamSynchronize(h->L.stream));
+    return QLSKUM_OK;
+}
+
+void zero(qlskum_handle *h, void *p, size_t bytes) { cudaMemsetAsync(p, 0, bytes, h->L.stream); }
+
+qlskum_status adj_alloc(qlskum_handle *h, bool geo)
+{
+    if (h->prm.precision != QLSKUM_FP64)
+        return fail(h, QLSKUM_ERR_UNSUPPORTED, "the discrete adjoint runs on FP64 handles");
+    if (h->adj && (h->adj->geo || !geo)) return QLSKUM_OK;
+    adj_free(h);
+    AdjBuf *a = new AdjBuf();
+    h->adj = a;
+    DeviceArena &A = a->arena;
+    const size_t np = h->np;
+    a->ni = h->prm.inner_iterations;
+    a->geo = geo;
+    for (auto &p : a->P) p = A.alloc<double4_32a>(np);
+    for (auto &p : a->q) p = A.alloc<double4_32a>(np);
+    for (auto &p : a->qm) p = A.alloc<double4_32a>(2 * np);
+    a->dq.resize(4 * (size_t)(a->ni + 1));
+    for (auto &p : a->dq) p = A.alloc<double4_32a>(2 * np);
+    a->delta = A.alloc<double>(np);
+    a->flux = A.alloc<double4_32a>(np);
+    for (auto *p : {&a->bP, &a->bPacc, &a->bF, &a->bq, &a->lam, &a->lam_prev, &a->seed})
+        *p = A.alloc<double4_32a>(np);
+    for (auto *p : {&a->bdqA, &a->bdqB, &a->bqm}) *p = A.alloc<double4_32a>(2 * np);
+    a->bdelta = A.alloc<double>(np);
+    a->bc = A.alloc<double>(np);
+    a->buinf = A.alloc<double>(2);
+    slice_bases(h, &a->ne);
+    if (geo) {
+        a->bedge = A.alloc<double4_32a>(a->ne);
+        a->bdist = A.alloc<double>(a->ne);
+        a->bnrm = A.alloc<double2>(np);
+        a->bgmom = A.alloc<double4_32a>(np);
+        a->bfmom = A.alloc<double4_32a>(4 * np);
+    }
+    if (A.err != cudaSuccess) {
+        qlskum_status st = fail(h, QLSKUM_ERR_CUDA, fmt("adjoint cudaMalloc: %s", cudaGetErrorString(A.err)));
+        adj_free(h);
+        return st;
+    }
+    // padding rows stay zero (and finite) in every buffer
+    for (auto *p : a->P) zero(h, p, sizeof(double4_32a) * np);
+    return QLSKUM_OK;
+}
+
+AdjView adj_view(qlskum_handle *h, bool geo)
+{
+    AdjView v;
+    v.c = h->dc;
+    AdjBuf *a = h->adj;
+    if (geo && a->geo) {
+        v.bedge = a->bedge;
+        v.bdist = a->bdist;
+        v.bnrm = a->bnrm;
+        v.bgmom = a->bgmom;
+        v.bfmom = a->bfmom;
+    }
+    return v;
+}
+
+void adj_zero_geometry(qlskum_handle *h)
+{
+    AdjBuf *a = h->adj;
+    zero(h, a->buinf, 2 * sizeof(double));
+    if (!a->geo) return;
+    const size_t np = h->np;
+    zero(h, a->bedge, sizeof(double4_32a) * a->ne);
+    zero(h, a->bdist, sizeof(double) * a->ne);
+    zero(h, a->bnrm, sizeof(double2) * np);
+    zero(h, a->bgmom, sizeof(double4_32a) * np);
+    zero(h, a->bfmom, sizeof(double4_32a) * 4 * np);
+}
+
+double4_32a *adj_dq(AdjBuf *a, int s, int j) { return a->dq[(size_t)s * (a->ni + 1) + j]; }
+
+// Stage s (0-based) from P[s]: q, the gradient and its inner-loop
+// corrections, the neighbour max / min and the flux residual (into a->flux)
+// (fpi_solver_mod.h:20-36).
+void adj_stage_forward(qlskum_handle *h, int s)
+{
+    AdjBuf *a = h->adj;
+    const DevCloud &c = h->dc;
+    fp64::q_variables(h->L, c, a->P[s], a->q[s]);
+    fp64::q_derivatives(h->L, c, a->q[s], adj_dq(a, s, 0), a->qm[s], nullptr, nullptr, 0.0);
+    for (int j = 1; j <= a->ni; j++) fp64::q_inner(h->L, c, a->q[s], adj_dq(a, s, j - 1), adj_dq(a, s, j));
+    fp64::flux_residual(h->L, c, a->q[s], adj_dq(a, s, a->ni), a->qm[s], a->delta, a->flux);
+}
+
+// The four stage states of one iteration from a->P[0] (fpi_solver_mod.h:14-40).
+void adj_iteration_forward(qlskum_handle *h)
+{
+    AdjBuf *a = h->adj;
+    fp64::func_delta(h->L, h->dc, a->P[0], a->delta, h->K.cfl);
+    for (int s = 0; s < 4; s++) {
+        adj_stage_forward(h, s);
+        fp64::copy_prim(h->L, h->n, a->P[s], a->P[s + 1]);
+        fp64::state_update(h->L, h->dc, h->K, a->P[s + 1], a->P[0], a->flux, s + 1, h->R);
+    }
+}
+
+// Reverse of stage s's residual chain for the bar in a->bF: adds to a->bP
+// (the bar of P[s]) and to a->bdelta.
+void adj_stage_reverse(qlskum_handle *h, int s, const AdjView &v)
+{
+    AdjBuf *a = h->adj;
+    const size_t np = h->np;
+    const int ni = a->ni;
+    zero(h, a->bq, sizeof(double4_32a) * np);
+    zero(h, a->bdqA, sizeof(double4_32a) * 2 * np);
+    zero(h, a->bqm, sizeof(double4_32a) * 2 * np);
+    adjl::flux(h->L, v, a->q[s], adj_dq(a, s, ni), a->qm[s], a->delta, a->bF, a->bq, a->bdqA, a->bqm, a->bdelta);
+    for (int j = ni; j >= 1; j--) {
+        zero(h, a->bdqB, sizeof(double4_32a) * 2 * np);
+        adjl::inner(h->L, v, a->q[s], adj_dq(a, s, j - 1), a->bdqA, a->bq, a->bdqB);
+        std::swap(a->bdqA, a->bdqB);
+    }
+    adjl::grad(h->L, v, a->q[s], a->bdqA, a->bqm, a->bq);
+    adjl::qvars(h->L, h->n, a->P[s], a->bq, a->bP);
+}
+
+// Reverse of one iteration after adj_iteration_forward: a->bP holds the bar of
+// P[4] on entry and the bar of P[0] on exit.  Free-stream bars add to
+// a->buinf, geometry bars to the view's accumulators.
+void adj_iteration_reverse(qlskum_handle *h, const AdjView &v)
+{
+    AdjBuf *a = h->adj;
+    const size_t np = h->np;
+    zero(h, a->bPacc, sizeof(double4_32a) * np);
+    zero(h, a->bdelta, sizeof(double) * np);
+    for (int s = 3; s >= 0; s--) {
+        adjl::update(h->L, v, h->K, a->P[s], a->P[0], a->P[s + 1], s + 1, a->bP, a->bPacc, a->bF, a->buinf);
+        adj_stage_reverse(h, s, v);
+    }
+    zero(h, a->bc, sizeof(double) * np);
+    adjl::delta(h->L, v, a->P[0], a->bdelta, h->K.cfl, a->bc, a->bPacc);
+    fp64::add_prim(h->L, h->n, a->bPacc, a->bP);
+}
+
+// Cl and Cd at `prim` (compute_force_coeffs_mod.h:37-67), and dJ/dprim of
+// objective `which` (0 Cl, 1 Cd) into `bP`.
+qlskum_status adj_seed(qlskum_handle *h, int which, const double4_32a *prim, double4_32a *bP, double *cl, double *cd)
+{
+    const double cp_scale = 0.5 * h->K.rho_inf * h->K.mach * h->K.mach;
+    fp64::objective(h->L, h->dc, prim, h->d_wall_perm, h->d_wall_geo, h->shape_points, cp_scale, h->K.pr_inf,
+                    h->K.gamma, h->d_entropy, h->d_obj, h->d_obj_partial);
+    zero(h, bP, sizeof(double4_32a) * h->np);
+    adjl::objective(h->L, adj_view(h, false), h->d_wall_perm, h->d_wall_geo, h->shape_points, cp_scale, h->K.theta,
+                    which, bP);
+    qlskum_status st = check_launch(h, "adjoint seed");
+    if (st) return st;
+    double o[4];
+    st = d2h(h, o, h->d_obj, sizeof o);
+    if (st) return st;
+    *cl = o[1] * std::cos(h->K.theta) - o[0] * std::sin(h->K.theta);
+    *cd = o[0] * std::cos(h->K.theta) + o[1] * std::sin(h->K.theta);
+    return QLSKUM_OK;
+}
+
+// dJ/dMach and dJ/dAoA (per degree).  The free stream (u1, u2) =
+// M (cos theta, sin theta) enters through the far-field states (bars in
+// buinf) and, for a run from the free stream, the initial state (bars in
+// binit); J itself scales with 1 / M^2 (cp) and rotates with theta:
+// dCl/dtheta = -Cd, dCd/dtheta = Cl.
+void adj_params(const qlskum_handle *h, int which, double cl, double cd, const double buinf[2],
+                const double binit[2], double *dmach, double *daoa)
+{
+    const double th = h->K.theta, M = h->K.mach;
+    const double b1 = buinf[0] + binit[0], b2 = buinf[1] + binit[1];
+    const double J = which == 0 ? cl : cd;
+    const double dM = -2.0 * J / M + b1 * std::cos(th) + b2 * std::sin(th);
+    const double dth = M * (-b1 * std::sin(th) + b2 * std::cos(th)) + (which == 0 ? -cd : cl);
+    if (dmach) *dmach = dM;
+    if (daoa) *daoa = dth * h->K.pi / 180.0;
+}
+
+// Reverse of the geometry (host, FP64).  The accumulated adjoints of the edge
+// vectors, rotated edge vectors, edge lengths, normals and least-squares
+// moments, and the objective's own geometry (panel lengths, normals), are
+// pulled back to the point coordinates, then projected on the unperturbed
+// wall normals of the shape points: x_m(s) = x_m + s n_m.  Unit weights
+// (power 0); the sub-stencil split and min_dist (the limiter's epsilon) are
+// held at their unperturbed values.
+qlskum_status adj_geometry(qlskum_handle *h, int which, const double4_32a *prim_dev, double *dJ_dwall)
+{
+    AdjBuf *a = h->adj;
+    const int n = h->n, NB = QLSKUM_MAX_NBHS;
+    const size_t np = h->np;
+    const std::vector<double> &X = h->hx, &Y = h->hy;
+    std::vector<double4_32a> bedge(a->ne), bgmom(np), bfmom(4 * np), prim(np);
+    std::vector<double> bdist(a->ne);
+    std::vector<double2> bnrm(np);
+    qlskum_status st;
+    if ((st = d2h(h, bedge.data(), a->bedge, sizeof(double4_32a) * a->ne))) return st;
+    if ((st = d2h(h, bdist.data(), a->bdist, sizeof(double) * a->ne))) return st;
+    if ((st = d2h(h, bnrm.data(), a->bnrm, sizeof(double2) * np))) return st;
+    if ((st = d2h(h, bgmom.data(), a->bgmom, sizeof(double4_32a) * np))) return st;
+    if ((st = d2h(h, bfmom.data(), a->bfmom, sizeof(double4_32a) * 4 * np))) return st;
+    if ((st = d2h(h, prim.data(), prim_dev, sizeof(double4_32a) * np))) return st;
+    const std::vector<long long> sbase = slice_bases(h, nullptr);
+    std::vector<double> bx(n, 0.0), by(n, 0.0), bnx(n, 0.0), bny(n, 0.0);
+    // (1/det) = 1 / (sxx syy - sxy^2): bars of the three sums from those of
+    // {sxx, syy, sxy, 1/det} as the kernels read them
+    auto mom_bar = [](double sxx, double syy, double sxy, const double4_32a &b, double &bxx, double &byy,
+                      double &bxy) {
+        bxx = b.x;
+        byy = b.y;
+        bxy = b.z;
+        if (b.w == 0.0) return;
+        const double ood = 1.0 / (sxx * syy - sxy * sxy);
+        const double bdet = -b.w * ood * ood;
+        bxx += bdet * syy;
+        byy += bdet * sxx;
+        bxy -= 2.0 * sxy * bdet;
+    };
+    std::vector<double> dx(NB), dy(NB), ds(NB), dn(NB);
+    for (int pp = 0; pp < n; pp++) {
+        const int i = h->iperm[pp];
+        const int nb = h->hnbhs[i];
+        const double nx = h->pc.nx[i], ny = h->pc.ny[i];
+        bnx[i] += bnrm[pp].x;
+        bny[i] += bnrm[pp].y;
+        double gxx = 0, gyy = 0, gxy = 0, fxx[4] = {0, 0, 0, 0}, fyy[4] = {0, 0, 0, 0}, fxy[4] = {0, 0, 0, 0};
+        for (int r = 0; r < nb; r++) {
+            const int k = h->hconn[(size_t)i * NB + r] - 1;
+            dx[r] = X[k] - X[i];
+            dy[r] = Y[k] - Y[i];
+            ds[r] = dx[r] * ny - dy[r] * nx;
+            dn[r] = dx[r] * nx + dy[r] * ny;
+            gxx += dx[r] * dx[r];
+            gyy += dy[r] * dy[r];
+            gxy += dx[r] * dy[r];
+            const unsigned bits = h->pc.edge_dir[(size_t)i * NB + r];
+            for (int d = 0; d < 4; d++)
+                if (bits & (1u << d)) {
+                    fxx[d] += ds[r] * ds[r];
+                    fyy[d] += dn[r] * dn[r];
+                    fxy[d] += ds[r] * dn[r];
+                }
+        }
+        double gbxx, gbyy, gbxy, fbxx[4], fbyy[4], fbxy[4];
+        mom_bar(gxx, gyy, gxy, bgmom[pp], gbxx, gbyy, gbxy);
+        for (int d = 0; d < 4; d++) mom_bar(fxx[d], fyy[d], fxy[d], bfmom[4 * (size_t)pp + d], fbxx[d], fbyy[d], fbxy[d]);
+        for (int r = 0; r < nb; r++) {
+            const size_t e = (size_t)(sbase[pp >> 5] + 32LL * r + (pp & 31));
+            const int k = h->hconn[(size_t)i * NB + r] - 1;
+            double bdx = bedge[e].x + 2.0 * dx[r] * gbxx + dy[r] * gbxy;
+            double bdy = bedge[e].y + 2.0 * dy[r] * gbyy + dx[r] * gbxy;
+            double bds = bedge[e].z, bdn = bedge[e].w;
+            const unsigned bits = h->pc.edge_dir[(size_t)i * NB + r];
+            for (int d = 0; d < 4; d++)
+                if (bits & (1u << d)) {
+                    bds += 2.0 * ds[r] * fbxx[d] + dn[r] * fbxy[d];
+                    bdn += 2.0 * dn[r] * fbyy[d] + ds[r] * fbxy[d];
+                }
+            // ds = dx ny - dy nx, dn = dx nx + dy ny
+            bdx += bds * ny + bdn * nx;
+            bdy += -bds * nx + bdn * ny;
+            bnx[i] += -bds * dy[r] + bdn * dx[r];
+            bny[i] += bds * dx[r] + bdn * dy[r];
+            if (bdist[e] != 0.0) {
+                const double dist = std::sqrt(dx[r] * dx[r] + dy[r] * dy[r]);
+                bdx += bdist[e] * dx[r] / dist;
+                bdy += bdist[e] * dy[r] / dist;
+            }
+            bx[k] += bdx;
+            bx[i] -= bdx;
+            by[k] += bdy;
+            by[i] -= bdy;
+        }
+    }
+    // the objective's geometry: H = sum cp nx ds, V = sum cp ny ds with
+    // ds = (|x_m - x_l| + |x_r - x_m|) / 2 (compute_force_coeffs_mod.h:37-59)
+    const double cp_scale = 0.5 * h->K.rho_inf * h->K.mach * h->K.mach;
+    const double th = h->K.theta;
+    const double bH = which == 0 ? -std::sin(th) : std::cos(th);
+    const double bV = which == 0 ? std::cos(th) : std::sin(th);
+    for (int m = 0; m < h->shape_points; m++) {
+        const int l = h->hleft[m] - 1, r = h->hright[m] - 1;
+        const double cp = -(prim[h->perm[m]].w - h->K.pr_inf) / cp_scale;
+        const double d1x = X[m] - X[l], d1y = Y[m] - Y[l], d2x = X[r] - X[m], d2y = Y[r] - Y[m];
+        const double ds1 = std::sqrt(d1x * d1x + d1y * d1y), ds2 = std::sqrt(d2x * d2x + d2y * d2y);
+        const double dsm = 0.5 * (ds1 + ds2);
+        bnx[m] += bH * cp * dsm;
+        bny[m] += bV * cp * dsm;
+        const double bds = cp * (bH * h->pc.nx[m] + bV * h->pc.ny[m]);
+        bx[m] += 0.5 * bds * (d1x / ds1 - d2x / ds2);
+        by[m] += 0.5 * bds * (d1y / ds1 - d2y / ds2);
+        bx[l] -= 0.5 * bds * d1x / ds1;
+        by[l] -= 0.5 * bds * d1y / ds1;
+        bx[r] += 0.5 * bds * d2x / ds2;
+        by[r] += 0.5 * bds * d2y / ds2;
+    }
+    // normals of wall and outer points: n = (-a, b) / |(a, b)| with
+    // a = (y_r - y_l) / 2, b = (x_r - x_l) / 2 (point_normals_mod.h:17-46)
+    for (int i = 0; i < n; i++) {
+        if (h->hflag[i] == kInterior || (bnx[i] == 0.0 && bny[i] == 0.0)) continue;
+        const int l = h->hleft[i] - 1, r = h->hright[i] - 1;
+        const double av = 0.5 * (Y[r] - Y[l]), bv = 0.5 * (X[r] - X[l]);
+        const double det = std::sqrt(av * av + bv * bv);
+        const double bdet = (bnx[i] * av - bny[i] * bv) / (det * det);
+        const double ba = -bnx[i] / det + bdet * av / det;
+        const double bb = bny[i] / det + bdet * bv / det;
+        by[r] += 0.5 * ba;
+        by[l] -= 0.5 * ba;
+        bx[r] += 0.5 * bb;
+        bx[l] -= 0.5 * bb;
+    }
+    for (int m = 0; m < h->shape_points; m++) dJ_dwall[m] = bx[m] * h->pc.nx[m] + by[m] * h->pc.ny[m];
+    return QLSKUM_OK;
+}
+
+qlskum_status upload_points(qlskum_handle *h, const double *src, double4_32a *dst, double pad)
+{
+    std::vector<double4_32a> dev(h->np, make_double4_32a(pad, 0, 0, pad));
+    for (int i = 0; i < h->n; i++)
+        dev[h->perm[i]] = make_double4_32a(src[4 * (size_t)i], src[4 * (size_t)i + 1], src[4 * (size_t)i + 2],
+                                           src[4 * (size_t)i + 3]);
+    CK(h, cudaMemcpyAsync(dst, dev.data(), sizeof(double4_32a) * h->np, cudaMemcpyHostToDevice, h->L.stream));
+    CK(h, cudaStreamSynchronize(h->L.stream));
+    return QLSKUM_OK;
+}
+
+qlskum_status download_points(qlskum_handle *h, const double4_32a *src, double *dst)
+{
+    std::vector<double4_32a> dev(h->np);
+    qlskum_status st = d2h(h, dev.data(), src, sizeof(double4_32a) * h->np);
+    if (st) return st;
+    for (int i = 0; i < h->n; i++) std::memcpy(dst + 4 * (size_t)i, &dev[h->perm[i]], sizeof(double4_32a));
+    return QLSKUM_OK;
+}
+
+qlskum_status adj_args(qlskum_handle *h, int objective, int count, const double *dJ_dwall)
+{
+    if (objective != QLSKUM_OBJECTIVE_CL && objective != QLSKUM_OBJECTIVE_CD)
+        return fail(h, QLSKUM_ERR_INVALID, fmt("unknown objective %d", objective));
+    if (count < 1) return fail(h, QLSKUM_ERR_INVALID, "iteration count must be >= 1");
+    if (dJ_dwall && h->prm.power != 0.0)
+        return fail(h, QLSKUM_ERR_UNSUPPORTED, "wall-displacement gradients need unit least-squares weights (power 0)");
+    return adj_alloc(h, dJ_dwall != nullptr);
+}
+
+}  // namespace
+
+extern "C" {
+
+qlskum_status qlskum_residual_forward(qlskum_handle *h, const double *prim, double *flux_res)
+{
+    NEED(h);
+    if (!prim || !flux_res) return fail(h, QLSKUM_ERR_INVALID, "null prim or flux_res");
+    qlskum_status st = adj_alloc(h, false);
+    if (st) return st;
+    AdjBuf *a = h->adj;
+    if ((st = upload_points(h, prim, a->P[0], 1.0))) return st;
+    fp64::func_delta(h->L, h->dc, a->P[0], a->delta, h->K.cfl);
+    adj_stage_forward(h, 0);
+    if ((st = check_launch(h, "residual_forward"))) return st;
+    return download_points(h, a->flux, flux_res);
+}
+
+qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const double *bar_flux_res, double *bar_prim)
+{
+    NEED(h);
+    if (!prim || !bar_flux_res || !bar_prim) return fail(h, QLSKUM_ERR_INVALID, "null argument");
+    qlskum_status st = adj_alloc(h, false);
+    if (st) return st;
+    AdjBuf *a = h->adj;
+    if ((st = upload_points(h, prim, a->P[0], 1.0))) return st;
+    if ((st = upload_points(h, bar_flux_res, a->bF, 0.0))) return st;
+    fp64::func_delta(h->L, h->dc, a->P[0], a->delta, h->K.cfl);
+    adj_stage_forward(h, 0);
+    const AdjView v = adj_view(h, false);
+    zero(h, a->bP, sizeof(double4_32a) * h->np);
+    zero(h, a->bdelta, sizeof(double) * h->np);
+    adj_stage_reverse(h, 0, v);
+    zero(h, a->bc, sizeof(double) * h->np);
+    adjl::delta(h->L, v, a->P[0], a->bdelta, h->K.cfl, a->bc, a->bP);
+    if ((st = check_launch(h, "residual_vjp"))) return st;
+    return download_points(h, a->bP, bar_prim);
+}
+
+qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters, const double *prim0, double *J,
+                                      double *dJ_dmach, double *dJ_daoa, double *dJ_dwall, double *dJ_dprim0)
+{
+    NEED(h);
+    qlskum_status st = adj_args(h, objective, iters, dJ_dwall);
+    if (st) return st;
+    AdjBuf *a = h->adj;
+    const size_t np = h->np;
+    if (a->ckpt_cap < iters) {
+        if (a->ckpt) cudaFree(a->ckpt);
+        a->ckpt = nullptr;
+        a->ckpt_cap = 0;
+        cudaError_t e = cudaMalloc(&a->ckpt, sizeof(double4_32a) * np * (size_t)iters);
+        if (e != cudaSuccess)
+            return fail(h, QLSKUM_ERR_CUDA,
+                        fmt("checkpoints of %d iterations (%.1f GB): %s", iters,
+                            1e-9 * sizeof(double4_32a) * np * iters, cudaGetErrorString(e)));
+        a->ckpt_cap = iters;
+    }
+    // primal from prim0 or the free stream (initial_conditions_mod.h:23-37),
+    // each iteration's starting state kept
+    if (prim0) {
+        if ((st = upload_points(h, prim0, h->s64.prim[h->pcur], 1.0))) return st;
+    } else {
+        std::vector<double4_32a> fs(np, make_double4_32a(h->K.rho_inf, h->K.u1_inf, h->K.u2_inf, h->K.pr_inf));
+        CK(h, cudaMemcpyAsync(h->s64.prim[h->pcur], fs.data(), sizeof(double4_32a) * np, cudaMemcpyHostToDevice,
+                              h->L.stream));
+        CK(h, cudaStreamSynchronize(h->L.stream));
+    }
+    CK(h, cudaMemsetAsync(h->R.status, 0, sizeof(int), h->L.stream));
+    h->derived_valid = false;
+    h->it = 0;
+    for (int t = 0; t < iters; t++) {
+        CK(h, cudaMemcpyAsync(a->ckpt + np * (size_t)t, h->s64.prim[h->pcur], sizeof(double4_32a) * np,
+                              cudaMemcpyDeviceToDevice, h->L.stream));
+        if ((st = qlskum_fpi_solver(h, t + 1))) return st;
+    }
+    if ((st = check_status(h))) return st;
+    double cl = 0, cd = 0;
+    if ((st = adj_seed(h, objective, h->s64.prim[h->pcur], a->bP, &cl, &cd))) return st;
+    adj_zero_geometry(h);
+    const AdjView v = adj_view(h, true);
+    for (int t = iters - 1; t >= 0; t--) {
+        CK(h, cudaMemcpyAsync(a->P[0], a->ckpt + np * (size_t)t, sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice,
+                              h->L.stream));
+        adj_iteration_forward(h);
+        adj_iteration_reverse(h, v);
+    }
+    if ((st = check_launch(h, "adjoint sweep"))) return st;
+    // bar of the initial state: returned for prim0, else (the free stream)
+    // summed over the points into the free-stream velocity
+    std::vector<double4_32a> b0(np);
+    double bu[2];
+    if ((st = d2h(h, b0.data(), a->bP, sizeof(double4_32a) * np))) return st;
+    if ((st = d2h(h, bu, a->buinf, sizeof bu))) return st;
+    double binit[2] = {0, 0};
+    if (!prim0) {
+        for (int pp = 0; pp < h->n; pp++) {
+            binit[0] += b0[pp].y;
+            binit[1] += b0[pp].z;
+        }
+    }
+    if (dJ_dprim0)
+        for (int i = 0; i < h->n; i++) std::memcpy(dJ_dprim0 + 4 * (size_t)i, &b0[h->perm[i]], sizeof(double4_32a));
+    if (J) *J = objective == QLSKUM_OBJECTIVE_CL ? cl : cd;
+    adj_params(h, objective, cl, cd, bu, binit, dJ_dmach, dJ_daoa);
+    if (dJ_dwall) return adj_geometry(h, objective, h->s64.prim[h->pcur], dJ_dwall);
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_adjoint_fixed_point(qlskum_handle *h, int objective, int adj_iters, double *J,
+                                         double *dJ_dmach, double *dJ_daoa, double *dJ_dwall, double *adj_change)
+{
+    NEED(h);
+    qlskum_status st = adj_args(h, objective, adj_iters, dJ_dwall);
+    if (st) return st;
+    AdjBuf *a = h->adj;
+    const size_t np = h->np;
+    double cl = 0, cd = 0;
+    if ((st = adj_seed(h, objective, h->s64.prim[h->pcur], a->seed, &cl, &cd))) return st;
+    CK(h, cudaMemcpyAsync(a->P[0], h->s64.prim[h->pcur], sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice,
+                          h->L.stream));
+    zero(h, a->lam, sizeof(double4_32a) * np);
+    const AdjView none = adj_view(h, false);
+    // the stage states of S at U, once: the reverse passes only read them
+    adj_iteration_forward(h);
+    // lam <- S_U^T lam + J_U at the current state U (one iteration map S)
+    for (int k = 0; k < adj_iters; k++) {
+        if (k == adj_iters - 1)
+            CK(h, cudaMemcpyAsync(a->lam_prev, a->lam, sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice,
+                                  h->L.stream));
+        CK(h, cudaMemcpyAsync(a->bP, a->lam, sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice, h->L.stream));
+        zero(h, a->buinf, 2 * sizeof(double));
+        adj_iteration_reverse(h, none);
+        CK(h, cudaMemcpyAsync(a->lam, a->seed, sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice, h->L.stream));
+        fp64::add_prim(h->L, h->n, a->bP, a->lam);
+    }
+    // lam^T dS/dalpha: one more reverse pass, accumulating the parameter bars
+    adj_zero_geometry(h);
+    CK(h, cudaMemcpyAsync(a->bP, a->lam, sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice, h->L.stream));
+    adj_iteration_reverse(h, adj_view(h, true));
+    if ((st = check_launch(h, "fixed-point adjoint"))) return st;
+    double bu[2];
+    if ((st = d2h(h, bu, a->buinf, sizeof bu))) return st;
+    if (adj_change) {
+        std::vector<double4_32a> l1(np), l0(np);
+        if ((st = d2h(h, l1.data(), a->lam, sizeof(double4_32a) * np))) return st;
+        if ((st = d2h(h, l0.data(), a->lam_prev, sizeof(double4_32a) * np))) return st;
+        double dmax = 0.0, lmax = 0.0;
+        for (int pp = 0; pp < h->n; pp++) {
+            const double *x1 = &l1[pp].x, *x0 = &l0[pp].x;
+            for (int r = 0; r < 4; r++) {
+                dmax = std::max(dmax, std::fabs(x1[r] - x0[r]));
+                lmax = std::max(lmax, std::fabs(x1[r]));
+            }
+        }
+        *adj_change = lmax > 0.0 ? dmax / lmax : dmax;
+    }
+    const double binit[2] = {0, 0};
+    if (J) *J = objective == QLSKUM_OBJECTIVE_CL ? cl : cd;
+    adj_params(h, objective, cl, cd, bu, binit, dJ_dmach, dJ_daoa);
+    if (dJ_dwall) return adj_geometry(h, objective, h->s64.prim[h->pcur], dJ_dwall);
     return QLSKUM_OK;
 }
 

@@ -138,6 +138,37 @@ struct Launch {
     long long *launches = nullptr;           // host counter
 };
 
+// ---------------------------------------------------------- adjoint (qlskum_adjoint.cu)
+// The geometry read by the adjoint kernels plus, when requested, the
+// accumulators of the geometry's adjoints (device order): per edge
+// {delx, dely, dels w, deln w} and |r_k - r_i|; per point the normal, the
+// gradient moments and the four directional moment sets.
+struct AdjView {
+    DevCloud c;
+    double4_32a *bedge = nullptr;
+    double *bdist = nullptr;
+    double2 *bnrm = nullptr;
+    double4_32a *bgmom = nullptr;
+    double4_32a *bfmom = nullptr;
+};
+
+namespace adjl {
+void update(const Launch &L, const AdjView &a, const CaseConst &K, const double4_32a *Pin, const double4_32a *Pold,
+            const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, double4_32a *bF, double *buinf);
+void flux(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
+          const double *delta, const double4_32a *bF, double4_32a *bq, double4_32a *bdq, double4_32a *bqm,
+          double *bdelta);
+void inner(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq_in,
+           const double4_32a *bdq_out, double4_32a *bq, double4_32a *bdq_in);
+void grad(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *bdq, const double4_32a *bqm,
+          double4_32a *bq);
+void qvars(const Launch &L, int n, const double4_32a *P, const double4_32a *bq, double4_32a *bP);
+void delta(const Launch &L, const AdjView &a, const double4_32a *P, const double *bdelta, double cfl, double *bc,
+           double4_32a *bP);
+void objective(const Launch &L, const AdjView &a, const int *wall_perm, const double4_32a *wall_geo, int n_wall,
+               double cp_scale, double theta, int which, double4_32a *bP);
+}  // namespace adjl
+
 // ---------------------------------------------------------- FP64 kernels (qlskum_fp64.cu)
 namespace fp64 {
 void q_variables(const Launch &L, const DevCloud &c, const double4_32a *prim, double4_32a *q);
@@ -155,6 +186,8 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const d
                  double4_32a *prim_next, double4_32a *q_next, double *cspeed_next, int rk, const Reduce &R);
 void reduce_residual(const Launch &L, const Reduce &R, int n, int it);
 void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
+// dst += src over n double4 rows
+void add_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
 // objectives: per-block partial sums into scratch ([4][ceil(max(n, n_wall)/256)]), then one ordered sum
 void objective(const Launch &L, const DevCloud &c, const double4_32a *prim, const int *wall_perm, const double4_32a *wall_geo,
                int n_wall, double cp_scale, double pr_inf, double gamma, double *entropy, double *out4, double *scratch);

@@ -8,8 +8,17 @@
 // IEEE subtraction is addition of the negation and s*b is exact, so the FP64
 // results are the reference's bit for bit apart from the device libm.
 #pragma once
+#include <cmath>
 #include <cuda_runtime.h>
 #include "qlskum_internal.h"
+
+// Host + device: the per-point arithmetic is also compiled for the host so
+// that its derivatives can be checked on the CPU.
+#ifdef __CUDACC__
+#define QLSKUM_HD __host__ __device__ __forceinline__
+#else
+#define QLSKUM_HD inline
+#endif
 
 namespace qlskum {
 
@@ -20,23 +29,29 @@ namespace qlskum {
 // accurate single-precision functions.
 template <typename R> struct M;
 template <> struct M<double> {
-    static __device__ __forceinline__ double ex(double x) { return exp(x); }
-    static __device__ __forceinline__ double lg(double x) { return log(x); }
-    static __device__ __forceinline__ double ef(double x) { return erf(x); }
-    static __device__ __forceinline__ double sq(double x) { return sqrt(x); }
-    static __device__ __forceinline__ double ab(double x) { return fabs(x); }
-    static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+    static QLSKUM_HD double ex(double x) { return exp(x); }
+    static QLSKUM_HD double lg(double x) { return log(x); }
+    static QLSKUM_HD double ef(double x) { return erf(x); }
+    static QLSKUM_HD double sq(double x) { return sqrt(x); }
+    static QLSKUM_HD double ab(double x) { return fabs(x); }
+    static QLSKUM_HD double div(double a, double b) { return a / b; }
     // a / sqrt(x)
-    static __device__ __forceinline__ double rdsq(double a, double x) { return a / sqrt(x); }
+    static QLSKUM_HD double rdsq(double a, double x) { return a / sqrt(x); }
 };
 template <> struct M<float> {
-    static __device__ __forceinline__ float ex(float x) { return expf(x); }
-    static __device__ __forceinline__ float lg(float x) { return logf(x); }
-    static __device__ __forceinline__ float ef(float x) { return erff(x); }
-    static __device__ __forceinline__ float sq(float x) { return x * rsqrtf(x); }
-    static __device__ __forceinline__ float ab(float x) { return fabsf(x); }
-    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
-    static __device__ __forceinline__ float rdsq(float a, float x) { return a * rsqrtf(x); }
+    static QLSKUM_HD float ex(float x) { return expf(x); }
+    static QLSKUM_HD float lg(float x) { return logf(x); }
+    static QLSKUM_HD float ef(float x) { return erff(x); }
+    static QLSKUM_HD float ab(float x) { return fabsf(x); }
+#ifdef __CUDA_ARCH__
+    static QLSKUM_HD float sq(float x) { return x * rsqrtf(x); }
+    static QLSKUM_HD float div(float a, float b) { return __fdividef(a, b); }
+    static QLSKUM_HD float rdsq(float a, float x) { return a * rsqrtf(x); }
+#else
+    static QLSKUM_HD float sq(float x) { return std::sqrt(x); }
+    static QLSKUM_HD float div(float a, float b) { return a / b; }
+    static QLSKUM_HD float rdsq(float a, float x) { return a / std::sqrt(x); }
+#endif
 };
 
 // 4 * atan(1.0) of parameter_mod.h:10, as a literal.
@@ -44,14 +59,14 @@ template <> struct M<float> {
 
 template <typename R> struct V4 { R v[4]; };
 
-__device__ __forceinline__ void ld4(const double4_32a &a, double o[4]) { o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; }
-__device__ __forceinline__ void ld4(const float4 &a, float o[4]) { o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; }
-__device__ __forceinline__ double4_32a mk4(const double o[4]) { return make_double4_32a(o[0], o[1], o[2], o[3]); }
-__device__ __forceinline__ float4 mk4(const float o[4]) { return make_float4(o[0], o[1], o[2], o[3]); }
+QLSKUM_HD void ld4(const double4_32a &a, double o[4]) { o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; }
+QLSKUM_HD void ld4(const float4 &a, float o[4]) { o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; }
+QLSKUM_HD double4_32a mk4(const double o[4]) { return make_double4_32a(o[0], o[1], o[2], o[3]); }
+QLSKUM_HD float4 mk4(const float o[4]) { return make_float4(o[0], o[1], o[2], o[3]); }
 
 // q_variables_mod.h:19-33: q from (rho, u1, u2, p).
 template <typename R>
-__device__ __forceinline__ void prim_to_q(R rho, R u1, R u2, R pr, R q[4])
+QLSKUM_HD void prim_to_q(R rho, R u1, R u2, R pr, R q[4])
 {
     R beta = M<R>::div(R(0.5) * rho, pr);
     q[0] = M<R>::lg(rho) + (M<R>::lg(beta) * R(2.5)) - beta * (u1 * u1 + u2 * u2);
@@ -64,7 +79,7 @@ __device__ __forceinline__ void prim_to_q(R rho, R u1, R u2, R pr, R q[4])
 // limiters_mod.h:64-104: Venkatakrishnan limiter of one component.
 // `eps2` is (pow(VL_CONST * min_dist, 3))^2 of the point the state belongs to.
 template <typename R>
-__device__ __forceinline__ R venkat(R qt, R q, R qmax, R qmin, R eps2)
+QLSKUM_HD R venkat(R qt, R q, R qmax, R qmin, R eps2)
 {
     R del_neg = qt - q;
     if (M<R>::ab(del_neg) <= R(10e-6)) return R(1.0);
@@ -80,7 +95,7 @@ __device__ __forceinline__ R venkat(R qt, R q, R qmax, R qmin, R eps2)
 
 // q_variables_mod.h:230-253
 template <typename R>
-__device__ __forceinline__ void qtilde_to_prim(const R qt[4], R &u1, R &u2, R &rho, R &pr)
+QLSKUM_HD void qtilde_to_prim(const R qt[4], R &u1, R &u2, R &rho, R &pr)
 {
     R beta = -qt[3] * R(0.5);
     R temp = M<R>::div(R(0.5), beta);
@@ -100,7 +115,7 @@ template <typename R> struct Kin {
 };
 
 template <typename R>
-__device__ __forceinline__ void kin_prep(R nx, R ny, R u1, R u2, R rho, R pr, Kin<R> &k)
+QLSKUM_HD void kin_prep(R nx, R ny, R u1, R u2, R rho, R pr, Kin<R> &k)
 {
     R tx = ny, ty = -nx;
     k.ut = u1 * tx + u2 * ty;
@@ -120,7 +135,7 @@ __device__ __forceinline__ void kin_prep(R nx, R ny, R u1, R u2, R rho, R pr, Ki
 
 // flux_Gxp (s1 = +1) / flux_Gxn (s1 = -1): split_fluxes_mod.h:6-84
 template <typename R>
-__device__ __forceinline__ void flux_x(const Kin<R> &k, R s1, R G[4])
+QLSKUM_HD void flux_x(const Kin<R> &k, R s1, R G[4])
 {
     R A1 = R(0.5) * (R(1.0) + s1 * k.E1);
     R B1 = s1 * k.B1;
@@ -138,7 +153,7 @@ __device__ __forceinline__ void flux_x(const Kin<R> &k, R s1, R G[4])
 
 // flux_Gyp (s2 = +1) / flux_Gyn (s2 = -1): split_fluxes_mod.h:86-164
 template <typename R>
-__device__ __forceinline__ void flux_y(const Kin<R> &k, R s2, R G[4])
+QLSKUM_HD void flux_y(const Kin<R> &k, R s2, R G[4])
 {
     R A2 = R(0.5) * (R(1.0) + s2 * k.E2);
     R B2 = s2 * k.B2;
@@ -157,7 +172,7 @@ __device__ __forceinline__ void flux_y(const Kin<R> &k, R s2, R G[4])
 // flux_quad_GxI (-,-), GxII (+,-), GxIII (+,+), GxIV (-,+):
 // quadrant_fluxes_mod.h:6-211, s1 the t half-range sign, s2 the n one.
 template <typename R>
-__device__ __forceinline__ void flux_quad(const Kin<R> &k, R s1, R s2, R G[4])
+QLSKUM_HD void flux_quad(const Kin<R> &k, R s1, R s2, R G[4])
 {
     R A1 = R(0.5) * (R(1.0) + s1 * k.E1);
     R A2 = R(0.5) * (R(1.0) + s2 * k.E2);
@@ -180,7 +195,7 @@ __device__ __forceinline__ void flux_quad(const Kin<R> &k, R s1, R s2, R G[4])
 // Flux at one end of an edge for sub-stencil d of a point of class f
 // (flux_residual_mod.h:18-87 picks the function per class and direction).
 template <typename R, int D>
-__device__ __forceinline__ void dir_flux(int f, const Kin<R> &k, R G[4])
+QLSKUM_HD void dir_flux(int f, const Kin<R> &k, R G[4])
 {
     if (D <= 1) {
         const R s1 = (D == 0) ? R(1) : R(-1);
@@ -195,7 +210,7 @@ __device__ __forceinline__ void dir_flux(int f, const Kin<R> &k, R G[4])
 // states (interior_fluxes_mod.h:50-89 and the identical blocks of the wall
 // and outer modules).  g = (delx, dely).
 template <typename R>
-__device__ __forceinline__ void edge_states(R delx, R dely, const R qi[4], const R dxi[4], const R dyi[4],
+QLSKUM_HD void edge_states(R delx, R dely, const R qi[4], const R dxi[4], const R dyi[4],
                                             const R mxi[4], const R mni[4], R e2i, const R qk[4],
                                             const R dxk[4], const R dyk[4], const R mxk[4], const R mnk[4],
                                             R e2k, R pi_[4], R pk_[4])
@@ -215,7 +230,7 @@ __device__ __forceinline__ void edge_states(R delx, R dely, const R qi[4], const
 }
 
 // state_update_mod.h:18-33
-__device__ __forceinline__ void primitive_to_conserved(const double P[4], double nx, double ny, double U[4])
+QLSKUM_HD void primitive_to_conserved(const double P[4], double nx, double ny, double U[4])
 {
     double rho = P[0];
     U[0] = rho;
@@ -227,7 +242,7 @@ __device__ __forceinline__ void primitive_to_conserved(const double P[4], double
 }
 
 // state_update_mod.h:35-90
-__device__ __forceinline__ void conserved_vector_Ubar(const CaseConst &K, const double P[4], double nx, double ny,
+QLSKUM_HD void conserved_vector_Ubar(const CaseConst &K, const double P[4], double nx, double ny,
                                                       double Ubar[4])
 {
     const double gamma_new = K.gamma, rho_inf = K.rho_inf, pr_inf = K.pr_inf, pi = K.pi;
@@ -262,7 +277,7 @@ __device__ __forceinline__ void conserved_vector_Ubar(const CaseConst &K, const 
 // One SSPRK stage of one point (state_update_mod.h:111-282).  P is updated in
 // place; returns the point's res_sqr (0 on outer points, which the reference
 // leaves out of the residual).
-__device__ __forceinline__ double stage_update(const CaseConst &K, int f, double nx, double ny, double P[4],
+QLSKUM_HD double stage_update(const CaseConst &K, int f, double nx, double ny, double P[4],
                                                const double4_32a *prim_old_i, const double F[4], int rk)
 {
     const double obt = 1.0 / 3.0, tbt = 2.0 / 3.0, euler = 1.0;
@@ -296,12 +311,13 @@ __device__ __forceinline__ double stage_update(const CaseConst &K, int f, double
 
 // |u| + 3 sqrt(p / rho) of state_update_mod.h:483-485, the denominator of the
 // local time step a neighbour contributes.
-__device__ __forceinline__ double wave_speed(const double P[4])
+QLSKUM_HD double wave_speed(const double P[4])
 {
     double mod_u = sqrt(P[1] * P[1] + P[2] * P[2]);
     return mod_u + 3.0 * sqrt(P[3] / P[0]);
 }
 
+#ifdef __CUDACC__
 // Deterministic block reduction (sum and max) of one value per thread.
 template <int BLOCK>
 __device__ __forceinline__ void block_sum_max(double v, double m, double *out_sum, double *out_max)
@@ -333,5 +349,7 @@ __device__ __forceinline__ long long ell(const DevCloud &c, int i, int j)
 {
     return c.slice_base[i >> 5] + 32LL * j + (i & 31);
 }
+
+#endif  // __CUDACC__
 
 }  // namespace qlskum

@@ -18,6 +18,9 @@ from . import build as _build
 FP64 = 0
 MIXED = 1
 
+OBJECTIVE_CL = 0
+OBJECTIVE_CD = 1
+
 FIELD_PRIM, FIELD_PRIM_OLD, FIELD_Q, FIELD_DQ, FIELD_QM, FIELD_FLUX_RES, FIELD_DELTA, FIELD_NORMALS, FIELD_ENTROPY = range(9)
 _FIELD_SHAPE = {FIELD_PRIM: (4,), FIELD_PRIM_OLD: (4,), FIELD_Q: (4,), FIELD_DQ: (2, 4), FIELD_QM: (2, 4),
                 FIELD_FLUX_RES: (4,), FIELD_DELTA: (), FIELD_NORMALS: (2,), FIELD_ENTROPY: ()}
@@ -107,6 +110,10 @@ def load(build_if_needed: bool = True):
         "qlskum_state_update_noalloc": (i, [i, i, C.c_double, C.c_double] + [C.c_void_p] * 7),
         "qlskum_set_kernel_timing": (i, [H, i]),
         "qlskum_get_kernel_timing": (i, [H, i, dp, C.POINTER(C.c_longlong)]),
+        "qlskum_residual_forward": (i, [H, dp, dp]),
+        "qlskum_residual_vjp": (i, [H, dp, dp, dp]),
+        "qlskum_adjoint_gradient": (i, [H, i, i, dp, dp, dp, dp, dp, dp]),
+        "qlskum_adjoint_fixed_point": (i, [H, i, i, dp, dp, dp, dp, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -160,6 +167,7 @@ class Solver:
             raise QlskumError(st, L.qlskum_last_error(None).decode())
         self._h = h
         self.n = cloud.n
+        self.shape_points = int((np.asarray(cloud.flag_2) > 0).sum())
         self.params = p
 
     # ---------------------------------------------------------------- plumbing
@@ -265,6 +273,56 @@ class Solver:
     @property
     def stream(self) -> int:
         return int(self._L.qlskum_stream(self._h) or 0)
+
+    # ------------------------------------------------------- discrete adjoint
+    def _state(self, a, name):
+        a = np.ascontiguousarray(a, np.float64)
+        if a.shape != (self.n, 4):
+            raise ValueError(f"{name} must be [n, 4]")
+        return a
+
+    def residual(self, prim) -> np.ndarray:
+        """Flux residual R(prim) of one stage, with the local time step of prim (FP64 handles)."""
+        a = self._state(prim, "prim")
+        out = np.empty((self.n, 4))
+        self._ck(self._L.qlskum_residual_forward(self._h, _dp(a), _dp(out)))
+        return out
+
+    def residual_vjp(self, prim, bar_res) -> np.ndarray:
+        """(dR/dprim)^T bar_res at prim."""
+        a = self._state(prim, "prim")
+        b = self._state(bar_res, "bar_res")
+        out = np.empty((self.n, 4))
+        self._ck(self._L.qlskum_residual_vjp(self._h, _dp(a), _dp(b), _dp(out)))
+        return out
+
+    def _adjoint_out(self, objective, wall):
+        obj = {"cl": OBJECTIVE_CL, "cd": OBJECTIVE_CD}.get(objective, objective)
+        vals = [C.c_double() for _ in range(4)]
+        dw = np.zeros(self.shape_points) if wall else None
+        return obj, vals, dw
+
+    def adjoint_gradient(self, objective="cl", iters=100, wall=False, prim0=None) -> dict:
+        """Runs `iters` iterations from prim0 (held fixed) or the free stream and
+        differentiates the objective ("cl" / "cd") at the end through all of
+        them: {"J", "dmach", "daoa" (per degree), "dwall" ([shape_points]
+        normal displacements) or None, "dprim0" ([n, 4]) or None}."""
+        obj, v, dw = self._adjoint_out(objective, wall)
+        p0 = None if prim0 is None else self._state(prim0, "prim0")
+        dp0 = None if prim0 is None else np.empty((self.n, 4))
+        self._ck(self._L.qlskum_adjoint_gradient(self._h, int(obj), int(iters), None if p0 is None else _dp(p0),
+                                                 C.byref(v[0]), C.byref(v[1]), C.byref(v[2]),
+                                                 _dp(dw) if wall else None, None if dp0 is None else _dp(dp0)))
+        return {"J": v[0].value, "dmach": v[1].value, "daoa": v[2].value, "dwall": dw, "dprim0": dp0}
+
+    def adjoint_fixed_point(self, objective="cl", adj_iters=500, wall=False) -> dict:
+        """Steady-state adjoint at the current state; adds "adj_change", the
+        relative change of the adjoint in its last iteration."""
+        obj, v, dw = self._adjoint_out(objective, wall)
+        self._ck(self._L.qlskum_adjoint_fixed_point(self._h, int(obj), int(adj_iters), C.byref(v[0]),
+                                                    C.byref(v[1]), C.byref(v[2]), _dp(dw) if wall else None,
+                                                    C.byref(v[3])))
+        return {"J": v[0].value, "dmach": v[1].value, "daoa": v[2].value, "dwall": dw, "adj_change": v[3].value}
 
 
 class Batch:

@@ -1,15 +1,18 @@
 """Build recipe of the in-tree CUDA library (libqlskum.so) for sm_103a.
 
-Four translation units compiled in parallel and linked into one shared
+Six translation units compiled in parallel and linked into one shared
 library with a C ABI (include/qlskum.h):
 
 * csrc/qlskum_fp64.cu  -- FP64 drop-in kernels, -fmad=false (no FMA
   contraction, the reference's rounding sequence);
 * csrc/qlskum_mixed.cu -- mixed-precision kernels (FP32 edge work, FMA on);
+* csrc/qlskum_adjoint.cu -- reverse-mode kernels of the FP64 iteration;
 * csrc/qlskum_noalloc.cu -- the stage update over caller buffers that
   allocates nothing (static device scratch), -fmad=false like the FP64 unit;
 * csrc/qlskum_host.cpp -- host layer, g++ -ffp-contract=off (bit-exact
-  sub-stencil classification on x86-64 and aarch64 alike).
+  sub-stencil classification on x86-64 and aarch64 alike);
+* csrc/qlskum_vjp_host.cpp -- the per-point arithmetic and its reverse mode
+  compiled for the host, for derivative checks without a GPU.
 
 Output: c-_serial_gb300/_build/libqlskum.so (git-ignored; rebuilt on the GPU
 machine because binaries do not travel between architectures).
@@ -48,7 +51,9 @@ def sources():
         "qlskum_fp64.cu": ["-fmad=false"],
         "qlskum_mixed.cu": ["-fmad=true"],
         "qlskum_noalloc.cu": ["-fmad=false"],
+        "qlskum_adjoint.cu": [],
         "qlskum_host.cpp": [],
+        "qlskum_vjp_host.cpp": [],
     }
 
 

@@ -209,6 +209,47 @@ void *qlskum_batch_stream(qlskum_batch *b);
 qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_tile, int *flux_min_blocks,
                                   int *points_per_warp);
 
+/* ------------------------------------------------------------ discrete adjoint */
+
+/* Reverse mode of the FP64 iteration, for gradients of the force
+ * coefficients.  No counterpart in the reference (which has no adjoint); the
+ * functions differentiate exactly what q_lskum / fpi_solver compute
+ * (fpi_solver_mod.h:14-151).  FP64 handles only (QLSKUM_ERR_UNSUPPORTED
+ * otherwise).  Arrays are in the cloud's point order. */
+#define QLSKUM_OBJECTIVE_CL 0
+#define QLSKUM_OBJECTIVE_CD 1
+
+/* flux_res = R(prim): the local time step of prim (state_update_mod.h:448-496)
+ * and the flux residual of the first stage (q_variables, q_derivatives, the
+ * inner loop, flux_residual).  prim and flux_res double [n][4].  Leaves the
+ * handle's own state alone. */
+qlskum_status qlskum_residual_forward(qlskum_handle *h, const double *prim, double *flux_res);
+/* bar_prim = (dR/dprim)^T bar_flux_res at prim: the vector-Jacobian product
+ * of qlskum_residual_forward, for an autograd.Function's backward. */
+qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const double *bar_flux_res,
+                                  double *bar_prim);
+/* Runs `iters` iterations (as qlskum_q_lskum would; the handle holds the
+ * final state afterwards) from prim0 (double [n][4]) or, when prim0 is NULL,
+ * from the free stream, keeping each iteration's state, then sweeps the
+ * iterations in reverse.  J: the objective (Cl or Cd) at the final state;
+ * dJ_dmach, dJ_daoa (per degree): its exact derivatives through all `iters`
+ * iterations (from the free stream these include the initial state's
+ * dependence on Mach and AoA; a given prim0 is held fixed); dJ_dwall (or
+ * NULL): double [shape_points], the derivative w.r.t. moving wall point m
+ * along its unit normal, with the connectivity, the sub-stencil split and
+ * min_dist held fixed (power 0 only); dJ_dprim0 (or NULL): double [n][4],
+ * the derivative w.r.t. the initial state.  Device memory: 32 bytes per
+ * point per iteration for the states. */
+qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters, const double *prim0, double *J,
+                                      double *dJ_dmach, double *dJ_daoa, double *dJ_dwall, double *dJ_dprim0);
+/* The steady-state adjoint at the handle's current state U (a converged
+ * solution): lam = S_U^T lam + J_U iterated `adj_iters` times from 0, S the
+ * map of one iteration, then dJ/dalpha = J_alpha + lam^T S_alpha.
+ * adj_change (or NULL): max |lam_k - lam_{k-1}| / max |lam_k| of the last
+ * adjoint iteration. */
+qlskum_status qlskum_adjoint_fixed_point(qlskum_handle *h, int objective, int adj_iters, double *J,
+                                         double *dJ_dmach, double *dJ_daoa, double *dJ_dwall, double *adj_change);
+
 /* ------------------------------------------- stage update without allocation */
 
 /* One SSPRK stage update (the arithmetic of qlskum_state_update) over device

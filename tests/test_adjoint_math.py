@@ -1,0 +1,213 @@
+"""Hand-written reverse mode of the per-point / per-edge arithmetic, checked on
+the CPU against central finite differences of the forward functions (the
+same source compiled for the host).  For a random direction v and a random
+output weight w:  w . (f(x + h v) - f(x - h v)) / 2h  ==  vjp(x, w) . v.
+Relative tolerance 1e-6 (h ~ 1e-6 relative; FP64)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+dp = C.POINTER(C.c_double)
+
+
+@pytest.fixture(scope="module")
+def L():
+    import qlskum
+    lib = qlskum.load()
+    sig = {
+        "qlskum_dbg_prim_to_q": [dp, dp], "qlskum_dbg_prim_to_q_vjp": [dp, dp, dp],
+        "qlskum_dbg_qtilde_to_prim": [dp, dp], "qlskum_dbg_qtilde_to_prim_vjp": [dp, dp, dp],
+        "qlskum_dbg_dir_flux": [C.c_int, C.c_int, C.c_double, C.c_double, dp, dp],
+        "qlskum_dbg_dir_flux_vjp": [C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp],
+        "qlskum_dbg_edge_end": [dp, C.c_double, C.c_double, C.c_double, dp],
+        "qlskum_dbg_edge_end_vjp": [dp, C.c_double, C.c_double, C.c_double, dp, dp],
+        "qlskum_dbg_stage_update": [C.c_int, C.c_double, C.c_double, dp, dp, dp, C.c_int, C.c_double, C.c_double, dp],
+        "qlskum_dbg_stage_update_vjp": [C.c_int, C.c_double, C.c_double, dp, dp, dp, C.c_int, C.c_double, C.c_double,
+                                        dp, dp],
+        "qlskum_dbg_wave_speed_vjp": [dp, C.c_double, dp],
+        "qlskum_dbg_venkat_vjp": [C.c_double] * 6 + [dp],
+    }
+    for k, a in sig.items():
+        getattr(lib, k).argtypes = a
+        getattr(lib, k).restype = None
+    lib.qlskum_dbg_wave_speed.argtypes = [dp]
+    lib.qlskum_dbg_wave_speed.restype = C.c_double
+    lib.qlskum_dbg_venkat.argtypes = [C.c_double] * 5
+    lib.qlskum_dbg_venkat.restype = C.c_double
+    return lib
+
+
+def P(a):
+    return np.ascontiguousarray(a, np.float64).ctypes.data_as(dp)
+
+
+def check(fwd, vjp, x, nout, rng, h=1e-6, rtol=1e-6, trials=4):
+    """Dot-product test of vjp against central differences of fwd."""
+    for _ in range(trials):
+        v = rng.standard_normal(x.shape)
+        w = rng.standard_normal(nout)
+        fp = fwd(x + h * v)
+        fm = fwd(x - h * v)
+        lhs = float(w @ (fp - fm) / (2 * h))
+        rhs = float(vjp(x, w) @ v)
+        assert abs(lhs - rhs) <= rtol * max(1.0, abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+def state(rng):
+    return np.array([rng.uniform(0.7, 1.3), rng.uniform(-0.9, 0.9), rng.uniform(-0.5, 0.5), rng.uniform(0.5, 0.9)])
+
+
+def test_prim_to_q(L):
+    rng = np.random.default_rng(1)
+    for _ in range(10):
+        x = state(rng)
+
+        def f(z):
+            o = np.zeros(4)
+            L.qlskum_dbg_prim_to_q(P(z), P(o))
+            return o
+
+        def vj(z, w):
+            o = np.zeros(4)
+            L.qlskum_dbg_prim_to_q_vjp(P(z), P(w), P(o))
+            return o
+        check(f, vj, x, 4, rng)
+
+
+def test_qtilde_to_prim(L):
+    rng = np.random.default_rng(2)
+    for _ in range(10):
+        pr = state(rng)
+        q = np.zeros(4)
+        L.qlskum_dbg_prim_to_q(P(pr), P(q))
+
+        def f(z):
+            o = np.zeros(4)
+            L.qlskum_dbg_qtilde_to_prim(P(z), P(o))
+            return o
+
+        def vj(z, w):
+            o = np.zeros(4)
+            L.qlskum_dbg_qtilde_to_prim_vjp(P(z), P(w), P(o))
+            return o
+        check(f, vj, q, 4, rng)
+
+
+@pytest.mark.parametrize("f,D", [(1, 0), (1, 1), (1, 2), (1, 3), (0, 0), (0, 1), (0, 3), (2, 0), (2, 1), (2, 2)])
+def test_dir_flux_state_and_normal(L, f, D):
+    """Split (interior) and quadrant (wall / outer) fluxes, w.r.t. state and normal."""
+    rng = np.random.default_rng(10 * f + D)
+    for _ in range(6):
+        th = rng.uniform(0, 2 * np.pi)
+        x = np.concatenate([state(rng), [np.cos(th), np.sin(th)]])
+
+        def fw(z):
+            o = np.zeros(4)
+            L.qlskum_dbg_dir_flux(f, D, z[4], z[5], P(z[:4]), P(o))
+            return o
+
+        def vj(z, w):
+            o = np.zeros(6)
+            L.qlskum_dbg_dir_flux_vjp(f, D, z[4], z[5], P(z[:4]), P(w), P(o))
+            return o
+        check(fw, vj, x, 4, rng)
+
+
+def test_venkat_limiter(L):
+    rng = np.random.default_rng(3)
+    n = 0
+    while n < 20:
+        q = rng.uniform(-1, 1)
+        qmax = q + rng.uniform(1e-3, 0.1)
+        qmin = q - rng.uniform(1e-3, 0.1)
+        qt = q + rng.uniform(-0.2, 0.2)
+        e2 = rng.uniform(1e-8, 1e-4)
+        if abs(qt - q) < 1e-4:
+            continue
+        phi = L.qlskum_dbg_venkat(qt, q, qmax, qmin, e2)
+        if phi >= 1.0 - 1e-6:
+            continue
+        n += 1
+        x = np.array([qt, q, qmax, qmin])
+
+        def f(z):
+            return np.array([L.qlskum_dbg_venkat(z[0], z[1], z[2], z[3], e2)])
+
+        def vj(z, w):
+            o = np.zeros(4)
+            L.qlskum_dbg_venkat_vjp(z[0], z[1], z[2], z[3], e2, float(w[0]), P(o))
+            return o
+        check(f, vj, x, 1, rng, h=1e-8)
+
+
+def test_edge_end_reconstruction(L):
+    """q~ = q - 0.5 phi g over 4 components: bars of q, dq, qm and the edge vector."""
+    rng = np.random.default_rng(4)
+    for _ in range(8):
+        q = rng.uniform(-1, 1, 4)
+        x = np.concatenate([q, rng.uniform(-5, 5, 8), q + rng.uniform(1e-3, 0.05, 4), q - rng.uniform(1e-3, 0.05, 4),
+                            rng.uniform(-0.01, 0.01, 2)])
+        e2 = 1e-7
+
+        def f(z):
+            o = np.zeros(4)
+            L.qlskum_dbg_edge_end(P(z[:20]), e2, z[20], z[21], P(o))
+            return o
+
+        def vj(z, w):
+            o = np.zeros(22)
+            L.qlskum_dbg_edge_end_vjp(P(z[:20]), e2, z[20], z[21], P(w), P(o))
+            return o
+        check(f, vj, x, 4, rng, h=1e-8)
+
+
+@pytest.mark.parametrize("flag", [0, 1, 2])
+@pytest.mark.parametrize("rk", [1, 3])
+def test_stage_update(L, flag, rk):
+    """SSPRK stage incl. the wall's no-penetration and the far-field mix: bars of
+    the state, prim_old, flux residual, normal and free-stream velocity (via
+    Mach and AoA)."""
+    rng = np.random.default_rng(100 * flag + rk)
+    for _ in range(5):
+        th = rng.uniform(0, 2 * np.pi)
+        mach, aoa = rng.uniform(0.4, 0.85), rng.uniform(-3, 4)
+        x = np.concatenate([state(rng), state(rng), rng.uniform(-1e-2, 1e-2, 4), [np.cos(th), np.sin(th)]])
+
+        def f(z, mach=mach, aoa=aoa):
+            o = np.zeros(4)
+            L.qlskum_dbg_stage_update(flag, z[12], z[13], P(z[:4]), P(z[4:8]), P(z[8:12]), rk, mach, aoa, P(o))
+            return o
+
+        def vj(z, w, mach=mach, aoa=aoa):
+            o = np.zeros(16)
+            L.qlskum_dbg_stage_update_vjp(flag, z[12], z[13], P(z[:4]), P(z[4:8]), P(z[8:12]), rk, mach, aoa, P(w),
+                                          P(o))
+            return o[:14]
+        check(f, vj, x, 4, rng)
+        if flag == 2:
+            # free-stream velocity through Mach and AoA
+            w = rng.standard_normal(4)
+            h = 1e-6
+            o = np.zeros(16)
+            L.qlskum_dbg_stage_update_vjp(flag, x[12], x[13], P(x[:4]), P(x[4:8]), P(x[8:12]), rk, mach, aoa, P(w),
+                                          P(o))
+            th = np.deg2rad(aoa)
+            dmach = o[14] * np.cos(th) + o[15] * np.sin(th)
+            fd = w @ (f(x, mach + h, aoa) - f(x, mach - h, aoa)) / (2 * h)
+            assert abs(fd - dmach) <= 1e-6 * max(1, abs(fd))
+
+
+def test_wave_speed(L):
+    rng = np.random.default_rng(5)
+    for _ in range(10):
+        x = state(rng)
+
+        def f(z):
+            return np.array([L.qlskum_dbg_wave_speed(P(z))])
+
+        def vj(z, w):
+            o = np.zeros(4)
+            L.qlskum_dbg_wave_speed_vjp(P(z), float(w[0]), P(o))
+            return o
+        check(f, vj, x, 1, rng)

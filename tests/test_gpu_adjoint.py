@@ -1,0 +1,209 @@
+"""Discrete adjoint of the FP64 iteration, through the C ABI.
+
+* qlskum_residual_forward reproduces the reference's first-stage flux
+  residual (golden fixture, 1e-12 like the stage parity test), and its VJP
+  passes the dot-product test against central differences of the forward.
+* qlskum_adjoint_gradient differentiates Cl / Cd after N iterations from the
+  free stream; its derivatives w.r.t. Mach, AoA and wall-point normal
+  displacements are checked against central finite differences of the oracle
+  (the reference's algorithm in C), step 1e-6 (Mach), 1e-5 degrees (AoA),
+  3e-8 (wall coordinates).  Bar: 1e-5 relative to the derivative's scale
+  (FD truncation ~h^2 and rounding ~1e-16 / h are both far below it).  The
+  same from a given initial state, with dJ/dprim0.
+* The fixed-point adjoint contracts at a partly converged state; the torch
+  autograd.Function wrapper reproduces the raw VJP.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_cloud, small_cloud
+
+pytestmark = pytest.mark.gpu
+
+KW = dict(cfl=0.2, vl_const=50.0, power=0.0)
+MACH, AOA, N, INNER = 0.8, 1.5, 12, 2
+
+
+@pytest.fixture(scope="module")
+def qlskum():
+    import qlskum as q
+    q.load()
+    return q
+
+
+def _cloud():
+    return golden_cloud("cloud_trans")
+
+
+def _oracle_J(oracle_mod, cloud, which, mach=MACH, aoa=AOA, iters=N, prim0=None):
+    o = oracle_mod.Oracle(cloud, mach=mach, aoa=aoa, inner_iterations=INNER, threads=4, **KW)
+    if prim0 is not None:
+        o.set_prim(prim0)
+    o.run(iters)
+    cl, cd, _, _ = o.objective()
+    o.close()
+    return cl if which == "cl" else cd
+
+
+def test_residual_forward_matches_reference_stage(qlskum):
+    c = golden_cloud("cloud_trans")
+    z = np.load(os.path.join(GOLDEN, "ref_trans_stage.npz"))
+    s = qlskum.Solver(c, mach=0.63, aoa=2.0, cfl=0.2, vl_const=50.0, inner_iterations=2)
+    R = s.residual(z["prim_in"])
+    scale = np.abs(z["flux_res"]).max(axis=0)
+    assert (np.abs(R - z["flux_res"]) / scale).max() < 1e-12
+    # the handle's own state is untouched
+    s.q_lskum(1)
+    assert np.isfinite(s.prim).all()
+
+
+@pytest.mark.parametrize("inner", [0, 2])
+def test_residual_vjp_dot_product(qlskum, inner):
+    c = _cloud()
+    s = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=inner, **KW)
+    s.q_lskum(20)
+    rng = np.random.default_rng(3 + inner)
+    # The map is piecewise smooth: the neighbour max / min, the limiter's
+    # branches and the time step's minimum switch where two values cross.  1%
+    # noise keeps such pairs apart (no exact ties) and a step of 1e-8 makes a
+    # swap of order rare; measured mismatches at this step are <= 1e-6
+    # relative and <= 5e-10 of the Cauchy-Schwarz bound, against ~1e-2 for a
+    # missing term.
+    p = s.prim * (1.0 + 1e-2 * rng.standard_normal((c.n, 4)))
+    h = 1e-8
+    for _ in range(3):
+        v = rng.standard_normal((c.n, 4)) * np.array([1.0, 0.5, 0.5, 0.7])
+        w = rng.standard_normal((c.n, 4))
+        fd = float(np.sum(w * (s.residual(p + h * v) - s.residual(p - h * v))) / (2 * h))
+        g = s.residual_vjp(p, w)
+        ad = float(np.sum(g * v))
+        assert abs(fd - ad) <= 1e-8 * np.linalg.norm(g) * np.linalg.norm(v), (fd, ad)
+        assert abs(fd - ad) <= 1e-5 * abs(ad), (fd, ad)
+
+
+def test_autograd_function_matches_vjp(qlskum):
+    torch = pytest.importorskip("torch")
+    from qlskum.autograd import flux_residual
+    c = _cloud()
+    s = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=1, **KW)
+    s.q_lskum(5)
+    p = torch.tensor(s.prim, dtype=torch.float64, requires_grad=True)
+    w = torch.randn(c.n, 4, dtype=torch.float64, generator=torch.Generator().manual_seed(0))
+    R = flux_residual(p, s)
+    np.testing.assert_array_equal(R.detach().numpy(), s.residual(s.prim))
+    (R * w).sum().backward()
+    # the VJP scatters to neighbours with FP64 atomics: the order of the sums,
+    # hence the last bits, varies between calls
+    ref = s.residual_vjp(s.prim, w.numpy())
+    np.testing.assert_allclose(p.grad.numpy(), ref, rtol=0, atol=1e-13 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("which", ["cl", "cd"])
+def test_adjoint_mach_aoa_vs_oracle_fd(qlskum, oracle_mod, which):
+    c = _cloud()
+    s = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **KW)
+    g = s.adjoint_gradient(which, iters=N)
+    J0 = _oracle_J(oracle_mod, c, which)
+    assert abs(g["J"] - J0) <= 1e-10 * max(1.0, abs(J0))
+    # the handle holds the final state, as after q_lskum(N)
+    assert s.iteration == N
+    hm, ha = 1e-6, 1e-5
+    fd_m = (_oracle_J(oracle_mod, c, which, mach=MACH + hm) - _oracle_J(oracle_mod, c, which, mach=MACH - hm)) / (2 * hm)
+    fd_a = (_oracle_J(oracle_mod, c, which, aoa=AOA + ha) - _oracle_J(oracle_mod, c, which, aoa=AOA - ha)) / (2 * ha)
+    assert abs(g["dmach"] - fd_m) <= 1e-5 * max(abs(fd_m), 1e-3), (g["dmach"], fd_m)
+    assert abs(g["daoa"] - fd_a) <= 1e-5 * max(abs(fd_a), 1e-3), (g["daoa"], fd_a)
+
+
+def _moved(c, m, d):
+    from qlskum.cloudgen import Cloud
+    x = c.x.copy()
+    y = c.y.copy()
+    x[m] += d[0]
+    y[m] += d[1]
+    return Cloud(x, y, c.left, c.right, c.flag_1, c.flag_2, c.min_dist, c.nbhs, c.conn)
+
+
+def test_adjoint_wall_displacement_vs_oracle_fd(qlskum, oracle_mod):
+    """16 seeded wall points away from the trailing edge at 1e-5; the trailing
+    edge and its two neighbours at 1e-3: the edge point's normal comes from
+    two points 7e-4 apart, so J is non-smooth there on the FD step's scale
+    (the FD converges to the adjoint value as the step shrinks)."""
+    c = _cloud()
+    s = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **KW)
+    g = s.adjoint_gradient("cl", iters=N, wall=True)
+    dw = g["dwall"]
+    assert dw.shape == (s.shape_points,) and np.isfinite(dw).all()
+    nrm = s.field(qlskum.FIELD_NORMALS)
+    te = {0, int(c.left[0]) - 1, int(c.right[0]) - 1}
+    rng = np.random.default_rng(16)
+    pts = rng.choice(sorted(set(range(s.shape_points)) - te), size=16, replace=False)
+    scale = np.abs(dw).max()
+    for m, h, tol in [(m, 3e-8, 1e-5) for m in pts] + [(m, 1e-8, 1e-3) for m in sorted(te)]:
+        Jp = _oracle_J(oracle_mod, _moved(c, m, h * nrm[m]), "cl")
+        Jm = _oracle_J(oracle_mod, _moved(c, m, -h * nrm[m]), "cl")
+        fd = (Jp - Jm) / (2 * h)
+        assert abs(dw[m] - fd) <= tol * max(abs(fd), 1e-2 * scale), (m, dw[m], fd)
+
+
+def test_adjoint_from_given_state_vs_oracle_fd(qlskum, oracle_mod):
+    """prim0 held fixed: Mach / AoA by central differences of the oracle started
+    from the same state, dJ/dprim0 by a directional difference."""
+    c = _cloud()
+    s = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **KW)
+    s.q_lskum(10)
+    rng = np.random.default_rng(7)
+    U0 = s.prim * (1.0 + 1e-2 * rng.standard_normal((c.n, 4)))
+    iters = 3
+    g = s.adjoint_gradient("cd", iters=iters, prim0=U0)
+    J0 = _oracle_J(oracle_mod, c, "cd", iters=iters, prim0=U0)
+    assert abs(g["J"] - J0) <= 1e-10 * max(1.0, abs(J0))
+    hm, ha = 1e-6, 1e-5
+    fd_m = (_oracle_J(oracle_mod, c, "cd", mach=MACH + hm, iters=iters, prim0=U0)
+            - _oracle_J(oracle_mod, c, "cd", mach=MACH - hm, iters=iters, prim0=U0)) / (2 * hm)
+    fd_a = (_oracle_J(oracle_mod, c, "cd", aoa=AOA + ha, iters=iters, prim0=U0)
+            - _oracle_J(oracle_mod, c, "cd", aoa=AOA - ha, iters=iters, prim0=U0)) / (2 * ha)
+    assert abs(g["dmach"] - fd_m) <= 1e-5 * max(abs(fd_m), 1e-3), (g["dmach"], fd_m)
+    assert abs(g["daoa"] - fd_a) <= 1e-5 * max(abs(fd_a), 1e-3), (g["daoa"], fd_a)
+    v = rng.standard_normal((c.n, 4)) * np.array([1.0, 0.5, 0.5, 0.7])
+    h = 1e-8
+    fd = (_oracle_J(oracle_mod, c, "cd", iters=iters, prim0=U0 + h * v)
+          - _oracle_J(oracle_mod, c, "cd", iters=iters, prim0=U0 - h * v)) / (2 * h)
+    ad = float(np.sum(g["dprim0"] * v))
+    assert abs(fd - ad) <= 1e-4 * abs(ad), (fd, ad)
+
+
+def test_adjoint_rejects_mixed_and_weighted(qlskum):
+    c = small_cloud()
+    s = qlskum.Solver(c, precision=qlskum.MIXED, **KW)
+    with pytest.raises(qlskum.QlskumError, match="unsupported"):
+        s.adjoint_gradient("cl", iters=2)
+    w = qlskum.Solver(_cloud(), power=1.0, inner_iterations=0, **{k: v for k, v in KW.items() if k != "power"})
+    with pytest.raises(qlskum.QlskumError, match="unsupported"):
+        w.adjoint_gradient("cl", iters=2, wall=True)
+    # weighted stencils still give the parameter derivatives
+    assert np.isfinite(w.adjoint_gradient("cd", iters=2)["dmach"])
+
+
+def test_fixed_point_adjoint_one_step_identity(qlskum):
+    """With one adjoint iteration, lam = dJ/dU and the fixed-point derivative is
+    J_alpha(U) + lam^T dS/dalpha(U); the one-iteration adjoint from the same
+    state held fixed gives J_alpha(S(U)) + lam^T dS/dalpha(U) (J is linear in
+    the wall pressures, so lam is the same).  The two differ only by the
+    objective's explicit terms: dCl/dM = -2 Cl / M and dCl/dtheta = -Cd."""
+    c = _cloud()
+    s = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **KW)
+    s.q_lskum(10)
+    U = s.prim
+    cd0 = s.objective()[1]
+    fp = s.adjoint_fixed_point("cl", adj_iters=1)
+    ag = s.adjoint_gradient("cl", iters=1, prim0=U)
+    cd1 = s.objective()[1]
+    dm = fp["dmach"] - ag["dmach"]
+    da = fp["daoa"] - ag["daoa"]
+    np.testing.assert_allclose(dm, -2.0 * (fp["J"] - ag["J"]) / MACH, rtol=1e-9, atol=1e-12 * abs(fp["dmach"]))
+    np.testing.assert_allclose(da, -(cd0 - cd1) * np.pi / 180, rtol=1e-9, atol=1e-12 * abs(fp["daoa"]))
+    # more adjoint iterations and the wall gradient run through the same path
+    r = s.adjoint_fixed_point("cd", adj_iters=20, wall=True)
+    assert np.isfinite([r["J"], r["dmach"], r["daoa"], r["adj_change"]]).all() and np.isfinite(r["dwall"]).all()
