@@ -451,16 +451,33 @@ qlskum_status tune(qlskum_handle *h)
         return ms;
     };
     long long launches0 = h->launches;
+    // gradient + inner-loop kernels: one gather per edge at four block sizes,
+    // then the staged forms; weighted as one iteration runs them (one
+    // gradient with the time step, inner_iterations inner steps per stage)
+    const int ni = std::max(1, h->prm.inner_iterations);
+    auto point_kernels = [&](const Launch &L) {
+        return ni * time3([&] { mixed::q_inner(L, c, S.q[0], S.dq[0], S.dq[1]); }) +
+               time3([&] { mixed::q_derivatives(L, c, S.q[0], S.dq[0], S.qm, S.cspeed, S.delta, (float)h->K.cfl); });
+    };
     static const int blocks[4] = {64, 128, 256, 512};
     float best = 1e30f;
-    int best_block = h->L.block;
+    Launch best_L = h->L;
     for (int bs : blocks) {
         Launch L = h->L;
         L.block = bs;
-        float ms = time3([&] { mixed::q_inner(L, c, S.q[0], S.dq[0], S.dq[1]); });
-        if (ms < best) { best = ms; best_block = bs; }
+        L.staged = 0;
+        const float ms = point_kernels(L);
+        if (ms < best) { best = ms; best_L = L; }
     }
-    h->L.block = best_block;
+    const int nst = mixed::staged_variants(c);
+    for (int v = 1; v <= nst; v++) {
+        Launch L = best_L;
+        L.staged = v;
+        const float ms = point_kernels(L);
+        if (ms < best) { best = ms; best_L = L; }
+    }
+    h->L.block = best_L.block;
+    h->L.staged = best_L.staged;
     mixed::q_derivatives(h->L, c, S.q[0], S.dq[0], S.qm, S.cspeed, S.delta, (float)h->K.cfl);
     best = 1e30f;
     for (int v = 0; v < mixed::flux_variants(); v++) {
@@ -738,6 +755,8 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
     dc.e_geo = d_egeo; dc.e_sn = d_esn; dc.e_dist = d_edist; dc.e_dir = d_edir; dc.nrm = d_nrm; dc.eps2 = d_eps2;
     dc.ggeo = d_ggeo; dc.fgeo = d_fgeo; dc.e_geo32 = d_egeo32; dc.e_sn32 = d_esn32; dc.eps2_32 = d_eps32;
     dc.e_dist32 = d_edist32; dc.fcoef = d_fcoef; dc.gcoef = d_gcoef; dc.unit_w = unit_w ? 1 : 0; dc.e_xy32 = d_exy32;
+    dc.max_nb = 0;
+    for (int i = 0; i < n; i++) dc.max_nb = std::max(dc.max_nb, c->nbhs[i]);
 
     G.d_wall_perm = A.alloc<int>(std::max(sp, 1));
     G.d_wall_geo = A.alloc<double4_32a>(std::max(sp, 1));
@@ -1203,13 +1222,37 @@ void *qlskum_stream(qlskum_handle *h) { return h ? (void *)h->L.stream : nullptr
 
 long long qlskum_launch_count(const qlskum_handle *h) { return h ? h->launches : 0; }
 
-qlskum_status qlskum_get_launch_config(qlskum_handle *h, int *flux_block, int *flux_min_blocks, int *point_block)
+qlskum_status qlskum_get_launch_config(qlskum_handle *h, int *flux_block, int *flux_min_blocks, int *point_block,
+                                       int *gather_depth)
 {
     NEED(h);
-    static const int minb[4] = {4, 5, 8, 2};
     if (flux_block) *flux_block = h->prm.precision == QLSKUM_MIXED ? mixed::flux_block(h->flux_variant) : 128;
-    if (flux_min_blocks) *flux_min_blocks = h->prm.precision == QLSKUM_MIXED ? minb[h->flux_variant] : 1;
-    if (point_block) *point_block = h->L.block;
+    if (flux_min_blocks) *flux_min_blocks = h->prm.precision == QLSKUM_MIXED ? mixed::flux_min_blocks(h->flux_variant) : 1;
+    if (point_block) *point_block = h->L.staged ? mixed::staged_block(h->L.staged) : h->L.block;
+    if (gather_depth) *gather_depth = h->L.staged ? mixed::staged_depth(h->L.staged) : 0;
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_set_launch_config(qlskum_handle *h, int flux_variant, int point_block, int staged)
+{
+    NEED(h);
+    if (flux_variant < 0 || flux_variant >= mixed::flux_variants())
+        return fail(h, QLSKUM_ERR_INVALID, fmt("flux_variant %d not in 0..%d", flux_variant, mixed::flux_variants() - 1));
+    if (point_block != 64 && point_block != 128 && point_block != 256 && point_block != 512)
+        return fail(h, QLSKUM_ERR_INVALID, "point_block must be 64, 128, 256 or 512");
+    if (staged < 0 || staged > 4) return fail(h, QLSKUM_ERR_INVALID, "staged must be in 0..4");
+    if (staged > 0 && h->prm.precision == QLSKUM_MIXED && staged > mixed::staged_variants(h->dc))
+        return fail(h, QLSKUM_ERR_UNSUPPORTED, "staged variant needs more shared memory than the device allows");
+    h->flux_variant = flux_variant;
+    h->L.block = point_block;
+    h->L.staged = h->prm.precision == QLSKUM_MIXED ? staged : 0;
+    h->tuned = true;
+    // captured iterations hold the old shapes
+    for (auto &g : h->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
     return QLSKUM_OK;
 }
 

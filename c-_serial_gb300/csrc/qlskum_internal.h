@@ -59,6 +59,8 @@ struct DevCloud {
     // per edge (FP32) and rotate it by the point normal themselves.
     int unit_w = 0;
     const float2 *e_xy32 = nullptr;
+    // largest neighbour count of the cloud (sizes the staged kernels' shared memory)
+    int max_nb = 0;
 };
 
 // Free-stream constants of one case (parameter_mod.h:4-30).
@@ -136,6 +138,10 @@ struct Launch {
     cudaStream_t stream = nullptr;
     int block = 128;
     long long *launches = nullptr;           // host counter
+    // mixed gradient / inner-loop kernels: 0 = one gather per edge in turn,
+    // v > 0 = staged variant v (edge list in shared memory, neighbour data
+    // streamed with cp.async a few edges ahead); picked by the autotuner
+    int staged = 0;
 };
 
 // ---------------------------------------------------------- adjoint (qlskum_adjoint.cu)
@@ -199,11 +205,17 @@ void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, float4
 void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *dq, float4 *qm,
                    const float *cspeed, float *delta, float cfl);
 void q_inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, float4 *dq_out);
+// staged variants of the gradient / inner-loop kernels usable on this cloud
+// (Launch::staged = 1 .. staged_variants()); sets their shared-memory limits
+int staged_variants(const DevCloud &c);
+int staged_block(int v);
+int staged_depth(int v);
 void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const float4 *q, const float4 *dq,
                  const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
                  double4_32a *prim_next, float4 *q_next, float *cspeed_next, int rk, const Reduce &R, int variant);
 int flux_variants();
 int flux_block(int variant);
+int flux_min_blocks(int variant);
 // batched (persistent) forms
 void batch_derived(const Launch &L, const BatchView &B, int tile, const double4_32a *prim, float4 *q, float *cs);
 void batch_q_derivatives(const Launch &L, const BatchView &B, int tile, const float4 *q, float4 *dq, float4 *qm,

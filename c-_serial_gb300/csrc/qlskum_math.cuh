@@ -24,9 +24,10 @@ namespace qlskum {
 
 // Elementary operations per real type.  For double they are exactly the
 // reference's: IEEE division and square root, libm-style exp / log / erf.
-// For float (mixed form only) divisions and square roots use the
-// reciprocal / reciprocal-square-root units (2 ulp), exp / log / erf stay the
-// accurate single-precision functions.
+// For float (mixed form only) the device uses the special-function unit:
+// divisions and square roots through the reciprocal / reciprocal-square-root
+// approximations (2 ulp), exp and log through ex2 / lg2 (relative error
+// about 2^-21 over the arguments met here); erf comes from erf_e below.
 template <typename R> struct M;
 template <> struct M<double> {
     static QLSKUM_HD double ex(double x) { return exp(x); }
@@ -39,20 +40,41 @@ template <> struct M<double> {
     static QLSKUM_HD double rdsq(double a, double x) { return a / sqrt(x); }
 };
 template <> struct M<float> {
-    static QLSKUM_HD float ex(float x) { return expf(x); }
-    static QLSKUM_HD float lg(float x) { return logf(x); }
     static QLSKUM_HD float ef(float x) { return erff(x); }
     static QLSKUM_HD float ab(float x) { return fabsf(x); }
 #ifdef __CUDA_ARCH__
+    static QLSKUM_HD float ex(float x) { return __expf(x); }
+    static QLSKUM_HD float lg(float x) { return __logf(x); }
     static QLSKUM_HD float sq(float x) { return x * rsqrtf(x); }
     static QLSKUM_HD float div(float a, float b) { return __fdividef(a, b); }
     static QLSKUM_HD float rdsq(float a, float x) { return a * rsqrtf(x); }
 #else
+    static QLSKUM_HD float ex(float x) { return std::exp(x); }
+    static QLSKUM_HD float lg(float x) { return std::log(x); }
     static QLSKUM_HD float sq(float x) { return std::sqrt(x); }
     static QLSKUM_HD float div(float a, float b) { return a / b; }
     static QLSKUM_HD float rdsq(float a, float x) { return a / std::sqrt(x); }
 #endif
 };
+
+// erf(x) given e = exp(-x^2), which the kinetic moments compute anyway.
+// double: the libm erf (the reference's; e unused).  float: Abramowitz &
+// Stegun 7.1.26, C. Hastings' approximation
+//   erf(x) = 1 - (a1 t + a2 t^2 + a3 t^3 + a4 t^4 + a5 t^5) exp(-x^2),
+//   t = 1 / (1 + p x),  x >= 0, odd extension,
+// absolute error <= 1.5e-7 for every x: one reciprocal and five FMAs in
+// place of a separate erf evaluation.
+template <typename R> QLSKUM_HD R erf_e(R x, R e);
+template <> QLSKUM_HD double erf_e<double>(double x, double) { return erf(x); }
+template <> QLSKUM_HD float erf_e<float>(float x, float e)
+{
+    const float t = M<float>::div(1.0f, fmaf(0.3275911f, fabsf(x), 1.0f));
+    float p = fmaf(1.061405429f, t, -1.453152027f);
+    p = fmaf(p, t, 1.421413741f);
+    p = fmaf(p, t, -0.284496736f);
+    p = fmaf(p, t, 0.254829592f);
+    return copysignf(fmaf(-p * t, e, 1.0f), x);
+}
 
 // 4 * atan(1.0) of parameter_mod.h:10, as a literal.
 #define QLSKUM_PI 3.141592653589793
@@ -124,10 +146,11 @@ QLSKUM_HD void kin_prep(R nx, R ny, R u1, R u2, R rho, R pr, Kin<R> &k)
     R sb = M<R>::sq(beta);
     R S1 = k.ut * sb;
     R S2 = k.un * sb;
-    k.B1 = M<R>::rdsq(R(0.5) * M<R>::ex(-S1 * S1), R(QLSKUM_PI) * beta);
-    k.B2 = M<R>::rdsq(R(0.5) * M<R>::ex(-S2 * S2), R(QLSKUM_PI) * beta);
-    k.E1 = M<R>::ef(S1);
-    k.E2 = M<R>::ef(S2);
+    const R e1 = M<R>::ex(-S1 * S1), e2 = M<R>::ex(-S2 * S2);
+    k.B1 = M<R>::rdsq(R(0.5) * e1, R(QLSKUM_PI) * beta);
+    k.B2 = M<R>::rdsq(R(0.5) * e2, R(QLSKUM_PI) * beta);
+    k.E1 = erf_e<R>(S1, e1);
+    k.E2 = erf_e<R>(S2, e2);
     k.pbr = M<R>::div(pr, rho);
     k.usq = k.ut * k.ut + k.un * k.un;
     k.rho = rho;

@@ -227,6 +227,360 @@ __device__ __forceinline__ void inner_point(const DevCloud &c, int i, const floa
     dq_out[2 * i + 1] = mk4(dy);
 }
 
+// ------------------------------------------------ staged neighbour gathers
+// A thread first copies its point's edge list (neighbour index and edge
+// vector: one coalesced row of the sliced-ELL arrays per edge) into shared
+// memory, then streams the neighbours' data through a private ring of D + 1
+// shared-memory slots with cp.async, D edges ahead of the arithmetic: the
+// gathers of the next edges are in flight while the current one is
+// computed, instead of one exposed gather latency per edge.  Slots are
+// private to their thread, so no barrier is needed (cp.async.wait_group
+// orders a thread's own copies; a slot is refilled only after the registers
+// read from it were consumed).  Layout per block of B threads (field-major,
+// thread-minor, conflict-free): ring [D + 1][F][B] float4, then the edge
+// list, neighbour index [max_nb][B] int and edge vector [max_nb][B] float2
+// (unit weights) or float4.
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async4(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// bytes of dynamic shared memory of a staged kernel: F float4 fields per ring slot
+constexpr size_t staged_bytes(int block, int depth, int fields, int max_nb, bool uw)
+{
+    return (size_t)(depth + 1) * fields * block * 16 + (size_t)max_nb * block * (4 + (uw ? 8 : 16));
+}
+
+// Edge list of point i into shared memory (neighbour index, edge vector).
+template <int B, bool UW>
+__device__ __forceinline__ void stage_edges(const DevCloud &c, long long base, int nb, int t, int *snbr, void *sgeo)
+{
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        cp_async4(snbr + j * B + t, c.e_nbr + e);
+        if (UW) cp_async8(static_cast<float2 *>(sgeo) + j * B + t, c.e_xy32 + e);
+        else cp_async16(static_cast<float4 *>(sgeo) + j * B + t, c.e_geo32 + e);
+    }
+    cp_commit();
+}
+
+template <int B, bool UW> __device__ __forceinline__ float4 staged_geo(const void *sgeo, int j, int t)
+{
+    if (UW) {
+        const float2 d = static_cast<const float2 *>(sgeo)[j * B + t];
+        return make_float4(d.x, d.y, d.x, d.y);
+    }
+    return static_cast<const float4 *>(sgeo)[j * B + t];
+}
+
+// q_variables_mod.h:120-213 with staged gathers (q, dq_x, dq_y of each neighbour).
+template <int B, int D, bool UW>
+__global__ void __launch_bounds__(B) k_q_inner_st(DevCloud c, const float4 *__restrict__ q,
+                                                  const float4 *__restrict__ dq_in, float4 *__restrict__ dq_out)
+{
+    extern __shared__ float4 smem4[];
+    float4 *ring = smem4;
+    int *snbr = reinterpret_cast<int *>(ring + (D + 1) * 3 * B);
+    void *sgeo = snbr + c.max_nb * B;
+    const int t = threadIdx.x;
+    const int i = blockIdx.x * B + t;
+    if (i >= c.n) return;
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    stage_edges<B, UW>(c, base, nb, t, snbr, sgeo);
+    float qi[4], dxi[4], dyi[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    ld4(q[i], qi);
+    ld4(dq_in[2 * i], dxi);
+    ld4(dq_in[2 * i + 1], dyi);
+    cp_wait<0>();
+    auto issue = [&](int j) {
+        const int k = snbr[j * B + t];
+        float4 *slot = ring + (j % (D + 1)) * 3 * B + t;
+        cp_async16(slot, q + k);
+        cp_async16(slot + B, dq_in + 2 * k);
+        cp_async16(slot + 2 * B, dq_in + 2 * k + 1);
+    };
+#pragma unroll
+    for (int j = 0; j < D; j++) {
+        if (j < nb) issue(j);
+        cp_commit();
+    }
+    for (int j = 0; j < nb; j++) {
+        if (j + D < nb) issue(j + D);
+        cp_commit();
+        cp_wait<D>();
+        const float4 *slot = ring + (j % (D + 1)) * 3 * B + t;
+        float qk[4], dxk[4], dyk[4];
+        ld4(slot[0], qk);
+        ld4(slot[B], dxk);
+        ld4(slot[2 * B], dyk);
+        const float4 g = staged_geo<B, UW>(sgeo, j, t);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            float t1 = qi[r] - 0.5f * (g.x * dxi[r] + g.y * dyi[r]);
+            float t2 = qk[r] - 0.5f * (g.x * dxk[r] + g.y * dyk[r]);
+            sdx[r] += g.z * (t2 - t1);
+            sdy[r] += g.w * (t2 - t1);
+        }
+    }
+    float dx[4], dy[4];
+    solve_grad(c.gcoef[i], sdx, sdy, dx, dy);
+    dq_out[2 * i] = mk4(dx);
+    dq_out[2 * i + 1] = mk4(dy);
+}
+
+// q_variables_mod.h:36-118 with staged gathers (q and, in the first stage,
+// the wave speed of each neighbour; the edge length for the time step).
+template <int B, int D, bool UW>
+__global__ void __launch_bounds__(B) k_q_derivatives_st(DevCloud c, const float4 *__restrict__ q,
+                                                        float4 *__restrict__ dq, float4 *__restrict__ qm,
+                                                        const float *__restrict__ cs, float *__restrict__ delta,
+                                                        float cfl)
+{
+    extern __shared__ float4 smem4[];
+    float4 *ring = smem4;                                  // [D + 1][2][B]: q, {cs, dist, -, -}
+    int *snbr = reinterpret_cast<int *>(ring + (D + 1) * 2 * B);
+    void *sgeo = snbr + c.max_nb * B;
+    const int t = threadIdx.x;
+    const int i = blockIdx.x * B + t;
+    if (i >= c.n) return;
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    stage_edges<B, UW>(c, base, nb, t, snbr, sgeo);
+    float qi[4], qmax[4], qmin[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    ld4(q[i], qi);
+#pragma unroll
+    for (int r = 0; r < 4; r++) { qmax[r] = qi[r]; qmin[r] = qi[r]; }
+    float min_dt = 1.0f;
+    cp_wait<0>();
+    auto issue = [&](int j) {
+        const int k = snbr[j * B + t];
+        float4 *slot = ring + (j % (D + 1)) * 2 * B + t;
+        cp_async16(slot, q + k);
+        if (delta) {
+            float *aux = reinterpret_cast<float *>(slot + B);
+            cp_async4(aux, cs + k);
+            cp_async4(aux + 1, c.e_dist32 + base + 32LL * j);
+        }
+    };
+#pragma unroll
+    for (int j = 0; j < D; j++) {
+        if (j < nb) issue(j);
+        cp_commit();
+    }
+    for (int j = 0; j < nb; j++) {
+        if (j + D < nb) issue(j + D);
+        cp_commit();
+        cp_wait<D>();
+        const float4 *slot = ring + (j % (D + 1)) * 2 * B + t;
+        float qk[4];
+        ld4(slot[0], qk);
+        const float4 g = staged_geo<B, UW>(sgeo, j, t);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            qmax[r] = fmaxf(qmax[r], qk[r]);
+            qmin[r] = fminf(qmin[r], qk[r]);
+            sdx[r] += g.z * (qk[r] - qi[r]);
+            sdy[r] += g.w * (qk[r] - qi[r]);
+        }
+        if (delta) {
+            const float4 aux = slot[B];
+            min_dt = fminf(min_dt, cfl * __fdividef(aux.y, aux.x));
+        }
+    }
+    float dx[4], dy[4];
+    solve_grad(c.gcoef[i], sdx, sdy, dx, dy);
+    dq[2 * i] = mk4(dx);
+    dq[2 * i + 1] = mk4(dy);
+    qm[2 * i] = mk4(qmax);
+    qm[2 * i + 1] = mk4(qmin);
+    if (delta) delta[i] = min_dt;
+}
+
+// limiters_mod.h:64-104 for the FP32 form, without branches: the common
+// factor del_neg of the numerator and the denominator cancels, and the
+// reference's |del_neg| <= 1e-5 cut is a select.
+__device__ __forceinline__ float venkat32(float qt, float q, float qmax, float qmin, float eps2)
+{
+    const float dn = qt - q;
+    const float dp = (dn > 0.f) ? qmax - q : qmin - q;
+    const float dp2 = dp * dp;
+    const float num = fmaf(2.0f * dn, dp, dp2 + eps2);
+    const float den = fmaf(dn, dp, fmaf(2.0f * dn, dn, dp2 + eps2));
+    const float phi = fminf(__fdividef(num, den), 1.0f);
+    return fabsf(dn) <= 10e-6f ? 1.0f : phi;
+}
+
+// Limited reconstruction of both ends of an edge and their primitive states
+// (interior_fluxes_mod.h:50-89), FP32.
+__device__ __forceinline__ void edge_states32(float delx, float dely, const float qi[4], const float dxi[4],
+                                              const float dyi[4], const float mxi[4], const float mni[4],
+                                              float e2i, const float qk[4], const float dxk[4], const float dyk[4],
+                                              const float mxk[4], const float mnk[4], float e2k, float pi_[4],
+                                              float pk_[4])
+{
+    float ti[4], tk[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const float gi = fmaf(delx, dxi[r], dely * dyi[r]);
+        const float gk = fmaf(delx, dxk[r], dely * dyk[r]);
+        const float phi_i = venkat32(fmaf(-0.5f, gi, qi[r]), qi[r], mxi[r], mni[r], e2i);
+        const float phi_k = venkat32(fmaf(-0.5f, gk, qk[r]), qk[r], mxk[r], mnk[r], e2k);
+        ti[r] = fmaf(-0.5f * phi_i, gi, qi[r]);
+        tk[r] = fmaf(-0.5f * phi_k, gk, qk[r]);
+    }
+    qtilde_to_prim(ti, pi_[1], pi_[2], pi_[0], pi_[3]);
+    qtilde_to_prim(tk, pk_[1], pk_[2], pk_[0], pk_[3]);
+}
+
+// x half-range flux of one end: split flux (interior) or the class's
+// quadrant flux (wall: n half-range -, outer: +), t sign s1.
+__device__ __forceinline__ void x_flux(int f, const Kin<float> &k, float s1, float G[4])
+{
+    if (f == kInterior) flux_x(k, s1, G);
+    else flux_quad(k, s1, (f == kOuter) ? 1.0f : -1.0f, G);
+}
+
+// Flux contribution of one edge (interior_fluxes_mod.h, wall_fluxes_mod.h,
+// outer_fluxes_mod.h): reconstruction and limiter at both ends, then the
+// edge's x and y half-range fluxes added to the directional sums Sx_d, Sy_d.
+// Every edge lies in exactly one of xpos / xneg and one of ypos / yneg,
+// except an edge with dels == 0 (deln == 0), which lies in both: the sign is
+// chosen per lane and the difference added with 0 / 1 weights, so the lanes
+// of a warp do not diverge on their edges' sub-stencils; the both-sides
+// edges take one extra (rare) pass.  Direction bits: 1 xpos, 2 xneg, 4 ypos,
+// 8 yneg (the wall holds only yneg, the outer boundary only ypos).
+__device__ __forceinline__ void flux_edge(int f, float nx, float ny, const float qi[4], const float dxi[4],
+                                          const float dyi[4], const float mxi[4], const float mni[4], float e2i,
+                                          float4 g, float2 sw, unsigned dir, const float qk[4], const float dxk[4],
+                                          const float dyk[4], const float mxk[4], const float mnk[4], float e2k,
+                                          float sx[4][4], float sy[4][4])
+{
+    float Pi[4], Pk[4];
+    edge_states32(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, e2k, Pi, Pk);
+    Kin<float> ki, kk;
+    kin_prep<float>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
+    kin_prep<float>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
+    float Gi[4], Gk[4];
+    // x: xpos (s1 = +1) when bit 1 is set, else xneg
+    const bool xp = dir & kXpos;
+    x_flux(f, ki, xp ? 1.0f : -1.0f, Gi);
+    x_flux(f, kk, xp ? 1.0f : -1.0f, Gk);
+    {
+        const float a0 = xp ? sw.x : 0.f, a1 = xp ? 0.f : sw.x, b0 = xp ? sw.y : 0.f, b1 = xp ? 0.f : sw.y;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const float dG = Gk[r] - Gi[r];
+            sx[0][r] = fmaf(a0, dG, sx[0][r]);
+            sx[1][r] = fmaf(a1, dG, sx[1][r]);
+            sy[0][r] = fmaf(b0, dG, sy[0][r]);
+            sy[1][r] = fmaf(b1, dG, sy[1][r]);
+        }
+    }
+    if ((dir & (kXpos | kXneg)) == (kXpos | kXneg)) {
+        x_flux(f, ki, -1.0f, Gi);
+        x_flux(f, kk, -1.0f, Gk);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const float dG = Gk[r] - Gi[r];
+            sx[1][r] = fmaf(sw.x, dG, sx[1][r]);
+            sy[1][r] = fmaf(sw.y, dG, sy[1][r]);
+        }
+    }
+    // y: ypos (s2 = +1) when bit 4 is set, else yneg
+    const bool yp = dir & kYpos;
+    flux_y(ki, yp ? 1.0f : -1.0f, Gi);
+    flux_y(kk, yp ? 1.0f : -1.0f, Gk);
+    {
+        const float a2 = yp ? sw.x : 0.f, a3 = yp ? 0.f : sw.x, b2 = yp ? sw.y : 0.f, b3 = yp ? 0.f : sw.y;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const float dG = Gk[r] - Gi[r];
+            sx[2][r] = fmaf(a2, dG, sx[2][r]);
+            sx[3][r] = fmaf(a3, dG, sx[3][r]);
+            sy[2][r] = fmaf(b2, dG, sy[2][r]);
+            sy[3][r] = fmaf(b3, dG, sy[3][r]);
+        }
+    }
+    if ((dir & (kYpos | kYneg)) == (kYpos | kYneg)) {
+        flux_y(ki, -1.0f, Gi);
+        flux_y(kk, -1.0f, Gk);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const float dG = Gk[r] - Gi[r];
+            sx[3][r] = fmaf(sw.x, dG, sx[3][r]);
+            sy[3][r] = fmaf(sw.y, dG, sy[3][r]);
+        }
+    }
+}
+
+// Edge geometry of edge e: {delx, dely, w delx, w dely} and {dels w, deln w}.
+template <bool UW>
+__device__ __forceinline__ void edge_geo(const DevCloud &c, long long e, float nx, float ny, float4 &g, float2 &sw)
+{
+    if (UW) {
+        // dels, deln of the point's (t, n) frame (interior_fluxes_mod.h:53-54), weight 1
+        const float2 d = c.e_xy32[e];
+        g = make_float4(d.x, d.y, 0.f, 0.f);
+        sw = make_float2(d.x * ny - d.y * nx, d.x * nx + d.y * ny);
+    } else {
+        g = c.e_geo32[e];
+        sw = c.e_sn32[e];
+    }
+}
+
+// F = delta * sum_d (a_d Sx_d + b_d Sy_d): the four solves and
+// flux_residual_mod.h's sum (with the wall's 2 delta) in FP64, then the SSPRK
+// stage, q and the wave speed of the new state.  Returns res_sqr.
+__device__ __forceinline__ double flux_tail(const DevCloud &c, const CaseConst &K, int i, int f, double2 nn,
+                                            const float sx[4][4], const float sy[4][4],
+                                            const float *__restrict__ delta, const double4_32a *__restrict__ prim,
+                                            const double4_32a *__restrict__ prim_old,
+                                            double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
+                                            float *__restrict__ cs_next, int rk)
+{
+    double2 cf[4];
+#pragma unroll
+    for (int d = 0; d < 4; d++) cf[d] = c.fcoef[4 * i + d];
+    const double dl = f2d(delta[i]);
+    double F[4], P[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        double acc = 0.0;
+#pragma unroll
+        for (int d = 0; d < 4; d++) {
+            acc = fma(cf[d].x, f2d(sx[d][r]), acc);
+            acc = fma(cf[d].y, f2d(sy[d][r]), acc);
+        }
+        F[r] = dl * acc;
+    }
+    ld4(prim[i], P);
+    const double r2 = stage_update_fast(K, f, nn.x, nn.y, P, prim_old + i, F, rk);
+    prim_next[i] = mk4(P);
+    float Q[4];
+    q_of(P, Q);
+    q_next[i] = mk4(Q);
+    if (cs_next) cs_next[i] = wave_speed32(P);
+    return r2;
+}
+
 // Fused stage of one point: FP32 edge work, FP64 solve / residual / update.
 // Returns the point's res_sqr.
 template <bool UW>
@@ -260,15 +614,7 @@ __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst 
         const int k = c.e_nbr[e];
         float4 g;
         float2 sw;
-        if (UW) {
-            // dels, deln of the point's (t, n) frame (interior_fluxes_mod.h:53-54), weight 1
-            const float2 d = c.e_xy32[e];
-            g = make_float4(d.x, d.y, 0.f, 0.f);
-            sw = make_float2(d.x * ny - d.y * nx, d.x * nx + d.y * ny);
-        } else {
-            g = c.e_geo32[e];
-            sw = c.e_sn32[e];
-        }
+        edge_geo<UW>(c, e, nx, ny, g, sw);
         const unsigned dir = c.e_dir[e];
         float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
         ld4(q[k], qk);
@@ -276,52 +622,88 @@ __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst 
         ld4(dq[2 * k + 1], dyk);
         ld4(qm[2 * k], mxk);
         ld4(qm[2 * k + 1], mnk);
-        float Pi[4], Pk[4];
-        edge_states<float>(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, c.eps2_32[k], Pi, Pk);
-        Kin<float> ki, kk;
-        kin_prep<float>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
-        kin_prep<float>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
-#define QLSKUM_ACC32(D)                                                       \
-        if (dir & (1u << D)) {                                                \
-            float Gi[4], Gk[4];                                               \
-            dir_flux<float, D>(f, ki, Gi);                                    \
-            dir_flux<float, D>(f, kk, Gk);                                    \
-            _Pragma("unroll") for (int r = 0; r < 4; r++) {                   \
-                sx[D][r] += (Gk[r] - Gi[r]) * sw.x;                           \
-                sy[D][r] += (Gk[r] - Gi[r]) * sw.y;                           \
-            }                                                                 \
-        }
-        QLSKUM_ACC32(0)
-        QLSKUM_ACC32(1)
-        QLSKUM_ACC32(2)
-        QLSKUM_ACC32(3)
-#undef QLSKUM_ACC32
+        flux_edge(f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, sw, dir, qk, dxk, dyk, mxk, mnk, c.eps2_32[k], sx, sy);
     }
-    // F = delta * sum_d (a_d Sx_d + b_d Sy_d): the four solves and
-    // flux_residual_mod.h's sum (with the wall's 2 delta) in FP64.
-    double2 cf[4];
-#pragma unroll
-    for (int d = 0; d < 4; d++) cf[d] = c.fcoef[4 * i + d];
-    const double dl = f2d(delta[i]);
-    double F[4], P[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        double acc = 0.0;
-#pragma unroll
-        for (int d = 0; d < 4; d++) {
-            acc = fma(cf[d].x, f2d(sx[d][r]), acc);
-            acc = fma(cf[d].y, f2d(sy[d][r]), acc);
-        }
-        F[r] = dl * acc;
+    return flux_tail(c, K, i, f, nn, sx, sy, delta, prim, prim_old, prim_next, q_next, cs_next, rk);
+}
+
+// The same with the next edge's gathers in flight during the current edge's
+// arithmetic: edge j + 1's neighbour data (q, dq, qm: five float4, and the
+// limiter's eps^2) goes by cp.async into a two-slot ring of the thread's own
+// shared memory ([2][5][B] float4 and [2][B] float), its neighbour index is
+// loaded one edge earlier still, and its geometry one edge ahead into
+// registers.  Same arithmetic in the same edge order as flux_point.
+template <int B, bool UW>
+__device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseConst &K, int i, int t,
+                                                float4 *ring, float *reps, const float4 *__restrict__ q,
+                                                const float4 *__restrict__ dq, const float4 *__restrict__ qm,
+                                                const float *__restrict__ delta,
+                                                const double4_32a *__restrict__ prim,
+                                                const double4_32a *__restrict__ prim_old,
+                                                double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
+                                                float *__restrict__ cs_next, int rk)
+{
+    const int f = c.flag[i];
+    const double2 nn = c.nrm[i];
+    const float nx = d2f(nn.x), ny = d2f(nn.y);
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    auto issue = [&](int j, int k) {
+        float4 *slot = ring + (j & 1) * 5 * B + t;
+        cp_async16(slot, q + k);
+        cp_async16(slot + B, dq + 2 * k);
+        cp_async16(slot + 2 * B, dq + 2 * k + 1);
+        cp_async16(slot + 3 * B, qm + 2 * k);
+        cp_async16(slot + 4 * B, qm + 2 * k + 1);
+        cp_async4(reps + (j & 1) * B + t, c.eps2_32 + k);
+    };
+    int kn = 0;
+    float4 gn = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 swn = make_float2(0.f, 0.f);
+    unsigned dn = 0;
+    if (nb > 0) {
+        issue(0, c.e_nbr[base]);
+        edge_geo<UW>(c, base, nx, ny, gn, swn);
+        dn = c.e_dir[base];
     }
-    ld4(prim[i], P);
-    const double r2 = stage_update_fast(K, f, nn.x, nn.y, P, prim_old + i, F, rk);
-    prim_next[i] = mk4(P);
-    float Q[4];
-    q_of(P, Q);
-    q_next[i] = mk4(Q);
-    if (cs_next) cs_next[i] = wave_speed32(P);
-    return r2;
+    cp_commit();
+    if (nb > 1) kn = c.e_nbr[base + 32];
+    float qi[4], dxi[4], dyi[4], mxi[4], mni[4];
+    ld4(q[i], qi);
+    ld4(dq[2 * i], dxi);
+    ld4(dq[2 * i + 1], dyi);
+    ld4(qm[2 * i], mxi);
+    ld4(qm[2 * i + 1], mni);
+    const float e2i = c.eps2_32[i];
+    float sx[4][4], sy[4][4];
+#pragma unroll
+    for (int d = 0; d < 4; d++)
+#pragma unroll
+        for (int r = 0; r < 4; r++) { sx[d][r] = 0.f; sy[d][r] = 0.f; }
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const float4 g = gn;
+        const float2 sw = swn;
+        const unsigned dir = dn;
+        if (j + 1 < nb) {
+            issue(j + 1, kn);
+            edge_geo<UW>(c, e + 32, nx, ny, gn, swn);
+            dn = c.e_dir[e + 32];
+        }
+        cp_commit();
+        if (j + 2 < nb) kn = c.e_nbr[e + 64];
+        cp_wait<1>();
+        const float4 *slot = ring + (j & 1) * 5 * B + t;
+        float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
+        ld4(slot[0], qk);
+        ld4(slot[B], dxk);
+        ld4(slot[2 * B], dyk);
+        ld4(slot[3 * B], mxk);
+        ld4(slot[4 * B], mnk);
+        const float e2k = reps[(j & 1) * B + t];
+        flux_edge(f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, sw, dir, qk, dxk, dyk, mxk, mnk, e2k, sx, sy);
+    }
+    return flux_tail(c, K, i, f, nn, sx, sy, delta, prim, prim_old, prim_next, q_next, cs_next, rk);
 }
 
 // ---------------------------------------------------- single-case kernels
@@ -356,6 +738,30 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseCon
     const int i = blockIdx.x * BLOCK + threadIdx.x;
     double r2 = 0.0;
     if (i < c.n) r2 = flux_point<UW>(c, K, i, q, dq, qm, delta, prim, prim_old, prim_next, q_next, cs_next, rk);
+    if (psum) block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
+}
+
+// Staged-gather form of k_flux_update; static shared ring of the block.
+template <int BLOCK, int MINB, bool UW>
+__global__ void __launch_bounds__(BLOCK, MINB) k_flux_update_st(DevCloud c, CaseConst K, const float4 *__restrict__ q,
+                                                          const float4 *__restrict__ dq,
+                                                          const float4 *__restrict__ qm,
+                                                          const float *__restrict__ delta,
+                                                          const double4_32a *__restrict__ prim,
+                                                          const double4_32a *__restrict__ prim_old,
+                                                          double4_32a *__restrict__ prim_next,
+                                                          float4 *__restrict__ q_next, float *__restrict__ cs_next,
+                                                          int rk, double *__restrict__ psum,
+                                                          double *__restrict__ pmax)
+{
+    __shared__ float4 ring[2 * 5 * BLOCK];
+    __shared__ float reps[2 * BLOCK];
+    const int t = threadIdx.x;
+    const int i = blockIdx.x * BLOCK + t;
+    double r2 = 0.0;
+    if (i < c.n)
+        r2 = flux_point_st<BLOCK, UW>(c, K, i, t, ring, reps, q, dq, qm, delta, prim, prim_old, prim_next, q_next,
+                                      cs_next, rk);
     if (psum) block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
 }
 
@@ -487,32 +893,104 @@ void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, float4
     QLSKUM_LAUNCHED(L);
 }
 
+// Staged variants (threads per block, gather depth D): Launch::staged = 1..4.
+const int kStagedVariants = 4;
+
+#define QLSKUM_STAGED_SWITCH(V, ...)                                                             \
+    switch (V) {                                                                                 \
+    case 1: { constexpr int B_ = 128, D_ = 2; __VA_ARGS__; } break;                             \
+    case 2: { constexpr int B_ = 128, D_ = 4; __VA_ARGS__; } break;                             \
+    case 3: { constexpr int B_ = 256, D_ = 3; __VA_ARGS__; } break;                             \
+    default: { constexpr int B_ = 64, D_ = 4; __VA_ARGS__; } break;                             \
+    }
+
+int staged_block(int v)
+{
+    int b = 0;
+    QLSKUM_STAGED_SWITCH(v, b = B_)
+    return b;
+}
+
+int staged_depth(int v)
+{
+    int d = 0;
+    QLSKUM_STAGED_SWITCH(v, d = D_)
+    return d;
+}
+
+template <typename K> static bool allow_smem(K kernel, size_t bytes)
+{
+    if (bytes <= 48 * 1024) return true;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess;
+}
+
+int staged_variants(const DevCloud &c)
+{
+    int usable = 0;
+    for (int v = 1; v <= kStagedVariants; v++) {
+        bool ok = true;
+        QLSKUM_STAGED_SWITCH(v,
+            if (c.unit_w) {
+                ok = allow_smem(k_q_inner_st<B_, D_, true>, staged_bytes(B_, D_, 3, c.max_nb, true)) &&
+                     allow_smem(k_q_derivatives_st<B_, D_, true>, staged_bytes(B_, D_, 2, c.max_nb, true));
+            } else {
+                ok = allow_smem(k_q_inner_st<B_, D_, false>, staged_bytes(B_, D_, 3, c.max_nb, false)) &&
+                     allow_smem(k_q_derivatives_st<B_, D_, false>, staged_bytes(B_, D_, 2, c.max_nb, false));
+            })
+        if (!ok) break;
+        usable = v;
+    }
+    cudaGetLastError();  // a refused limit is not an error of the next launch
+    return usable;
+}
+
 void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *dq, float4 *qm, const float *cspeed,
                    float *delta, float cfl)
 {
-    if (c.unit_w)
+    if (L.staged > 0) {
+        QLSKUM_STAGED_SWITCH(L.staged,
+            if (c.unit_w)
+                k_q_derivatives_st<B_, D_, true><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 2, c.max_nb, true),
+                                                   L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
+            else
+                k_q_derivatives_st<B_, D_, false><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 2, c.max_nb, false),
+                                                    L.stream>>>(c, q, dq, qm, cspeed, delta, cfl))
+    } else if (c.unit_w) {
         k_q_derivatives<true><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
-    else
+    } else {
         k_q_derivatives<false><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
+    }
     QLSKUM_LAUNCHED(L);
 }
 
 void q_inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, float4 *dq_out)
 {
-    if (c.unit_w)
+    if (L.staged > 0) {
+        QLSKUM_STAGED_SWITCH(L.staged,
+            if (c.unit_w)
+                k_q_inner_st<B_, D_, true><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 3, c.max_nb, true),
+                                             L.stream>>>(c, q, dq_in, dq_out);
+            else
+                k_q_inner_st<B_, D_, false><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 3, c.max_nb, false),
+                                              L.stream>>>(c, q, dq_in, dq_out))
+    } else if (c.unit_w) {
         k_q_inner<true><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq_in, dq_out);
-    else
+    } else {
         k_q_inner<false><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq_in, dq_out);
+    }
     QLSKUM_LAUNCHED(L);
 }
 
 // Launch-shape variants of the fused kernel (threads per block, minimum
-// resident blocks per SM -> register cap), picked by the host's autotuner.
-const int kFluxVariants = 4;
-static const int kFluxBlock[kFluxVariants] = {128, 128, 64, 256};
+// resident blocks per SM -> register cap; 4..7 the staged-gather form),
+// picked by the host's autotuner.
+const int kFluxVariants = 8;
+static const int kFluxBlock[kFluxVariants] = {128, 128, 64, 256, 128, 128, 64, 256};
+static const int kFluxMinBlocks[kFluxVariants] = {4, 5, 8, 2, 4, 5, 8, 2};
 
 int flux_variants() { return kFluxVariants; }
 int flux_block(int v) { return kFluxBlock[v]; }
+int flux_min_blocks(int v) { return kFluxMinBlocks[v]; }
 
 void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const float4 *q, const float4 *dq,
                  const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
@@ -529,13 +1007,29 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
                                                                        prim_old, prim_next, q_next,        \
                                                                        cspeed_next, rk, R.partial_sum,     \
                                                                        R.partial_max)
+#define QLSKUM_FLUX_ST(B, MB)                                                                               \
+    if (c.unit_w)                                                                                           \
+        k_flux_update_st<B, MB, true><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,   \
+                                                                         prim_old, prim_next, q_next,      \
+                                                                         cspeed_next, rk, R.partial_sum,   \
+                                                                         R.partial_max);                   \
+    else                                                                                                    \
+        k_flux_update_st<B, MB, false><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,  \
+                                                                          prim_old, prim_next, q_next,     \
+                                                                          cspeed_next, rk, R.partial_sum,  \
+                                                                          R.partial_max)
     switch (variant) {
     case 1: QLSKUM_FLUX(128, 5); break;
     case 2: QLSKUM_FLUX(64, 8); break;
     case 3: QLSKUM_FLUX(256, 2); break;
+    case 4: QLSKUM_FLUX_ST(128, 4); break;
+    case 5: QLSKUM_FLUX_ST(128, 5); break;
+    case 6: QLSKUM_FLUX_ST(64, 8); break;
+    case 7: QLSKUM_FLUX_ST(256, 2); break;
     default: QLSKUM_FLUX(128, 4); break;
     }
 #undef QLSKUM_FLUX
+#undef QLSKUM_FLUX_ST
     QLSKUM_LAUNCHED(L);
 }
 

@@ -125,6 +125,9 @@ void qlskum_dbg_stage_update_vjp(int f, double nx, double ny, const double *Pin,
                           out[15]);
 }
 
+// the FP32 erf of the mixed form's kinetic moments (host build of the same source)
+float qlskum_dbg_erf32(float x) { return erf_e<float>(x, std::exp(-x * x)); }
+
 double qlskum_dbg_wave_speed(const double *P) { return wave_speed(P); }
 
 void qlskum_dbg_wave_speed_vjp(const double *P, double bc, double *bP)

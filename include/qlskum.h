@@ -159,11 +159,22 @@ void *qlskum_stream(qlskum_handle *h);
 long long qlskum_launch_count(const qlskum_handle *h);
 
 /* Launch shape in use: threads per block and minimum resident blocks per SM
- * (register cap) of the fused flux + update kernel, and threads per block of
- * the gradient / inner-loop kernels.  With params.block_size == 0 the mixed
- * form picks them on its first fused iteration by timing the candidates on
- * the handle's own cloud (the autotuner). */
-qlskum_status qlskum_get_launch_config(qlskum_handle *h, int *flux_block, int *flux_min_blocks, int *point_block);
+ * (register cap) of the fused flux + update kernel, threads per block of the
+ * gradient / inner-loop kernels and their gather depth (0: one neighbour
+ * gather per edge in turn; D > 0: edge list staged in shared memory and the
+ * neighbours' data streamed with cp.async D edges ahead).  With
+ * params.block_size == 0 the mixed form picks them on its first fused
+ * iteration by timing the candidates on the handle's own cloud (the
+ * autotuner).  Any pointer may be NULL. */
+qlskum_status qlskum_get_launch_config(qlskum_handle *h, int *flux_block, int *flux_min_blocks, int *point_block,
+                                       int *gather_depth);
+/* Pin the mixed form's launch shape instead of autotuning it: flux_variant in
+ * 0 .. 3 (threads x min blocks 128x4, 128x5, 64x8, 256x2), point_block one of
+ * 64 / 128 / 256 / 512 for the per-edge gather form, staged 0 (that form) or
+ * 1 .. 4 (staged gathers: 128 threads depth 2, 128 / 4, 256 / 3, 64 / 4).
+ * QLSKUM_ERR_UNSUPPORTED if a staged variant does not fit the device's
+ * shared memory for this cloud's neighbour count. */
+qlskum_status qlskum_set_launch_config(qlskum_handle *h, int flux_variant, int point_block, int staged);
 
 /* Per-kernel device time from CUDA events recorded on the handle's stream.
  * While enabled, qlskum_q_lskum launches each iteration's kernels one by one

@@ -211,3 +211,16 @@ def test_wave_speed(L):
             L.qlskum_dbg_wave_speed_vjp(P(z), float(w[0]), P(o))
             return o
         check(f, vj, x, 1, rng)
+
+
+def test_fp32_erf_error_bound(L):
+    """The mixed form's erf (Abramowitz & Stegun 7.1.26 from the exp(-x^2) the
+    kinetic moments already hold): within its published 1.5e-7 absolute bound
+    plus FP32 rounding of the evaluation, over the whole real line."""
+    import math
+    L.qlskum_dbg_erf32.argtypes = [C.c_float]
+    L.qlskum_dbg_erf32.restype = C.c_float
+    xs = np.concatenate([np.linspace(-6, 6, 4001), np.geomspace(1e-8, 1, 200), -np.geomspace(1e-8, 1, 200)])
+    err = max(abs(L.qlskum_dbg_erf32(float(x)) - math.erf(float(np.float32(x)))) for x in xs)
+    assert err < 1.5e-7 + 2.4e-7, err
+    assert L.qlskum_dbg_erf32(0.0) == 0.0
