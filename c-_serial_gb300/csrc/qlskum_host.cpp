@@ -480,10 +480,12 @@ qlskum_status tune(qlskum_handle *h)
     h->L.staged = best_L.staged;
     mixed::q_derivatives(h->L, c, S.q[0], S.dq[0], S.qm, S.cspeed, S.delta, (float)h->K.cfl);
     best = 1e30f;
+    Reduce none = h->R;  // stage 1 writes no residual partials
+    none.partial_sum = none.partial_max = nullptr;
     for (int v = 0; v < mixed::flux_variants(); v++) {
         float ms = time3([&] {
             mixed::flux_update(h->L, c, h->K, S.q[0], S.dq[0], S.qm, S.delta, h->s64.prim[o], h->s64.prim[o],
-                               h->s64.prim[x], S.q[1], nullptr, 1, h->R, v);
+                               h->s64.prim[x], S.q[1], nullptr, 1, none, v);
         });
         if (ms < best) { best = ms; h->flux_variant = v; }
     }
@@ -660,7 +662,7 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
     std::vector<float> eps2_32(G.np, 0.0f);
     std::vector<double4_32a> ggeo(G.np, make_double4_32a(0, 0, 0, 0));
     std::vector<double4_32a> fgeo((size_t)G.np * 4, make_double4_32a(0, 0, 0, 0));
-    std::vector<double2> fcoef((size_t)G.np * 4, make_double2(0, 0));
+    std::vector<float2> e_w32(ne, make_float2(0, 0)), e_w32b(ne, make_float2(0, 0));
     std::vector<double4_32a> gcoef(G.np, make_double4_32a(0, 0, 0, 0));
     std::vector<float2> e_xy32(ne, make_float2(0, 0));
     const bool unit_w = p->power == 0.0;
@@ -682,6 +684,7 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
         static const bool used[3][4] = {{true, true, false, true}, {true, true, true, true}, {true, true, true, false}};
         const int fl = c->flag_1[i];
         const double scale = fl == kWall ? 2.0 : 1.0;  // flux_residual_mod.h:29
+        double ca[4], cb[4];
         for (int d = 0; d < 4; d++) {
             const double *F = &P.fgeo[((size_t)i * 4 + d) * 4];
             fgeo[(size_t)pp * 4 + d] = make_double4_32a(F[0], F[1], F[2], F[3]);
@@ -691,7 +694,8 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
                 if (d < 2) { a = scale * F[1] * F[3]; b = -scale * F[2] * F[3]; }
                 else { a = -scale * F[2] * F[3]; b = scale * F[0] * F[3]; }
             }
-            fcoef[(size_t)pp * 4 + d] = make_double2(a, b);
+            ca[d] = a;
+            cb[d] = b;
         }
         for (int r = 0; r < c->nbhs[i]; r++) {
             const size_t e = (size_t)(sbase[pp >> 5] + 32LL * r + (pp & 31));
@@ -706,6 +710,16 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
             e_geo32[e] = make_float4((float)P.geo[4 * src], (float)P.geo[4 * src + 1], (float)P.geo[4 * src + 2],
                                      (float)P.geo[4 * src + 3]);
             e_sn32[e] = make_float2((float)P.sn[2 * src], (float)P.sn[2 * src + 1]);
+            // per-edge solve weights c_ed = a_d dels_w + b_d deln_w (FP64, then FP32)
+            {
+                const unsigned bits = P.edge_dir[src];
+                const double sw = P.sn[2 * src], nw = P.sn[2 * src + 1];
+                auto cw = [&](int d) { return (float)(ca[d] * sw + cb[d] * nw); };
+                const int dx = (bits & kXpos) ? 0 : 1, dy = (bits & kYpos) ? 2 : 3;
+                e_w32[e] = make_float2(cw(dx), cw(dy));
+                e_w32b[e] = make_float2((bits & (kXpos | kXneg)) == (kXpos | kXneg) ? cw(1) : 0.f,
+                                        (bits & (kYpos | kYneg)) == (kYpos | kYneg) ? cw(3) : 0.f);
+            }
         }
     }
 
@@ -731,7 +745,7 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
     float4 *d_egeo32 = nullptr;
     float2 *d_esn32 = nullptr;
     float *d_eps32 = nullptr, *d_edist32 = nullptr;
-    double2 *d_fcoef = nullptr;
+    float2 *d_ew32 = nullptr, *d_ew32b = nullptr;
     double4_32a *d_gcoef = nullptr;
     float2 *d_exy32 = nullptr;
     if (need_mixed) {
@@ -743,18 +757,19 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
         }
         d_eps32 = A.alloc<float>(G.np);
         d_edist32 = A.alloc<float>(ne);
-        d_fcoef = A.alloc<double2>((size_t)G.np * 4);
+        d_ew32 = A.alloc<float2>(ne);
+        d_ew32b = A.alloc<float2>(ne);
         d_gcoef = A.alloc<double4_32a>(G.np);
     }
     up(d_flag, flag); up(d_nb, nbh); up(d_sb, sbase); up(d_enbr, e_nbr); up(d_egeo, e_geo); up(d_esn, e_sn);
     up(d_edist, e_dist); up(d_edir, e_dir); up(d_nrm, nrm); up(d_eps2, eps2); up(d_ggeo, ggeo); up(d_fgeo, fgeo);
-    up(d_egeo32, e_geo32); up(d_esn32, e_sn32); up(d_eps32, eps2_32); up(d_edist32, e_dist32); up(d_fcoef, fcoef);
+    up(d_egeo32, e_geo32); up(d_esn32, e_sn32); up(d_eps32, eps2_32); up(d_edist32, e_dist32); up(d_ew32, e_w32); up(d_ew32b, e_w32b);
     up(d_gcoef, gcoef); up(d_exy32, e_xy32);
     DevCloud &dc = G.dc;
     dc.n = n; dc.np = G.np; dc.flag = d_flag; dc.nbhs = d_nb; dc.slice_base = d_sb; dc.e_nbr = d_enbr;
     dc.e_geo = d_egeo; dc.e_sn = d_esn; dc.e_dist = d_edist; dc.e_dir = d_edir; dc.nrm = d_nrm; dc.eps2 = d_eps2;
     dc.ggeo = d_ggeo; dc.fgeo = d_fgeo; dc.e_geo32 = d_egeo32; dc.e_sn32 = d_esn32; dc.eps2_32 = d_eps32;
-    dc.e_dist32 = d_edist32; dc.fcoef = d_fcoef; dc.gcoef = d_gcoef; dc.unit_w = unit_w ? 1 : 0; dc.e_xy32 = d_exy32;
+    dc.e_dist32 = d_edist32; dc.e_w32 = d_ew32; dc.e_w32b = d_ew32b; dc.gcoef = d_gcoef; dc.unit_w = unit_w ? 1 : 0; dc.e_xy32 = d_exy32;
     dc.max_nb = 0;
     for (int i = 0; i < n; i++) dc.max_nb = std::max(dc.max_nb, c->nbhs[i]);
 
@@ -885,7 +900,7 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
         h->s32.cspeed = A.alloc<float>(h->np);
     }
     h->R.blocks = (n + 127) / 128;
-    h->R.max_blocks = (n + 63) / 64;
+    h->R.max_blocks = (n + 31) / 32;  // one partial per block of the smallest launch shape (32 threads)
     h->R.partial_sum = A.alloc<double>(h->R.max_blocks);
     h->R.partial_max = A.alloc<double>(h->R.max_blocks);
     h->R.res_old = A.alloc<double>(1);

@@ -45,13 +45,20 @@ struct DevCloud {
     const float2 *e_sn32 = nullptr;          // dels*w, deln*w
     const float *e_dist32 = nullptr;         // |r_k - r_i|
     const float *eps2_32 = nullptr;
-    // Mixed form: the four directional 2x2 solves and their combination into
-    // the flux residual folded into one coefficient pair per direction,
-    // F = delta * sum_d (a_d * Sx_d + b_d * Sy_d) with Sx_d = sum dG dels w,
-    // Sy_d = sum dG deln w; a_d, b_d carry 1/det, the x / y row of the
-    // inverse, the wall's factor 2 and zero for directions a class does not
-    // use.  FP64, [np][4].
-    const double2 *fcoef = nullptr;
+    // Mixed form: the four directional 2x2 solves and their sum into the flux
+    // residual folded into per-edge weights.  With Sx_d = sum dG dels w and
+    // Sy_d = sum dG deln w over the edges of sub-stencil d, the residual is
+    // F = delta * sum_d (a_d Sx_d + b_d Sy_d), a_d, b_d the x / y row of the
+    // inverse moment matrix (1/det included, the wall's factor 2, zero for a
+    // direction the class does not use); so F = delta * sum_e sum_{d ∋ e}
+    // c_ed dG_ed with c_ed = a_d dels_w + b_d deln_w, computed on the host in
+    // FP64 (where the near-singular inverse meets the edge vector) and stored
+    // in FP32: {c of the edge's x half-range (xpos if it lies there, else
+    // xneg), c of its y half-range (ypos, else yneg)} per edge, and the same
+    // for the second half-range of an edge with dels == 0 / deln == 0 (which
+    // lies in both; zero otherwise).
+    const float2 *e_w32 = nullptr;
+    const float2 *e_w32b = nullptr;
     // Mixed form, gradient and inner loop: the 2x2 solve as coefficients
     // {syy/det, sxy/det, sxx/det} (FP64), dq_x = Sx a - Sy b, dq_y = Sy c - Sx b.
     const double4_32a *gcoef = nullptr;
@@ -131,7 +138,7 @@ struct Reduce {
     int *status = nullptr;                   // [1] 0 ok, 1 non-finite residual
     int capacity = 0;
     int blocks = 0;                          // partials written by the last stage kernel
-    int max_blocks = 0;                      // partials allocated (n / 64 rounded up)
+    int max_blocks = 0;                      // partials allocated (n / 32 rounded up)
 };
 
 struct Launch {

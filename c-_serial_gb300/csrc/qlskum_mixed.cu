@@ -1,14 +1,17 @@
 // Mixed-precision kernels: q variables, the Venkatakrishnan limiter, the
 // reconstruction and the kinetic split fluxes in FP32; the 2x2
 // least-squares solves (their determinants are near-singular on anisotropic
-// wall stencils), the flux residual, the SSPRK update and the residual sum in
-// FP64.  Same algorithm, edge order and data layout as the FP64 kernels
+// wall stencils: the gradient's on the device, the flux's folded into
+// per-edge weights on the host), the flux residual's time-step scaling, the
+// SSPRK update and the residual sum in FP64.  Same algorithm, edge order and data layout as the FP64 kernels
 // (qlskum_fp64.cu); q, dq and qm are stored in FP32, which halves the bytes
 // gathered per neighbour.  Built with FMA contraction on.
 //
 // On GB300 FP64 runs at about 1/64 of the FP32 rate, so the O(points) FP64
-// work is kept to a minimum: the four directional solves and their sum are
-// one FMA chain over precomputed coefficient pairs (DevCloud::fcoef), the
+// work is kept to a minimum: the four directional solves are linear in the
+// edge sums and are folded, in FP64 on the host, into one weight per edge and
+// half-range (DevCloud::e_w32), so the near-singular inverses never meet FP32
+// arithmetic and the kernel adds weighted flux differences; the
 // conserved-variable update has no FP64 division (one reciprocal from an FP32
 // seed and two Newton steps), and the local time step and its wave speed are
 // FP32 (they only set the pseudo-time step, not the steady state).
@@ -460,18 +463,19 @@ __device__ __forceinline__ void x_flux(int f, const Kin<float> &k, float s1, flo
 
 // Flux contribution of one edge (interior_fluxes_mod.h, wall_fluxes_mod.h,
 // outer_fluxes_mod.h): reconstruction and limiter at both ends, then the
-// edge's x and y half-range fluxes added to the directional sums Sx_d, Sy_d.
-// Every edge lies in exactly one of xpos / xneg and one of ypos / yneg,
-// except an edge with dels == 0 (deln == 0), which lies in both: the sign is
-// chosen per lane and the difference added with 0 / 1 weights, so the lanes
-// of a warp do not diverge on their edges' sub-stencils; the both-sides
-// edges take one extra (rare) pass.  Direction bits: 1 xpos, 2 xneg, 4 ypos,
-// 8 yneg (the wall holds only yneg, the outer boundary only ypos).
-__device__ __forceinline__ void flux_edge(int f, float nx, float ny, const float qi[4], const float dxi[4],
-                                          const float dyi[4], const float mxi[4], const float mni[4], float e2i,
-                                          float4 g, float2 sw, unsigned dir, const float qk[4], const float dxk[4],
-                                          const float dyk[4], const float mxk[4], const float mnk[4], float e2k,
-                                          float sx[4][4], float sy[4][4])
+// edge's x and y half-range fluxes, each difference Gk - Gi weighted by the
+// edge's folded solve weight (DevCloud::e_w32) and added to acc.  Every edge
+// lies in exactly one of xpos / xneg and one of ypos / yneg, except an edge
+// with dels == 0 (deln == 0), which lies in both: the sign is chosen per
+// lane, so the lanes of a warp do not diverge on their edges' sub-stencils;
+// the both-sides edges take one extra (rare) pass with the second weight.
+// Direction bits: 1 xpos, 2 xneg, 4 ypos, 8 yneg (the wall holds only yneg,
+// the outer boundary only ypos).
+__device__ __forceinline__ void flux_edge(const DevCloud &c, long long e, int f, float nx, float ny,
+                                          const float qi[4], const float dxi[4], const float dyi[4],
+                                          const float mxi[4], const float mni[4], float e2i, float4 g, float2 w,
+                                          unsigned dir, const float qk[4], const float dxk[4], const float dyk[4],
+                                          const float mxk[4], const float mnk[4], float e2k, float acc[4])
 {
     float Pi[4], Pk[4];
     edge_states32(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, e2k, Pi, Pk);
@@ -480,97 +484,62 @@ __device__ __forceinline__ void flux_edge(int f, float nx, float ny, const float
     kin_prep<float>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
     float Gi[4], Gk[4];
     // x: xpos (s1 = +1) when bit 1 is set, else xneg
-    const bool xp = dir & kXpos;
-    x_flux(f, ki, xp ? 1.0f : -1.0f, Gi);
-    x_flux(f, kk, xp ? 1.0f : -1.0f, Gk);
-    {
-        const float a0 = xp ? sw.x : 0.f, a1 = xp ? 0.f : sw.x, b0 = xp ? sw.y : 0.f, b1 = xp ? 0.f : sw.y;
+    const float s1 = (dir & kXpos) ? 1.0f : -1.0f;
+    x_flux(f, ki, s1, Gi);
+    x_flux(f, kk, s1, Gk);
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const float dG = Gk[r] - Gi[r];
-            sx[0][r] = fmaf(a0, dG, sx[0][r]);
-            sx[1][r] = fmaf(a1, dG, sx[1][r]);
-            sy[0][r] = fmaf(b0, dG, sy[0][r]);
-            sy[1][r] = fmaf(b1, dG, sy[1][r]);
-        }
-    }
-    if ((dir & (kXpos | kXneg)) == (kXpos | kXneg)) {
-        x_flux(f, ki, -1.0f, Gi);
-        x_flux(f, kk, -1.0f, Gk);
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const float dG = Gk[r] - Gi[r];
-            sx[1][r] = fmaf(sw.x, dG, sx[1][r]);
-            sy[1][r] = fmaf(sw.y, dG, sy[1][r]);
-        }
-    }
+    for (int r = 0; r < 4; r++) acc[r] = fmaf(w.x, Gk[r] - Gi[r], acc[r]);
     // y: ypos (s2 = +1) when bit 4 is set, else yneg
-    const bool yp = dir & kYpos;
-    flux_y(ki, yp ? 1.0f : -1.0f, Gi);
-    flux_y(kk, yp ? 1.0f : -1.0f, Gk);
-    {
-        const float a2 = yp ? sw.x : 0.f, a3 = yp ? 0.f : sw.x, b2 = yp ? sw.y : 0.f, b3 = yp ? 0.f : sw.y;
+    const float s2 = (dir & kYpos) ? 1.0f : -1.0f;
+    flux_y(ki, s2, Gi);
+    flux_y(kk, s2, Gk);
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const float dG = Gk[r] - Gi[r];
-            sx[2][r] = fmaf(a2, dG, sx[2][r]);
-            sx[3][r] = fmaf(a3, dG, sx[3][r]);
-            sy[2][r] = fmaf(b2, dG, sy[2][r]);
-            sy[3][r] = fmaf(b3, dG, sy[3][r]);
+    for (int r = 0; r < 4; r++) acc[r] = fmaf(w.y, Gk[r] - Gi[r], acc[r]);
+    const bool xb = (dir & (kXpos | kXneg)) == (kXpos | kXneg), yb = (dir & (kYpos | kYneg)) == (kYpos | kYneg);
+    if (xb || yb) {
+        const float2 w2 = c.e_w32b[e];
+        if (xb) {
+            x_flux(f, ki, -1.0f, Gi);
+            x_flux(f, kk, -1.0f, Gk);
+#pragma unroll
+            for (int r = 0; r < 4; r++) acc[r] = fmaf(w2.x, Gk[r] - Gi[r], acc[r]);
         }
-    }
-    if ((dir & (kYpos | kYneg)) == (kYpos | kYneg)) {
-        flux_y(ki, -1.0f, Gi);
-        flux_y(kk, -1.0f, Gk);
+        if (yb) {
+            flux_y(ki, -1.0f, Gi);
+            flux_y(kk, -1.0f, Gk);
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const float dG = Gk[r] - Gi[r];
-            sx[3][r] = fmaf(sw.x, dG, sx[3][r]);
-            sy[3][r] = fmaf(sw.y, dG, sy[3][r]);
+            for (int r = 0; r < 4; r++) acc[r] = fmaf(w2.y, Gk[r] - Gi[r], acc[r]);
         }
     }
 }
 
-// Edge geometry of edge e: {delx, dely, w delx, w dely} and {dels w, deln w}.
+// Edge vector of edge e (delx, dely) for the reconstruction, and its folded
+// solve weights.
 template <bool UW>
-__device__ __forceinline__ void edge_geo(const DevCloud &c, long long e, float nx, float ny, float4 &g, float2 &sw)
+__device__ __forceinline__ void edge_geo(const DevCloud &c, long long e, float4 &g, float2 &w)
 {
     if (UW) {
-        // dels, deln of the point's (t, n) frame (interior_fluxes_mod.h:53-54), weight 1
         const float2 d = c.e_xy32[e];
         g = make_float4(d.x, d.y, 0.f, 0.f);
-        sw = make_float2(d.x * ny - d.y * nx, d.x * nx + d.y * ny);
     } else {
         g = c.e_geo32[e];
-        sw = c.e_sn32[e];
     }
+    w = c.e_w32[e];
 }
 
-// F = delta * sum_d (a_d Sx_d + b_d Sy_d): the four solves and
-// flux_residual_mod.h's sum (with the wall's 2 delta) in FP64, then the SSPRK
-// stage, q and the wave speed of the new state.  Returns res_sqr.
-__device__ __forceinline__ double flux_tail(const DevCloud &c, const CaseConst &K, int i, int f, double2 nn,
-                                            const float sx[4][4], const float sy[4][4],
+// F = delta * acc (the weighted sum of the folded solves, flux_residual_mod.h
+// with the wall's 2 delta) in FP64, then the SSPRK stage, q and the wave
+// speed of the new state.  Returns res_sqr.
+__device__ __forceinline__ double flux_tail(const CaseConst &K, int i, int f, double2 nn, const float acc[4],
                                             const float *__restrict__ delta, const double4_32a *__restrict__ prim,
                                             const double4_32a *__restrict__ prim_old,
                                             double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
                                             float *__restrict__ cs_next, int rk)
 {
-    double2 cf[4];
-#pragma unroll
-    for (int d = 0; d < 4; d++) cf[d] = c.fcoef[4 * i + d];
     const double dl = f2d(delta[i]);
     double F[4], P[4];
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
-        double acc = 0.0;
-#pragma unroll
-        for (int d = 0; d < 4; d++) {
-            acc = fma(cf[d].x, f2d(sx[d][r]), acc);
-            acc = fma(cf[d].y, f2d(sy[d][r]), acc);
-        }
-        F[r] = dl * acc;
-    }
+    for (int r = 0; r < 4; r++) F[r] = dl * f2d(acc[r]);
     ld4(prim[i], P);
     const double r2 = stage_update_fast(K, f, nn.x, nn.y, P, prim_old + i, F, rk);
     prim_next[i] = mk4(P);
@@ -581,7 +550,8 @@ __device__ __forceinline__ double flux_tail(const DevCloud &c, const CaseConst &
     return r2;
 }
 
-// Fused stage of one point: FP32 edge work, FP64 solve / residual / update.
+// Fused stage of one point: FP32 edge work with the FP64-folded solve
+// weights, FP64 residual scaling and update.
 // Returns the point's res_sqr.
 template <bool UW>
 __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst &K, int i,
@@ -602,19 +572,15 @@ __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst 
     ld4(qm[2 * i], mxi);
     ld4(qm[2 * i + 1], mni);
     const float e2i = c.eps2_32[i];
-    float sx[4][4], sy[4][4];
-#pragma unroll
-    for (int d = 0; d < 4; d++)
-#pragma unroll
-        for (int r = 0; r < 4; r++) { sx[d][r] = 0.f; sy[d][r] = 0.f; }
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         float4 g;
-        float2 sw;
-        edge_geo<UW>(c, e, nx, ny, g, sw);
+        float2 w;
+        edge_geo<UW>(c, e, g, w);
         const unsigned dir = c.e_dir[e];
         float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
         ld4(q[k], qk);
@@ -622,17 +588,17 @@ __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst 
         ld4(dq[2 * k + 1], dyk);
         ld4(qm[2 * k], mxk);
         ld4(qm[2 * k + 1], mnk);
-        flux_edge(f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, sw, dir, qk, dxk, dyk, mxk, mnk, c.eps2_32[k], sx, sy);
+        flux_edge(c, e, f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, w, dir, qk, dxk, dyk, mxk, mnk, c.eps2_32[k], acc);
     }
-    return flux_tail(c, K, i, f, nn, sx, sy, delta, prim, prim_old, prim_next, q_next, cs_next, rk);
+    return flux_tail(K, i, f, nn, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk);
 }
 
 // The same with the next edge's gathers in flight during the current edge's
 // arithmetic: edge j + 1's neighbour data (q, dq, qm: five float4, and the
 // limiter's eps^2) goes by cp.async into a two-slot ring of the thread's own
 // shared memory ([2][5][B] float4 and [2][B] float), its neighbour index is
-// loaded one edge earlier still, and its geometry one edge ahead into
-// registers.  Same arithmetic in the same edge order as flux_point.
+// loaded one edge earlier still, and its streamed edge data one edge ahead
+// into registers.  Same arithmetic in the same edge order as flux_point.
 template <int B, bool UW>
 __device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseConst &K, int i, int t,
                                                 float4 *ring, float *reps, const float4 *__restrict__ q,
@@ -659,11 +625,11 @@ __device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseCon
     };
     int kn = 0;
     float4 gn = make_float4(0.f, 0.f, 0.f, 0.f);
-    float2 swn = make_float2(0.f, 0.f);
+    float2 wn = make_float2(0.f, 0.f);
     unsigned dn = 0;
     if (nb > 0) {
         issue(0, c.e_nbr[base]);
-        edge_geo<UW>(c, base, nx, ny, gn, swn);
+        edge_geo<UW>(c, base, gn, wn);
         dn = c.e_dir[base];
     }
     cp_commit();
@@ -675,19 +641,15 @@ __device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseCon
     ld4(qm[2 * i], mxi);
     ld4(qm[2 * i + 1], mni);
     const float e2i = c.eps2_32[i];
-    float sx[4][4], sy[4][4];
-#pragma unroll
-    for (int d = 0; d < 4; d++)
-#pragma unroll
-        for (int r = 0; r < 4; r++) { sx[d][r] = 0.f; sy[d][r] = 0.f; }
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
         const float4 g = gn;
-        const float2 sw = swn;
+        const float2 w = wn;
         const unsigned dir = dn;
         if (j + 1 < nb) {
             issue(j + 1, kn);
-            edge_geo<UW>(c, e + 32, nx, ny, gn, swn);
+            edge_geo<UW>(c, e + 32, gn, wn);
             dn = c.e_dir[e + 32];
         }
         cp_commit();
@@ -701,9 +663,9 @@ __device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseCon
         ld4(slot[3 * B], mxk);
         ld4(slot[4 * B], mnk);
         const float e2k = reps[(j & 1) * B + t];
-        flux_edge(f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, sw, dir, qk, dxk, dyk, mxk, mnk, e2k, sx, sy);
+        flux_edge(c, e, f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, w, dir, qk, dxk, dyk, mxk, mnk, e2k, acc);
     }
-    return flux_tail(c, K, i, f, nn, sx, sy, delta, prim, prim_old, prim_next, q_next, cs_next, rk);
+    return flux_tail(K, i, f, nn, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk);
 }
 
 // ---------------------------------------------------- single-case kernels
@@ -907,14 +869,14 @@ const int kStagedVariants = 4;
 int staged_block(int v)
 {
     int b = 0;
-    QLSKUM_STAGED_SWITCH(v, b = B_)
+    QLSKUM_STAGED_SWITCH(v, b = B_; (void)D_)
     return b;
 }
 
 int staged_depth(int v)
 {
     int d = 0;
-    QLSKUM_STAGED_SWITCH(v, d = D_)
+    QLSKUM_STAGED_SWITCH(v, d = D_; (void)B_)
     return d;
 }
 

@@ -169,7 +169,9 @@ long long qlskum_launch_count(const qlskum_handle *h);
 qlskum_status qlskum_get_launch_config(qlskum_handle *h, int *flux_block, int *flux_min_blocks, int *point_block,
                                        int *gather_depth);
 /* Pin the mixed form's launch shape instead of autotuning it: flux_variant in
- * 0 .. 3 (threads x min blocks 128x4, 128x5, 64x8, 256x2), point_block one of
+ * 0 .. 7 (threads x min blocks 128x4, 128x5, 64x8, 256x2 with one gather per
+ * edge in turn; 128x4, 128x5, 64x8, 256x2 with the next edge's neighbour data
+ * in flight by cp.async), point_block one of
  * 64 / 128 / 256 / 512 for the per-edge gather form, staged 0 (that form) or
  * 1 .. 4 (staged gathers: 128 threads depth 2, 128 / 4, 256 / 3, 64 / 4).
  * QLSKUM_ERR_UNSUPPORTED if a staged variant does not fit the device's
