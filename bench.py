@@ -132,23 +132,39 @@ def make_cloud(workload):
 def flux_update_bytes(cloud, precision: str, unit_weights: bool = True) -> float:
     """Compulsory bytes one fused flux + update launch moves (each array once).
 
-    Per point: own q / dq / qm, normal, limiter eps^2, delta, flag, nbhs, the
-    directional solve data (mixed: 4 coefficient pairs, 64 B; FP64: 4 LSQ
-    moment sets, 128 B), prim in, prim out, q out, prim_old on 1 stage of 4 and
-    the wave speed on 1 of 4 (averaged), slice base; per edge: neighbour index,
-    edge vector / weights, rotated weights, membership byte.  Neighbour
-    gathers are served from cache (counted once, as the point's own rows).
+    Per point: own q / dq / qm, normal, limiter eps^2, delta, flag, nbhs, (FP64:
+    the 4 LSQ moment sets, 128 B), prim in, prim out, q out, prim_old on 1
+    stage of 4 and the wave speed on 1 of 4 (averaged), slice base; per edge:
+    neighbour index, edge vector (mixed, power 0: {delx, dely} FP32; else
+    {delx, dely, w delx, w dely}), the folded solve weights of its x and y
+    half-ranges (mixed: FP32 pair; FP64: rotated weights {dels w, deln w}),
+    membership byte.  Neighbour gathers are served from cache (counted once,
+    as the point's own rows).
     """
     n = cloud.n
     e = int(cloud.nbhs.sum())
     if precision == "mixed":
-        per_pt = 16 + 32 + 32 + 16 + 4 + 4 + 1 + 4 + 64 + 32 + 32 + 16 + 32 / 4 + 4 / 4 + 8 / 32
-        # power 0: {delx, dely} FP32 per edge, rotated in the kernel; else + {w delx, w dely, dels w, deln w}
-        per_edge = 4 + 8 + 1 if unit_weights else 4 + 16 + 8 + 1
+        per_pt = 16 + 32 + 32 + 16 + 4 + 4 + 1 + 4 + 32 + 32 + 16 + 32 / 4 + 4 / 4 + 8 / 32
+        per_edge = 4 + 8 + 8 + 1 if unit_weights else 4 + 16 + 8 + 1
     else:
         per_pt = 32 + 64 + 64 + 16 + 8 + 8 + 1 + 4 + 128 + 32 + 32 + 32 + 32 / 4 + 8 / 4 + 8 / 32
         per_edge = 4 + 32 + 16 + 1
     return n * per_pt + e * per_edge
+
+
+def measured_traffic(workload, precision, kernel):
+    """DRAM bytes per launch of `kernel` (dram__bytes_read.sum + dram__bytes_write.sum)
+    from the committed ncu summary of this workload, or None when none was captured.
+    The summaries carry lines 'traffic <precision> <kernel> <bytes>'."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"k_flux_update_{workload}_1M.md")
+    try:
+        for line in open(path):
+            f = line.strip().strip("`").split()
+            if len(f) == 4 and f[0] == "traffic" and f[1] == precision and f[2] == kernel:
+                return float(f[3])
+    except OSError:
+        pass
+    return None
 
 
 def time_solver(qlskum, torch, solver, steps):
@@ -323,6 +339,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--adjoint-iters", type=int, default=3,
                     help="iterations differentiated by the adjoint timing on the FP64 handle (0: skip)")
+    ap.add_argument("--launch", default="auto",
+                    help="mixed launch shape 'flux_variant,point_block,staged' (e.g. 6,64,0) instead of autotuning")
     args = ap.parse_args()
     rank, world, local = dist_env()
 
@@ -349,6 +367,8 @@ def main():
     kw = WORKLOADS[args.workload]["solver"]
     prec = qlskum.MIXED if args.precision == "mixed" else qlskum.FP64
     solver = qlskum.Solver(cloud, precision=prec, **kw)
+    if args.launch != "auto" and prec == qlskum.MIXED:
+        solver.set_launch_config(*[int(v) for v in args.launch.split(",")])
     solver.q_lskum(args.warmup)
     solver.synchronize()
 
@@ -375,8 +395,12 @@ def main():
     peak, peak_kind = measured_peaks()
     nbytes = flux_update_bytes(cloud, args.precision, kw["power"] == 0.0)
     achieved = nbytes / (fl_ms / fl_n / 1e3) / 1e9
+    lc = solver.launch_config()
+    kname = (f"k_flux_update{'_st' if lc['flux_variant'] >= 4 else ''}<{lc['flux_block']},{lc['flux_min_blocks']}>"
+             if prec == qlskum.MIXED else "k_flux_update<128>")
+    traffic = measured_traffic(args.workload, args.precision, kname)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": f"k_flux_update ({args.precision})",
+                "traffic": traffic, "kernel": f"{kname} ({args.precision})",
                 "algorithmic_bytes_per_launch": nbytes, "avg_launch_ms": fl_ms / fl_n,
                 "kernel_share": fl_ms / total_ms, "peak_source": f"{peak_kind} hbm_gbs"}
 
@@ -410,9 +434,22 @@ def main():
         sf.q_lskum(k)
         sf.synchronize()
         t_pr = time.perf_counter() - t0
-        adjoint = {"objective": "cl", "iterations": k, "points": cloud.n, "seconds": t_adj,
-                   "primal_seconds": t_pr, "adjoint_over_primal": t_adj / t_pr,
-                   "point_iter_s": cloud.n * k / t_adj, "dcl_dmach": g["dmach"], "dcl_daoa_per_deg": g["daoa"]}
+        # steady-state form: adjoint iterations at the current state, per iteration
+        sf.adjoint_fixed_point("cl", adj_iters=1)
+        t0 = time.perf_counter()
+        sf.adjoint_fixed_point("cl", adj_iters=k)
+        t_a = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        sf.adjoint_fixed_point("cl", adj_iters=2 * k)
+        t_b = time.perf_counter() - t0
+        fp_it = max(t_b - t_a, 1e-9) / k
+        adjoint = {"objective": "cl", "iterations": k, "points": cloud.n,
+                   "checkpointed": {"seconds": t_adj, "primal_seconds": t_pr, "adjoint_over_primal": t_adj / t_pr,
+                                    "note": "K primal iterations from the free stream, kept, then reversed"},
+                   "fixed_point": {"seconds_per_adjoint_iteration": fp_it,
+                                   "seconds_per_primal_iteration": t_pr / k,
+                                   "adjoint_over_primal": fp_it / (t_pr / k)},
+                   "dcl_dmach": g["dmach"], "dcl_daoa_per_deg": g["daoa"]}
     del s2
 
     # end to end through the C ABI with host buffers

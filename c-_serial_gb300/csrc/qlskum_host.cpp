@@ -1248,6 +1248,11 @@ qlskum_status qlskum_get_launch_config(qlskum_handle *h, int *flux_block, int *f
     return QLSKUM_OK;
 }
 
+int qlskum_get_flux_variant(const qlskum_handle *h)
+{
+    return h && h->prm.precision == QLSKUM_MIXED ? h->flux_variant : 0;
+}
+
 qlskum_status qlskum_set_launch_config(qlskum_handle *h, int flux_variant, int point_block, int staged)
 {
     NEED(h);

@@ -97,6 +97,7 @@ def load(build_if_needed: bool = True):
         "qlskum_launch_count": (C.c_longlong, [H]),
         "qlskum_get_launch_config": (i, [H, ip, ip, ip, ip]),
         "qlskum_set_launch_config": (i, [H, i, i, i]),
+        "qlskum_get_flux_variant": (i, [H]),
         "qlskum_batch_create": (i, [C.POINTER(CloudStruct), i, ip, dp, dp, i, C.POINTER(ParamsStruct), C.POINTER(H)]),
         "qlskum_batch_destroy": (i, [H]),
         "qlskum_batch_last_error": (C.c_char_p, [H]),
@@ -255,7 +256,7 @@ class Solver:
         v = [C.c_int() for _ in range(4)]
         self._ck(self._L.qlskum_get_launch_config(self._h, *[C.byref(t) for t in v]))
         return {"flux_block": v[0].value, "flux_min_blocks": v[1].value, "point_block": v[2].value,
-                "gather_depth": v[3].value}
+                "gather_depth": v[3].value, "flux_variant": int(self._L.qlskum_get_flux_variant(self._h))}
 
     def set_launch_config(self, flux_variant=0, point_block=128, staged=0):
         """Pin the mixed form's launch shape (no autotuning)."""

@@ -177,6 +177,8 @@ qlskum_status qlskum_get_launch_config(qlskum_handle *h, int *flux_block, int *f
  * QLSKUM_ERR_UNSUPPORTED if a staged variant does not fit the device's
  * shared memory for this cloud's neighbour count. */
 qlskum_status qlskum_set_launch_config(qlskum_handle *h, int flux_variant, int point_block, int staged);
+/* The flux_variant in use (as qlskum_set_launch_config numbers them; 0 for FP64 handles). */
+int qlskum_get_flux_variant(const qlskum_handle *h);
 
 /* Per-kernel device time from CUDA events recorded on the handle's stream.
  * While enabled, qlskum_q_lskum launches each iteration's kernels one by one

@@ -60,7 +60,8 @@ def test_autotuner_shape_and_result(qlskum):
     assert cfg["gather_depth"] in (0, 2, 3, 4)
     b = qlskum.Solver(c, block_size=128, **kw)
     b.q_lskum(3)
-    assert b.launch_config() == {"flux_block": 128, "flux_min_blocks": 4, "point_block": 128, "gather_depth": 0}
+    assert b.launch_config() == {"flux_block": 128, "flux_min_blocks": 4, "point_block": 128, "gather_depth": 0,
+                                 "flux_variant": 0}
     assert _close(a.prim, b.prim, 1e-5)
     np.testing.assert_allclose(a.residual_history(), b.residual_history(), rtol=1e-3)
     c2 = qlskum.Solver(c, block_size=128, **kw)
