@@ -46,6 +46,10 @@ WORKLOADS = {
                       solver=dict(mach=0.85, aoa=1.0, cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=3)),
     "subsonic": dict(cloud=dict(n_wall=160, n_layers=60, first_spacing=2e-3, radius=20.0, seed=1),
                      solver=dict(mach=0.63, aoa=2.0, cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=0)),
+    # main element + 30%-chord flap at 20 deg, 1.5%-chord slot, ~16M points (two_element_cloud
+    # defaults); M 0.2, AoA 8; CFL / VL_CONST / inner iterations as config 1 (the recipe gives none)
+    "two_element": dict(cloud=dict(), solver=dict(mach=0.2, aoa=8.0, cfl=0.2, vl_const=50.0, power=0.0,
+                                                  inner_iterations=0)),
 }
 
 
@@ -61,38 +65,48 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms while running
+    (nvidia-smi's own loop, one child process, stopped by its own PID)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, period_ms: int = 50):
         self.gpu = gpu_index
+        self.period = period_ms
         self.rows = []
-        self._stop = threading.Event()
+        self._p = None
         self._t = None
 
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                for line in out.stdout.strip().splitlines():
-                    self.rows.append([v.strip() for v in line.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+    def _read(self):
+        for line in self._p.stdout:
+            f = [v.strip() for v in line.split(",")]
+            if len(f) >= 9:
+                self.rows.append(f)
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
-        self._t.start()
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                        "--format=csv,noheader,nounits", f"-lms={self.period}"],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+            time.sleep(2.5 * self.period / 1000.0)      # first samples before the timed work
+        except Exception:
+            self._p = None
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        if self._t:
-            self._t.join(timeout=10)
+        if self._p is not None:
+            time.sleep(self.period / 1000.0)
+            self._p.terminate()
+            try:
+                self._p.wait(timeout=5)
+            except Exception:
+                self._p.kill()
+            if self._t:
+                self._t.join(timeout=5)
 
     def summary(self):
         if not self.rows:
@@ -126,6 +140,8 @@ def measured_peaks():
 
 def make_cloud(workload):
     from qlskum import cloudgen
+    if workload == "two_element":
+        return cloudgen.two_element_cloud(**WORKLOADS[workload]["cloud"])
     return cloudgen.make_cloud(**WORKLOADS[workload]["cloud"])
 
 
@@ -320,6 +336,11 @@ def run_reference(args, rank, world):
 
 def workload_config(workload, cloud=None):
     w = WORKLOADS[workload]
+    if workload == "two_element":
+        c = dict(workload="naca0012_plus_30pct_flap_20deg_slot1.5pct", **w["solver"])
+        c["points"] = cloud.n if cloud is not None else None
+        c["l2"] = "inputs larger than L2; no flush"
+        return c
     c = dict(workload=f"naca0012_{w['cloud']['n_wall']}x{w['cloud']['n_layers']}", **w["solver"])
     c["points"] = w["cloud"]["n_wall"] * w["cloud"]["n_layers"]
     c["l2"] = "inputs larger than L2 (edge arrays alone > 129 MB); no flush" if workload == "transonic" else \
@@ -330,11 +351,13 @@ def workload_config(workload, cloud=None):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--workload", default="transonic", choices=sorted(WORKLOADS) + ["batch"])
+    ap.add_argument("--adjoint-stride", type=int, default=1,
+                    help="adjoint checkpoint stride in iterations (2 = every 8 SSPRK steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--adjoint-iters", type=int, default=3,
@@ -424,11 +447,12 @@ def main():
     # against the same K primal iterations; host-synchronous calls, wall clock
     adjoint = None
     if args.adjoint_iters > 0:
-        sf = s2 if other == qlskum.FP64 else solver
+        # FP64 handle (the drop-in form) unless the workload asks for the adjoint of the mixed run
+        sf = solver if (args.workload == "two_element" or other != qlskum.FP64) else s2
         k = args.adjoint_iters
-        sf.adjoint_gradient("cl", iters=k)          # first call allocates
+        sf.adjoint_gradient("cl", iters=k, stride=args.adjoint_stride)          # first call allocates
         t0 = time.perf_counter()
-        g = sf.adjoint_gradient("cl", iters=k)
+        g = sf.adjoint_gradient("cl", iters=k, stride=args.adjoint_stride)
         t_adj = time.perf_counter() - t0
         t0 = time.perf_counter()
         sf.q_lskum(k)
@@ -443,7 +467,8 @@ def main():
         sf.adjoint_fixed_point("cl", adj_iters=2 * k)
         t_b = time.perf_counter() - t0
         fp_it = max(t_b - t_a, 1e-9) / k
-        adjoint = {"objective": "cl", "iterations": k, "points": cloud.n,
+        adjoint = {"objective": "cl", "iterations": k, "points": cloud.n, "checkpoint_stride": args.adjoint_stride,
+                   "primal_precision": "mixed" if sf is solver and prec == qlskum.MIXED else "fp64",
                    "checkpointed": {"seconds": t_adj, "primal_seconds": t_pr, "adjoint_over_primal": t_adj / t_pr,
                                     "note": "K primal iterations from the free stream, kept, then reversed"},
                    "fixed_point": {"seconds_per_adjoint_iteration": fp_it,
@@ -471,7 +496,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
-            "config": dict(workload_config(args.workload), precision=args.precision,
+            "config": dict(workload_config(args.workload, cloud), precision=args.precision,
                            parallelism="replicas" if world > 1 else "single"),
             "clocks": clocks.summary(), "gpu_launches": launches,
             "e2e": {"value": e2e_v, "unit": "point-iter/s", "h2d_bytes_per_step": h2d,

@@ -127,8 +127,9 @@ struct qlskum_handle {
     // the cloud as given (original order), for the geometry part of the adjoint
     std::vector<double> hx, hy;
     std::vector<int> hleft, hright, hflag, hnbhs, hconn;
-    // discrete adjoint buffers, allocated on first use
+    // discrete adjoint buffers, allocated on first use; checkpoint stride (iterations)
     struct AdjBuf *adj = nullptr;
+    int adj_stride = 1;
     // per-kernel event timing (qlskum_set_kernel_timing)
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -1742,15 +1743,19 @@ struct AdjBuf {
     double *bdist = nullptr;
     double2 *bnrm = nullptr;
     double4_32a *bgmom = nullptr, *bfmom = nullptr;
-    // one state per iteration of the checkpointed primal
+    // the checkpointed primal: the state of every stride-th iteration, and
+    // the states of one stride-long segment recomputed during the reverse sweep
     double4_32a *ckpt = nullptr;
     int ckpt_cap = 0;
+    double4_32a *seg = nullptr;
+    int seg_cap = 0;
 };
 
 void adj_free(qlskum_handle *h)
 {
     if (!h->adj) return;
     if (h->adj->ckpt) cudaFree(h->adj->ckpt);
+    if (h->adj->seg) cudaFree(h->adj->seg);
     h->adj->arena.release();
     delete h->adj;
     h->adj = nullptr;
@@ -1788,8 +1793,6 @@ void zero(qlskum_handle *h, void *p, size_t bytes) { cudaMemsetAsync(p, 0, bytes
 
 qlskum_status adj_alloc(qlskum_handle *h, bool geo)
 {
-    if (h->prm.precision != QLSKUM_FP64)
-        return fail(h, QLSKUM_ERR_UNSUPPORTED, "the discrete adjoint runs on FP64 handles");
     if (h->adj && (h->adj->geo || !geo)) return QLSKUM_OK;
     adj_free(h);
     AdjBuf *a = new AdjBuf();
@@ -2172,19 +2175,24 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     if (st) return st;
     AdjBuf *a = h->adj;
     const size_t np = h->np;
-    if (a->ckpt_cap < iters) {
-        if (a->ckpt) cudaFree(a->ckpt);
-        a->ckpt = nullptr;
-        a->ckpt_cap = 0;
-        cudaError_t e = cudaMalloc(&a->ckpt, sizeof(double4_32a) * np * (size_t)iters);
+    const int S = std::max(1, h->adj_stride);
+    const int nck = (iters + S - 1) / S;
+    auto grow = [&](double4_32a *&buf, int &cap, int want, const char *what) -> qlskum_status {
+        if (cap >= want) return QLSKUM_OK;
+        if (buf) cudaFree(buf);
+        buf = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&buf, sizeof(double4_32a) * np * (size_t)want);
         if (e != cudaSuccess)
-            return fail(h, QLSKUM_ERR_CUDA,
-                        fmt("checkpoints of %d iterations (%.1f GB): %s", iters,
-                            1e-9 * sizeof(double4_32a) * np * iters, cudaGetErrorString(e)));
-        a->ckpt_cap = iters;
-    }
+            return fail(h, QLSKUM_ERR_CUDA, fmt("%s: %d states (%.1f GB): %s", what, want,
+                                                1e-9 * sizeof(double4_32a) * np * want, cudaGetErrorString(e)));
+        cap = want;
+        return QLSKUM_OK;
+    };
+    if ((st = grow(a->ckpt, a->ckpt_cap, nck, "adjoint checkpoints"))) return st;
+    if (S > 1 && (st = grow(a->seg, a->seg_cap, S, "adjoint segment"))) return st;
     // primal from prim0 or the free stream (initial_conditions_mod.h:23-37),
-    // each iteration's starting state kept
+    // every S-th iteration's starting state kept
     if (prim0) {
         if ((st = upload_points(h, prim0, h->s64.prim[h->pcur], 1.0))) return st;
     } else {
@@ -2197,8 +2205,9 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     h->derived_valid = false;
     h->it = 0;
     for (int t = 0; t < iters; t++) {
-        CK(h, cudaMemcpyAsync(a->ckpt + np * (size_t)t, h->s64.prim[h->pcur], sizeof(double4_32a) * np,
-                              cudaMemcpyDeviceToDevice, h->L.stream));
+        if (t % S == 0)
+            CK(h, cudaMemcpyAsync(a->ckpt + np * (size_t)(t / S), h->s64.prim[h->pcur], sizeof(double4_32a) * np,
+                                  cudaMemcpyDeviceToDevice, h->L.stream));
         if ((st = qlskum_fpi_solver(h, t + 1))) return st;
     }
     if ((st = check_status(h))) return st;
@@ -2206,11 +2215,27 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     if ((st = adj_seed(h, objective, h->s64.prim[h->pcur], a->bP, &cl, &cd))) return st;
     adj_zero_geometry(h);
     const AdjView v = adj_view(h, true);
-    for (int t = iters - 1; t >= 0; t--) {
-        CK(h, cudaMemcpyAsync(a->P[0], a->ckpt + np * (size_t)t, sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice,
-                              h->L.stream));
-        adj_iteration_forward(h);
-        adj_iteration_reverse(h, v);
+    const size_t bytes = sizeof(double4_32a) * np;
+    for (int c0 = nck - 1; c0 >= 0; c0--) {
+        const int t0 = c0 * S, t1 = std::min(iters, t0 + S);
+        // states t0 .. t1 - 1 of this segment: the checkpoint, then FP64 iterations from it
+        const double4_32a *state_at0 = a->ckpt + np * (size_t)c0;
+        if (S > 1) {
+            CK(h, cudaMemcpyAsync(a->seg, state_at0, bytes, cudaMemcpyDeviceToDevice, h->L.stream));
+            for (int t = t0 + 1; t < t1; t++) {
+                CK(h, cudaMemcpyAsync(a->P[0], a->seg + np * (size_t)(t - 1 - t0), bytes, cudaMemcpyDeviceToDevice,
+                                      h->L.stream));
+                adj_iteration_forward(h);
+                CK(h, cudaMemcpyAsync(a->seg + np * (size_t)(t - t0), a->P[4], bytes, cudaMemcpyDeviceToDevice,
+                                      h->L.stream));
+            }
+        }
+        for (int t = t1 - 1; t >= t0; t--) {
+            const double4_32a *state = S > 1 ? a->seg + np * (size_t)(t - t0) : state_at0;
+            CK(h, cudaMemcpyAsync(a->P[0], state, bytes, cudaMemcpyDeviceToDevice, h->L.stream));
+            adj_iteration_forward(h);
+            adj_iteration_reverse(h, v);
+        }
     }
     if ((st = check_launch(h, "adjoint sweep"))) return st;
     // bar of the initial state: returned for prim0, else (the free stream)
@@ -2231,6 +2256,14 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     if (J) *J = objective == QLSKUM_OBJECTIVE_CL ? cl : cd;
     adj_params(h, objective, cl, cd, bu, binit, dJ_dmach, dJ_daoa);
     if (dJ_dwall) return adj_geometry(h, objective, h->s64.prim[h->pcur], dJ_dwall);
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_set_adjoint_stride(qlskum_handle *h, int stride)
+{
+    NEED(h);
+    if (stride < 1) return fail(h, QLSKUM_ERR_INVALID, "stride must be >= 1");
+    h->adj_stride = stride;
     return QLSKUM_OK;
 }
 

@@ -116,6 +116,7 @@ def load(build_if_needed: bool = True):
         "qlskum_residual_vjp": (i, [H, dp, dp, dp]),
         "qlskum_adjoint_gradient": (i, [H, i, i, dp, dp, dp, dp, dp, dp]),
         "qlskum_adjoint_fixed_point": (i, [H, i, i, dp, dp, dp, dp, dp]),
+        "qlskum_set_adjoint_stride": (i, [H, i]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -309,11 +310,13 @@ class Solver:
         dw = np.zeros(self.shape_points) if wall else None
         return obj, vals, dw
 
-    def adjoint_gradient(self, objective="cl", iters=100, wall=False, prim0=None) -> dict:
+    def adjoint_gradient(self, objective="cl", iters=100, wall=False, prim0=None, stride=1) -> dict:
         """Runs `iters` iterations from prim0 (held fixed) or the free stream and
         differentiates the objective ("cl" / "cd") at the end through all of
         them: {"J", "dmach", "daoa" (per degree), "dwall" ([shape_points]
-        normal displacements) or None, "dprim0" ([n, 4]) or None}."""
+        normal displacements) or None, "dprim0" ([n, 4]) or None}.  stride:
+        keep every stride-th iteration's state and recompute the rest."""
+        self._ck(self._L.qlskum_set_adjoint_stride(self._h, int(stride)))
         obj, v, dw = self._adjoint_out(objective, wall)
         p0 = None if prim0 is None else self._state(prim0, "prim0")
         dp0 = None if prim0 is None else np.empty((self.n, 4))

@@ -267,7 +267,7 @@ def _stencil_ok(dels, deln, valid, flag, min_count=2, min_rcond=1e-3):
     return ok
 
 
-def _visible(x, y, nx, ny, flag, rows, idx, dx, dy, dist, wall):
+def _visible(x, y, nx, ny, flag, rows, idx, dx, dy, dist, wall, cache=None):
     """Mask of candidate neighbours that see the point through the fluid.
 
     `wall` is a list of closed polygons (0-based point indices, in ring order).
@@ -284,12 +284,16 @@ def _visible(x, y, nx, ny, flag, rows, idx, dx, dy, dist, wall):
     wmask = flag[rows] == 0
     deln = dx * nx[rows][:, None] + dy * ny[rows][:, None]
     ok &= ~(wmask[:, None] & (deln < -0.25 * dist))
-    ea = np.concatenate([np.asarray(w) for w in wall])
-    eb = np.concatenate([np.roll(np.asarray(w), -1) for w in wall])
-    mids = np.stack([(x[ea] + x[eb]) * 0.5, (y[ea] + y[eb]) * 0.5], 1)
-    etree = cKDTree(mids)
-    wpts = np.unique(ea)
-    dw, _ = cKDTree(np.stack([x[wpts], y[wpts]], 1)).query(np.stack([x, y], 1), workers=-1)
+    if cache is None:
+        cache = {}
+    if "dw" not in cache:
+        ea = np.concatenate([np.asarray(w) for w in wall])
+        eb = np.concatenate([np.roll(np.asarray(w), -1) for w in wall])
+        mids = np.stack([(x[ea] + x[eb]) * 0.5, (y[ea] + y[eb]) * 0.5], 1)
+        wpts = np.unique(ea)
+        dw, _ = cKDTree(np.stack([x[wpts], y[wpts]], 1)).query(np.stack([x, y], 1), workers=-1)
+        cache.update(ea=ea, eb=eb, mids=mids, etree=cKDTree(mids), dw=dw)
+    ea, eb, mids, etree, dw = cache["ea"], cache["eb"], cache["mids"], cache["etree"], cache["dw"]
     need = (np.minimum(dw[rows][:, None], dw[idx]) <= dist) & np.isfinite(dist)
     rr, jj = np.nonzero(need)
     if rr.size == 0:
@@ -318,13 +322,14 @@ def _visible(x, y, nx, ny, flag, rows, idx, dx, dy, dist, wall):
 
 
 def build_connectivity(x, y, nx, ny, flag, ht, hn, tx_, ty_, n_nbrs=10, nbr_radius=2.5,
-                       n_cand=32, min_rcond=1e-3, wall=None):
+                       n_cand=32, min_rcond=1e-3, wall=None, chunk=1 << 20):
     """conn [N, 20] (0-based, -1 padded) and counts.
 
     Candidates come from a k-d tree; they are ranked by distance in the local
     spacing frame (tangent (tx_, ty_) scaled by ht, normal scaled by hn), kept
     within nbr_radius * max(ht, hn), and the first n_nbrs are taken.  Points
     whose sub-stencils fail `_stencil_ok` take further candidates one by one.
+    Rows are processed `chunk` at a time to bound memory on large clouds.
     """
     from scipy.spatial import cKDTree
 
@@ -333,43 +338,53 @@ def build_connectivity(x, y, nx, ny, flag, ht, hn, tx_, ty_, n_nbrs=10, nbr_radi
     tree = cKDTree(pts)
     hmax = np.maximum(ht, hn)
     k = min(n_cand + 1, n)
-    _, idx = tree.query(pts, k=k, workers=-1)
-    idx = idx[:, 1:]                                       # drop self
-    dx = x[idx] - x[:, None]
-    dy = y[idx] - y[:, None]
-    dist = np.sqrt(dx * dx + dy * dy)
-    st = (dx * tx_[:, None] + dy * ty_[:, None]) / ht[:, None]
-    sn = (dx * (-ty_)[:, None] + dy * tx_[:, None]) / hn[:, None]
-    sd = np.sqrt(st * st + sn * sn)
-    inside = dist <= nbr_radius * hmax[:, None]
-    if wall is not None:
-        inside &= _visible(x, y, nx, ny, flag, None, idx, dx, dy, dist, wall)
-    sd = np.where(inside, sd, np.inf)
-    order = np.argsort(sd, axis=1, kind="stable")
-    idx = np.take_along_axis(idx, order, 1)
-    sd = np.take_along_axis(sd, order, 1)
-    dx = np.take_along_axis(dx, order, 1)
-    dy = np.take_along_axis(dy, order, 1)
-    finite = np.isfinite(sd)
-    # reference split frame: t = (ny, -nx), n = (nx, ny)
-    dels_all = dx * ny[:, None] - dy * nx[:, None]
-    deln_all = dx * nx[:, None] + dy * ny[:, None]
-    take = np.minimum(n_nbrs, finite.sum(1))
-    kk = np.arange(idx.shape[1])[None, :]
-    valid = (kk < take[:, None]) & finite
-    ok = _stencil_ok(dels_all, deln_all, valid, flag, min_rcond=min_rcond)
-    bad = np.nonzero(~ok)[0]
-    # grow failing stencils one candidate at a time, up to MAX_NBHS
-    for extra in range(MAX_NBHS - n_nbrs):
-        if bad.size == 0:
-            break
-        take[bad] = np.minimum(take[bad] + 1, np.minimum(MAX_NBHS, finite[bad].sum(1)))
-        vb = (kk < take[bad][:, None]) & finite[bad]
-        okb = _stencil_ok(dels_all[bad], deln_all[bad], vb, flag[bad], min_rcond=min_rcond)
-        bad = bad[~okb]
-    valid = (kk < take[:, None]) & finite
-    conn = np.where(valid, idx, -1)[:, :MAX_NBHS].astype(np.int64)
-    cnt = valid.sum(1)
+    conn = np.full((n, MAX_NBHS), -1, np.int64)
+    cnt = np.zeros(n, np.int64)
+    bad_all = []
+    vis_cache = {}
+    for r0 in range(0, n, chunk):
+        rows = np.arange(r0, min(n, r0 + chunk))
+        _, idx = tree.query(pts[rows], k=k, workers=-1)
+        idx = idx[:, 1:]                                   # drop self
+        dx = x[idx] - x[rows, None]
+        dy = y[idx] - y[rows, None]
+        dist = np.sqrt(dx * dx + dy * dy)
+        st = (dx * tx_[rows, None] + dy * ty_[rows, None]) / ht[rows, None]
+        sn = (dx * (-ty_)[rows, None] + dy * tx_[rows, None]) / hn[rows, None]
+        sd = np.sqrt(st * st + sn * sn)
+        del st, sn
+        inside = dist <= nbr_radius * hmax[rows, None]
+        if wall is not None:
+            inside &= _visible(x, y, nx, ny, flag, rows, idx, dx, dy, dist, wall, vis_cache)
+        sd = np.where(inside, sd, np.inf)
+        order = np.argsort(sd, axis=1, kind="stable")
+        idx = np.take_along_axis(idx, order, 1)
+        sd = np.take_along_axis(sd, order, 1)
+        dx = np.take_along_axis(dx, order, 1)
+        dy = np.take_along_axis(dy, order, 1)
+        finite = np.isfinite(sd)
+        # reference split frame: t = (ny, -nx), n = (nx, ny)
+        dels_all = dx * ny[rows, None] - dy * nx[rows, None]
+        deln_all = dx * nx[rows, None] + dy * ny[rows, None]
+        take = np.minimum(n_nbrs, finite.sum(1))
+        kk = np.arange(idx.shape[1])[None, :]
+        valid = (kk < take[:, None]) & finite
+        fl = flag[rows]
+        ok = _stencil_ok(dels_all, deln_all, valid, fl, min_rcond=min_rcond)
+        bad = np.nonzero(~ok)[0]
+        # grow failing stencils one candidate at a time, up to MAX_NBHS
+        for extra in range(MAX_NBHS - n_nbrs):
+            if bad.size == 0:
+                break
+            take[bad] = np.minimum(take[bad] + 1, np.minimum(MAX_NBHS, finite[bad].sum(1)))
+            vb = (kk < take[bad][:, None]) & finite[bad]
+            okb = _stencil_ok(dels_all[bad], deln_all[bad], vb, fl[bad], min_rcond=min_rcond)
+            bad = bad[~okb]
+        valid = (kk < take[:, None]) & finite
+        conn[rows] = np.where(valid, idx, -1)[:, :MAX_NBHS]
+        cnt[rows] = valid.sum(1)
+        bad_all.append(rows[bad])
+    bad = np.concatenate(bad_all) if bad_all else np.zeros(0, np.int64)
     if bad.size:
         conn, cnt, bad = _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, wall)
     return conn, cnt, bad
@@ -533,3 +548,237 @@ def config1_cloud(seed: int = 1) -> Cloud:
 def config2_cloud(seed: int = 2) -> Cloud:
     """NACA 0012, 1024 wall points x 1000 rings = 1,024,000 points."""
     return make_cloud(n_wall=1024, n_layers=1000, first_spacing=2e-3, radius=20.0, seed=seed)
+
+
+# ---------------------------------------------------------------------------
+# Two-element (main element + slotted flap) clouds
+# ---------------------------------------------------------------------------
+
+def _naca_thickness(xc: np.ndarray, t: float) -> np.ndarray:
+    xc = np.clip(xc, 0.0, 1.0)
+    return 5.0 * t * (0.2969 * np.sqrt(xc) - 0.1260 * xc - 0.3516 * xc**2 + 0.2843 * xc**3 - 0.1036 * xc**4)
+
+
+@dataclasses.dataclass
+class _Body:
+    """A symmetric NACA 00tt section of chord `chord`, leading edge at `le`,
+    chord line turned by `deflect` degrees (positive: trailing edge down)."""
+
+    chord: float
+    le: tuple
+    deflect: float = 0.0
+    t: float = 0.12
+
+    def _frame(self):
+        d = math.radians(self.deflect)
+        return math.cos(d), math.sin(d)
+
+    def surface(self, theta):
+        """Points at surface parameter theta (naca4_surface), counter-clockwise."""
+        u, v = naca4_surface(theta, 0.0, 0.4, self.t)
+        c, s = self._frame()
+        u = u * self.chord
+        v = v * self.chord
+        return self.le[0] + u * c + v * s, self.le[1] - u * s + v * c
+
+    def inside(self, x, y):
+        c, s = self._frame()
+        dx, dy = x - self.le[0], y - self.le[1]
+        u = (dx * c - dy * s) / self.chord
+        v = (dx * s + dy * c) / self.chord
+        return (u >= 0.0) & (u <= 1.0) & (np.abs(v) <= _naca_thickness(u, self.t))
+
+
+def _offset_rings(wx, wy, first, thickness, n_layers, smooth):
+    """Rings 1..n_layers-1 off a closed wall ring along smoothed normals, offsets
+    growing geometrically from `first` to `thickness`; returns X, Y [L, W], d."""
+    nx, ny = _rot_normals(wx, wy)
+    for _ in range(smooth):
+        sx = np.roll(nx, 1) + 2.0 * nx + np.roll(nx, -1)
+        sy = np.roll(ny, 1) + 2.0 * ny + np.roll(ny, -1)
+        ln = np.sqrt(sx * sx + sy * sy)
+        nx, ny = sx / ln, sy / ln
+    g = solve_growth(first, n_layers - 1, thickness)
+    j = np.arange(n_layers, dtype=np.float64)
+    d = first * j if g == 1.0 else first * (g**j - 1.0) / (g - 1.0)
+    return wx[None, :] + d[:, None] * nx[None, :], wy[None, :] + d[:, None] * ny[None, :], d
+
+
+def _ring_frame(X, Y, d):
+    """Tangent, tangential and normal spacing of ring points [L, W]."""
+    tx = np.roll(X, -1, 1) - np.roll(X, 1, 1)
+    ty = np.roll(Y, -1, 1) - np.roll(Y, 1, 1)
+    tl = np.sqrt(tx * tx + ty * ty)
+    ht = 0.5 * tl
+    dd = np.gradient(d)
+    hn = np.broadcast_to(dd[:, None], X.shape).copy()
+    return tx / tl, ty / tl, ht, hn
+
+
+def two_element_cloud(n_main: int = 4096, n_flap: int = 1024, flap_chord: float = 0.3, deflect: float = 20.0,
+                      gap: float = 0.015, overlap: float = 0.01, n_layers: int = 12, first_spacing: float = 1e-4,
+                      h0: float = 1.5e-4, growth: float = 0.004, radius: float = 20.0, seed: int = 5,
+                      jitter: float = 0.1, n_nbrs: int = 10, nbr_radius: float = 2.5,
+                      min_rcond: float = 1e-3, smooth: int = 30) -> Cloud:
+    """Seeded two-element cloud: NACA 0012 main element (chord 1, leading edge
+    at the origin) and a NACA 0012 flap of chord `flap_chord` turned by
+    `deflect` degrees whose leading edge sits `overlap` ahead of the main
+    trailing edge, lowered until the closest distance between the two
+    surfaces is `gap` (the slot).
+
+    * Walls: `n_main` and `n_flap` cosine-spaced points (flag_2 1 and 2, both
+      rings first, main then flap; ring order and left / right as in
+      make_cloud, so the reference's normals point into the fluid).
+    * Layers: `n_layers` - 1 geometric rings off each wall up to a thickness
+      of 0.4 gap (so the two stacks never meet in the slot), rays smoothed
+      along the ring at the sharp trailing edges.
+    * Background: Poisson-like jittered points from nested grids whose spacing
+      h = h0 + growth * (distance beyond the layers) doubles from one grid to
+      the next, a grid keeping the points whose h falls in its octave;
+      points inside a body or closer to a wall than the layers' edge are
+      dropped.  h0 and growth set the size (about 16M points by default).
+    * Far field: a ring of radius `radius` about mid-chord at the local h.
+    """
+    from scipy.spatial import cKDTree
+
+    rng = np.random.default_rng(seed)
+    main = _Body(1.0, (0.0, 0.0))
+    th = lambda n: 2.0 * np.pi * np.arange(n) / n
+    mx, my = main.surface(th(n_main))
+    # slot: lower the flap until the closest surface distance is `gap`
+    dense_m = np.stack(main.surface(th(20000)), 1)
+    tm = cKDTree(dense_m)
+
+    def slot(yoff):
+        fb = _Body(flap_chord, (1.0 - overlap, yoff), deflect)
+        return float(tm.query(np.stack(fb.surface(th(8000)), 1))[0].min())
+
+    lo, hi = -0.3, 0.0
+    for _ in range(60):
+        mid = 0.5 * (lo + hi)
+        lo, hi = (lo, mid) if slot(mid) < gap else (mid, hi)
+    flap = _Body(flap_chord, (1.0 - overlap, lo), deflect)
+    fx, fy = flap.surface(th(n_flap))
+    thick = 0.4 * gap
+    Xm, Ym, dm = _offset_rings(mx, my, first_spacing, thick, n_layers, smooth)
+    Xf, Yf, df = _offset_rings(fx, fy, first_spacing, thick, n_layers, smooth)
+    tmx, tmy, htm, hnm = _ring_frame(Xm, Ym, dm)
+    tfx, tfy, htf, hnf = _ring_frame(Xf, Yf, df)
+
+    # layer jitter (not on the walls)
+    def jit(X, Y, tx, ty, ht, hn):
+        u = rng.uniform(-1.0, 1.0, size=(2,) + X.shape) * 0.1
+        jx = u[0] * ht * tx - u[1] * hn * ty
+        jy = u[0] * ht * ty + u[1] * hn * tx
+        jx[0] = jy[0] = 0.0
+        return X + jx, Y + jy
+
+    Xm, Ym = jit(Xm, Ym, tmx, tmy, htm, hnm)
+    Xf, Yf = jit(Xf, Yf, tfx, tfy, htf, hnf)
+
+    # distance to the bodies from dense surface samples
+    dense = np.concatenate([dense_m, np.stack(flap.surface(th(20000)), 1)])
+    tb = cKDTree(dense)
+    center = np.array([0.5, 0.0])
+    h_of = lambda dist: h0 + growth * np.maximum(dist - thick, 0.0)
+    r_far = radius
+    h_far = float(h_of(np.array([r_far - 0.5]))[0])
+
+    bx0, bx1 = float(dense[:, 0].min()), float(dense[:, 0].max())
+    by0, by1 = float(dense[:, 1].min()), float(dense[:, 1].max())
+    pts_bg, h_bg = [], []
+    level = 0
+    while True:
+        s_l = h0 * 2.0**level
+        lo_d = thick + (s_l - h0) / growth if level > 0 else 0.0
+        hi_d = thick + (2.0 * s_l - h0) / growth
+        m = min(hi_d, r_far + 1.0)
+        x0, x1 = max(bx0 - m, center[0] - r_far), min(bx1 + m, center[0] + r_far)
+        y0, y1 = max(by0 - m, -r_far), min(by1 + m, r_far)
+        # coarse cells that can hold points of this octave
+        cs = 32.0 * s_l
+        cxs = np.arange(x0, x1, cs) + 0.5 * cs
+        cys = np.arange(y0, y1, cs) + 0.5 * cs
+        CX, CY = np.meshgrid(cxs, cys, indexing="xy")
+        cc = np.stack([CX.ravel(), CY.ravel()], 1)
+        cd, _ = tb.query(cc, workers=-1)
+        rad = np.sqrt(((cc - center) ** 2).sum(1))
+        half = 0.75 * cs
+        keep = (cd + half >= lo_d) & (cd - half < hi_d) & (rad - half < r_far)
+        cc = cc[keep]
+        nper = int(round(cs / s_l))
+        if cc.size:
+            g = (np.arange(nper) + 0.5) * s_l - 0.5 * cs
+            GX, GY = np.meshgrid(g, g, indexing="xy")
+            for c0 in range(0, cc.shape[0], 2048):
+                blk = cc[c0:c0 + 2048]
+                px = (blk[:, 0:1] + GX.ravel()[None, :]).ravel()
+                py = (blk[:, 1:2] + GY.ravel()[None, :]).ravel()
+                u = rng.uniform(-0.5, 0.5, size=(2, px.size)) * jitter * s_l
+                px += u[0]
+                py += u[1]
+                dd, _ = tb.query(np.stack([px, py], 1), workers=-1)
+                rr = np.sqrt((px - center[0]) ** 2 + (py - center[1]) ** 2)
+                ok = (dd >= max(lo_d, thick + 0.5 * s_l)) & (dd < hi_d) & (rr < r_far - 0.5 * h_far)
+                ok &= ~main.inside(px, py) & ~flap.inside(px, py)
+                pts_bg.append(np.stack([px[ok], py[ok]], 1))
+                h_bg.append(np.full(int(ok.sum()), s_l))
+        if hi_d > r_far + 2.0 * (bx1 - bx0) or s_l > h_far * 2.0:
+            break
+        level += 1
+    bg = np.concatenate(pts_bg) if pts_bg else np.zeros((0, 2))
+    hb = np.concatenate(h_bg) if h_bg else np.zeros(0)
+
+    n_out = max(64, int(round(2.0 * np.pi * r_far / h_far)))
+    tho = th(n_out)
+    ox = center[0] + r_far * np.cos(tho)
+    oy = center[1] + r_far * np.sin(tho)
+
+    # assemble: main wall, flap wall, layers, background, outer ring
+    Wm, Wf = n_main, n_flap
+    x = np.concatenate([Xm[0], Xf[0], Xm[1:].ravel(), Xf[1:].ravel(), bg[:, 0], ox])
+    y = np.concatenate([Ym[0], Yf[0], Ym[1:].ravel(), Yf[1:].ravel(), bg[:, 1], oy])
+    ht = np.concatenate([htm[0], htf[0], htm[1:].ravel(), htf[1:].ravel(), hb, np.full(n_out, h_far)])
+    hn = np.concatenate([hnm[0], hnf[0], hnm[1:].ravel(), hnf[1:].ravel(), hb, np.full(n_out, h_far)])
+    tx_ = np.concatenate([tmx[0], tfx[0], tmx[1:].ravel(), tfx[1:].ravel(), np.ones(hb.size), -np.sin(tho)])
+    ty_ = np.concatenate([tmy[0], tfy[0], tmy[1:].ravel(), tfy[1:].ravel(), np.zeros(hb.size), np.cos(tho)])
+    n = x.size
+    flag = np.ones(n, np.int32)
+    flag[:Wm + Wf] = 0
+    flag[-n_out:] = 2
+    f2 = np.zeros(n, np.int32)
+    f2[:Wm] = 1
+    f2[Wm:Wm + Wf] = 2
+    left = np.zeros(n, np.int32)
+    right = np.zeros(n, np.int32)
+    for start, w in ((0, Wm), (Wm, Wf), (n - n_out, n_out)):
+        ring = np.arange(w)
+        left[start:start + w] = start + (ring + 1) % w + 1
+        right[start:start + w] = start + (ring - 1) % w + 1
+    nx = np.zeros(n)
+    ny = np.ones(n)
+    for sl in (slice(0, Wm + Wf), slice(n - n_out, n)):
+        li = left[sl] - 1
+        ri = right[sl] - 1
+        nxx = 0.5 * ((y[sl] - y[li]) + (y[ri] - y[sl]))
+        nyy = 0.5 * ((x[sl] - x[li]) + (x[ri] - x[sl]))
+        d = np.sqrt(nxx * nxx + nyy * nyy)
+        nx[sl] = -nxx / d
+        ny[sl] = nyy / d
+    conn0, cnt, bad = build_connectivity(x, y, nx, ny, flag, ht, hn, tx_, ty_, n_nbrs=n_nbrs,
+                                         nbr_radius=nbr_radius, min_rcond=min_rcond,
+                                         wall=[np.arange(Wm), Wm + np.arange(Wf)])
+    if bad.size:
+        raise RuntimeError(f"{bad.size} points have degenerate sub-stencils even with {MAX_NBHS} neighbours")
+    conn = np.zeros((n, MAX_NBHS), np.int32)
+    valid = conn0 >= 0
+    conn[valid] = (conn0[valid] + 1).astype(np.int32)
+    md = np.full(n, np.inf)
+    for r0 in range(0, n, 1 << 20):
+        sl = slice(r0, min(n, r0 + (1 << 20)))
+        v = valid[sl]
+        c0 = np.maximum(conn0[sl], 0)
+        dxs = np.where(v, x[c0] - x[sl, None], np.inf)
+        dys = np.where(v, y[c0] - y[sl, None], np.inf)
+        md[sl] = np.sqrt(dxs * dxs + dys * dys).min(1)
+    return Cloud(x, y, left, right, flag, f2, md, cnt.astype(np.int32), conn)

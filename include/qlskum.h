@@ -228,9 +228,11 @@ qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_ti
 
 /* Reverse mode of the FP64 iteration, for gradients of the force
  * coefficients.  No counterpart in the reference (which has no adjoint); the
- * functions differentiate exactly what q_lskum / fpi_solver compute
- * (fpi_solver_mod.h:14-151).  FP64 handles only (QLSKUM_ERR_UNSUPPORTED
- * otherwise).  Arrays are in the cloud's point order. */
+ * functions differentiate exactly what q_lskum / fpi_solver compute in FP64
+ * (fpi_solver_mod.h:14-151).  On a MIXED handle the primal trajectory is the
+ * mixed solver's and the reverse sweep differentiates the FP64 iteration at
+ * those states (an FP64 adjoint of the mixed run).  Arrays are in the
+ * cloud's point order. */
 #define QLSKUM_OBJECTIVE_CL 0
 #define QLSKUM_OBJECTIVE_CD 1
 
@@ -257,6 +259,11 @@ qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const do
  * point per iteration for the states. */
 qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters, const double *prim0, double *J,
                                       double *dJ_dmach, double *dJ_daoa, double *dJ_dwall, double *dJ_dprim0);
+/* Keep the state of every stride-th iteration only (default 1: every
+ * iteration); the reverse sweep recomputes the others segment by segment in
+ * FP64, trading one extra forward iteration per stored one for device memory:
+ * ceil(iters / stride) + stride states instead of iters. */
+qlskum_status qlskum_set_adjoint_stride(qlskum_handle *h, int stride);
 /* The steady-state adjoint at the handle's current state U (a converged
  * solution): lam = S_U^T lam + J_U iterated `adj_iters` times from 0, S the
  * map of one iteration, then dJ/dalpha = J_alpha + lam^T S_alpha.

@@ -174,11 +174,32 @@ def test_adjoint_from_given_state_vs_oracle_fd(qlskum, oracle_mod):
     assert abs(fd - ad) <= 1e-4 * abs(ad), (fd, ad)
 
 
-def test_adjoint_rejects_mixed_and_weighted(qlskum):
-    c = small_cloud()
-    s = qlskum.Solver(c, precision=qlskum.MIXED, **KW)
-    with pytest.raises(qlskum.QlskumError, match="unsupported"):
-        s.adjoint_gradient("cl", iters=2)
+def test_checkpoint_stride_same_gradient(qlskum):
+    """Keeping every 2nd / 3rd state and recomputing the rest in FP64 gives the
+    same gradient (the recomputed states equal the fused solver's bit for bit)."""
+    c = _cloud()
+    s = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **KW)
+    g1 = s.adjoint_gradient("cd", iters=7, wall=True)
+    for stride in (2, 3):
+        g = s.adjoint_gradient("cd", iters=7, wall=True, stride=stride)
+        assert g["J"] == g1["J"]
+        np.testing.assert_allclose([g["dmach"], g["daoa"]], [g1["dmach"], g1["daoa"]], rtol=1e-11)
+        np.testing.assert_allclose(g["dwall"], g1["dwall"], rtol=1e-9, atol=1e-12 * np.abs(g1["dwall"]).max())
+
+
+def test_adjoint_of_mixed_run_close_to_fp64(qlskum):
+    """On a mixed handle the reverse sweep differentiates the FP64 iteration at
+    the mixed trajectory's states: the gradient agrees with the FP64 one to
+    the mixed form's state error."""
+    c = _cloud()
+    f = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **KW).adjoint_gradient("cl", iters=N)
+    m = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, precision=qlskum.MIXED,
+                      **KW).adjoint_gradient("cl", iters=N, stride=2)
+    assert abs(m["J"] - f["J"]) < 1e-6
+    np.testing.assert_allclose([m["dmach"], m["daoa"]], [f["dmach"], f["daoa"]], rtol=1e-3)
+
+
+def test_adjoint_rejects_weighted_wall_gradient(qlskum):
     w = qlskum.Solver(_cloud(), power=1.0, inner_iterations=0, **{k: v for k, v in KW.items() if k != "power"})
     with pytest.raises(qlskum.QlskumError, match="unsupported"):
         w.adjoint_gradient("cl", iters=2, wall=True)
