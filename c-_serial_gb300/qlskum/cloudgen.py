@@ -386,7 +386,7 @@ def build_connectivity(x, y, nx, ny, flag, ht, hn, tx_, ty_, n_nbrs=10, nbr_radi
         bad_all.append(rows[bad])
     bad = np.concatenate(bad_all) if bad_all else np.zeros(0, np.int64)
     if bad.size:
-        conn, cnt, bad = _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, wall)
+        conn, cnt, bad = _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, wall, vis_cache)
     return conn, cnt, bad
 
 
@@ -402,7 +402,7 @@ def _rcond(dels, deln):
     return (tr * 0.5 - disc) / lmax if lmax > 0 else 0.0
 
 
-def _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, wall=None):
+def _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, wall=None, vis_cache=None):
     """Fix the few stencils the ranked selection leaves ill-posed.
 
     For each such point: restart from its n_nbrs nearest (Euclidean) points
@@ -418,7 +418,7 @@ def _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, w
         dy = y[cand] - y[i]
         if wall is not None:
             vis = _visible(x, y, nx, ny, flag, i, cand[None, :], dx[None, :], dy[None, :],
-                           np.sqrt(dx * dx + dy * dy)[None, :], wall)[0]
+                           np.sqrt(dx * dx + dy * dy)[None, :], wall, vis_cache)[0]
             cand, dx, dy = cand[vis], dx[vis], dy[vis]
         dels = dx * ny[i] - dy * nx[i]
         deln = dx * nx[i] + dy * ny[i]
