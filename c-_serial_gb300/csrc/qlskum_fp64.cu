@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(BLOCK) k_flux_update(DevCloud c, CaseConst K, 
 // latched at iterations 1 and 2; one block, fixed summation order.
 __global__ void k_reduce_residual(int nblocks, const double *__restrict__ psum, const double *__restrict__ pmax,
                                   int n, int it_arg, double *hist, int capacity, double *res_old, int *iter,
-                                  int *status)
+                                  int *status, int latch)
 {
     __shared__ double ss[256], sm[256];
     double v = 0.0, m = 0.0;
@@ -330,7 +330,7 @@ __global__ void k_reduce_residual(int nblocks, const double *__restrict__ psum, 
         int it = it_arg > 0 ? it_arg : *iter + 1;
         double res_new = sqrt(ss[0]) / n;
         double residue;
-        if (it <= 2) {
+        if (it <= 2 && latch) {
             *res_old = res_new;
             residue = 0;
         } else {
@@ -422,6 +422,93 @@ __global__ void k_objective_finish(int nblocks, const double *__restrict__ parti
     if (threadIdx.x < 4) out4[threadIdx.x] = sh[threadIdx.x][0];
 }
 
+// ------------------------------------------------------------ diagnostics
+
+// compute_enstrophy_mod.h:5-75: vorticity du2/dx - du1/dy by least squares
+// over the full stencil (the gradient's weights and moments), its square, and
+// per-block partial sums of the squares.
+__global__ void __launch_bounds__(256) k_enstrophy(DevCloud c, const double4_32a *__restrict__ prim,
+                                                   double *__restrict__ vort, double *__restrict__ partial)
+{
+    __shared__ double sh[256];
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    double v2 = 0.0;
+    if (i < c.n) {
+        const double4_32a Pi = prim[i];
+        double sx1 = 0., sx2 = 0., sy1 = 0., sy2 = 0.;
+        const int nb = c.nbhs[i];
+        const long long base = c.slice_base[i >> 5] + (i & 31);
+        for (int j = 0; j < nb; j++) {
+            const long long e = base + 32LL * j;
+            const int k = c.e_nbr[e];
+            const double4_32a g = c.e_geo[e];       // delx, dely, w delx, w dely
+            const double4_32a Pk = prim[k];
+            sx1 = sx1 + g.z * (Pk.y - Pi.y);
+            sx2 = sx2 + g.z * (Pk.z - Pi.z);
+            sy1 = sy1 + g.w * (Pk.y - Pi.y);
+            sy2 = sy2 + g.w * (Pk.z - Pi.z);
+        }
+        const double4_32a m = c.ggeo[i];           // sxx, syy, sxy, 1/det
+        const double du2_dx = (sx2 * m.y - sy2 * m.z) * m.w;
+        const double du1_dy = (sy1 * m.x - sx1 * m.z) * m.w;
+        const double t = du2_dx - du1_dy;
+        vort[i] = t;
+        v2 = t * t;
+    }
+    sh[threadIdx.x] = v2;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+// Stagnation pressure p0 = p (1 + (gamma - 1)/2 M^2)^(gamma / (gamma - 1)) per
+// point (stagnation_values_mod.h:9-48): per block the minimum and maximum
+// (first index on ties) and the sum of (p0_inf - p0)^2 (:51-80).
+// partial [blocks][5]: min, argmin, max, argmax, sum.
+__global__ void __launch_bounds__(256) k_stagnation(int n, const double4_32a *__restrict__ prim, double gamma,
+                                                    double p0_inf, double *__restrict__ partial)
+{
+    __shared__ double smin[256], smax[256], ssum[256];
+    __shared__ int imin[256], imax[256];
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    double p0 = 0.0, sq = 0.0;
+    const double gp = gamma / (gamma - 1);
+    if (i < n) {
+        const double4_32a P = prim[i];
+        const double angle = sqrt(gamma * P.w / P.x);
+        const double mach_t = sqrt(pow(P.y, 2) + pow(P.z, 2)) / angle;
+        p0 = P.w * pow(1 + ((gamma - 1) / 2) * mach_t * mach_t, gp);
+        sq = pow(p0_inf - p0, 2);
+    }
+    const bool ok = i < n;
+    smin[threadIdx.x] = ok ? p0 : INFINITY;
+    smax[threadIdx.x] = ok ? p0 : -INFINITY;
+    imin[threadIdx.x] = imax[threadIdx.x] = ok ? i : 0x7fffffff;
+    ssum[threadIdx.x] = sq;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        const int t = threadIdx.x;
+        if (t < st) {
+            const int u = t + st;
+            if (smin[u] < smin[t] || (smin[u] == smin[t] && imin[u] < imin[t])) { smin[t] = smin[u]; imin[t] = imin[u]; }
+            if (smax[u] > smax[t] || (smax[u] == smax[t] && imax[u] < imax[t])) { smax[t] = smax[u]; imax[t] = imax[u]; }
+            ssum[t] += ssum[u];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double *o = partial + 5 * (size_t)blockIdx.x;
+        o[0] = smin[0];
+        o[1] = (double)imin[0];
+        o[2] = smax[0];
+        o[3] = (double)imax[0];
+        o[4] = ssum[0];
+    }
+}
+
 // ------------------------------------------------------------- launchers
 
 #define QLSKUM_LAUNCHED(L) \
@@ -486,7 +573,7 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const d
 void reduce_residual(const Launch &L, const Reduce &R, int n, int it)
 {
     k_reduce_residual<<<1, 256, 0, L.stream>>>(R.blocks, R.partial_sum, R.partial_max, n, it, R.hist, R.capacity,
-                                               R.res_old, R.iter, R.status);
+                                               R.res_old, R.iter, R.status, R.latch);
     QLSKUM_LAUNCHED(L);
 }
 
@@ -499,6 +586,18 @@ void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
 void add_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
 {
     k_add<<<grid_for(n, 256), 256, 0, L.stream>>>(n, src, dst);
+    QLSKUM_LAUNCHED(L);
+}
+
+void enstrophy(const Launch &L, const DevCloud &c, const double4_32a *prim, double *vort, double *partial)
+{
+    k_enstrophy<<<grid_for(c.n, 256), 256, 0, L.stream>>>(c, prim, vort, partial);
+    QLSKUM_LAUNCHED(L);
+}
+
+void stagnation(const Launch &L, int n, const double4_32a *prim, double gamma, double p0_inf, double *partial)
+{
+    k_stagnation<<<grid_for(n, 256), 256, 0, L.stream>>>(n, prim, gamma, p0_inf, partial);
     QLSKUM_LAUNCHED(L);
 }
 

@@ -117,6 +117,9 @@ struct qlskum_handle {
     double *d_obj_partial = nullptr;
     double *d_entropy = nullptr;
     double *d_last = nullptr;
+    double *d_vort = nullptr;     // vorticity [np] (qlskum_enstrophy)
+    double *d_diag = nullptr;     // per-256-block partials of the diagnostics [5][blocks]
+    bool restarted = false;       // state and res_old came from a restart file
     int *d_wall_perm = nullptr;
     double4_32a *d_wall_geo = nullptr;
     cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
@@ -911,6 +914,8 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
     h->d_obj_partial = A.alloc<double>(4 * (size_t)((std::max(n, sp) + 255) / 256));
     h->d_entropy = A.alloc<double>(h->np);
     h->d_last = A.alloc<double>(2);
+    h->d_vort = A.alloc<double>(h->np);
+    h->d_diag = A.alloc<double>(5 * (size_t)((n + 255) / 256));
     if (A.err != cudaSuccess) {
         qlskum_status s2 = fail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(A.err)));
         A.release();
@@ -1716,6 +1721,164 @@ qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_ti
 
 }  // extern "C"
 
+
+// ============================================================ diagnostics and files
+
+namespace {
+
+qlskum_status download_prim(qlskum_handle *h, std::vector<double4_32a> &dev)
+{
+    dev.resize(h->np);
+    CK(h, cudaMemcpyAsync(dev.data(), h->s64.prim[h->pcur], sizeof(double4_32a) * h->np, cudaMemcpyDeviceToHost,
+                          h->L.stream));
+    CK(h, cudaStreamSynchronize(h->L.stream));
+    return QLSKUM_OK;
+}
+
+// Rows "<n> <it> <res_old>" then per point x y flag_1 and, in `order`, the
+// primitive state, Mach number and entropy (compute_entropy_mod.h:5-24).
+qlskum_status write_state(qlskum_handle *h, const char *path, bool restart_order)
+{
+    if (!path) return fail(h, QLSKUM_ERR_INVALID, "null path");
+    qlskum_status st = qlskum_objective(h, nullptr, nullptr, nullptr, nullptr);  // fills the entropy field
+    if (st) return st;
+    std::vector<double4_32a> dev;
+    if ((st = download_prim(h, dev))) return st;
+    std::vector<double> ent(h->np);
+    double res_old = 0.0;
+    CK(h, cudaMemcpyAsync(ent.data(), h->d_entropy, sizeof(double) * h->np, cudaMemcpyDeviceToHost, h->L.stream));
+    CK(h, cudaMemcpyAsync(&res_old, h->R.res_old, sizeof(double), cudaMemcpyDeviceToHost, h->L.stream));
+    CK(h, cudaStreamSynchronize(h->L.stream));
+    FILE *f = std::fopen(path, "w");
+    if (!f) return fail(h, QLSKUM_ERR_INVALID, fmt("cannot open %s", path));
+    std::fprintf(f, "%d %d %.17g\n", h->n, h->it, res_old);
+    for (int i = 0; i < h->n; i++) {
+        const int pp = h->perm[i];
+        const double4_32a P = dev[pp];
+        const double sos = std::sqrt(h->K.gamma * P.w / P.x);
+        const double mach = std::sqrt(P.y * P.y + P.z * P.z) / sos;
+        if (restart_order)
+            std::fprintf(f, "%.17g %.17g %d %.17g %.17g %.17g %.17g %.17g %.17g\n", h->hx[i], h->hy[i], h->hflag[i],
+                         mach, ent[pp], P.x, P.y, P.z, P.w);
+        else
+            std::fprintf(f, "%.17g %.17g %d %.17g %.17g %.17g %.17g %.17g %.17g\n", h->hx[i], h->hy[i], h->hflag[i],
+                         P.x, P.y, P.z, P.w, mach, ent[pp]);
+    }
+    const bool ok = std::fflush(f) == 0 && !std::ferror(f);
+    std::fclose(f);
+    return ok ? QLSKUM_OK : fail(h, QLSKUM_ERR_INVALID, fmt("write failed: %s", path));
+}
+
+}  // namespace
+
+extern "C" {
+
+qlskum_status qlskum_enstrophy(qlskum_handle *h, double *total, double *vorticity)
+{
+    NEED(h);
+    fp64::enstrophy(h->L, h->dc, h->s64.prim[h->pcur], h->d_vort, h->d_diag);
+    qlskum_status st = check_launch(h, "enstrophy");
+    if (st) return st;
+    const int blocks = (h->n + 255) / 256;
+    std::vector<double> part(blocks);
+    CK(h, cudaMemcpyAsync(part.data(), h->d_diag, sizeof(double) * blocks, cudaMemcpyDeviceToHost, h->L.stream));
+    std::vector<double> vort;
+    if (vorticity) {
+        vort.resize(h->np);
+        CK(h, cudaMemcpyAsync(vort.data(), h->d_vort, sizeof(double) * h->np, cudaMemcpyDeviceToHost, h->L.stream));
+    }
+    CK(h, cudaStreamSynchronize(h->L.stream));
+    double t = 0.0;
+    for (double v : part) t += v;
+    if (total) *total = t;
+    if (vorticity) unpermute(h, vort, vorticity, 1);
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_stagnation(qlskum_handle *h, double *p0_min, double *p0_max, int *i_min, int *i_max, double *J)
+{
+    NEED(h);
+    const double g = h->K.gamma, gp = g / (g - 1);
+    const double p0_inf = h->K.pr_inf * std::pow(1 + ((g - 1) / 2) * h->K.mach * h->K.mach, gp);
+    fp64::stagnation(h->L, h->n, h->s64.prim[h->pcur], g, p0_inf, h->d_diag);
+    qlskum_status st = check_launch(h, "stagnation");
+    if (st) return st;
+    const int blocks = (h->n + 255) / 256;
+    std::vector<double> part(5 * (size_t)blocks);
+    CK(h, cudaMemcpyAsync(part.data(), h->d_diag, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->L.stream));
+    CK(h, cudaStreamSynchronize(h->L.stream));
+    double mn = part[0], mx = part[2], sum = 0.0;
+    long long imn = (long long)part[1], imx = (long long)part[3];
+    for (int b = 0; b < blocks; b++) {
+        const double *o = &part[5 * (size_t)b];
+        if (o[0] < mn || (o[0] == mn && (long long)o[1] < imn)) { mn = o[0]; imn = (long long)o[1]; }
+        if (o[2] > mx || (o[2] == mx && (long long)o[3] < imx)) { mx = o[2]; imx = (long long)o[3]; }
+        sum += o[4];
+    }
+    if (p0_min) *p0_min = mn;
+    if (p0_max) *p0_max = mx;
+    if (i_min) *i_min = h->iperm[imn] + 1;
+    if (i_max) *i_max = h->iperm[imx] + 1;
+    // objective_function_J (stagnation_values_mod.h:51-80) with the sum it
+    // accumulates and plen = the number of points summed (the reference
+    // multiplies an uninitialised total and never sets plen)
+    if (J) *J = sum / (p0_inf * p0_inf * (double)h->n);
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_write_restart(qlskum_handle *h, const char *path)
+{
+    NEED(h);
+    return write_state(h, path, true);
+}
+
+qlskum_status qlskum_write_output(qlskum_handle *h, const char *path)
+{
+    NEED(h);
+    return write_state(h, path, false);
+}
+
+// restart_sol (initial_conditions_mod.h:7-21): "<nop> <itr> <res_old>", then
+// per point five skipped numbers and rho u1 u2 p.
+qlskum_status qlskum_read_restart(qlskum_handle *h, const char *path)
+{
+    NEED(h);
+    if (!path) return fail(h, QLSKUM_ERR_INVALID, "null path");
+    FILE *f = std::fopen(path, "r");
+    if (!f) return fail(h, QLSKUM_ERR_INVALID, fmt("cannot open %s", path));
+    double nop = 0, itr = 0, res_old = 0;
+    if (std::fscanf(f, "%lf %lf %lf", &nop, &itr, &res_old) != 3) {
+        std::fclose(f);
+        return fail(h, QLSKUM_ERR_INVALID, "malformed restart header");
+    }
+    std::vector<double> prim((size_t)h->n * 4);
+    for (int i = 0; i < h->n; i++) {
+        double s5[5];
+        double *p = &prim[(size_t)i * 4];
+        if (std::fscanf(f, "%lf %lf %lf %lf %lf %lf %lf %lf %lf", &s5[0], &s5[1], &s5[2], &s5[3], &s5[4], &p[0], &p[1],
+                        &p[2], &p[3]) != 9) {
+            std::fclose(f);
+            return fail(h, QLSKUM_ERR_INVALID, fmt("restart file ends before point %d of %d", i + 1, h->n));
+        }
+    }
+    std::fclose(f);
+    qlskum_status st = qlskum_set_prim(h, prim.data());
+    if (st) return st;
+    h->it = (int)itr;
+    CK(h, cudaMemcpyAsync(h->R.res_old, &res_old, sizeof(double), cudaMemcpyHostToDevice, h->L.stream));
+    CK(h, cudaStreamSynchronize(h->L.stream));
+    // fpi_solver_mod.h:139: a restarted run keeps the file's res_old
+    h->R.latch = 0;
+    h->restarted = true;
+    for (auto &g : h->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    return ensure_hist(h, h->it + 1);
+}
+
+}  // extern "C"
 
 // ============================================================ discrete adjoint
 //

@@ -139,6 +139,9 @@ struct Reduce {
     int capacity = 0;
     int blocks = 0;                          // partials written by the last stage kernel
     int max_blocks = 0;                      // partials allocated (n / 32 rounded up)
+    // res_old latches at iterations 1 and 2 unless the run continues from a
+    // restart file, which carries its own (fpi_solver_mod.h:139)
+    int latch = 1;
 };
 
 struct Launch {
@@ -201,6 +204,10 @@ void reduce_residual(const Launch &L, const Reduce &R, int n, int it);
 void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
 // dst += src over n double4 rows
 void add_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
+// diagnostics: vorticity [n] and per-256-block partial sums of its square;
+// stagnation pressure per-256-block {min, argmin, max, argmax, sum (p0_inf - p0)^2}
+void enstrophy(const Launch &L, const DevCloud &c, const double4_32a *prim, double *vort, double *partial);
+void stagnation(const Launch &L, int n, const double4_32a *prim, double gamma, double p0_inf, double *partial);
 // objectives: per-block partial sums into scratch ([4][ceil(max(n, n_wall)/256)]), then one ordered sum
 void objective(const Launch &L, const DevCloud &c, const double4_32a *prim, const int *wall_perm, const double4_32a *wall_geo,
                int n_wall, double cp_scale, double pr_inf, double gamma, double *entropy, double *out4, double *scratch);

@@ -117,6 +117,16 @@ def load(build_if_needed: bool = True):
         "qlskum_adjoint_gradient": (i, [H, i, i, dp, dp, dp, dp, dp, dp]),
         "qlskum_adjoint_fixed_point": (i, [H, i, i, dp, dp, dp, dp, dp]),
         "qlskum_set_adjoint_stride": (i, [H, i]),
+        "qlskum_enstrophy": (i, [H, dp, dp]),
+        "qlskum_stagnation": (i, [H, dp, dp, ip, ip, dp]),
+        "qlskum_write_restart": (i, [H, C.c_char_p]),
+        "qlskum_read_restart": (i, [H, C.c_char_p]),
+        "qlskum_write_output": (i, [H, C.c_char_p]),
+        "qlskum_partgrid_read": (i, [C.c_char_p, C.POINTER(CloudStruct)]),
+        "qlskum_partgrid_free": (None, [C.POINTER(CloudStruct)]),
+        "qlskum_partgrid_write": (i, [C.c_char_p, C.POINTER(CloudStruct)]),
+        "qlskum_io_last_error": (C.c_char_p, []),
+        "qlskum_check_stencils": (i, [C.POINTER(CloudStruct), C.c_double, C.c_double, dp, ip]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -147,6 +157,46 @@ def cloud_struct(cloud):
     s = CloudStruct(cloud.n, _dp(keep["x"]), _dp(keep["y"]), _ip(keep["left"]), _ip(keep["right"]),
                     _ip(keep["f1"]), _ip(keep["f2"]), _dp(keep["md"]), _ip(keep["nb"]), _ip(keep["conn"]))
     return s, keep
+
+
+def _io_ck(L, st):
+    if st != 0:
+        raise QlskumError(st, L.qlskum_io_last_error().decode())
+
+
+def partgrid_read(path):
+    """Read a partGrid file with the library's C reader (main.cpp:16-58) into a cloudgen.Cloud."""
+    from .cloudgen import Cloud
+    L = load()
+    c = CloudStruct()
+    _io_ck(L, L.qlskum_partgrid_read(os.fsencode(path), C.byref(c)))
+    try:
+        n = c.n
+        arr = lambda ptr, shape, dt: np.ctypeslib.as_array(ptr, shape=shape).astype(dt).copy()
+        cloud = Cloud(arr(c.x, (n,), np.float64), arr(c.y, (n,), np.float64), arr(c.left, (n,), np.int32),
+                      arr(c.right, (n,), np.int32), arr(c.flag_1, (n,), np.int32), arr(c.flag_2, (n,), np.int32),
+                      arr(c.min_dist, (n,), np.float64), arr(c.nbhs, (n,), np.int32),
+                      arr(c.conn, (n, 20), np.int32))
+    finally:
+        L.qlskum_partgrid_free(C.byref(c))
+    return cloud
+
+
+def partgrid_write(cloud, path):
+    """Write a cloud with the library's C writer."""
+    L = load()
+    s, keep = cloud_struct(cloud)
+    _io_ck(L, L.qlskum_partgrid_write(os.fsencode(path), C.byref(s)))
+
+
+def check_stencils(cloud, power=0.0, min_rcond=1e-3):
+    """(rcond [n, 4], number of points with a used sub-stencil below min_rcond)."""
+    L = load()
+    s, keep = cloud_struct(cloud)
+    rc = np.empty((cloud.n, 4))
+    bad = C.c_int()
+    _io_ck(L, L.qlskum_check_stencils(C.byref(s), float(power), float(min_rcond), _dp(rc), C.byref(bad)))
+    return rc, bad.value
 
 
 class Solver:
@@ -281,6 +331,31 @@ class Solver:
     @property
     def stream(self) -> int:
         return int(self._L.qlskum_stream(self._h) or 0)
+
+    # ------------------------------------------------ diagnostics and state files
+    def enstrophy(self):
+        """(total enstrophy, vorticity [n]) of the current state (compute_enstrophy)."""
+        t = C.c_double()
+        v = np.empty(self.n)
+        self._ck(self._L.qlskum_enstrophy(self._h, C.byref(t), _dp(v)))
+        return t.value, v
+
+    def stagnation(self):
+        """(p0 min, p0 max, 1-based point of the min, of the max, J)."""
+        d = [C.c_double() for _ in range(3)]
+        ii = [C.c_int() for _ in range(2)]
+        self._ck(self._L.qlskum_stagnation(self._h, C.byref(d[0]), C.byref(d[1]), C.byref(ii[0]), C.byref(ii[1]),
+                                           C.byref(d[2])))
+        return d[0].value, d[1].value, ii[0].value, ii[1].value, d[2].value
+
+    def write_restart(self, path):
+        self._ck(self._L.qlskum_write_restart(self._h, os.fsencode(path)))
+
+    def read_restart(self, path):
+        self._ck(self._L.qlskum_read_restart(self._h, os.fsencode(path)))
+
+    def write_output(self, path):
+        self._ck(self._L.qlskum_write_output(self._h, os.fsencode(path)))
 
     # ------------------------------------------------------- discrete adjoint
     def _state(self, a, name):

@@ -1,6 +1,6 @@
 """Build recipe of the in-tree CUDA library (libqlskum.so) for sm_103a.
 
-Six translation units compiled in parallel and linked into one shared
+Seven translation units compiled in parallel and linked into one shared
 library with a C ABI (include/qlskum.h):
 
 * csrc/qlskum_fp64.cu  -- FP64 drop-in kernels, -fmad=false (no FMA
@@ -11,6 +11,8 @@ library with a C ABI (include/qlskum.h):
   allocates nothing (static device scratch), -fmad=false like the FP64 unit;
 * csrc/qlskum_host.cpp -- host layer, g++ -ffp-contract=off (bit-exact
   sub-stencil classification on x86-64 and aarch64 alike);
+* csrc/qlskum_io.cpp -- partGrid file I/O and the sub-stencil quality check
+  (host only, no GPU needed);
 * csrc/qlskum_vjp_host.cpp -- the per-point arithmetic and its reverse mode
   compiled for the host, for derivative checks without a GPU.
 
@@ -53,6 +55,7 @@ def sources():
         "qlskum_noalloc.cu": ["-fmad=false"],
         "qlskum_adjoint.cu": [],
         "qlskum_host.cpp": [],
+        "qlskum_io.cpp": [],
         "qlskum_vjp_host.cpp": [],
     }
 

@@ -617,7 +617,7 @@ def _ring_frame(X, Y, d):
 
 def two_element_cloud(n_main: int = 4096, n_flap: int = 1024, flap_chord: float = 0.3, deflect: float = 20.0,
                       gap: float = 0.015, overlap: float = 0.01, n_layers: int = 12, first_spacing: float = 1e-4,
-                      h0: float = 1.5e-4, growth: float = 0.004, radius: float = 20.0, seed: int = 5,
+                      h0: float = 1.5e-4, growth: float = 0.0033, radius: float = 20.0, seed: int = 5,
                       jitter: float = 0.1, n_nbrs: int = 10, nbr_radius: float = 2.5,
                       min_rcond: float = 1e-3, smooth: int = 30) -> Cloud:
     """Seeded two-element cloud: NACA 0012 main element (chord 1, leading edge

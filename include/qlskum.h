@@ -224,6 +224,53 @@ void *qlskum_batch_stream(qlskum_batch *b);
 qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_tile, int *flux_min_blocks,
                                   int *points_per_warp);
 
+/* ------------------------------------------------- diagnostics and state files */
+
+/* compute_enstrophy_mod.h:5-75 on the device (FP64): vorticity
+ * du2/dx - du1/dy of every point by least squares over its full stencil, and
+ * total = the sum of its squares.  vorticity (or NULL): double [n]. */
+qlskum_status qlskum_enstrophy(qlskum_handle *h, double *total, double *vorticity);
+/* stagnation_values_mod.h: the smallest and largest stagnation pressure
+ * p0 = p (1 + (gamma-1)/2 M^2)^(gamma/(gamma-1)) over the points and their
+ * 1-based point numbers (stagnation_pressure, :9-48), and the objective
+ * J = sum (p0_inf - p0)^2 / (p0_inf^2 n) (objective_function_J, :51-80, with
+ * the sum it accumulates and plen = n: the reference multiplies an
+ * uninitialised total and never sets plen).  Any pointer may be NULL. */
+qlskum_status qlskum_stagnation(qlskum_handle *h, double *p0_min, double *p0_max, int *i_min, int *i_max,
+                                double *J);
+/* restart.dat as restart_sol reads it (initial_conditions_mod.h:7-21): a line
+ * "<n> <it> <res_old>", then per point "x y flag_1 mach entropy rho u1 u2 p"
+ * (five columns restart_sol skips, then the state), 17 significant digits. */
+qlskum_status qlskum_write_restart(qlskum_handle *h, const char *path);
+/* Continue from a restart file: the state, the iteration count (the next
+ * iteration is it + 1, q_lskum_mod.h:31-35) and res_old, which the run then
+ * keeps instead of latching it at iterations 1-2 (fpi_solver_mod.h:139). */
+qlskum_status qlskum_read_restart(qlskum_handle *h, const char *path);
+/* print_primal_output (post_processing_mod.h:7-26) with one point per line
+ * and the Mach number |u| / sqrt(gamma p / rho) (the reference writes no line
+ * breaks and takes a square root of |u|^2 / c): "<n> <it> <res_old>", then
+ * "x y flag_1 rho u1 u2 p mach entropy". */
+qlskum_status qlskum_write_output(qlskum_handle *h, const char *path);
+
+/* --------------------------------------------------- cloud files (no GPU needed) */
+
+/* The partGrid text file main.cpp:16-58 reads.  qlskum_partgrid_read
+ * allocates the cloud's arrays (release with qlskum_partgrid_free); errors
+ * leave a message for qlskum_io_last_error(). */
+qlskum_status qlskum_partgrid_read(const char *path, qlskum_cloud *out);
+void qlskum_partgrid_free(qlskum_cloud *cloud);
+qlskum_status qlskum_partgrid_write(const char *path, const qlskum_cloud *cloud);
+const char *qlskum_io_last_error(void);
+/* The sub-stencil quality check the reference leaves as a stub
+ * (check_condition_number, generate_connectivity_mod.h:84-89): for every
+ * point and direction (xpos, xneg, ypos, yneg) the reciprocal condition number
+ * of its weighted 2x2 least-squares matrix, split as generate_connectivity
+ * does (1 for a direction the point's class does not use, 0 below two
+ * members); *n_bad = points with a used direction below min_rcond.
+ * rcond: double [n][4] or NULL. */
+qlskum_status qlskum_check_stencils(const qlskum_cloud *cloud, double power, double min_rcond, double *rcond,
+                                    int *n_bad);
+
 /* ------------------------------------------------------------ discrete adjoint */
 
 /* Reverse mode of the FP64 iteration, for gradients of the force

@@ -694,6 +694,73 @@ void qo_objective(qo_solver *s, double *cl, double *cd, double *cm, double *tota
     *total_entropy = tot;
 }
 
+/* compute_enstrophy_mod.h:5-75: vorticity du2/dx - du1/dy by weighted least
+ * squares over the full stencil; vort [n] (may be NULL); returns the sum of
+ * its squares in point order. */
+double qo_enstrophy(qo_solver *s, double *vort)
+{
+    double total = 0.0;
+    for (int i = 0; i < s->n; i++) {
+        double x_i = s->x[i], y_i = s->y[i];
+        double sum_delx_sqr = 0., sum_dely_sqr = 0., sum_delx_dely = 0.;
+        double sum_delx_delu1 = 0., sum_dely_delu1 = 0., sum_delx_delu2 = 0., sum_dely_delu2 = 0.;
+        for (int k = 0; k < s->nbhs[i]; k++) {
+            int nbh = s->conn[i * NB + k];
+            double delx = s->x[nbh] - x_i, dely = s->y[nbh] - y_i;
+            double dist = sqrt(delx * delx + dely * dely);
+            double weights = pow(dist, s->p.power);
+            sum_delx_sqr = sum_delx_sqr + delx * delx * weights;
+            sum_dely_sqr = sum_dely_sqr + dely * dely * weights;
+            sum_delx_dely = sum_delx_dely + delx * dely * weights;
+            sum_delx_delu1 = sum_delx_delu1 + weights * delx * (s->prim[4 * nbh + 1] - s->prim[4 * i + 1]);
+            sum_delx_delu2 = sum_delx_delu2 + weights * delx * (s->prim[4 * nbh + 2] - s->prim[4 * i + 2]);
+            sum_dely_delu1 = sum_dely_delu1 + weights * dely * (s->prim[4 * nbh + 1] - s->prim[4 * i + 1]);
+            sum_dely_delu2 = sum_dely_delu2 + weights * dely * (s->prim[4 * nbh + 2] - s->prim[4 * i + 2]);
+        }
+        double det = sum_delx_sqr * sum_dely_sqr - sum_delx_dely * sum_delx_dely;
+        double one_by_det = 1.0 / det;
+        double du2_dx = (sum_delx_delu2 * sum_dely_sqr - sum_dely_delu2 * sum_delx_dely) * one_by_det;
+        double du1_dy = (sum_dely_delu1 * sum_delx_sqr - sum_delx_delu1 * sum_delx_dely) * one_by_det;
+        double temp = du2_dx - du1_dy;
+        if (vort) vort[i] = temp;
+        total = total + temp * temp;
+    }
+    return total;
+}
+
+/* stagnation_values_mod.h:9-48 (extremes of p0 and their 1-based point
+ * numbers) and :51-80 (J, with the sum it accumulates and plen = n). */
+void qo_stagnation(qo_solver *s, double *p_min, double *p_max, int *i_min, int *i_max, double *J)
+{
+    double g = s->gamma, gammaPower = g / (g - 1);
+    double p0_inf = s->pr_inf * (pow((1 + ((g - 1) / 2) * s->p.mach * s->p.mach), gammaPower));
+    double pMin = 0, pMax = 0, p0_sum = 0.0;
+    int indexMin = 1, indexMax = 1;
+    for (int i = 0; i < s->n; i++) {
+        const double *prim = s->prim + 4 * i;
+        double angle = sqrt(g * prim[3] / prim[0]);
+        double mach_t = sqrt(pow(prim[1], 2) + pow(prim[2], 2)) / angle;
+        double p0 = prim[3] * (pow((1 + ((g - 1) / 2) * mach_t * mach_t), gammaPower));
+        if (i == 0) {
+            pMin = p0;
+            pMax = p0;
+            indexMin = indexMax = 1;
+        } else if (p0 < pMin) {
+            pMin = p0;
+            indexMin = i + 1;
+        } else if (p0 > pMax) {
+            pMax = p0;
+            indexMax = i + 1;
+        }
+        p0_sum = p0_sum + pow((p0_inf - p0), 2);
+    }
+    *p_min = pMin;
+    *p_max = pMax;
+    *i_min = indexMin;
+    *i_max = indexMax;
+    *J = p0_sum * (1 / (pow(p0_inf, 2) * s->n));
+}
+
 double *qo_prim(qo_solver *s) { return s->prim; }
 double *qo_prim_old(qo_solver *s) { return s->prim_old; }
 double *qo_q(qo_solver *s) { return s->q; }

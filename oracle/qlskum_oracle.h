@@ -55,6 +55,8 @@ void qo_state_update(qo_solver *s, int rk);
 /* One pseudo-time iteration; returns res_new, writes residue / max_res. */
 double qo_fpi_solver(qo_solver *s, int it, double *residue, double *max_res);
 void qo_objective(qo_solver *s, double *cl, double *cd, double *cm, double *total_entropy);
+double qo_enstrophy(qo_solver *s, double *vort);
+void qo_stagnation(qo_solver *s, double *p_min, double *p_max, int *i_min, int *i_max, double *J);
 
 /* Direct access to the state (point-major, 0-based). */
 double *qo_prim(qo_solver *s);       /* [n][4] */

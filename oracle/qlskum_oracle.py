@@ -77,6 +77,10 @@ def lib():
         L.qo_fpi_solver.argtypes = [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         dp = C.POINTER(C.c_double)
         L.qo_objective.argtypes = [P, dp, dp, dp, dp]
+        L.qo_enstrophy.restype = C.c_double
+        L.qo_enstrophy.argtypes = [P, dp]
+        ip = C.POINTER(C.c_int)
+        L.qo_stagnation.argtypes = [P, dp, dp, ip, ip, dp]
         for name in ("qo_prim", "qo_prim_old", "qo_q", "qo_dq", "qo_qm", "qo_flux_res", "qo_delta",
                      "qo_normals", "qo_entropy"):
             getattr(L, name).restype = dp
@@ -177,6 +181,19 @@ class Oracle:
         v = [C.c_double() for _ in range(4)]
         lib().qo_objective(self._h, *[C.byref(t) for t in v])
         return tuple(t.value for t in v)
+
+    def enstrophy(self):
+        """(total enstrophy, vorticity [n]) of the current state."""
+        v = np.zeros(self.n)
+        t = lib().qo_enstrophy(self._h, v.ctypes.data_as(C.POINTER(C.c_double)))
+        return t, v
+
+    def stagnation(self):
+        """(p0 min, p0 max, 1-based point of the min, of the max, J)."""
+        d = [C.c_double() for _ in range(3)]
+        ii = [C.c_int() for _ in range(2)]
+        lib().qo_stagnation(self._h, C.byref(d[0]), C.byref(d[1]), C.byref(ii[0]), C.byref(ii[1]), C.byref(d[2]))
+        return d[0].value, d[1].value, ii[0].value, ii[1].value, d[2].value
 
     @property
     def prim(self): return self._arr("qo_prim", (self.n, 4))

@@ -37,6 +37,7 @@
 
 #include "data_structure_mod.h"
 #include "q_lskum_mod.h"          // pulls in fpi_solver, fluxes, limiter, state update, objectives
+#include "compute_enstrophy_mod.h"
 #include "split_fluxes_mod.h"
 #include "quadrant_fluxes_mod.h"
 
@@ -222,6 +223,11 @@ int main(int argc, char **argv)
     if (mode == "run") {
         write_f64("prim.f64", pm4(point.prim));
         objective_dump();
+        // compute_enstrophy_mod.h:5-75 (never called by the reference's driver)
+        compute_enstrophy();
+        std::vector<double> ens(1, total_enstrophy);
+        for (int i = 1; i <= max_points; i++) ens.push_back(point.vorticity[i]);
+        write_f64("enstrophy.f64", ens);
         return 0;
     }
 

@@ -132,3 +132,7 @@ def test_against_reference_build(oracle_mod):
     assert np.array_equal(hist, rh)
     assert np.array_equal(o.prim, rp)
     assert np.array_equal(np.array(o.objective()), ro)
+    # enstrophy of the final state (compute_enstrophy_mod.h), bit for bit
+    re = np.fromfile(os.path.join(tmp, "enstrophy.f64"))
+    tot, vort = o.enstrophy()
+    assert tot == re[0] and np.array_equal(vort, re[1:])
