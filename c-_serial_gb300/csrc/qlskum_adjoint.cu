@@ -519,6 +519,31 @@ __global__ void k_objective(AdjView a, const int *__restrict__ wall_perm, const 
     bP[m].w += -(bH * nn.x + bV * nn.y) * ds / cp_scale;
 }
 
+// bP += dJ/dprim of the stagnation-pressure loss J = sum (p0_inf - p0)^2 /
+// (p0_inf^2 n) (stagnation_values_mod.h:51-80), p0 = p A^g, A = 1 + (gamma-1)/2
+// M^2, M^2 = rho |u|^2 / (gamma p), g = gamma / (gamma - 1).
+__global__ void k_objective_J(int n, const double4_32a *__restrict__ P, double gamma, double p0_inf,
+                              double4_32a *__restrict__ bP)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double4_32a p = P[i];
+    const double g = gamma / (gamma - 1);
+    const double u2 = p.y * p.y + p.z * p.z;
+    const double M2 = p.x * u2 / (gamma * p.w);
+    const double A = 1 + 0.5 * (gamma - 1) * M2;
+    const double Ag = pow(A, g);
+    const double p0 = p.w * Ag;
+    const double bp0 = -2.0 * (p0_inf - p0) / (p0_inf * p0_inf * n);
+    const double dA = p.w * g * Ag / A * 0.5 * (gamma - 1);   // dp0 / dM^2
+    double4_32a b = bP[i];
+    b.x += bp0 * dA * (u2 / (gamma * p.w));
+    b.y += bp0 * dA * (2.0 * p.x * p.y / (gamma * p.w));
+    b.z += bp0 * dA * (2.0 * p.x * p.z / (gamma * p.w));
+    b.w += bp0 * (Ag - dA * M2 / p.w);
+    bP[i] = b;
+}
+
 }  // namespace adjk
 
 // ------------------------------------------------------------- launchers
@@ -574,6 +599,11 @@ void delta(const Launch &L, const AdjView &a, const double4_32a *P, const double
     else
         adjk::k_delta<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, P, bdelta, cfl, bc);
     adjk::k_wave<<<adjk::grid_for(a.c.n, 256), 256, 0, L.stream>>>(a.c.n, P, bc, bP);
+}
+
+void objective_J(const Launch &L, int n, const double4_32a *P, double gamma, double p0_inf, double4_32a *bP)
+{
+    adjk::k_objective_J<<<adjk::grid_for(n, 256), 256, 0, L.stream>>>(n, P, gamma, p0_inf, bP);
 }
 
 void objective(const Launch &L, const AdjView &a, const int *wall_perm, const double4_32a *wall_geo, int n_wall,

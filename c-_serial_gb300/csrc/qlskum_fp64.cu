@@ -466,12 +466,12 @@ __global__ void __launch_bounds__(256) k_enstrophy(DevCloud c, const double4_32a
 
 // Stagnation pressure p0 = p (1 + (gamma - 1)/2 M^2)^(gamma / (gamma - 1)) per
 // point (stagnation_values_mod.h:9-48): per block the minimum and maximum
-// (first index on ties) and the sum of (p0_inf - p0)^2 (:51-80).
-// partial [blocks][5]: min, argmin, max, argmax, sum.
+// (first index on ties), the sum of (p0_inf - p0)^2 (:51-80) and of p0.
+// partial [blocks][6]: min, argmin, max, argmax, sum of squares, sum.
 __global__ void __launch_bounds__(256) k_stagnation(int n, const double4_32a *__restrict__ prim, double gamma,
                                                     double p0_inf, double *__restrict__ partial)
 {
-    __shared__ double smin[256], smax[256], ssum[256];
+    __shared__ double smin[256], smax[256], ssum[256], sp0[256];
     __shared__ int imin[256], imax[256];
     const int i = blockIdx.x * 256 + threadIdx.x;
     double p0 = 0.0, sq = 0.0;
@@ -488,6 +488,7 @@ __global__ void __launch_bounds__(256) k_stagnation(int n, const double4_32a *__
     smax[threadIdx.x] = ok ? p0 : -INFINITY;
     imin[threadIdx.x] = imax[threadIdx.x] = ok ? i : 0x7fffffff;
     ssum[threadIdx.x] = sq;
+    sp0[threadIdx.x] = p0;
     __syncthreads();
     for (int st = 128; st > 0; st >>= 1) {
         const int t = threadIdx.x;
@@ -496,16 +497,18 @@ __global__ void __launch_bounds__(256) k_stagnation(int n, const double4_32a *__
             if (smin[u] < smin[t] || (smin[u] == smin[t] && imin[u] < imin[t])) { smin[t] = smin[u]; imin[t] = imin[u]; }
             if (smax[u] > smax[t] || (smax[u] == smax[t] && imax[u] < imax[t])) { smax[t] = smax[u]; imax[t] = imax[u]; }
             ssum[t] += ssum[u];
+            sp0[t] += sp0[u];
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        double *o = partial + 5 * (size_t)blockIdx.x;
+        double *o = partial + 6 * (size_t)blockIdx.x;
         o[0] = smin[0];
         o[1] = (double)imin[0];
         o[2] = smax[0];
         o[3] = (double)imax[0];
         o[4] = ssum[0];
+        o[5] = sp0[0];
     }
 }
 

@@ -118,7 +118,7 @@ struct qlskum_handle {
     double *d_entropy = nullptr;
     double *d_last = nullptr;
     double *d_vort = nullptr;     // vorticity [np] (qlskum_enstrophy)
-    double *d_diag = nullptr;     // per-256-block partials of the diagnostics [5][blocks]
+    double *d_diag = nullptr;     // per-256-block partials of the diagnostics [6][blocks]
     bool restarted = false;       // state and res_old came from a restart file
     int *d_wall_perm = nullptr;
     double4_32a *d_wall_geo = nullptr;
@@ -915,7 +915,7 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
     h->d_entropy = A.alloc<double>(h->np);
     h->d_last = A.alloc<double>(2);
     h->d_vort = A.alloc<double>(h->np);
-    h->d_diag = A.alloc<double>(5 * (size_t)((n + 255) / 256));
+    h->d_diag = A.alloc<double>(6 * (size_t)((n + 255) / 256));
     if (A.err != cudaSuccess) {
         qlskum_status s2 = fail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(A.err)));
         A.release();
@@ -1726,6 +1726,41 @@ qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_ti
 
 namespace {
 
+struct Stagnation {
+    double p0_inf, p0_min, p0_max, sum_sq, sum_p0, J;
+    long long i_min, i_max;  // device order
+};
+
+// stagnation_values_mod.h at `prim`: extremes, and objective_function_J
+// (:51-80) with the sum it accumulates and plen = the number of points summed
+// (the reference multiplies an uninitialised total and never sets plen).
+qlskum_status stagnation_values(qlskum_handle *h, const double4_32a *prim, Stagnation &sv)
+{
+    const double g = h->K.gamma, gp = g / (g - 1);
+    sv.p0_inf = h->K.pr_inf * std::pow(1 + ((g - 1) / 2) * h->K.mach * h->K.mach, gp);
+    fp64::stagnation(h->L, h->n, prim, g, sv.p0_inf, h->d_diag);
+    qlskum_status st = check_launch(h, "stagnation");
+    if (st) return st;
+    const int blocks = (h->n + 255) / 256;
+    std::vector<double> part(6 * (size_t)blocks);
+    CK(h, cudaMemcpyAsync(part.data(), h->d_diag, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->L.stream));
+    CK(h, cudaStreamSynchronize(h->L.stream));
+    sv.p0_min = part[0];
+    sv.p0_max = part[2];
+    sv.i_min = (long long)part[1];
+    sv.i_max = (long long)part[3];
+    sv.sum_sq = sv.sum_p0 = 0.0;
+    for (int b = 0; b < blocks; b++) {
+        const double *o = &part[6 * (size_t)b];
+        if (o[0] < sv.p0_min || (o[0] == sv.p0_min && (long long)o[1] < sv.i_min)) { sv.p0_min = o[0]; sv.i_min = (long long)o[1]; }
+        if (o[2] > sv.p0_max || (o[2] == sv.p0_max && (long long)o[3] < sv.i_max)) { sv.p0_max = o[2]; sv.i_max = (long long)o[3]; }
+        sv.sum_sq += o[4];
+        sv.sum_p0 += o[5];
+    }
+    sv.J = sv.sum_sq / (sv.p0_inf * sv.p0_inf * (double)h->n);
+    return QLSKUM_OK;
+}
+
 qlskum_status download_prim(qlskum_handle *h, std::vector<double4_32a> &dev)
 {
     dev.resize(h->np);
@@ -1798,31 +1833,14 @@ qlskum_status qlskum_enstrophy(qlskum_handle *h, double *total, double *vorticit
 qlskum_status qlskum_stagnation(qlskum_handle *h, double *p0_min, double *p0_max, int *i_min, int *i_max, double *J)
 {
     NEED(h);
-    const double g = h->K.gamma, gp = g / (g - 1);
-    const double p0_inf = h->K.pr_inf * std::pow(1 + ((g - 1) / 2) * h->K.mach * h->K.mach, gp);
-    fp64::stagnation(h->L, h->n, h->s64.prim[h->pcur], g, p0_inf, h->d_diag);
-    qlskum_status st = check_launch(h, "stagnation");
+    Stagnation sv;
+    qlskum_status st = stagnation_values(h, h->s64.prim[h->pcur], sv);
     if (st) return st;
-    const int blocks = (h->n + 255) / 256;
-    std::vector<double> part(5 * (size_t)blocks);
-    CK(h, cudaMemcpyAsync(part.data(), h->d_diag, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->L.stream));
-    CK(h, cudaStreamSynchronize(h->L.stream));
-    double mn = part[0], mx = part[2], sum = 0.0;
-    long long imn = (long long)part[1], imx = (long long)part[3];
-    for (int b = 0; b < blocks; b++) {
-        const double *o = &part[5 * (size_t)b];
-        if (o[0] < mn || (o[0] == mn && (long long)o[1] < imn)) { mn = o[0]; imn = (long long)o[1]; }
-        if (o[2] > mx || (o[2] == mx && (long long)o[3] < imx)) { mx = o[2]; imx = (long long)o[3]; }
-        sum += o[4];
-    }
-    if (p0_min) *p0_min = mn;
-    if (p0_max) *p0_max = mx;
-    if (i_min) *i_min = h->iperm[imn] + 1;
-    if (i_max) *i_max = h->iperm[imx] + 1;
-    // objective_function_J (stagnation_values_mod.h:51-80) with the sum it
-    // accumulates and plen = the number of points summed (the reference
-    // multiplies an uninitialised total and never sets plen)
-    if (J) *J = sum / (p0_inf * p0_inf * (double)h->n);
+    if (p0_min) *p0_min = sv.p0_min;
+    if (p0_max) *p0_max = sv.p0_max;
+    if (i_min) *i_min = h->iperm[sv.i_min] + 1;
+    if (i_max) *i_max = h->iperm[sv.i_max] + 1;
+    if (J) *J = sv.J;
     return QLSKUM_OK;
 }
 
@@ -2090,37 +2108,60 @@ void adj_iteration_reverse(qlskum_handle *h, const AdjView &v)
 
 // Cl and Cd at `prim` (compute_force_coeffs_mod.h:37-67), and dJ/dprim of
 // objective `which` (0 Cl, 1 Cd) into `bP`.
-qlskum_status adj_seed(qlskum_handle *h, int which, const double4_32a *prim, double4_32a *bP, double *cl, double *cd)
+// The objective's value and its explicit dependence on Mach and AoA (the
+// part not carried by the state).
+struct ObjSeed {
+    double J = 0.0, dM = 0.0, dth = 0.0;
+};
+
+// J at `prim` and dJ/dprim into bP: Cl / Cd (compute_force_coeffs_mod.h:37-67;
+// c_p scales with 1 / M^2 and the axes rotate with theta: dCl/dtheta = -Cd,
+// dCd/dtheta = Cl) or the stagnation-pressure loss (its p0_inf depends on M).
+qlskum_status adj_seed(qlskum_handle *h, int which, const double4_32a *prim, double4_32a *bP, ObjSeed &o)
 {
+    zero(h, bP, sizeof(double4_32a) * h->np);
+    qlskum_status st;
+    if (which == QLSKUM_OBJECTIVE_J) {
+        Stagnation sv;
+        if ((st = stagnation_values(h, prim, sv))) return st;
+        adjl::objective_J(h->L, h->n, prim, h->K.gamma, sv.p0_inf, bP);
+        if ((st = check_launch(h, "adjoint seed"))) return st;
+        const double n = (double)h->n, g = h->K.gamma, M = h->K.mach, gp = g / (g - 1);
+        const double dJ_dp0inf = 2.0 * (n * sv.p0_inf - sv.sum_p0) / (sv.p0_inf * sv.p0_inf * n) -
+                                 2.0 * sv.sum_sq / (sv.p0_inf * sv.p0_inf * sv.p0_inf * n);
+        const double dp0inf_dM = h->K.pr_inf * gp * std::pow(1 + 0.5 * (g - 1) * M * M, gp - 1) * (g - 1) * M;
+        o.J = sv.J;
+        o.dM = dJ_dp0inf * dp0inf_dM;
+        o.dth = 0.0;
+        return QLSKUM_OK;
+    }
     const double cp_scale = 0.5 * h->K.rho_inf * h->K.mach * h->K.mach;
     fp64::objective(h->L, h->dc, prim, h->d_wall_perm, h->d_wall_geo, h->shape_points, cp_scale, h->K.pr_inf,
                     h->K.gamma, h->d_entropy, h->d_obj, h->d_obj_partial);
-    zero(h, bP, sizeof(double4_32a) * h->np);
     adjl::objective(h->L, adj_view(h, false), h->d_wall_perm, h->d_wall_geo, h->shape_points, cp_scale, h->K.theta,
                     which, bP);
-    qlskum_status st = check_launch(h, "adjoint seed");
-    if (st) return st;
-    double o[4];
-    st = d2h(h, o, h->d_obj, sizeof o);
-    if (st) return st;
-    *cl = o[1] * std::cos(h->K.theta) - o[0] * std::sin(h->K.theta);
-    *cd = o[0] * std::cos(h->K.theta) + o[1] * std::sin(h->K.theta);
+    if ((st = check_launch(h, "adjoint seed"))) return st;
+    double v[4];
+    if ((st = d2h(h, v, h->d_obj, sizeof v))) return st;
+    const double cl = v[1] * std::cos(h->K.theta) - v[0] * std::sin(h->K.theta);
+    const double cd = v[0] * std::cos(h->K.theta) + v[1] * std::sin(h->K.theta);
+    o.J = which == QLSKUM_OBJECTIVE_CL ? cl : cd;
+    o.dM = -2.0 * o.J / h->K.mach;
+    o.dth = which == QLSKUM_OBJECTIVE_CL ? -cd : cl;
     return QLSKUM_OK;
 }
 
 // dJ/dMach and dJ/dAoA (per degree).  The free stream (u1, u2) =
 // M (cos theta, sin theta) enters through the far-field states (bars in
 // buinf) and, for a run from the free stream, the initial state (bars in
-// binit); J itself scales with 1 / M^2 (cp) and rotates with theta:
-// dCl/dtheta = -Cd, dCd/dtheta = Cl.
-void adj_params(const qlskum_handle *h, int which, double cl, double cd, const double buinf[2],
-                const double binit[2], double *dmach, double *daoa)
+// binit); plus the objective's explicit terms.
+void adj_params(const qlskum_handle *h, const ObjSeed &o, const double buinf[2], const double binit[2],
+                double *dmach, double *daoa)
 {
     const double th = h->K.theta, M = h->K.mach;
     const double b1 = buinf[0] + binit[0], b2 = buinf[1] + binit[1];
-    const double J = which == 0 ? cl : cd;
-    const double dM = -2.0 * J / M + b1 * std::cos(th) + b2 * std::sin(th);
-    const double dth = M * (-b1 * std::sin(th) + b2 * std::cos(th)) + (which == 0 ? -cd : cl);
+    const double dM = o.dM + b1 * std::cos(th) + b2 * std::sin(th);
+    const double dth = M * (-b1 * std::sin(th) + b2 * std::cos(th)) + o.dth;
     if (dmach) *dmach = dM;
     if (daoa) *daoa = dth * h->K.pi / 180.0;
 }
@@ -2221,12 +2262,13 @@ qlskum_status adj_geometry(qlskum_handle *h, int which, const double4_32a *prim_
         }
     }
     // the objective's geometry: H = sum cp nx ds, V = sum cp ny ds with
-    // ds = (|x_m - x_l| + |x_r - x_m|) / 2 (compute_force_coeffs_mod.h:37-59)
+    // ds = (|x_m - x_l| + |x_r - x_m|) / 2 (compute_force_coeffs_mod.h:37-59);
+    // the stagnation-pressure loss has none
     const double cp_scale = 0.5 * h->K.rho_inf * h->K.mach * h->K.mach;
     const double th = h->K.theta;
     const double bH = which == 0 ? -std::sin(th) : std::cos(th);
     const double bV = which == 0 ? std::cos(th) : std::sin(th);
-    for (int m = 0; m < h->shape_points; m++) {
+    for (int m = 0; m < (which == QLSKUM_OBJECTIVE_J ? 0 : h->shape_points); m++) {
         const int l = h->hleft[m] - 1, r = h->hright[m] - 1;
         const double cp = -(prim[h->perm[m]].w - h->K.pr_inf) / cp_scale;
         const double d1x = X[m] - X[l], d1y = Y[m] - Y[l], d2x = X[r] - X[m], d2y = Y[r] - Y[m];
@@ -2283,7 +2325,7 @@ qlskum_status download_points(qlskum_handle *h, const double4_32a *src, double *
 
 qlskum_status adj_args(qlskum_handle *h, int objective, int count, const double *dJ_dwall)
 {
-    if (objective != QLSKUM_OBJECTIVE_CL && objective != QLSKUM_OBJECTIVE_CD)
+    if (objective != QLSKUM_OBJECTIVE_CL && objective != QLSKUM_OBJECTIVE_CD && objective != QLSKUM_OBJECTIVE_J)
         return fail(h, QLSKUM_ERR_INVALID, fmt("unknown objective %d", objective));
     if (count < 1) return fail(h, QLSKUM_ERR_INVALID, "iteration count must be >= 1");
     if (dJ_dwall && h->prm.power != 0.0)
@@ -2374,8 +2416,8 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
         if ((st = qlskum_fpi_solver(h, t + 1))) return st;
     }
     if ((st = check_status(h))) return st;
-    double cl = 0, cd = 0;
-    if ((st = adj_seed(h, objective, h->s64.prim[h->pcur], a->bP, &cl, &cd))) return st;
+    ObjSeed os;
+    if ((st = adj_seed(h, objective, h->s64.prim[h->pcur], a->bP, os))) return st;
     adj_zero_geometry(h);
     const AdjView v = adj_view(h, true);
     const size_t bytes = sizeof(double4_32a) * np;
@@ -2416,8 +2458,8 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     }
     if (dJ_dprim0)
         for (int i = 0; i < h->n; i++) std::memcpy(dJ_dprim0 + 4 * (size_t)i, &b0[h->perm[i]], sizeof(double4_32a));
-    if (J) *J = objective == QLSKUM_OBJECTIVE_CL ? cl : cd;
-    adj_params(h, objective, cl, cd, bu, binit, dJ_dmach, dJ_daoa);
+    if (J) *J = os.J;
+    adj_params(h, os, bu, binit, dJ_dmach, dJ_daoa);
     if (dJ_dwall) return adj_geometry(h, objective, h->s64.prim[h->pcur], dJ_dwall);
     return QLSKUM_OK;
 }
@@ -2438,8 +2480,8 @@ qlskum_status qlskum_adjoint_fixed_point(qlskum_handle *h, int objective, int ad
     if (st) return st;
     AdjBuf *a = h->adj;
     const size_t np = h->np;
-    double cl = 0, cd = 0;
-    if ((st = adj_seed(h, objective, h->s64.prim[h->pcur], a->seed, &cl, &cd))) return st;
+    ObjSeed os;
+    if ((st = adj_seed(h, objective, h->s64.prim[h->pcur], a->seed, os))) return st;
     CK(h, cudaMemcpyAsync(a->P[0], h->s64.prim[h->pcur], sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice,
                           h->L.stream));
     zero(h, a->lam, sizeof(double4_32a) * np);
@@ -2479,8 +2521,8 @@ qlskum_status qlskum_adjoint_fixed_point(qlskum_handle *h, int objective, int ad
         *adj_change = lmax > 0.0 ? dmax / lmax : dmax;
     }
     const double binit[2] = {0, 0};
-    if (J) *J = objective == QLSKUM_OBJECTIVE_CL ? cl : cd;
-    adj_params(h, objective, cl, cd, bu, binit, dJ_dmach, dJ_daoa);
+    if (J) *J = os.J;
+    adj_params(h, os, bu, binit, dJ_dmach, dJ_daoa);
     if (dJ_dwall) return adj_geometry(h, objective, h->s64.prim[h->pcur], dJ_dwall);
     return QLSKUM_OK;
 }

@@ -183,6 +183,8 @@ void delta(const Launch &L, const AdjView &a, const double4_32a *P, const double
            double4_32a *bP);
 void objective(const Launch &L, const AdjView &a, const int *wall_perm, const double4_32a *wall_geo, int n_wall,
                double cp_scale, double theta, int which, double4_32a *bP);
+// bP += dJ/dprim of the stagnation-pressure loss
+void objective_J(const Launch &L, int n, const double4_32a *P, double gamma, double p0_inf, double4_32a *bP);
 }  // namespace adjl
 
 // ---------------------------------------------------------- FP64 kernels (qlskum_fp64.cu)
@@ -205,7 +207,7 @@ void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
 // dst += src over n double4 rows
 void add_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
 // diagnostics: vorticity [n] and per-256-block partial sums of its square;
-// stagnation pressure per-256-block {min, argmin, max, argmax, sum (p0_inf - p0)^2}
+// stagnation pressure per-256-block {min, argmin, max, argmax, sum (p0_inf - p0)^2, sum p0}
 void enstrophy(const Launch &L, const DevCloud &c, const double4_32a *prim, double *vort, double *partial);
 void stagnation(const Launch &L, int n, const double4_32a *prim, double gamma, double p0_inf, double *partial);
 // objectives: per-block partial sums into scratch ([4][ceil(max(n, n_wall)/256)]), then one ordered sum

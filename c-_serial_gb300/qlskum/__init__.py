@@ -20,6 +20,7 @@ MIXED = 1
 
 OBJECTIVE_CL = 0
 OBJECTIVE_CD = 1
+OBJECTIVE_J = 2
 
 FIELD_PRIM, FIELD_PRIM_OLD, FIELD_Q, FIELD_DQ, FIELD_QM, FIELD_FLUX_RES, FIELD_DELTA, FIELD_NORMALS, FIELD_ENTROPY = range(9)
 _FIELD_SHAPE = {FIELD_PRIM: (4,), FIELD_PRIM_OLD: (4,), FIELD_Q: (4,), FIELD_DQ: (2, 4), FIELD_QM: (2, 4),
@@ -380,7 +381,7 @@ class Solver:
         return out
 
     def _adjoint_out(self, objective, wall):
-        obj = {"cl": OBJECTIVE_CL, "cd": OBJECTIVE_CD}.get(objective, objective)
+        obj = {"cl": OBJECTIVE_CL, "cd": OBJECTIVE_CD, "j": OBJECTIVE_J}.get(objective, objective)
         vals = [C.c_double() for _ in range(4)]
         dw = np.zeros(self.shape_points) if wall else None
         return obj, vals, dw

@@ -282,6 +282,8 @@ qlskum_status qlskum_check_stencils(const qlskum_cloud *cloud, double power, dou
  * cloud's point order. */
 #define QLSKUM_OBJECTIVE_CL 0
 #define QLSKUM_OBJECTIVE_CD 1
+/* the stagnation-pressure loss J of qlskum_stagnation */
+#define QLSKUM_OBJECTIVE_J 2
 
 /* flux_res = R(prim): the local time step of prim (state_update_mod.h:448-496)
  * and the flux residual of the first stage (q_variables, q_derivatives, the
@@ -295,7 +297,8 @@ qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const do
 /* Runs `iters` iterations (as qlskum_q_lskum would; the handle holds the
  * final state afterwards) from prim0 (double [n][4]) or, when prim0 is NULL,
  * from the free stream, keeping each iteration's state, then sweeps the
- * iterations in reverse.  J: the objective (Cl or Cd) at the final state;
+ * iterations in reverse.  J: the objective (Cl, Cd or the stagnation loss)
+ * at the final state;
  * dJ_dmach, dJ_daoa (per degree): its exact derivatives through all `iters`
  * iterations (from the free stream these include the initial state's
  * dependence on Mach and AoA; a given prim0 is held fixed); dJ_dwall (or

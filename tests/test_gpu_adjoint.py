@@ -228,3 +228,34 @@ def test_fixed_point_adjoint_one_step_identity(qlskum):
     # more adjoint iterations and the wall gradient run through the same path
     r = s.adjoint_fixed_point("cd", adj_iters=20, wall=True)
     assert np.isfinite([r["J"], r["dmach"], r["daoa"], r["adj_change"]]).all() and np.isfinite(r["dwall"]).all()
+
+
+def _oracle_stag_J(oracle_mod, cloud, mach=MACH, aoa=AOA, iters=N):
+    o = oracle_mod.Oracle(cloud, mach=mach, aoa=aoa, inner_iterations=INNER, threads=4, **KW)
+    o.run(iters)
+    J = o.stagnation()[4]
+    o.close()
+    return J
+
+
+def test_adjoint_stagnation_loss_vs_oracle_fd(qlskum, oracle_mod):
+    """The stagnation-pressure loss J (qlskum_stagnation) as the adjoint's
+    objective: Mach (incl. p0_inf's own dependence), AoA and wall points."""
+    c = _cloud()
+    s = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **KW)
+    g = s.adjoint_gradient("j", iters=N, wall=True)
+    J0 = _oracle_stag_J(oracle_mod, c)
+    assert abs(g["J"] - J0) <= 1e-10 * abs(J0)
+    hm, ha = 1e-6, 1e-5
+    fd_m = (_oracle_stag_J(oracle_mod, c, mach=MACH + hm) - _oracle_stag_J(oracle_mod, c, mach=MACH - hm)) / (2 * hm)
+    fd_a = (_oracle_stag_J(oracle_mod, c, aoa=AOA + ha) - _oracle_stag_J(oracle_mod, c, aoa=AOA - ha)) / (2 * ha)
+    assert abs(g["dmach"] - fd_m) <= 1e-5 * abs(fd_m), (g["dmach"], fd_m)
+    assert abs(g["daoa"] - fd_a) <= 1e-5 * max(abs(fd_a), 1e-3 * abs(fd_m)), (g["daoa"], fd_a)
+    nrm = s.field(qlskum.FIELD_NORMALS)
+    dw = g["dwall"]
+    scale = np.abs(dw).max()
+    for m in (5, 17, 40):
+        h = 3e-8
+        fd = (_oracle_stag_J(oracle_mod, _moved(c, m, h * nrm[m])) -
+              _oracle_stag_J(oracle_mod, _moved(c, m, -h * nrm[m]))) / (2 * h)
+        assert abs(dw[m] - fd) <= 1e-5 * max(abs(fd), 1e-2 * scale), (m, dw[m], fd)
