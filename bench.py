@@ -355,6 +355,38 @@ def workload_config(workload, cloud=None):
     return c
 
 
+def measure_adjoint(sf, precision, k, stride, n):
+    """Wall-clock cost of one adjoint gradient (K kept iterations reversed)
+    and of one fixed-point adjoint iteration, each over the same handle's
+    primal iteration."""
+    sf.adjoint_gradient("cl", iters=k, stride=stride)          # first call allocates
+    t0 = time.perf_counter()
+    g = sf.adjoint_gradient("cl", iters=k, stride=stride)
+    t_adj = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sf.q_lskum(k)
+    sf.synchronize()
+    t_pr = time.perf_counter() - t0
+    # steady-state form: adjoint iterations at the current state, per iteration
+    sf.adjoint_fixed_point("cl", adj_iters=1)
+    t0 = time.perf_counter()
+    sf.adjoint_fixed_point("cl", adj_iters=k)
+    t_a = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sf.adjoint_fixed_point("cl", adj_iters=2 * k)
+    t_b = time.perf_counter() - t0
+    fp_it = max(t_b - t_a, 1e-9) / k
+    return {"objective": "cl", "iterations": k, "points": n, "checkpoint_stride": stride,
+            "primal_precision": precision,
+            "reverse": "mixed iteration (FP32 edge work, FP64 update)" if precision == "mixed" else "FP64 iteration",
+            "checkpointed": {"seconds": t_adj, "primal_seconds": t_pr, "adjoint_over_primal": t_adj / t_pr,
+                             "note": "K primal iterations from the free stream, kept, then reversed"},
+            "fixed_point": {"seconds_per_adjoint_iteration": fp_it,
+                            "seconds_per_primal_iteration": t_pr / k,
+                            "adjoint_over_primal": fp_it / (t_pr / k)},
+            "dcl_dmach": g["dmach"], "dcl_daoa_per_deg": g["daoa"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -368,7 +400,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--adjoint-iters", type=int, default=3,
-                    help="iterations differentiated by the adjoint timing on the FP64 handle (0: skip)")
+                    help="iterations differentiated by the adjoint timings (FP64 and mixed handles; 0: skip)")
     ap.add_argument("--launch", default="auto",
                     help="mixed launch shape 'flux_variant,point_block,staged' (e.g. 6,64,0) instead of autotuning")
     args = ap.parse_args()
@@ -449,39 +481,19 @@ def main():
                "after_iterations": args.warmup + args.steps,
                "cl": cl, "cd": cd, "abs_dcl": abs(cl - cl2), "abs_dcd": abs(cd - cd2)}
 
-    # discrete adjoint on the FP64 handle: dCl/dMach, dCl/dAoA through K
-    # iterations from the free stream (checkpointed primal + reverse sweep),
-    # against the same K primal iterations; host-synchronous calls, wall clock
-    adjoint = None
+    # discrete adjoint: dCl/dMach, dCl/dAoA through K iterations from the
+    # free stream (checkpointed primal + reverse sweep), against the same K
+    # primal iterations on the same handle; host-synchronous calls, wall
+    # clock.  The FP64 handle (the drop-in form) and the mixed handle (the
+    # reverse of the mixed iteration); the two-element workload only the
+    # mixed one.
+    adjoint = adjoint_mixed = None
     if args.adjoint_iters > 0:
-        # FP64 handle (the drop-in form) unless the workload asks for the adjoint of the mixed run
-        sf = solver if (args.workload == "two_element" or other != qlskum.FP64) else s2
-        k = args.adjoint_iters
-        sf.adjoint_gradient("cl", iters=k, stride=args.adjoint_stride)          # first call allocates
-        t0 = time.perf_counter()
-        g = sf.adjoint_gradient("cl", iters=k, stride=args.adjoint_stride)
-        t_adj = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        sf.q_lskum(k)
-        sf.synchronize()
-        t_pr = time.perf_counter() - t0
-        # steady-state form: adjoint iterations at the current state, per iteration
-        sf.adjoint_fixed_point("cl", adj_iters=1)
-        t0 = time.perf_counter()
-        sf.adjoint_fixed_point("cl", adj_iters=k)
-        t_a = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        sf.adjoint_fixed_point("cl", adj_iters=2 * k)
-        t_b = time.perf_counter() - t0
-        fp_it = max(t_b - t_a, 1e-9) / k
-        adjoint = {"objective": "cl", "iterations": k, "points": cloud.n, "checkpoint_stride": args.adjoint_stride,
-                   "primal_precision": "mixed" if sf is solver and prec == qlskum.MIXED else "fp64",
-                   "checkpointed": {"seconds": t_adj, "primal_seconds": t_pr, "adjoint_over_primal": t_adj / t_pr,
-                                    "note": "K primal iterations from the free stream, kept, then reversed"},
-                   "fixed_point": {"seconds_per_adjoint_iteration": fp_it,
-                                   "seconds_per_primal_iteration": t_pr / k,
-                                   "adjoint_over_primal": fp_it / (t_pr / k)},
-                   "dcl_dmach": g["dmach"], "dcl_daoa_per_deg": g["daoa"]}
+        mixed_h = solver if prec == qlskum.MIXED else s2
+        fp64_h = s2 if prec == qlskum.MIXED else solver
+        adjoint_mixed = measure_adjoint(mixed_h, "mixed", args.adjoint_iters, args.adjoint_stride, cloud.n)
+        if args.workload != "two_element":
+            adjoint = measure_adjoint(fp64_h, "fp64", args.adjoint_iters, args.adjoint_stride, cloud.n)
     del s2
 
     # end to end through the C ABI with host buffers
@@ -513,6 +525,7 @@ def main():
             "e2e": {"value": e2e_v, "unit": "point-iter/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "roofline": roofline, "cpu_baseline": cpu, "fp64_vs_mixed": compare, "adjoint": adjoint,
+            "adjoint_mixed": adjoint_mixed,
             "kernel_ms_per_iteration": {k: v[0] / max(1, 2) for k, v in kt.items()},
             "launch_config": solver.launch_config(),
         }

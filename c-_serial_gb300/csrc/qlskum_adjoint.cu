@@ -546,6 +546,350 @@ __global__ void k_objective_J(int n, const double4_32a *__restrict__ P, double g
 
 }  // namespace adjk
 
+// ---------------------------------------------------------------------------
+// Reverse of the mixed-precision iteration (qlskum_mixed.cu): the per-edge
+// work in FP32 with the FP32 instantiations of the reverse-mode functions,
+// neighbour bars scattered with FP32 atomics, the stage update's reverse in
+// FP64 (adjk::k_update).  Each kernel differentiates what its forward kernel
+// computes: the flux kernel's folded solve weights and branch-free half-range
+// selection, the gradient's FP32 sums with the FP64 solve coefficients, q of
+// the FP32-rounded state, the FP32 time step and wave speed.
+namespace adjm {
+
+using adj::KinBarT;
+
+// one 16-byte vector reduction (sm_90 and later; float4 arrays are 16-byte aligned)
+__device__ __forceinline__ void atomic_add4(float4 *p, const float v[4])
+{
+    atomicAdd(p, make_float4(v[0], v[1], v[2], v[3]));
+}
+
+__device__ __forceinline__ void ldf4(const float4 &a, float o[4]) { o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; }
+
+// limiters_mod.h:64-104 as the mixed forward evaluates it (venkat32)
+__device__ __forceinline__ float venkat_f(float qt, float q, float qmax, float qmin, float eps2)
+{
+    const float dn = qt - q;
+    const float dp = (dn > 0.f) ? qmax - q : qmin - q;
+    const float dp2 = dp * dp;
+    const float num = fmaf(2.0f * dn, dp, dp2 + eps2);
+    const float den = fmaf(dn, dp, fmaf(2.0f * dn, dn, dp2 + eps2));
+    const float phi = fminf(__fdividef(num, den), 1.0f);
+    return fabsf(dn) <= 10e-6f ? 1.0f : phi;
+}
+
+// reconstructed end q~ of one edge end, as edge_states32 computes it
+__device__ __forceinline__ void qtilde_f(float delx, float dely, const float q[4], const float dx[4],
+                                        const float dy[4], const float mx[4], const float mn[4], float e2, float t[4])
+{
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const float g = fmaf(delx, dx[r], dely * dy[r]);
+        const float phi = venkat_f(fmaf(-0.5f, g, q[r]), q[r], mx[r], mn[r], e2);
+        t[r] = fmaf(-0.5f * phi, g, q[r]);
+    }
+}
+
+__device__ __forceinline__ void x_flux_vjp(int f, const Kin<float> &k, float s1, const float bG[4], KinBarT<float> &kb)
+{
+    if (f == kInterior) adj::flux_x_vjp<float>(k, s1, bG, kb);
+    else adj::flux_quad_vjp<float>(k, s1, (f == kOuter) ? 1.0f : -1.0f, bG, kb);
+}
+
+// Reverse of the flux part of the mixed flux + update kernel for stage
+// state (q, dq, qm): F = delta * acc, acc = sum_e w_e (G_k - G_i) over each
+// edge's x and y half-ranges.  bF (FP64, from adjk::k_update) in; bars of
+// q, dq, qm (own and neighbours'), and of delta (owner) out.
+template <bool UW>
+__global__ void __launch_bounds__(128) k_flux(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ dq,
+                                               const float4 *__restrict__ qm, const float *__restrict__ delta,
+                                               const float4 *__restrict__ acc, const double4_32a *__restrict__ bF,
+                                               float4 *__restrict__ bq, float4 *__restrict__ bdq,
+                                               float4 *__restrict__ bqm, float *__restrict__ bdelta)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const int f = c.flag[i];
+    const double2 nn = c.nrm[i];
+    const float nx = (float)nn.x, ny = (float)nn.y;
+    float qi[4], dxi[4], dyi[4], mxi[4], mni[4];
+    ldf4(q[i], qi);
+    ldf4(dq[2 * i], dxi);
+    ldf4(dq[2 * i + 1], dyi);
+    ldf4(qm[2 * i], mxi);
+    ldf4(qm[2 * i + 1], mni);
+    const float e2i = c.eps2_32[i];
+    const double4_32a bFi = bF[i];
+    const float4 ac = acc[i];
+    const float dl = delta[i];
+    bdelta[i] += (float)(bFi.x * ac.x + bFi.y * ac.y + bFi.z * ac.z + bFi.w * ac.w);
+    const float bacc[4] = {(float)(dl * bFi.x), (float)(dl * bFi.y), (float)(dl * bFi.z), (float)(dl * bFi.w)};
+    float bqi[4] = {0, 0, 0, 0}, bdxi[4] = {0, 0, 0, 0}, bdyi[4] = {0, 0, 0, 0}, bmxi[4] = {0, 0, 0, 0},
+          bmni[4] = {0, 0, 0, 0};
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        float delx, dely;
+        if (UW) {
+            const float2 d = c.e_xy32[e];
+            delx = d.x;
+            dely = d.y;
+        } else {
+            const float4 g = c.e_geo32[e];
+            delx = g.x;
+            dely = g.y;
+        }
+        const float2 w = c.e_w32[e];
+        const unsigned dir = c.e_dir[e];
+        float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
+        ldf4(q[k], qk);
+        ldf4(dq[2 * k], dxk);
+        ldf4(dq[2 * k + 1], dyk);
+        ldf4(qm[2 * k], mxk);
+        ldf4(qm[2 * k + 1], mnk);
+        const float e2k = c.eps2_32[k];
+        float ti[4], tk[4], Pi[4], Pk[4];
+        qtilde_f(delx, dely, qi, dxi, dyi, mxi, mni, e2i, ti);
+        qtilde_f(delx, dely, qk, dxk, dyk, mxk, mnk, e2k, tk);
+        qtilde_to_prim<float>(ti, Pi[1], Pi[2], Pi[0], Pi[3]);
+        qtilde_to_prim<float>(tk, Pk[1], Pk[2], Pk[0], Pk[3]);
+        Kin<float> ki, kk;
+        kin_prep<float>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
+        kin_prep<float>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
+        KinBarT<float> kbi, kbk;
+        float bGk[4], bGi[4];
+        const float s1 = (dir & kXpos) ? 1.0f : -1.0f;
+#pragma unroll
+        for (int r = 0; r < 4; r++) { bGk[r] = w.x * bacc[r]; bGi[r] = -bGk[r]; }
+        x_flux_vjp(f, kk, s1, bGk, kbk);
+        x_flux_vjp(f, ki, s1, bGi, kbi);
+        const float s2 = (dir & kYpos) ? 1.0f : -1.0f;
+#pragma unroll
+        for (int r = 0; r < 4; r++) { bGk[r] = w.y * bacc[r]; bGi[r] = -bGk[r]; }
+        adj::flux_y_vjp<float>(kk, s2, bGk, kbk);
+        adj::flux_y_vjp<float>(ki, s2, bGi, kbi);
+        const bool xb = (dir & (kXpos | kXneg)) == (kXpos | kXneg), yb = (dir & (kYpos | kYneg)) == (kYpos | kYneg);
+        if (xb || yb) {
+            const float2 w2 = c.e_w32b[e];
+            if (xb) {
+#pragma unroll
+                for (int r = 0; r < 4; r++) { bGk[r] = w2.x * bacc[r]; bGi[r] = -bGk[r]; }
+                x_flux_vjp(f, kk, -1.0f, bGk, kbk);
+                x_flux_vjp(f, ki, -1.0f, bGi, kbi);
+            }
+            if (yb) {
+#pragma unroll
+                for (int r = 0; r < 4; r++) { bGk[r] = w2.y * bacc[r]; bGi[r] = -bGk[r]; }
+                adj::flux_y_vjp<float>(kk, -1.0f, bGk, kbk);
+                adj::flux_y_vjp<float>(ki, -1.0f, bGi, kbi);
+            }
+        }
+        float bPi[4] = {0, 0, 0, 0}, bPk[4] = {0, 0, 0, 0}, bn0 = 0.f, bn1 = 0.f;
+        adj::kin_vjp<float>(nx, ny, Pi, ki, kbi, bPi, bn0, bn1);
+        adj::kin_vjp<float>(nx, ny, Pk, kk, kbk, bPk, bn0, bn1);
+        float bti[4] = {0, 0, 0, 0}, btk[4] = {0, 0, 0, 0};
+        adj::qtilde_to_prim_vjp<float>(ti, bPi, bti);
+        adj::qtilde_to_prim_vjp<float>(tk, bPk, btk);
+        float bdelx = 0.f, bdely = 0.f;
+        adj::edge_end_vjp<float>(delx, dely, qi, dxi, dyi, mxi, mni, e2i, bti, bqi, bdxi, bdyi, bmxi, bmni, bdelx,
+                                 bdely);
+        float bqk[4] = {0, 0, 0, 0}, bdxk[4] = {0, 0, 0, 0}, bdyk[4] = {0, 0, 0, 0}, bmxk[4] = {0, 0, 0, 0},
+              bmnk[4] = {0, 0, 0, 0};
+        adj::edge_end_vjp<float>(delx, dely, qk, dxk, dyk, mxk, mnk, e2k, btk, bqk, bdxk, bdyk, bmxk, bmnk, bdelx,
+                                 bdely);
+        atomic_add4(bq + k, bqk);
+        atomic_add4(bdq + 2 * k, bdxk);
+        atomic_add4(bdq + 2 * k + 1, bdyk);
+        atomic_add4(bqm + 2 * k, bmxk);
+        atomic_add4(bqm + 2 * k + 1, bmnk);
+    }
+    atomic_add4(bq + i, bqi);
+    atomic_add4(bdq + 2 * i, bdxi);
+    atomic_add4(bdq + 2 * i + 1, bdyi);
+    atomic_add4(bqm + 2 * i, bmxi);
+    atomic_add4(bqm + 2 * i + 1, bmni);
+}
+
+// The FP64 2x2 solve dx = X a - Y b, dy = Y c - X b (a = syy/det, b =
+// sxy/det, c = sxx/det) in reverse, in FP32.
+__device__ __forceinline__ void solve_vjp(const double4_32a &m, const float bx[4], const float by[4], float bX[4],
+                                          float bY[4])
+{
+    const float a = (float)m.x, b = (float)m.y, cc = (float)m.z;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        bX[r] = bx[r] * a - by[r] * b;
+        bY[r] = by[r] * cc - bx[r] * b;
+    }
+}
+
+template <bool UW> __device__ __forceinline__ float4 edge_w(const DevCloud &c, long long e)
+{
+    if (UW) {
+        const float2 d = c.e_xy32[e];
+        return make_float4(d.x, d.y, d.x, d.y);
+    }
+    return c.e_geo32[e];
+}
+
+// Reverse of one mixed inner iteration (q_variables_mod.h:120-213).
+template <bool UW>
+__global__ void k_inner(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ dq_in,
+                        const float4 *__restrict__ bdq_out, float4 *__restrict__ bq, float4 *__restrict__ bdq_in)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    float bx[4], by[4], bsdx[4], bsdy[4];
+    ldf4(bdq_out[2 * i], bx);
+    ldf4(bdq_out[2 * i + 1], by);
+    solve_vjp(c.gcoef[i], bx, by, bsdx, bsdy);
+    float dxi[4], dyi[4];
+    ldf4(dq_in[2 * i], dxi);
+    ldf4(dq_in[2 * i + 1], dyi);
+    float bqi[4] = {0, 0, 0, 0}, bdxi[4] = {0, 0, 0, 0}, bdyi[4] = {0, 0, 0, 0};
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const float4 g = edge_w<UW>(c, e);
+        float bqk[4], bdxk[4], bdyk[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const float bt = g.z * bsdx[r] + g.w * bsdy[r];
+            bqk[r] = bt;
+            bdxk[r] = -0.5f * g.x * bt;
+            bdyk[r] = -0.5f * g.y * bt;
+            bqi[r] -= bt;
+            bdxi[r] += 0.5f * g.x * bt;
+            bdyi[r] += 0.5f * g.y * bt;
+        }
+        atomic_add4(bq + k, bqk);
+        atomic_add4(bdq_in + 2 * k, bdxk);
+        atomic_add4(bdq_in + 2 * k + 1, bdyk);
+    }
+    atomic_add4(bq + i, bqi);
+    atomic_add4(bdq_in + 2 * i, bdxi);
+    atomic_add4(bdq_in + 2 * i + 1, bdyi);
+}
+
+// Reverse of the mixed gradient and neighbour max / min (q_variables_mod.h:36-118).
+template <bool UW>
+__global__ void k_grad(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ bdq,
+                       const float4 *__restrict__ bqm, float4 *__restrict__ bq)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    float bx[4], by[4], bsdx[4], bsdy[4], bmax[4], bmin[4], qi[4];
+    ldf4(bdq[2 * i], bx);
+    ldf4(bdq[2 * i + 1], by);
+    ldf4(bqm[2 * i], bmax);
+    ldf4(bqm[2 * i + 1], bmin);
+    ldf4(q[i], qi);
+    solve_vjp(c.gcoef[i], bx, by, bsdx, bsdy);
+    float qmax[4], qmin[4];
+    int amax[4], amin[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        qmax[r] = qmin[r] = qi[r];
+        amax[r] = amin[r] = i;
+    }
+    float bqi[4] = {0, 0, 0, 0};
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const float4 g = edge_w<UW>(c, e);
+        float qk[4], bqk[4];
+        ldf4(q[k], qk);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            if (qk[r] > qmax[r]) { qmax[r] = qk[r]; amax[r] = k; }
+            if (qk[r] < qmin[r]) { qmin[r] = qk[r]; amin[r] = k; }
+            const float bt = g.z * bsdx[r] + g.w * bsdy[r];
+            bqk[r] = bt;
+            bqi[r] -= bt;
+        }
+        atomic_add4(bq + k, bqk);
+    }
+    atomic_add4(bq + i, bqi);
+    float *bqd = reinterpret_cast<float *>(bq);
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        if (bmax[r] != 0.f) atomicAdd(bqd + 4 * (size_t)amax[r] + r, bmax[r]);
+        if (bmin[r] != 0.f) atomicAdd(bqd + 4 * (size_t)amin[r] + r, bmin[r]);
+    }
+}
+
+// bP += (dq/dP)^T bq for q = prim_to_q of the FP32-rounded state.
+__global__ void k_q(int n, const double4_32a *__restrict__ P, const float4 *__restrict__ bq,
+                    double4_32a *__restrict__ bP)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double4_32a p = P[i];
+    const float pf[4] = {(float)p.x, (float)p.y, (float)p.z, (float)p.w};
+    float b[4], g[4] = {0, 0, 0, 0};
+    ldf4(bq[i], b);
+    adj::prim_to_q_vjp<float>(pf, b, g);
+    double4_32a acc = bP[i];
+    acc.x += g[0];
+    acc.y += g[1];
+    acc.z += g[2];
+    acc.w += g[3];
+    bP[i] = acc;
+}
+
+// Reverse of the FP32 local time step min(1, min_k cfl |dr| / c_k): the bar
+// goes to the wave speed of the neighbour that set the minimum.
+template <bool UW>
+__global__ void k_delta(DevCloud c, const float *__restrict__ cs, const float *__restrict__ bdelta, float cfl,
+                        float *__restrict__ bcs)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n || bdelta[i] == 0.f) return;
+    float min_dt = 1.0f, carg = 0.f, darg = 0.f;
+    int arg = -1;
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const float d = c.e_dist32[e], ck = cs[k];
+        const float dt = cfl * __fdividef(d, ck);
+        if (dt < min_dt) {
+            min_dt = dt;
+            arg = k;
+            carg = ck;
+            darg = d;
+        }
+    }
+    if (arg >= 0) atomicAdd(bcs + arg, -bdelta[i] * cfl * darg / (carg * carg));
+}
+
+// bP += (dc/dP)^T bc for the FP32 wave speed |u| + 3 sqrt(p / rho).
+__global__ void k_wave(int n, const double4_32a *__restrict__ P, const float *__restrict__ bc,
+                       double4_32a *__restrict__ bP)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || bc[i] == 0.f) return;
+    const double4_32a p = P[i];
+    const float pf[4] = {(float)p.x, (float)p.y, (float)p.z, (float)p.w};
+    float g[4] = {0, 0, 0, 0};
+    adj::wave_speed_vjp<float>(pf, bc[i], g);
+    double4_32a acc = bP[i];
+    acc.x += g[0];
+    acc.y += g[1];
+    acc.z += g[2];
+    acc.w += g[3];
+    bP[i] = acc;
+}
+
+}  // namespace adjm
+
 // ------------------------------------------------------------- launchers
 
 namespace adjl {
@@ -615,4 +959,48 @@ void objective(const Launch &L, const AdjView &a, const int *wall_perm, const do
 }
 
 }  // namespace adjl
+
+namespace adjml {
+
+static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
+
+void flux(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq, const float4 *qm, const float *delta,
+          const float4 *acc, const double4_32a *bF, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta)
+{
+    if (c.unit_w)
+        adjm::k_flux<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq, qm, delta, acc, bF, bq, bdq, bqm, bdelta);
+    else
+        adjm::k_flux<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq, qm, delta, acc, bF, bq, bdq, bqm,
+                                                                      bdelta);
+}
+
+void inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, const float4 *bdq_out,
+           float4 *bq, float4 *bdq_in)
+{
+    if (c.unit_w)
+        adjm::k_inner<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq_in, bdq_out, bq, bdq_in);
+    else
+        adjm::k_inner<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq_in, bdq_out, bq, bdq_in);
+}
+
+void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq, const float4 *bqm, float4 *bq)
+{
+    if (c.unit_w) adjm::k_grad<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, bdq, bqm, bq);
+    else adjm::k_grad<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, bdq, bqm, bq);
+}
+
+void qvars(const Launch &L, int n, const double4_32a *P, const float4 *bq, double4_32a *bP)
+{
+    adjm::k_q<<<grid_for(n, 256), 256, 0, L.stream>>>(n, P, bq, bP);
+}
+
+void delta(const Launch &L, const DevCloud &c, const double4_32a *P, const float *cs, const float *bdelta, float cfl,
+           float *bcs, double4_32a *bP)
+{
+    if (c.unit_w) adjm::k_delta<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, cs, bdelta, cfl, bcs);
+    else adjm::k_delta<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, cs, bdelta, cfl, bcs);
+    adjm::k_wave<<<grid_for(c.n, 256), 256, 0, L.stream>>>(c.n, P, bcs, bP);
+}
+
+}  // namespace adjml
 }  // namespace qlskum

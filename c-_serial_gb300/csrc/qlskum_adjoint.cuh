@@ -1,5 +1,8 @@
 // Reverse mode (vector-Jacobian products) of the per-point and per-edge
-// arithmetic of qlskum_math.cuh, FP64, host + device.
+// arithmetic of qlskum_math.cuh, host + device.  The per-edge functions are
+// templates on the real type: FP64 for the adjoint of the drop-in form, FP32
+// for the adjoint of the mixed form (with its SFU exp / log); the boundary
+// update stays FP64 in both.
 //
 // Each *_vjp function takes the forward inputs (it recomputes what it needs)
 // and the bar (adjoint) of the forward outputs, and ADDS the bars of the
@@ -18,34 +21,34 @@ namespace qlskum {
 namespace adj {
 
 // q_variables_mod.h:19-33
-QLSKUM_HD void prim_to_q_vjp(const double P[4], const double bq[4], double bP[4])
+template <typename R> QLSKUM_HD void prim_to_q_vjp(const R P[4], const R bq[4], R bP[4])
 {
-    const double rho = P[0], u1 = P[1], u2 = P[2], p = P[3];
-    const double beta = 0.5 * rho / p;
-    const double usq = u1 * u1 + u2 * u2;
-    const double bbeta = bq[0] * (2.5 / beta - usq) + bq[1] * 2.0 * u1 + bq[2] * 2.0 * u2 - 2.0 * bq[3];
-    bP[0] += bq[0] / rho + bbeta * 0.5 / p;
-    bP[1] += -bq[0] * 2.0 * beta * u1 + bq[1] * 2.0 * beta;
-    bP[2] += -bq[0] * 2.0 * beta * u2 + bq[2] * 2.0 * beta;
+    const R rho = P[0], u1 = P[1], u2 = P[2], p = P[3];
+    const R beta = R(0.5) * rho / p;
+    const R usq = u1 * u1 + u2 * u2;
+    const R bbeta = bq[0] * (R(2.5) / beta - usq) + bq[1] * R(2.0) * u1 + bq[2] * R(2.0) * u2 - R(2.0) * bq[3];
+    bP[0] += bq[0] / rho + bbeta * R(0.5) / p;
+    bP[1] += -bq[0] * R(2.0) * beta * u1 + bq[1] * R(2.0) * beta;
+    bP[2] += -bq[0] * R(2.0) * beta * u2 + bq[2] * R(2.0) * beta;
     bP[3] += -bbeta * beta / p;
 }
 
 // limiters_mod.h:64-104 for one component.
-QLSKUM_HD void venkat_vjp(double qt, double q, double qmax, double qmin, double eps2, double bphi, double &bqt,
-                          double &bq, double &bqmax, double &bqmin)
+template <typename R> QLSKUM_HD void venkat_vjp(R qt, R q, R qmax, R qmin, R eps2, R bphi, R &bqt,
+                          R &bq, R &bqmax, R &bqmin)
 {
-    const double dn = qt - q;
-    if (fabs(dn) <= 10e-6) return;
+    const R dn = qt - q;
+    if (M<R>::ab(dn) <= R(10e-6)) return;
     const bool up = dn > 0;
-    const double dp = (up ? qmax : qmin) - q;
-    const double num = (dp * dp + eps2) * dn + 2.0 * dn * dn * dp;
-    const double den = (dp * dp + 2.0 * dn * dn + dn * dp + eps2) * dn;
-    const double t = num / den;
-    if (!(t < 1.0)) return;
-    const double bnum = bphi / den, bden = -bphi * t / den;
-    const double bdn = bnum * (dp * dp + eps2 + 4.0 * dn * dp) +
-                       bden * ((dp * dp + 2.0 * dn * dn + dn * dp + eps2) + dn * (4.0 * dn + dp));
-    const double bdp = bnum * (2.0 * dp * dn + 2.0 * dn * dn) + bden * (dn * (2.0 * dp + dn));
+    const R dp = (up ? qmax : qmin) - q;
+    const R num = (dp * dp + eps2) * dn + R(2.0) * dn * dn * dp;
+    const R den = (dp * dp + R(2.0) * dn * dn + dn * dp + eps2) * dn;
+    const R t = num / den;
+    if (!(t < R(1.0))) return;
+    const R bnum = bphi / den, bden = -bphi * t / den;
+    const R bdn = bnum * (dp * dp + eps2 + R(4.0) * dn * dp) +
+                       bden * ((dp * dp + R(2.0) * dn * dn + dn * dp + eps2) + dn * (R(4.0) * dn + dp));
+    const R bdp = bnum * (R(2.0) * dp * dn + R(2.0) * dn * dn) + bden * (dn * (R(2.0) * dp + dn));
     bqt += bdn;
     bq -= bdn + bdp;
     if (up) bqmax += bdp;
@@ -53,49 +56,50 @@ QLSKUM_HD void venkat_vjp(double qt, double q, double qmax, double qmin, double 
 }
 
 // q_variables_mod.h:230-253; P = (rho, u1, u2, p).
-QLSKUM_HD void qtilde_to_prim_vjp(const double qt[4], const double bP[4], double bqt[4])
+template <typename R> QLSKUM_HD void qtilde_to_prim_vjp(const R qt[4], const R bP[4], R bqt[4])
 {
-    const double gm1 = 1.4 - 1.0;
-    const double beta = -qt[3] * 0.5;
-    const double t = 0.5 / beta;
-    const double u1 = qt[1] * t, u2 = qt[2] * t;
-    const double T1 = qt[0] + beta * (u1 * u1 + u2 * u2);
-    const double rho = exp(T1 - log(beta) / gm1);
-    const double brho = bP[0] + bP[3] * t;
-    const double bT2 = brho * rho, bT1 = bT2;
-    const double bu1 = bP[1] + bT1 * 2.0 * beta * u1;
-    const double bu2 = bP[2] + bT1 * 2.0 * beta * u2;
-    const double bt = bP[3] * rho + bu1 * qt[1] + bu2 * qt[2];
-    const double bbeta = bT1 * (u1 * u1 + u2 * u2) - bT2 / (gm1 * beta) - bt * 0.5 / (beta * beta);
+    const R gm1 = R(1.4) - R(1.0);
+    const R beta = -qt[3] * R(0.5);
+    const R t = R(0.5) / beta;
+    const R u1 = qt[1] * t, u2 = qt[2] * t;
+    const R T1 = qt[0] + beta * (u1 * u1 + u2 * u2);
+    const R rho = M<R>::ex(T1 - M<R>::lg(beta) / gm1);
+    const R brho = bP[0] + bP[3] * t;
+    const R bT2 = brho * rho, bT1 = bT2;
+    const R bu1 = bP[1] + bT1 * R(2.0) * beta * u1;
+    const R bu2 = bP[2] + bT1 * R(2.0) * beta * u2;
+    const R bt = bP[3] * rho + bu1 * qt[1] + bu2 * qt[2];
+    const R bbeta = bT1 * (u1 * u1 + u2 * u2) - bT2 / (gm1 * beta) - bt * R(0.5) / (beta * beta);
     bqt[0] += bT1;
     bqt[1] += bu1 * t;
     bqt[2] += bu2 * t;
-    bqt[3] += -0.5 * bbeta;
+    bqt[3] += -R(0.5) * bbeta;
 }
 
-// Bars of the fields of Kin<double>.
-struct KinBar {
-    double rho = 0, ut = 0, un = 0, pbr = 0, usq = 0, B1 = 0, B2 = 0, E1 = 0, E2 = 0;
+// Bars of the fields of Kin<R>.
+template <typename R> struct KinBarT {
+    R rho = 0, ut = 0, un = 0, pbr = 0, usq = 0, B1 = 0, B2 = 0, E1 = 0, E2 = 0;
 };
+using KinBar = KinBarT<double>;
 
 // kin_prep (split_fluxes_mod.h:14-26): bars of (u1, u2, rho, p) and of the normal.
-QLSKUM_HD void kin_vjp(double nx, double ny, const double P[4], const Kin<double> &k, const KinBar &kb, double bP[4],
-                       double &bnx, double &bny)
+template <typename R> QLSKUM_HD void kin_vjp(R nx, R ny, const R P[4], const Kin<R> &k, const KinBarT<R> &kb, R bP[4],
+                       R &bnx, R &bny)
 {
-    const double rho = P[0], u1 = P[1], u2 = P[2], p = P[3];
-    const double beta = 0.5 * rho / p;
-    const double sb = sqrt(beta);
-    const double S1 = k.ut * sb, S2 = k.un * sb;
-    const double two_over_sqrtpi = 1.1283791670955126;
-    double but = kb.ut + 2.0 * k.ut * kb.usq;
-    double bun = kb.un + 2.0 * k.un * kb.usq;
-    const double bS1 = kb.E1 * two_over_sqrtpi * exp(-S1 * S1) + kb.B1 * k.B1 * (-2.0 * S1);
-    const double bS2 = kb.E2 * two_over_sqrtpi * exp(-S2 * S2) + kb.B2 * k.B2 * (-2.0 * S2);
+    const R rho = P[0], u1 = P[1], u2 = P[2], p = P[3];
+    const R beta = R(0.5) * rho / p;
+    const R sb = M<R>::sq(beta);
+    const R S1 = k.ut * sb, S2 = k.un * sb;
+    const R two_over_sqrtpi = R(1.1283791670955126);
+    R but = kb.ut + R(2.0) * k.ut * kb.usq;
+    R bun = kb.un + R(2.0) * k.un * kb.usq;
+    const R bS1 = kb.E1 * two_over_sqrtpi * M<R>::ex(-S1 * S1) + kb.B1 * k.B1 * (-R(2.0) * S1);
+    const R bS2 = kb.E2 * two_over_sqrtpi * M<R>::ex(-S2 * S2) + kb.B2 * k.B2 * (-R(2.0) * S2);
     but += bS1 * sb;
     bun += bS2 * sb;
-    const double bsb = bS1 * k.ut + bS2 * k.un;
-    const double bbeta = bsb * 0.5 / sb - (kb.B1 * k.B1 + kb.B2 * k.B2) * 0.5 / beta;
-    bP[0] += kb.rho + bbeta * 0.5 / p - kb.pbr * p / (rho * rho);
+    const R bsb = bS1 * k.ut + bS2 * k.un;
+    const R bbeta = bsb * R(0.5) / sb - (kb.B1 * k.B1 + kb.B2 * k.B2) * R(0.5) / beta;
+    bP[0] += kb.rho + bbeta * R(0.5) / p - kb.pbr * p / (rho * rho);
     bP[3] += -bbeta * beta / p + kb.pbr / rho;
     bP[1] += but * ny + bun * nx;
     bP[2] += -but * nx + bun * ny;
@@ -104,71 +108,71 @@ QLSKUM_HD void kin_vjp(double nx, double ny, const double P[4], const Kin<double
 }
 
 // flux_Gxp / flux_Gxn
-QLSKUM_HD void flux_x_vjp(const Kin<double> &k, double s1, const double bG[4], KinBar &kb)
+template <typename R> QLSKUM_HD void flux_x_vjp(const Kin<R> &k, R s1, const R bG[4], KinBarT<R> &kb)
 {
-    const double A1 = 0.5 * (1.0 + s1 * k.E1), B1s = s1 * k.B1;
-    const double ut = k.ut, un = k.un, pbr = k.pbr, usq = k.usq, rho = k.rho;
-    const double a0 = ut * A1 + B1s, a1 = (pbr + ut * ut) * A1 + ut * B1s, a2 = ut * un * A1 + un * B1s;
-    const double a3 = 0.5 * ut * (7.0 * pbr + usq) * A1 + 0.5 * (6.0 * pbr + usq) * B1s;
+    const R A1 = R(0.5) * (R(1.0) + s1 * k.E1), B1s = s1 * k.B1;
+    const R ut = k.ut, un = k.un, pbr = k.pbr, usq = k.usq, rho = k.rho;
+    const R a0 = ut * A1 + B1s, a1 = (pbr + ut * ut) * A1 + ut * B1s, a2 = ut * un * A1 + un * B1s;
+    const R a3 = R(0.5) * ut * (R(7.0) * pbr + usq) * A1 + R(0.5) * (R(6.0) * pbr + usq) * B1s;
     kb.rho += bG[0] * a0 + bG[1] * a1 + bG[2] * a2 + bG[3] * a3;
-    const double b0 = rho * bG[0], b1 = rho * bG[1], b2 = rho * bG[2], b3 = rho * bG[3];
-    const double bA1 = b0 * ut + b1 * (pbr + ut * ut) + b2 * ut * un + b3 * 0.5 * ut * (7.0 * pbr + usq);
-    const double bB1s = b0 + b1 * ut + b2 * un + b3 * 0.5 * (6.0 * pbr + usq);
-    kb.ut += b0 * A1 + b1 * (2.0 * ut * A1 + B1s) + b2 * un * A1 + b3 * 0.5 * (7.0 * pbr + usq) * A1;
+    const R b0 = rho * bG[0], b1 = rho * bG[1], b2 = rho * bG[2], b3 = rho * bG[3];
+    const R bA1 = b0 * ut + b1 * (pbr + ut * ut) + b2 * ut * un + b3 * R(0.5) * ut * (R(7.0) * pbr + usq);
+    const R bB1s = b0 + b1 * ut + b2 * un + b3 * R(0.5) * (R(6.0) * pbr + usq);
+    kb.ut += b0 * A1 + b1 * (R(2.0) * ut * A1 + B1s) + b2 * un * A1 + b3 * R(0.5) * (R(7.0) * pbr + usq) * A1;
     kb.un += b2 * (ut * A1 + B1s);
-    kb.pbr += b1 * A1 + b3 * (3.5 * ut * A1 + 3.0 * B1s);
-    kb.usq += b3 * (0.5 * ut * A1 + 0.5 * B1s);
-    kb.E1 += 0.5 * s1 * bA1;
+    kb.pbr += b1 * A1 + b3 * (R(3.5) * ut * A1 + R(3.0) * B1s);
+    kb.usq += b3 * (R(0.5) * ut * A1 + R(0.5) * B1s);
+    kb.E1 += R(0.5) * s1 * bA1;
     kb.B1 += s1 * bB1s;
 }
 
 // flux_Gyp / flux_Gyn
-QLSKUM_HD void flux_y_vjp(const Kin<double> &k, double s2, const double bG[4], KinBar &kb)
+template <typename R> QLSKUM_HD void flux_y_vjp(const Kin<R> &k, R s2, const R bG[4], KinBarT<R> &kb)
 {
-    const double A2 = 0.5 * (1.0 + s2 * k.E2), B2s = s2 * k.B2;
-    const double ut = k.ut, un = k.un, pbr = k.pbr, usq = k.usq, rho = k.rho;
-    const double a0 = un * A2 + B2s, a2 = (pbr + un * un) * A2 + un * B2s, a1 = ut * un * A2 + ut * B2s;
-    const double a3 = 0.5 * un * (7.0 * pbr + usq) * A2 + 0.5 * (6.0 * pbr + usq) * B2s;
+    const R A2 = R(0.5) * (R(1.0) + s2 * k.E2), B2s = s2 * k.B2;
+    const R ut = k.ut, un = k.un, pbr = k.pbr, usq = k.usq, rho = k.rho;
+    const R a0 = un * A2 + B2s, a2 = (pbr + un * un) * A2 + un * B2s, a1 = ut * un * A2 + ut * B2s;
+    const R a3 = R(0.5) * un * (R(7.0) * pbr + usq) * A2 + R(0.5) * (R(6.0) * pbr + usq) * B2s;
     kb.rho += bG[0] * a0 + bG[1] * a1 + bG[2] * a2 + bG[3] * a3;
-    const double b0 = rho * bG[0], b1 = rho * bG[1], b2 = rho * bG[2], b3 = rho * bG[3];
-    const double bA2 = b0 * un + b2 * (pbr + un * un) + b1 * ut * un + b3 * 0.5 * un * (7.0 * pbr + usq);
-    const double bB2s = b0 + b2 * un + b1 * ut + b3 * 0.5 * (6.0 * pbr + usq);
-    kb.un += b0 * A2 + b2 * (2.0 * un * A2 + B2s) + b1 * ut * A2 + b3 * 0.5 * (7.0 * pbr + usq) * A2;
+    const R b0 = rho * bG[0], b1 = rho * bG[1], b2 = rho * bG[2], b3 = rho * bG[3];
+    const R bA2 = b0 * un + b2 * (pbr + un * un) + b1 * ut * un + b3 * R(0.5) * un * (R(7.0) * pbr + usq);
+    const R bB2s = b0 + b2 * un + b1 * ut + b3 * R(0.5) * (R(6.0) * pbr + usq);
+    kb.un += b0 * A2 + b2 * (R(2.0) * un * A2 + B2s) + b1 * ut * A2 + b3 * R(0.5) * (R(7.0) * pbr + usq) * A2;
     kb.ut += b1 * (un * A2 + B2s);
-    kb.pbr += b2 * A2 + b3 * (3.5 * un * A2 + 3.0 * B2s);
-    kb.usq += b3 * (0.5 * un * A2 + 0.5 * B2s);
-    kb.E2 += 0.5 * s2 * bA2;
+    kb.pbr += b2 * A2 + b3 * (R(3.5) * un * A2 + R(3.0) * B2s);
+    kb.usq += b3 * (R(0.5) * un * A2 + R(0.5) * B2s);
+    kb.E2 += R(0.5) * s2 * bA2;
     kb.B2 += s2 * bB2s;
 }
 
 // flux_quad_GxI..IV
-QLSKUM_HD void flux_quad_vjp(const Kin<double> &k, double s1, double s2, const double bG[4], KinBar &kb)
+template <typename R> QLSKUM_HD void flux_quad_vjp(const Kin<R> &k, R s1, R s2, const R bG[4], KinBarT<R> &kb)
 {
-    const double ut = k.ut, un = k.un, pbr = k.pbr, usq = k.usq, rho = k.rho;
-    const double A1 = 0.5 * (1.0 + s1 * k.E1), A2 = 0.5 * (1.0 + s2 * k.E2), B1s = s1 * k.B1;
-    const double f1 = ut * A1 + B1s;
-    const double h = (pbr + ut * ut) * A1 + ut * B1s;
-    const double m = un * A2 + s2 * k.B2;
-    const double t2 = 0.5 * ut * (7.0 * pbr + usq) * A1, t3 = 0.5 * k.B1 * (6.0 * pbr + usq);
-    const double bt4 = s2 * bG[3];
+    const R ut = k.ut, un = k.un, pbr = k.pbr, usq = k.usq, rho = k.rho;
+    const R A1 = R(0.5) * (R(1.0) + s1 * k.E1), A2 = R(0.5) * (R(1.0) + s2 * k.E2), B1s = s1 * k.B1;
+    const R f1 = ut * A1 + B1s;
+    const R h = (pbr + ut * ut) * A1 + ut * B1s;
+    const R m = un * A2 + s2 * k.B2;
+    const R t2 = R(0.5) * ut * (R(7.0) * pbr + usq) * A1, t3 = R(0.5) * k.B1 * (R(6.0) * pbr + usq);
+    const R bt4 = s2 * bG[3];
     kb.rho += bG[0] * A2 * f1 + bG[1] * A2 * h + bG[2] * f1 * m + bG[3] * A2 * (t2 + s1 * t3) +
-              bt4 * 0.5 * un * k.B2 * f1;
-    double bA2 = rho * (bG[0] * f1 + bG[1] * h + bG[3] * (t2 + s1 * t3));
-    double bf1 = rho * (bG[0] * A2 + bG[2] * m) + bt4 * 0.5 * rho * un * k.B2;
-    const double bh = rho * A2 * bG[1];
-    const double bm = rho * f1 * bG[2];
-    const double bt2 = rho * A2 * bG[3], bt3 = rho * A2 * s1 * bG[3];
-    kb.un += bt4 * 0.5 * rho * k.B2 * f1 + bm * A2;
-    kb.B2 += bt4 * 0.5 * rho * un * f1 + bm * s2;
+              bt4 * R(0.5) * un * k.B2 * f1;
+    R bA2 = rho * (bG[0] * f1 + bG[1] * h + bG[3] * (t2 + s1 * t3));
+    R bf1 = rho * (bG[0] * A2 + bG[2] * m) + bt4 * R(0.5) * rho * un * k.B2;
+    const R bh = rho * A2 * bG[1];
+    const R bm = rho * f1 * bG[2];
+    const R bt2 = rho * A2 * bG[3], bt3 = rho * A2 * s1 * bG[3];
+    kb.un += bt4 * R(0.5) * rho * k.B2 * f1 + bm * A2;
+    kb.B2 += bt4 * R(0.5) * rho * un * f1 + bm * s2;
     bA2 += bm * un;
-    kb.pbr += bh * A1 + bt2 * 3.5 * ut * A1 + bt3 * 3.0 * k.B1;
-    kb.ut += bh * (2.0 * ut * A1 + B1s) + bf1 * A1 + bt2 * 0.5 * (7.0 * pbr + usq) * A1;
-    double bA1 = bh * (pbr + ut * ut) + bf1 * ut + bt2 * 0.5 * ut * (7.0 * pbr + usq);
-    const double bB1s = bh * ut + bf1;
-    kb.usq += bt2 * 0.5 * ut * A1 + bt3 * 0.5 * k.B1;
-    kb.B1 += bt3 * 0.5 * (6.0 * pbr + usq) + s1 * bB1s;
-    kb.E1 += 0.5 * s1 * bA1;
-    kb.E2 += 0.5 * s2 * bA2;
+    kb.pbr += bh * A1 + bt2 * R(3.5) * ut * A1 + bt3 * R(3.0) * k.B1;
+    kb.ut += bh * (R(2.0) * ut * A1 + B1s) + bf1 * A1 + bt2 * R(0.5) * (R(7.0) * pbr + usq) * A1;
+    R bA1 = bh * (pbr + ut * ut) + bf1 * ut + bt2 * R(0.5) * ut * (R(7.0) * pbr + usq);
+    const R bB1s = bh * ut + bf1;
+    kb.usq += bt2 * R(0.5) * ut * A1 + bt3 * R(0.5) * k.B1;
+    kb.B1 += bt3 * R(0.5) * (R(6.0) * pbr + usq) + s1 * bB1s;
+    kb.E1 += R(0.5) * s1 * bA1;
+    kb.E2 += R(0.5) * s2 * bA2;
 }
 
 template <int D> QLSKUM_HD void dir_flux_vjp(int f, const Kin<double> &k, const double bG[4], KinBar &kb)
@@ -185,21 +189,21 @@ template <int D> QLSKUM_HD void dir_flux_vjp(int f, const Kin<double> &k, const 
 // Reconstruction of one edge end (interior_fluxes_mod.h:72-83) for all four
 // components: q~ = q - 0.5 phi(q - 0.5 g) g with g = delx dqx + dely dqy.
 // Adds bars of q, dq (x, y), qm (max, min) and of the edge vector.
-QLSKUM_HD void edge_end_vjp(double delx, double dely, const double q[4], const double dx[4], const double dy[4],
-                            const double mx[4], const double mn[4], double e2, const double bqt[4], double bq[4],
-                            double bdx[4], double bdy[4], double bmx[4], double bmn[4], double &bdelx, double &bdely)
+template <typename R> QLSKUM_HD void edge_end_vjp(R delx, R dely, const R q[4], const R dx[4], const R dy[4],
+                            const R mx[4], const R mn[4], R e2, const R bqt[4], R bq[4],
+                            R bdx[4], R bdy[4], R bmx[4], R bmn[4], R &bdelx, R &bdely)
 {
     for (int r = 0; r < 4; r++) {
-        const double g = delx * dx[r] + dely * dy[r];
-        const double qtu = q[r] - 0.5 * g;
-        const double phi = venkat(qtu, q[r], mx[r], mn[r], e2);
+        const R g = delx * dx[r] + dely * dy[r];
+        const R qtu = q[r] - R(0.5) * g;
+        const R phi = venkat<R>(qtu, q[r], mx[r], mn[r], e2);
         bq[r] += bqt[r];
-        const double bphi = -0.5 * g * bqt[r];
-        double bg = -0.5 * phi * bqt[r];
-        double bqtu = 0.0;
+        const R bphi = -R(0.5) * g * bqt[r];
+        R bg = -R(0.5) * phi * bqt[r];
+        R bqtu = R(0.0);
         venkat_vjp(qtu, q[r], mx[r], mn[r], e2, bphi, bqtu, bq[r], bmx[r], bmn[r]);
         bq[r] += bqtu;
-        bg += -0.5 * bqtu;
+        bg += -R(0.5) * bqtu;
         bdx[r] += bg * delx;
         bdy[r] += bg * dely;
         bdelx += bg * dx[r];
@@ -323,15 +327,16 @@ QLSKUM_HD void stage_update_vjp(const CaseConst &K, int f, double nx, double ny,
 }
 
 // |u| + 3 sqrt(p / rho) (state_update_mod.h:483-485)
-QLSKUM_HD void wave_speed_vjp(const double P[4], double bc, double bP[4])
+template <typename R> QLSKUM_HD void wave_speed_vjp(const R P[4], R bc, R bP[4])
 {
-    const double mod_u = sqrt(P[1] * P[1] + P[2] * P[2]);
-    if (mod_u > 0.0) {
+    const R usq = P[1] * P[1] + P[2] * P[2];
+    const R mod_u = usq > R(0.0) ? M<R>::sq(usq) : R(0.0);
+    if (mod_u > R(0.0)) {
         bP[1] += bc * P[1] / mod_u;
         bP[2] += bc * P[2] / mod_u;
     }
-    const double a = P[3] / P[0], sa = sqrt(a);
-    const double ba = bc * 1.5 / sa;
+    const R a = P[3] / P[0], sa = M<R>::sq(a);
+    const R ba = bc * R(1.5) / sa;
     bP[3] += ba / P[0];
     bP[0] += -ba * P[3] / (P[0] * P[0]);
 }

@@ -1900,15 +1900,18 @@ qlskum_status qlskum_read_restart(qlskum_handle *h, const char *path)
 
 // ============================================================ discrete adjoint
 //
-// Reverse mode of the FP64 iteration (qlskum_adjoint.cu holds the kernels).
+// Reverse mode of the iteration (qlskum_adjoint.cu holds the kernels).
 // The stage states of an iteration are recomputed from its checkpointed
-// state by the FP64 module kernels, whose results equal the fused solver's
-// bit for bit; the reverse sweep then runs stage by stage from the last.
+// state by the module kernels of the handle's precision, whose results equal
+// the fused solver's; the reverse sweep then runs stage by stage from the
+// last.  FP64 handles, and wall-displacement gradients on any handle, take
+// the FP64 reverse; Mach / AoA / initial-state gradients of a mixed handle
+// take the reverse of the mixed iteration (FP32 edge work, FP64 update).
 
 struct AdjBuf {
     DeviceArena arena;
     int ni = 0;
-    bool geo = false;
+    bool geo = false, has64 = false, has32 = false;
     size_t ne = 0;
     double4_32a *P[5] = {};            // stage states of one iteration
     double4_32a *q[4] = {};            // q of P[0 .. 3]
@@ -1930,6 +1933,14 @@ struct AdjBuf {
     int ckpt_cap = 0;
     double4_32a *seg = nullptr;
     int seg_cap = 0;
+    // the mixed iteration's stage data (FP32) and bars
+    float4 *q32[4] = {};
+    std::vector<float4 *> dq32;        // [stage][inner step 0 .. ni], each [np][2]
+    float4 *qm32[4] = {};
+    float4 *acc32[4] = {};             // the flux kernel's weighted sums
+    float *delta32 = nullptr, *cs32 = nullptr;
+    float4 *bq32 = nullptr, *bdqA32 = nullptr, *bdqB32 = nullptr, *bqm32 = nullptr;
+    float *bdelta32 = nullptr, *bcs32 = nullptr;
 };
 
 void adj_free(qlskum_handle *h)
@@ -1972,9 +1983,17 @@ qlskum_status d2h(qlskum_handle *h, void *dst, const void *src, size_t bytes)
 
 void zero(qlskum_handle *h, void *p, size_t bytes) { cudaMemsetAsync(p, 0, bytes, h->L.stream); }
 
-qlskum_status adj_alloc(qlskum_handle *h, bool geo)
+// The adjoint's buffers: the FP64 stage data (need64), the mixed stage data
+// (need32) and the geometry bars (geo), each kept once allocated.
+qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
 {
-    if (h->adj && (h->adj->geo || !geo)) return QLSKUM_OK;
+    if (h->adj && (h->adj->geo || !geo) && (h->adj->has64 || !need64) && (h->adj->has32 || !need32))
+        return QLSKUM_OK;
+    if (h->adj) {
+        geo |= h->adj->geo;
+        need64 |= h->adj->has64;
+        need32 |= h->adj->has32;
+    }
     adj_free(h);
     AdjBuf *a = new AdjBuf();
     h->adj = a;
@@ -1982,19 +2001,36 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo)
     const size_t np = h->np;
     a->ni = h->prm.inner_iterations;
     a->geo = geo;
+    a->has64 = need64;
+    a->has32 = need32;
     for (auto &p : a->P) p = A.alloc<double4_32a>(np);
-    for (auto &p : a->q) p = A.alloc<double4_32a>(np);
-    for (auto &p : a->qm) p = A.alloc<double4_32a>(2 * np);
-    a->dq.resize(4 * (size_t)(a->ni + 1));
-    for (auto &p : a->dq) p = A.alloc<double4_32a>(2 * np);
-    a->delta = A.alloc<double>(np);
-    a->flux = A.alloc<double4_32a>(np);
-    for (auto *p : {&a->bP, &a->bPacc, &a->bF, &a->bq, &a->lam, &a->lam_prev, &a->seed})
-        *p = A.alloc<double4_32a>(np);
-    for (auto *p : {&a->bdqA, &a->bdqB, &a->bqm}) *p = A.alloc<double4_32a>(2 * np);
-    a->bdelta = A.alloc<double>(np);
-    a->bc = A.alloc<double>(np);
+    for (auto *p : {&a->bP, &a->bPacc, &a->bF, &a->lam, &a->lam_prev, &a->seed}) *p = A.alloc<double4_32a>(np);
     a->buinf = A.alloc<double>(2);
+    if (need64) {
+        for (auto &p : a->q) p = A.alloc<double4_32a>(np);
+        for (auto &p : a->qm) p = A.alloc<double4_32a>(2 * np);
+        a->dq.resize(4 * (size_t)(a->ni + 1));
+        for (auto &p : a->dq) p = A.alloc<double4_32a>(2 * np);
+        a->delta = A.alloc<double>(np);
+        a->flux = A.alloc<double4_32a>(np);
+        a->bq = A.alloc<double4_32a>(np);
+        for (auto *p : {&a->bdqA, &a->bdqB, &a->bqm}) *p = A.alloc<double4_32a>(2 * np);
+        a->bdelta = A.alloc<double>(np);
+        a->bc = A.alloc<double>(np);
+    }
+    if (need32) {
+        for (auto &p : a->q32) p = A.alloc<float4>(np);
+        for (auto &p : a->qm32) p = A.alloc<float4>(2 * np);
+        for (auto &p : a->acc32) p = A.alloc<float4>(np);
+        a->dq32.resize(4 * (size_t)(a->ni + 1));
+        for (auto &p : a->dq32) p = A.alloc<float4>(2 * np);
+        a->delta32 = A.alloc<float>(np);
+        a->cs32 = A.alloc<float>(np);
+        a->bq32 = A.alloc<float4>(np);
+        for (auto *p : {&a->bdqA32, &a->bdqB32, &a->bqm32}) *p = A.alloc<float4>(2 * np);
+        a->bdelta32 = A.alloc<float>(np);
+        a->bcs32 = A.alloc<float>(np);
+    }
     slice_bases(h, &a->ne);
     if (geo) {
         a->bedge = A.alloc<double4_32a>(a->ne);
@@ -2057,7 +2093,7 @@ void adj_stage_forward(qlskum_handle *h, int s)
 }
 
 // The four stage states of one iteration from a->P[0] (fpi_solver_mod.h:14-40).
-void adj_iteration_forward(qlskum_handle *h)
+void adj_iteration_forward64(qlskum_handle *h)
 {
     AdjBuf *a = h->adj;
     fp64::func_delta(h->L, h->dc, a->P[0], a->delta, h->K.cfl);
@@ -2091,7 +2127,7 @@ void adj_stage_reverse(qlskum_handle *h, int s, const AdjView &v)
 // Reverse of one iteration after adj_iteration_forward: a->bP holds the bar of
 // P[4] on entry and the bar of P[0] on exit.  Free-stream bars add to
 // a->buinf, geometry bars to the view's accumulators.
-void adj_iteration_reverse(qlskum_handle *h, const AdjView &v)
+void adj_iteration_reverse64(qlskum_handle *h, const AdjView &v)
 {
     AdjBuf *a = h->adj;
     const size_t np = h->np;
@@ -2104,6 +2140,77 @@ void adj_iteration_reverse(qlskum_handle *h, const AdjView &v)
     zero(h, a->bc, sizeof(double) * np);
     adjl::delta(h->L, v, a->P[0], a->bdelta, h->K.cfl, a->bc, a->bPacc);
     fp64::add_prim(h->L, h->n, a->bPacc, a->bP);
+}
+
+float4 *adj_dq32(AdjBuf *a, int s, int j) { return a->dq32[(size_t)s * (a->ni + 1) + j]; }
+
+// The mixed iteration from a->P[0] with the solver's own kernels and launch
+// shapes (enqueue_iteration), every stage's FP32 data kept: q, the gradient
+// after each inner step, max / min, the flux kernel's weighted sums, the
+// local time step and the wave speed it came from.
+void adj_iteration_forward32(qlskum_handle *h)
+{
+    AdjBuf *a = h->adj;
+    const DevCloud &c = h->dc;
+    const int ni = a->ni;
+    Reduce none = h->R;
+    none.partial_sum = none.partial_max = nullptr;
+    mixed::derived(h->L, c, a->P[0], a->q32[0], a->cs32);
+    for (int s = 0; s < 4; s++) {
+        mixed::q_derivatives(h->L, c, a->q32[s], adj_dq32(a, s, 0), a->qm32[s], a->cs32, s == 0 ? a->delta32 : nullptr,
+                             (float)h->K.cfl);
+        for (int j = 1; j <= ni; j++) mixed::q_inner(h->L, c, a->q32[s], adj_dq32(a, s, j - 1), adj_dq32(a, s, j));
+        // the last stage's q goes to the bar buffer, which the reverse zeroes before use
+        float4 *q_next = s < 3 ? a->q32[s + 1] : a->bq32;
+        mixed::flux_update(h->L, c, h->K, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->delta32, a->P[s], a->P[0],
+                           a->P[s + 1], q_next, nullptr, s + 1, none, h->flux_variant, a->acc32[s]);
+    }
+}
+
+// Reverse of adj_iteration_forward32 (same contract as the FP64 reverse,
+// without geometry bars).
+void adj_iteration_reverse32(qlskum_handle *h, const AdjView &v)
+{
+    AdjBuf *a = h->adj;
+    const size_t np = h->np;
+    const int ni = a->ni;
+    const DevCloud &c = h->dc;
+    zero(h, a->bPacc, sizeof(double4_32a) * np);
+    zero(h, a->bdelta32, sizeof(float) * np);
+    for (int s = 3; s >= 0; s--) {
+        adjl::update(h->L, v, h->K, a->P[s], a->P[0], a->P[s + 1], s + 1, a->bP, a->bPacc, a->bF, a->buinf);
+        zero(h, a->bq32, sizeof(float4) * np);
+        zero(h, a->bdqA32, sizeof(float4) * 2 * np);
+        zero(h, a->bqm32, sizeof(float4) * 2 * np);
+        adjml::flux(h->L, c, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->delta32, a->acc32[s], a->bF, a->bq32,
+                    a->bdqA32, a->bqm32, a->bdelta32);
+        for (int j = ni; j >= 1; j--) {
+            zero(h, a->bdqB32, sizeof(float4) * 2 * np);
+            adjml::inner(h->L, c, a->q32[s], adj_dq32(a, s, j - 1), a->bdqA32, a->bq32, a->bdqB32);
+            std::swap(a->bdqA32, a->bdqB32);
+        }
+        adjml::grad(h->L, c, a->q32[s], a->bdqA32, a->bqm32, a->bq32);
+        adjml::qvars(h->L, h->n, a->P[s], a->bq32, a->bP);
+    }
+    zero(h, a->bcs32, sizeof(float) * np);
+    adjml::delta(h->L, c, a->P[0], a->cs32, a->bdelta32, (float)h->K.cfl, a->bcs32, a->bPacc);
+    fp64::add_prim(h->L, h->n, a->bPacc, a->bP);
+}
+
+// The reverse of a mixed handle's own iteration where no geometry bars are
+// wanted, else the FP64 reverse.
+bool adj_use32(const qlskum_handle *h, bool geo) { return h->prm.precision == QLSKUM_MIXED && !geo; }
+
+void adj_iteration_forward(qlskum_handle *h, bool m32)
+{
+    if (m32) adj_iteration_forward32(h);
+    else adj_iteration_forward64(h);
+}
+
+void adj_iteration_reverse(qlskum_handle *h, const AdjView &v, bool m32)
+{
+    if (m32) adj_iteration_reverse32(h, v);
+    else adj_iteration_reverse64(h, v);
 }
 
 // Cl and Cd at `prim` (compute_force_coeffs_mod.h:37-67), and dJ/dprim of
@@ -2330,7 +2437,8 @@ qlskum_status adj_args(qlskum_handle *h, int objective, int count, const double 
     if (count < 1) return fail(h, QLSKUM_ERR_INVALID, "iteration count must be >= 1");
     if (dJ_dwall && h->prm.power != 0.0)
         return fail(h, QLSKUM_ERR_UNSUPPORTED, "wall-displacement gradients need unit least-squares weights (power 0)");
-    return adj_alloc(h, dJ_dwall != nullptr);
+    const bool geo = dJ_dwall != nullptr;
+    return adj_alloc(h, geo, !adj_use32(h, geo), adj_use32(h, geo));
 }
 
 }  // namespace
@@ -2341,7 +2449,7 @@ qlskum_status qlskum_residual_forward(qlskum_handle *h, const double *prim, doub
 {
     NEED(h);
     if (!prim || !flux_res) return fail(h, QLSKUM_ERR_INVALID, "null prim or flux_res");
-    qlskum_status st = adj_alloc(h, false);
+    qlskum_status st = adj_alloc(h, false, true, false);
     if (st) return st;
     AdjBuf *a = h->adj;
     if ((st = upload_points(h, prim, a->P[0], 1.0))) return st;
@@ -2355,7 +2463,7 @@ qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const do
 {
     NEED(h);
     if (!prim || !bar_flux_res || !bar_prim) return fail(h, QLSKUM_ERR_INVALID, "null argument");
-    qlskum_status st = adj_alloc(h, false);
+    qlskum_status st = adj_alloc(h, false, true, false);
     if (st) return st;
     AdjBuf *a = h->adj;
     if ((st = upload_points(h, prim, a->P[0], 1.0))) return st;
@@ -2380,6 +2488,7 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     if (st) return st;
     AdjBuf *a = h->adj;
     const size_t np = h->np;
+    const bool m32 = adj_use32(h, dJ_dwall != nullptr);
     const int S = std::max(1, h->adj_stride);
     const int nck = (iters + S - 1) / S;
     auto grow = [&](double4_32a *&buf, int &cap, int want, const char *what) -> qlskum_status {
@@ -2423,14 +2532,14 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     const size_t bytes = sizeof(double4_32a) * np;
     for (int c0 = nck - 1; c0 >= 0; c0--) {
         const int t0 = c0 * S, t1 = std::min(iters, t0 + S);
-        // states t0 .. t1 - 1 of this segment: the checkpoint, then FP64 iterations from it
+        // states t0 .. t1 - 1 of this segment: the checkpoint, then the reverse's own iterations from it
         const double4_32a *state_at0 = a->ckpt + np * (size_t)c0;
         if (S > 1) {
             CK(h, cudaMemcpyAsync(a->seg, state_at0, bytes, cudaMemcpyDeviceToDevice, h->L.stream));
             for (int t = t0 + 1; t < t1; t++) {
                 CK(h, cudaMemcpyAsync(a->P[0], a->seg + np * (size_t)(t - 1 - t0), bytes, cudaMemcpyDeviceToDevice,
                                       h->L.stream));
-                adj_iteration_forward(h);
+                adj_iteration_forward(h, m32);
                 CK(h, cudaMemcpyAsync(a->seg + np * (size_t)(t - t0), a->P[4], bytes, cudaMemcpyDeviceToDevice,
                                       h->L.stream));
             }
@@ -2438,8 +2547,8 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
         for (int t = t1 - 1; t >= t0; t--) {
             const double4_32a *state = S > 1 ? a->seg + np * (size_t)(t - t0) : state_at0;
             CK(h, cudaMemcpyAsync(a->P[0], state, bytes, cudaMemcpyDeviceToDevice, h->L.stream));
-            adj_iteration_forward(h);
-            adj_iteration_reverse(h, v);
+            adj_iteration_forward(h, m32);
+            adj_iteration_reverse(h, v, m32);
         }
     }
     if ((st = check_launch(h, "adjoint sweep"))) return st;
@@ -2480,6 +2589,7 @@ qlskum_status qlskum_adjoint_fixed_point(qlskum_handle *h, int objective, int ad
     if (st) return st;
     AdjBuf *a = h->adj;
     const size_t np = h->np;
+    const bool m32 = adj_use32(h, dJ_dwall != nullptr);
     ObjSeed os;
     if ((st = adj_seed(h, objective, h->s64.prim[h->pcur], a->seed, os))) return st;
     CK(h, cudaMemcpyAsync(a->P[0], h->s64.prim[h->pcur], sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice,
@@ -2487,7 +2597,7 @@ qlskum_status qlskum_adjoint_fixed_point(qlskum_handle *h, int objective, int ad
     zero(h, a->lam, sizeof(double4_32a) * np);
     const AdjView none = adj_view(h, false);
     // the stage states of S at U, once: the reverse passes only read them
-    adj_iteration_forward(h);
+    adj_iteration_forward(h, m32);
     // lam <- S_U^T lam + J_U at the current state U (one iteration map S)
     for (int k = 0; k < adj_iters; k++) {
         if (k == adj_iters - 1)
@@ -2495,14 +2605,14 @@ qlskum_status qlskum_adjoint_fixed_point(qlskum_handle *h, int objective, int ad
                                   h->L.stream));
         CK(h, cudaMemcpyAsync(a->bP, a->lam, sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice, h->L.stream));
         zero(h, a->buinf, 2 * sizeof(double));
-        adj_iteration_reverse(h, none);
+        adj_iteration_reverse(h, none, m32);
         CK(h, cudaMemcpyAsync(a->lam, a->seed, sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice, h->L.stream));
         fp64::add_prim(h->L, h->n, a->bP, a->lam);
     }
     // lam^T dS/dalpha: one more reverse pass, accumulating the parameter bars
     adj_zero_geometry(h);
     CK(h, cudaMemcpyAsync(a->bP, a->lam, sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice, h->L.stream));
-    adj_iteration_reverse(h, adj_view(h, true));
+    adj_iteration_reverse(h, adj_view(h, true), m32);
     if ((st = check_launch(h, "fixed-point adjoint"))) return st;
     double bu[2];
     if ((st = d2h(h, bu, a->buinf, sizeof bu))) return st;

@@ -187,6 +187,21 @@ void objective(const Launch &L, const AdjView &a, const int *wall_perm, const do
 void objective_J(const Launch &L, int n, const double4_32a *P, double gamma, double p0_inf, double4_32a *bP);
 }  // namespace adjl
 
+// Reverse of the mixed iteration (qlskum_adjoint.cu, FP32 edge work): bars of
+// the FP32 q / dq / qm in float4 arrays (atomically accumulated), of delta in
+// float, of the FP64 states in double4.
+namespace adjml {
+void flux(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq, const float4 *qm, const float *delta,
+          const float4 *acc, const double4_32a *bF, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta);
+void inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, const float4 *bdq_out,
+           float4 *bq, float4 *bdq_in);
+void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq, const float4 *bqm, float4 *bq);
+void qvars(const Launch &L, int n, const double4_32a *P, const float4 *bq, double4_32a *bP);
+// reverse of the time step and of the wave speed it came from; bP += ...
+void delta(const Launch &L, const DevCloud &c, const double4_32a *P, const float *cs, const float *bdelta, float cfl,
+           float *bcs, double4_32a *bP);
+}  // namespace adjml
+
 // ---------------------------------------------------------- FP64 kernels (qlskum_fp64.cu)
 namespace fp64 {
 void q_variables(const Launch &L, const DevCloud &c, const double4_32a *prim, double4_32a *q);
@@ -228,7 +243,8 @@ int staged_block(int v);
 int staged_depth(int v);
 void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const float4 *q, const float4 *dq,
                  const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
-                 double4_32a *prim_next, float4 *q_next, float *cspeed_next, int rk, const Reduce &R, int variant);
+                 double4_32a *prim_next, float4 *q_next, float *cspeed_next, int rk, const Reduce &R, int variant,
+                 float4 *acc_out = nullptr);  // acc_out: the point's flux accumulator (F / delta) when non-null
 int flux_variants();
 int flux_block(int variant);
 int flux_min_blocks(int variant);

@@ -534,8 +534,9 @@ __device__ __forceinline__ double flux_tail(const CaseConst &K, int i, int f, do
                                             const float *__restrict__ delta, const double4_32a *__restrict__ prim,
                                             const double4_32a *__restrict__ prim_old,
                                             double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
-                                            float *__restrict__ cs_next, int rk)
+                                            float *__restrict__ cs_next, int rk, float4 *__restrict__ acc_out)
 {
+    if (acc_out) acc_out[i] = mk4(acc);
     const double dl = f2d(delta[i]);
     double F[4], P[4];
 #pragma unroll
@@ -560,7 +561,7 @@ __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst 
                                              const double4_32a *__restrict__ prim,
                                              const double4_32a *__restrict__ prim_old,
                                              double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
-                                             float *__restrict__ cs_next, int rk)
+                                             float *__restrict__ cs_next, int rk, float4 *__restrict__ acc_out)
 {
     const int f = c.flag[i];
     const double2 nn = c.nrm[i];
@@ -590,7 +591,7 @@ __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst 
         ld4(qm[2 * k + 1], mnk);
         flux_edge(c, e, f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, w, dir, qk, dxk, dyk, mxk, mnk, c.eps2_32[k], acc);
     }
-    return flux_tail(K, i, f, nn, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk);
+    return flux_tail(K, i, f, nn, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
 }
 
 // The same with the next edge's gathers in flight during the current edge's
@@ -607,7 +608,7 @@ __device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseCon
                                                 const double4_32a *__restrict__ prim,
                                                 const double4_32a *__restrict__ prim_old,
                                                 double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
-                                                float *__restrict__ cs_next, int rk)
+                                                float *__restrict__ cs_next, int rk, float4 *__restrict__ acc_out)
 {
     const int f = c.flag[i];
     const double2 nn = c.nrm[i];
@@ -665,7 +666,7 @@ __device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseCon
         const float e2k = reps[(j & 1) * B + t];
         flux_edge(c, e, f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, w, dir, qk, dxk, dyk, mxk, mnk, e2k, acc);
     }
-    return flux_tail(K, i, f, nn, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk);
+    return flux_tail(K, i, f, nn, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
 }
 
 // ---------------------------------------------------- single-case kernels
@@ -695,11 +696,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseCon
                                                        const double4_32a *__restrict__ prim_old,
                                                        double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
                                                        float *__restrict__ cs_next, int rk,
-                                                       double *__restrict__ psum, double *__restrict__ pmax)
+                                                       double *__restrict__ psum, double *__restrict__ pmax,
+                                                       float4 *__restrict__ acc_out)
 {
     const int i = blockIdx.x * BLOCK + threadIdx.x;
     double r2 = 0.0;
-    if (i < c.n) r2 = flux_point<UW>(c, K, i, q, dq, qm, delta, prim, prim_old, prim_next, q_next, cs_next, rk);
+    if (i < c.n)
+        r2 = flux_point<UW>(c, K, i, q, dq, qm, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
     if (psum) block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
 }
 
@@ -714,7 +717,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update_st(DevCloud c, Case
                                                           double4_32a *__restrict__ prim_next,
                                                           float4 *__restrict__ q_next, float *__restrict__ cs_next,
                                                           int rk, double *__restrict__ psum,
-                                                          double *__restrict__ pmax)
+                                                          double *__restrict__ pmax, float4 *__restrict__ acc_out)
 {
     __shared__ float4 ring[2 * 5 * BLOCK];
     __shared__ float reps[2 * BLOCK];
@@ -723,7 +726,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update_st(DevCloud c, Case
     double r2 = 0.0;
     if (i < c.n)
         r2 = flux_point_st<BLOCK, UW>(c, K, i, t, ring, reps, q, dq, qm, delta, prim, prim_old, prim_next, q_next,
-                                      cs_next, rk);
+                                      cs_next, rk, acc_out);
     if (psum) block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
 }
 
@@ -810,7 +813,8 @@ __global__ void __launch_bounds__(TILE, MINB) kb_flux_update(const DevCloud *__r
         if (i < C.n) {
             const long long o = C.off;
             r2 = flux_point<UW>(clouds[C.cloud], C.K, i, q + o, dq + 2 * o, qm + 2 * o, delta + o, prim + o,
-                                prim_old + o, prim_next + o, q_next + o, cs_next ? cs_next + o : nullptr, rk);
+                                prim_old + o, prim_next + o, q_next + o, cs_next ? cs_next + o : nullptr, rk,
+                                nullptr);
         }
         if (psum) block_sum_max<TILE>(r2, r2, psum + t, pmax + t);
     }
@@ -956,30 +960,31 @@ int flux_min_blocks(int v) { return kFluxMinBlocks[v]; }
 
 void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const float4 *q, const float4 *dq,
                  const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
-                 double4_32a *prim_next, float4 *q_next, float *cspeed_next, int rk, const Reduce &R, int variant)
+                 double4_32a *prim_next, float4 *q_next, float *cspeed_next, int rk, const Reduce &R, int variant,
+                 float4 *acc_out)
 {
 #define QLSKUM_FLUX(B, MB)                                                                                  \
     if (c.unit_w)                                                                                           \
         k_flux_update<B, MB, true><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,      \
                                                                       prim_old, prim_next, q_next,         \
                                                                       cspeed_next, rk, R.partial_sum,      \
-                                                                      R.partial_max);                      \
+                                                                      R.partial_max, acc_out);             \
     else                                                                                                    \
         k_flux_update<B, MB, false><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,     \
                                                                        prim_old, prim_next, q_next,        \
                                                                        cspeed_next, rk, R.partial_sum,     \
-                                                                       R.partial_max)
+                                                                       R.partial_max, acc_out)
 #define QLSKUM_FLUX_ST(B, MB)                                                                               \
     if (c.unit_w)                                                                                           \
         k_flux_update_st<B, MB, true><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,   \
                                                                          prim_old, prim_next, q_next,      \
                                                                          cspeed_next, rk, R.partial_sum,   \
-                                                                         R.partial_max);                   \
+                                                                         R.partial_max, acc_out);          \
     else                                                                                                    \
         k_flux_update_st<B, MB, false><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,  \
                                                                           prim_old, prim_next, q_next,     \
                                                                           cspeed_next, rk, R.partial_sum,  \
-                                                                          R.partial_max)
+                                                                          R.partial_max, acc_out)
     switch (variant) {
     case 1: QLSKUM_FLUX(128, 5); break;
     case 2: QLSKUM_FLUX(64, 8); break;

@@ -137,3 +137,59 @@ void qlskum_dbg_wave_speed_vjp(const double *P, double bc, double *bP)
 }
 
 }  // extern "C"
+
+// FP32 instantiations of the same reverse-mode functions (the adjoint of the
+// mixed form), for comparison with the FP64 ones on the CPU.
+extern "C" {
+
+void qlskum_dbg_prim_to_q_vjp32(const float *P, const float *bq, float *bP)
+{
+    for (int r = 0; r < 4; r++) bP[r] = 0;
+    adj::prim_to_q_vjp<float>(P, bq, bP);
+}
+
+void qlskum_dbg_qtilde_to_prim_vjp32(const float *qt, const float *bP, float *bqt)
+{
+    for (int r = 0; r < 4; r++) bqt[r] = 0;
+    adj::qtilde_to_prim_vjp<float>(qt, bP, bqt);
+}
+
+// out: bP[4], bnx, bny; kind 0 x split, 1 y split, 2 quadrant (s2 = -1)
+void qlskum_dbg_flux_vjp32(int kind, float s, float nx, float ny, const float *P, const float *bG, float *out)
+{
+    Kin<float> k;
+    kin_prep<float>(nx, ny, P[1], P[2], P[0], P[3], k);
+    adj::KinBarT<float> kb;
+    if (kind == 0) adj::flux_x_vjp<float>(k, s, bG, kb);
+    else if (kind == 1) adj::flux_y_vjp<float>(k, s, bG, kb);
+    else adj::flux_quad_vjp<float>(k, s, -1.0f, bG, kb);
+    for (int r = 0; r < 6; r++) out[r] = 0;
+    adj::kin_vjp<float>(nx, ny, P, k, kb, out, out[4], out[5]);
+}
+
+void qlskum_dbg_flux_vjp64(int kind, double s, double nx, double ny, const double *P, const double *bG, double *out)
+{
+    Kin<double> k;
+    kin_prep<double>(nx, ny, P[1], P[2], P[0], P[3], k);
+    adj::KinBar kb;
+    if (kind == 0) adj::flux_x_vjp<double>(k, s, bG, kb);
+    else if (kind == 1) adj::flux_y_vjp<double>(k, s, bG, kb);
+    else adj::flux_quad_vjp<double>(k, s, -1.0, bG, kb);
+    for (int r = 0; r < 6; r++) out[r] = 0;
+    adj::kin_vjp<double>(nx, ny, P, k, kb, out, out[4], out[5]);
+}
+
+void qlskum_dbg_edge_end_vjp32(const float *in, float e2, float delx, float dely, const float *bqt, float *out)
+{
+    for (int r = 0; r < 22; r++) out[r] = 0;
+    adj::edge_end_vjp<float>(delx, dely, in, in + 4, in + 8, in + 12, in + 16, e2, bqt, out, out + 4, out + 8,
+                             out + 12, out + 16, out[20], out[21]);
+}
+
+void qlskum_dbg_wave_speed_vjp32(const float *P, float bc, float *bP)
+{
+    for (int r = 0; r < 4; r++) bP[r] = 0;
+    adj::wave_speed_vjp<float>(P, bc, bP);
+}
+
+}  // extern "C"

@@ -391,7 +391,9 @@ class Solver:
         differentiates the objective ("cl" / "cd") at the end through all of
         them: {"J", "dmach", "daoa" (per degree), "dwall" ([shape_points]
         normal displacements) or None, "dprim0" ([n, 4]) or None}.  stride:
-        keep every stride-th iteration's state and recompute the rest."""
+        keep every stride-th iteration's state and recompute the rest.  A
+        mixed handle differentiates the mixed iteration (the wall gradient:
+        the FP64 iteration at the mixed states)."""
         self._ck(self._L.qlskum_set_adjoint_stride(self._h, int(stride)))
         obj, v, dw = self._adjoint_out(objective, wall)
         p0 = None if prim0 is None else self._state(prim0, "prim0")

@@ -273,12 +273,15 @@ qlskum_status qlskum_check_stencils(const qlskum_cloud *cloud, double power, dou
 
 /* ------------------------------------------------------------ discrete adjoint */
 
-/* Reverse mode of the FP64 iteration, for gradients of the force
- * coefficients.  No counterpart in the reference (which has no adjoint); the
- * functions differentiate exactly what q_lskum / fpi_solver compute in FP64
- * (fpi_solver_mod.h:14-151).  On a MIXED handle the primal trajectory is the
- * mixed solver's and the reverse sweep differentiates the FP64 iteration at
- * those states (an FP64 adjoint of the mixed run).  Arrays are in the
+/* Reverse mode of the iteration, for gradients of the force coefficients.
+ * No counterpart in the reference (which has no adjoint); the functions
+ * differentiate exactly what q_lskum / fpi_solver compute
+ * (fpi_solver_mod.h:14-151).  On an FP64 handle that is the FP64 iteration.
+ * On a MIXED handle the Mach / AoA / initial-state gradients differentiate
+ * the mixed iteration along the mixed trajectory (FP32 edge work, FP64
+ * stage update, as the forward); its wall-displacement gradients take the
+ * FP64 reverse at the mixed trajectory's states.  qlskum_residual_forward
+ * and qlskum_residual_vjp are FP64 on either handle.  Arrays are in the
  * cloud's point order. */
 #define QLSKUM_OBJECTIVE_CL 0
 #define QLSKUM_OBJECTIVE_CD 1

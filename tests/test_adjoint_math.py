@@ -224,3 +224,61 @@ def test_fp32_erf_error_bound(L):
     err = max(abs(L.qlskum_dbg_erf32(float(x)) - math.erf(float(np.float32(x)))) for x in xs)
     assert err < 1.5e-7 + 2.4e-7, err
     assert L.qlskum_dbg_erf32(0.0) == 0.0
+
+
+fp = C.POINTER(C.c_float)
+
+
+def F32(a):
+    return np.ascontiguousarray(a, np.float32).ctypes.data_as(fp)
+
+
+def test_fp32_instantiations_match_fp64(L):
+    """The adjoint of the mixed form runs the same reverse-mode functions in
+    FP32: they agree with the FP64 ones to FP32 accuracy (1e-4 of the
+    result's scale; the host build uses the libm float functions)."""
+    for nm, a in (("qlskum_dbg_prim_to_q_vjp32", [fp] * 3), ("qlskum_dbg_qtilde_to_prim_vjp32", [fp] * 3),
+                  ("qlskum_dbg_flux_vjp32", [C.c_int, C.c_float, C.c_float, C.c_float, fp, fp, fp]),
+                  ("qlskum_dbg_flux_vjp64", [C.c_int, C.c_double, C.c_double, C.c_double, dp, dp, dp]),
+                  ("qlskum_dbg_edge_end_vjp32", [fp, C.c_float, C.c_float, C.c_float, fp, fp]),
+                  ("qlskum_dbg_wave_speed_vjp32", [fp, C.c_float, fp])):
+        getattr(L, nm).argtypes = a
+        getattr(L, nm).restype = None
+    rng = np.random.default_rng(9)
+
+    def close(a, b):
+        a, b = np.asarray(a, float), np.asarray(b, float)
+        assert np.abs(a - b).max() <= 1e-4 * max(1.0, np.abs(b).max()), (a, b)
+
+    for _ in range(20):
+        Pst = state(rng)
+        bq = rng.standard_normal(4)
+        o32, o64 = np.zeros(4, np.float32), np.zeros(4)
+        L.qlskum_dbg_prim_to_q_vjp32(F32(Pst), F32(bq), F32(o32))
+        L.qlskum_dbg_prim_to_q_vjp(P(Pst), P(bq), P(o64))
+        close(o32, o64)
+        q = np.zeros(4)
+        L.qlskum_dbg_prim_to_q(P(Pst), P(q))
+        L.qlskum_dbg_qtilde_to_prim_vjp32(F32(q), F32(bq), F32(o32))
+        L.qlskum_dbg_qtilde_to_prim_vjp(P(q), P(bq), P(o64))
+        close(o32, o64)
+        th = rng.uniform(0, 2 * np.pi)
+        for kind in (0, 1, 2):
+            s = float(rng.choice([-1.0, 1.0]))
+            f32, f64 = np.zeros(6, np.float32), np.zeros(6)
+            L.qlskum_dbg_flux_vjp32(kind, s, np.cos(th), np.sin(th), F32(Pst), F32(bq), F32(f32))
+            L.qlskum_dbg_flux_vjp64(kind, s, np.cos(th), np.sin(th), P(Pst), P(bq), P(f64))
+            close(f32, f64)
+        o32 = np.zeros(4, np.float32)
+        L.qlskum_dbg_wave_speed_vjp32(F32(Pst), 0.7, F32(o32))
+        L.qlskum_dbg_wave_speed_vjp(P(Pst), 0.7, P(o64))
+        close(o32, o64)
+    for _ in range(10):
+        qv = rng.uniform(-1, 1, 4)
+        x = np.concatenate([qv, rng.uniform(-5, 5, 8), qv + rng.uniform(1e-2, 0.05, 4), qv - rng.uniform(1e-2, 0.05, 4)])
+        bqt = rng.standard_normal(4)
+        d = rng.uniform(-0.01, 0.01, 2)
+        o32, o64 = np.zeros(22, np.float32), np.zeros(22)
+        L.qlskum_dbg_edge_end_vjp32(F32(x), 1e-7, float(d[0]), float(d[1]), F32(bqt), F32(o32))
+        L.qlskum_dbg_edge_end_vjp(P(x), 1e-7, float(d[0]), float(d[1]), P(bqt), P(o64))
+        close(o32, o64)

@@ -1,4 +1,4 @@
-"""Discrete adjoint of the FP64 iteration, through the C ABI.
+"""Discrete adjoint of the iteration (FP64, and the mixed form), through the C ABI.
 
 * qlskum_residual_forward reproduces the reference's first-stage flux
   residual (golden fixture, 1e-12 like the stage parity test), and its VJP
@@ -12,6 +12,8 @@
   same from a given initial state, with dJ/dprim0.
 * The fixed-point adjoint contracts at a partly converged state; the torch
   autograd.Function wrapper reproduces the raw VJP.
+* On a mixed handle the reverse of the mixed iteration (FP32 edge work)
+  agrees with the FP64 reverse at the same state to the FP32 rounding.
 """
 import os
 
@@ -188,15 +190,67 @@ def test_checkpoint_stride_same_gradient(qlskum):
 
 
 def test_adjoint_of_mixed_run_close_to_fp64(qlskum):
-    """On a mixed handle the reverse sweep differentiates the FP64 iteration at
-    the mixed trajectory's states: the gradient agrees with the FP64 one to
-    the mixed form's state error."""
+    """On a mixed handle the reverse sweep differentiates the mixed iteration
+    (FP32 edge work, FP64 update) along its own trajectory: the gradient
+    agrees with the FP64 one to the mixed form's rounding.  Recomputing the
+    segment states (stride 2) gives the same gradient up to the order of
+    the FP32 atomic sums; the wall gradient on a mixed handle takes the FP64
+    reverse."""
     c = _cloud()
     f = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **KW).adjoint_gradient("cl", iters=N)
-    m = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, precision=qlskum.MIXED,
-                      **KW).adjoint_gradient("cl", iters=N, stride=2)
+    ms = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, precision=qlskum.MIXED, **KW)
+    m = ms.adjoint_gradient("cl", iters=N)
     assert abs(m["J"] - f["J"]) < 1e-6
-    np.testing.assert_allclose([m["dmach"], m["daoa"]], [f["dmach"], f["daoa"]], rtol=1e-3)
+    np.testing.assert_allclose([m["dmach"], m["daoa"]], [f["dmach"], f["daoa"]], rtol=1e-4)
+    m2 = ms.adjoint_gradient("cl", iters=N, stride=2)
+    assert m2["J"] == m["J"]
+    np.testing.assert_allclose([m2["dmach"], m2["daoa"]], [m["dmach"], m["daoa"]], rtol=1e-5)
+    mw = ms.adjoint_gradient("cl", iters=N, wall=True)
+    np.testing.assert_allclose([mw["dmach"], mw["daoa"]], [f["dmach"], f["daoa"]], rtol=1e-4)
+    assert np.isfinite(mw["dwall"]).all()
+
+
+@pytest.mark.parametrize("iters", [1, 3])
+def test_mixed_reverse_matches_fp64_reverse_at_same_state(qlskum, iters):
+    """From one partly converged state, the mixed handle's dJ/dprim0 (reverse
+    of the mixed iteration) against the FP64 handle's (reverse of the FP64
+    iteration): the two iterations are the same map up to FP32 rounding, so
+    their transposed Jacobians applied to the same seed agree to ~1e-5 in
+    norm (points where a limiter or half-range switch falls on the other
+    side in FP32 are the few local exceptions)."""
+    c = _cloud()
+    f = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **KW)
+    f.q_lskum(10)
+    U0 = f.prim
+    m = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, precision=qlskum.MIXED, **KW)
+    for which in ("cl", "cd", "j"):
+        gf = f.adjoint_gradient(which, iters=iters, prim0=U0)
+        gm = m.adjoint_gradient(which, iters=iters, prim0=U0)
+        assert abs(gm["J"] - gf["J"]) <= 1e-5 * max(abs(gf["J"]), 1e-3)
+        d = gm["dprim0"] - gf["dprim0"]
+        assert np.linalg.norm(d) <= 1e-4 * np.linalg.norm(gf["dprim0"]), (which, np.linalg.norm(d))
+        np.testing.assert_allclose([gm["dmach"], gm["daoa"]], [gf["dmach"], gf["daoa"]], rtol=1e-4,
+                                   atol=1e-6 * abs(gf["dmach"]))
+
+
+def test_mixed_fixed_point_one_step_identity(qlskum):
+    """The one-step identity of the fixed-point adjoint on a mixed handle
+    (both sides run the mixed reverse; the FP32 atomic sums leave ~1e-7 of
+    the derivative's scale)."""
+    c = _cloud()
+    s = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, precision=qlskum.MIXED, **KW)
+    s.q_lskum(10)
+    U = s.prim
+    cd0 = s.objective()[1]
+    fp = s.adjoint_fixed_point("cl", adj_iters=1)
+    ag = s.adjoint_gradient("cl", iters=1, prim0=U)
+    cd1 = s.objective()[1]
+    np.testing.assert_allclose(fp["dmach"] - ag["dmach"], -2.0 * (fp["J"] - ag["J"]) / MACH, rtol=0,
+                               atol=1e-5 * abs(fp["dmach"]))
+    np.testing.assert_allclose(fp["daoa"] - ag["daoa"], -(cd0 - cd1) * np.pi / 180, rtol=0,
+                               atol=1e-5 * abs(fp["daoa"]))
+    r = s.adjoint_fixed_point("cd", adj_iters=20)
+    assert np.isfinite([r["J"], r["dmach"], r["daoa"], r["adj_change"]]).all()
 
 
 def test_adjoint_rejects_weighted_wall_gradient(qlskum):
