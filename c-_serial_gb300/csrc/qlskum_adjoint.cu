@@ -596,16 +596,74 @@ __device__ __forceinline__ void x_flux_vjp(int f, const Kin<float> &k, float s1,
     else adj::flux_quad_vjp<float>(k, s1, (f == kOuter) ? 1.0f : -1.0f, bG, kb);
 }
 
+// Reverse of one end of one edge of the mixed flux kernel: the end's
+// reconstruction (q, dq, max / min of the point the end belongs to), its
+// primitive state and half-range moments, then the bars of the x and y
+// half-range fluxes it enters, weighted by the folded solve weights (bs: the
+// bar of the owner's weighted sum, signed + for the neighbour end, - for the
+// owner's), back to the end's q, dq and max / min (added to bq ... bmn).
+__device__ __forceinline__ void end_vjp(const DevCloud &c, long long e, int f, float nx, float ny, float delx,
+                                        float dely, float2 w, unsigned dir, const float bs[4], const float q[4],
+                                        const float dx[4], const float dy[4], const float mx[4], const float mn[4],
+                                        float e2, float bq[4], float bdx[4], float bdy[4], float bmx[4], float bmn[4])
+{
+    float t[4], P[4];
+    qtilde_f(delx, dely, q, dx, dy, mx, mn, e2, t);
+    qtilde_to_prim<float>(t, P[1], P[2], P[0], P[3]);
+    Kin<float> k;
+    kin_prep<float>(nx, ny, P[1], P[2], P[0], P[3], k);
+    KinBarT<float> kb;
+    float bG[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) bG[r] = w.x * bs[r];
+    x_flux_vjp(f, k, (dir & kXpos) ? 1.0f : -1.0f, bG, kb);
+#pragma unroll
+    for (int r = 0; r < 4; r++) bG[r] = w.y * bs[r];
+    adj::flux_y_vjp<float>(k, (dir & kYpos) ? 1.0f : -1.0f, bG, kb);
+    const bool xb = (dir & (kXpos | kXneg)) == (kXpos | kXneg), yb = (dir & (kYpos | kYneg)) == (kYpos | kYneg);
+    if (xb || yb) {
+        const float2 w2 = c.e_w32b[e];
+        if (xb) {
+#pragma unroll
+            for (int r = 0; r < 4; r++) bG[r] = w2.x * bs[r];
+            x_flux_vjp(f, k, -1.0f, bG, kb);
+        }
+        if (yb) {
+#pragma unroll
+            for (int r = 0; r < 4; r++) bG[r] = w2.y * bs[r];
+            adj::flux_y_vjp<float>(k, -1.0f, bG, kb);
+        }
+    }
+    float bP[4] = {0, 0, 0, 0}, bn0 = 0.f, bn1 = 0.f;
+    adj::kin_vjp<float>(nx, ny, P, k, kb, bP, bn0, bn1);
+    float bt[4] = {0, 0, 0, 0};
+    adj::qtilde_to_prim_vjp<float>(t, bP, bt);
+    float bdelx = 0.f, bdely = 0.f;
+    adj::edge_end_vjp<float>(delx, dely, q, dx, dy, mx, mn, e2, bt, bq, bdx, bdy, bmx, bmn, bdelx, bdely);
+}
+
+template <bool UW> __device__ __forceinline__ float2 edge_del(const DevCloud &c, long long e)
+{
+    if (UW) return c.e_xy32[e];
+    const float4 g = c.e_geo32[e];
+    return make_float2(g.x, g.y);
+}
+
 // Reverse of the flux part of the mixed flux + update kernel for stage
 // state (q, dq, qm): F = delta * acc, acc = sum_e w_e (G_k - G_i) over each
-// edge's x and y half-ranges.  bF (FP64, from adjk::k_update) in; bars of
-// q, dq, qm (own and neighbours'), and of delta (owner) out.
+// edge's x and y half-ranges.  The two ends of an edge are independent given
+// the bar of acc, so the owner ends (k_flux_own: the point's own data only,
+// bars kept in registers, and the bar of delta) and the neighbour ends
+// (k_flux_nbr: the neighbour's data gathered, bars scattered with vector
+// reductions) run as two kernels, each holding one end's state.  bF (FP64,
+// from adjk::k_update) in.
 template <bool UW>
-__global__ void __launch_bounds__(128) k_flux(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ dq,
-                                               const float4 *__restrict__ qm, const float *__restrict__ delta,
-                                               const float4 *__restrict__ acc, const double4_32a *__restrict__ bF,
-                                               float4 *__restrict__ bq, float4 *__restrict__ bdq,
-                                               float4 *__restrict__ bqm, float *__restrict__ bdelta)
+__global__ void __launch_bounds__(128) k_flux_own(DevCloud c, const float4 *__restrict__ q,
+                                                   const float4 *__restrict__ dq, const float4 *__restrict__ qm,
+                                                   const float *__restrict__ delta, const float4 *__restrict__ acc,
+                                                   const double4_32a *__restrict__ bF, float4 *__restrict__ bq,
+                                                   float4 *__restrict__ bdq, float4 *__restrict__ bqm,
+                                                   float *__restrict__ bdelta)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
@@ -623,93 +681,61 @@ __global__ void __launch_bounds__(128) k_flux(DevCloud c, const float4 *__restri
     const float4 ac = acc[i];
     const float dl = delta[i];
     bdelta[i] += (float)(bFi.x * ac.x + bFi.y * ac.y + bFi.z * ac.z + bFi.w * ac.w);
-    const float bacc[4] = {(float)(dl * bFi.x), (float)(dl * bFi.y), (float)(dl * bFi.z), (float)(dl * bFi.w)};
+    const float bs[4] = {(float)(-dl * bFi.x), (float)(-dl * bFi.y), (float)(-dl * bFi.z), (float)(-dl * bFi.w)};
     float bqi[4] = {0, 0, 0, 0}, bdxi[4] = {0, 0, 0, 0}, bdyi[4] = {0, 0, 0, 0}, bmxi[4] = {0, 0, 0, 0},
           bmni[4] = {0, 0, 0, 0};
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
-        const int k = c.e_nbr[e];
-        float delx, dely;
-        if (UW) {
-            const float2 d = c.e_xy32[e];
-            delx = d.x;
-            dely = d.y;
-        } else {
-            const float4 g = c.e_geo32[e];
-            delx = g.x;
-            dely = g.y;
-        }
-        const float2 w = c.e_w32[e];
-        const unsigned dir = c.e_dir[e];
-        float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
-        ldf4(q[k], qk);
-        ldf4(dq[2 * k], dxk);
-        ldf4(dq[2 * k + 1], dyk);
-        ldf4(qm[2 * k], mxk);
-        ldf4(qm[2 * k + 1], mnk);
-        const float e2k = c.eps2_32[k];
-        float ti[4], tk[4], Pi[4], Pk[4];
-        qtilde_f(delx, dely, qi, dxi, dyi, mxi, mni, e2i, ti);
-        qtilde_f(delx, dely, qk, dxk, dyk, mxk, mnk, e2k, tk);
-        qtilde_to_prim<float>(ti, Pi[1], Pi[2], Pi[0], Pi[3]);
-        qtilde_to_prim<float>(tk, Pk[1], Pk[2], Pk[0], Pk[3]);
-        Kin<float> ki, kk;
-        kin_prep<float>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
-        kin_prep<float>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
-        KinBarT<float> kbi, kbk;
-        float bGk[4], bGi[4];
-        const float s1 = (dir & kXpos) ? 1.0f : -1.0f;
-#pragma unroll
-        for (int r = 0; r < 4; r++) { bGk[r] = w.x * bacc[r]; bGi[r] = -bGk[r]; }
-        x_flux_vjp(f, kk, s1, bGk, kbk);
-        x_flux_vjp(f, ki, s1, bGi, kbi);
-        const float s2 = (dir & kYpos) ? 1.0f : -1.0f;
-#pragma unroll
-        for (int r = 0; r < 4; r++) { bGk[r] = w.y * bacc[r]; bGi[r] = -bGk[r]; }
-        adj::flux_y_vjp<float>(kk, s2, bGk, kbk);
-        adj::flux_y_vjp<float>(ki, s2, bGi, kbi);
-        const bool xb = (dir & (kXpos | kXneg)) == (kXpos | kXneg), yb = (dir & (kYpos | kYneg)) == (kYpos | kYneg);
-        if (xb || yb) {
-            const float2 w2 = c.e_w32b[e];
-            if (xb) {
-#pragma unroll
-                for (int r = 0; r < 4; r++) { bGk[r] = w2.x * bacc[r]; bGi[r] = -bGk[r]; }
-                x_flux_vjp(f, kk, -1.0f, bGk, kbk);
-                x_flux_vjp(f, ki, -1.0f, bGi, kbi);
-            }
-            if (yb) {
-#pragma unroll
-                for (int r = 0; r < 4; r++) { bGk[r] = w2.y * bacc[r]; bGi[r] = -bGk[r]; }
-                adj::flux_y_vjp<float>(kk, -1.0f, bGk, kbk);
-                adj::flux_y_vjp<float>(ki, -1.0f, bGi, kbi);
-            }
-        }
-        float bPi[4] = {0, 0, 0, 0}, bPk[4] = {0, 0, 0, 0}, bn0 = 0.f, bn1 = 0.f;
-        adj::kin_vjp<float>(nx, ny, Pi, ki, kbi, bPi, bn0, bn1);
-        adj::kin_vjp<float>(nx, ny, Pk, kk, kbk, bPk, bn0, bn1);
-        float bti[4] = {0, 0, 0, 0}, btk[4] = {0, 0, 0, 0};
-        adj::qtilde_to_prim_vjp<float>(ti, bPi, bti);
-        adj::qtilde_to_prim_vjp<float>(tk, bPk, btk);
-        float bdelx = 0.f, bdely = 0.f;
-        adj::edge_end_vjp<float>(delx, dely, qi, dxi, dyi, mxi, mni, e2i, bti, bqi, bdxi, bdyi, bmxi, bmni, bdelx,
-                                 bdely);
-        float bqk[4] = {0, 0, 0, 0}, bdxk[4] = {0, 0, 0, 0}, bdyk[4] = {0, 0, 0, 0}, bmxk[4] = {0, 0, 0, 0},
-              bmnk[4] = {0, 0, 0, 0};
-        adj::edge_end_vjp<float>(delx, dely, qk, dxk, dyk, mxk, mnk, e2k, btk, bqk, bdxk, bdyk, bmxk, bmnk, bdelx,
-                                 bdely);
-        atomic_add4(bq + k, bqk);
-        atomic_add4(bdq + 2 * k, bdxk);
-        atomic_add4(bdq + 2 * k + 1, bdyk);
-        atomic_add4(bqm + 2 * k, bmxk);
-        atomic_add4(bqm + 2 * k + 1, bmnk);
+        const float2 d = edge_del<UW>(c, e);
+        end_vjp(c, e, f, nx, ny, d.x, d.y, c.e_w32[e], c.e_dir[e], bs, qi, dxi, dyi, mxi, mni, e2i, bqi, bdxi, bdyi,
+                bmxi, bmni);
     }
     atomic_add4(bq + i, bqi);
     atomic_add4(bdq + 2 * i, bdxi);
     atomic_add4(bdq + 2 * i + 1, bdyi);
     atomic_add4(bqm + 2 * i, bmxi);
     atomic_add4(bqm + 2 * i + 1, bmni);
+}
+
+template <bool UW>
+__global__ void __launch_bounds__(128) k_flux_nbr(DevCloud c, const float4 *__restrict__ q,
+                                                   const float4 *__restrict__ dq, const float4 *__restrict__ qm,
+                                                   const float *__restrict__ delta, const double4_32a *__restrict__ bF,
+                                                   float4 *__restrict__ bq, float4 *__restrict__ bdq,
+                                                   float4 *__restrict__ bqm)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const int f = c.flag[i];
+    const double2 nn = c.nrm[i];
+    const float nx = (float)nn.x, ny = (float)nn.y;
+    const double4_32a bFi = bF[i];
+    const float dl = delta[i];
+    const float bs[4] = {(float)(dl * bFi.x), (float)(dl * bFi.y), (float)(dl * bFi.z), (float)(dl * bFi.w)};
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const float2 d = edge_del<UW>(c, e);
+        float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
+        ldf4(q[k], qk);
+        ldf4(dq[2 * k], dxk);
+        ldf4(dq[2 * k + 1], dyk);
+        ldf4(qm[2 * k], mxk);
+        ldf4(qm[2 * k + 1], mnk);
+        float bqk[4] = {0, 0, 0, 0}, bdxk[4] = {0, 0, 0, 0}, bdyk[4] = {0, 0, 0, 0}, bmxk[4] = {0, 0, 0, 0},
+              bmnk[4] = {0, 0, 0, 0};
+        end_vjp(c, e, f, nx, ny, d.x, d.y, c.e_w32[e], c.e_dir[e], bs, qk, dxk, dyk, mxk, mnk, c.eps2_32[k], bqk,
+                bdxk, bdyk, bmxk, bmnk);
+        atomic_add4(bq + k, bqk);
+        atomic_add4(bdq + 2 * k, bdxk);
+        atomic_add4(bdq + 2 * k + 1, bdyk);
+        atomic_add4(bqm + 2 * k, bmxk);
+        atomic_add4(bqm + 2 * k + 1, bmnk);
+    }
 }
 
 // The FP64 2x2 solve dx = X a - Y b, dy = Y c - X b (a = syy/det, b =
@@ -888,6 +914,51 @@ __global__ void k_wave(int n, const double4_32a *__restrict__ P, const float *__
     bP[i] = acc;
 }
 
+// Reverse of one SSPRK stage update (the FP64 update of the mixed flux
+// kernel), evaluated in FP32 on FP64-stored states and bars: bP (the bar of
+// Pout on entry) becomes the update's part of the bar of Pin; bF the bar of
+// the flux residual; stage 4 adds to bPold; outer points add the free-stream
+// velocity bars (one FP64 atomic per warp).
+__global__ void k_update(DevCloud c, CaseConst K, const double4_32a *__restrict__ Pin,
+                         const double4_32a *__restrict__ Pold, const double4_32a *__restrict__ Pout, int rk,
+                         double4_32a *__restrict__ bP, double4_32a *__restrict__ bPold, double4_32a *__restrict__ bF,
+                         double *__restrict__ buinf)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float bu1 = 0.f, bu2 = 0.f;
+    if (i < c.n) {
+        const int f = c.flag[i];
+        const double2 nn = c.nrm[i];
+        const double4_32a a = Pin[i], b = Pold[i], o = Pout[i], g = bP[i];
+        const float pin[4] = {(float)a.x, (float)a.y, (float)a.z, (float)a.w};
+        const float pold[4] = {(float)b.x, (float)b.y, (float)b.z, (float)b.w};
+        const float pout[4] = {(float)o.x, (float)o.y, (float)o.z, (float)o.w};
+        const float bout[4] = {(float)g.x, (float)g.y, (float)g.z, (float)g.w};
+        float bin[4] = {0, 0, 0, 0}, bo[4] = {0, 0, 0, 0}, bf[4] = {0, 0, 0, 0}, bnx = 0.f, bny = 0.f;
+        adj::stage_update_vjp<float>(K, f, (float)nn.x, (float)nn.y, pin, pold, pout, rk, bout, bin, bo, bf, bnx, bny,
+                                     bu1, bu2);
+        bP[i] = make_double4_32a(bin[0], bin[1], bin[2], bin[3]);
+        bF[i] = make_double4_32a(bf[0], bf[1], bf[2], bf[3]);
+        if (rk == 3) {
+            double4_32a acc = bPold[i];
+            acc.x += bo[0];
+            acc.y += bo[1];
+            acc.z += bo[2];
+            acc.w += bo[3];
+            bPold[i] = acc;
+        }
+    }
+    double d1 = bu1, d2 = bu2;
+    for (int o = 16; o > 0; o >>= 1) {
+        d1 += __shfl_down_sync(0xffffffffu, d1, o);
+        d2 += __shfl_down_sync(0xffffffffu, d2, o);
+    }
+    if ((threadIdx.x & 31) == 0 && (d1 != 0.0 || d2 != 0.0)) {
+        atomicAdd(buinf, d1);
+        atomicAdd(buinf + 1, d2);
+    }
+}
+
 }  // namespace adjm
 
 // ------------------------------------------------------------- launchers
@@ -967,11 +1038,14 @@ static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
 void flux(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq, const float4 *qm, const float *delta,
           const float4 *acc, const double4_32a *bF, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta)
 {
-    if (c.unit_w)
-        adjm::k_flux<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq, qm, delta, acc, bF, bq, bdq, bqm, bdelta);
-    else
-        adjm::k_flux<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq, qm, delta, acc, bF, bq, bdq, bqm,
-                                                                      bdelta);
+    const int g = grid_for(c.n, 128);
+    if (c.unit_w) {
+        adjm::k_flux_own<true><<<g, 128, 0, L.stream>>>(c, q, dq, qm, delta, acc, bF, bq, bdq, bqm, bdelta);
+        adjm::k_flux_nbr<true><<<g, 128, 0, L.stream>>>(c, q, dq, qm, delta, bF, bq, bdq, bqm);
+    } else {
+        adjm::k_flux_own<false><<<g, 128, 0, L.stream>>>(c, q, dq, qm, delta, acc, bF, bq, bdq, bqm, bdelta);
+        adjm::k_flux_nbr<false><<<g, 128, 0, L.stream>>>(c, q, dq, qm, delta, bF, bq, bdq, bqm);
+    }
 }
 
 void inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, const float4 *bdq_out,
@@ -987,6 +1061,12 @@ void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq
 {
     if (c.unit_w) adjm::k_grad<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, bdq, bqm, bq);
     else adjm::k_grad<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, bdq, bqm, bq);
+}
+
+void update(const Launch &L, const DevCloud &c, const CaseConst &K, const double4_32a *Pin, const double4_32a *Pold,
+            const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, double4_32a *bF, double *buinf)
+{
+    adjm::k_update<<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, K, Pin, Pold, Pout, rk, bP, bPold, bF, buinf);
 }
 
 void qvars(const Launch &L, int n, const double4_32a *P, const float4 *bq, double4_32a *bP)

@@ -24,13 +24,13 @@ namespace adj {
 template <typename R> QLSKUM_HD void prim_to_q_vjp(const R P[4], const R bq[4], R bP[4])
 {
     const R rho = P[0], u1 = P[1], u2 = P[2], p = P[3];
-    const R beta = R(0.5) * rho / p;
+    const R beta = M<R>::div(R(0.5) * rho, p);
     const R usq = u1 * u1 + u2 * u2;
-    const R bbeta = bq[0] * (R(2.5) / beta - usq) + bq[1] * R(2.0) * u1 + bq[2] * R(2.0) * u2 - R(2.0) * bq[3];
-    bP[0] += bq[0] / rho + bbeta * R(0.5) / p;
+    const R bbeta = bq[0] * (M<R>::div(R(2.5), beta) - usq) + bq[1] * R(2.0) * u1 + bq[2] * R(2.0) * u2 - R(2.0) * bq[3];
+    bP[0] += M<R>::div(bq[0], rho) + M<R>::div(bbeta * R(0.5), p);
     bP[1] += -bq[0] * R(2.0) * beta * u1 + bq[1] * R(2.0) * beta;
     bP[2] += -bq[0] * R(2.0) * beta * u2 + bq[2] * R(2.0) * beta;
-    bP[3] += -bbeta * beta / p;
+    bP[3] += -M<R>::div(bbeta * beta, p);
 }
 
 // limiters_mod.h:64-104 for one component.
@@ -43,9 +43,10 @@ template <typename R> QLSKUM_HD void venkat_vjp(R qt, R q, R qmax, R qmin, R eps
     const R dp = (up ? qmax : qmin) - q;
     const R num = (dp * dp + eps2) * dn + R(2.0) * dn * dn * dp;
     const R den = (dp * dp + R(2.0) * dn * dn + dn * dp + eps2) * dn;
-    const R t = num / den;
+    const R rden = M<R>::div(R(1.0), den);
+    const R t = num * rden;
     if (!(t < R(1.0))) return;
-    const R bnum = bphi / den, bden = -bphi * t / den;
+    const R bnum = bphi * rden, bden = -bphi * t * rden;
     const R bdn = bnum * (dp * dp + eps2 + R(4.0) * dn * dp) +
                        bden * ((dp * dp + R(2.0) * dn * dn + dn * dp + eps2) + dn * (R(4.0) * dn + dp));
     const R bdp = bnum * (R(2.0) * dp * dn + R(2.0) * dn * dn) + bden * (dn * (R(2.0) * dp + dn));
@@ -60,16 +61,16 @@ template <typename R> QLSKUM_HD void qtilde_to_prim_vjp(const R qt[4], const R b
 {
     const R gm1 = R(1.4) - R(1.0);
     const R beta = -qt[3] * R(0.5);
-    const R t = R(0.5) / beta;
+    const R t = M<R>::div(R(0.5), beta);
     const R u1 = qt[1] * t, u2 = qt[2] * t;
     const R T1 = qt[0] + beta * (u1 * u1 + u2 * u2);
-    const R rho = M<R>::ex(T1 - M<R>::lg(beta) / gm1);
+    const R rho = M<R>::ex(T1 - M<R>::div(M<R>::lg(beta), gm1));
     const R brho = bP[0] + bP[3] * t;
     const R bT2 = brho * rho, bT1 = bT2;
     const R bu1 = bP[1] + bT1 * R(2.0) * beta * u1;
     const R bu2 = bP[2] + bT1 * R(2.0) * beta * u2;
     const R bt = bP[3] * rho + bu1 * qt[1] + bu2 * qt[2];
-    const R bbeta = bT1 * (u1 * u1 + u2 * u2) - bT2 / (gm1 * beta) - bt * R(0.5) / (beta * beta);
+    const R bbeta = bT1 * (u1 * u1 + u2 * u2) - M<R>::div(bT2, gm1 * beta) - M<R>::div(bt * R(0.5), beta * beta);
     bqt[0] += bT1;
     bqt[1] += bu1 * t;
     bqt[2] += bu2 * t;
@@ -87,7 +88,7 @@ template <typename R> QLSKUM_HD void kin_vjp(R nx, R ny, const R P[4], const Kin
                        R &bnx, R &bny)
 {
     const R rho = P[0], u1 = P[1], u2 = P[2], p = P[3];
-    const R beta = R(0.5) * rho / p;
+    const R beta = M<R>::div(R(0.5) * rho, p);
     const R sb = M<R>::sq(beta);
     const R S1 = k.ut * sb, S2 = k.un * sb;
     const R two_over_sqrtpi = R(1.1283791670955126);
@@ -98,9 +99,9 @@ template <typename R> QLSKUM_HD void kin_vjp(R nx, R ny, const R P[4], const Kin
     but += bS1 * sb;
     bun += bS2 * sb;
     const R bsb = bS1 * k.ut + bS2 * k.un;
-    const R bbeta = bsb * R(0.5) / sb - (kb.B1 * k.B1 + kb.B2 * k.B2) * R(0.5) / beta;
-    bP[0] += kb.rho + bbeta * R(0.5) / p - kb.pbr * p / (rho * rho);
-    bP[3] += -bbeta * beta / p + kb.pbr / rho;
+    const R bbeta = M<R>::div(bsb * R(0.5), sb) - M<R>::div((kb.B1 * k.B1 + kb.B2 * k.B2) * R(0.5), beta);
+    bP[0] += kb.rho + M<R>::div(bbeta * R(0.5), p) - M<R>::div(kb.pbr * p, rho * rho);
+    bP[3] += -M<R>::div(bbeta * beta, p) + M<R>::div(kb.pbr, rho);
     bP[1] += but * ny + bun * nx;
     bP[2] += -but * nx + bun * ny;
     bnx += -but * u2 + bun * u1;
@@ -212,65 +213,69 @@ template <typename R> QLSKUM_HD void edge_end_vjp(R delx, R dely, const R q[4], 
 }
 
 // primitive_to_conserved (state_update_mod.h:18-33)
-QLSKUM_HD void p2c_vjp(const double P[4], double nx, double ny, const double bU[4], double bP[4], double &bnx,
-                       double &bny)
+template <typename R>
+QLSKUM_HD void p2c_vjp(const R P[4], R nx, R ny, const R bU[4], R bP[4], R &bnx, R &bny)
 {
-    const double rho = P[0], t1 = rho * P[1], t2 = rho * P[2];
-    const double bt1 = bU[3] * t1 / rho + bU[1] * ny + bU[2] * nx;
-    const double bt2 = bU[3] * t2 / rho - bU[1] * nx + bU[2] * ny;
-    bP[0] += bU[0] - bU[3] * 0.5 * (t1 * t1 + t2 * t2) / (rho * rho) + bt1 * P[1] + bt2 * P[2];
+    const R rho = P[0], t1 = rho * P[1], t2 = rho * P[2];
+    const R bt1 = M<R>::div(bU[3] * t1, rho) + bU[1] * ny + bU[2] * nx;
+    const R bt2 = M<R>::div(bU[3] * t2, rho) - bU[1] * nx + bU[2] * ny;
+    bP[0] += bU[0] - M<R>::div(bU[3] * R(0.5) * (t1 * t1 + t2 * t2), rho * rho) + bt1 * P[1] + bt2 * P[2];
     bP[1] += bt1 * rho;
     bP[2] += bt2 * rho;
-    bP[3] += 2.5 * bU[3];
+    bP[3] += R(2.5) * bU[3];
     bnx += -bU[1] * t2 + bU[2] * t1;
     bny += bU[1] * t1 + bU[2] * t2;
 }
 
 // conserved_vector_Ubar (state_update_mod.h:35-90): bars of the point's
 // state, of the normal and of the free-stream velocity (u1_inf, u2_inf).
-QLSKUM_HD void ubar_vjp(const CaseConst &K, const double P[4], double nx, double ny, const double bU[4], double bP[4],
-                        double &bnx, double &bny, double &bu1i, double &bu2i)
+template <typename R>
+QLSKUM_HD void ubar_vjp(const CaseConst &K, const R P[4], R nx, R ny, const R bU[4], R bP[4], R &bnx, R &bny,
+                        R &bu1i, R &bu2i)
 {
-    const double g1 = K.gamma - 1.0, pi = K.pi, rhoi = K.rho_inf, pri = K.pr_inf;
-    const double tx = ny, ty = -nx;
-    const double inv_sqrtpi = 0.5641895835477563;
+    const R g1 = R(K.gamma) - R(1.0), pi = R(K.pi), rhoi = R(K.rho_inf), pri = R(K.pr_inf);
+    const R u1inf = R(K.u1_inf), u2inf = R(K.u2_inf);
+    const R tx = ny, ty = -nx;
+    const R inv_sqrtpi = R(0.5641895835477563);
     // free-stream half
-    const double u1ri = K.u1_inf * tx + K.u2_inf * ty, u2ri = K.u1_inf * nx + K.u2_inf * ny;
-    const double einf = pri / (rhoi * g1) + 0.5 * (u1ri * u1ri + u2ri * u2ri);
-    const double bi = (0.5 * rhoi) / pri, sbi = sqrt(bi);
-    const double Si = u2ri * sbi;
-    const double Bi = exp(-Si * Si) / (2.0 * sqrt(pi * bi));
-    const double Ai = 0.5 * (1.0 - erf(Si));
-    const double bAi = bU[0] * rhoi + bU[1] * rhoi * u1ri + bU[2] * rhoi * u2ri + bU[3] * rhoi * einf;
-    const double bBi = -bU[2] * rhoi - bU[3] * 0.5 * rhoi * u2ri;
-    const double bei = bU[3] * rhoi * Ai;
-    const double bSi = -bAi * inv_sqrtpi * exp(-Si * Si) + bBi * Bi * (-2.0 * Si);
-    const double bu1ri = bU[1] * rhoi * Ai + bei * u1ri;
-    const double bu2ri = bU[2] * rhoi * Ai - bU[3] * 0.5 * rhoi * Bi + bei * u2ri + bSi * sbi;
+    const R u1ri = u1inf * tx + u2inf * ty, u2ri = u1inf * nx + u2inf * ny;
+    const R einf = M<R>::div(pri, rhoi * g1) + R(0.5) * (u1ri * u1ri + u2ri * u2ri);
+    const R bi = M<R>::div(R(0.5) * rhoi, pri), sbi = M<R>::sq(bi);
+    const R Si = u2ri * sbi;
+    const R ei = M<R>::ex(-Si * Si);
+    const R Bi = M<R>::div(ei, R(2.0) * M<R>::sq(pi * bi));
+    const R Ai = R(0.5) * (R(1.0) - erf_e<R>(Si, ei));
+    const R bAi = bU[0] * rhoi + bU[1] * rhoi * u1ri + bU[2] * rhoi * u2ri + bU[3] * rhoi * einf;
+    const R bBi = -bU[2] * rhoi - bU[3] * R(0.5) * rhoi * u2ri;
+    const R bei = bU[3] * rhoi * Ai;
+    const R bSi = -bAi * inv_sqrtpi * ei + bBi * Bi * (R(-2.0) * Si);
+    const R bu1ri = bU[1] * rhoi * Ai + bei * u1ri;
+    const R bu2ri = bU[2] * rhoi * Ai - bU[3] * R(0.5) * rhoi * Bi + bei * u2ri + bSi * sbi;
     bu1i += bu1ri * tx + bu2ri * nx;
     bu2i += bu1ri * ty + bu2ri * ny;
-    bnx += -bu1ri * K.u2_inf + bu2ri * K.u1_inf;
-    bny += bu1ri * K.u1_inf + bu2ri * K.u2_inf;
+    bnx += -bu1ri * u2inf + bu2ri * u1inf;
+    bny += bu1ri * u1inf + bu2ri * u2inf;
     // the point's half
-    const double rho = P[0], u1 = P[1], u2 = P[2], p = P[3];
-    const double u1r = u1 * tx + u2 * ty, u2r = u1 * nx + u2 * ny;
-    const double e = p / (rho * g1) + 0.5 * (u1r * u1r + u2r * u2r);
-    const double beta = rho / (2.0 * p), sb = sqrt(beta);
-    const double S = u2r * sb;
-    const double B = exp(-S * S) / (2.0 * sqrt(pi * beta));
-    const double A = 0.5 * (1.0 + erf(S));
-    const double bA = bU[0] * rho + bU[1] * rho * u1r + bU[2] * rho * u2r + bU[3] * rho * e;
-    const double bB = bU[2] * rho + bU[3] * 0.5 * rho * u2r;
-    const double be = bU[3] * rho * A;
-    double brho = bU[0] * A + bU[1] * u1r * A + bU[2] * (u2r * A + B) + bU[3] * (A * e + 0.5 * u2r * B);
-    const double bS = bA * inv_sqrtpi * exp(-S * S) + bB * B * (-2.0 * S);
-    const double bu1r = bU[1] * rho * A + be * u1r;
-    const double bu2r = bU[2] * rho * A + bU[3] * 0.5 * rho * B + be * u2r + bS * sb;
-    const double bbeta = bS * u2r * 0.5 / sb - bB * B * 0.5 / beta;
-    double bp = be / (rho * g1);
-    brho += -be * p / (rho * rho * g1);
-    brho += bbeta / (2.0 * p);
-    bp += -bbeta * beta / p;
+    const R rho = P[0], u1 = P[1], u2 = P[2], p = P[3];
+    const R u1r = u1 * tx + u2 * ty, u2r = u1 * nx + u2 * ny;
+    const R e = M<R>::div(p, rho * g1) + R(0.5) * (u1r * u1r + u2r * u2r);
+    const R beta = M<R>::div(rho, R(2.0) * p), sb = M<R>::sq(beta);
+    const R S = u2r * sb;
+    const R es = M<R>::ex(-S * S);
+    const R B = M<R>::div(es, R(2.0) * M<R>::sq(pi * beta));
+    const R A = R(0.5) * (R(1.0) + erf_e<R>(S, es));
+    const R bA = bU[0] * rho + bU[1] * rho * u1r + bU[2] * rho * u2r + bU[3] * rho * e;
+    const R bB = bU[2] * rho + bU[3] * R(0.5) * rho * u2r;
+    const R be = bU[3] * rho * A;
+    R brho = bU[0] * A + bU[1] * u1r * A + bU[2] * (u2r * A + B) + bU[3] * (A * e + R(0.5) * u2r * B);
+    const R bS = bA * inv_sqrtpi * es + bB * B * (R(-2.0) * S);
+    const R bu1r = bU[1] * rho * A + be * u1r;
+    const R bu2r = bU[2] * rho * A + bU[3] * R(0.5) * rho * B + be * u2r + bS * sb;
+    const R bbeta = M<R>::div(bS * u2r * R(0.5), sb) - M<R>::div(bB * B * R(0.5), beta);
+    R bp = M<R>::div(be, rho * g1);
+    brho += -M<R>::div(be * p, rho * rho * g1);
+    brho += M<R>::div(bbeta, R(2.0) * p);
+    bp += -M<R>::div(bbeta * beta, p);
     bP[0] += brho;
     bP[1] += bu1r * tx + bu2r * nx;
     bP[2] += bu1r * ty + bu2r * ny;
@@ -282,47 +287,49 @@ QLSKUM_HD void ubar_vjp(const CaseConst &K, const double P[4], double nx, double
 // One SSPRK stage of one point (state_update_mod.h:111-282) in reverse.
 // Pout is the stage's output state (it carries U' and 1/U'0).  Adds the bars
 // of the input state, of prim_old (stage 3), of the flux residual, of the
-// normal and of the free-stream velocity (outer points).
-QLSKUM_HD void stage_update_vjp(const CaseConst &K, int f, double nx, double ny, const double Pin[4],
-                                const double Pold[4], const double Pout[4], int rk, const double bPout[4],
-                                double bPin[4], double bPold[4], double bF[4], double &bnx, double &bny,
-                                double &bu1i, double &bu2i)
+// normal and of the free-stream velocity (outer points).  R = double for the
+// FP64 iteration; float for the reverse of the mixed one (whose forward
+// update is FP64: its reverse needs only the bars' relative accuracy).
+template <typename R>
+QLSKUM_HD void stage_update_vjp(const CaseConst &K, int f, R nx, R ny, const R Pin[4], const R Pold[4],
+                                const R Pout[4], int rk, const R bPout[4], R bPin[4], R bPold[4], R bF[4], R &bnx,
+                                R &bny, R &bu1i, R &bu2i)
 {
-    const double obt = 1.0 / 3.0, tbt = 2.0 / 3.0;
-    const double U0 = Pout[0], inv = 1.0 / U0;
-    const double V1 = Pout[1] * U0, V2 = Pout[2] * U0;  // rotated-back momentum
-    double bU[4];
-    double binv = bPout[1] * V1 + bPout[2] * V2 - 0.2 * bPout[3] * (V1 * V1 + V2 * V2);
-    const double bV1 = bPout[1] * inv - 0.4 * bPout[3] * inv * V1;
-    const double bV2 = bPout[2] * inv - 0.4 * bPout[3] * inv * V2;
+    const R obt = R(1.0) / R(3.0), tbt = R(2.0) / R(3.0);
+    const R U0 = Pout[0], inv = M<R>::div(R(1.0), U0);
+    const R V1 = Pout[1] * U0, V2 = Pout[2] * U0;  // rotated-back momentum
+    R bU[4];
+    R binv = bPout[1] * V1 + bPout[2] * V2 - R(0.2) * bPout[3] * (V1 * V1 + V2 * V2);
+    const R bV1 = bPout[1] * inv - R(0.4) * bPout[3] * inv * V1;
+    const R bV2 = bPout[2] * inv - R(0.4) * bPout[3] * inv * V2;
     bU[0] = bPout[0] - binv * inv * inv;
-    bU[3] = 0.4 * bPout[3];
+    bU[3] = R(0.4) * bPout[3];
     // V1 = U1 ny + U2 nx, V2 = U2 ny - U1 nx (U in the (t, n) frame)
     bU[1] = bV1 * ny - bV2 * nx;
     bU[2] = bV1 * nx + bV2 * ny;
     // the frame of the output: U1 = V1 ny - V2 nx, U2 = V1 nx + V2 ny
-    const double U1 = V1 * ny - V2 * nx, U2 = V1 * nx + V2 * ny;
+    const R U1 = V1 * ny - V2 * nx, U2 = V1 * nx + V2 * ny;
     bny += bV1 * U1 + bV2 * U2;
     bnx += bV1 * U2 - bV2 * U1;
-    if (f == kWall) bU[2] = 0.0;
-    double bUin[4], bUold[4];
+    if (f == kWall) bU[2] = R(0.0);
+    R bUin[4], bUold[4];
     for (int j = 0; j < 4; j++) {
         if (rk != 3) {
             bUin[j] = bU[j];
-            bF[j] += -0.5 * bU[j];
-            bUold[j] = 0.0;
+            bF[j] += R(-0.5) * bU[j];
+            bUold[j] = R(0.0);
         } else {
             bUold[j] = tbt * bU[j];
             bUin[j] = obt * bU[j];
-            bF[j] += -0.5 * obt * bU[j];
+            bF[j] += R(-0.5) * obt * bU[j];
         }
     }
     if (f == kOuter) {
-        ubar_vjp(K, Pin, nx, ny, bUin, bPin, bnx, bny, bu1i, bu2i);
-        if (rk == 3) ubar_vjp(K, Pold, nx, ny, bUold, bPold, bnx, bny, bu1i, bu2i);
+        ubar_vjp<R>(K, Pin, nx, ny, bUin, bPin, bnx, bny, bu1i, bu2i);
+        if (rk == 3) ubar_vjp<R>(K, Pold, nx, ny, bUold, bPold, bnx, bny, bu1i, bu2i);
     } else {
-        p2c_vjp(Pin, nx, ny, bUin, bPin, bnx, bny);
-        if (rk == 3) p2c_vjp(Pold, nx, ny, bUold, bPold, bnx, bny);
+        p2c_vjp<R>(Pin, nx, ny, bUin, bPin, bnx, bny);
+        if (rk == 3) p2c_vjp<R>(Pold, nx, ny, bUold, bPold, bnx, bny);
     }
 }
 
@@ -332,13 +339,13 @@ template <typename R> QLSKUM_HD void wave_speed_vjp(const R P[4], R bc, R bP[4])
     const R usq = P[1] * P[1] + P[2] * P[2];
     const R mod_u = usq > R(0.0) ? M<R>::sq(usq) : R(0.0);
     if (mod_u > R(0.0)) {
-        bP[1] += bc * P[1] / mod_u;
-        bP[2] += bc * P[2] / mod_u;
+        bP[1] += M<R>::div(bc * P[1], mod_u);
+        bP[2] += M<R>::div(bc * P[2], mod_u);
     }
-    const R a = P[3] / P[0], sa = M<R>::sq(a);
-    const R ba = bc * R(1.5) / sa;
-    bP[3] += ba / P[0];
-    bP[0] += -ba * P[3] / (P[0] * P[0]);
+    const R a = M<R>::div(P[3], P[0]), sa = M<R>::sq(a);
+    const R ba = M<R>::div(bc * R(1.5), sa);
+    bP[3] += M<R>::div(ba, P[0]);
+    bP[0] += -M<R>::div(ba * P[3], P[0] * P[0]);
 }
 
 }  // namespace adj

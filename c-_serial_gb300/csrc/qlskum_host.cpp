@@ -2178,7 +2178,7 @@ void adj_iteration_reverse32(qlskum_handle *h, const AdjView &v)
     zero(h, a->bPacc, sizeof(double4_32a) * np);
     zero(h, a->bdelta32, sizeof(float) * np);
     for (int s = 3; s >= 0; s--) {
-        adjl::update(h->L, v, h->K, a->P[s], a->P[0], a->P[s + 1], s + 1, a->bP, a->bPacc, a->bF, a->buinf);
+        adjml::update(h->L, c, h->K, a->P[s], a->P[0], a->P[s + 1], s + 1, a->bP, a->bPacc, a->bF, a->buinf);
         zero(h, a->bq32, sizeof(float4) * np);
         zero(h, a->bdqA32, sizeof(float4) * 2 * np);
         zero(h, a->bqm32, sizeof(float4) * 2 * np);

@@ -191,6 +191,9 @@ void objective_J(const Launch &L, int n, const double4_32a *P, double gamma, dou
 // the FP32 q / dq / qm in float4 arrays (atomically accumulated), of delta in
 // float, of the FP64 states in double4.
 namespace adjml {
+// reverse of the stage update (rk 1..4 as the forward), FP32 arithmetic
+void update(const Launch &L, const DevCloud &c, const CaseConst &K, const double4_32a *Pin, const double4_32a *Pold,
+            const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, double4_32a *bF, double *buinf);
 void flux(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq, const float4 *qm, const float *delta,
           const float4 *acc, const double4_32a *bF, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta);
 void inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, const float4 *bdq_out,
