@@ -760,57 +760,74 @@ template <bool UW> __device__ __forceinline__ float4 edge_w(const DevCloud &c, l
     return c.e_geo32[e];
 }
 
-// Reverse of one mixed inner iteration (q_variables_mod.h:120-213).
+// Reverse of one mixed inner step, dq_out = dq0 + 0.5 (dq_in - solve(S)),
+// S = sum w d (d.dq_in_k) (inner_point of the mixed kernels): the bar of
+// dq_out goes to dq0 (accumulated over the steps in bdq0, the point's own
+// entry only), half of it to the point's own dq_in, and through the solve
+// and S to the neighbours' dq_in.
 template <bool UW>
-__global__ void k_inner(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ dq_in,
-                        const float4 *__restrict__ bdq_out, float4 *__restrict__ bq, float4 *__restrict__ bdq_in)
+__global__ void k_inner(DevCloud c, const float4 *__restrict__ bdq_out, float4 *__restrict__ bdq_in,
+                        float4 *__restrict__ bdq0)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
-    float bx[4], by[4], bsdx[4], bsdy[4];
+    float bx[4], by[4], bax[4], bay[4], bsx[4], bsy[4];
     ldf4(bdq_out[2 * i], bx);
     ldf4(bdq_out[2 * i + 1], by);
-    solve_vjp(c.gcoef[i], bx, by, bsdx, bsdy);
-    float dxi[4], dyi[4];
-    ldf4(dq_in[2 * i], dxi);
-    ldf4(dq_in[2 * i + 1], dyi);
-    float bqi[4] = {0, 0, 0, 0}, bdxi[4] = {0, 0, 0, 0}, bdyi[4] = {0, 0, 0, 0};
+    float a0[4], a1[4];
+    ldf4(bdq0[2 * i], a0);
+    ldf4(bdq0[2 * i + 1], a1);
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        a0[r] += bx[r];
+        a1[r] += by[r];
+        bax[r] = -0.5f * bx[r];
+        bay[r] = -0.5f * by[r];
+        bx[r] *= 0.5f;
+        by[r] *= 0.5f;
+    }
+    bdq0[2 * i] = make_float4(a0[0], a0[1], a0[2], a0[3]);
+    bdq0[2 * i + 1] = make_float4(a1[0], a1[1], a1[2], a1[3]);
+    atomic_add4(bdq_in + 2 * i, bx);
+    atomic_add4(bdq_in + 2 * i + 1, by);
+    solve_vjp(c.gcoef[i], bax, bay, bsx, bsy);
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         const float4 g = edge_w<UW>(c, e);
-        float bqk[4], bdxk[4], bdyk[4];
+        float bdxk[4], bdyk[4];
 #pragma unroll
         for (int r = 0; r < 4; r++) {
-            const float bt = g.z * bsdx[r] + g.w * bsdy[r];
-            bqk[r] = bt;
-            bdxk[r] = -0.5f * g.x * bt;
-            bdyk[r] = -0.5f * g.y * bt;
-            bqi[r] -= bt;
-            bdxi[r] += 0.5f * g.x * bt;
-            bdyi[r] += 0.5f * g.y * bt;
+            const float bu = g.z * bsx[r] + g.w * bsy[r];
+            bdxk[r] = g.x * bu;
+            bdyk[r] = g.y * bu;
         }
-        atomic_add4(bq + k, bqk);
         atomic_add4(bdq_in + 2 * k, bdxk);
         atomic_add4(bdq_in + 2 * k + 1, bdyk);
     }
-    atomic_add4(bq + i, bqi);
-    atomic_add4(bdq_in + 2 * i, bdxi);
-    atomic_add4(bdq_in + 2 * i + 1, bdyi);
 }
 
 // Reverse of the mixed gradient and neighbour max / min (q_variables_mod.h:36-118).
+// The bar of the stage's first-order gradient is bdq + bdq0 (the inner
+// steps' direct part).
 template <bool UW>
 __global__ void k_grad(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ bdq,
-                       const float4 *__restrict__ bqm, float4 *__restrict__ bq)
+                       const float4 *__restrict__ bdq0, const float4 *__restrict__ bqm, float4 *__restrict__ bq)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
-    float bx[4], by[4], bsdx[4], bsdy[4], bmax[4], bmin[4], qi[4];
+    float bx[4], by[4], bsdx[4], bsdy[4], bmax[4], bmin[4], qi[4], b0x[4], b0y[4];
     ldf4(bdq[2 * i], bx);
     ldf4(bdq[2 * i + 1], by);
+    ldf4(bdq0[2 * i], b0x);
+    ldf4(bdq0[2 * i + 1], b0y);
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        bx[r] += b0x[r];
+        by[r] += b0y[r];
+    }
     ldf4(bqm[2 * i], bmax);
     ldf4(bqm[2 * i + 1], bmin);
     ldf4(q[i], qi);
@@ -1048,19 +1065,17 @@ void flux(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq,
     }
 }
 
-void inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, const float4 *bdq_out,
-           float4 *bq, float4 *bdq_in)
+void inner(const Launch &L, const DevCloud &c, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0)
 {
-    if (c.unit_w)
-        adjm::k_inner<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq_in, bdq_out, bq, bdq_in);
-    else
-        adjm::k_inner<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq_in, bdq_out, bq, bdq_in);
+    if (c.unit_w) adjm::k_inner<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, bdq_out, bdq_in, bdq0);
+    else adjm::k_inner<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, bdq_out, bdq_in, bdq0);
 }
 
-void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq, const float4 *bqm, float4 *bq)
+void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq, const float4 *bdq0,
+          const float4 *bqm, float4 *bq)
 {
-    if (c.unit_w) adjm::k_grad<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, bdq, bqm, bq);
-    else adjm::k_grad<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, bdq, bqm, bq);
+    if (c.unit_w) adjm::k_grad<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, bdq, bdq0, bqm, bq);
+    else adjm::k_grad<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, bdq, bdq0, bqm, bq);
 }
 
 void update(const Launch &L, const DevCloud &c, const CaseConst &K, const double4_32a *Pin, const double4_32a *Pold,

@@ -460,7 +460,7 @@ qlskum_status tune(qlskum_handle *h)
     // gradient with the time step, inner_iterations inner steps per stage)
     const int ni = std::max(1, h->prm.inner_iterations);
     auto point_kernels = [&](const Launch &L) {
-        return ni * time3([&] { mixed::q_inner(L, c, S.q[0], S.dq[0], S.dq[1]); }) +
+        return ni * time3([&] { mixed::q_inner(L, c, S.dq[0], S.dq[0], S.dq[1]); }) +
                time3([&] { mixed::q_derivatives(L, c, S.q[0], S.dq[0], S.qm, S.cspeed, S.delta, (float)h->K.cfl); });
     };
     static const int blocks[4] = {64, 128, 256, 512};
@@ -527,9 +527,10 @@ void enqueue_iteration(qlskum_handle *h, int o, int it_arg)
                 mixed::q_derivatives(L, c, S.q[qa], S.dq[0], S.qm, S.cspeed, dl32, (float)h->K.cfl);
             });
             for (int j = 0; j < ni; j++)
-                timed(h, QLSKUM_KERNEL_INNER, [&] { mixed::q_inner(L, c, S.q[qa], S.dq[j & 1], S.dq[(j + 1) & 1]); });
+                timed(h, QLSKUM_KERNEL_INNER,
+                      [&] { mixed::q_inner(L, c, S.dq[0], S.dq[mixed_dq_in(j)], S.dq[mixed_dq_out(j)]); });
             timed(h, QLSKUM_KERNEL_FLUX_UPDATE, [&] {
-                mixed::flux_update(L, c, h->K, S.q[qa], S.dq[ni & 1], S.qm, S.delta, pin, pold, pout, S.q[qb], cs32,
+                mixed::flux_update(L, c, h->K, S.q[qa], S.dq[mixed_dq_final(ni)], S.qm, S.delta, pin, pold, pout, S.q[qb], cs32,
                                    rk, Rk, h->flux_variant);
             });
         } else {
@@ -895,10 +896,8 @@ qlskum_status qlskum_create(const qlskum_cloud *c, const qlskum_params *p, qlsku
     h->s64.delta = A.alloc<double>(h->np);
     h->s64.cspeed = A.alloc<double>(h->np);
     if (p->precision == QLSKUM_MIXED) {
-        for (int b = 0; b < 2; b++) {
-            h->s32.q[b] = A.alloc<float4>(h->np);
-            h->s32.dq[b] = A.alloc<float4>((size_t)h->np * 2);
-        }
+        for (int b = 0; b < 2; b++) h->s32.q[b] = A.alloc<float4>(h->np);
+        for (int b = 0; b < 3; b++) h->s32.dq[b] = A.alloc<float4>((size_t)h->np * 2);
         h->s32.qm = A.alloc<float4>((size_t)h->np * 2);
         h->s32.delta = A.alloc<float>(h->np);
         h->s32.cspeed = A.alloc<float>(h->np);
@@ -1156,7 +1155,10 @@ qlskum_status qlskum_get_field(qlskum_handle *h, int field, double *out)
         else src = h->s64.q[0];
         break;
     case QLSKUM_FIELD_DQ:
-        if (h->prm.precision == QLSKUM_MIXED && h->derived_valid) { src = h->s32.dq[h->dcur]; f32 = true; }
+        if (h->prm.precision == QLSKUM_MIXED && h->derived_valid) {
+            src = h->s32.dq[mixed_dq_final(h->prm.inner_iterations)];
+            f32 = true;
+        }
         else src = h->s64.dq[h->dcur];
         width = 8;
         break;
@@ -1322,7 +1324,7 @@ struct qlskum_batch {
     long long total = 0;                       // state points over all cases
     double4_32a *prim[3] = {nullptr, nullptr, nullptr};
     float4 *q[2] = {nullptr, nullptr};
-    float4 *dq[2] = {nullptr, nullptr};
+    float4 *dq[3] = {nullptr, nullptr, nullptr};  // as State32::dq
     float4 *qm = nullptr;
     float *delta = nullptr, *cspeed = nullptr;
     double *psum = nullptr, *pmax = nullptr;   // per flux tile
@@ -1367,8 +1369,9 @@ void batch_enqueue_iteration(qlskum_batch *b, int o)
         const int qa = (rk - 1) & 1, qb = rk & 1;
         mixed::batch_q_derivatives(b->L, b->view, b->tile, b->q[qa], b->dq[0], b->qm, b->cspeed,
                                    rk == 1 ? b->delta : nullptr, b->cfl);
-        for (int j = 0; j < ni; j++) mixed::batch_q_inner(b->L, b->view, b->tile, b->q[qa], b->dq[j & 1], b->dq[(j + 1) & 1]);
-        mixed::batch_flux_update(b->L, b->view, b->flux_variant, b->q[qa], b->dq[ni & 1], b->qm, b->delta,
+        for (int j = 0; j < ni; j++)
+            mixed::batch_q_inner(b->L, b->view, b->tile, b->dq[0], b->dq[mixed_dq_in(j)], b->dq[mixed_dq_out(j)]);
+        mixed::batch_flux_update(b->L, b->view, b->flux_variant, b->q[qa], b->dq[mixed_dq_final(ni)], b->qm, b->delta,
                                  b->prim[src[rk - 1]], b->prim[o], b->prim[dst[rk - 1]], b->q[qb],
                                  rk == 4 ? b->cspeed : nullptr, rk, rk == 4 ? b->psum : nullptr,
                                  rk == 4 ? b->pmax : nullptr);
@@ -1428,7 +1431,7 @@ qlskum_status batch_tune(qlskum_batch *b)
     const long long l0 = b->launches;
     float best = 1e30f;
     for (int t : {64, 128, 256}) {
-        float ms = time3([&] { mixed::batch_q_inner(b->L, b->view, t, b->q[0], b->dq[0], b->dq[1]); });
+        float ms = time3([&] { mixed::batch_q_inner(b->L, b->view, t, b->dq[0], b->dq[0], b->dq[1]); });
         if (ms < best) { best = ms; b->tile = t; }
     }
     const int o = b->pcur, x = (o + 1) % 3;
@@ -1535,10 +1538,8 @@ qlskum_status qlskum_batch_create(const qlskum_cloud *clouds, int n_clouds, cons
     for (int ti = 0; ti < 3; ti++) d_tiles[ti] = A.alloc<BatchTile>(b->tiles[ti].size());
     const size_t T = (size_t)b->total;
     for (int k = 0; k < 3; k++) b->prim[k] = A.alloc<double4_32a>(T);
-    for (int k = 0; k < 2; k++) {
-        b->q[k] = A.alloc<float4>(T);
-        b->dq[k] = A.alloc<float4>(2 * T);
-    }
+    for (int k = 0; k < 2; k++) b->q[k] = A.alloc<float4>(T);
+    for (int k = 0; k < 3; k++) b->dq[k] = A.alloc<float4>(2 * T);
     b->qm = A.alloc<float4>(2 * T);
     b->delta = A.alloc<float>(T);
     b->cspeed = A.alloc<float>(T);
@@ -1571,8 +1572,7 @@ qlskum_status qlskum_batch_create(const qlskum_cloud *clouds, int n_clouds, cons
     cudaMemsetAsync(b->d_status, 0, sizeof(int), s);
     cudaMemsetAsync(b->res_old, 0, sizeof(double) * n_cases, s);
     cudaMemsetAsync(b->res_new, 0, sizeof(double) * n_cases, s);
-    cudaMemsetAsync(b->dq[0], 0, sizeof(float4) * 2 * T, s);
-    cudaMemsetAsync(b->dq[1], 0, sizeof(float4) * 2 * T, s);
+    for (int k = 0; k < 3; k++) cudaMemsetAsync(b->dq[k], 0, sizeof(float4) * 2 * T, s);
     ce = cudaStreamSynchronize(s);
     if (ce == cudaSuccess) ce = cudaGetLastError();
     if (ce != cudaSuccess) return cleanup(QLSKUM_ERR_CUDA, fmt("batch upload: %s", cudaGetErrorString(ce)));
@@ -1939,7 +1939,7 @@ struct AdjBuf {
     float4 *qm32[4] = {};
     float4 *acc32[4] = {};             // the flux kernel's weighted sums
     float *delta32 = nullptr, *cs32 = nullptr;
-    float4 *bq32 = nullptr, *bdqA32 = nullptr, *bdqB32 = nullptr, *bqm32 = nullptr;
+    float4 *bq32 = nullptr, *bdqA32 = nullptr, *bdqB32 = nullptr, *bdq0_32 = nullptr, *bqm32 = nullptr;
     float *bdelta32 = nullptr, *bcs32 = nullptr;
 };
 
@@ -2027,7 +2027,7 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
         a->delta32 = A.alloc<float>(np);
         a->cs32 = A.alloc<float>(np);
         a->bq32 = A.alloc<float4>(np);
-        for (auto *p : {&a->bdqA32, &a->bdqB32, &a->bqm32}) *p = A.alloc<float4>(2 * np);
+        for (auto *p : {&a->bdqA32, &a->bdqB32, &a->bdq0_32, &a->bqm32}) *p = A.alloc<float4>(2 * np);
         a->bdelta32 = A.alloc<float>(np);
         a->bcs32 = A.alloc<float>(np);
     }
@@ -2159,7 +2159,8 @@ void adj_iteration_forward32(qlskum_handle *h)
     for (int s = 0; s < 4; s++) {
         mixed::q_derivatives(h->L, c, a->q32[s], adj_dq32(a, s, 0), a->qm32[s], a->cs32, s == 0 ? a->delta32 : nullptr,
                              (float)h->K.cfl);
-        for (int j = 1; j <= ni; j++) mixed::q_inner(h->L, c, a->q32[s], adj_dq32(a, s, j - 1), adj_dq32(a, s, j));
+        for (int j = 1; j <= ni; j++)
+            mixed::q_inner(h->L, c, adj_dq32(a, s, 0), adj_dq32(a, s, j - 1), adj_dq32(a, s, j));
         // the last stage's q goes to the bar buffer, which the reverse zeroes before use
         float4 *q_next = s < 3 ? a->q32[s + 1] : a->bq32;
         mixed::flux_update(h->L, c, h->K, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->delta32, a->P[s], a->P[0],
@@ -2184,12 +2185,13 @@ void adj_iteration_reverse32(qlskum_handle *h, const AdjView &v)
         zero(h, a->bqm32, sizeof(float4) * 2 * np);
         adjml::flux(h->L, c, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->delta32, a->acc32[s], a->bF, a->bq32,
                     a->bdqA32, a->bqm32, a->bdelta32);
+        zero(h, a->bdq0_32, sizeof(float4) * 2 * np);
         for (int j = ni; j >= 1; j--) {
             zero(h, a->bdqB32, sizeof(float4) * 2 * np);
-            adjml::inner(h->L, c, a->q32[s], adj_dq32(a, s, j - 1), a->bdqA32, a->bq32, a->bdqB32);
+            adjml::inner(h->L, c, a->bdqA32, a->bdqB32, a->bdq0_32);
             std::swap(a->bdqA32, a->bdqB32);
         }
-        adjml::grad(h->L, c, a->q32[s], a->bdqA32, a->bqm32, a->bq32);
+        adjml::grad(h->L, c, a->q32[s], a->bdqA32, a->bdq0_32, a->bqm32, a->bq32);
         adjml::qvars(h->L, h->n, a->P[s], a->bq32, a->bP);
     }
     zero(h, a->bcs32, sizeof(float) * np);

@@ -122,11 +122,19 @@ struct State64 {
 // rounding does not move the steady state).
 struct State32 {
     float4 *q[2] = {nullptr, nullptr};
-    float4 *dq[2] = {nullptr, nullptr};      // [np][2]
+    // [np][2] each: dq[0] the stage's first-order gradient, dq[1] / dq[2]
+    // the inner steps' outputs in turn (mixed_dq_in / mixed_dq_out)
+    float4 *dq[3] = {nullptr, nullptr, nullptr};
     float4 *qm = nullptr;                    // [np][2]
     float *delta = nullptr;
     float *cspeed = nullptr;
 };
+
+// Buffers of the mixed inner loop: step j (0-based) reads dq[mixed_dq_in(j)]
+// and writes dq[mixed_dq_out(j)]; the flux kernel reads dq[mixed_dq_final(ni)].
+inline int mixed_dq_in(int j) { return j == 0 ? 0 : 1 + ((j - 1) & 1); }
+inline int mixed_dq_out(int j) { return 1 + (j & 1); }
+inline int mixed_dq_final(int ni) { return ni == 0 ? 0 : mixed_dq_out(ni - 1); }
 
 // Residual reduction scratch.
 struct Reduce {
@@ -196,9 +204,11 @@ void update(const Launch &L, const DevCloud &c, const CaseConst &K, const double
             const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, double4_32a *bF, double *buinf);
 void flux(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq, const float4 *qm, const float *delta,
           const float4 *acc, const double4_32a *bF, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta);
-void inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, const float4 *bdq_out,
-           float4 *bq, float4 *bdq_in);
-void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq, const float4 *bqm, float4 *bq);
+// reverse of one mixed inner step: bdq_in += ..., bdq0 += bdq_out (the dq0 term)
+void inner(const Launch &L, const DevCloud &c, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0);
+// reverse of the gradient and max / min; the gradient's bar is bdq + bdq0
+void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq, const float4 *bdq0,
+          const float4 *bqm, float4 *bq);
 void qvars(const Launch &L, int n, const double4_32a *P, const float4 *bq, double4_32a *bP);
 // reverse of the time step and of the wave speed it came from; bP += ...
 void delta(const Launch &L, const DevCloud &c, const double4_32a *P, const float *cs, const float *bdelta, float cfl,
@@ -238,7 +248,9 @@ namespace mixed {
 void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, float4 *q, float *cspeed);
 void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *dq, float4 *qm,
                    const float *cspeed, float *delta, float cfl);
-void q_inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, float4 *dq_out);
+// one inner step: dq_out = dq0 + 0.5 (dq_in - solve(sum w d (d.dq_in_k))), dq0 the stage's
+// first-order gradient (the reference's step, reassociated)
+void q_inner(const Launch &L, const DevCloud &c, const float4 *dq0, const float4 *dq_in, float4 *dq_out);
 // staged variants of the gradient / inner-loop kernels usable on this cloud
 // (Launch::staged = 1 .. staged_variants()); sets their shared-memory limits
 int staged_variants(const DevCloud &c);
@@ -255,7 +267,7 @@ int flux_min_blocks(int variant);
 void batch_derived(const Launch &L, const BatchView &B, int tile, const double4_32a *prim, float4 *q, float *cs);
 void batch_q_derivatives(const Launch &L, const BatchView &B, int tile, const float4 *q, float4 *dq, float4 *qm,
                          const float *cs, float *delta, float cfl);
-void batch_q_inner(const Launch &L, const BatchView &B, int tile, const float4 *q, const float4 *dq_in,
+void batch_q_inner(const Launch &L, const BatchView &B, int tile, const float4 *dq0, const float4 *dq_in,
                    float4 *dq_out);
 void batch_flux_update(const Launch &L, const BatchView &B, int variant, const float4 *q, const float4 *dq,
                        const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,

@@ -197,13 +197,37 @@ __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float
     if (delta) delta[i] = min_dt;
 }
 
-// q_variables_mod.h:120-213
+// q_variables_mod.h:120-213 in the mixed form.  The reference's sums over
+// w d (t_k - t_i), t = q - 0.5 d.dq, split by linearity into three parts:
+// sum w d (q_k - q_i), whose solve is the stage's first-order gradient dq0;
+// sum w d (0.5 d.dq_i), whose solve is 0.5 dq_i (the solve inverts exactly
+// those moments); and sum w d (d.dq_k), the only part that needs the
+// neighbours.  So dq_out = dq0 + 0.5 (dq_i - solve(sum w d (d.dq_k))): the
+// same value up to FP32 rounding, with one gather (dq_k) per edge instead
+// of two and a quarter of the arithmetic.  The FP64 form keeps the
+// reference's order of operations.
+__device__ __forceinline__ void inner_finish(const double4_32a &m, const float sdx[4], const float sdy[4],
+                                             const float4 &d0x, const float4 &d0y, const float dxi[4],
+                                             const float dyi[4], float4 *__restrict__ out)
+{
+    float ax[4], ay[4];
+    solve_grad(m, sdx, sdy, ax, ay);
+    const float o0[4] = {d0x.x, d0x.y, d0x.z, d0x.w}, o1[4] = {d0y.x, d0y.y, d0y.z, d0y.w};
+    float rx[4], ry[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        rx[r] = fmaf(0.5f, dxi[r] - ax[r], o0[r]);
+        ry[r] = fmaf(0.5f, dyi[r] - ay[r], o1[r]);
+    }
+    out[0] = mk4(rx);
+    out[1] = mk4(ry);
+}
+
 template <bool UW>
-__device__ __forceinline__ void inner_point(const DevCloud &c, int i, const float4 *__restrict__ q,
+__device__ __forceinline__ void inner_point(const DevCloud &c, int i, const float4 *__restrict__ dq0,
                                             const float4 *__restrict__ dq_in, float4 *__restrict__ dq_out)
 {
-    float qi[4], dxi[4], dyi[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
-    ld4(q[i], qi);
+    float dxi[4], dyi[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
     ld4(dq_in[2 * i], dxi);
     ld4(dq_in[2 * i + 1], dyi);
     const int nb = c.nbhs[i];
@@ -212,22 +236,17 @@ __device__ __forceinline__ void inner_point(const DevCloud &c, int i, const floa
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         const float4 g = edge_w<UW>(c, e);
-        float qk[4], dxk[4], dyk[4];
-        ld4(q[k], qk);
+        float dxk[4], dyk[4];
         ld4(dq_in[2 * k], dxk);
         ld4(dq_in[2 * k + 1], dyk);
 #pragma unroll
         for (int r = 0; r < 4; r++) {
-            float t1 = qi[r] - 0.5f * (g.x * dxi[r] + g.y * dyi[r]);
-            float t2 = qk[r] - 0.5f * (g.x * dxk[r] + g.y * dyk[r]);
-            sdx[r] += g.z * (t2 - t1);
-            sdy[r] += g.w * (t2 - t1);
+            const float u = fmaf(g.x, dxk[r], g.y * dyk[r]);
+            sdx[r] = fmaf(g.z, u, sdx[r]);
+            sdy[r] = fmaf(g.w, u, sdy[r]);
         }
     }
-    float dx[4], dy[4];
-    solve_grad(c.gcoef[i], sdx, sdy, dx, dy);
-    dq_out[2 * i] = mk4(dx);
-    dq_out[2 * i + 1] = mk4(dy);
+    inner_finish(c.gcoef[i], sdx, sdy, dq0[2 * i], dq0[2 * i + 1], dxi, dyi, dq_out + 2 * i);
 }
 
 // ------------------------------------------------ staged neighbour gathers
@@ -293,14 +312,14 @@ template <int B, bool UW> __device__ __forceinline__ float4 staged_geo(const voi
     return static_cast<const float4 *>(sgeo)[j * B + t];
 }
 
-// q_variables_mod.h:120-213 with staged gathers (q, dq_x, dq_y of each neighbour).
+// The mixed inner step (inner_point) with staged gathers (dq_x, dq_y of each neighbour).
 template <int B, int D, bool UW>
-__global__ void __launch_bounds__(B) k_q_inner_st(DevCloud c, const float4 *__restrict__ q,
+__global__ void __launch_bounds__(B) k_q_inner_st(DevCloud c, const float4 *__restrict__ dq0,
                                                   const float4 *__restrict__ dq_in, float4 *__restrict__ dq_out)
 {
     extern __shared__ float4 smem4[];
     float4 *ring = smem4;
-    int *snbr = reinterpret_cast<int *>(ring + (D + 1) * 3 * B);
+    int *snbr = reinterpret_cast<int *>(ring + (D + 1) * 2 * B);
     void *sgeo = snbr + c.max_nb * B;
     const int t = threadIdx.x;
     const int i = blockIdx.x * B + t;
@@ -308,17 +327,15 @@ __global__ void __launch_bounds__(B) k_q_inner_st(DevCloud c, const float4 *__re
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
     stage_edges<B, UW>(c, base, nb, t, snbr, sgeo);
-    float qi[4], dxi[4], dyi[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
-    ld4(q[i], qi);
+    float dxi[4], dyi[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
     ld4(dq_in[2 * i], dxi);
     ld4(dq_in[2 * i + 1], dyi);
     cp_wait<0>();
     auto issue = [&](int j) {
         const int k = snbr[j * B + t];
-        float4 *slot = ring + (j % (D + 1)) * 3 * B + t;
-        cp_async16(slot, q + k);
-        cp_async16(slot + B, dq_in + 2 * k);
-        cp_async16(slot + 2 * B, dq_in + 2 * k + 1);
+        float4 *slot = ring + (j % (D + 1)) * 2 * B + t;
+        cp_async16(slot, dq_in + 2 * k);
+        cp_async16(slot + B, dq_in + 2 * k + 1);
     };
 #pragma unroll
     for (int j = 0; j < D; j++) {
@@ -329,24 +346,19 @@ __global__ void __launch_bounds__(B) k_q_inner_st(DevCloud c, const float4 *__re
         if (j + D < nb) issue(j + D);
         cp_commit();
         cp_wait<D>();
-        const float4 *slot = ring + (j % (D + 1)) * 3 * B + t;
-        float qk[4], dxk[4], dyk[4];
-        ld4(slot[0], qk);
-        ld4(slot[B], dxk);
-        ld4(slot[2 * B], dyk);
+        const float4 *slot = ring + (j % (D + 1)) * 2 * B + t;
+        float dxk[4], dyk[4];
+        ld4(slot[0], dxk);
+        ld4(slot[B], dyk);
         const float4 g = staged_geo<B, UW>(sgeo, j, t);
 #pragma unroll
         for (int r = 0; r < 4; r++) {
-            float t1 = qi[r] - 0.5f * (g.x * dxi[r] + g.y * dyi[r]);
-            float t2 = qk[r] - 0.5f * (g.x * dxk[r] + g.y * dyk[r]);
-            sdx[r] += g.z * (t2 - t1);
-            sdy[r] += g.w * (t2 - t1);
+            const float u = fmaf(g.x, dxk[r], g.y * dyk[r]);
+            sdx[r] = fmaf(g.z, u, sdx[r]);
+            sdy[r] = fmaf(g.w, u, sdy[r]);
         }
     }
-    float dx[4], dy[4];
-    solve_grad(c.gcoef[i], sdx, sdy, dx, dy);
-    dq_out[2 * i] = mk4(dx);
-    dq_out[2 * i + 1] = mk4(dy);
+    inner_finish(c.gcoef[i], sdx, sdy, dq0[2 * i], dq0[2 * i + 1], dxi, dyi, dq_out + 2 * i);
 }
 
 // q_variables_mod.h:36-118 with staged gathers (q and, in the first stage,
@@ -681,11 +693,11 @@ __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4
 }
 
 template <bool UW>
-__global__ void k_q_inner(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ dq_in,
+__global__ void k_q_inner(DevCloud c, const float4 *__restrict__ dq0, const float4 *__restrict__ dq_in,
                           float4 *__restrict__ dq_out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < c.n) inner_point<UW>(c, i, q, dq_in, dq_out);
+    if (i < c.n) inner_point<UW>(c, i, dq0, dq_in, dq_out);
 }
 
 template <int BLOCK, int MINB, bool UW>
@@ -779,14 +791,14 @@ template <int TILE, bool UW>
 __global__ void __launch_bounds__(TILE) kb_q_inner(const DevCloud *__restrict__ clouds,
                                                    const BatchCase *__restrict__ cases,
                                                    const BatchTile *__restrict__ tiles, int ntiles,
-                                                   const float4 *__restrict__ q, const float4 *__restrict__ dq_in,
+                                                   const float4 *__restrict__ dq0, const float4 *__restrict__ dq_in,
                                                    float4 *__restrict__ dq_out)
 {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const BatchTile T = tiles[t];
         const BatchCase &C = cases[T.cas];
         const int i = T.first + threadIdx.x;
-        if (i < C.n) inner_point<UW>(clouds[C.cloud], i, q + C.off, dq_in + 2 * C.off, dq_out + 2 * C.off);
+        if (i < C.n) inner_point<UW>(clouds[C.cloud], i, dq0 + 2 * C.off, dq_in + 2 * C.off, dq_out + 2 * C.off);
     }
 }
 
@@ -897,10 +909,10 @@ int staged_variants(const DevCloud &c)
         bool ok = true;
         QLSKUM_STAGED_SWITCH(v,
             if (c.unit_w) {
-                ok = allow_smem(k_q_inner_st<B_, D_, true>, staged_bytes(B_, D_, 3, c.max_nb, true)) &&
+                ok = allow_smem(k_q_inner_st<B_, D_, true>, staged_bytes(B_, D_, 2, c.max_nb, true)) &&
                      allow_smem(k_q_derivatives_st<B_, D_, true>, staged_bytes(B_, D_, 2, c.max_nb, true));
             } else {
-                ok = allow_smem(k_q_inner_st<B_, D_, false>, staged_bytes(B_, D_, 3, c.max_nb, false)) &&
+                ok = allow_smem(k_q_inner_st<B_, D_, false>, staged_bytes(B_, D_, 2, c.max_nb, false)) &&
                      allow_smem(k_q_derivatives_st<B_, D_, false>, staged_bytes(B_, D_, 2, c.max_nb, false));
             })
         if (!ok) break;
@@ -929,20 +941,20 @@ void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *
     QLSKUM_LAUNCHED(L);
 }
 
-void q_inner(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq_in, float4 *dq_out)
+void q_inner(const Launch &L, const DevCloud &c, const float4 *dq0, const float4 *dq_in, float4 *dq_out)
 {
     if (L.staged > 0) {
         QLSKUM_STAGED_SWITCH(L.staged,
             if (c.unit_w)
-                k_q_inner_st<B_, D_, true><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 3, c.max_nb, true),
-                                             L.stream>>>(c, q, dq_in, dq_out);
+                k_q_inner_st<B_, D_, true><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 2, c.max_nb, true),
+                                             L.stream>>>(c, dq0, dq_in, dq_out);
             else
-                k_q_inner_st<B_, D_, false><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 3, c.max_nb, false),
-                                              L.stream>>>(c, q, dq_in, dq_out))
+                k_q_inner_st<B_, D_, false><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 2, c.max_nb, false),
+                                              L.stream>>>(c, dq0, dq_in, dq_out))
     } else if (c.unit_w) {
-        k_q_inner<true><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq_in, dq_out);
+        k_q_inner<true><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, dq0, dq_in, dq_out);
     } else {
-        k_q_inner<false><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq_in, dq_out);
+        k_q_inner<false><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, dq0, dq_in, dq_out);
     }
     QLSKUM_LAUNCHED(L);
 }
@@ -1046,17 +1058,17 @@ void batch_q_derivatives(const Launch &L, const BatchView &B, int tile, const fl
     QLSKUM_LAUNCHED(L);
 }
 
-void batch_q_inner(const Launch &L, const BatchView &B, int tile, const float4 *q, const float4 *dq_in,
+void batch_q_inner(const Launch &L, const BatchView &B, int tile, const float4 *dq0, const float4 *dq_in,
                    float4 *dq_out)
 {
     QLSKUM_TILE_SWITCH(tile, {
         const int ti = tile_index(T_);
         if (B.unit_w) {
             const int g = persistent_grid(kb_q_inner<T_, true>, T_, B.ntiles[ti]);
-            kb_q_inner<T_, true><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq_in, dq_out);
+            kb_q_inner<T_, true><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], dq0, dq_in, dq_out);
         } else {
             const int g = persistent_grid(kb_q_inner<T_, false>, T_, B.ntiles[ti]);
-            kb_q_inner<T_, false><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq_in,
+            kb_q_inner<T_, false><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], dq0, dq_in,
                                                           dq_out);
         }
     })
