@@ -602,16 +602,53 @@ __device__ __forceinline__ void x_flux_vjp(int f, const Kin<float> &k, float s1,
 // half-range fluxes it enters, weighted by the folded solve weights (bs: the
 // bar of the owner's weighted sum, signed + for the neighbour end, - for the
 // owner's), back to the end's q, dq and max / min (added to bq ... bmn).
+// The forward quantities are computed once and reused by the reverse: the
+// limiter's dn = -g/2 and dp, the state's beta and 1 / (2 beta) (which is
+// also the moments' p / rho), sqrt(beta) and the moments' exp(-S^2) (taken
+// back from B = exp(-S^2) / (2 sqrt(pi beta))), so the reverse has one
+// division per active limiter component and no other division, exp or log.
+// The same derivatives as the generic reverse-mode functions
+// (qtilde_to_prim_vjp, kin_vjp, edge_end_vjp) up to rounding.
 __device__ __forceinline__ void end_vjp(const DevCloud &c, long long e, int f, float nx, float ny, float delx,
                                         float dely, float2 w, unsigned dir, const float bs[4], const float q[4],
                                         const float dx[4], const float dy[4], const float mx[4], const float mn[4],
                                         float e2, float bq[4], float bdx[4], float bdy[4], float bmx[4], float bmn[4])
 {
-    float t[4], P[4];
-    qtilde_f(delx, dely, q, dx, dy, mx, mn, e2, t);
-    qtilde_to_prim<float>(t, P[1], P[2], P[0], P[3]);
+    // reconstruction q~ = q + phi dn, dn = -(delx dqx + dely dqy) / 2 (limiters_mod.h:64-104)
+    float dn[4], dp[4], phi[4], t[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        dn[r] = -0.5f * fmaf(delx, dx[r], dely * dy[r]);
+        dp[r] = ((dn[r] > 0.f) ? mx[r] : mn[r]) - q[r];
+        const float base = fmaf(dp[r], dp[r], e2);
+        const float num = fmaf(2.0f * dn[r], dp[r], base);
+        const float den = fmaf(dn[r], dp[r], fmaf(2.0f * dn[r], dn[r], base));
+        const float ph = fminf(__fdividef(num, den), 1.0f);
+        phi[r] = fabsf(dn[r]) <= 10e-6f ? 1.0f : ph;
+        t[r] = fmaf(phi[r], dn[r], q[r]);
+    }
+    // q~ -> (rho, u1, u2), beta, tm = 1 / (2 beta) = p / rho (q_variables_mod.h:230-253)
+    const float beta = -0.5f * t[3];
+    const float tm = __fdividef(0.5f, beta);
+    const float u1 = t[1] * tm, u2 = t[2] * tm;
+    const float uq = fmaf(u1, u1, u2 * u2);
+    const float rho = __expf(fmaf(beta, uq, t[0]) - 2.5f * __logf(beta));
+    // half-range moments in the (t, n) frame (split_fluxes_mod.h:14-26)
+    const float rsb = rsqrtf(beta), sb = beta * rsb;
     Kin<float> k;
-    kin_prep<float>(nx, ny, P[1], P[2], P[0], P[3], k);
+    k.ut = u1 * ny - u2 * nx;
+    k.un = u1 * nx + u2 * ny;
+    const float S1 = k.ut * sb, S2 = k.un * sb;
+    const float e1 = __expf(-S1 * S1), e2x = __expf(-S2 * S2);
+    const float rpi = 0.5641895835477563f;  // 1 / sqrt(pi)
+    k.B1 = 0.5f * e1 * rsb * rpi;
+    k.B2 = 0.5f * e2x * rsb * rpi;
+    k.E1 = erf_e<float>(S1, e1);
+    k.E2 = erf_e<float>(S2, e2x);
+    k.pbr = tm;
+    k.usq = fmaf(k.ut, k.ut, k.un * k.un);
+    k.rho = rho;
+    // the fluxes' reverse
     KinBarT<float> kb;
     float bG[4];
 #pragma unroll
@@ -634,12 +671,44 @@ __device__ __forceinline__ void end_vjp(const DevCloud &c, long long e, int f, f
             adj::flux_y_vjp<float>(k, -1.0f, bG, kb);
         }
     }
-    float bP[4] = {0, 0, 0, 0}, bn0 = 0.f, bn1 = 0.f;
-    adj::kin_vjp<float>(nx, ny, P, k, kb, bP, bn0, bn1);
-    float bt[4] = {0, 0, 0, 0};
-    adj::qtilde_to_prim_vjp<float>(t, bP, bt);
-    float bdelx = 0.f, bdely = 0.f;
-    adj::edge_end_vjp<float>(delx, dely, q, dx, dy, mx, mn, e2, bt, bq, bdx, bdy, bmx, bmn, bdelx, bdely);
+    // moments' reverse: (2 / sqrt(pi)) exp(-S^2) = 4 sb B
+    float but = fmaf(2.0f * k.ut, kb.usq, kb.ut), bun = fmaf(2.0f * k.un, kb.usq, kb.un);
+    const float bS1 = k.B1 * (4.0f * sb * kb.E1 - 2.0f * S1 * kb.B1);
+    const float bS2 = k.B2 * (4.0f * sb * kb.E2 - 2.0f * S2 * kb.B2);
+    but = fmaf(bS1, sb, but);
+    bun = fmaf(bS2, sb, bun);
+    float bbeta = (bS1 * k.ut + bS2 * k.un) * 0.5f * rsb - (kb.B1 * k.B1 + kb.B2 * k.B2) * tm;
+    float btm = kb.pbr;
+    float bu1 = but * ny + bun * nx, bu2 = bun * ny - but * nx;
+    // state's reverse: rho = exp(t0 + beta uq - 2.5 log beta), u = (t1, t2) tm, tm = 1 / (2 beta)
+    const float bT = kb.rho * rho;
+    bbeta = fmaf(bT, uq - 5.0f * tm, bbeta);
+    bu1 = fmaf(2.0f * bT * beta, u1, bu1);
+    bu2 = fmaf(2.0f * bT * beta, u2, bu2);
+    btm = fmaf(bu1, t[1], fmaf(bu2, t[2], btm));
+    bbeta = fmaf(-2.0f * tm * tm, btm, bbeta);
+    const float bt[4] = {bT, bu1 * tm, bu2 * tm, -0.5f * bbeta};
+    // reconstruction's reverse (num / den with the common factor dn cancelled)
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        bq[r] += bt[r];
+        float bdn = phi[r] * bt[r];
+        if (phi[r] < 1.0f) {
+            const float bphi = dn[r] * bt[r];
+            const float base = fmaf(dp[r], dp[r], e2);
+            const float den = fmaf(dn[r], dp[r], fmaf(2.0f * dn[r], dn[r], base));
+            const float rden = __fdividef(1.0f, den);
+            const float bnum = bphi * rden, bden = -bphi * phi[r] * rden;
+            bdn += bnum * 2.0f * dp[r] + bden * fmaf(4.0f, dn[r], dp[r]);
+            const float bdp = bnum * 2.0f * (dp[r] + dn[r]) + bden * fmaf(2.0f, dp[r], dn[r]);
+            bq[r] -= bdp;
+            if (dn[r] > 0.f) bmx[r] += bdp;
+            else bmn[r] += bdp;
+        }
+        const float bg = -0.5f * bdn;
+        bdx[r] = fmaf(bg, delx, bdx[r]);
+        bdy[r] = fmaf(bg, dely, bdy[r]);
+    }
 }
 
 template <bool UW> __device__ __forceinline__ float2 edge_del(const DevCloud &c, long long e)
@@ -658,7 +727,7 @@ template <bool UW> __device__ __forceinline__ float2 edge_del(const DevCloud &c,
 // reductions) run as two kernels, each holding one end's state.  bF (FP64,
 // from adjk::k_update) in.
 template <bool UW>
-__global__ void __launch_bounds__(128) k_flux_own(DevCloud c, const float4 *__restrict__ q,
+__global__ void __launch_bounds__(128, 4) k_flux_own(DevCloud c, const float4 *__restrict__ q,
                                                    const float4 *__restrict__ dq, const float4 *__restrict__ qm,
                                                    const float *__restrict__ delta, const float4 *__restrict__ acc,
                                                    const double4_32a *__restrict__ bF, float4 *__restrict__ bq,

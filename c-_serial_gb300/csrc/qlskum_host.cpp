@@ -2372,12 +2372,12 @@ qlskum_status adj_geometry(qlskum_handle *h, int which, const double4_32a *prim_
     }
     // the objective's geometry: H = sum cp nx ds, V = sum cp ny ds with
     // ds = (|x_m - x_l| + |x_r - x_m|) / 2 (compute_force_coeffs_mod.h:37-59);
-    // the stagnation-pressure loss has none
+    // the stagnation-pressure loss has none, nor has a residual VJP (which < 0)
     const double cp_scale = 0.5 * h->K.rho_inf * h->K.mach * h->K.mach;
     const double th = h->K.theta;
     const double bH = which == 0 ? -std::sin(th) : std::cos(th);
     const double bV = which == 0 ? std::cos(th) : std::sin(th);
-    for (int m = 0; m < (which == QLSKUM_OBJECTIVE_J ? 0 : h->shape_points); m++) {
+    for (int m = 0; m < ((which < 0 || which == QLSKUM_OBJECTIVE_J) ? 0 : h->shape_points); m++) {
         const int l = h->hleft[m] - 1, r = h->hright[m] - 1;
         const double cp = -(prim[h->perm[m]].w - h->K.pr_inf) / cp_scale;
         const double d1x = X[m] - X[l], d1y = Y[m] - Y[l], d2x = X[r] - X[m], d2y = Y[r] - Y[m];
@@ -2480,6 +2480,37 @@ qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const do
     adjl::delta(h->L, v, a->P[0], a->bdelta, h->K.cfl, a->bc, a->bP);
     if ((st = check_launch(h, "residual_vjp"))) return st;
     return download_points(h, a->bP, bar_prim);
+}
+
+qlskum_status qlskum_residual_vjp_full(qlskum_handle *h, const double *prim, const double *bar_flux_res,
+                                      double *bar_prim, double *bar_params, double *bar_wall_disp)
+{
+    NEED(h);
+    if (!prim || !bar_flux_res || !bar_prim) return fail(h, QLSKUM_ERR_INVALID, "null argument");
+    if (bar_wall_disp && h->prm.power != 0.0)
+        return fail(h, QLSKUM_ERR_UNSUPPORTED, "wall-displacement gradients need unit least-squares weights (power 0)");
+    const bool geo = bar_wall_disp != nullptr;
+    qlskum_status st = adj_alloc(h, geo, true, false);
+    if (st) return st;
+    AdjBuf *a = h->adj;
+    if ((st = upload_points(h, prim, a->P[0], 1.0))) return st;
+    if ((st = upload_points(h, bar_flux_res, a->bF, 0.0))) return st;
+    fp64::func_delta(h->L, h->dc, a->P[0], a->delta, h->K.cfl);
+    adj_stage_forward(h, 0);
+    adj_zero_geometry(h);
+    const AdjView v = adj_view(h, geo);
+    zero(h, a->bP, sizeof(double4_32a) * h->np);
+    zero(h, a->bdelta, sizeof(double) * h->np);
+    adj_stage_reverse(h, 0, v);
+    zero(h, a->bc, sizeof(double) * h->np);
+    adjl::delta(h->L, v, a->P[0], a->bdelta, h->K.cfl, a->bc, a->bP);
+    if ((st = check_launch(h, "residual_vjp_full"))) return st;
+    if ((st = download_points(h, a->bP, bar_prim))) return st;
+    // R(prim) is the flux residual of one stage and its time step: neither
+    // reads the free stream, which enters through the stage update
+    if (bar_params) bar_params[0] = bar_params[1] = 0.0;
+    if (geo) return adj_geometry(h, -1, a->P[0], bar_wall_disp);
+    return QLSKUM_OK;
 }
 
 qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters, const double *prim0, double *J,

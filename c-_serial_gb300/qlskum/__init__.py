@@ -115,6 +115,7 @@ def load(build_if_needed: bool = True):
         "qlskum_get_kernel_timing": (i, [H, i, dp, C.POINTER(C.c_longlong)]),
         "qlskum_residual_forward": (i, [H, dp, dp]),
         "qlskum_residual_vjp": (i, [H, dp, dp, dp]),
+        "qlskum_residual_vjp_full": (i, [H, dp, dp, dp, dp, dp]),
         "qlskum_adjoint_gradient": (i, [H, i, i, dp, dp, dp, dp, dp, dp]),
         "qlskum_adjoint_fixed_point": (i, [H, i, i, dp, dp, dp, dp, dp]),
         "qlskum_set_adjoint_stride": (i, [H, i]),
@@ -372,13 +373,20 @@ class Solver:
         self._ck(self._L.qlskum_residual_forward(self._h, _dp(a), _dp(out)))
         return out
 
-    def residual_vjp(self, prim, bar_res) -> np.ndarray:
-        """(dR/dprim)^T bar_res at prim."""
+    def residual_vjp(self, prim, bar_res, wall=False):
+        """(dR/dprim)^T bar_res at prim; with wall=True also
+        (bar_params [d/dMach, d/dAoA] (zero: R reads no free stream),
+        bar_wall [shape_points] normal displacements) as a tuple."""
         a = self._state(prim, "prim")
         b = self._state(bar_res, "bar_res")
         out = np.empty((self.n, 4))
-        self._ck(self._L.qlskum_residual_vjp(self._h, _dp(a), _dp(b), _dp(out)))
-        return out
+        if not wall:
+            self._ck(self._L.qlskum_residual_vjp(self._h, _dp(a), _dp(b), _dp(out)))
+            return out
+        bp = np.empty(2)
+        bw = np.empty(self.shape_points)
+        self._ck(self._L.qlskum_residual_vjp_full(self._h, _dp(a), _dp(b), _dp(out), _dp(bp), _dp(bw)))
+        return out, bp, bw
 
     def _adjoint_out(self, objective, wall):
         obj = {"cl": OBJECTIVE_CL, "cd": OBJECTIVE_CD, "j": OBJECTIVE_J}.get(objective, objective)

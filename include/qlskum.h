@@ -297,6 +297,17 @@ qlskum_status qlskum_residual_forward(qlskum_handle *h, const double *prim, doub
  * of qlskum_residual_forward, for an autograd.Function's backward. */
 qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const double *bar_flux_res,
                                   double *bar_prim);
+/* The same VJP with the bars of the case parameters and of the geometry:
+ * bar_params (double [2] or NULL) = d/dMach, d/dAoA of bar_flux_res . R,
+ * which are zero (R reads no free-stream quantity; Mach and AoA enter the
+ * iteration through the stage update's far-field state), and bar_wall_disp
+ * (double [shape_points] or NULL) = its derivative w.r.t. the normal
+ * displacement of each shape point (edge vectors, least-squares moments,
+ * lengths and normals pulled back to the coordinates; the sub-stencil split
+ * and min_dist held; unit weights, params.power 0, else
+ * QLSKUM_ERR_UNSUPPORTED). */
+qlskum_status qlskum_residual_vjp_full(qlskum_handle *h, const double *prim, const double *bar_flux_res,
+                                      double *bar_prim, double *bar_params, double *bar_wall_disp);
 /* Runs `iters` iterations (as qlskum_q_lskum would; the handle holds the
  * final state afterwards) from prim0 (double [n][4]) or, when prim0 is NULL,
  * from the free stream, keeping each iteration's state, then sweeps the
