@@ -15,6 +15,7 @@
 // least-squares moments) for the wall-displacement gradient, which the host
 // finishes (qlskum_host.cpp).
 #include "qlskum_adjoint.cuh"
+#include "qlskum_conv.cuh"
 
 namespace qlskum {
 namespace adjk {
@@ -725,12 +726,13 @@ template <bool UW> __device__ __forceinline__ float2 edge_del(const DevCloud &c,
 // bars kept in registers, and the bar of delta) and the neighbour ends
 // (k_flux_nbr: the neighbour's data gathered, bars scattered with vector
 // reductions) run as two kernels, each holding one end's state.  bF (FP64,
-// from adjk::k_update) in.
+// from adjk::k_update) in; k_flux_own stores the stage's bars of q, dq and qm
+// (every point's, so they need no zeroing) and k_flux_nbr adds to them.
 template <bool UW>
 __global__ void __launch_bounds__(128, 4) k_flux_own(DevCloud c, const float4 *__restrict__ q,
                                                    const float4 *__restrict__ dq, const float4 *__restrict__ qm,
                                                    const float *__restrict__ delta, const float4 *__restrict__ acc,
-                                                   const double4_32a *__restrict__ bF, float4 *__restrict__ bq,
+                                                   const float4 *__restrict__ bF, float4 *__restrict__ bq,
                                                    float4 *__restrict__ bdq, float4 *__restrict__ bqm,
                                                    float *__restrict__ bdelta)
 {
@@ -738,7 +740,7 @@ __global__ void __launch_bounds__(128, 4) k_flux_own(DevCloud c, const float4 *_
     if (i >= c.n) return;
     const int f = c.flag[i];
     const double2 nn = c.nrm[i];
-    const float nx = (float)nn.x, ny = (float)nn.y;
+    const float nx = d2f(nn.x), ny = d2f(nn.y);
     float qi[4], dxi[4], dyi[4], mxi[4], mni[4];
     ldf4(q[i], qi);
     ldf4(dq[2 * i], dxi);
@@ -746,11 +748,11 @@ __global__ void __launch_bounds__(128, 4) k_flux_own(DevCloud c, const float4 *_
     ldf4(qm[2 * i], mxi);
     ldf4(qm[2 * i + 1], mni);
     const float e2i = c.eps2_32[i];
-    const double4_32a bFi = bF[i];
+    const float4 bFi = bF[i];
     const float4 ac = acc[i];
     const float dl = delta[i];
-    bdelta[i] += (float)(bFi.x * ac.x + bFi.y * ac.y + bFi.z * ac.z + bFi.w * ac.w);
-    const float bs[4] = {(float)(-dl * bFi.x), (float)(-dl * bFi.y), (float)(-dl * bFi.z), (float)(-dl * bFi.w)};
+    bdelta[i] += bFi.x * ac.x + bFi.y * ac.y + bFi.z * ac.z + bFi.w * ac.w;
+    const float bs[4] = {-dl * bFi.x, -dl * bFi.y, -dl * bFi.z, -dl * bFi.w};
     float bqi[4] = {0, 0, 0, 0}, bdxi[4] = {0, 0, 0, 0}, bdyi[4] = {0, 0, 0, 0}, bmxi[4] = {0, 0, 0, 0},
           bmni[4] = {0, 0, 0, 0};
     const int nb = c.nbhs[i];
@@ -761,17 +763,18 @@ __global__ void __launch_bounds__(128, 4) k_flux_own(DevCloud c, const float4 *_
         end_vjp(c, e, f, nx, ny, d.x, d.y, c.e_w32[e], c.e_dir[e], bs, qi, dxi, dyi, mxi, mni, e2i, bqi, bdxi, bdyi,
                 bmxi, bmni);
     }
-    atomic_add4(bq + i, bqi);
-    atomic_add4(bdq + 2 * i, bdxi);
-    atomic_add4(bdq + 2 * i + 1, bdyi);
-    atomic_add4(bqm + 2 * i, bmxi);
-    atomic_add4(bqm + 2 * i + 1, bmni);
+    // the first writer of this stage's bars: plain stores (k_flux_nbr adds after)
+    bq[i] = mk4(bqi);
+    bdq[2 * i] = mk4(bdxi);
+    bdq[2 * i + 1] = mk4(bdyi);
+    bqm[2 * i] = mk4(bmxi);
+    bqm[2 * i + 1] = mk4(bmni);
 }
 
 template <bool UW>
 __global__ void __launch_bounds__(128) k_flux_nbr(DevCloud c, const float4 *__restrict__ q,
                                                    const float4 *__restrict__ dq, const float4 *__restrict__ qm,
-                                                   const float *__restrict__ delta, const double4_32a *__restrict__ bF,
+                                                   const float *__restrict__ delta, const float4 *__restrict__ bF,
                                                    float4 *__restrict__ bq, float4 *__restrict__ bdq,
                                                    float4 *__restrict__ bqm)
 {
@@ -779,10 +782,10 @@ __global__ void __launch_bounds__(128) k_flux_nbr(DevCloud c, const float4 *__re
     if (i >= c.n) return;
     const int f = c.flag[i];
     const double2 nn = c.nrm[i];
-    const float nx = (float)nn.x, ny = (float)nn.y;
-    const double4_32a bFi = bF[i];
+    const float nx = d2f(nn.x), ny = d2f(nn.y);
+    const float4 bFi = bF[i];
     const float dl = delta[i];
-    const float bs[4] = {(float)(dl * bFi.x), (float)(dl * bFi.y), (float)(dl * bFi.z), (float)(dl * bFi.w)};
+    const float bs[4] = {dl * bFi.x, dl * bFi.y, dl * bFi.z, dl * bFi.w};
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
     for (int j = 0; j < nb; j++) {
@@ -812,7 +815,7 @@ __global__ void __launch_bounds__(128) k_flux_nbr(DevCloud c, const float4 *__re
 __device__ __forceinline__ void solve_vjp(const double4_32a &m, const float bx[4], const float by[4], float bX[4],
                                           float bY[4])
 {
-    const float a = (float)m.x, b = (float)m.y, cc = (float)m.z;
+    const float a = d2f(m.x), b = d2f(m.y), cc = d2f(m.z);
 #pragma unroll
     for (int r = 0; r < 4; r++) {
         bX[r] = bx[r] * a - by[r] * b;
@@ -836,16 +839,18 @@ template <bool UW> __device__ __forceinline__ float4 edge_w(const DevCloud &c, l
 // and S to the neighbours' dq_in.
 template <bool UW>
 __global__ void k_inner(DevCloud c, const float4 *__restrict__ bdq_out, float4 *__restrict__ bdq_in,
-                        float4 *__restrict__ bdq0)
+                        float4 *__restrict__ bdq0, int first)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     float bx[4], by[4], bax[4], bay[4], bsx[4], bsy[4];
     ldf4(bdq_out[2 * i], bx);
     ldf4(bdq_out[2 * i + 1], by);
-    float a0[4], a1[4];
-    ldf4(bdq0[2 * i], a0);
-    ldf4(bdq0[2 * i + 1], a1);
+    float a0[4] = {0, 0, 0, 0}, a1[4] = {0, 0, 0, 0};
+    if (!first) {
+        ldf4(bdq0[2 * i], a0);
+        ldf4(bdq0[2 * i + 1], a1);
+    }
 #pragma unroll
     for (int r = 0; r < 4; r++) {
         a0[r] += bx[r];
@@ -880,7 +885,7 @@ __global__ void k_inner(DevCloud c, const float4 *__restrict__ bdq_out, float4 *
 
 // Reverse of the mixed gradient and neighbour max / min (q_variables_mod.h:36-118).
 // The bar of the stage's first-order gradient is bdq + bdq0 (the inner
-// steps' direct part).
+// steps' direct part; bdq0 NULL without inner steps).
 template <bool UW>
 __global__ void k_grad(DevCloud c, const float4 *__restrict__ q, const float4 *__restrict__ bdq,
                        const float4 *__restrict__ bdq0, const float4 *__restrict__ bqm, float4 *__restrict__ bq)
@@ -890,12 +895,14 @@ __global__ void k_grad(DevCloud c, const float4 *__restrict__ q, const float4 *_
     float bx[4], by[4], bsdx[4], bsdy[4], bmax[4], bmin[4], qi[4], b0x[4], b0y[4];
     ldf4(bdq[2 * i], bx);
     ldf4(bdq[2 * i + 1], by);
-    ldf4(bdq0[2 * i], b0x);
-    ldf4(bdq0[2 * i + 1], b0y);
+    if (bdq0) {
+        ldf4(bdq0[2 * i], b0x);
+        ldf4(bdq0[2 * i + 1], b0y);
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
-        bx[r] += b0x[r];
-        by[r] += b0y[r];
+        for (int r = 0; r < 4; r++) {
+            bx[r] += b0x[r];
+            by[r] += b0y[r];
+        }
     }
     ldf4(bqm[2 * i], bmax);
     ldf4(bqm[2 * i + 1], bmin);
@@ -943,15 +950,15 @@ __global__ void k_q(int n, const double4_32a *__restrict__ P, const float4 *__re
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double4_32a p = P[i];
-    const float pf[4] = {(float)p.x, (float)p.y, (float)p.z, (float)p.w};
+    const float pf[4] = {d2f(p.x), d2f(p.y), d2f(p.z), d2f(p.w)};
     float b[4], g[4] = {0, 0, 0, 0};
     ldf4(bq[i], b);
     adj::prim_to_q_vjp<float>(pf, b, g);
     double4_32a acc = bP[i];
-    acc.x += g[0];
-    acc.y += g[1];
-    acc.z += g[2];
-    acc.w += g[3];
+    acc.x += f2d(g[0]);
+    acc.y += f2d(g[1]);
+    acc.z += f2d(g[2]);
+    acc.w += f2d(g[3]);
     bP[i] = acc;
 }
 
@@ -989,14 +996,14 @@ __global__ void k_wave(int n, const double4_32a *__restrict__ P, const float *__
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || bc[i] == 0.f) return;
     const double4_32a p = P[i];
-    const float pf[4] = {(float)p.x, (float)p.y, (float)p.z, (float)p.w};
+    const float pf[4] = {d2f(p.x), d2f(p.y), d2f(p.z), d2f(p.w)};
     float g[4] = {0, 0, 0, 0};
     adj::wave_speed_vjp<float>(pf, bc[i], g);
     double4_32a acc = bP[i];
-    acc.x += g[0];
-    acc.y += g[1];
-    acc.z += g[2];
-    acc.w += g[3];
+    acc.x += f2d(g[0]);
+    acc.y += f2d(g[1]);
+    acc.z += f2d(g[2]);
+    acc.w += f2d(g[3]);
     bP[i] = acc;
 }
 
@@ -1007,7 +1014,7 @@ __global__ void k_wave(int n, const double4_32a *__restrict__ P, const float *__
 // velocity bars (one FP64 atomic per warp).
 __global__ void k_update(DevCloud c, CaseConst K, const double4_32a *__restrict__ Pin,
                          const double4_32a *__restrict__ Pold, const double4_32a *__restrict__ Pout, int rk,
-                         double4_32a *__restrict__ bP, double4_32a *__restrict__ bPold, double4_32a *__restrict__ bF,
+                         double4_32a *__restrict__ bP, double4_32a *__restrict__ bPold, float4 *__restrict__ bF,
                          double *__restrict__ buinf)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1016,25 +1023,25 @@ __global__ void k_update(DevCloud c, CaseConst K, const double4_32a *__restrict_
         const int f = c.flag[i];
         const double2 nn = c.nrm[i];
         const double4_32a a = Pin[i], b = Pold[i], o = Pout[i], g = bP[i];
-        const float pin[4] = {(float)a.x, (float)a.y, (float)a.z, (float)a.w};
-        const float pold[4] = {(float)b.x, (float)b.y, (float)b.z, (float)b.w};
-        const float pout[4] = {(float)o.x, (float)o.y, (float)o.z, (float)o.w};
-        const float bout[4] = {(float)g.x, (float)g.y, (float)g.z, (float)g.w};
+        const float pin[4] = {d2f(a.x), d2f(a.y), d2f(a.z), d2f(a.w)};
+        const float pold[4] = {d2f(b.x), d2f(b.y), d2f(b.z), d2f(b.w)};
+        const float pout[4] = {d2f(o.x), d2f(o.y), d2f(o.z), d2f(o.w)};
+        const float bout[4] = {d2f(g.x), d2f(g.y), d2f(g.z), d2f(g.w)};
         float bin[4] = {0, 0, 0, 0}, bo[4] = {0, 0, 0, 0}, bf[4] = {0, 0, 0, 0}, bnx = 0.f, bny = 0.f;
-        adj::stage_update_vjp<float>(K, f, (float)nn.x, (float)nn.y, pin, pold, pout, rk, bout, bin, bo, bf, bnx, bny,
+        adj::stage_update_vjp<float>(K, f, d2f(nn.x), d2f(nn.y), pin, pold, pout, rk, bout, bin, bo, bf, bnx, bny,
                                      bu1, bu2);
-        bP[i] = make_double4_32a(bin[0], bin[1], bin[2], bin[3]);
-        bF[i] = make_double4_32a(bf[0], bf[1], bf[2], bf[3]);
+        bP[i] = make_double4_32a(f2d(bin[0]), f2d(bin[1]), f2d(bin[2]), f2d(bin[3]));
+        bF[i] = make_float4(bf[0], bf[1], bf[2], bf[3]);
         if (rk == 3) {
             double4_32a acc = bPold[i];
-            acc.x += bo[0];
-            acc.y += bo[1];
-            acc.z += bo[2];
-            acc.w += bo[3];
+            acc.x += f2d(bo[0]);
+            acc.y += f2d(bo[1]);
+            acc.z += f2d(bo[2]);
+            acc.w += f2d(bo[3]);
             bPold[i] = acc;
         }
     }
-    double d1 = bu1, d2 = bu2;
+    double d1 = f2d(bu1), d2 = f2d(bu2);
     for (int o = 16; o > 0; o >>= 1) {
         d1 += __shfl_down_sync(0xffffffffu, d1, o);
         d2 += __shfl_down_sync(0xffffffffu, d2, o);
@@ -1122,7 +1129,7 @@ namespace adjml {
 static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
 
 void flux(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq, const float4 *qm, const float *delta,
-          const float4 *acc, const double4_32a *bF, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta)
+          const float4 *acc, const float4 *bF, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta)
 {
     const int g = grid_for(c.n, 128);
     if (c.unit_w) {
@@ -1134,10 +1141,10 @@ void flux(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq,
     }
 }
 
-void inner(const Launch &L, const DevCloud &c, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0)
+void inner(const Launch &L, const DevCloud &c, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0, bool first)
 {
-    if (c.unit_w) adjm::k_inner<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, bdq_out, bdq_in, bdq0);
-    else adjm::k_inner<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, bdq_out, bdq_in, bdq0);
+    if (c.unit_w) adjm::k_inner<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, bdq_out, bdq_in, bdq0, first);
+    else adjm::k_inner<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, bdq_out, bdq_in, bdq0, first);
 }
 
 void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq, const float4 *bdq0,
@@ -1148,7 +1155,7 @@ void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq
 }
 
 void update(const Launch &L, const DevCloud &c, const CaseConst &K, const double4_32a *Pin, const double4_32a *Pold,
-            const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, double4_32a *bF, double *buinf)
+            const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, float4 *bF, double *buinf)
 {
     adjm::k_update<<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, K, Pin, Pold, Pout, rk, bP, bPold, bF, buinf);
 }

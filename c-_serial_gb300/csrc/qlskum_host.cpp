@@ -1938,6 +1938,7 @@ struct AdjBuf {
     std::vector<float4 *> dq32;        // [stage][inner step 0 .. ni], each [np][2]
     float4 *qm32[4] = {};
     float4 *acc32[4] = {};             // the flux kernel's weighted sums
+    float4 *bF32 = nullptr;            // bar of the flux residual
     float *delta32 = nullptr, *cs32 = nullptr;
     float4 *bq32 = nullptr, *bdqA32 = nullptr, *bdqB32 = nullptr, *bdq0_32 = nullptr, *bqm32 = nullptr;
     float *bdelta32 = nullptr, *bcs32 = nullptr;
@@ -2027,6 +2028,7 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
         a->delta32 = A.alloc<float>(np);
         a->cs32 = A.alloc<float>(np);
         a->bq32 = A.alloc<float4>(np);
+        a->bF32 = A.alloc<float4>(np);
         for (auto *p : {&a->bdqA32, &a->bdqB32, &a->bdq0_32, &a->bqm32}) *p = A.alloc<float4>(2 * np);
         a->bdelta32 = A.alloc<float>(np);
         a->bcs32 = A.alloc<float>(np);
@@ -2179,19 +2181,16 @@ void adj_iteration_reverse32(qlskum_handle *h, const AdjView &v)
     zero(h, a->bPacc, sizeof(double4_32a) * np);
     zero(h, a->bdelta32, sizeof(float) * np);
     for (int s = 3; s >= 0; s--) {
-        adjml::update(h->L, c, h->K, a->P[s], a->P[0], a->P[s + 1], s + 1, a->bP, a->bPacc, a->bF, a->buinf);
-        zero(h, a->bq32, sizeof(float4) * np);
-        zero(h, a->bdqA32, sizeof(float4) * 2 * np);
-        zero(h, a->bqm32, sizeof(float4) * 2 * np);
-        adjml::flux(h->L, c, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->delta32, a->acc32[s], a->bF, a->bq32,
+        adjml::update(h->L, c, h->K, a->P[s], a->P[0], a->P[s + 1], s + 1, a->bP, a->bPacc, a->bF32, a->buinf);
+        // the flux reverse stores every point's bars of q, dq and qm first
+        adjml::flux(h->L, c, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->delta32, a->acc32[s], a->bF32, a->bq32,
                     a->bdqA32, a->bqm32, a->bdelta32);
-        zero(h, a->bdq0_32, sizeof(float4) * 2 * np);
         for (int j = ni; j >= 1; j--) {
             zero(h, a->bdqB32, sizeof(float4) * 2 * np);
-            adjml::inner(h->L, c, a->bdqA32, a->bdqB32, a->bdq0_32);
+            adjml::inner(h->L, c, a->bdqA32, a->bdqB32, a->bdq0_32, j == ni);
             std::swap(a->bdqA32, a->bdqB32);
         }
-        adjml::grad(h->L, c, a->q32[s], a->bdqA32, a->bdq0_32, a->bqm32, a->bq32);
+        adjml::grad(h->L, c, a->q32[s], a->bdqA32, ni > 0 ? a->bdq0_32 : nullptr, a->bqm32, a->bq32);
         adjml::qvars(h->L, h->n, a->P[s], a->bq32, a->bP);
     }
     zero(h, a->bcs32, sizeof(float) * np);

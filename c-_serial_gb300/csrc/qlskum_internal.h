@@ -201,11 +201,12 @@ void objective_J(const Launch &L, int n, const double4_32a *P, double gamma, dou
 namespace adjml {
 // reverse of the stage update (rk 1..4 as the forward), FP32 arithmetic
 void update(const Launch &L, const DevCloud &c, const CaseConst &K, const double4_32a *Pin, const double4_32a *Pold,
-            const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, double4_32a *bF, double *buinf);
+            const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, float4 *bF, double *buinf);
 void flux(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq, const float4 *qm, const float *delta,
-          const float4 *acc, const double4_32a *bF, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta);
-// reverse of one mixed inner step: bdq_in += ..., bdq0 += bdq_out (the dq0 term)
-void inner(const Launch &L, const DevCloud &c, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0);
+          const float4 *acc, const float4 *bF, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta);
+// reverse of one mixed inner step: bdq_in += ..., bdq0 += bdq_out (the dq0 term; = for the
+// stage's first reverse step)
+void inner(const Launch &L, const DevCloud &c, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0, bool first);
 // reverse of the gradient and max / min; the gradient's bar is bdq + bdq0
 void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq, const float4 *bdq0,
           const float4 *bqm, float4 *bq);

@@ -16,41 +16,12 @@
 // seed and two Newton steps), and the local time step and its wave speed are
 // FP32 (they only set the pseudo-time step, not the steady state).
 #include "qlskum_math.cuh"
+#include "qlskum_conv.cuh"
 
 namespace qlskum {
 namespace mixed {
 
 static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
-
-// float -> double on the integer pipe.  The hardware conversion issues on the
-// FP64 pipe, which on this chip is the scarce one; this is exact for normal
-// numbers and zero, flushes subnormals to zero and keeps Inf / NaN.
-__device__ __forceinline__ double f2d(float x)
-{
-    const unsigned b = __float_as_uint(x);
-    const unsigned mag = b & 0x7fffffffu;
-    const unsigned sign = b & 0x80000000u;
-    unsigned hi = sign | (((mag >> 23) + 896u) << 20) | ((mag & 0x7fffffu) >> 3);
-    unsigned lo = b << 29;
-    if (mag < 0x00800000u) { hi = sign; lo = 0u; }
-    if (mag >= 0x7f800000u) hi = sign | 0x7ff00000u | ((mag & 0x7fffffu) >> 3);
-    return __hiloint2double((int)hi, (int)lo);
-}
-
-// double -> float on the integer pipe, truncating the mantissa (< 1 ulp);
-// underflow goes to zero, overflow and Inf to Inf, NaN stays NaN.
-__device__ __forceinline__ float d2f(double x)
-{
-    const unsigned h = (unsigned)__double2hiint(x), l = (unsigned)__double2loint(x);
-    const unsigned mag = h & 0x7fffffffu;
-    const unsigned sign = h & 0x80000000u;
-    const int e = (int)(mag >> 20) - 896;
-    const unsigned m = ((mag & 0xfffffu) << 3) | (l >> 29);
-    unsigned b = sign | ((unsigned)e << 23) | m;
-    if (e <= 0) b = sign;
-    if (e >= 255) b = sign | 0x7f800000u | ((mag >= 0x7ff00000u && (m | (mag & 0xfffffu) | l)) ? 0x400000u : 0u);
-    return __uint_as_float(b);
-}
 
 __device__ __forceinline__ void q_of(const double P[4], float Q[4])
 {
