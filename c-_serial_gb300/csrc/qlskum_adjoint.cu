@@ -15,7 +15,7 @@
 // least-squares moments) for the wall-displacement gradient, which the host
 // finishes (qlskum_host.cpp).
 #include "qlskum_adjoint.cuh"
-#include "qlskum_conv.cuh"
+#include "qlskum_dev.cuh"
 
 namespace qlskum {
 namespace adjk {
@@ -757,11 +757,24 @@ __global__ void __launch_bounds__(128, 4) k_flux_own(DevCloud c, const float4 *_
           bmni[4] = {0, 0, 0, 0};
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
+    // the next edge's data one edge ahead in registers
+    float2 dn2 = make_float2(0.f, 0.f), wn = make_float2(0.f, 0.f);
+    unsigned dirn = 0;
+    if (nb > 0) {
+        dn2 = edge_del<UW>(c, base);
+        wn = c.e_w32[base];
+        dirn = c.e_dir[base];
+    }
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
-        const float2 d = edge_del<UW>(c, e);
-        end_vjp(c, e, f, nx, ny, d.x, d.y, c.e_w32[e], c.e_dir[e], bs, qi, dxi, dyi, mxi, mni, e2i, bqi, bdxi, bdyi,
-                bmxi, bmni);
+        const float2 d = dn2, w = wn;
+        const unsigned dir = dirn;
+        if (j + 1 < nb) {
+            dn2 = edge_del<UW>(c, e + 32);
+            wn = c.e_w32[e + 32];
+            dirn = c.e_dir[e + 32];
+        }
+        end_vjp(c, e, f, nx, ny, d.x, d.y, w, dir, bs, qi, dxi, dyi, mxi, mni, e2i, bqi, bdxi, bdyi, bmxi, bmni);
     }
     // the first writer of this stage's bars: plain stores (k_flux_nbr adds after)
     bq[i] = mk4(bqi);
@@ -771,6 +784,11 @@ __global__ void __launch_bounds__(128, 4) k_flux_own(DevCloud c, const float4 *_
     bqm[2 * i + 1] = mk4(bmni);
 }
 
+// The neighbour ends, with the next edge's neighbour data (q, dq, qm: five
+// float4, and eps^2) in flight by cp.async into a two-slot ring of the
+// thread's own shared memory while the current edge is reversed (as the
+// forward's staged flux kernel); the neighbour index two edges ahead and
+// the edge data one edge ahead in registers.
 template <bool UW>
 __global__ void __launch_bounds__(128) k_flux_nbr(DevCloud c, const float4 *__restrict__ q,
                                                    const float4 *__restrict__ dq, const float4 *__restrict__ qm,
@@ -778,7 +796,11 @@ __global__ void __launch_bounds__(128) k_flux_nbr(DevCloud c, const float4 *__re
                                                    float4 *__restrict__ bq, float4 *__restrict__ bdq,
                                                    float4 *__restrict__ bqm)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    constexpr int B = 128;
+    __shared__ float4 ring[2 * 5 * B];
+    __shared__ float reps[2 * B];
+    const int t = threadIdx.x;
+    const int i = blockIdx.x * B + t;
     if (i >= c.n) return;
     const int f = c.flag[i];
     const double2 nn = c.nrm[i];
@@ -788,20 +810,53 @@ __global__ void __launch_bounds__(128) k_flux_nbr(DevCloud c, const float4 *__re
     const float bs[4] = {dl * bFi.x, dl * bFi.y, dl * bFi.z, dl * bFi.w};
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
+    auto issue = [&](int j, int k) {
+        float4 *slot = ring + (j & 1) * 5 * B + t;
+        cp_async16(slot, q + k);
+        cp_async16(slot + B, dq + 2 * k);
+        cp_async16(slot + 2 * B, dq + 2 * k + 1);
+        cp_async16(slot + 3 * B, qm + 2 * k);
+        cp_async16(slot + 4 * B, qm + 2 * k + 1);
+        cp_async4(reps + (j & 1) * B + t, c.eps2_32 + k);
+    };
+    int kc = 0, kn = 0;
+    float2 dn2 = make_float2(0.f, 0.f), wn = make_float2(0.f, 0.f);
+    unsigned dirn = 0;
+    if (nb > 0) {
+        kc = c.e_nbr[base];
+        issue(0, kc);
+        dn2 = edge_del<UW>(c, base);
+        wn = c.e_w32[base];
+        dirn = c.e_dir[base];
+    }
+    cp_commit();
+    if (nb > 1) kn = c.e_nbr[base + 32];
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
-        const int k = c.e_nbr[e];
-        const float2 d = edge_del<UW>(c, e);
+        const int k = kc;
+        const float2 d = dn2, w = wn;
+        const unsigned dir = dirn;
+        if (j + 1 < nb) {
+            issue(j + 1, kn);
+            kc = kn;
+            dn2 = edge_del<UW>(c, e + 32);
+            wn = c.e_w32[e + 32];
+            dirn = c.e_dir[e + 32];
+        }
+        cp_commit();
+        if (j + 2 < nb) kn = c.e_nbr[e + 64];
+        cp_wait<1>();
+        const float4 *slot = ring + (j & 1) * 5 * B + t;
         float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
-        ldf4(q[k], qk);
-        ldf4(dq[2 * k], dxk);
-        ldf4(dq[2 * k + 1], dyk);
-        ldf4(qm[2 * k], mxk);
-        ldf4(qm[2 * k + 1], mnk);
+        ldf4(slot[0], qk);
+        ldf4(slot[B], dxk);
+        ldf4(slot[2 * B], dyk);
+        ldf4(slot[3 * B], mxk);
+        ldf4(slot[4 * B], mnk);
+        const float e2k = reps[(j & 1) * B + t];
         float bqk[4] = {0, 0, 0, 0}, bdxk[4] = {0, 0, 0, 0}, bdyk[4] = {0, 0, 0, 0}, bmxk[4] = {0, 0, 0, 0},
               bmnk[4] = {0, 0, 0, 0};
-        end_vjp(c, e, f, nx, ny, d.x, d.y, c.e_w32[e], c.e_dir[e], bs, qk, dxk, dyk, mxk, mnk, c.eps2_32[k], bqk,
-                bdxk, bdyk, bmxk, bmnk);
+        end_vjp(c, e, f, nx, ny, d.x, d.y, w, dir, bs, qk, dxk, dyk, mxk, mnk, e2k, bqk, bdxk, bdyk, bmxk, bmnk);
         atomic_add4(bq + k, bqk);
         atomic_add4(bdq + 2 * k, bdxk);
         atomic_add4(bdq + 2 * k + 1, bdyk);

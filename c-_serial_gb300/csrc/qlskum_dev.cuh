@@ -1,6 +1,8 @@
-// Conversions between FP32 and FP64 on the integer pipe, for the mixed
-// kernels and their reverse: the hardware conversion issues on the FP64
-// pipe, which on this chip is the scarce one.
+// Device helpers shared by the mixed kernels and their reverse: conversions
+// between FP32 and FP64 on the integer pipe (the hardware conversion issues
+// on the FP64 pipe, which on this chip is the scarce one) and the cp.async
+// copies of the staged neighbour gathers (global -> the thread's own shared
+// memory; 16- and 8-byte copies need 16- / 8-byte aligned addresses).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -35,5 +37,26 @@ __device__ __forceinline__ float d2f(double x)
     if (e >= 255) b = sign | 0x7f800000u | ((mag >= 0x7ff00000u && (m | (mag & 0xfffffu) | l)) ? 0x400000u : 0u);
     return __uint_as_float(b);
 }
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async4(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 }  // namespace qlskum

@@ -16,7 +16,7 @@
 // seed and two Newton steps), and the local time step and its wave speed are
 // FP32 (they only set the pseudo-time step, not the steady state).
 #include "qlskum_math.cuh"
-#include "qlskum_conv.cuh"
+#include "qlskum_dev.cuh"
 
 namespace qlskum {
 namespace mixed {
@@ -233,27 +233,6 @@ __device__ __forceinline__ void inner_point(const DevCloud &c, int i, const floa
 // thread-minor, conflict-free): ring [D + 1][F][B] float4, then the edge
 // list, neighbour index [max_nb][B] int and edge vector [max_nb][B] float2
 // (unit weights) or float4.
-
-__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void cp_async16(void *dst, const void *src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-
-__device__ __forceinline__ void cp_async8(void *dst, const void *src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-
-__device__ __forceinline__ void cp_async4(void *dst, const void *src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-
-template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // bytes of dynamic shared memory of a staged kernel: F float4 fields per ring slot
 constexpr size_t staged_bytes(int block, int depth, int fields, int max_nb, bool uw)
