@@ -865,19 +865,6 @@ __global__ void __launch_bounds__(128) k_flux_nbr(DevCloud c, const float4 *__re
     }
 }
 
-// The FP64 2x2 solve dx = X a - Y b, dy = Y c - X b (a = syy/det, b =
-// sxy/det, c = sxx/det) in reverse, in FP32.
-__device__ __forceinline__ void solve_vjp(const double4_32a &m, const float bx[4], const float by[4], float bX[4],
-                                          float bY[4])
-{
-    const float a = d2f(m.x), b = d2f(m.y), cc = d2f(m.z);
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        bX[r] = bx[r] * a - by[r] * b;
-        bY[r] = by[r] * cc - bx[r] * b;
-    }
-}
-
 template <bool UW> __device__ __forceinline__ float4 edge_w(const DevCloud &c, long long e)
 {
     if (UW) {
@@ -887,18 +874,18 @@ template <bool UW> __device__ __forceinline__ float4 edge_w(const DevCloud &c, l
     return c.e_geo32[e];
 }
 
-// Reverse of one mixed inner step, dq_out = dq0 + 0.5 (dq_in - solve(S)),
-// S = sum w d (d.dq_in_k) (inner_point of the mixed kernels): the bar of
-// dq_out goes to dq0 (accumulated over the steps in bdq0, the point's own
-// entry only), half of it to the point's own dq_in, and through the solve
-// and S to the neighbours' dq_in.
+// Reverse of one mixed inner step, dq_out = dq0 + 0.5 (dq_in - A),
+// A = sum_e g_e (d_e.dq_in_k) with the folded solve weights g_e
+// (inner_point of the mixed kernels): the bar of dq_out goes to dq0
+// (accumulated over the steps in bdq0, the point's own entry only), half of
+// it to the point's own dq_in, and through A to the neighbours' dq_in.
 template <bool UW>
 __global__ void k_inner(DevCloud c, const float4 *__restrict__ bdq_out, float4 *__restrict__ bdq_in,
                         float4 *__restrict__ bdq0, int first)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
-    float bx[4], by[4], bax[4], bay[4], bsx[4], bsy[4];
+    float bx[4], by[4], bax[4], bay[4];
     ldf4(bdq_out[2 * i], bx);
     ldf4(bdq_out[2 * i + 1], by);
     float a0[4] = {0, 0, 0, 0}, a1[4] = {0, 0, 0, 0};
@@ -919,17 +906,17 @@ __global__ void k_inner(DevCloud c, const float4 *__restrict__ bdq_out, float4 *
     bdq0[2 * i + 1] = make_float4(a1[0], a1[1], a1[2], a1[3]);
     atomic_add4(bdq_in + 2 * i, bx);
     atomic_add4(bdq_in + 2 * i + 1, by);
-    solve_vjp(c.gcoef[i], bax, bay, bsx, bsy);
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         const float4 g = edge_w<UW>(c, e);
+        const float2 gw = c.e_gw32[e];
         float bdxk[4], bdyk[4];
 #pragma unroll
         for (int r = 0; r < 4; r++) {
-            const float bu = g.z * bsx[r] + g.w * bsy[r];
+            const float bu = fmaf(gw.x, bax[r], gw.y * bay[r]);
             bdxk[r] = g.x * bu;
             bdyk[r] = g.y * bu;
         }
@@ -947,7 +934,7 @@ __global__ void k_grad(DevCloud c, const float4 *__restrict__ q, const float4 *_
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
-    float bx[4], by[4], bsdx[4], bsdy[4], bmax[4], bmin[4], qi[4], b0x[4], b0y[4];
+    float bx[4], by[4], bmax[4], bmin[4], qi[4], b0x[4], b0y[4];
     ldf4(bdq[2 * i], bx);
     ldf4(bdq[2 * i + 1], by);
     if (bdq0) {
@@ -962,7 +949,6 @@ __global__ void k_grad(DevCloud c, const float4 *__restrict__ q, const float4 *_
     ldf4(bqm[2 * i], bmax);
     ldf4(bqm[2 * i + 1], bmin);
     ldf4(q[i], qi);
-    solve_vjp(c.gcoef[i], bx, by, bsdx, bsdy);
     float qmax[4], qmin[4];
     int amax[4], amin[4];
 #pragma unroll
@@ -976,14 +962,14 @@ __global__ void k_grad(DevCloud c, const float4 *__restrict__ q, const float4 *_
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
-        const float4 g = edge_w<UW>(c, e);
+        const float2 gw = c.e_gw32[e];
         float qk[4], bqk[4];
         ldf4(q[k], qk);
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             if (qk[r] > qmax[r]) { qmax[r] = qk[r]; amax[r] = k; }
             if (qk[r] < qmin[r]) { qmin[r] = qk[r]; amin[r] = k; }
-            const float bt = g.z * bsdx[r] + g.w * bsdy[r];
+            const float bt = fmaf(gw.x, bx[r], gw.y * by[r]);
             bqk[r] = bt;
             bqi[r] -= bt;
         }

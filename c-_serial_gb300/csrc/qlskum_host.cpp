@@ -669,7 +669,7 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
     std::vector<double4_32a> fgeo((size_t)G.np * 4, make_double4_32a(0, 0, 0, 0));
     std::vector<float2> e_w32(ne, make_float2(0, 0)), e_w32b(ne, make_float2(0, 0));
     std::vector<double4_32a> gcoef(G.np, make_double4_32a(0, 0, 0, 0));
-    std::vector<float2> e_xy32(ne, make_float2(0, 0));
+    std::vector<float2> e_xy32(ne, make_float2(0, 0)), e_gw32(ne, make_float2(0, 0));
     const bool unit_w = p->power == 0.0;
     std::vector<float> e_dist32(ne, 1.0f);
     const Precomp &P = G.pc;
@@ -683,6 +683,7 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
         ggeo[pp] = make_double4_32a(P.ggeo[4 * (size_t)i], P.ggeo[4 * (size_t)i + 1], P.ggeo[4 * (size_t)i + 2],
                                 P.ggeo[4 * (size_t)i + 3]);
         // q_variables_mod.h:112-116 as coefficients: dq_x = Sx syy/det - Sy sxy/det, dq_y = Sy sxx/det - Sx sxy/det
+        // (folded into the per-edge gradient weights below)
         gcoef[pp] = make_double4_32a(P.ggeo[4 * (size_t)i + 1] * P.ggeo[4 * (size_t)i + 3],
                                      P.ggeo[4 * (size_t)i + 2] * P.ggeo[4 * (size_t)i + 3],
                                      P.ggeo[4 * (size_t)i + 0] * P.ggeo[4 * (size_t)i + 3], 0.0);
@@ -715,6 +716,12 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
             e_geo32[e] = make_float4((float)P.geo[4 * src], (float)P.geo[4 * src + 1], (float)P.geo[4 * src + 2],
                                      (float)P.geo[4 * src + 3]);
             e_sn32[e] = make_float2((float)P.sn[2 * src], (float)P.sn[2 * src + 1]);
+            // per-edge gradient weights gx = a w delx - b w dely, gy = c w dely - b w delx (FP64, then FP32)
+            {
+                const double4_32a &gc = gcoef[pp];
+                const double wx = P.geo[4 * src + 2], wy = P.geo[4 * src + 3];
+                e_gw32[e] = make_float2((float)(gc.x * wx - gc.y * wy), (float)(gc.z * wy - gc.y * wx));
+            }
             // per-edge solve weights c_ed = a_d dels_w + b_d deln_w (FP64, then FP32)
             {
                 const unsigned bits = P.edge_dir[src];
@@ -751,8 +758,7 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
     float2 *d_esn32 = nullptr;
     float *d_eps32 = nullptr, *d_edist32 = nullptr;
     float2 *d_ew32 = nullptr, *d_ew32b = nullptr;
-    double4_32a *d_gcoef = nullptr;
-    float2 *d_exy32 = nullptr;
+    float2 *d_exy32 = nullptr, *d_egw32 = nullptr;
     if (need_mixed) {
         if (unit_w) {
             d_exy32 = A.alloc<float2>(ne);
@@ -764,17 +770,18 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
         d_edist32 = A.alloc<float>(ne);
         d_ew32 = A.alloc<float2>(ne);
         d_ew32b = A.alloc<float2>(ne);
-        d_gcoef = A.alloc<double4_32a>(G.np);
+        d_egw32 = A.alloc<float2>(ne);
     }
     up(d_flag, flag); up(d_nb, nbh); up(d_sb, sbase); up(d_enbr, e_nbr); up(d_egeo, e_geo); up(d_esn, e_sn);
     up(d_edist, e_dist); up(d_edir, e_dir); up(d_nrm, nrm); up(d_eps2, eps2); up(d_ggeo, ggeo); up(d_fgeo, fgeo);
     up(d_egeo32, e_geo32); up(d_esn32, e_sn32); up(d_eps32, eps2_32); up(d_edist32, e_dist32); up(d_ew32, e_w32); up(d_ew32b, e_w32b);
-    up(d_gcoef, gcoef); up(d_exy32, e_xy32);
+    up(d_exy32, e_xy32); up(d_egw32, e_gw32);
     DevCloud &dc = G.dc;
     dc.n = n; dc.np = G.np; dc.flag = d_flag; dc.nbhs = d_nb; dc.slice_base = d_sb; dc.e_nbr = d_enbr;
     dc.e_geo = d_egeo; dc.e_sn = d_esn; dc.e_dist = d_edist; dc.e_dir = d_edir; dc.nrm = d_nrm; dc.eps2 = d_eps2;
     dc.ggeo = d_ggeo; dc.fgeo = d_fgeo; dc.e_geo32 = d_egeo32; dc.e_sn32 = d_esn32; dc.eps2_32 = d_eps32;
-    dc.e_dist32 = d_edist32; dc.e_w32 = d_ew32; dc.e_w32b = d_ew32b; dc.gcoef = d_gcoef; dc.unit_w = unit_w ? 1 : 0; dc.e_xy32 = d_exy32;
+    dc.e_dist32 = d_edist32; dc.e_w32 = d_ew32; dc.e_w32b = d_ew32b; dc.unit_w = unit_w ? 1 : 0; dc.e_xy32 = d_exy32;
+    dc.e_gw32 = d_egw32;
     dc.max_nb = 0;
     for (int i = 0; i < n; i++) dc.max_nb = std::max(dc.max_nb, c->nbhs[i]);
 

@@ -59,9 +59,13 @@ struct DevCloud {
     // lies in both; zero otherwise).
     const float2 *e_w32 = nullptr;
     const float2 *e_w32b = nullptr;
-    // Mixed form, gradient and inner loop: the 2x2 solve as coefficients
-    // {syy/det, sxy/det, sxx/det} (FP64), dq_x = Sx a - Sy b, dq_y = Sy c - Sx b.
-    const double4_32a *gcoef = nullptr;
+    // Mixed form, gradient and inner loop: the 2x2 solve dq_x = Sx a - Sy b,
+    // dq_y = Sy c - Sx b ({a, b, c} = {syy, sxy, sxx} / det) folded into
+    // per-edge weights as for the flux: with Sx = sum w delx dq and
+    // Sy = sum w dely dq, dq_x = sum_e gx_e dq_e and dq_y = sum_e gy_e dq_e,
+    // gx = a w delx - b w dely, gy = c w dely - b w delx, computed on the
+    // host in FP64 and stored in FP32 {gx, gy} per edge.
+    const float2 *e_gw32 = nullptr;
     // power == 0 (all weights 1): the mixed kernels read only {delx, dely}
     // per edge (FP32) and rotate it by the point normal themselves.
     int unit_w = 0;

@@ -112,32 +112,21 @@ __device__ __forceinline__ float4 edge_w(const DevCloud &c, long long e)
     return c.e_geo32[e];
 }
 
-// dq = the 2x2 solve of the sums (Sx, Sy), FP64 (dq_x = Sx a - Sy b, dq_y = Sy c - Sx b).
-__device__ __forceinline__ void solve_grad(const double4_32a &m, const float sdx[4], const float sdy[4], float dx[4],
-                                           float dy[4])
-{
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const double X = f2d(sdx[r]), Y = f2d(sdy[r]);
-        dx[r] = d2f(fma(X, m.x, -Y * m.y));
-        dy[r] = d2f(fma(Y, m.z, -X * m.y));
-    }
-}
-
 // ----------------------------------------------------------- point bodies
 // One point's work, shared by the single-case kernels and the batched
 // persistent kernels.  Geometry (c) is indexed by the cloud-local point i;
 // the state pointers are already offset to the case's first point, so
 // neighbour indices from the edge list address them directly.
 
-// q_variables_mod.h:36-118: FP32 differences and sums, FP64 solve; in the
-// first stage also the local time step (state_update_mod.h:448-496) in FP32.
+// q_variables_mod.h:36-118: FP32 differences, weighted by the FP64-folded
+// per-edge solve weights (DevCloud::e_gw32); in the first stage also the
+// local time step (state_update_mod.h:448-496) in FP32.
 template <bool UW>
 __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float4 *__restrict__ q,
                                            float4 *__restrict__ dq, float4 *__restrict__ qm,
                                            const float *__restrict__ cs, float *__restrict__ delta, float cfl)
 {
-    float qi[4], qmax[4], qmin[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    float qi[4], qmax[4], qmin[4], dx[4] = {0, 0, 0, 0}, dy[4] = {0, 0, 0, 0};
     ld4(q[i], qi);
 #pragma unroll
     for (int r = 0; r < 4; r++) { qmax[r] = qi[r]; qmin[r] = qi[r]; }
@@ -147,20 +136,19 @@ __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
-        const float4 g = edge_w<UW>(c, e);
+        const float2 gw = c.e_gw32[e];
         float qk[4];
         ld4(q[k], qk);
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             qmax[r] = fmaxf(qmax[r], qk[r]);
             qmin[r] = fminf(qmin[r], qk[r]);
-            sdx[r] += g.z * (qk[r] - qi[r]);
-            sdy[r] += g.w * (qk[r] - qi[r]);
+            const float d = qk[r] - qi[r];
+            dx[r] = fmaf(gw.x, d, dx[r]);
+            dy[r] = fmaf(gw.y, d, dy[r]);
         }
         if (delta) min_dt = fminf(min_dt, cfl * __fdividef(c.e_dist32[e], cs[k]));
     }
-    float dx[4], dy[4];
-    solve_grad(c.gcoef[i], sdx, sdy, dx, dy);
     dq[2 * i] = mk4(dx);
     dq[2 * i + 1] = mk4(dy);
     qm[2 * i] = mk4(qmax);
@@ -175,14 +163,13 @@ __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float
 // those moments); and sum w d (d.dq_k), the only part that needs the
 // neighbours.  So dq_out = dq0 + 0.5 (dq_i - solve(sum w d (d.dq_k))): the
 // same value up to FP32 rounding, with one gather (dq_k) per edge instead
-// of two and a quarter of the arithmetic.  The FP64 form keeps the
-// reference's order of operations.
-__device__ __forceinline__ void inner_finish(const double4_32a &m, const float sdx[4], const float sdy[4],
-                                             const float4 &d0x, const float4 &d0y, const float dxi[4],
-                                             const float dyi[4], float4 *__restrict__ out)
+// of two and a quarter of the arithmetic; the solve is applied through the
+// folded per-edge weights (DevCloud::e_gw32): solve(sum w d (d.dq_k)) =
+// sum g_e (d.dq_k).  The FP64 form keeps the reference's order of operations.
+__device__ __forceinline__ void inner_finish(const float ax[4], const float ay[4], const float4 &d0x,
+                                             const float4 &d0y, const float dxi[4], const float dyi[4],
+                                             float4 *__restrict__ out)
 {
-    float ax[4], ay[4];
-    solve_grad(m, sdx, sdy, ax, ay);
     const float o0[4] = {d0x.x, d0x.y, d0x.z, d0x.w}, o1[4] = {d0y.x, d0y.y, d0y.z, d0y.w};
     float rx[4], ry[4];
 #pragma unroll
@@ -198,7 +185,7 @@ template <bool UW>
 __device__ __forceinline__ void inner_point(const DevCloud &c, int i, const float4 *__restrict__ dq0,
                                             const float4 *__restrict__ dq_in, float4 *__restrict__ dq_out)
 {
-    float dxi[4], dyi[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    float dxi[4], dyi[4], ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0};
     ld4(dq_in[2 * i], dxi);
     ld4(dq_in[2 * i + 1], dyi);
     const int nb = c.nbhs[i];
@@ -207,17 +194,18 @@ __device__ __forceinline__ void inner_point(const DevCloud &c, int i, const floa
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         const float4 g = edge_w<UW>(c, e);
+        const float2 gw = c.e_gw32[e];
         float dxk[4], dyk[4];
         ld4(dq_in[2 * k], dxk);
         ld4(dq_in[2 * k + 1], dyk);
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             const float u = fmaf(g.x, dxk[r], g.y * dyk[r]);
-            sdx[r] = fmaf(g.z, u, sdx[r]);
-            sdy[r] = fmaf(g.w, u, sdy[r]);
+            ax[r] = fmaf(gw.x, u, ax[r]);
+            ay[r] = fmaf(gw.y, u, ay[r]);
         }
     }
-    inner_finish(c.gcoef[i], sdx, sdy, dq0[2 * i], dq0[2 * i + 1], dxi, dyi, dq_out + 2 * i);
+    inner_finish(ax, ay, dq0[2 * i], dq0[2 * i + 1], dxi, dyi, dq_out + 2 * i);
 }
 
 // ------------------------------------------------ staged neighbour gathers
@@ -277,7 +265,7 @@ __global__ void __launch_bounds__(B) k_q_inner_st(DevCloud c, const float4 *__re
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
     stage_edges<B, UW>(c, base, nb, t, snbr, sgeo);
-    float dxi[4], dyi[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    float dxi[4], dyi[4], ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0};
     ld4(dq_in[2 * i], dxi);
     ld4(dq_in[2 * i + 1], dyi);
     cp_wait<0>();
@@ -301,14 +289,15 @@ __global__ void __launch_bounds__(B) k_q_inner_st(DevCloud c, const float4 *__re
         ld4(slot[0], dxk);
         ld4(slot[B], dyk);
         const float4 g = staged_geo<B, UW>(sgeo, j, t);
+        const float2 gw = c.e_gw32[base + 32LL * j];
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             const float u = fmaf(g.x, dxk[r], g.y * dyk[r]);
-            sdx[r] = fmaf(g.z, u, sdx[r]);
-            sdy[r] = fmaf(g.w, u, sdy[r]);
+            ax[r] = fmaf(gw.x, u, ax[r]);
+            ay[r] = fmaf(gw.y, u, ay[r]);
         }
     }
-    inner_finish(c.gcoef[i], sdx, sdy, dq0[2 * i], dq0[2 * i + 1], dxi, dyi, dq_out + 2 * i);
+    inner_finish(ax, ay, dq0[2 * i], dq0[2 * i + 1], dxi, dyi, dq_out + 2 * i);
 }
 
 // q_variables_mod.h:36-118 with staged gathers (q and, in the first stage,
@@ -328,8 +317,14 @@ __global__ void __launch_bounds__(B) k_q_derivatives_st(DevCloud c, const float4
     if (i >= c.n) return;
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
-    stage_edges<B, UW>(c, base, nb, t, snbr, sgeo);
-    float qi[4], qmax[4], qmin[4], sdx[4] = {0, 0, 0, 0}, sdy[4] = {0, 0, 0, 0};
+    // the edge list: neighbour index and folded gradient weights (8 B per edge whatever the weights)
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        cp_async4(snbr + j * B + t, c.e_nbr + e);
+        cp_async8(static_cast<float2 *>(sgeo) + j * B + t, c.e_gw32 + e);
+    }
+    cp_commit();
+    float qi[4], qmax[4], qmin[4], dx[4] = {0, 0, 0, 0}, dy[4] = {0, 0, 0, 0};
     ld4(q[i], qi);
 #pragma unroll
     for (int r = 0; r < 4; r++) { qmax[r] = qi[r]; qmin[r] = qi[r]; }
@@ -357,21 +352,20 @@ __global__ void __launch_bounds__(B) k_q_derivatives_st(DevCloud c, const float4
         const float4 *slot = ring + (j % (D + 1)) * 2 * B + t;
         float qk[4];
         ld4(slot[0], qk);
-        const float4 g = staged_geo<B, UW>(sgeo, j, t);
+        const float2 gw = static_cast<const float2 *>(sgeo)[j * B + t];
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             qmax[r] = fmaxf(qmax[r], qk[r]);
             qmin[r] = fminf(qmin[r], qk[r]);
-            sdx[r] += g.z * (qk[r] - qi[r]);
-            sdy[r] += g.w * (qk[r] - qi[r]);
+            const float d = qk[r] - qi[r];
+            dx[r] = fmaf(gw.x, d, dx[r]);
+            dy[r] = fmaf(gw.y, d, dy[r]);
         }
         if (delta) {
             const float4 aux = slot[B];
             min_dt = fminf(min_dt, cfl * __fdividef(aux.y, aux.x));
         }
     }
-    float dx[4], dy[4];
-    solve_grad(c.gcoef[i], sdx, sdy, dx, dy);
     dq[2 * i] = mk4(dx);
     dq[2 * i + 1] = mk4(dy);
     qm[2 * i] = mk4(qmax);
@@ -863,7 +857,7 @@ int staged_variants(const DevCloud &c)
                      allow_smem(k_q_derivatives_st<B_, D_, true>, staged_bytes(B_, D_, 2, c.max_nb, true));
             } else {
                 ok = allow_smem(k_q_inner_st<B_, D_, false>, staged_bytes(B_, D_, 2, c.max_nb, false)) &&
-                     allow_smem(k_q_derivatives_st<B_, D_, false>, staged_bytes(B_, D_, 2, c.max_nb, false));
+                     allow_smem(k_q_derivatives_st<B_, D_, false>, staged_bytes(B_, D_, 2, c.max_nb, true));
             })
         if (!ok) break;
         usable = v;
@@ -881,7 +875,7 @@ void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *
                 k_q_derivatives_st<B_, D_, true><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 2, c.max_nb, true),
                                                    L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
             else
-                k_q_derivatives_st<B_, D_, false><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 2, c.max_nb, false),
+                k_q_derivatives_st<B_, D_, false><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 2, c.max_nb, true),
                                                     L.stream>>>(c, q, dq, qm, cspeed, delta, cfl))
     } else if (c.unit_w) {
         k_q_derivatives<true><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
