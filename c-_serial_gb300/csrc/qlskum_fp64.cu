@@ -352,6 +352,22 @@ __global__ void k_copy(int n, const double4_32a *__restrict__ src, double4_32a *
     if (i < n) dst[i] = src[i];
 }
 
+// Point states between the cloud's order and the handle's (Morton / class)
+// order: dst[perm[i]] = src[i] (in) or dst[i] = src[perm[i]] (out).
+__global__ void k_permute_in(int n, const int *__restrict__ perm, const double4_32a *__restrict__ src,
+                             double4_32a *__restrict__ dst)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[perm[i]] = src[i];
+}
+
+__global__ void k_permute_out(int n, const int *__restrict__ perm, const double4_32a *__restrict__ src,
+                              double4_32a *__restrict__ dst)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[perm[i]];
+}
+
 __global__ void k_add(int n, const double4_32a *__restrict__ src, double4_32a *__restrict__ dst)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -583,6 +599,18 @@ void reduce_residual(const Launch &L, const Reduce &R, int n, int it)
 void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
 {
     k_copy<<<grid_for(n, 256), 256, 0, L.stream>>>(n, src, dst);
+    QLSKUM_LAUNCHED(L);
+}
+
+void permute_in(const Launch &L, int n, const int *perm, const double4_32a *src, double4_32a *dst)
+{
+    k_permute_in<<<grid_for(n, 256), 256, 0, L.stream>>>(n, perm, src, dst);
+    QLSKUM_LAUNCHED(L);
+}
+
+void permute_out(const Launch &L, int n, const int *perm, const double4_32a *src, double4_32a *dst)
+{
+    k_permute_out<<<grid_for(n, 256), 256, 0, L.stream>>>(n, perm, src, dst);
     QLSKUM_LAUNCHED(L);
 }
 

@@ -122,6 +122,10 @@ struct qlskum_handle {
     bool restarted = false;       // state and res_old came from a restart file
     int *d_wall_perm = nullptr;
     double4_32a *d_wall_geo = nullptr;
+    // the point permutation on the device and a staging buffer in the cloud's
+    // order, for moving states across the C ABI (allocated on first use)
+    int *d_perm = nullptr;
+    double4_32a *d_stage = nullptr;
     cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
     // launch shape of the mixed fused kernel and of the point kernels, set by
     // tune() on the first fused iteration unless params.block_size fixes it
@@ -973,6 +977,8 @@ qlskum_status qlskum_destroy(qlskum_handle *h)
     }
     for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
     if (h->R.hist) cudaFree(h->R.hist);
+    if (h->d_perm) cudaFree(h->d_perm);
+    if (h->d_stage) cudaFree(h->d_stage);
     adj_free(h);
     h->arena.release();
     if (h->L.stream) cudaStreamDestroy(h->L.stream);
@@ -1193,19 +1199,51 @@ qlskum_status qlskum_get_field(qlskum_handle *h, int field, double *out)
     return QLSKUM_OK;
 }
 
-qlskum_status qlskum_get_prim(qlskum_handle *h, double *out) { return qlskum_get_field(h, QLSKUM_FIELD_PRIM, out); }
+namespace {
+// The device copy of the permutation and the staging buffer (first use).
+qlskum_status ensure_stage(qlskum_handle *h)
+{
+    if (h->d_stage) return QLSKUM_OK;
+    cudaError_t e = cudaMalloc(&h->d_perm, sizeof(int) * (size_t)h->n);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_stage, sizeof(double4_32a) * (size_t)h->n);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->d_perm, h->perm.data(), sizeof(int) * (size_t)h->n, cudaMemcpyHostToDevice, h->L.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->L.stream);
+    if (e != cudaSuccess) {
+        if (h->d_perm) cudaFree(h->d_perm);
+        if (h->d_stage) cudaFree(h->d_stage);
+        h->d_perm = nullptr;
+        h->d_stage = nullptr;
+        return fail(h, QLSKUM_ERR_CUDA, fmt("state staging buffers: %s", cudaGetErrorString(e)));
+    }
+    return QLSKUM_OK;
+}
+}  // namespace
+
+// prim in the cloud's order: one copy of [n][4] doubles from the caller's
+// buffer (a DMA at the link's rate when the caller's memory is pinned), the
+// reordering on the device.
+qlskum_status qlskum_get_prim(qlskum_handle *h, double *out)
+{
+    NEED(h);
+    if (!out) return fail(h, QLSKUM_ERR_INVALID, "null output");
+    qlskum_status st = ensure_stage(h);
+    if (st) return st;
+    fp64::permute_out(h->L, h->n, h->d_perm, h->s64.prim[h->pcur], h->d_stage);
+    CK(h, cudaMemcpyAsync(out, h->d_stage, sizeof(double4_32a) * (size_t)h->n, cudaMemcpyDeviceToHost, h->L.stream));
+    CK(h, cudaStreamSynchronize(h->L.stream));
+    return QLSKUM_OK;
+}
 
 qlskum_status qlskum_set_prim(qlskum_handle *h, const double *prim)
 {
     NEED(h);
     if (!prim) return fail(h, QLSKUM_ERR_INVALID, "null prim");
-    std::vector<double4_32a> dev(h->np, make_double4_32a(1, 0, 0, 1));
-    for (int i = 0; i < h->n; i++) {
-        const double *s = prim + 4 * (size_t)i;
-        dev[h->perm[i]] = make_double4_32a(s[0], s[1], s[2], s[3]);
-    }
-    CK(h, cudaMemcpyAsync(h->s64.prim[h->pcur], dev.data(), sizeof(double4_32a) * h->np, cudaMemcpyHostToDevice,
-                          h->L.stream));
+    qlskum_status st = ensure_stage(h);
+    if (st) return st;
+    CK(h, cudaMemcpyAsync(h->d_stage, prim, sizeof(double4_32a) * (size_t)h->n, cudaMemcpyHostToDevice, h->L.stream));
+    // padding rows of the state keep the finite values they were created with
+    fp64::permute_in(h->L, h->n, h->d_perm, h->d_stage, h->s64.prim[h->pcur]);
     // a new state clears a non-finite flag raised by the old one
     CK(h, cudaMemsetAsync(h->R.status, 0, sizeof(int), h->L.stream));
     CK(h, cudaStreamSynchronize(h->L.stream));

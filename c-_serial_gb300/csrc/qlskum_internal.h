@@ -239,6 +239,9 @@ void reduce_residual(const Launch &L, const Reduce &R, int n, int it);
 void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
 // dst += src over n double4 rows
 void add_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
+// [n] point states from the cloud's order into the handle's (dst[perm[i]] = src[i]) and back
+void permute_in(const Launch &L, int n, const int *perm, const double4_32a *src, double4_32a *dst);
+void permute_out(const Launch &L, int n, const int *perm, const double4_32a *src, double4_32a *dst);
 // diagnostics: vorticity [n] and per-256-block partial sums of its square;
 // stagnation pressure per-256-block {min, argmin, max, argmax, sum (p0_inf - p0)^2, sum p0}
 void enstrophy(const Launch &L, const DevCloud &c, const double4_32a *prim, double *vort, double *partial);

@@ -119,9 +119,9 @@ __device__ __forceinline__ float4 edge_w(const DevCloud &c, long long e)
 // neighbour indices from the edge list address them directly.
 
 // q_variables_mod.h:36-118: FP32 differences, weighted by the FP64-folded
-// per-edge solve weights (DevCloud::e_gw32); in the first stage also the
-// local time step (state_update_mod.h:448-496) in FP32.
-template <bool UW>
+// per-edge solve weights (DevCloud::e_gw32); with DT (the first stage) also
+// the local time step (state_update_mod.h:448-496) in FP32.
+template <bool DT>
 __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float4 *__restrict__ q,
                                            float4 *__restrict__ dq, float4 *__restrict__ qm,
                                            const float *__restrict__ cs, float *__restrict__ delta, float cfl)
@@ -147,13 +147,13 @@ __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float
             dx[r] = fmaf(gw.x, d, dx[r]);
             dy[r] = fmaf(gw.y, d, dy[r]);
         }
-        if (delta) min_dt = fminf(min_dt, cfl * __fdividef(c.e_dist32[e], cs[k]));
+        if (DT) min_dt = fminf(min_dt, cfl * __fdividef(c.e_dist32[e], cs[k]));
     }
     dq[2 * i] = mk4(dx);
     dq[2 * i + 1] = mk4(dy);
     qm[2 * i] = mk4(qmax);
     qm[2 * i + 1] = mk4(qmin);
-    if (delta) delta[i] = min_dt;
+    if (DT) delta[i] = min_dt;
 }
 
 // q_variables_mod.h:120-213 in the mixed form.  The reference's sums over
@@ -186,8 +186,6 @@ __device__ __forceinline__ void inner_point(const DevCloud &c, int i, const floa
                                             const float4 *__restrict__ dq_in, float4 *__restrict__ dq_out)
 {
     float dxi[4], dyi[4], ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0};
-    ld4(dq_in[2 * i], dxi);
-    ld4(dq_in[2 * i + 1], dyi);
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
     for (int j = 0; j < nb; j++) {
@@ -205,6 +203,9 @@ __device__ __forceinline__ void inner_point(const DevCloud &c, int i, const floa
             ay[r] = fmaf(gw.y, u, ay[r]);
         }
     }
+    // the point's own gradient only after the loop: fewer registers live across it
+    ld4(dq_in[2 * i], dxi);
+    ld4(dq_in[2 * i + 1], dyi);
     inner_finish(ax, ay, dq0[2 * i], dq0[2 * i + 1], dxi, dyi, dq_out + 2 * i);
 }
 
@@ -627,13 +628,13 @@ __device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseCon
 
 // ---------------------------------------------------- single-case kernels
 
-template <bool UW>
+template <bool DT>
 __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4 *__restrict__ dq,
                                 float4 *__restrict__ qm, const float *__restrict__ cs, float *__restrict__ delta,
                                 float cfl)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < c.n) grad_point<UW>(c, i, q, dq, qm, cs, delta, cfl);
+    if (i < c.n) grad_point<DT>(c, i, q, dq, qm, cs, delta, cfl);
 }
 
 template <bool UW>
@@ -713,7 +714,7 @@ __global__ void __launch_bounds__(TILE) kb_derived(const BatchCase *__restrict__
     }
 }
 
-template <int TILE, bool UW>
+template <int TILE, bool DT>
 __global__ void __launch_bounds__(TILE) kb_q_derivatives(const DevCloud *__restrict__ clouds,
                                                          const BatchCase *__restrict__ cases,
                                                          const BatchTile *__restrict__ tiles, int ntiles,
@@ -726,8 +727,8 @@ __global__ void __launch_bounds__(TILE) kb_q_derivatives(const DevCloud *__restr
         const BatchCase &C = cases[T.cas];
         const int i = T.first + threadIdx.x;
         if (i < C.n)
-            grad_point<UW>(clouds[C.cloud], i, q + C.off, dq + 2 * C.off, qm + 2 * C.off, cs + C.off,
-                           delta ? delta + C.off : nullptr, cfl);
+            grad_point<DT>(clouds[C.cloud], i, q + C.off, dq + 2 * C.off, qm + 2 * C.off, cs + C.off,
+                           DT ? delta + C.off : nullptr, cfl);
     }
 }
 
@@ -877,7 +878,7 @@ void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *
             else
                 k_q_derivatives_st<B_, D_, false><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 2, c.max_nb, true),
                                                     L.stream>>>(c, q, dq, qm, cspeed, delta, cfl))
-    } else if (c.unit_w) {
+    } else if (delta) {
         k_q_derivatives<true><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
     } else {
         k_q_derivatives<false><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
@@ -989,7 +990,7 @@ void batch_q_derivatives(const Launch &L, const BatchView &B, int tile, const fl
 {
     QLSKUM_TILE_SWITCH(tile, {
         const int ti = tile_index(T_);
-        if (B.unit_w) {
+        if (delta) {
             const int g = persistent_grid(kb_q_derivatives<T_, true>, T_, B.ntiles[ti]);
             kb_q_derivatives<T_, true><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq, qm,
                                                                cs, delta, cfl);
