@@ -260,6 +260,89 @@ def batch_workload(seed=3, n_clouds=32, n_cases=64):
     return clouds, cases
 
 
+def run_adjoint_check(args):
+    """The discrete adjoint on the 1.02 M-point NACA 0012 cloud at M 0.63,
+    AoA 2: FP64 handle, dCl and dCd w.r.t. Mach, AoA and the normal
+    displacement of every wall point through K iterations from the free
+    stream (each iteration's state checkpointed), timed against the same K
+    primal iterations; checked against central differences of the FP64
+    solver (which matches the reference's serial path to 1e-10) on 16 seeded
+    wall points (away from the trailing edge) and both scalars.  Wall clock,
+    host-synchronous calls."""
+    import qlskum
+    qlskum.load()
+    cloud = make_cloud("transonic")
+    kw = dict(WORKLOADS["transonic"]["solver"], mach=0.63, aoa=2.0)
+    k, stride = max(1, args.adjoint_iters), args.adjoint_stride
+    s = qlskum.Solver(cloud, precision=qlskum.FP64, **kw)
+    s.adjoint_gradient("cl", iters=1, wall=True)                      # allocation
+    grads, t_adj = {}, {}
+    for obj in ("cl", "cd"):
+        t0 = time.perf_counter()
+        grads[obj] = s.adjoint_gradient(obj, iters=k, wall=True, stride=stride)
+        t_adj[obj] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    s.q_lskum(k)
+    s.synchronize()
+    t_pr = time.perf_counter() - t0
+    nrm = s.field(qlskum.FIELD_NORMALS)
+    shape = s.shape_points
+    s.close()
+
+    def objective(mach=kw["mach"], aoa=kw["aoa"], c=cloud):
+        t = qlskum.Solver(c, precision=qlskum.FP64, **dict(kw, mach=mach, aoa=aoa))
+        t.q_lskum(k)
+        cl, cd = t.objective()[:2]
+        t.close()
+        return {"cl": cl, "cd": cd}
+
+    def moved(m, d):
+        from qlskum.cloudgen import Cloud
+        x, y = cloud.x.copy(), cloud.y.copy()
+        x[m] += d * nrm[m][0]
+        y[m] += d * nrm[m][1]
+        return Cloud(x, y, cloud.left, cloud.right, cloud.flag_1, cloud.flag_2, cloud.min_dist, cloud.nbhs, cloud.conn)
+
+    t_fd = time.perf_counter()
+    hm, ha, hw = 1e-6, 1e-5, 3e-8
+    fd = {"dmach": {}, "daoa": {}}
+    a, b = objective(mach=kw["mach"] + hm), objective(mach=kw["mach"] - hm)
+    fd["dmach"] = {o: (a[o] - b[o]) / (2 * hm) for o in ("cl", "cd")}
+    a, b = objective(aoa=kw["aoa"] + ha), objective(aoa=kw["aoa"] - ha)
+    fd["daoa"] = {o: (a[o] - b[o]) / (2 * ha) for o in ("cl", "cd")}
+    te = {0, int(cloud.left[0]) - 1, int(cloud.right[0]) - 1}
+    rng = np.random.default_rng(16)
+    pts = rng.choice(sorted(set(range(shape)) - te), size=16, replace=False)
+    err = {"cl": {"dmach": 0.0, "daoa": 0.0, "dwall": 0.0}, "cd": {"dmach": 0.0, "daoa": 0.0, "dwall": 0.0}}
+    for o in ("cl", "cd"):
+        for key in ("dmach", "daoa"):
+            err[o][key] = abs(grads[o][key] - fd[key][o]) / max(abs(fd[key][o]), 1e-12)
+    for m in pts:
+        a, b = objective(c=moved(m, hw)), objective(c=moved(m, -hw))
+        for o in ("cl", "cd"):
+            f = (a[o] - b[o]) / (2 * hw)
+            scale = np.abs(grads[o]["dwall"]).max()
+            err[o]["dwall"] = max(err[o]["dwall"], abs(grads[o]["dwall"][m] - f) / max(abs(f), 1e-2 * scale))
+    t_fd = time.perf_counter() - t_fd
+    ratio = max(t_adj.values()) / t_pr
+    line = {
+        "metric": "adjoint_over_primal", "value": ratio, "unit": "x", "n_gpus": 1, "steps": k, "warmup": 1,
+        "ms_per_step": 1e3 * max(t_adj.values()) / k, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "naca0012_1024x1000_adjoint", "points": cloud.n, "mach": kw["mach"], "aoa": kw["aoa"],
+                   "inner_iterations": kw["inner_iterations"], "iterations_differentiated": k,
+                   "checkpoint_stride": stride, "wall_points": shape, "precision": "fp64",
+                   "parallelism": "single"},
+        "adjoint": {o: {"seconds": t_adj[o], "dmach": grads[o]["dmach"], "daoa_per_deg": grads[o]["daoa"],
+                        "dwall_max_abs": float(np.abs(grads[o]["dwall"]).max())} for o in ("cl", "cd")},
+        "primal_seconds": t_pr,
+        "fd_check": {"steps": {"mach": hm, "aoa_deg": ha, "wall": hw}, "wall_points": [int(m) for m in pts],
+                     "max_rel_err": err, "seconds": t_fd,
+                     "note": "central differences of the FP64 solver, K iterations from the free stream"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_batch(args):
     """Batched launch: 64 flight conditions over 32 uneven clouds, mixed precision."""
     import torch
@@ -312,10 +395,15 @@ def run_batch(args):
 def run_reference(args, rank, world):
     if rank != 0:
         return
+    workload = args.workload
+    if workload not in WORKLOADS:
+        # the batch and adjoint measurements have no single-cloud CPU counterpart
+        print(json.dumps({"impl": "reference", "unavailable": f"no CPU reference run for the {workload} workload"}),
+              flush=True)
+        return
     import qlskum_oracle
     qlskum_oracle.build()
     threads = os.cpu_count() or 1
-    workload = args.workload
     sample = workload
     if args.steps + args.warmup > 30 and workload == "transonic":
         sample = "subsonic"  # bounded: the 9,600-point cloud of the same recipe
@@ -394,7 +482,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="transonic", choices=sorted(WORKLOADS) + ["batch"])
+    ap.add_argument("--workload", default="transonic", choices=sorted(WORKLOADS) + ["batch", "adjoint"],
+                    help="adjoint: the FP64 adjoint on the 1.02 M cloud at M 0.63, AoA 2, with its FD check")
     ap.add_argument("--adjoint-stride", type=int, default=1,
                     help="adjoint checkpoint stride in iterations (2 = every 8 SSPRK steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -412,6 +501,10 @@ def main():
     if args.workload == "batch":
         if rank == 0:
             run_batch(args)
+        return
+    if args.workload == "adjoint":
+        if rank == 0:
+            run_adjoint_check(args)
         return
 
     import torch
