@@ -304,7 +304,7 @@ def run_adjoint_check(args):
         return Cloud(x, y, cloud.left, cloud.right, cloud.flag_1, cloud.flag_2, cloud.min_dist, cloud.nbhs, cloud.conn)
 
     t_fd = time.perf_counter()
-    hm, ha, hw = 1e-6, 1e-5, 3e-8
+    hm, ha, hws = 1e-6, 1e-5, (1e-8, 3e-8)
     fd = {"dmach": {}, "daoa": {}}
     a, b = objective(mach=kw["mach"] + hm), objective(mach=kw["mach"] - hm)
     fd["dmach"] = {o: (a[o] - b[o]) / (2 * hm) for o in ("cl", "cd")}
@@ -313,16 +313,30 @@ def run_adjoint_check(args):
     te = {0, int(cloud.left[0]) - 1, int(cloud.right[0]) - 1}
     rng = np.random.default_rng(16)
     pts = rng.choice(sorted(set(range(shape)) - te), size=16, replace=False)
-    err = {"cl": {"dmach": 0.0, "daoa": 0.0, "dwall": 0.0}, "cd": {"dmach": 0.0, "daoa": 0.0, "dwall": 0.0}}
-    for o in ("cl", "cd"):
-        for key in ("dmach", "daoa"):
-            err[o][key] = abs(grads[o][key] - fd[key][o]) / max(abs(fd[key][o]), 1e-12)
+    err = {o: {"dmach": abs(grads[o]["dmach"] - fd["dmach"][o]) / max(abs(fd["dmach"][o]), 1e-12),
+               "daoa": abs(grads[o]["daoa"] - fd["daoa"][o]) / max(abs(fd["daoa"][o]), 1e-12)} for o in ("cl", "cd")}
+    # each wall point at two steps: a difference quotient that moves with the
+    # step straddles a discontinuity of the map (the limiter's |dn| <= 1e-5
+    # cut, a switch of the time step's minimum), which the adjoint, the
+    # derivative of the branch taken, does not see
+    wall = {o: [] for o in ("cl", "cd")}
     for m in pts:
-        a, b = objective(c=moved(m, hw)), objective(c=moved(m, -hw))
+        q = {o: [] for o in ("cl", "cd")}
+        for hw in hws:
+            a, b = objective(c=moved(m, hw)), objective(c=moved(m, -hw))
+            for o in ("cl", "cd"):
+                q[o].append((a[o] - b[o]) / (2 * hw))
         for o in ("cl", "cd"):
-            f = (a[o] - b[o]) / (2 * hw)
-            scale = np.abs(grads[o]["dwall"]).max()
-            err[o]["dwall"] = max(err[o]["dwall"], abs(grads[o]["dwall"][m] - f) / max(abs(f), 1e-2 * scale))
+            wall[o].append({"point": int(m), "adjoint": float(grads[o]["dwall"][m]), "fd": q[o]})
+    for o in ("cl", "cd"):
+        scale = float(np.abs(grads[o]["dwall"]).max())
+        rel = lambda ad, f: abs(ad - f) / max(abs(f), 1e-2 * scale)
+        err[o]["dwall_step_small"] = max(rel(w["adjoint"], w["fd"][0]) for w in wall[o])
+        err[o]["dwall_step_large"] = max(rel(w["adjoint"], w["fd"][1]) for w in wall[o])
+        # points whose two quotients agree to 1e-3 (no discontinuity within the steps)
+        smooth = [w for w in wall[o] if abs(w["fd"][0] - w["fd"][1]) <= 1e-3 * max(abs(w["fd"][0]), 1e-2 * scale)]
+        err[o]["dwall_smooth_points"] = len(smooth)
+        err[o]["dwall_smooth_max"] = max((rel(w["adjoint"], w["fd"][0]) for w in smooth), default=None)
     t_fd = time.perf_counter() - t_fd
     ratio = max(t_adj.values()) / t_pr
     line = {
@@ -336,7 +350,7 @@ def run_adjoint_check(args):
         "adjoint": {o: {"seconds": t_adj[o], "dmach": grads[o]["dmach"], "daoa_per_deg": grads[o]["daoa"],
                         "dwall_max_abs": float(np.abs(grads[o]["dwall"]).max())} for o in ("cl", "cd")},
         "primal_seconds": t_pr,
-        "fd_check": {"steps": {"mach": hm, "aoa_deg": ha, "wall": hw}, "wall_points": [int(m) for m in pts],
+        "fd_check": {"steps": {"mach": hm, "aoa_deg": ha, "wall": list(hws)}, "wall": wall,
                      "max_rel_err": err, "seconds": t_fd,
                      "note": "central differences of the FP64 solver, K iterations from the free stream"},
     }

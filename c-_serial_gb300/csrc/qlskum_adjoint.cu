@@ -567,30 +567,6 @@ __device__ __forceinline__ void atomic_add4(float4 *p, const float v[4])
 
 __device__ __forceinline__ void ldf4(const float4 &a, float o[4]) { o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; }
 
-// limiters_mod.h:64-104 as the mixed forward evaluates it (venkat32)
-__device__ __forceinline__ float venkat_f(float qt, float q, float qmax, float qmin, float eps2)
-{
-    const float dn = qt - q;
-    const float dp = (dn > 0.f) ? qmax - q : qmin - q;
-    const float dp2 = dp * dp;
-    const float num = fmaf(2.0f * dn, dp, dp2 + eps2);
-    const float den = fmaf(dn, dp, fmaf(2.0f * dn, dn, dp2 + eps2));
-    const float phi = fminf(__fdividef(num, den), 1.0f);
-    return fabsf(dn) <= 10e-6f ? 1.0f : phi;
-}
-
-// reconstructed end q~ of one edge end, as edge_states32 computes it
-__device__ __forceinline__ void qtilde_f(float delx, float dely, const float q[4], const float dx[4],
-                                        const float dy[4], const float mx[4], const float mn[4], float e2, float t[4])
-{
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const float g = fmaf(delx, dx[r], dely * dy[r]);
-        const float phi = venkat_f(fmaf(-0.5f, g, q[r]), q[r], mx[r], mn[r], e2);
-        t[r] = fmaf(-0.5f * phi, g, q[r]);
-    }
-}
-
 __device__ __forceinline__ void x_flux_vjp(int f, const Kin<float> &k, float s1, const float bG[4], KinBarT<float> &kb)
 {
     if (f == kInterior) adj::flux_x_vjp<float>(k, s1, bG, kb);
@@ -603,52 +579,26 @@ __device__ __forceinline__ void x_flux_vjp(int f, const Kin<float> &k, float s1,
 // half-range fluxes it enters, weighted by the folded solve weights (bs: the
 // bar of the owner's weighted sum, signed + for the neighbour end, - for the
 // owner's), back to the end's q, dq and max / min (added to bq ... bmn).
-// The forward quantities are computed once and reused by the reverse: the
-// limiter's dn = -g/2 and dp, the state's beta and 1 / (2 beta) (which is
-// also the moments' p / rho), sqrt(beta) and the moments' exp(-S^2) (taken
-// back from B = exp(-S^2) / (2 sqrt(pi beta))), so the reverse has one
-// division per active limiter component and no other division, exp or log.
-// The same derivatives as the generic reverse-mode functions
-// (qtilde_to_prim_vjp, kin_vjp, edge_end_vjp) up to rounding.
+// The forward quantities come from mixed_end, the forward kernel's own
+// function, once, and are reused by the reverse: the limiter's dn and dp,
+// the state's beta and 1 / (2 beta) (which is also the moments' p / rho),
+// sqrt(beta) and the moments' exp(-S^2) (taken back from
+// B = exp(-S^2) / (2 sqrt(pi beta))), so the reverse has one division per
+// active limiter component and no other division, exp or log.  The same
+// derivatives as the generic reverse-mode functions (qtilde_to_prim_vjp,
+// kin_vjp, edge_end_vjp) up to rounding.
 __device__ __forceinline__ void end_vjp(const DevCloud &c, long long e, int f, float nx, float ny, float delx,
                                         float dely, float2 w, unsigned dir, const float bs[4], const float q[4],
                                         const float dx[4], const float dy[4], const float mx[4], const float mn[4],
                                         float e2, float bq[4], float bdx[4], float bdy[4], float bmx[4], float bmn[4])
 {
-    // reconstruction q~ = q + phi dn, dn = -(delx dqx + dely dqy) / 2 (limiters_mod.h:64-104)
-    float dn[4], dp[4], phi[4], t[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        dn[r] = -0.5f * fmaf(delx, dx[r], dely * dy[r]);
-        dp[r] = ((dn[r] > 0.f) ? mx[r] : mn[r]) - q[r];
-        const float base = fmaf(dp[r], dp[r], e2);
-        const float num = fmaf(2.0f * dn[r], dp[r], base);
-        const float den = fmaf(dn[r], dp[r], fmaf(2.0f * dn[r], dn[r], base));
-        const float ph = fminf(__fdividef(num, den), 1.0f);
-        phi[r] = fabsf(dn[r]) <= 10e-6f ? 1.0f : ph;
-        t[r] = fmaf(phi[r], dn[r], q[r]);
-    }
-    // q~ -> (rho, u1, u2), beta, tm = 1 / (2 beta) = p / rho (q_variables_mod.h:230-253)
-    const float beta = -0.5f * t[3];
-    const float tm = __fdividef(0.5f, beta);
-    const float u1 = t[1] * tm, u2 = t[2] * tm;
-    const float uq = fmaf(u1, u1, u2 * u2);
-    const float rho = __expf(fmaf(beta, uq, t[0]) - 2.5f * __logf(beta));
-    // half-range moments in the (t, n) frame (split_fluxes_mod.h:14-26)
-    const float rsb = rsqrtf(beta), sb = beta * rsb;
-    Kin<float> k;
-    k.ut = u1 * ny - u2 * nx;
-    k.un = u1 * nx + u2 * ny;
-    const float S1 = k.ut * sb, S2 = k.un * sb;
-    const float e1 = __expf(-S1 * S1), e2x = __expf(-S2 * S2);
-    const float rpi = 0.5641895835477563f;  // 1 / sqrt(pi)
-    k.B1 = 0.5f * e1 * rsb * rpi;
-    k.B2 = 0.5f * e2x * rsb * rpi;
-    k.E1 = erf_e<float>(S1, e1);
-    k.E2 = erf_e<float>(S2, e2x);
-    k.pbr = tm;
-    k.usq = fmaf(k.ut, k.ut, k.un * k.un);
-    k.rho = rho;
+    // the forward state of the end (mixed_end: the forward kernel's own function)
+    MixedEnd st;
+    mixed_end(nx, ny, delx, dely, q, dx, dy, mx, mn, e2, st);
+    const Kin<float> &k = st.k;
+    const float *dn = st.dn, *dp = st.dp, *phi = st.phi, *t = st.t;
+    const float beta = st.beta, tm = st.tm, u1 = st.u1, u2 = st.u2, uq = st.uq, rsb = st.rsb, sb = st.sb;
+    const float S1 = st.S1, S2 = st.S2, rho = k.rho;
     // the fluxes' reverse
     KinBarT<float> kb;
     float bG[4];

@@ -374,42 +374,6 @@ __global__ void __launch_bounds__(B) k_q_derivatives_st(DevCloud c, const float4
     if (delta) delta[i] = min_dt;
 }
 
-// limiters_mod.h:64-104 for the FP32 form, without branches: the common
-// factor del_neg of the numerator and the denominator cancels, and the
-// reference's |del_neg| <= 1e-5 cut is a select.
-__device__ __forceinline__ float venkat32(float qt, float q, float qmax, float qmin, float eps2)
-{
-    const float dn = qt - q;
-    const float dp = (dn > 0.f) ? qmax - q : qmin - q;
-    const float dp2 = dp * dp;
-    const float num = fmaf(2.0f * dn, dp, dp2 + eps2);
-    const float den = fmaf(dn, dp, fmaf(2.0f * dn, dn, dp2 + eps2));
-    const float phi = fminf(__fdividef(num, den), 1.0f);
-    return fabsf(dn) <= 10e-6f ? 1.0f : phi;
-}
-
-// Limited reconstruction of both ends of an edge and their primitive states
-// (interior_fluxes_mod.h:50-89), FP32.
-__device__ __forceinline__ void edge_states32(float delx, float dely, const float qi[4], const float dxi[4],
-                                              const float dyi[4], const float mxi[4], const float mni[4],
-                                              float e2i, const float qk[4], const float dxk[4], const float dyk[4],
-                                              const float mxk[4], const float mnk[4], float e2k, float pi_[4],
-                                              float pk_[4])
-{
-    float ti[4], tk[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const float gi = fmaf(delx, dxi[r], dely * dyi[r]);
-        const float gk = fmaf(delx, dxk[r], dely * dyk[r]);
-        const float phi_i = venkat32(fmaf(-0.5f, gi, qi[r]), qi[r], mxi[r], mni[r], e2i);
-        const float phi_k = venkat32(fmaf(-0.5f, gk, qk[r]), qk[r], mxk[r], mnk[r], e2k);
-        ti[r] = fmaf(-0.5f * phi_i, gi, qi[r]);
-        tk[r] = fmaf(-0.5f * phi_k, gk, qk[r]);
-    }
-    qtilde_to_prim(ti, pi_[1], pi_[2], pi_[0], pi_[3]);
-    qtilde_to_prim(tk, pk_[1], pk_[2], pk_[0], pk_[3]);
-}
-
 // x half-range flux of one end: split flux (interior) or the class's
 // quadrant flux (wall: n half-range -, outer: +), t sign s1.
 __device__ __forceinline__ void x_flux(int f, const Kin<float> &k, float s1, float G[4])
@@ -434,11 +398,10 @@ __device__ __forceinline__ void flux_edge(const DevCloud &c, long long e, int f,
                                           unsigned dir, const float qk[4], const float dxk[4], const float dyk[4],
                                           const float mxk[4], const float mnk[4], float e2k, float acc[4])
 {
-    float Pi[4], Pk[4];
-    edge_states32(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, e2k, Pi, Pk);
-    Kin<float> ki, kk;
-    kin_prep<float>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
-    kin_prep<float>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
+    MixedEnd si, sk;
+    mixed_end(nx, ny, g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, si);
+    mixed_end(nx, ny, g.x, g.y, qk, dxk, dyk, mxk, mnk, e2k, sk);
+    const Kin<float> &ki = si.k, &kk = sk.k;
     float Gi[4], Gk[4];
     // x: xpos (s1 = +1) when bit 1 is set, else xneg
     const float s1 = (dir & kXpos) ? 1.0f : -1.0f;
