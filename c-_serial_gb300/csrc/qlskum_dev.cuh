@@ -78,6 +78,8 @@ struct MixedEnd {
     Kin<float> k;
 };
 
+// DQM: mx / mn hold qmax - q / qmin - q already (the owner's end, formed once per point).
+template <bool DQM = false>
 __device__ __forceinline__ void mixed_end(float nx, float ny, float delx, float dely, const float q[4],
                                           const float dx[4], const float dy[4], const float mx[4],
                                           const float mn[4], float e2, MixedEnd &s)
@@ -85,7 +87,7 @@ __device__ __forceinline__ void mixed_end(float nx, float ny, float delx, float 
 #pragma unroll
     for (int r = 0; r < 4; r++) {
         const float dn = -0.5f * fmaf(delx, dx[r], dely * dy[r]);
-        const float dp = ((dn > 0.f) ? mx[r] : mn[r]) - q[r];
+        const float dp = DQM ? ((dn > 0.f) ? mx[r] : mn[r]) : ((dn > 0.f) ? mx[r] : mn[r]) - q[r];
         const float base = fmaf(dp, dp, e2);
         const float num = fmaf(2.0f * dn, dp, base);
         const float den = fmaf(dn, dp, fmaf(2.0f * dn, dn, base));

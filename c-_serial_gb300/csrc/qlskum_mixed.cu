@@ -383,7 +383,8 @@ __device__ __forceinline__ void x_flux(int f, const Kin<float> &k, float s1, flo
 }
 
 // Flux contribution of one edge (interior_fluxes_mod.h, wall_fluxes_mod.h,
-// outer_fluxes_mod.h): reconstruction and limiter at both ends, then the
+// outer_fluxes_mod.h), the owner's mxi / mni given as qmax - q / qmin - q:
+// reconstruction and limiter at both ends, then the
 // edge's x and y half-range fluxes, each difference Gk - Gi weighted by the
 // edge's folded solve weight (DevCloud::e_w32) and added to acc.  Every edge
 // lies in exactly one of xpos / xneg and one of ypos / yneg, except an edge
@@ -399,22 +400,27 @@ __device__ __forceinline__ void flux_edge(const DevCloud &c, long long e, int f,
                                           const float mxk[4], const float mnk[4], float e2k, float acc[4])
 {
     MixedEnd si, sk;
-    mixed_end(nx, ny, g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, si);
+    mixed_end<true>(nx, ny, g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, si);
     mixed_end(nx, ny, g.x, g.y, qk, dxk, dyk, mxk, mnk, e2k, sk);
-    const Kin<float> &ki = si.k, &kk = sk.k;
+    // every component of every split / quadrant flux carries the factor rho:
+    // the fluxes are evaluated with rho = 1 and rho goes into the edge weight
+    Kin<float> ki = si.k, kk = sk.k;
+    ki.rho = 1.0f;
+    kk.rho = 1.0f;
+    const float ri = si.k.rho, rk = sk.k.rho;
     float Gi[4], Gk[4];
     // x: xpos (s1 = +1) when bit 1 is set, else xneg
     const float s1 = (dir & kXpos) ? 1.0f : -1.0f;
     x_flux(f, ki, s1, Gi);
     x_flux(f, kk, s1, Gk);
 #pragma unroll
-    for (int r = 0; r < 4; r++) acc[r] = fmaf(w.x, Gk[r] - Gi[r], acc[r]);
+    for (int r = 0; r < 4; r++) acc[r] = fmaf(w.x * rk, Gk[r], fmaf(-w.x * ri, Gi[r], acc[r]));
     // y: ypos (s2 = +1) when bit 4 is set, else yneg
     const float s2 = (dir & kYpos) ? 1.0f : -1.0f;
     flux_y(ki, s2, Gi);
     flux_y(kk, s2, Gk);
 #pragma unroll
-    for (int r = 0; r < 4; r++) acc[r] = fmaf(w.y, Gk[r] - Gi[r], acc[r]);
+    for (int r = 0; r < 4; r++) acc[r] = fmaf(w.y * rk, Gk[r], fmaf(-w.y * ri, Gi[r], acc[r]));
     const bool xb = (dir & (kXpos | kXneg)) == (kXpos | kXneg), yb = (dir & (kYpos | kYneg)) == (kYpos | kYneg);
     if (xb || yb) {
         const float2 w2 = c.e_w32b[e];
@@ -422,13 +428,13 @@ __device__ __forceinline__ void flux_edge(const DevCloud &c, long long e, int f,
             x_flux(f, ki, -1.0f, Gi);
             x_flux(f, kk, -1.0f, Gk);
 #pragma unroll
-            for (int r = 0; r < 4; r++) acc[r] = fmaf(w2.x, Gk[r] - Gi[r], acc[r]);
+            for (int r = 0; r < 4; r++) acc[r] = fmaf(w2.x * rk, Gk[r], fmaf(-w2.x * ri, Gi[r], acc[r]));
         }
         if (yb) {
             flux_y(ki, -1.0f, Gi);
             flux_y(kk, -1.0f, Gk);
 #pragma unroll
-            for (int r = 0; r < 4; r++) acc[r] = fmaf(w2.y, Gk[r] - Gi[r], acc[r]);
+            for (int r = 0; r < 4; r++) acc[r] = fmaf(w2.y * rk, Gk[r], fmaf(-w2.y * ri, Gi[r], acc[r]));
         }
     }
 }
@@ -492,6 +498,12 @@ __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst 
     ld4(dq[2 * i + 1], dyi);
     ld4(qm[2 * i], mxi);
     ld4(qm[2 * i + 1], mni);
+    // the owner end's limiter reads qmax - q and qmin - q (flux_edge)
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        mxi[r] -= qi[r];
+        mni[r] -= qi[r];
+    }
     const float e2i = c.eps2_32[i];
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     const int nb = c.nbhs[i];
@@ -561,6 +573,12 @@ __device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseCon
     ld4(dq[2 * i + 1], dyi);
     ld4(qm[2 * i], mxi);
     ld4(qm[2 * i + 1], mni);
+    // the owner end's limiter reads qmax - q and qmin - q (flux_edge)
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        mxi[r] -= qi[r];
+        mni[r] -= qi[r];
+    }
     const float e2i = c.eps2_32[i];
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     for (int j = 0; j < nb; j++) {
