@@ -587,7 +587,7 @@ __device__ __forceinline__ void x_flux_vjp(int f, const Kin<float> &k, float s1,
 // active limiter component and no other division, exp or log.  The same
 // derivatives as the generic reverse-mode functions (qtilde_to_prim_vjp,
 // kin_vjp, edge_end_vjp) up to rounding.
-__device__ __forceinline__ void end_vjp(const DevCloud &c, long long e, int f, float nx, float ny, float delx,
+__device__ __forceinline__ void end_vjp(const float2 *w2p, int f, float nx, float ny, float delx,
                                         float dely, float2 w, unsigned dir, const float bs[4], const float q[4],
                                         const float dx[4], const float dy[4], const float mx[4], const float mn[4],
                                         float e2, float bq[4], float bdx[4], float bdy[4], float bmx[4], float bmn[4])
@@ -610,7 +610,7 @@ __device__ __forceinline__ void end_vjp(const DevCloud &c, long long e, int f, f
     adj::flux_y_vjp<float>(k, (dir & kYpos) ? 1.0f : -1.0f, bG, kb);
     const bool xb = (dir & (kXpos | kXneg)) == (kXpos | kXneg), yb = (dir & (kYpos | kYneg)) == (kYpos | kYneg);
     if (xb || yb) {
-        const float2 w2 = c.e_w32b[e];
+        const float2 w2 = *w2p;
         if (xb) {
 #pragma unroll
             for (int r = 0; r < 4; r++) bG[r] = w2.x * bs[r];
@@ -671,20 +671,20 @@ template <bool UW> __device__ __forceinline__ float2 edge_del(const DevCloud &c,
 
 // Reverse of the flux part of the mixed flux + update kernel for stage
 // state (q, dq, qm): F = delta * acc, acc = sum_e w_e (G_k - G_i) over each
-// edge's x and y half-ranges.  The two ends of an edge are independent given
-// the bar of acc, so the owner ends (k_flux_own: the point's own data only,
-// bars kept in registers, and the bar of delta) and the neighbour ends
-// (k_flux_nbr: the neighbour's data gathered, bars scattered with vector
-// reductions) run as two kernels, each holding one end's state.  bF (FP64,
-// from adjk::k_update) in; k_flux_own stores the stage's bars of q, dq and qm
-// (every point's, so they need no zeroing) and k_flux_nbr adds to them.
+// edge's x and y half-ranges.  Given the bar of acc, bs = delta * bF
+// (adjm::k_update), the two ends of an edge are independent, so each point
+// reverses the ends that are its own: the owner ends of its edges (bar
+// -bs_i, its class and normal) and the neighbour ends of the edges that have
+// it as neighbour (bar +bs of the edge's owner, the owner's class and normal),
+// pulled through the transposed list T.  The point's data and bars stay in
+// registers, the bars are stored once (no atomics, no zeroing).
 template <bool UW>
-__global__ void __launch_bounds__(128, 4) k_flux_own(DevCloud c, const float4 *__restrict__ q,
-                                                   const float4 *__restrict__ dq, const float4 *__restrict__ qm,
-                                                   const float *__restrict__ delta, const float4 *__restrict__ acc,
-                                                   const float4 *__restrict__ bF, float4 *__restrict__ bq,
-                                                   float4 *__restrict__ bdq, float4 *__restrict__ bqm,
-                                                   float *__restrict__ bdelta)
+__global__ void __launch_bounds__(128) k_flux(DevCloud c, AdjT T, const float4 *__restrict__ q,
+                                                 const float4 *__restrict__ dq, const float4 *__restrict__ qm,
+                                                 const float *__restrict__ delta, const float4 *__restrict__ acc,
+                                                 const float4 *__restrict__ bF, const float4 *__restrict__ bsum,
+                                                 float4 *__restrict__ bq, float4 *__restrict__ bdq,
+                                                 float4 *__restrict__ bqm, float *__restrict__ bdelta)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
@@ -698,35 +698,73 @@ __global__ void __launch_bounds__(128, 4) k_flux_own(DevCloud c, const float4 *_
     ldf4(qm[2 * i], mxi);
     ldf4(qm[2 * i + 1], mni);
     const float e2i = c.eps2_32[i];
-    const float4 bFi = bF[i];
-    const float4 ac = acc[i];
-    const float dl = delta[i];
+    const float4 bFi = bF[i], ac = acc[i], bsi = bsum[i];
+    (void)delta;
     bdelta[i] += bFi.x * ac.x + bFi.y * ac.y + bFi.z * ac.z + bFi.w * ac.w;
-    const float bs[4] = {-dl * bFi.x, -dl * bFi.y, -dl * bFi.z, -dl * bFi.w};
     float bqi[4] = {0, 0, 0, 0}, bdxi[4] = {0, 0, 0, 0}, bdyi[4] = {0, 0, 0, 0}, bmxi[4] = {0, 0, 0, 0},
           bmni[4] = {0, 0, 0, 0};
-    const int nb = c.nbhs[i];
-    const long long base = c.slice_base[i >> 5] + (i & 31);
-    // the next edge's data one edge ahead in registers
-    float2 dn2 = make_float2(0.f, 0.f), wn = make_float2(0.f, 0.f);
-    unsigned dirn = 0;
-    if (nb > 0) {
-        dn2 = edge_del<UW>(c, base);
-        wn = c.e_w32[base];
-        dirn = c.e_dir[base];
-    }
-    for (int j = 0; j < nb; j++) {
-        const long long e = base + 32LL * j;
-        const float2 d = dn2, w = wn;
-        const unsigned dir = dirn;
-        if (j + 1 < nb) {
-            dn2 = edge_del<UW>(c, e + 32);
-            wn = c.e_w32[e + 32];
-            dirn = c.e_dir[e + 32];
+    // the owner ends of the point's edges, the next edge's data one edge ahead in registers
+    {
+        const float bs[4] = {-bsi.x, -bsi.y, -bsi.z, -bsi.w};
+        const int nb = c.nbhs[i];
+        const long long base = c.slice_base[i >> 5] + (i & 31);
+        float2 dn2 = make_float2(0.f, 0.f), wn = make_float2(0.f, 0.f);
+        unsigned dirn = 0;
+        if (nb > 0) {
+            dn2 = edge_del<UW>(c, base);
+            wn = c.e_w32[base];
+            dirn = c.e_dir[base];
         }
-        end_vjp(c, e, f, nx, ny, d.x, d.y, w, dir, bs, qi, dxi, dyi, mxi, mni, e2i, bqi, bdxi, bdyi, bmxi, bmni);
+        for (int j = 0; j < nb; j++) {
+            const long long e = base + 32LL * j;
+            const float2 d = dn2, w = wn;
+            const unsigned dir = dirn;
+            if (j + 1 < nb) {
+                dn2 = edge_del<UW>(c, e + 32);
+                wn = c.e_w32[e + 32];
+                dirn = c.e_dir[e + 32];
+            }
+            end_vjp(c.e_w32b + e, f, nx, ny, d.x, d.y, w, dir, bs, qi, dxi, dyi, mxi, mni, e2i, bqi, bdxi, bdyi,
+                    bmxi, bmni);
+        }
     }
-    // the first writer of this stage's bars: plain stores (k_flux_nbr adds after)
+    // the neighbour ends of the edges into the point: the next slot's data and
+    // its owner's bar one edge ahead in registers, the owner index two ahead
+    {
+        const int nb = T.nb[i];
+        const long long base = T.sbase[i >> 5] + (i & 31);
+        float4 bn = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 dn2 = make_float2(0.f, 0.f), wn = make_float2(0.f, 0.f), onn = make_float2(0.f, 1.f);
+        unsigned dfn = 0;
+        int en = 0, srcnn = 0;
+        if (nb > 0) {
+            bn = bsum[T.src[base]];
+            dn2 = T.xy[base];
+            wn = T.w[base];
+            onn = T.nrm[base];
+            dfn = T.df[base];
+            en = T.e[base];
+        }
+        if (nb > 1) srcnn = T.src[base + 32];
+        for (int j = 0; j < nb; j++) {
+            const long long t = base + 32LL * j;
+            const float bs[4] = {bn.x, bn.y, bn.z, bn.w};
+            const float2 d = dn2, w = wn, on = onn;
+            const unsigned df = dfn;
+            const int e = en;
+            if (j + 1 < nb) {
+                bn = bsum[srcnn];
+                dn2 = T.xy[t + 32];
+                wn = T.w[t + 32];
+                onn = T.nrm[t + 32];
+                dfn = T.df[t + 32];
+                en = T.e[t + 32];
+            }
+            if (j + 2 < nb) srcnn = T.src[t + 64];
+            end_vjp(c.e_w32b + e, (int)(df >> 4), on.x, on.y, d.x, d.y, w, df & 15u, bs, qi, dxi, dyi, mxi, mni,
+                    e2i, bqi, bdxi, bdyi, bmxi, bmni);
+        }
+    }
     bq[i] = mk4(bqi);
     bdq[2 * i] = mk4(bdxi);
     bdq[2 * i + 1] = mk4(bdyi);
@@ -734,108 +772,35 @@ __global__ void __launch_bounds__(128, 4) k_flux_own(DevCloud c, const float4 *_
     bqm[2 * i + 1] = mk4(bmni);
 }
 
-// The neighbour ends, with the next edge's neighbour data (q, dq, qm: five
-// float4, and eps^2) in flight by cp.async into a two-slot ring of the
-// thread's own shared memory while the current edge is reversed (as the
-// forward's staged flux kernel); the neighbour index two edges ahead and
-// the edge data one edge ahead in registers.
-template <bool UW>
-__global__ void __launch_bounds__(128) k_flux_nbr(DevCloud c, const float4 *__restrict__ q,
-                                                   const float4 *__restrict__ dq, const float4 *__restrict__ qm,
-                                                   const float *__restrict__ delta, const float4 *__restrict__ bF,
-                                                   float4 *__restrict__ bq, float4 *__restrict__ bdq,
-                                                   float4 *__restrict__ bqm)
-{
-    constexpr int B = 128;
-    __shared__ float4 ring[2 * 5 * B];
-    __shared__ float reps[2 * B];
-    const int t = threadIdx.x;
-    const int i = blockIdx.x * B + t;
-    if (i >= c.n) return;
-    const int f = c.flag[i];
-    const double2 nn = c.nrm[i];
-    const float nx = d2f(nn.x), ny = d2f(nn.y);
-    const float4 bFi = bF[i];
-    const float dl = delta[i];
-    const float bs[4] = {dl * bFi.x, dl * bFi.y, dl * bFi.z, dl * bFi.w};
-    const int nb = c.nbhs[i];
-    const long long base = c.slice_base[i >> 5] + (i & 31);
-    auto issue = [&](int j, int k) {
-        float4 *slot = ring + (j & 1) * 5 * B + t;
-        cp_async16(slot, q + k);
-        cp_async16(slot + B, dq + 2 * k);
-        cp_async16(slot + 2 * B, dq + 2 * k + 1);
-        cp_async16(slot + 3 * B, qm + 2 * k);
-        cp_async16(slot + 4 * B, qm + 2 * k + 1);
-        cp_async4(reps + (j & 1) * B + t, c.eps2_32 + k);
-    };
-    int kc = 0, kn = 0;
-    float2 dn2 = make_float2(0.f, 0.f), wn = make_float2(0.f, 0.f);
-    unsigned dirn = 0;
-    if (nb > 0) {
-        kc = c.e_nbr[base];
-        issue(0, kc);
-        dn2 = edge_del<UW>(c, base);
-        wn = c.e_w32[base];
-        dirn = c.e_dir[base];
-    }
-    cp_commit();
-    if (nb > 1) kn = c.e_nbr[base + 32];
-    for (int j = 0; j < nb; j++) {
-        const long long e = base + 32LL * j;
-        const int k = kc;
-        const float2 d = dn2, w = wn;
-        const unsigned dir = dirn;
-        if (j + 1 < nb) {
-            issue(j + 1, kn);
-            kc = kn;
-            dn2 = edge_del<UW>(c, e + 32);
-            wn = c.e_w32[e + 32];
-            dirn = c.e_dir[e + 32];
-        }
-        cp_commit();
-        if (j + 2 < nb) kn = c.e_nbr[e + 64];
-        cp_wait<1>();
-        const float4 *slot = ring + (j & 1) * 5 * B + t;
-        float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
-        ldf4(slot[0], qk);
-        ldf4(slot[B], dxk);
-        ldf4(slot[2 * B], dyk);
-        ldf4(slot[3 * B], mxk);
-        ldf4(slot[4 * B], mnk);
-        const float e2k = reps[(j & 1) * B + t];
-        float bqk[4] = {0, 0, 0, 0}, bdxk[4] = {0, 0, 0, 0}, bdyk[4] = {0, 0, 0, 0}, bmxk[4] = {0, 0, 0, 0},
-              bmnk[4] = {0, 0, 0, 0};
-        end_vjp(c, e, f, nx, ny, d.x, d.y, w, dir, bs, qk, dxk, dyk, mxk, mnk, e2k, bqk, bdxk, bdyk, bmxk, bmnk);
-        atomic_add4(bq + k, bqk);
-        atomic_add4(bdq + 2 * k, bdxk);
-        atomic_add4(bdq + 2 * k + 1, bdyk);
-        atomic_add4(bqm + 2 * k, bmxk);
-        atomic_add4(bqm + 2 * k + 1, bmnk);
-    }
-}
-
-template <bool UW> __device__ __forceinline__ float4 edge_w(const DevCloud &c, long long e)
-{
-    if (UW) {
-        const float2 d = c.e_xy32[e];
-        return make_float4(d.x, d.y, d.x, d.y);
-    }
-    return c.e_geo32[e];
-}
-
 // Reverse of one mixed inner step, dq_out = dq0 + 0.5 (dq_in - A),
 // A = sum_e g_e (d_e.dq_in_k) with the folded solve weights g_e
 // (inner_point of the mixed kernels): the bar of dq_out goes to dq0
-// (accumulated over the steps in bdq0, the point's own entry only), half of
-// it to the point's own dq_in, and through A to the neighbours' dq_in.
-template <bool UW>
-__global__ void k_inner(DevCloud c, const float4 *__restrict__ bdq_out, float4 *__restrict__ bdq_in,
+// (accumulated over the steps in bdq0), half of it to the point's own dq_in,
+// and through A of each edge's owner i to the neighbour's dq_in: the point
+// pulls -0.5 d (g . bdq_out_i) over the edges into it.  Stores bdq_in.
+__global__ void k_inner(DevCloud c, AdjT T, const float4 *__restrict__ bdq_out, float4 *__restrict__ bdq_in,
                         float4 *__restrict__ bdq0, int first)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
-    float bx[4], by[4], bax[4], bay[4];
+    float ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0};
+    const int nb = T.nb[i];
+    const long long base = T.sbase[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long t = base + 32LL * j;
+        const int src = T.src[t];
+        const float2 d = T.xy[t], gw = T.gw[t];
+        float bx[4], by[4];
+        ldf4(bdq_out[2 * src], bx);
+        ldf4(bdq_out[2 * src + 1], by);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const float bu = fmaf(gw.x, bx[r], gw.y * by[r]);
+            ax[r] = fmaf(d.x, bu, ax[r]);
+            ay[r] = fmaf(d.y, bu, ay[r]);
+        }
+    }
+    float bx[4], by[4];
     ldf4(bdq_out[2 * i], bx);
     ldf4(bdq_out[2 * i + 1], by);
     float a0[4] = {0, 0, 0, 0}, a1[4] = {0, 0, 0, 0};
@@ -843,36 +808,18 @@ __global__ void k_inner(DevCloud c, const float4 *__restrict__ bdq_out, float4 *
         ldf4(bdq0[2 * i], a0);
         ldf4(bdq0[2 * i + 1], a1);
     }
+    float ox[4], oy[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
         a0[r] += bx[r];
         a1[r] += by[r];
-        bax[r] = -0.5f * bx[r];
-        bay[r] = -0.5f * by[r];
-        bx[r] *= 0.5f;
-        by[r] *= 0.5f;
+        ox[r] = 0.5f * (bx[r] - ax[r]);
+        oy[r] = 0.5f * (by[r] - ay[r]);
     }
-    bdq0[2 * i] = make_float4(a0[0], a0[1], a0[2], a0[3]);
-    bdq0[2 * i + 1] = make_float4(a1[0], a1[1], a1[2], a1[3]);
-    atomic_add4(bdq_in + 2 * i, bx);
-    atomic_add4(bdq_in + 2 * i + 1, by);
-    const int nb = c.nbhs[i];
-    const long long base = c.slice_base[i >> 5] + (i & 31);
-    for (int j = 0; j < nb; j++) {
-        const long long e = base + 32LL * j;
-        const int k = c.e_nbr[e];
-        const float4 g = edge_w<UW>(c, e);
-        const float2 gw = c.e_gw32[e];
-        float bdxk[4], bdyk[4];
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const float bu = fmaf(gw.x, bax[r], gw.y * bay[r]);
-            bdxk[r] = g.x * bu;
-            bdyk[r] = g.y * bu;
-        }
-        atomic_add4(bdq_in + 2 * k, bdxk);
-        atomic_add4(bdq_in + 2 * k + 1, bdyk);
-    }
+    bdq0[2 * i] = mk4(a0);
+    bdq0[2 * i + 1] = mk4(a1);
+    bdq_in[2 * i] = mk4(ox);
+    bdq_in[2 * i + 1] = mk4(oy);
 }
 
 // Reverse of the mixed gradient and neighbour max / min (q_variables_mod.h:36-118).
@@ -1001,11 +948,13 @@ __global__ void k_wave(int n, const double4_32a *__restrict__ P, const float *__
 // Reverse of one SSPRK stage update (the FP64 update of the mixed flux
 // kernel), evaluated in FP32 on FP64-stored states and bars: bP (the bar of
 // Pout on entry) becomes the update's part of the bar of Pin; bF the bar of
-// the flux residual; stage 4 adds to bPold; outer points add the free-stream
+// the flux residual and bsum = delta * bF the bar of the flux kernel's
+// weighted sum; stage 4 adds to bPold; outer points add the free-stream
 // velocity bars (one FP64 atomic per warp).
 __global__ void k_update(DevCloud c, CaseConst K, const double4_32a *__restrict__ Pin,
                          const double4_32a *__restrict__ Pold, const double4_32a *__restrict__ Pout, int rk,
-                         double4_32a *__restrict__ bP, double4_32a *__restrict__ bPold, float4 *__restrict__ bF,
+                         const float *__restrict__ delta, double4_32a *__restrict__ bP,
+                         double4_32a *__restrict__ bPold, float4 *__restrict__ bF, float4 *__restrict__ bsum,
                          double *__restrict__ buinf)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1023,6 +972,8 @@ __global__ void k_update(DevCloud c, CaseConst K, const double4_32a *__restrict_
                                      bu1, bu2);
         bP[i] = make_double4_32a(f2d(bin[0]), f2d(bin[1]), f2d(bin[2]), f2d(bin[3]));
         bF[i] = make_float4(bf[0], bf[1], bf[2], bf[3]);
+        const float dl = delta[i];
+        bsum[i] = make_float4(dl * bf[0], dl * bf[1], dl * bf[2], dl * bf[3]);
         if (rk == 3) {
             double4_32a acc = bPold[i];
             acc.x += f2d(bo[0]);
@@ -1119,23 +1070,21 @@ namespace adjml {
 
 static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
 
-void flux(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq, const float4 *qm, const float *delta,
-          const float4 *acc, const float4 *bF, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta)
+void flux(const Launch &L, const DevCloud &c, const AdjT &T, const float4 *q, const float4 *dq, const float4 *qm,
+          const float *delta, const float4 *acc, const float4 *bF, const float4 *bs, float4 *bq, float4 *bdq,
+          float4 *bqm, float *bdelta)
 {
     const int g = grid_for(c.n, 128);
-    if (c.unit_w) {
-        adjm::k_flux_own<true><<<g, 128, 0, L.stream>>>(c, q, dq, qm, delta, acc, bF, bq, bdq, bqm, bdelta);
-        adjm::k_flux_nbr<true><<<g, 128, 0, L.stream>>>(c, q, dq, qm, delta, bF, bq, bdq, bqm);
-    } else {
-        adjm::k_flux_own<false><<<g, 128, 0, L.stream>>>(c, q, dq, qm, delta, acc, bF, bq, bdq, bqm, bdelta);
-        adjm::k_flux_nbr<false><<<g, 128, 0, L.stream>>>(c, q, dq, qm, delta, bF, bq, bdq, bqm);
-    }
+    if (c.unit_w)
+        adjm::k_flux<true><<<g, 128, 0, L.stream>>>(c, T, q, dq, qm, delta, acc, bF, bs, bq, bdq, bqm, bdelta);
+    else
+        adjm::k_flux<false><<<g, 128, 0, L.stream>>>(c, T, q, dq, qm, delta, acc, bF, bs, bq, bdq, bqm, bdelta);
 }
 
-void inner(const Launch &L, const DevCloud &c, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0, bool first)
+void inner(const Launch &L, const DevCloud &c, const AdjT &T, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0,
+           bool first)
 {
-    if (c.unit_w) adjm::k_inner<true><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, bdq_out, bdq_in, bdq0, first);
-    else adjm::k_inner<false><<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, bdq_out, bdq_in, bdq0, first);
+    adjm::k_inner<<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, T, bdq_out, bdq_in, bdq0, first);
 }
 
 void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq, const float4 *bdq0,
@@ -1146,9 +1095,11 @@ void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq
 }
 
 void update(const Launch &L, const DevCloud &c, const CaseConst &K, const double4_32a *Pin, const double4_32a *Pold,
-            const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, float4 *bF, double *buinf)
+            const double4_32a *Pout, int rk, const float *delta, double4_32a *bP, double4_32a *bPold, float4 *bF,
+            float4 *bs, double *buinf)
 {
-    adjm::k_update<<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, K, Pin, Pold, Pout, rk, bP, bPold, bF, buinf);
+    adjm::k_update<<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, K, Pin, Pold, Pout, rk, delta, bP, bPold, bF, bs,
+                                                           buinf);
 }
 
 void qvars(const Launch &L, int n, const double4_32a *P, const float4 *bq, double4_32a *bP)

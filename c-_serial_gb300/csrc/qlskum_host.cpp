@@ -1984,6 +1984,8 @@ struct AdjBuf {
     float4 *qm32[4] = {};
     float4 *acc32[4] = {};             // the flux kernel's weighted sums
     float4 *bF32 = nullptr;            // bar of the flux residual
+    float4 *bs32 = nullptr;            // bar of the weighted sums (delta * bF)
+    AdjT T;                            // the edge list transposed (mixed reverse)
     float *delta32 = nullptr, *cs32 = nullptr;
     float4 *bq32 = nullptr, *bdqA32 = nullptr, *bdqB32 = nullptr, *bdq0_32 = nullptr, *bqm32 = nullptr;
     float *bdelta32 = nullptr, *bcs32 = nullptr;
@@ -2028,6 +2030,103 @@ qlskum_status d2h(qlskum_handle *h, void *dst, const void *src, size_t bytes)
 }
 
 void zero(qlskum_handle *h, void *p, size_t bytes) { cudaMemsetAsync(p, 0, bytes, h->L.stream); }
+
+// The forward edge list transposed (AdjT), from the device's own copies of
+// the per-edge data so that the reverse reads exactly what the forward did.
+qlskum_status adj_transpose(qlskum_handle *h)
+{
+    AdjBuf *a = h->adj;
+    const DevCloud &c = h->dc;
+    const int n = h->n, np = h->np, ns = h->nslices;
+    size_t ne = 0;
+    slice_bases(h, &ne);
+    std::vector<long long> sb(ns);
+    std::vector<int> nbh(np), enbr(ne);
+    std::vector<float2> exy(ne), egw(ne), ew(ne);
+    std::vector<uint8_t> edir(ne);
+    std::vector<double2> nrm(np);
+    std::vector<int8_t> flag(np);
+    qlskum_status st;
+    if ((st = d2h(h, sb.data(), c.slice_base, sizeof(long long) * ns))) return st;
+    if ((st = d2h(h, nbh.data(), c.nbhs, sizeof(int) * np))) return st;
+    if ((st = d2h(h, enbr.data(), c.e_nbr, sizeof(int) * ne))) return st;
+    if (c.unit_w) {
+        if ((st = d2h(h, exy.data(), c.e_xy32, sizeof(float2) * ne))) return st;
+    } else {
+        std::vector<float4> g(ne);
+        if ((st = d2h(h, g.data(), c.e_geo32, sizeof(float4) * ne))) return st;
+        for (size_t e = 0; e < ne; e++) exy[e] = make_float2(g[e].x, g[e].y);
+    }
+    if ((st = d2h(h, egw.data(), c.e_gw32, sizeof(float2) * ne))) return st;
+    if ((st = d2h(h, ew.data(), c.e_w32, sizeof(float2) * ne))) return st;
+    if ((st = d2h(h, edir.data(), c.e_dir, ne))) return st;
+    if ((st = d2h(h, nrm.data(), c.nrm, sizeof(double2) * np))) return st;
+    if ((st = d2h(h, flag.data(), c.flag, np))) return st;
+    // incoming counts, then the transposed slices
+    std::vector<int> tnb(np, 0);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < nbh[i]; j++) tnb[enbr[(size_t)(sb[i >> 5] + 32LL * j + (i & 31))]]++;
+    std::vector<long long> tsb(ns);
+    long long tot = 0;
+    for (int s2 = 0; s2 < ns; s2++) {
+        int w = 0;
+        for (int l = 0; l < 32; l++) w = std::max(w, tnb[s2 * 32 + l]);
+        tsb[s2] = tot;
+        tot += 32LL * w;
+    }
+    const size_t nt = (size_t)std::max(tot, 32LL);
+    std::vector<int> tsrc(nt, 0), te(nt, 0);
+    std::vector<float2> txy(nt, make_float2(0, 0)), tgw(nt, make_float2(0, 0)), tw(nt, make_float2(0, 0)),
+        tnrm(nt, make_float2(0, 1));
+    std::vector<uint8_t> tdf(nt, 0);
+    std::vector<int> fill(np, 0);
+    for (int i = 0; i < n; i++) {
+        const float2 on = make_float2((float)nrm[i].x, (float)nrm[i].y);
+        for (int j = 0; j < nbh[i]; j++) {
+            const size_t e = (size_t)(sb[i >> 5] + 32LL * j + (i & 31));
+            const int k = enbr[e];
+            const size_t t = (size_t)(tsb[k >> 5] + 32LL * fill[k]++ + (k & 31));
+            tsrc[t] = i;
+            te[t] = (int)e;
+            txy[t] = exy[e];
+            tgw[t] = egw[e];
+            tw[t] = ew[e];
+            tnrm[t] = on;
+            tdf[t] = (uint8_t)((edir[e] & 15u) | ((unsigned)flag[i] << 4));
+        }
+    }
+    DeviceArena &A = a->arena;
+    long long *d_sb = A.alloc<long long>(ns);
+    int *d_nb = A.alloc<int>(np), *d_src = A.alloc<int>(nt), *d_e = A.alloc<int>(nt);
+    float2 *d_xy = A.alloc<float2>(nt), *d_gw = A.alloc<float2>(nt), *d_w = A.alloc<float2>(nt),
+           *d_nrm = A.alloc<float2>(nt);
+    uint8_t *d_df = A.alloc<uint8_t>(nt);
+    if (A.err != cudaSuccess)
+        return fail(h, QLSKUM_ERR_CUDA, fmt("adjoint transposed edges: %s", cudaGetErrorString(A.err)));
+    auto up = [&](void *dst, const void *src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->L.stream);
+    };
+    CK(h, up(d_sb, tsb.data(), sizeof(long long) * ns));
+    CK(h, up(d_nb, tnb.data(), sizeof(int) * np));
+    CK(h, up(d_src, tsrc.data(), sizeof(int) * nt));
+    CK(h, up(d_e, te.data(), sizeof(int) * nt));
+    CK(h, up(d_xy, txy.data(), sizeof(float2) * nt));
+    CK(h, up(d_gw, tgw.data(), sizeof(float2) * nt));
+    CK(h, up(d_w, tw.data(), sizeof(float2) * nt));
+    CK(h, up(d_nrm, tnrm.data(), sizeof(float2) * nt));
+    CK(h, up(d_df, tdf.data(), nt));
+    CK(h, cudaStreamSynchronize(h->L.stream));
+    a->T.sbase = d_sb;
+    a->T.nb = d_nb;
+    a->T.src = d_src;
+    a->T.e = d_e;
+    a->T.xy = d_xy;
+    a->T.gw = d_gw;
+    a->T.w = d_w;
+    a->T.nrm = d_nrm;
+    a->T.df = d_df;
+    return QLSKUM_OK;
+}
 
 // The adjoint's buffers: the FP64 stage data (need64), the mixed stage data
 // (need32) and the geometry bars (geo), each kept once allocated.
@@ -2074,6 +2173,7 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
         a->cs32 = A.alloc<float>(np);
         a->bq32 = A.alloc<float4>(np);
         a->bF32 = A.alloc<float4>(np);
+        a->bs32 = A.alloc<float4>(np);
         for (auto *p : {&a->bdqA32, &a->bdqB32, &a->bdq0_32, &a->bqm32}) *p = A.alloc<float4>(2 * np);
         a->bdelta32 = A.alloc<float>(np);
         a->bcs32 = A.alloc<float>(np);
@@ -2093,6 +2193,11 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
     }
     // padding rows stay zero (and finite) in every buffer
     for (auto *p : a->P) zero(h, p, sizeof(double4_32a) * np);
+    if (need32) {
+        qlskum_status st = adj_transpose(h);
+        if (st) adj_free(h);
+        return st;
+    }
     return QLSKUM_OK;
 }
 
@@ -2226,13 +2331,13 @@ void adj_iteration_reverse32(qlskum_handle *h, const AdjView &v)
     zero(h, a->bPacc, sizeof(double4_32a) * np);
     zero(h, a->bdelta32, sizeof(float) * np);
     for (int s = 3; s >= 0; s--) {
-        adjml::update(h->L, c, h->K, a->P[s], a->P[0], a->P[s + 1], s + 1, a->bP, a->bPacc, a->bF32, a->buinf);
+        adjml::update(h->L, c, h->K, a->P[s], a->P[0], a->P[s + 1], s + 1, a->delta32, a->bP, a->bPacc, a->bF32,
+                      a->bs32, a->buinf);
         // the flux reverse stores every point's bars of q, dq and qm first
-        adjml::flux(h->L, c, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->delta32, a->acc32[s], a->bF32, a->bq32,
-                    a->bdqA32, a->bqm32, a->bdelta32);
+        adjml::flux(h->L, c, a->T, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->delta32, a->acc32[s], a->bF32,
+                    a->bs32, a->bq32, a->bdqA32, a->bqm32, a->bdelta32);
         for (int j = ni; j >= 1; j--) {
-            zero(h, a->bdqB32, sizeof(float4) * 2 * np);
-            adjml::inner(h->L, c, a->bdqA32, a->bdqB32, a->bdq0_32, j == ni);
+            adjml::inner(h->L, c, a->T, a->bdqA32, a->bdqB32, a->bdq0_32, j == ni);
             std::swap(a->bdqA32, a->bdqB32);
         }
         adjml::grad(h->L, c, a->q32[s], a->bdqA32, ni > 0 ? a->bdq0_32 : nullptr, a->bqm32, a->bq32);

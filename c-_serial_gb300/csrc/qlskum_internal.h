@@ -202,15 +202,40 @@ void objective_J(const Launch &L, int n, const double4_32a *P, double gamma, dou
 // Reverse of the mixed iteration (qlskum_adjoint.cu, FP32 edge work): bars of
 // the FP32 q / dq / qm in float4 arrays (atomically accumulated), of delta in
 // float, of the FP64 states in double4.
+// The forward edge list transposed for the reverse of the mixed iteration:
+// for each point k, the edges (i -> k) that have k as their neighbour, in a
+// sliced ELL like the forward list (slot sbase[k >> 5] + 32 m + (k & 31),
+// m < nb[k]), each slot carrying a copy of the forward edge's data, so a
+// reverse kernel pulls its point's bars from the edges' owners instead of
+// the owners scattering them with atomics.
+struct AdjT {
+    const long long *sbase = nullptr;  // [nslices]
+    const int *nb = nullptr;           // [np] incoming edges
+    const int *src = nullptr;          // the edge's owner i
+    const int *e = nullptr;            // the forward slot (for the rare second flux weight)
+    const float2 *xy = nullptr;        // the edge vector x_k - x_i
+    const float2 *gw = nullptr;        // folded gradient weights (DevCloud::e_gw32)
+    const float2 *w = nullptr;         // folded flux weights (DevCloud::e_w32)
+    const float2 *nrm = nullptr;       // the owner's normal
+    const uint8_t *df = nullptr;       // direction bits | the owner's class << 4
+};
+
 namespace adjml {
-// reverse of the stage update (rk 1..4 as the forward), FP32 arithmetic
+// reverse of the stage update (rk 1..4 as the forward), FP32 arithmetic; also
+// bs = delta * bF, the bar of each point's weighted flux sum
 void update(const Launch &L, const DevCloud &c, const CaseConst &K, const double4_32a *Pin, const double4_32a *Pold,
-            const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, float4 *bF, double *buinf);
-void flux(const Launch &L, const DevCloud &c, const float4 *q, const float4 *dq, const float4 *qm, const float *delta,
-          const float4 *acc, const float4 *bF, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta);
-// reverse of one mixed inner step: bdq_in += ..., bdq0 += bdq_out (the dq0 term; = for the
-// stage's first reverse step)
-void inner(const Launch &L, const DevCloud &c, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0, bool first);
+            const double4_32a *Pout, int rk, const float *delta, double4_32a *bP, double4_32a *bPold, float4 *bF,
+            float4 *bs, double *buinf);
+// reverse of the flux part: stores every point's bars of q, dq and qm (both
+// ends of the edges it owns and the ends of the edges that have it as
+// neighbour, pulled through T), adds to bdelta
+void flux(const Launch &L, const DevCloud &c, const AdjT &T, const float4 *q, const float4 *dq, const float4 *qm,
+          const float *delta, const float4 *acc, const float4 *bF, const float4 *bs, float4 *bq, float4 *bdq,
+          float4 *bqm, float *bdelta);
+// reverse of one mixed inner step: stores bdq_in, bdq0 += bdq_out (the dq0
+// term; = for the stage's first reverse step)
+void inner(const Launch &L, const DevCloud &c, const AdjT &T, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0,
+           bool first);
 // reverse of the gradient and max / min; the gradient's bar is bdq + bdq0
 void grad(const Launch &L, const DevCloud &c, const float4 *q, const float4 *bdq, const float4 *bdq0,
           const float4 *bqm, float4 *bq);
