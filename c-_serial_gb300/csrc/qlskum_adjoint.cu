@@ -681,8 +681,8 @@ template <bool UW> __device__ __forceinline__ float2 edge_del(const DevCloud &c,
 template <bool UW>
 __global__ void __launch_bounds__(128) k_flux(DevCloud c, AdjT T, const float4 *__restrict__ q,
                                                  const float4 *__restrict__ dq, const float4 *__restrict__ qm,
-                                                 const float *__restrict__ delta, const float4 *__restrict__ acc,
-                                                 const float4 *__restrict__ bF, const float4 *__restrict__ bsum,
+                                                 const float4 *__restrict__ acc, const float4 *__restrict__ bF,
+                                                 const float4 *__restrict__ bsum,
                                                  float4 *__restrict__ bq, float4 *__restrict__ bdq,
                                                  float4 *__restrict__ bqm, float *__restrict__ bdelta)
 {
@@ -699,7 +699,6 @@ __global__ void __launch_bounds__(128) k_flux(DevCloud c, AdjT T, const float4 *
     ldf4(qm[2 * i + 1], mni);
     const float e2i = c.eps2_32[i];
     const float4 bFi = bF[i], ac = acc[i], bsi = bsum[i];
-    (void)delta;
     bdelta[i] += bFi.x * ac.x + bFi.y * ac.y + bFi.z * ac.z + bFi.w * ac.w;
     float bqi[4] = {0, 0, 0, 0}, bdxi[4] = {0, 0, 0, 0}, bdyi[4] = {0, 0, 0, 0}, bmxi[4] = {0, 0, 0, 0},
           bmni[4] = {0, 0, 0, 0};
@@ -1071,14 +1070,11 @@ namespace adjml {
 static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
 
 void flux(const Launch &L, const DevCloud &c, const AdjT &T, const float4 *q, const float4 *dq, const float4 *qm,
-          const float *delta, const float4 *acc, const float4 *bF, const float4 *bs, float4 *bq, float4 *bdq,
-          float4 *bqm, float *bdelta)
+          const float4 *acc, const float4 *bF, const float4 *bs, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta)
 {
     const int g = grid_for(c.n, 128);
-    if (c.unit_w)
-        adjm::k_flux<true><<<g, 128, 0, L.stream>>>(c, T, q, dq, qm, delta, acc, bF, bs, bq, bdq, bqm, bdelta);
-    else
-        adjm::k_flux<false><<<g, 128, 0, L.stream>>>(c, T, q, dq, qm, delta, acc, bF, bs, bq, bdq, bqm, bdelta);
+    if (c.unit_w) adjm::k_flux<true><<<g, 128, 0, L.stream>>>(c, T, q, dq, qm, acc, bF, bs, bq, bdq, bqm, bdelta);
+    else adjm::k_flux<false><<<g, 128, 0, L.stream>>>(c, T, q, dq, qm, acc, bF, bs, bq, bdq, bqm, bdelta);
 }
 
 void inner(const Launch &L, const DevCloud &c, const AdjT &T, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0,

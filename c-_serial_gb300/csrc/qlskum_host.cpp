@@ -2334,8 +2334,8 @@ void adj_iteration_reverse32(qlskum_handle *h, const AdjView &v)
         adjml::update(h->L, c, h->K, a->P[s], a->P[0], a->P[s + 1], s + 1, a->delta32, a->bP, a->bPacc, a->bF32,
                       a->bs32, a->buinf);
         // the flux reverse stores every point's bars of q, dq and qm first
-        adjml::flux(h->L, c, a->T, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->delta32, a->acc32[s], a->bF32,
-                    a->bs32, a->bq32, a->bdqA32, a->bqm32, a->bdelta32);
+        adjml::flux(h->L, c, a->T, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->acc32[s], a->bF32, a->bs32,
+                    a->bq32, a->bdqA32, a->bqm32, a->bdelta32);
         for (int j = ni; j >= 1; j--) {
             adjml::inner(h->L, c, a->T, a->bdqA32, a->bdqB32, a->bdq0_32, j == ni);
             std::swap(a->bdqA32, a->bdqB32);

@@ -230,8 +230,7 @@ void update(const Launch &L, const DevCloud &c, const CaseConst &K, const double
 // ends of the edges it owns and the ends of the edges that have it as
 // neighbour, pulled through T), adds to bdelta
 void flux(const Launch &L, const DevCloud &c, const AdjT &T, const float4 *q, const float4 *dq, const float4 *qm,
-          const float *delta, const float4 *acc, const float4 *bF, const float4 *bs, float4 *bq, float4 *bdq,
-          float4 *bqm, float *bdelta);
+          const float4 *acc, const float4 *bF, const float4 *bs, float4 *bq, float4 *bdq, float4 *bqm, float *bdelta);
 // reverse of one mixed inner step: stores bdq_in, bdq0 += bdq_out (the dq0
 // term; = for the stage's first reverse step)
 void inner(const Launch &L, const DevCloud &c, const AdjT &T, const float4 *bdq_out, float4 *bdq_in, float4 *bdq0,
