@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(256) k_objective(DevCloud c, const double4_32a
         V = cp * nn.y * w.x;
         Mo = (-cp * nn.y * w.x * w.y + cp * nn.x * w.x * w.z);
     }
-    if (t < c.n) {
+    if (entropy && t < c.n) {
         const double4_32a P = prim[t];
         double temp1 = pow(P.x, gamma);
         temp1 = P.w / temp1;
@@ -602,6 +602,33 @@ void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
     QLSKUM_LAUNCHED(L);
 }
 
+// out[0] += sum of src.y, out[1] += sum of src.z over the n points (warp
+// sums, one atomic per warp).
+__global__ void k_sum_yz(int n, const double4_32a *__restrict__ src, double *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double a = 0.0, b = 0.0;
+    if (i < n) {
+        const double4_32a v = src[i];
+        a = v.y;
+        b = v.z;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out, a);
+        atomicAdd(out + 1, b);
+    }
+}
+
+void sum_yz(const Launch &L, int n, const double4_32a *src, double *out)
+{
+    k_sum_yz<<<grid_for(n, 256), 256, 0, L.stream>>>(n, src, out);
+    QLSKUM_LAUNCHED(L);
+}
+
 void permute_in(const Launch &L, int n, const int *perm, const double4_32a *src, double4_32a *dst)
 {
     k_permute_in<<<grid_for(n, 256), 256, 0, L.stream>>>(n, perm, src, dst);
@@ -636,7 +663,8 @@ void objective(const Launch &L, const DevCloud &c, const double4_32a *prim, cons
                const double4_32a *wall_geo, int n_wall, double cp_scale, double pr_inf, double gamma, double *entropy,
                double *out4, double *scratch)
 {
-    const int items = c.n > n_wall ? c.n : n_wall;
+    // entropy NULL: the force coefficients only (the wall points)
+    const int items = (entropy && c.n > n_wall) ? c.n : n_wall;
     const int blocks = grid_for(items, 256);
     k_objective<<<blocks, 256, 0, L.stream>>>(c, prim, wall_perm, wall_geo, n_wall, cp_scale, pr_inf, gamma, entropy,
                                               scratch);

@@ -1953,6 +1953,17 @@ qlskum_status qlskum_read_restart(qlskum_handle *h, const char *path)
 // the FP64 reverse; Mach / AoA / initial-state gradients of a mixed handle
 // take the reverse of the mixed iteration (FP32 edge work, FP64 update).
 
+// One iteration's stage data of the mixed form (FP32) with its five stage
+// states: what the reverse of that iteration reads.
+struct Set32 {
+    double4_32a *P[5] = {};
+    float4 *q32[4] = {};
+    std::vector<float4 *> dq32;        // [stage][inner step 0 .. ni], each [np][2]
+    float4 *qm32[4] = {};
+    float4 *acc32[4] = {};             // the flux kernel's weighted sums
+    float *delta32 = nullptr, *cs32 = nullptr;
+};
+
 struct AdjBuf {
     DeviceArena arena;
     int ni = 0;
@@ -1978,15 +1989,14 @@ struct AdjBuf {
     int ckpt_cap = 0;
     double4_32a *seg = nullptr;
     int seg_cap = 0;
-    // the mixed iteration's stage data (FP32) and bars
-    float4 *q32[4] = {};
-    std::vector<float4 *> dq32;        // [stage][inner step 0 .. ni], each [np][2]
-    float4 *qm32[4] = {};
-    float4 *acc32[4] = {};             // the flux kernel's weighted sums
+    // the mixed iteration's stage data (FP32): set 0 (its states are P) and,
+    // on demand, one set per iteration of a segment (own states, own arena)
+    Set32 set0;
+    std::vector<Set32> sets;
+    DeviceArena set_arena;
     float4 *bF32 = nullptr;            // bar of the flux residual
     float4 *bs32 = nullptr;            // bar of the weighted sums (delta * bF)
     AdjT T;                            // the edge list transposed (mixed reverse)
-    float *delta32 = nullptr, *cs32 = nullptr;
     float4 *bq32 = nullptr, *bdqA32 = nullptr, *bdqB32 = nullptr, *bdq0_32 = nullptr, *bqm32 = nullptr;
     float *bdelta32 = nullptr, *bcs32 = nullptr;
 };
@@ -1996,6 +2006,7 @@ void adj_free(qlskum_handle *h)
     if (!h->adj) return;
     if (h->adj->ckpt) cudaFree(h->adj->ckpt);
     if (h->adj->seg) cudaFree(h->adj->seg);
+    h->adj->set_arena.release();
     h->adj->arena.release();
     delete h->adj;
     h->adj = nullptr;
@@ -2128,6 +2139,24 @@ qlskum_status adj_transpose(qlskum_handle *h)
     return QLSKUM_OK;
 }
 
+// The FP32 arrays of one stage-data set (its states are assigned by the caller).
+void alloc_set32(DeviceArena &A, size_t np, int ni, Set32 &st)
+{
+    for (auto &p : st.q32) p = A.alloc<float4>(np);
+    for (auto &p : st.qm32) p = A.alloc<float4>(2 * np);
+    for (auto &p : st.acc32) p = A.alloc<float4>(np);
+    st.dq32.resize(4 * (size_t)(ni + 1));
+    for (auto &p : st.dq32) p = A.alloc<float4>(2 * np);
+    st.delta32 = A.alloc<float>(np);
+    st.cs32 = A.alloc<float>(np);
+}
+
+// Bytes of one set with its own states.
+size_t set32_bytes(size_t np, int ni)
+{
+    return np * (5 * sizeof(double4_32a) + 4 * 16 + 4 * 32 + 4 * 16 + 4 * (size_t)(ni + 1) * 32 + 8);
+}
+
 // The adjoint's buffers: the FP64 stage data (need64), the mixed stage data
 // (need32) and the geometry bars (geo), each kept once allocated.
 qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
@@ -2150,7 +2179,7 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
     a->has32 = need32;
     for (auto &p : a->P) p = A.alloc<double4_32a>(np);
     for (auto *p : {&a->bP, &a->bPacc, &a->bF, &a->lam, &a->lam_prev, &a->seed}) *p = A.alloc<double4_32a>(np);
-    a->buinf = A.alloc<double>(2);
+    a->buinf = A.alloc<double>(4);  // free-stream velocity bars, then the initial-state sums
     if (need64) {
         for (auto &p : a->q) p = A.alloc<double4_32a>(np);
         for (auto &p : a->qm) p = A.alloc<double4_32a>(2 * np);
@@ -2164,13 +2193,8 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
         a->bc = A.alloc<double>(np);
     }
     if (need32) {
-        for (auto &p : a->q32) p = A.alloc<float4>(np);
-        for (auto &p : a->qm32) p = A.alloc<float4>(2 * np);
-        for (auto &p : a->acc32) p = A.alloc<float4>(np);
-        a->dq32.resize(4 * (size_t)(a->ni + 1));
-        for (auto &p : a->dq32) p = A.alloc<float4>(2 * np);
-        a->delta32 = A.alloc<float>(np);
-        a->cs32 = A.alloc<float>(np);
+        alloc_set32(A, np, a->ni, a->set0);
+        for (int k = 0; k < 5; k++) a->set0.P[k] = a->P[k];
         a->bq32 = A.alloc<float4>(np);
         a->bF32 = A.alloc<float4>(np);
         a->bs32 = A.alloc<float4>(np);
@@ -2294,35 +2318,72 @@ void adj_iteration_reverse64(qlskum_handle *h, const AdjView &v)
     fp64::add_prim(h->L, h->n, a->bPacc, a->bP);
 }
 
-float4 *adj_dq32(AdjBuf *a, int s, int j) { return a->dq32[(size_t)s * (a->ni + 1) + j]; }
+float4 *adj_dq32(const Set32 &st, int ni, int s, int j) { return st.dq32[(size_t)s * (ni + 1) + j]; }
 
-// The mixed iteration from a->P[0] with the solver's own kernels and launch
-// shapes (enqueue_iteration), every stage's FP32 data kept: q, the gradient
-// after each inner step, max / min, the flux kernel's weighted sums, the
-// local time step and the wave speed it came from.
-void adj_iteration_forward32(qlskum_handle *h)
+// `count` sets with their own states for a segment's iterations (first use
+// and growth only); false when they do not fit.
+bool adj_sets(qlskum_handle *h, int count)
+{
+    AdjBuf *a = h->adj;
+    if ((int)a->sets.size() >= count) return true;
+    a->sets.clear();
+    a->set_arena.release();
+    a->set_arena.err = cudaSuccess;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
+    // keep a quarter of the free memory for everything else
+    if ((double)set32_bytes(h->np, a->ni) * count > 0.75 * (double)free_b) return false;
+    a->sets.resize(count);
+    for (auto &st : a->sets) {
+        alloc_set32(a->set_arena, h->np, a->ni, st);
+        for (auto &p : st.P) p = a->set_arena.alloc<double4_32a>(h->np);
+    }
+    if (a->set_arena.err != cudaSuccess) {
+        cudaGetLastError();
+        a->sets.clear();
+        a->set_arena.release();
+        a->set_arena.err = cudaSuccess;
+        return false;
+    }
+    for (auto &st : a->sets) zero(h, st.P[0], sizeof(double4_32a) * h->np);
+    return true;
+}
+
+// The mixed iteration from st.P[0] with the solver's own kernels and launch
+// shapes (enqueue_iteration), every stage's FP32 data kept in `st`: q, the
+// gradient after each inner step, max / min, the flux kernel's weighted
+// sums, the local time step and the wave speed it came from.  it_rec > 0:
+// the iteration is the primal's own iteration it_rec (its residual row is
+// reduced and recorded, as qlskum_fpi_solver does).
+void adj_iteration_forward32(qlskum_handle *h, Set32 &st, int it_rec = 0)
 {
     AdjBuf *a = h->adj;
     const DevCloud &c = h->dc;
     const int ni = a->ni;
     Reduce none = h->R;
     none.partial_sum = none.partial_max = nullptr;
-    mixed::derived(h->L, c, a->P[0], a->q32[0], a->cs32);
+    mixed::derived(h->L, c, st.P[0], st.q32[0], st.cs32);
     for (int s = 0; s < 4; s++) {
-        mixed::q_derivatives(h->L, c, a->q32[s], adj_dq32(a, s, 0), a->qm32[s], a->cs32, s == 0 ? a->delta32 : nullptr,
-                             (float)h->K.cfl);
+        mixed::q_derivatives(h->L, c, st.q32[s], adj_dq32(st, ni, s, 0), st.qm32[s], st.cs32,
+                             s == 0 ? st.delta32 : nullptr, (float)h->K.cfl);
         for (int j = 1; j <= ni; j++)
-            mixed::q_inner(h->L, c, adj_dq32(a, s, 0), adj_dq32(a, s, j - 1), adj_dq32(a, s, j));
-        // the last stage's q goes to the bar buffer, which the reverse zeroes before use
-        float4 *q_next = s < 3 ? a->q32[s + 1] : a->bq32;
-        mixed::flux_update(h->L, c, h->K, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->delta32, a->P[s], a->P[0],
-                           a->P[s + 1], q_next, nullptr, s + 1, none, h->flux_variant, a->acc32[s]);
+            mixed::q_inner(h->L, c, adj_dq32(st, ni, s, 0), adj_dq32(st, ni, s, j - 1), adj_dq32(st, ni, s, j));
+        // the last stage's q goes to the bar buffer, which the reverse overwrites
+        float4 *q_next = s < 3 ? st.q32[s + 1] : a->bq32;
+        mixed::flux_update(h->L, c, h->K, st.q32[s], adj_dq32(st, ni, s, ni), st.qm32[s], st.delta32, st.P[s],
+                           st.P[0], st.P[s + 1], q_next, nullptr, s + 1, (it_rec > 0 && s == 3) ? h->R : none,
+                           h->flux_variant, st.acc32[s]);
+    }
+    if (it_rec > 0) {
+        Reduce R = h->R;
+        R.blocks = (h->n + mixed::flux_block(h->flux_variant) - 1) / mixed::flux_block(h->flux_variant);
+        fp64::reduce_residual(h->L, R, h->n, it_rec);
     }
 }
 
-// Reverse of adj_iteration_forward32 (same contract as the FP64 reverse,
-// without geometry bars).
-void adj_iteration_reverse32(qlskum_handle *h, const AdjView &v)
+// Reverse of adj_iteration_forward32 for the stage data in `st` (same
+// contract as the FP64 reverse, without geometry bars).
+void adj_iteration_reverse32(qlskum_handle *h, const Set32 &st)
 {
     AdjBuf *a = h->adj;
     const size_t np = h->np;
@@ -2331,20 +2392,20 @@ void adj_iteration_reverse32(qlskum_handle *h, const AdjView &v)
     zero(h, a->bPacc, sizeof(double4_32a) * np);
     zero(h, a->bdelta32, sizeof(float) * np);
     for (int s = 3; s >= 0; s--) {
-        adjml::update(h->L, c, h->K, a->P[s], a->P[0], a->P[s + 1], s + 1, a->delta32, a->bP, a->bPacc, a->bF32,
+        adjml::update(h->L, c, h->K, st.P[s], st.P[0], st.P[s + 1], s + 1, st.delta32, a->bP, a->bPacc, a->bF32,
                       a->bs32, a->buinf);
         // the flux reverse stores every point's bars of q, dq and qm first
-        adjml::flux(h->L, c, a->T, a->q32[s], adj_dq32(a, s, ni), a->qm32[s], a->acc32[s], a->bF32, a->bs32,
+        adjml::flux(h->L, c, a->T, st.q32[s], adj_dq32(st, ni, s, ni), st.qm32[s], st.acc32[s], a->bF32, a->bs32,
                     a->bq32, a->bdqA32, a->bqm32, a->bdelta32);
         for (int j = ni; j >= 1; j--) {
             adjml::inner(h->L, c, a->T, a->bdqA32, a->bdqB32, a->bdq0_32, j == ni);
             std::swap(a->bdqA32, a->bdqB32);
         }
-        adjml::grad(h->L, c, a->q32[s], a->bdqA32, ni > 0 ? a->bdq0_32 : nullptr, a->bqm32, a->bq32);
-        adjml::qvars(h->L, h->n, a->P[s], a->bq32, a->bP);
+        adjml::grad(h->L, c, st.q32[s], a->bdqA32, ni > 0 ? a->bdq0_32 : nullptr, a->bqm32, a->bq32);
+        adjml::qvars(h->L, h->n, st.P[s], a->bq32, a->bP);
     }
     zero(h, a->bcs32, sizeof(float) * np);
-    adjml::delta(h->L, c, a->P[0], a->cs32, a->bdelta32, (float)h->K.cfl, a->bcs32, a->bPacc);
+    adjml::delta(h->L, c, st.P[0], st.cs32, a->bdelta32, (float)h->K.cfl, a->bcs32, a->bPacc);
     fp64::add_prim(h->L, h->n, a->bPacc, a->bP);
 }
 
@@ -2354,13 +2415,13 @@ bool adj_use32(const qlskum_handle *h, bool geo) { return h->prm.precision == QL
 
 void adj_iteration_forward(qlskum_handle *h, bool m32)
 {
-    if (m32) adj_iteration_forward32(h);
+    if (m32) adj_iteration_forward32(h, h->adj->set0);
     else adj_iteration_forward64(h);
 }
 
 void adj_iteration_reverse(qlskum_handle *h, const AdjView &v, bool m32)
 {
-    if (m32) adj_iteration_reverse32(h, v);
+    if (m32) adj_iteration_reverse32(h, h->adj->set0);
     else adj_iteration_reverse64(h, v);
 }
 
@@ -2395,7 +2456,7 @@ qlskum_status adj_seed(qlskum_handle *h, int which, const double4_32a *prim, dou
     }
     const double cp_scale = 0.5 * h->K.rho_inf * h->K.mach * h->K.mach;
     fp64::objective(h->L, h->dc, prim, h->d_wall_perm, h->d_wall_geo, h->shape_points, cp_scale, h->K.pr_inf,
-                    h->K.gamma, h->d_entropy, h->d_obj, h->d_obj_partial);
+                    h->K.gamma, nullptr, h->d_obj, h->d_obj_partial);
     adjl::objective(h->L, adj_view(h, false), h->d_wall_perm, h->d_wall_geo, h->shape_points, cp_scale, h->K.theta,
                     which, bP);
     if ((st = check_launch(h, "adjoint seed"))) return st;
@@ -2673,6 +2734,13 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     const bool m32 = adj_use32(h, dJ_dwall != nullptr);
     const int S = std::max(1, h->adj_stride);
     const int nck = (iters + S - 1) / S;
+    // mixed handles keep each iteration's stage data in its own set where the
+    // sets fit: with stride 1 all `iters` of them (the primal then runs as the
+    // recording iteration and nothing is recomputed), with a larger stride one
+    // segment's (each segment recomputed once); otherwise set 0 is refilled
+    // for every iteration of the reverse sweep
+    const bool store_all = m32 && S == 1 && adj_sets(h, iters);
+    const bool seg_sets = m32 && !store_all && S > 1 && adj_sets(h, S);
     auto grow = [&](double4_32a *&buf, int &cap, int want, const char *what) -> qlskum_status {
         if (cap >= want) return QLSKUM_OK;
         if (buf) cudaFree(buf);
@@ -2685,8 +2753,8 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
         cap = want;
         return QLSKUM_OK;
     };
-    if ((st = grow(a->ckpt, a->ckpt_cap, nck, "adjoint checkpoints"))) return st;
-    if (S > 1 && (st = grow(a->seg, a->seg_cap, S, "adjoint segment"))) return st;
+    if (!store_all && (st = grow(a->ckpt, a->ckpt_cap, nck, "adjoint checkpoints"))) return st;
+    if (S > 1 && !seg_sets && (st = grow(a->seg, a->seg_cap, S, "adjoint segment"))) return st;
     // primal from prim0 or the free stream (initial_conditions_mod.h:23-37),
     // every S-th iteration's starting state kept
     if (prim0) {
@@ -2700,22 +2768,55 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     CK(h, cudaMemsetAsync(h->R.status, 0, sizeof(int), h->L.stream));
     h->derived_valid = false;
     h->it = 0;
-    for (int t = 0; t < iters; t++) {
-        if (t % S == 0)
-            CK(h, cudaMemcpyAsync(a->ckpt + np * (size_t)(t / S), h->s64.prim[h->pcur], sizeof(double4_32a) * np,
-                                  cudaMemcpyDeviceToDevice, h->L.stream));
-        if ((st = qlskum_fpi_solver(h, t + 1))) return st;
+    const size_t bytes = sizeof(double4_32a) * np;
+    if (store_all) {
+        // the primal's iterations as the recording iteration (the same kernels,
+        // launch shapes and residual rows as qlskum_fpi_solver), each into its set
+        if ((st = ensure_hist(h, iters))) return st;
+        if ((st = ensure_derived(h))) return st;
+        const int o = h->pcur;
+        for (int t = 0; t < iters; t++) {
+            const double4_32a *from = t == 0 ? h->s64.prim[o] : a->sets[t - 1].P[4];
+            CK(h, cudaMemcpyAsync(a->sets[t].P[0], from, bytes, cudaMemcpyDeviceToDevice, h->L.stream));
+            adj_iteration_forward32(h, a->sets[t], t + 1);
+        }
+        // the handle as after qlskum_q_lskum(iters): state and prim_old of the last iteration
+        CK(h, cudaMemcpyAsync(h->s64.prim[o], a->sets[iters - 1].P[0], bytes, cudaMemcpyDeviceToDevice,
+                              h->L.stream));
+        CK(h, cudaMemcpyAsync(h->s64.prim[(o + 2) % 3], a->sets[iters - 1].P[4], bytes, cudaMemcpyDeviceToDevice,
+                              h->L.stream));
+        after_iteration(h, o);
+        h->derived_valid = false;
+        h->it = iters;
+        if ((st = check_launch(h, "adjoint primal"))) return st;
+        if (h->prm.verbose && (st = print_iters(h, 0, iters))) return st;
+    } else {
+        for (int t = 0; t < iters; t++) {
+            if (t % S == 0)
+                CK(h, cudaMemcpyAsync(a->ckpt + np * (size_t)(t / S), h->s64.prim[h->pcur], bytes,
+                                      cudaMemcpyDeviceToDevice, h->L.stream));
+            if ((st = qlskum_fpi_solver(h, t + 1))) return st;
+        }
     }
     if ((st = check_status(h))) return st;
     ObjSeed os;
     if ((st = adj_seed(h, objective, h->s64.prim[h->pcur], a->bP, os))) return st;
     adj_zero_geometry(h);
     const AdjView v = adj_view(h, true);
-    const size_t bytes = sizeof(double4_32a) * np;
-    for (int c0 = nck - 1; c0 >= 0; c0--) {
+    for (int c0 = store_all ? -1 : nck - 1; c0 >= 0; c0--) {
         const int t0 = c0 * S, t1 = std::min(iters, t0 + S);
         // states t0 .. t1 - 1 of this segment: the checkpoint, then the reverse's own iterations from it
         const double4_32a *state_at0 = a->ckpt + np * (size_t)c0;
+        if (seg_sets) {
+            // the segment's iterations once, each into its set, then reversed
+            for (int t = t0; t < t1; t++) {
+                const double4_32a *from = t == t0 ? state_at0 : a->sets[t - 1 - t0].P[4];
+                CK(h, cudaMemcpyAsync(a->sets[t - t0].P[0], from, bytes, cudaMemcpyDeviceToDevice, h->L.stream));
+                adj_iteration_forward32(h, a->sets[t - t0]);
+            }
+            for (int t = t1 - 1; t >= t0; t--) adj_iteration_reverse32(h, a->sets[t - t0]);
+            continue;
+        }
         if (S > 1) {
             CK(h, cudaMemcpyAsync(a->seg, state_at0, bytes, cudaMemcpyDeviceToDevice, h->L.stream));
             for (int t = t0 + 1; t < t1; t++) {
@@ -2733,22 +2834,20 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
             adj_iteration_reverse(h, v, m32);
         }
     }
+    if (store_all)
+        for (int t = iters - 1; t >= 0; t--) adj_iteration_reverse32(h, a->sets[t]);
     if ((st = check_launch(h, "adjoint sweep"))) return st;
     // bar of the initial state: returned for prim0, else (the free stream)
-    // summed over the points into the free-stream velocity
-    std::vector<double4_32a> b0(np);
-    double bu[2];
-    if ((st = d2h(h, b0.data(), a->bP, sizeof(double4_32a) * np))) return st;
-    if ((st = d2h(h, bu, a->buinf, sizeof bu))) return st;
-    double binit[2] = {0, 0};
+    // summed over the points into the free-stream velocity (on the device)
+    double bu[2], binit[2] = {0, 0};
     if (!prim0) {
-        for (int pp = 0; pp < h->n; pp++) {
-            binit[0] += b0[pp].y;
-            binit[1] += b0[pp].z;
-        }
+        double *d_init = a->buinf + 2;
+        zero(h, d_init, 2 * sizeof(double));
+        fp64::sum_yz(h->L, h->n, a->bP, d_init);
+        if ((st = d2h(h, binit, d_init, sizeof binit))) return st;
     }
-    if (dJ_dprim0)
-        for (int i = 0; i < h->n; i++) std::memcpy(dJ_dprim0 + 4 * (size_t)i, &b0[h->perm[i]], sizeof(double4_32a));
+    if ((st = d2h(h, bu, a->buinf, sizeof bu))) return st;
+    if (dJ_dprim0 && (st = download_points(h, a->bP, dJ_dprim0))) return st;
     if (J) *J = os.J;
     adj_params(h, os, bu, binit, dJ_dmach, dJ_daoa);
     if (dJ_dwall) return adj_geometry(h, objective, h->s64.prim[h->pcur], dJ_dwall);

@@ -263,6 +263,8 @@ void reduce_residual(const Launch &L, const Reduce &R, int n, int it);
 void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
 // dst += src over n double4 rows
 void add_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
+// out[0] += sum_i src[i].y, out[1] += sum_i src[i].z
+void sum_yz(const Launch &L, int n, const double4_32a *src, double *out);
 // [n] point states from the cloud's order into the handle's (dst[perm[i]] = src[i]) and back
 void permute_in(const Launch &L, int n, const int *perm, const double4_32a *src, double4_32a *dst);
 void permute_out(const Launch &L, int n, const int *perm, const double4_32a *src, double4_32a *dst);
@@ -270,7 +272,8 @@ void permute_out(const Launch &L, int n, const int *perm, const double4_32a *src
 // stagnation pressure per-256-block {min, argmin, max, argmax, sum (p0_inf - p0)^2, sum p0}
 void enstrophy(const Launch &L, const DevCloud &c, const double4_32a *prim, double *vort, double *partial);
 void stagnation(const Launch &L, int n, const double4_32a *prim, double gamma, double p0_inf, double *partial);
-// objectives: per-block partial sums into scratch ([4][ceil(max(n, n_wall)/256)]), then one ordered sum
+// objectives: per-block partial sums into scratch ([4][ceil(max(n, n_wall)/256)]), then one ordered sum;
+// entropy NULL: the force sums only (wall points), the entropy sum left 0
 void objective(const Launch &L, const DevCloud &c, const double4_32a *prim, const int *wall_perm, const double4_32a *wall_geo,
                int n_wall, double cp_scale, double pr_inf, double gamma, double *entropy, double *out4, double *scratch);
 }  // namespace fp64

@@ -261,6 +261,29 @@ def test_mixed_reverse_matches_fp64_reverse_at_same_state(qlskum, iters):
                                    atol=1e-6 * abs(gf["dmach"]))
 
 
+def test_mixed_adjoint_primal_is_the_solver_run(qlskum):
+    """On a mixed handle the adjoint's primal iterations (run by the recording
+    kernels, which keep every stage's data for the reverse) leave the same
+    state, prim_old and residual history as qlskum_q_lskum, bit for bit; the
+    stride-2 sweep (each segment recomputed once) gives the same gradient up
+    to the FP32 atomic sums of the gradient reverse."""
+    c = _cloud()
+    kw = dict(mach=MACH, aoa=AOA, inner_iterations=INNER, precision=qlskum.MIXED, **KW)
+    a = qlskum.Solver(c, **kw)
+    a.set_launch_config(0, 128, 0)
+    g1 = a.adjoint_gradient("cl", iters=5)
+    b = qlskum.Solver(c, **kw)
+    b.set_launch_config(0, 128, 0)
+    b.q_lskum(5)
+    assert a.iteration == b.iteration == 5
+    assert np.array_equal(a.prim, b.prim)
+    assert np.array_equal(a.field(qlskum.FIELD_PRIM_OLD), b.field(qlskum.FIELD_PRIM_OLD))
+    np.testing.assert_array_equal(a.residual_history(), b.residual_history())
+    g2 = a.adjoint_gradient("cl", iters=5, stride=2)
+    assert g2["J"] == g1["J"]
+    np.testing.assert_allclose([g2["dmach"], g2["daoa"]], [g1["dmach"], g1["daoa"]], rtol=1e-5)
+
+
 def test_mixed_fixed_point_one_step_identity(qlskum):
     """The one-step identity of the fixed-point adjoint on a mixed handle
     (both sides run the mixed reverse; the FP32 atomic sums leave ~1e-7 of
