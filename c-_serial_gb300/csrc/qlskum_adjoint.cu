@@ -84,9 +84,10 @@ __global__ void k_update(AdjView a, CaseConst K, const double4_32a *__restrict__
 template <bool GEO>
 __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__restrict__ q,
                                                const double4_32a *__restrict__ dq, const double4_32a *__restrict__ qm,
-                                               const double *__restrict__ delta, const double4_32a *__restrict__ bF,
-                                               double4_32a *__restrict__ bq, double4_32a *__restrict__ bdq,
-                                               double4_32a *__restrict__ bqm, double *__restrict__ bdelta)
+                                               const double *__restrict__ delta, const double4_32a *__restrict__ flux,
+                                               const double4_32a *__restrict__ bF, double4_32a *__restrict__ bq,
+                                               double4_32a *__restrict__ bdq, double4_32a *__restrict__ bqm,
+                                               double *__restrict__ bdelta)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.c.n) return;
@@ -106,11 +107,13 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
     const double scale = (f == kWall) ? 2.0 : 1.0;
     const bool used[4] = {true, true, f != kWall, f != kOuter};
 
-    // forward: the directional sums (for the bars of delta and of the moments)
+    // forward: the directional sums, for the bars of the moments (GEO only;
+    // without them the bar of delta comes from the stage's flux residual,
+    // F = delta * scale * sum_d G_d, so dF/ddelta = F / delta)
     double sx[4][4], sy[4][4];
     for (int d = 0; d < 4; d++)
         for (int r = 0; r < 4; r++) sx[d][r] = sy[d][r] = 0.0;
-    for (int j = 0; j < nb; j++) {
+    for (int j = 0; GEO && j < nb; j++) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         const double4_32a g = c.e_geo[e];
@@ -157,7 +160,7 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
             const double bG = scale * dl * bFi[r];
             if (d < 2) {
                 const double G = (sx[d][r] * m.y - sy[d][r] * m.z) * m.w;
-                bdl += scale * bFi[r] * G;
+                if (GEO) bdl += scale * bFi[r] * G;
                 bsx[d][r] = bG * m.y * m.w;
                 bsy[d][r] = -bG * m.z * m.w;
                 bm[1] += bG * sx[d][r] * m.w;
@@ -165,7 +168,7 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
                 bm[3] += bG * (sx[d][r] * m.y - sy[d][r] * m.z);
             } else {
                 const double G = (sy[d][r] * m.x - sx[d][r] * m.z) * m.w;
-                bdl += scale * bFi[r] * G;
+                if (GEO) bdl += scale * bFi[r] * G;
                 bsy[d][r] = bG * m.x * m.w;
                 bsx[d][r] = -bG * m.z * m.w;
                 bm[0] += bG * sy[d][r] * m.w;
@@ -180,6 +183,11 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
             acc.z += bm[2];
             acc.w += bm[3];
         }
+    }
+    if (!GEO) {
+        double F[4];
+        ld4(flux[i], F);
+        bdl = (bFi[0] * F[0] + bFi[1] * F[1] + bFi[2] * F[2] + bFi[3] * F[3]) / dl;
     }
     bdelta[i] += bdl;
 
@@ -1006,15 +1014,15 @@ void update(const Launch &L, const AdjView &a, const CaseConst &K, const double4
 }
 
 void flux(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
-          const double *delta, const double4_32a *bF, double4_32a *bq, double4_32a *bdq, double4_32a *bqm,
-          double *bdelta)
+          const double *delta, const double4_32a *flux, const double4_32a *bF, double4_32a *bq, double4_32a *bdq,
+          double4_32a *bqm, double *bdelta)
 {
     if (a.bedge)
-        adjk::k_flux<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, bF, bq, bdq, bqm,
-                                                                             bdelta);
+        adjk::k_flux<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, bF, bq, bdq,
+                                                                             bqm, bdelta);
     else
-        adjk::k_flux<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, bF, bq, bdq, bqm,
-                                                                              bdelta);
+        adjk::k_flux<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, bF, bq,
+                                                                              bdq, bqm, bdelta);
 }
 
 void inner(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq_in,

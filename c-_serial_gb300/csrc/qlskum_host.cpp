@@ -1974,7 +1974,7 @@ struct AdjBuf {
     std::vector<double4_32a *> dq;     // [stage][inner step 0 .. ni], each [np][2]
     double4_32a *qm[4] = {};
     double *delta = nullptr;
-    double4_32a *flux = nullptr;
+    double4_32a *flux[4] = {};        // each stage's flux residual
     double4_32a *bP = nullptr, *bPacc = nullptr, *bF = nullptr, *bq = nullptr, *bdqA = nullptr, *bdqB = nullptr,
                 *bqm = nullptr, *lam = nullptr, *lam_prev = nullptr, *seed = nullptr;
     double *bdelta = nullptr, *bc = nullptr, *buinf = nullptr;
@@ -2186,7 +2186,7 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
         a->dq.resize(4 * (size_t)(a->ni + 1));
         for (auto &p : a->dq) p = A.alloc<double4_32a>(2 * np);
         a->delta = A.alloc<double>(np);
-        a->flux = A.alloc<double4_32a>(np);
+        for (auto &p : a->flux) p = A.alloc<double4_32a>(np);
         a->bq = A.alloc<double4_32a>(np);
         for (auto *p : {&a->bdqA, &a->bdqB, &a->bqm}) *p = A.alloc<double4_32a>(2 * np);
         a->bdelta = A.alloc<double>(np);
@@ -2256,7 +2256,7 @@ void adj_zero_geometry(qlskum_handle *h)
 double4_32a *adj_dq(AdjBuf *a, int s, int j) { return a->dq[(size_t)s * (a->ni + 1) + j]; }
 
 // Stage s (0-based) from P[s]: q, the gradient and its inner-loop
-// corrections, the neighbour max / min and the flux residual (into a->flux)
+// corrections, the neighbour max / min and the flux residual (into a->flux[s])
 // (fpi_solver_mod.h:20-36).
 void adj_stage_forward(qlskum_handle *h, int s)
 {
@@ -2265,7 +2265,7 @@ void adj_stage_forward(qlskum_handle *h, int s)
     fp64::q_variables(h->L, c, a->P[s], a->q[s]);
     fp64::q_derivatives(h->L, c, a->q[s], adj_dq(a, s, 0), a->qm[s], nullptr, nullptr, 0.0);
     for (int j = 1; j <= a->ni; j++) fp64::q_inner(h->L, c, a->q[s], adj_dq(a, s, j - 1), adj_dq(a, s, j));
-    fp64::flux_residual(h->L, c, a->q[s], adj_dq(a, s, a->ni), a->qm[s], a->delta, a->flux);
+    fp64::flux_residual(h->L, c, a->q[s], adj_dq(a, s, a->ni), a->qm[s], a->delta, a->flux[s]);
 }
 
 // The four stage states of one iteration from a->P[0] (fpi_solver_mod.h:14-40).
@@ -2276,7 +2276,7 @@ void adj_iteration_forward64(qlskum_handle *h)
     for (int s = 0; s < 4; s++) {
         adj_stage_forward(h, s);
         fp64::copy_prim(h->L, h->n, a->P[s], a->P[s + 1]);
-        fp64::state_update(h->L, h->dc, h->K, a->P[s + 1], a->P[0], a->flux, s + 1, h->R);
+        fp64::state_update(h->L, h->dc, h->K, a->P[s + 1], a->P[0], a->flux[s], s + 1, h->R);
     }
 }
 
@@ -2290,7 +2290,8 @@ void adj_stage_reverse(qlskum_handle *h, int s, const AdjView &v)
     zero(h, a->bq, sizeof(double4_32a) * np);
     zero(h, a->bdqA, sizeof(double4_32a) * 2 * np);
     zero(h, a->bqm, sizeof(double4_32a) * 2 * np);
-    adjl::flux(h->L, v, a->q[s], adj_dq(a, s, ni), a->qm[s], a->delta, a->bF, a->bq, a->bdqA, a->bqm, a->bdelta);
+    adjl::flux(h->L, v, a->q[s], adj_dq(a, s, ni), a->qm[s], a->delta, a->flux[s], a->bF, a->bq, a->bdqA, a->bqm,
+               a->bdelta);
     for (int j = ni; j >= 1; j--) {
         zero(h, a->bdqB, sizeof(double4_32a) * 2 * np);
         adjl::inner(h->L, v, a->q[s], adj_dq(a, s, j - 1), a->bdqA, a->bq, a->bdqB);
@@ -2668,7 +2669,7 @@ qlskum_status qlskum_residual_forward(qlskum_handle *h, const double *prim, doub
     fp64::func_delta(h->L, h->dc, a->P[0], a->delta, h->K.cfl);
     adj_stage_forward(h, 0);
     if ((st = check_launch(h, "residual_forward"))) return st;
-    return download_points(h, a->flux, flux_res);
+    return download_points(h, a->flux[0], flux_res);
 }
 
 qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const double *bar_flux_res, double *bar_prim)

@@ -183,9 +183,10 @@ struct AdjView {
 namespace adjl {
 void update(const Launch &L, const AdjView &a, const CaseConst &K, const double4_32a *Pin, const double4_32a *Pold,
             const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, double4_32a *bF, double *buinf);
+// flux: the stage's flux residual (the bar of delta without geometry bars)
 void flux(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
-          const double *delta, const double4_32a *bF, double4_32a *bq, double4_32a *bdq, double4_32a *bqm,
-          double *bdelta);
+          const double *delta, const double4_32a *flux, const double4_32a *bF, double4_32a *bq, double4_32a *bdq,
+          double4_32a *bqm, double *bdelta);
 void inner(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq_in,
            const double4_32a *bdq_out, double4_32a *bq, double4_32a *bdq_in);
 void grad(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *bdq, const double4_32a *bqm,

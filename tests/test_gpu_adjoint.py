@@ -284,6 +284,24 @@ def test_mixed_adjoint_primal_is_the_solver_run(qlskum):
     np.testing.assert_allclose([g2["dmach"], g2["daoa"]], [g1["dmach"], g1["daoa"]], rtol=1e-5)
 
 
+def test_mixed_reverse_weighted_stencils(qlskum):
+    """The mixed reverse with distance-weighted least squares (power 1: the
+    edge vectors and the folded weights are the weighted ones) against the
+    FP64 reverse at the same state."""
+    c = _cloud()
+    kw = dict(KW, power=1.0)
+    f = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **kw)
+    f.q_lskum(5)
+    U0 = f.prim
+    m = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, precision=qlskum.MIXED, **kw)
+    gf = f.adjoint_gradient("cd", iters=2, prim0=U0)
+    gm = m.adjoint_gradient("cd", iters=2, prim0=U0)
+    d = gm["dprim0"] - gf["dprim0"]
+    assert np.linalg.norm(d) <= 1e-4 * np.linalg.norm(gf["dprim0"])
+    np.testing.assert_allclose([gm["dmach"], gm["daoa"]], [gf["dmach"], gf["daoa"]], rtol=1e-4,
+                               atol=1e-6 * abs(gf["dmach"]))
+
+
 def test_mixed_fixed_point_one_step_identity(qlskum):
     """The one-step identity of the fixed-point adjoint on a mixed handle
     (both sides run the mixed reverse; the FP32 atomic sums leave ~1e-7 of
