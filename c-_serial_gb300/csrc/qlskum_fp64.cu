@@ -602,6 +602,19 @@ void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
     QLSKUM_LAUNCHED(L);
 }
 
+// dst[i] = v for the n points.
+__global__ void k_fill(int n, double4_32a v, double4_32a *__restrict__ dst)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = v;
+}
+
+void fill_prim(const Launch &L, int n, double4_32a v, double4_32a *dst)
+{
+    k_fill<<<grid_for(n, 256), 256, 0, L.stream>>>(n, v, dst);
+    QLSKUM_LAUNCHED(L);
+}
+
 // out[0] += sum of src.y, out[1] += sum of src.z over the n points (warp
 // sums, one atomic per warp).
 __global__ void k_sum_yz(int n, const double4_32a *__restrict__ src, double *__restrict__ out)

@@ -1964,17 +1964,24 @@ struct Set32 {
     float *delta32 = nullptr, *cs32 = nullptr;
 };
 
+// One iteration's stage data of the FP64 form with its five stage states.
+struct Set64 {
+    double4_32a *P[5] = {};
+    double4_32a *q[4] = {};            // q of P[0 .. 3]
+    std::vector<double4_32a *> dq;     // [stage][inner step 0 .. ni], each [np][2]
+    double4_32a *qm[4] = {};
+    double *delta = nullptr;
+    double4_32a *flux[4] = {};         // each stage's flux residual
+};
+
 struct AdjBuf {
     DeviceArena arena;
     int ni = 0;
     bool geo = false, has64 = false, has32 = false;
     size_t ne = 0;
     double4_32a *P[5] = {};            // stage states of one iteration
-    double4_32a *q[4] = {};            // q of P[0 .. 3]
-    std::vector<double4_32a *> dq;     // [stage][inner step 0 .. ni], each [np][2]
-    double4_32a *qm[4] = {};
-    double *delta = nullptr;
-    double4_32a *flux[4] = {};        // each stage's flux residual
+    Set64 set64;                       // the FP64 stage data of one iteration (its states are P)
+    std::vector<Set64> sets64;         // one per iteration of a segment, on demand (set_arena)
     double4_32a *bP = nullptr, *bPacc = nullptr, *bF = nullptr, *bq = nullptr, *bdqA = nullptr, *bdqB = nullptr,
                 *bqm = nullptr, *lam = nullptr, *lam_prev = nullptr, *seed = nullptr;
     double *bdelta = nullptr, *bc = nullptr, *buinf = nullptr;
@@ -1993,7 +2000,7 @@ struct AdjBuf {
     // on demand, one set per iteration of a segment (own states, own arena)
     Set32 set0;
     std::vector<Set32> sets;
-    DeviceArena set_arena;
+    DeviceArena set_arena;             // the on-demand sets (FP32 or FP64, one kind at a time)
     float4 *bF32 = nullptr;            // bar of the flux residual
     float4 *bs32 = nullptr;            // bar of the weighted sums (delta * bF)
     AdjT T;                            // the edge list transposed (mixed reverse)
@@ -2151,6 +2158,22 @@ void alloc_set32(DeviceArena &A, size_t np, int ni, Set32 &st)
     st.cs32 = A.alloc<float>(np);
 }
 
+// The FP64 arrays of one stage-data set (its states are assigned by the caller).
+void alloc_set64(DeviceArena &A, size_t np, int ni, Set64 &st)
+{
+    for (auto &p : st.q) p = A.alloc<double4_32a>(np);
+    for (auto &p : st.qm) p = A.alloc<double4_32a>(2 * np);
+    st.dq.resize(4 * (size_t)(ni + 1));
+    for (auto &p : st.dq) p = A.alloc<double4_32a>(2 * np);
+    st.delta = A.alloc<double>(np);
+    for (auto &p : st.flux) p = A.alloc<double4_32a>(np);
+}
+
+size_t set64_bytes(size_t np, int ni)
+{
+    return np * (5 * sizeof(double4_32a) + 4 * 32 + 4 * 64 + 4 * (size_t)(ni + 1) * 64 + 8 + 4 * 32);
+}
+
 // Bytes of one set with its own states.
 size_t set32_bytes(size_t np, int ni)
 {
@@ -2181,12 +2204,8 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
     for (auto *p : {&a->bP, &a->bPacc, &a->bF, &a->lam, &a->lam_prev, &a->seed}) *p = A.alloc<double4_32a>(np);
     a->buinf = A.alloc<double>(4);  // free-stream velocity bars, then the initial-state sums
     if (need64) {
-        for (auto &p : a->q) p = A.alloc<double4_32a>(np);
-        for (auto &p : a->qm) p = A.alloc<double4_32a>(2 * np);
-        a->dq.resize(4 * (size_t)(a->ni + 1));
-        for (auto &p : a->dq) p = A.alloc<double4_32a>(2 * np);
-        a->delta = A.alloc<double>(np);
-        for (auto &p : a->flux) p = A.alloc<double4_32a>(np);
+        alloc_set64(A, np, a->ni, a->set64);
+        for (int k = 0; k < 5; k++) a->set64.P[k] = a->P[k];
         a->bq = A.alloc<double4_32a>(np);
         for (auto *p : {&a->bdqA, &a->bdqB, &a->bqm}) *p = A.alloc<double4_32a>(2 * np);
         a->bdelta = A.alloc<double>(np);
@@ -2253,36 +2272,43 @@ void adj_zero_geometry(qlskum_handle *h)
     zero(h, a->bfmom, sizeof(double4_32a) * 4 * np);
 }
 
-double4_32a *adj_dq(AdjBuf *a, int s, int j) { return a->dq[(size_t)s * (a->ni + 1) + j]; }
+double4_32a *adj_dq(const Set64 &st, int ni, int s, int j) { return st.dq[(size_t)s * (ni + 1) + j]; }
 
-// Stage s (0-based) from P[s]: q, the gradient and its inner-loop
-// corrections, the neighbour max / min and the flux residual (into a->flux[s])
-// (fpi_solver_mod.h:20-36).
-void adj_stage_forward(qlskum_handle *h, int s)
+// Stage s (0-based) from st.P[s]: q, the gradient and its inner-loop
+// corrections, the neighbour max / min and the flux residual (into
+// st.flux[s]) (fpi_solver_mod.h:20-36).
+void adj_stage_forward(qlskum_handle *h, Set64 &st, int s)
 {
-    AdjBuf *a = h->adj;
+    const int ni = h->adj->ni;
     const DevCloud &c = h->dc;
-    fp64::q_variables(h->L, c, a->P[s], a->q[s]);
-    fp64::q_derivatives(h->L, c, a->q[s], adj_dq(a, s, 0), a->qm[s], nullptr, nullptr, 0.0);
-    for (int j = 1; j <= a->ni; j++) fp64::q_inner(h->L, c, a->q[s], adj_dq(a, s, j - 1), adj_dq(a, s, j));
-    fp64::flux_residual(h->L, c, a->q[s], adj_dq(a, s, a->ni), a->qm[s], a->delta, a->flux[s]);
+    fp64::q_variables(h->L, c, st.P[s], st.q[s]);
+    fp64::q_derivatives(h->L, c, st.q[s], adj_dq(st, ni, s, 0), st.qm[s], nullptr, nullptr, 0.0);
+    for (int j = 1; j <= ni; j++) fp64::q_inner(h->L, c, st.q[s], adj_dq(st, ni, s, j - 1), adj_dq(st, ni, s, j));
+    fp64::flux_residual(h->L, c, st.q[s], adj_dq(st, ni, s, ni), st.qm[s], st.delta, st.flux[s]);
 }
 
-// The four stage states of one iteration from a->P[0] (fpi_solver_mod.h:14-40).
-void adj_iteration_forward64(qlskum_handle *h)
+// The four stage states of one iteration from st.P[0] (fpi_solver_mod.h:14-40)
+// with the module kernels, whose results equal the fused solver's bit for
+// bit.  it_rec > 0: the iteration is the primal's own iteration it_rec (its
+// residual row is reduced and recorded, as qlskum_fpi_solver does).
+void adj_iteration_forward64(qlskum_handle *h, Set64 &st, int it_rec = 0)
 {
-    AdjBuf *a = h->adj;
-    fp64::func_delta(h->L, h->dc, a->P[0], a->delta, h->K.cfl);
+    fp64::func_delta(h->L, h->dc, st.P[0], st.delta, h->K.cfl);
     for (int s = 0; s < 4; s++) {
-        adj_stage_forward(h, s);
-        fp64::copy_prim(h->L, h->n, a->P[s], a->P[s + 1]);
-        fp64::state_update(h->L, h->dc, h->K, a->P[s + 1], a->P[0], a->flux[s], s + 1, h->R);
+        adj_stage_forward(h, st, s);
+        fp64::copy_prim(h->L, h->n, st.P[s], st.P[s + 1]);
+        fp64::state_update(h->L, h->dc, h->K, st.P[s + 1], st.P[0], st.flux[s], s + 1, h->R);
+    }
+    if (it_rec > 0) {
+        Reduce R = h->R;
+        R.blocks = (h->n + 127) / 128;
+        fp64::reduce_residual(h->L, R, h->n, it_rec);
     }
 }
 
 // Reverse of stage s's residual chain for the bar in a->bF: adds to a->bP
 // (the bar of P[s]) and to a->bdelta.
-void adj_stage_reverse(qlskum_handle *h, int s, const AdjView &v)
+void adj_stage_reverse(qlskum_handle *h, const Set64 &st, int s, const AdjView &v)
 {
     AdjBuf *a = h->adj;
     const size_t np = h->np;
@@ -2290,63 +2316,77 @@ void adj_stage_reverse(qlskum_handle *h, int s, const AdjView &v)
     zero(h, a->bq, sizeof(double4_32a) * np);
     zero(h, a->bdqA, sizeof(double4_32a) * 2 * np);
     zero(h, a->bqm, sizeof(double4_32a) * 2 * np);
-    adjl::flux(h->L, v, a->q[s], adj_dq(a, s, ni), a->qm[s], a->delta, a->flux[s], a->bF, a->bq, a->bdqA, a->bqm,
-               a->bdelta);
+    adjl::flux(h->L, v, st.q[s], adj_dq(st, ni, s, ni), st.qm[s], st.delta, st.flux[s], a->bF, a->bq, a->bdqA,
+               a->bqm, a->bdelta);
     for (int j = ni; j >= 1; j--) {
         zero(h, a->bdqB, sizeof(double4_32a) * 2 * np);
-        adjl::inner(h->L, v, a->q[s], adj_dq(a, s, j - 1), a->bdqA, a->bq, a->bdqB);
+        adjl::inner(h->L, v, st.q[s], adj_dq(st, ni, s, j - 1), a->bdqA, a->bq, a->bdqB);
         std::swap(a->bdqA, a->bdqB);
     }
-    adjl::grad(h->L, v, a->q[s], a->bdqA, a->bqm, a->bq);
-    adjl::qvars(h->L, h->n, a->P[s], a->bq, a->bP);
+    adjl::grad(h->L, v, st.q[s], a->bdqA, a->bqm, a->bq);
+    adjl::qvars(h->L, h->n, st.P[s], a->bq, a->bP);
 }
 
-// Reverse of one iteration after adj_iteration_forward: a->bP holds the bar of
-// P[4] on entry and the bar of P[0] on exit.  Free-stream bars add to
+// Reverse of one iteration after adj_iteration_forward64: a->bP holds the
+// bar of P[4] on entry and the bar of P[0] on exit.  Free-stream bars add to
 // a->buinf, geometry bars to the view's accumulators.
-void adj_iteration_reverse64(qlskum_handle *h, const AdjView &v)
+void adj_iteration_reverse64(qlskum_handle *h, const Set64 &st, const AdjView &v)
 {
     AdjBuf *a = h->adj;
     const size_t np = h->np;
     zero(h, a->bPacc, sizeof(double4_32a) * np);
     zero(h, a->bdelta, sizeof(double) * np);
     for (int s = 3; s >= 0; s--) {
-        adjl::update(h->L, v, h->K, a->P[s], a->P[0], a->P[s + 1], s + 1, a->bP, a->bPacc, a->bF, a->buinf);
-        adj_stage_reverse(h, s, v);
+        adjl::update(h->L, v, h->K, st.P[s], st.P[0], st.P[s + 1], s + 1, a->bP, a->bPacc, a->bF, a->buinf);
+        adj_stage_reverse(h, st, s, v);
     }
     zero(h, a->bc, sizeof(double) * np);
-    adjl::delta(h->L, v, a->P[0], a->bdelta, h->K.cfl, a->bc, a->bPacc);
+    adjl::delta(h->L, v, st.P[0], a->bdelta, h->K.cfl, a->bc, a->bPacc);
     fp64::add_prim(h->L, h->n, a->bPacc, a->bP);
 }
 
 float4 *adj_dq32(const Set32 &st, int ni, int s, int j) { return st.dq32[(size_t)s * (ni + 1) + j]; }
 
-// `count` sets with their own states for a segment's iterations (first use
-// and growth only); false when they do not fit.
-bool adj_sets(qlskum_handle *h, int count)
+// `count` stage-data sets with their own states (FP64 or FP32 kind; first
+// use, growth and change of kind only); false when they do not fit.
+bool adj_sets(qlskum_handle *h, int count, bool f64)
 {
     AdjBuf *a = h->adj;
-    if ((int)a->sets.size() >= count) return true;
-    a->sets.clear();
-    a->set_arena.release();
-    a->set_arena.err = cudaSuccess;
+    if ((f64 ? (int)a->sets64.size() : (int)a->sets.size()) >= count) return true;
+    auto drop = [&]() {
+        a->sets.clear();
+        a->sets64.clear();
+        a->set_arena.release();
+        a->set_arena.err = cudaSuccess;
+    };
+    drop();
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
     // keep a quarter of the free memory for everything else
-    if ((double)set32_bytes(h->np, a->ni) * count > 0.75 * (double)free_b) return false;
-    a->sets.resize(count);
-    for (auto &st : a->sets) {
-        alloc_set32(a->set_arena, h->np, a->ni, st);
-        for (auto &p : st.P) p = a->set_arena.alloc<double4_32a>(h->np);
+    const size_t each = f64 ? set64_bytes(h->np, a->ni) : set32_bytes(h->np, a->ni);
+    if ((double)each * count > 0.75 * (double)free_b) return false;
+    std::vector<double4_32a *> p0;
+    if (f64) {
+        a->sets64.resize(count);
+        for (auto &st : a->sets64) {
+            alloc_set64(a->set_arena, h->np, a->ni, st);
+            for (auto &p : st.P) p = a->set_arena.alloc<double4_32a>(h->np);
+            p0.push_back(st.P[0]);
+        }
+    } else {
+        a->sets.resize(count);
+        for (auto &st : a->sets) {
+            alloc_set32(a->set_arena, h->np, a->ni, st);
+            for (auto &p : st.P) p = a->set_arena.alloc<double4_32a>(h->np);
+            p0.push_back(st.P[0]);
+        }
     }
     if (a->set_arena.err != cudaSuccess) {
         cudaGetLastError();
-        a->sets.clear();
-        a->set_arena.release();
-        a->set_arena.err = cudaSuccess;
+        drop();
         return false;
     }
-    for (auto &st : a->sets) zero(h, st.P[0], sizeof(double4_32a) * h->np);
+    for (auto *p : p0) zero(h, p, sizeof(double4_32a) * h->np);
     return true;
 }
 
@@ -2417,13 +2457,13 @@ bool adj_use32(const qlskum_handle *h, bool geo) { return h->prm.precision == QL
 void adj_iteration_forward(qlskum_handle *h, bool m32)
 {
     if (m32) adj_iteration_forward32(h, h->adj->set0);
-    else adj_iteration_forward64(h);
+    else adj_iteration_forward64(h, h->adj->set64);
 }
 
 void adj_iteration_reverse(qlskum_handle *h, const AdjView &v, bool m32)
 {
     if (m32) adj_iteration_reverse32(h, h->adj->set0);
-    else adj_iteration_reverse64(h, v);
+    else adj_iteration_reverse64(h, h->adj->set64, v);
 }
 
 // Cl and Cd at `prim` (compute_force_coeffs_mod.h:37-67), and dJ/dprim of
@@ -2666,10 +2706,10 @@ qlskum_status qlskum_residual_forward(qlskum_handle *h, const double *prim, doub
     if (st) return st;
     AdjBuf *a = h->adj;
     if ((st = upload_points(h, prim, a->P[0], 1.0))) return st;
-    fp64::func_delta(h->L, h->dc, a->P[0], a->delta, h->K.cfl);
-    adj_stage_forward(h, 0);
+    fp64::func_delta(h->L, h->dc, a->P[0], a->set64.delta, h->K.cfl);
+    adj_stage_forward(h, a->set64, 0);
     if ((st = check_launch(h, "residual_forward"))) return st;
-    return download_points(h, a->flux[0], flux_res);
+    return download_points(h, a->set64.flux[0], flux_res);
 }
 
 qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const double *bar_flux_res, double *bar_prim)
@@ -2681,12 +2721,12 @@ qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const do
     AdjBuf *a = h->adj;
     if ((st = upload_points(h, prim, a->P[0], 1.0))) return st;
     if ((st = upload_points(h, bar_flux_res, a->bF, 0.0))) return st;
-    fp64::func_delta(h->L, h->dc, a->P[0], a->delta, h->K.cfl);
-    adj_stage_forward(h, 0);
+    fp64::func_delta(h->L, h->dc, a->P[0], a->set64.delta, h->K.cfl);
+    adj_stage_forward(h, a->set64, 0);
     const AdjView v = adj_view(h, false);
     zero(h, a->bP, sizeof(double4_32a) * h->np);
     zero(h, a->bdelta, sizeof(double) * h->np);
-    adj_stage_reverse(h, 0, v);
+    adj_stage_reverse(h, a->set64, 0, v);
     zero(h, a->bc, sizeof(double) * h->np);
     adjl::delta(h->L, v, a->P[0], a->bdelta, h->K.cfl, a->bc, a->bP);
     if ((st = check_launch(h, "residual_vjp"))) return st;
@@ -2706,13 +2746,13 @@ qlskum_status qlskum_residual_vjp_full(qlskum_handle *h, const double *prim, con
     AdjBuf *a = h->adj;
     if ((st = upload_points(h, prim, a->P[0], 1.0))) return st;
     if ((st = upload_points(h, bar_flux_res, a->bF, 0.0))) return st;
-    fp64::func_delta(h->L, h->dc, a->P[0], a->delta, h->K.cfl);
-    adj_stage_forward(h, 0);
+    fp64::func_delta(h->L, h->dc, a->P[0], a->set64.delta, h->K.cfl);
+    adj_stage_forward(h, a->set64, 0);
     adj_zero_geometry(h);
     const AdjView v = adj_view(h, geo);
     zero(h, a->bP, sizeof(double4_32a) * h->np);
     zero(h, a->bdelta, sizeof(double) * h->np);
-    adj_stage_reverse(h, 0, v);
+    adj_stage_reverse(h, a->set64, 0, v);
     zero(h, a->bc, sizeof(double) * h->np);
     adjl::delta(h->L, v, a->P[0], a->bdelta, h->K.cfl, a->bc, a->bP);
     if ((st = check_launch(h, "residual_vjp_full"))) return st;
@@ -2740,8 +2780,16 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     // recording iteration and nothing is recomputed), with a larger stride one
     // segment's (each segment recomputed once); otherwise set 0 is refilled
     // for every iteration of the reverse sweep
-    const bool store_all = m32 && S == 1 && adj_sets(h, iters);
-    const bool seg_sets = m32 && !store_all && S > 1 && adj_sets(h, S);
+    // (FP64 handles the same with FP64 stage data; a mixed handle's FP64 reverse
+    // for wall gradients keeps the fused mixed primal and recomputes in FP64)
+    const bool f64h = h->prm.precision == QLSKUM_FP64;
+    const bool store_all = S == 1 && (m32 || f64h) && adj_sets(h, iters, !m32);
+    const bool seg_sets = !store_all && S > 1 && adj_sets(h, S, !m32);
+    auto set_P = [&](int t, int k) { return m32 ? a->sets[t].P[k] : a->sets64[t].P[k]; };
+    auto fwd_set = [&](int t, int it_rec) {
+        if (m32) adj_iteration_forward32(h, a->sets[t], it_rec);
+        else adj_iteration_forward64(h, a->sets64[t], it_rec);
+    };
     auto grow = [&](double4_32a *&buf, int &cap, int want, const char *what) -> qlskum_status {
         if (cap >= want) return QLSKUM_OK;
         if (buf) cudaFree(buf);
@@ -2759,12 +2807,11 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     // primal from prim0 or the free stream (initial_conditions_mod.h:23-37),
     // every S-th iteration's starting state kept
     if (prim0) {
-        if ((st = upload_points(h, prim0, h->s64.prim[h->pcur], 1.0))) return st;
+        // the caller's [n][4] state reordered on the device (qlskum_set_prim's path)
+        if ((st = qlskum_set_prim(h, prim0))) return st;
     } else {
-        std::vector<double4_32a> fs(np, make_double4_32a(h->K.rho_inf, h->K.u1_inf, h->K.u2_inf, h->K.pr_inf));
-        CK(h, cudaMemcpyAsync(h->s64.prim[h->pcur], fs.data(), sizeof(double4_32a) * np, cudaMemcpyHostToDevice,
-                              h->L.stream));
-        CK(h, cudaStreamSynchronize(h->L.stream));
+        fp64::fill_prim(h->L, (int)np, make_double4_32a(h->K.rho_inf, h->K.u1_inf, h->K.u2_inf, h->K.pr_inf),
+                        h->s64.prim[h->pcur]);
     }
     CK(h, cudaMemsetAsync(h->R.status, 0, sizeof(int), h->L.stream));
     h->derived_valid = false;
@@ -2777,14 +2824,13 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
         if ((st = ensure_derived(h))) return st;
         const int o = h->pcur;
         for (int t = 0; t < iters; t++) {
-            const double4_32a *from = t == 0 ? h->s64.prim[o] : a->sets[t - 1].P[4];
-            CK(h, cudaMemcpyAsync(a->sets[t].P[0], from, bytes, cudaMemcpyDeviceToDevice, h->L.stream));
-            adj_iteration_forward32(h, a->sets[t], t + 1);
+            const double4_32a *from = t == 0 ? h->s64.prim[o] : set_P(t - 1, 4);
+            CK(h, cudaMemcpyAsync(set_P(t, 0), from, bytes, cudaMemcpyDeviceToDevice, h->L.stream));
+            fwd_set(t, t + 1);
         }
         // the handle as after qlskum_q_lskum(iters): state and prim_old of the last iteration
-        CK(h, cudaMemcpyAsync(h->s64.prim[o], a->sets[iters - 1].P[0], bytes, cudaMemcpyDeviceToDevice,
-                              h->L.stream));
-        CK(h, cudaMemcpyAsync(h->s64.prim[(o + 2) % 3], a->sets[iters - 1].P[4], bytes, cudaMemcpyDeviceToDevice,
+        CK(h, cudaMemcpyAsync(h->s64.prim[o], set_P(iters - 1, 0), bytes, cudaMemcpyDeviceToDevice, h->L.stream));
+        CK(h, cudaMemcpyAsync(h->s64.prim[(o + 2) % 3], set_P(iters - 1, 4), bytes, cudaMemcpyDeviceToDevice,
                               h->L.stream));
         after_iteration(h, o);
         h->derived_valid = false;
@@ -2811,11 +2857,14 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
         if (seg_sets) {
             // the segment's iterations once, each into its set, then reversed
             for (int t = t0; t < t1; t++) {
-                const double4_32a *from = t == t0 ? state_at0 : a->sets[t - 1 - t0].P[4];
-                CK(h, cudaMemcpyAsync(a->sets[t - t0].P[0], from, bytes, cudaMemcpyDeviceToDevice, h->L.stream));
-                adj_iteration_forward32(h, a->sets[t - t0]);
+                const double4_32a *from = t == t0 ? state_at0 : set_P(t - 1 - t0, 4);
+                CK(h, cudaMemcpyAsync(set_P(t - t0, 0), from, bytes, cudaMemcpyDeviceToDevice, h->L.stream));
+                fwd_set(t - t0, 0);
             }
-            for (int t = t1 - 1; t >= t0; t--) adj_iteration_reverse32(h, a->sets[t - t0]);
+            for (int t = t1 - 1; t >= t0; t--) {
+                if (m32) adj_iteration_reverse32(h, a->sets[t - t0]);
+                else adj_iteration_reverse64(h, a->sets64[t - t0], v);
+            }
             continue;
         }
         if (S > 1) {
@@ -2836,7 +2885,10 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
         }
     }
     if (store_all)
-        for (int t = iters - 1; t >= 0; t--) adj_iteration_reverse32(h, a->sets[t]);
+        for (int t = iters - 1; t >= 0; t--) {
+            if (m32) adj_iteration_reverse32(h, a->sets[t]);
+            else adj_iteration_reverse64(h, a->sets64[t], v);
+        }
     if ((st = check_launch(h, "adjoint sweep"))) return st;
     // bar of the initial state: returned for prim0, else (the free stream)
     // summed over the points into the free-stream velocity (on the device)

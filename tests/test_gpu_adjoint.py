@@ -302,6 +302,20 @@ def test_mixed_reverse_weighted_stencils(qlskum):
                                atol=1e-6 * abs(gf["dmach"]))
 
 
+def test_fp64_adjoint_primal_is_the_solver_run(qlskum):
+    """On an FP64 handle the adjoint's primal iterations run as the recording
+    iteration (module kernels, every stage's data kept): the same state and
+    residual history as qlskum_q_lskum, bit for bit."""
+    c = _cloud()
+    a = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **KW)
+    a.adjoint_gradient("cd", iters=4)
+    b = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=INNER, **KW)
+    b.q_lskum(4)
+    assert a.iteration == b.iteration == 4
+    assert np.array_equal(a.prim, b.prim)
+    np.testing.assert_array_equal(a.residual_history(), b.residual_history())
+
+
 def test_mixed_fixed_point_one_step_identity(qlskum):
     """The one-step identity of the fixed-point adjoint on a mixed handle
     (both sides run the mixed reverse; the FP32 atomic sums leave ~1e-7 of
