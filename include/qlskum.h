@@ -321,14 +321,15 @@ qlskum_status qlskum_residual_vjp_full(qlskum_handle *h, const double *prim, con
  * min_dist held fixed (power 0 only); dJ_dprim0 (or NULL): double [n][4],
  * the derivative w.r.t. the initial state.  Device memory: 32 bytes per
  * point per kept state (every stride-th iteration, qlskum_set_adjoint_stride).
- * A MIXED handle without dJ_dwall also keeps each iteration's FP32 stage data
- * where it fits in three quarters of the free device memory (about 1 KB per
- * point per iteration at 3 inner steps): with stride 1 for all `iters`
- * iterations (the primal then runs as the recording iteration, with the same
- * state, prim_old and residual history as qlskum_q_lskum, and the reverse
- * recomputes nothing), with a larger stride for one stride-long segment
- * (each segment recomputed once); otherwise every iteration's stage data is
- * recomputed from its state during the reverse sweep. */
+ * Each iteration's stage data is also kept where it fits in three quarters
+ * of the free device memory (FP64 handles about 1.7 KB, MIXED handles without
+ * dJ_dwall about 1 KB per point per iteration at 3 inner steps): with stride 1
+ * for all `iters` iterations (the primal then runs as the recording
+ * iteration, with the same state, prim_old and residual history as
+ * qlskum_q_lskum, and the reverse recomputes nothing), with a larger stride
+ * for one stride-long segment (each segment recomputed once); otherwise every
+ * iteration's stage data is recomputed from its state during the reverse
+ * sweep. */
 qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters, const double *prim0, double *J,
                                       double *dJ_dmach, double *dJ_daoa, double *dJ_dwall, double *dJ_dprim0);
 /* Keep the state of every stride-th iteration only (default 1: every
