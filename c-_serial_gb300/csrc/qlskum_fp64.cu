@@ -602,6 +602,14 @@ void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
     QLSKUM_LAUNCHED(L);
 }
 
+__global__ void k_set_int(int *p, int v) { *p = v; }
+
+void set_counter(const Launch &L, int *p, int v)
+{
+    k_set_int<<<1, 1, 0, L.stream>>>(p, v);
+    QLSKUM_LAUNCHED(L);
+}
+
 // dst[i] = v for the n points.
 __global__ void k_fill(int n, double4_32a v, double4_32a *__restrict__ dst)
 {

@@ -1054,6 +1054,32 @@ qlskum_status qlskum_snapshot_prim_old(qlskum_handle *h)
     return check_launch(h, "snapshot_prim_old");
 }
 
+}  // extern "C"
+
+namespace {
+// One graph per buffer-rotation phase (enqueue_iteration with the device's
+// iteration counter), all three captured on first use.
+qlskum_status ensure_graphs(qlskum_handle *h)
+{
+    for (int o = 0; o < 3; o++) {
+        if (h->graph[o]) continue;
+        cudaGraph_t g = nullptr;
+        CK(h, cudaStreamBeginCapture(h->L.stream, cudaStreamCaptureModeThreadLocal));
+        long long before = h->launches;
+        enqueue_iteration(h, o, 0);
+        h->launches = before;  // counted when replayed
+        cudaError_t e = cudaStreamEndCapture(h->L.stream, &g);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&h->graph[o], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+    }
+    return QLSKUM_OK;
+}
+}  // namespace
+
+extern "C" {
+
 qlskum_status qlskum_fpi_solver(qlskum_handle *h, int it)
 {
     NEED(h);
@@ -1063,7 +1089,15 @@ qlskum_status qlskum_fpi_solver(qlskum_handle *h, int it)
     st = ensure_derived(h);
     if (st) return st;
     const int o = h->pcur;
-    enqueue_iteration(h, o, it);
+    if (h->timing) {
+        enqueue_iteration(h, o, it);
+    } else {
+        // the captured iteration, its counter set to it - 1 on the device
+        if ((st = ensure_graphs(h))) return st;
+        fp64::set_counter(h->L, h->R.iter, it - 1);
+        CK(h, cudaGraphLaunch(h->graph[o], h->L.stream));
+        h->launches += 4 * (2 + h->prm.inner_iterations) + 1;
+    }
     st = check_launch(h, "fpi_solver");
     if (st) return st;
     after_iteration(h, o);
@@ -1088,20 +1122,7 @@ qlskum_status qlskum_q_lskum(qlskum_handle *h, int iters)
     // the device counter continues from the host's
     CK(h, cudaMemcpyAsync(h->R.iter, &h->it, sizeof(int), cudaMemcpyHostToDevice, h->L.stream));
     CK(h, cudaStreamSynchronize(h->L.stream));
-    // one graph per buffer-rotation phase, all three captured up front
-    for (int o = 0; o < 3 && !h->timing && iters > 0; o++) {
-        if (h->graph[o]) continue;
-        cudaGraph_t g = nullptr;
-        CK(h, cudaStreamBeginCapture(h->L.stream, cudaStreamCaptureModeThreadLocal));
-        long long before = h->launches;
-        enqueue_iteration(h, o, 0);
-        h->launches = before;  // counted when replayed
-        cudaError_t e = cudaStreamEndCapture(h->L.stream, &g);
-        if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&h->graph[o], g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
-    }
+    if (!h->timing && iters > 0 && (st = ensure_graphs(h))) return st;
     for (int t = 0; t < iters; t++) {
         const int o = h->pcur;
         if (h->timing) {
