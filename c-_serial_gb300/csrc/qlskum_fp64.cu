@@ -602,6 +602,35 @@ void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
     QLSKUM_LAUNCHED(L);
 }
 
+// out[0] = max over the n points and components of |a - b|, out[1] of |a|,
+// as the bit patterns of non-negative doubles (which order like the values),
+// per-warp maxima then one atomicMax per warp; out zeroed by the caller.
+__global__ void k_max_change(int n, const double4_32a *__restrict__ a, const double4_32a *__restrict__ b,
+                             unsigned long long *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double d = 0.0, m = 0.0;
+    if (i < n) {
+        const double4_32a x = a[i], y = b[i];
+        d = fmax(fmax(fabs(x.x - y.x), fabs(x.y - y.y)), fmax(fabs(x.z - y.z), fabs(x.w - y.w)));
+        m = fmax(fmax(fabs(x.x), fabs(x.y)), fmax(fabs(x.z), fabs(x.w)));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        d = fmax(d, __shfl_down_sync(0xffffffffu, d, o));
+        m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, (unsigned long long)__double_as_longlong(d));
+        atomicMax(out + 1, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+void max_change(const Launch &L, int n, const double4_32a *a, const double4_32a *b, unsigned long long *out)
+{
+    k_max_change<<<grid_for(n, 256), 256, 0, L.stream>>>(n, a, b, out);
+    QLSKUM_LAUNCHED(L);
+}
+
 __global__ void k_set_int(int *p, int v) { *p = v; }
 
 void set_counter(const Launch &L, int *p, int v)

@@ -2972,17 +2972,15 @@ qlskum_status qlskum_adjoint_fixed_point(qlskum_handle *h, int objective, int ad
     double bu[2];
     if ((st = d2h(h, bu, a->buinf, sizeof bu))) return st;
     if (adj_change) {
-        std::vector<double4_32a> l1(np), l0(np);
-        if ((st = d2h(h, l1.data(), a->lam, sizeof(double4_32a) * np))) return st;
-        if ((st = d2h(h, l0.data(), a->lam_prev, sizeof(double4_32a) * np))) return st;
-        double dmax = 0.0, lmax = 0.0;
-        for (int pp = 0; pp < h->n; pp++) {
-            const double *x1 = &l1[pp].x, *x0 = &l0[pp].x;
-            for (int r = 0; r < 4; r++) {
-                dmax = std::max(dmax, std::fabs(x1[r] - x0[r]));
-                lmax = std::max(lmax, std::fabs(x1[r]));
-            }
-        }
+        // relative change of the last adjoint iteration, reduced on the device
+        unsigned long long *d_mx = reinterpret_cast<unsigned long long *>(a->buinf + 2);
+        zero(h, d_mx, 2 * sizeof(unsigned long long));
+        fp64::max_change(h->L, h->n, a->lam, a->lam_prev, d_mx);
+        unsigned long long mx[2];
+        if ((st = d2h(h, mx, d_mx, sizeof mx))) return st;
+        double dmax, lmax;
+        std::memcpy(&dmax, &mx[0], sizeof dmax);
+        std::memcpy(&lmax, &mx[1], sizeof lmax);
         *adj_change = lmax > 0.0 ? dmax / lmax : dmax;
     }
     const double binit[2] = {0, 0};

@@ -266,6 +266,8 @@ void copy_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst)
 void add_prim(const Launch &L, int n, const double4_32a *src, double4_32a *dst);
 // dst[i] = v for i < n
 void fill_prim(const Launch &L, int n, double4_32a v, double4_32a *dst);
+// out[0] = max |a - b|, out[1] = max |a| over n points (as non-negative double bit patterns; out zeroed first)
+void max_change(const Launch &L, int n, const double4_32a *a, const double4_32a *b, unsigned long long *out);
 // *p = v on the stream (the iteration counter a captured iteration reads)
 void set_counter(const Launch &L, int *p, int v);
 // out[0] += sum_i src[i].y, out[1] += sum_i src[i].z
