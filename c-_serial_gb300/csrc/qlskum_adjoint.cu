@@ -85,9 +85,9 @@ template <bool GEO>
 __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__restrict__ q,
                                                const double4_32a *__restrict__ dq, const double4_32a *__restrict__ qm,
                                                const double *__restrict__ delta, const double4_32a *__restrict__ flux,
-                                               const double4_32a *__restrict__ bF, double4_32a *__restrict__ bq,
-                                               double4_32a *__restrict__ bdq, double4_32a *__restrict__ bqm,
-                                               double *__restrict__ bdelta)
+                                               const double *__restrict__ sums, const double4_32a *__restrict__ bF,
+                                               double4_32a *__restrict__ bq, double4_32a *__restrict__ bdq,
+                                               double4_32a *__restrict__ bqm, double *__restrict__ bdelta)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.c.n) return;
@@ -107,13 +107,22 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
     const double scale = (f == kWall) ? 2.0 : 1.0;
     const bool used[4] = {true, true, f != kWall, f != kOuter};
 
-    // forward: the directional sums, for the bars of the moments (GEO only;
-    // without them the bar of delta comes from the stage's flux residual,
-    // F = delta * scale * sum_d G_d, so dF/ddelta = F / delta)
+    // forward: the directional sums, for the bars of the moments (GEO only:
+    // the forward kernel's stored sums, or recomputed; without them the bar of
+    // delta comes from the stage's flux residual, F = delta * scale * sum_d G_d,
+    // so dF/ddelta = F / delta)
     double sx[4][4], sy[4][4];
     for (int d = 0; d < 4; d++)
         for (int r = 0; r < 4; r++) sx[d][r] = sy[d][r] = 0.0;
-    for (int j = 0; GEO && j < nb; j++) {
+    if (GEO && sums) {
+        const double *o = sums + 32 * (size_t)i;
+        for (int d = 0; d < 4; d++)
+            for (int r = 0; r < 4; r++) {
+                sx[d][r] = o[8 * d + r];
+                sy[d][r] = o[8 * d + 4 + r];
+            }
+    }
+    for (int j = 0; GEO && !sums && j < nb; j++) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         const double4_32a g = c.e_geo[e];
@@ -1014,15 +1023,15 @@ void update(const Launch &L, const AdjView &a, const CaseConst &K, const double4
 }
 
 void flux(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
-          const double *delta, const double4_32a *flux, const double4_32a *bF, double4_32a *bq, double4_32a *bdq,
-          double4_32a *bqm, double *bdelta)
+          const double *delta, const double4_32a *flux, const double *sums, const double4_32a *bF, double4_32a *bq,
+          double4_32a *bdq, double4_32a *bqm, double *bdelta)
 {
     if (a.bedge)
-        adjk::k_flux<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, bF, bq, bdq,
-                                                                             bqm, bdelta);
+        adjk::k_flux<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, sums, bF, bq,
+                                                                             bdq, bqm, bdelta);
     else
-        adjk::k_flux<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, bF, bq,
-                                                                              bdq, bqm, bdelta);
+        adjk::k_flux<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, nullptr, bF,
+                                                                              bq, bdq, bqm, bdelta);
 }
 
 void inner(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq_in,

@@ -164,9 +164,12 @@ __global__ void k_func_delta(DevCloud c, const double4_32a *__restrict__ prim, d
 // in the reference's neighbour order, so the sums are the reference's.
 // G[d] returns the solved derivative of sub-stencil d (xpos, xneg, ypos,
 // yneg); unused directions are left at 0.
+// sums (or NULL): the directional sums {sx[d][0..3], sy[d][0..3]} of each d,
+// 32 doubles per point, kept for the reverse's moment bars.
 __device__ __forceinline__ void point_flux(const DevCloud &c, int i, int f, double nx, double ny,
                                            const double4_32a *__restrict__ q, const double4_32a *__restrict__ dq,
-                                           const double4_32a *__restrict__ qm, double G[4][4])
+                                           const double4_32a *__restrict__ qm, double G[4][4],
+                                           double *__restrict__ sums = nullptr)
 {
     double qi[4], dxi[4], dyi[4], mxi[4], mni[4];
     ld4(q[i], qi);
@@ -216,6 +219,16 @@ __device__ __forceinline__ void point_flux(const DevCloud &c, int i, int f, doub
         QLSKUM_ACC(3)
 #undef QLSKUM_ACC
     }
+    if (sums) {
+        double *o = sums + 32 * (size_t)i;
+#pragma unroll
+        for (int d = 0; d < 4; d++)
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                o[8 * d + r] = sx[d][r];
+                o[8 * d + 4 + r] = sy[d][r];
+            }
+    }
 #pragma unroll
     for (int d = 0; d < 4; d++) {
         const double4_32a m = c.fgeo[4 * i + d];  // sxx, syy, sxy, 1/det
@@ -239,14 +252,15 @@ __device__ __forceinline__ void combine(int f, double delta, const double G[4][4
 
 __global__ void __launch_bounds__(128) k_flux_residual(DevCloud c, const double4_32a *__restrict__ q,
                                                        const double4_32a *__restrict__ dq, const double4_32a *__restrict__ qm,
-                                                       const double *__restrict__ delta, double4_32a *__restrict__ flux_res)
+                                                       const double *__restrict__ delta, double4_32a *__restrict__ flux_res,
+                                                       double *__restrict__ sums)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     const int f = c.flag[i];
     const double2 nn = c.nrm[i];
     double G[4][4], F[4];
-    point_flux(c, i, f, nn.x, nn.y, q, dq, qm, G);
+    point_flux(c, i, f, nn.x, nn.y, q, dq, qm, G, sums);
     combine(f, delta[i], G, F);
     flux_res[i] = mk4(F);
 }
@@ -565,9 +579,9 @@ void func_delta(const Launch &L, const DevCloud &c, const double4_32a *prim, dou
 }
 
 void flux_residual(const Launch &L, const DevCloud &c, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
-                   const double *delta, double4_32a *flux_res)
+                   const double *delta, double4_32a *flux_res, double *sums)
 {
-    k_flux_residual<<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq, qm, delta, flux_res);
+    k_flux_residual<<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq, qm, delta, flux_res, sums);
     QLSKUM_LAUNCHED(L);
 }
 

@@ -1993,6 +1993,7 @@ struct Set64 {
     double4_32a *qm[4] = {};
     double *delta = nullptr;
     double4_32a *flux[4] = {};         // each stage's flux residual
+    double *sums[4] = {};              // each stage's directional sums (wall gradients only), [n][32]
 };
 
 struct AdjBuf {
@@ -2022,6 +2023,7 @@ struct AdjBuf {
     Set32 set0;
     std::vector<Set32> sets;
     DeviceArena set_arena;             // the on-demand sets (FP32 or FP64, one kind at a time)
+    bool sets_geo = false;             // the FP64 sets carry the directional sums
     float4 *bF32 = nullptr;            // bar of the flux residual
     float4 *bs32 = nullptr;            // bar of the weighted sums (delta * bF)
     AdjT T;                            // the edge list transposed (mixed reverse)
@@ -2179,9 +2181,12 @@ void alloc_set32(DeviceArena &A, size_t np, int ni, Set32 &st)
     st.cs32 = A.alloc<float>(np);
 }
 
-// The FP64 arrays of one stage-data set (its states are assigned by the caller).
-void alloc_set64(DeviceArena &A, size_t np, int ni, Set64 &st)
+// The FP64 arrays of one stage-data set (its states are assigned by the
+// caller); geo: also the directional sums of the wall-gradient reverse.
+void alloc_set64(DeviceArena &A, size_t np, int ni, Set64 &st, bool geo)
 {
+    if (geo)
+        for (auto &p : st.sums) p = A.alloc<double>(32 * np);
     for (auto &p : st.q) p = A.alloc<double4_32a>(np);
     for (auto &p : st.qm) p = A.alloc<double4_32a>(2 * np);
     st.dq.resize(4 * (size_t)(ni + 1));
@@ -2190,9 +2195,10 @@ void alloc_set64(DeviceArena &A, size_t np, int ni, Set64 &st)
     for (auto &p : st.flux) p = A.alloc<double4_32a>(np);
 }
 
-size_t set64_bytes(size_t np, int ni)
+size_t set64_bytes(size_t np, int ni, bool geo)
 {
-    return np * (5 * sizeof(double4_32a) + 4 * 32 + 4 * 64 + 4 * (size_t)(ni + 1) * 64 + 8 + 4 * 32);
+    return np * (5 * sizeof(double4_32a) + 4 * 32 + 4 * 64 + 4 * (size_t)(ni + 1) * 64 + 8 + 4 * 32 +
+                 (geo ? 4 * 32 * sizeof(double) : 0));
 }
 
 // Bytes of one set with its own states.
@@ -2225,7 +2231,7 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
     for (auto *p : {&a->bP, &a->bPacc, &a->bF, &a->lam, &a->lam_prev, &a->seed}) *p = A.alloc<double4_32a>(np);
     a->buinf = A.alloc<double>(4);  // free-stream velocity bars, then the initial-state sums
     if (need64) {
-        alloc_set64(A, np, a->ni, a->set64);
+        alloc_set64(A, np, a->ni, a->set64, geo);
         for (int k = 0; k < 5; k++) a->set64.P[k] = a->P[k];
         a->bq = A.alloc<double4_32a>(np);
         for (auto *p : {&a->bdqA, &a->bdqB, &a->bqm}) *p = A.alloc<double4_32a>(2 * np);
@@ -2305,7 +2311,7 @@ void adj_stage_forward(qlskum_handle *h, Set64 &st, int s)
     fp64::q_variables(h->L, c, st.P[s], st.q[s]);
     fp64::q_derivatives(h->L, c, st.q[s], adj_dq(st, ni, s, 0), st.qm[s], nullptr, nullptr, 0.0);
     for (int j = 1; j <= ni; j++) fp64::q_inner(h->L, c, st.q[s], adj_dq(st, ni, s, j - 1), adj_dq(st, ni, s, j));
-    fp64::flux_residual(h->L, c, st.q[s], adj_dq(st, ni, s, ni), st.qm[s], st.delta, st.flux[s]);
+    fp64::flux_residual(h->L, c, st.q[s], adj_dq(st, ni, s, ni), st.qm[s], st.delta, st.flux[s], st.sums[s]);
 }
 
 // The four stage states of one iteration from st.P[0] (fpi_solver_mod.h:14-40)
@@ -2337,8 +2343,8 @@ void adj_stage_reverse(qlskum_handle *h, const Set64 &st, int s, const AdjView &
     zero(h, a->bq, sizeof(double4_32a) * np);
     zero(h, a->bdqA, sizeof(double4_32a) * 2 * np);
     zero(h, a->bqm, sizeof(double4_32a) * 2 * np);
-    adjl::flux(h->L, v, st.q[s], adj_dq(st, ni, s, ni), st.qm[s], st.delta, st.flux[s], a->bF, a->bq, a->bdqA,
-               a->bqm, a->bdelta);
+    adjl::flux(h->L, v, st.q[s], adj_dq(st, ni, s, ni), st.qm[s], st.delta, st.flux[s], st.sums[s], a->bF, a->bq,
+               a->bdqA, a->bqm, a->bdelta);
     for (int j = ni; j >= 1; j--) {
         zero(h, a->bdqB, sizeof(double4_32a) * 2 * np);
         adjl::inner(h->L, v, st.q[s], adj_dq(st, ni, s, j - 1), a->bdqA, a->bq, a->bdqB);
@@ -2373,7 +2379,8 @@ float4 *adj_dq32(const Set32 &st, int ni, int s, int j) { return st.dq32[(size_t
 bool adj_sets(qlskum_handle *h, int count, bool f64)
 {
     AdjBuf *a = h->adj;
-    if ((f64 ? (int)a->sets64.size() : (int)a->sets.size()) >= count) return true;
+    const bool geo = f64 && a->geo;
+    if ((f64 ? (int)a->sets64.size() : (int)a->sets.size()) >= count && (!geo || a->sets_geo)) return true;
     auto drop = [&]() {
         a->sets.clear();
         a->sets64.clear();
@@ -2384,13 +2391,13 @@ bool adj_sets(qlskum_handle *h, int count, bool f64)
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
     // keep a quarter of the free memory for everything else
-    const size_t each = f64 ? set64_bytes(h->np, a->ni) : set32_bytes(h->np, a->ni);
+    const size_t each = f64 ? set64_bytes(h->np, a->ni, geo) : set32_bytes(h->np, a->ni);
     if ((double)each * count > 0.75 * (double)free_b) return false;
     std::vector<double4_32a *> p0;
     if (f64) {
         a->sets64.resize(count);
         for (auto &st : a->sets64) {
-            alloc_set64(a->set_arena, h->np, a->ni, st);
+            alloc_set64(a->set_arena, h->np, a->ni, st, geo);
             for (auto &p : st.P) p = a->set_arena.alloc<double4_32a>(h->np);
             p0.push_back(st.P[0]);
         }
@@ -2408,6 +2415,7 @@ bool adj_sets(qlskum_handle *h, int count, bool f64)
         return false;
     }
     for (auto *p : p0) zero(h, p, sizeof(double4_32a) * h->np);
+    a->sets_geo = geo;
     return true;
 }
 
@@ -2870,7 +2878,9 @@ qlskum_status qlskum_adjoint_gradient(qlskum_handle *h, int objective, int iters
     ObjSeed os;
     if ((st = adj_seed(h, objective, h->s64.prim[h->pcur], a->bP, os))) return st;
     adj_zero_geometry(h);
-    const AdjView v = adj_view(h, true);
+    // geometry bars only when this call asks for the wall gradient (the
+    // buffers may exist from an earlier call)
+    const AdjView v = adj_view(h, dJ_dwall != nullptr);
     for (int c0 = store_all ? -1 : nck - 1; c0 >= 0; c0--) {
         const int t0 = c0 * S, t1 = std::min(iters, t0 + S);
         // states t0 .. t1 - 1 of this segment: the checkpoint, then the reverse's own iterations from it
@@ -2967,7 +2977,7 @@ qlskum_status qlskum_adjoint_fixed_point(qlskum_handle *h, int objective, int ad
     // lam^T dS/dalpha: one more reverse pass, accumulating the parameter bars
     adj_zero_geometry(h);
     CK(h, cudaMemcpyAsync(a->bP, a->lam, sizeof(double4_32a) * np, cudaMemcpyDeviceToDevice, h->L.stream));
-    adj_iteration_reverse(h, adj_view(h, true), m32);
+    adj_iteration_reverse(h, adj_view(h, dJ_dwall != nullptr), m32);
     if ((st = check_launch(h, "fixed-point adjoint"))) return st;
     double bu[2];
     if ((st = d2h(h, bu, a->buinf, sizeof bu))) return st;
