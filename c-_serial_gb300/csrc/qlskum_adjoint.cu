@@ -562,6 +562,74 @@ __global__ void k_objective_J(int n, const double4_32a *__restrict__ P, double g
     bP[i] = b;
 }
 
+// The geometry bars the reverse kernels accumulated (per edge: vector,
+// rotated vector, length; per point: normal, gradient and directional LSQ
+// moments) pulled back to the point coordinates, unit weights: each point's
+// edges add to its neighbour's and its own coordinate bars (FP64 atomics),
+// and the point's normal bar (the accumulated one plus its edges' rotated
+// vectors') is stored for the host's normal pull-back.  bx, by zeroed first.
+__global__ void k_geom_pullback(AdjView a, double *__restrict__ bx, double *__restrict__ by,
+                                double2 *__restrict__ bn)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.c.n) return;
+    const DevCloud &c = a.c;
+    const double2 nn = c.nrm[i];
+    const double nx = nn.x, ny = nn.y;
+    // bars of the three sums from those of {sxx, syy, sxy, 1/det} as the kernels read them
+    auto mom_bar = [](const double4_32a &m, const double4_32a &b, double &bxx, double &byy, double &bxy) {
+        bxx = b.x;
+        byy = b.y;
+        bxy = b.z;
+        if (b.w == 0.0) return;
+        const double bdet = -b.w * m.w * m.w;
+        bxx += bdet * m.y;
+        byy += bdet * m.x;
+        bxy -= 2.0 * m.z * bdet;
+    };
+    double gbxx, gbyy, gbxy, fbxx[4], fbyy[4], fbxy[4];
+    mom_bar(c.ggeo[i], a.bgmom[i], gbxx, gbyy, gbxy);
+    for (int d = 0; d < 4; d++) mom_bar(c.fgeo[4 * i + d], a.bfmom[4 * i + d], fbxx[d], fbyy[d], fbxy[d]);
+    double2 bni = a.bnrm[i];
+    double sx = 0.0, sy = 0.0;
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const int k = c.e_nbr[e];
+        const double4_32a g = c.e_geo[e], be = a.bedge[e];
+        const double2 sn = c.e_sn[e];
+        const double dx = g.x, dy = g.y, ds = sn.x, dn = sn.y;
+        double bdx = be.x + 2.0 * dx * gbxx + dy * gbxy;
+        double bdy = be.y + 2.0 * dy * gbyy + dx * gbxy;
+        double bds = be.z, bdn = be.w;
+        const unsigned bits = c.e_dir[e];
+        for (int d = 0; d < 4; d++)
+            if (bits & (1u << d)) {
+                bds += 2.0 * ds * fbxx[d] + dn * fbxy[d];
+                bdn += 2.0 * dn * fbyy[d] + ds * fbxy[d];
+            }
+        // ds = dx ny - dy nx, dn = dx nx + dy ny
+        bdx += bds * ny + bdn * nx;
+        bdy += -bds * nx + bdn * ny;
+        bni.x += -bds * dy + bdn * dx;
+        bni.y += bds * dx + bdn * dy;
+        const double bd = a.bdist[e];
+        if (bd != 0.0) {
+            const double dist = c.e_dist[e];
+            bdx += bd * dx / dist;
+            bdy += bd * dy / dist;
+        }
+        atomicAdd(bx + k, bdx);
+        atomicAdd(by + k, bdy);
+        sx += bdx;
+        sy += bdy;
+    }
+    atomicAdd(bx + i, -sx);
+    atomicAdd(by + i, -sy);
+    bn[i] = bni;
+}
+
 }  // namespace adjk
 
 // ---------------------------------------------------------------------------
@@ -1078,6 +1146,11 @@ void objective(const Launch &L, const AdjView &a, const int *wall_perm, const do
     if (n_wall > 0)
         adjk::k_objective<<<adjk::grid_for(n_wall, 128), 128, 0, L.stream>>>(a, wall_perm, wall_geo, n_wall, cp_scale,
                                                                             theta, which, bP);
+}
+
+void geom_pullback(const Launch &L, const AdjView &a, double *bx, double *by, double2 *bn)
+{
+    adjk::k_geom_pullback<<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, bx, by, bn);
 }
 
 }  // namespace adjl

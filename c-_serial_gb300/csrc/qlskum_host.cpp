@@ -2012,6 +2012,8 @@ struct AdjBuf {
     double *bdist = nullptr;
     double2 *bnrm = nullptr;
     double4_32a *bgmom = nullptr, *bfmom = nullptr;
+    double *gbx = nullptr, *gby = nullptr;  // coordinate bars (geom_pullback)
+    double2 *gbn = nullptr;                 // normal bars (geom_pullback)
     // the checkpointed primal: the state of every stride-th iteration, and
     // the states of one stride-long segment recomputed during the reverse sweep
     double4_32a *ckpt = nullptr;
@@ -2254,6 +2256,9 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
         a->bdist = A.alloc<double>(a->ne);
         a->bnrm = A.alloc<double2>(np);
         a->bgmom = A.alloc<double4_32a>(np);
+        a->gbx = A.alloc<double>(np);
+        a->gby = A.alloc<double>(np);
+        a->gbn = A.alloc<double2>(np);
         a->bfmom = A.alloc<double4_32a>(4 * np);
     }
     if (A.err != cudaSuccess) {
@@ -2565,90 +2570,30 @@ void adj_params(const qlskum_handle *h, const ObjSeed &o, const double buinf[2],
 qlskum_status adj_geometry(qlskum_handle *h, int which, const double4_32a *prim_dev, double *dJ_dwall)
 {
     AdjBuf *a = h->adj;
-    const int n = h->n, NB = QLSKUM_MAX_NBHS;
+    const int n = h->n;
     const size_t np = h->np;
     const std::vector<double> &X = h->hx, &Y = h->hy;
-    std::vector<double4_32a> bedge(a->ne), bgmom(np), bfmom(4 * np), prim(np);
-    std::vector<double> bdist(a->ne);
-    std::vector<double2> bnrm(np);
+    // the edge and moment bars to coordinate bars on the device
+    zero(h, a->gbx, sizeof(double) * np);
+    zero(h, a->gby, sizeof(double) * np);
+    adjl::geom_pullback(h->L, adj_view(h, true), a->gbx, a->gby, a->gbn);
     qlskum_status st;
-    if ((st = d2h(h, bedge.data(), a->bedge, sizeof(double4_32a) * a->ne))) return st;
-    if ((st = d2h(h, bdist.data(), a->bdist, sizeof(double) * a->ne))) return st;
-    if ((st = d2h(h, bnrm.data(), a->bnrm, sizeof(double2) * np))) return st;
-    if ((st = d2h(h, bgmom.data(), a->bgmom, sizeof(double4_32a) * np))) return st;
-    if ((st = d2h(h, bfmom.data(), a->bfmom, sizeof(double4_32a) * 4 * np))) return st;
+    if ((st = check_launch(h, "geometry pull-back"))) return st;
+    std::vector<double> gx(np), gy(np);
+    std::vector<double2> gn(np);
+    std::vector<double4_32a> prim(np);
+    if ((st = d2h(h, gx.data(), a->gbx, sizeof(double) * np))) return st;
+    if ((st = d2h(h, gy.data(), a->gby, sizeof(double) * np))) return st;
+    if ((st = d2h(h, gn.data(), a->gbn, sizeof(double2) * np))) return st;
     if ((st = d2h(h, prim.data(), prim_dev, sizeof(double4_32a) * np))) return st;
-    const std::vector<long long> sbase = slice_bases(h, nullptr);
-    std::vector<double> bx(n, 0.0), by(n, 0.0), bnx(n, 0.0), bny(n, 0.0);
-    // (1/det) = 1 / (sxx syy - sxy^2): bars of the three sums from those of
-    // {sxx, syy, sxy, 1/det} as the kernels read them
-    auto mom_bar = [](double sxx, double syy, double sxy, const double4_32a &b, double &bxx, double &byy,
-                      double &bxy) {
-        bxx = b.x;
-        byy = b.y;
-        bxy = b.z;
-        if (b.w == 0.0) return;
-        const double ood = 1.0 / (sxx * syy - sxy * sxy);
-        const double bdet = -b.w * ood * ood;
-        bxx += bdet * syy;
-        byy += bdet * sxx;
-        bxy -= 2.0 * sxy * bdet;
-    };
-    std::vector<double> dx(NB), dy(NB), ds(NB), dn(NB);
-    for (int pp = 0; pp < n; pp++) {
-        const int i = h->iperm[pp];
-        const int nb = h->hnbhs[i];
-        const double nx = h->pc.nx[i], ny = h->pc.ny[i];
-        bnx[i] += bnrm[pp].x;
-        bny[i] += bnrm[pp].y;
-        double gxx = 0, gyy = 0, gxy = 0, fxx[4] = {0, 0, 0, 0}, fyy[4] = {0, 0, 0, 0}, fxy[4] = {0, 0, 0, 0};
-        for (int r = 0; r < nb; r++) {
-            const int k = h->hconn[(size_t)i * NB + r] - 1;
-            dx[r] = X[k] - X[i];
-            dy[r] = Y[k] - Y[i];
-            ds[r] = dx[r] * ny - dy[r] * nx;
-            dn[r] = dx[r] * nx + dy[r] * ny;
-            gxx += dx[r] * dx[r];
-            gyy += dy[r] * dy[r];
-            gxy += dx[r] * dy[r];
-            const unsigned bits = h->pc.edge_dir[(size_t)i * NB + r];
-            for (int d = 0; d < 4; d++)
-                if (bits & (1u << d)) {
-                    fxx[d] += ds[r] * ds[r];
-                    fyy[d] += dn[r] * dn[r];
-                    fxy[d] += ds[r] * dn[r];
-                }
-        }
-        double gbxx, gbyy, gbxy, fbxx[4], fbyy[4], fbxy[4];
-        mom_bar(gxx, gyy, gxy, bgmom[pp], gbxx, gbyy, gbxy);
-        for (int d = 0; d < 4; d++) mom_bar(fxx[d], fyy[d], fxy[d], bfmom[4 * (size_t)pp + d], fbxx[d], fbyy[d], fbxy[d]);
-        for (int r = 0; r < nb; r++) {
-            const size_t e = (size_t)(sbase[pp >> 5] + 32LL * r + (pp & 31));
-            const int k = h->hconn[(size_t)i * NB + r] - 1;
-            double bdx = bedge[e].x + 2.0 * dx[r] * gbxx + dy[r] * gbxy;
-            double bdy = bedge[e].y + 2.0 * dy[r] * gbyy + dx[r] * gbxy;
-            double bds = bedge[e].z, bdn = bedge[e].w;
-            const unsigned bits = h->pc.edge_dir[(size_t)i * NB + r];
-            for (int d = 0; d < 4; d++)
-                if (bits & (1u << d)) {
-                    bds += 2.0 * ds[r] * fbxx[d] + dn[r] * fbxy[d];
-                    bdn += 2.0 * dn[r] * fbyy[d] + ds[r] * fbxy[d];
-                }
-            // ds = dx ny - dy nx, dn = dx nx + dy ny
-            bdx += bds * ny + bdn * nx;
-            bdy += -bds * nx + bdn * ny;
-            bnx[i] += -bds * dy[r] + bdn * dx[r];
-            bny[i] += bds * dx[r] + bdn * dy[r];
-            if (bdist[e] != 0.0) {
-                const double dist = std::sqrt(dx[r] * dx[r] + dy[r] * dy[r]);
-                bdx += bdist[e] * dx[r] / dist;
-                bdy += bdist[e] * dy[r] / dist;
-            }
-            bx[k] += bdx;
-            bx[i] -= bdx;
-            by[k] += bdy;
-            by[i] -= bdy;
-        }
+    // in the cloud's order
+    std::vector<double> bx(n), by(n), bnx(n), bny(n);
+    for (int i = 0; i < n; i++) {
+        const int pp = h->perm[i];
+        bx[i] = gx[pp];
+        by[i] = gy[pp];
+        bnx[i] = gn[pp].x;
+        bny[i] = gn[pp].y;
     }
     // the objective's geometry: H = sum cp nx ds, V = sum cp ny ds with
     // ds = (|x_m - x_l| + |x_r - x_m|) / 2 (compute_force_coeffs_mod.h:37-59);

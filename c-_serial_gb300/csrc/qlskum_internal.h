@@ -200,6 +200,9 @@ void objective(const Launch &L, const AdjView &a, const int *wall_perm, const do
                double cp_scale, double theta, int which, double4_32a *bP);
 // bP += dJ/dprim of the stagnation-pressure loss
 void objective_J(const Launch &L, int n, const double4_32a *P, double gamma, double p0_inf, double4_32a *bP);
+// the geometry bars of a reverse sweep pulled back to the point coordinates
+// (bx, by zeroed first; bn: each point's normal bar), unit weights
+void geom_pullback(const Launch &L, const AdjView &a, double *bx, double *by, double2 *bn);
 }  // namespace adjl
 
 // Reverse of the mixed iteration (qlskum_adjoint.cu, FP32 edge work): bars of
