@@ -163,3 +163,26 @@ def test_mixed_precision_error(qlskum):
     zl, zd, zm, ze = z["objectives"]
     assert abs(cl - zl) < 1e-4 and abs(cd - zd) < 1e-4, (cl, zl, cd, zd)
     assert abs(ent - ze) / ze < 1e-3
+
+
+def test_mixed_vs_fp64_full_size_transonic(qlskum):
+    """The mixed form against the FP64 form at full size: the 1,024,000-point
+    transonic cloud (1024 wall points x 1000 layers, M 0.85, AoA 1, 3 inner
+    iterations), 20 iterations from the free stream.  The tolerance the mixed
+    form is held to: |dCl|, |dCd| <= 1e-5; the state within 1e-4 of the
+    largest magnitude per component; the residual norm (res_new) of every
+    iteration within 1e-3 relative."""
+    from qlskum import cloudgen
+    c = cloudgen.make_cloud(n_wall=1024, n_layers=1000, first_spacing=2e-3, radius=20.0, seed=2)
+    kw = dict(mach=0.85, aoa=1.0, cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=3)
+    m = qlskum.Solver(c, precision=qlskum.MIXED, **kw)
+    d = qlskum.Solver(c, precision=qlskum.FP64, **kw)
+    m.q_lskum(20)
+    d.q_lskum(20)
+    cl_m, cd_m, _, _ = m.objective()
+    cl_d, cd_d, _, _ = d.objective()
+    assert abs(cl_m - cl_d) <= 1e-5 and abs(cd_m - cd_d) <= 1e-5, (cl_m, cl_d, cd_m, cd_d)
+    pm, pd = m.prim, d.prim
+    assert np.isfinite(pm).all()
+    assert rel_err(pm, pd) < 1e-4
+    np.testing.assert_allclose(m.residual_history()[:, 0], d.residual_history()[:, 0], rtol=1e-3)
