@@ -200,7 +200,8 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
     }
     bdelta[i] += bdl;
 
-    // reverse over the edges
+    // reverse over the edges, one end at a time (end64 / end64_vjp): the
+    // neighbour's end first, its bars scattered, then the owner's
     double bqi[4] = {0, 0, 0, 0}, bdxi[4] = {0, 0, 0, 0}, bdyi[4] = {0, 0, 0, 0}, bmxi[4] = {0, 0, 0, 0},
            bmni[4] = {0, 0, 0, 0};
     double bnx = 0.0, bny = 0.0;
@@ -210,69 +211,56 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
         const double4_32a g = c.e_geo[e];
         const double2 sw = c.e_sn[e];
         const unsigned dir = c.e_dir[e];
-        double qk[4], dxk[4], dyk[4], mxk[4], mnk[4], Pi[4], Pk[4];
-        ld4(q[k], qk);
-        ld4(dq[2 * k], dxk);
-        ld4(dq[2 * k + 1], dyk);
-        ld4(qm[2 * k], mxk);
-        ld4(qm[2 * k + 1], mnk);
-        edge_states<double>(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, c.eps2[k], Pi, Pk);
-        Kin<double> ki, kk;
-        kin_prep<double>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
-        kin_prep<double>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
-        KinBar kbi, kbk;
-        double bsw_x = 0.0, bsw_y = 0.0;
-#define QLSKUM_REV(D)                                                                \
+        double bdelx = 0.0, bdely = 0.0, bsw_x = 0.0, bsw_y = 0.0;
+        // the bar of G_k on half-range D is bsx sw.x + bsy sw.y, that of G_i its negative
+#define QLSKUM_REV(D, SGN, KIN, KB)                                                  \
         if (dir & (1u << D)) {                                                       \
-            double bGk[4], bGi[4];                                                   \
-            for (int r = 0; r < 4; r++) {                                            \
-                bGk[r] = bsx[D][r] * sw.x + bsy[D][r] * sw.y;                        \
-                bGi[r] = -bGk[r];                                                    \
-            }                                                                        \
-            adj::dir_flux_vjp<D>(f, kk, bGk, kbk);                                   \
-            adj::dir_flux_vjp<D>(f, ki, bGi, kbi);                                   \
+            double bG[4];                                                            \
+            for (int r = 0; r < 4; r++) bG[r] = SGN * (bsx[D][r] * sw.x + bsy[D][r] * sw.y); \
+            adj::dir_flux_vjp<D>(f, KIN, bG, KB);                                    \
             if (GEO) {                                                               \
-                double Gi[4], Gk[4];                                                 \
-                dir_flux<double, D>(f, ki, Gi);                                      \
-                dir_flux<double, D>(f, kk, Gk);                                      \
+                double G[4];                                                         \
+                dir_flux<double, D>(f, KIN, G);                                      \
                 for (int r = 0; r < 4; r++) {                                        \
-                    bsw_x += bsx[D][r] * (Gk[r] - Gi[r]);                            \
-                    bsw_y += bsy[D][r] * (Gk[r] - Gi[r]);                            \
+                    bsw_x += SGN * bsx[D][r] * G[r];                                 \
+                    bsw_y += SGN * bsy[D][r] * G[r];                                 \
                 }                                                                    \
             }                                                                        \
         }
-        QLSKUM_REV(0)
-        QLSKUM_REV(1)
-        QLSKUM_REV(2)
-        QLSKUM_REV(3)
-#undef QLSKUM_REV
-        double bPi[4] = {0, 0, 0, 0}, bPk[4] = {0, 0, 0, 0};
-        adj::kin_vjp(nx, ny, Pi, ki, kbi, bPi, bnx, bny);
-        adj::kin_vjp(nx, ny, Pk, kk, kbk, bPk, bnx, bny);
-        // qtilde_to_prim outputs are (u1, u2, rho, p) in the edge_states order P = (rho, u1, u2, p)
-        double ti[4], tk[4];
-        for (int r = 0; r < 4; r++) {
-            const double gi = g.x * dxi[r] + g.y * dyi[r];
-            const double gk = g.x * dxk[r] + g.y * dyk[r];
-            const double phi_i = venkat(qi[r] - 0.5 * gi, qi[r], mxi[r], mni[r], e2i);
-            const double phi_k = venkat(qk[r] - 0.5 * gk, qk[r], mxk[r], mnk[r], c.eps2[k]);
-            ti[r] = qi[r] - 0.5 * phi_i * gi;
-            tk[r] = qk[r] - 0.5 * phi_k * gk;
+        {
+            double qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
+            ld4(q[k], qk);
+            ld4(dq[2 * k], dxk);
+            ld4(dq[2 * k + 1], dyk);
+            ld4(qm[2 * k], mxk);
+            ld4(qm[2 * k + 1], mnk);
+            adj::End64 s;
+            adj::end64(nx, ny, g.x, g.y, qk, dxk, dyk, mxk, mnk, c.eps2[k], s);
+            KinBar kb;
+            QLSKUM_REV(0, 1.0, s.k, kb)
+            QLSKUM_REV(1, 1.0, s.k, kb)
+            QLSKUM_REV(2, 1.0, s.k, kb)
+            QLSKUM_REV(3, 1.0, s.k, kb)
+            double bqk[4] = {0, 0, 0, 0}, bdxk[4] = {0, 0, 0, 0}, bdyk[4] = {0, 0, 0, 0}, bmxk[4] = {0, 0, 0, 0},
+                   bmnk[4] = {0, 0, 0, 0};
+            adj::end64_vjp(s, nx, ny, g.x, g.y, dxk, dyk, kb, bqk, bdxk, bdyk, bmxk, bmnk, bdelx, bdely, bnx, bny);
+            atomic_add4(bq + k, bqk);
+            atomic_add4(bdq + 2 * k, bdxk);
+            atomic_add4(bdq + 2 * k + 1, bdyk);
+            atomic_add4(bqm + 2 * k, bmxk);
+            atomic_add4(bqm + 2 * k + 1, bmnk);
         }
-        double bti[4] = {0, 0, 0, 0}, btk[4] = {0, 0, 0, 0};
-        adj::qtilde_to_prim_vjp(ti, bPi, bti);
-        adj::qtilde_to_prim_vjp(tk, bPk, btk);
-        double bdelx = 0.0, bdely = 0.0;
-        adj::edge_end_vjp(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, bti, bqi, bdxi, bdyi, bmxi, bmni, bdelx, bdely);
-        double bqk[4] = {0, 0, 0, 0}, bdxk[4] = {0, 0, 0, 0}, bdyk[4] = {0, 0, 0, 0}, bmxk[4] = {0, 0, 0, 0},
-               bmnk[4] = {0, 0, 0, 0};
-        adj::edge_end_vjp(g.x, g.y, qk, dxk, dyk, mxk, mnk, c.eps2[k], btk, bqk, bdxk, bdyk, bmxk, bmnk, bdelx,
-                          bdely);
-        atomic_add4(bq + k, bqk);
-        atomic_add4(bdq + 2 * k, bdxk);
-        atomic_add4(bdq + 2 * k + 1, bdyk);
-        atomic_add4(bqm + 2 * k, bmxk);
-        atomic_add4(bqm + 2 * k + 1, bmnk);
+        {
+            adj::End64 s;
+            adj::end64(nx, ny, g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, s);
+            KinBar kb;
+            QLSKUM_REV(0, -1.0, s.k, kb)
+            QLSKUM_REV(1, -1.0, s.k, kb)
+            QLSKUM_REV(2, -1.0, s.k, kb)
+            QLSKUM_REV(3, -1.0, s.k, kb)
+            adj::end64_vjp(s, nx, ny, g.x, g.y, dxi, dyi, kb, bqi, bdxi, bdyi, bmxi, bmni, bdelx, bdely, bnx, bny);
+        }
+#undef QLSKUM_REV
         if (GEO) {
             double4_32a &ge = a.bedge[e];
             ge.x += bdelx;

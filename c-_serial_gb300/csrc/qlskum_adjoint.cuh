@@ -212,6 +212,135 @@ template <typename R> QLSKUM_HD void edge_end_vjp(R delx, R dely, const R q[4], 
     }
 }
 
+// One edge end of the FP64 reverse, evaluated once per edge and end: the
+// limited reconstruction (interior_fluxes_mod.h:72-83, limiters_mod.h:64-104),
+// q~ -> prim (q_variables_mod.h:230-253) and the half-range moments
+// (split_fluxes_mod.h:14-26), keeping what end64_vjp reads.  The functions
+// above recompute each quantity they need (an edge end then costs 33 FP64
+// divisions, 6 exps and 2 logs); here one end costs 7 divisions, 3 exps and
+// 1 log.  The forward values are those of edge_states / kin_prep up to
+// last-bit roundings: the limiter's ratio is num * (1 / den), whose
+// reciprocal the VJP reads too; kin_prep's beta = rho / (2 p) and
+// p / rho are the q~ -> prim step's beta and 1 / (2 beta); 1 / (gamma - 1)
+// and 1 / sqrt(pi beta) are multiplications.  The reverse is the derivative
+// at that state, along the branches it took.
+struct End64 {
+    double g[4], dn[4], dp[4], rden[4], t[4];  // per component: g, q~u - q, qmax|qmin - q, 1 / den, num / den
+    double eps2, qt1, qt2, beta, tm, u1, u2, rho, sb, rsb, e1, e2;
+    Kin<double> k;
+};
+
+QLSKUM_HD void end64(double nx, double ny, double delx, double dely, const double q[4], const double dx[4],
+                     const double dy[4], const double mx[4], const double mn[4], double e2, End64 &s)
+{
+    constexpr double inv_gm1 = 1.0 / (1.4 - 1.0);
+    double qt[4];
+    for (int r = 0; r < 4; r++) {
+        const double g = delx * dx[r] + dely * dy[r];
+        const double dn = (q[r] - 0.5 * g) - q[r];
+        const double dp = ((dn > 0.0) ? mx[r] : mn[r]) - q[r];
+        const double num = (dp * dp + e2) * dn + 2.0 * dn * dn * dp;
+        const double den = ((dp * dp + 2.0 * dn * dn) + dn * dp + e2) * dn;
+        const bool cut = fabs(dn) <= 10e-6;
+        const double rden = 1.0 / (cut ? 1.0 : den);
+        const double t = num * rden;
+        const double phi = (cut || !(t < 1.0)) ? 1.0 : t;
+        s.g[r] = g;
+        s.dn[r] = dn;
+        s.dp[r] = dp;
+        s.rden[r] = rden;
+        s.t[r] = cut ? 1.0 : t;
+        qt[r] = q[r] - 0.5 * phi * g;
+    }
+    s.eps2 = e2;
+    s.qt1 = qt[1];
+    s.qt2 = qt[2];
+    s.beta = -qt[3] * 0.5;
+    s.tm = 0.5 / s.beta;
+    s.u1 = qt[1] * s.tm;
+    s.u2 = qt[2] * s.tm;
+    s.rho = M<double>::ex(qt[0] + s.beta * (s.u1 * s.u1 + s.u2 * s.u2) - M<double>::lg(s.beta) * inv_gm1);
+    s.k.rho = s.rho;
+    s.k.ut = s.u1 * ny - s.u2 * nx;
+    s.k.un = s.u1 * nx + s.u2 * ny;
+    s.sb = M<double>::sq(s.beta);
+    s.rsb = 1.0 / s.sb;
+    const double S1 = s.k.ut * s.sb, S2 = s.k.un * s.sb;
+    s.e1 = M<double>::ex(-S1 * S1);
+    s.e2 = M<double>::ex(-S2 * S2);
+    const double half_rpi = 0.28209479177387814;  // 1 / (2 sqrt(pi))
+    s.k.B1 = half_rpi * s.e1 * s.rsb;
+    s.k.B2 = half_rpi * s.e2 * s.rsb;
+    s.k.E1 = erf_e<double>(S1, s.e1);
+    s.k.E2 = erf_e<double>(S2, s.e2);
+    s.k.pbr = s.tm;
+    s.k.usq = s.k.ut * s.k.ut + s.k.un * s.k.un;
+}
+
+// Reverse of end64 for the bar kb of its moments (the sum of dir_flux_vjp
+// over the edge's half-ranges): kin_vjp, qtilde_to_prim_vjp and edge_end_vjp
+// on the kept intermediates.  Adds the bars of the end's q, dq (x, y), qm
+// (max, min), of the edge vector and of the normal.
+QLSKUM_HD void end64_vjp(const End64 &s, double nx, double ny, double delx, double dely, const double dx[4],
+                         const double dy[4], const KinBar &kb, double bq[4], double bdx[4], double bdy[4],
+                         double bmx[4], double bmn[4], double &bdelx, double &bdely, double &bnx, double &bny)
+{
+    constexpr double inv_gm1 = 1.0 / (1.4 - 1.0);
+    const double two_over_sqrtpi = 1.1283791670955126;
+    // kin_prep of P = (rho, u1, u2, p), p = rho tm, beta = rho / (2 p)
+    const double ut = s.k.ut, un = s.k.un;
+    const double S1 = ut * s.sb, S2 = un * s.sb;
+    double but = kb.ut + 2.0 * ut * kb.usq;
+    double bun = kb.un + 2.0 * un * kb.usq;
+    const double bS1 = kb.E1 * two_over_sqrtpi * s.e1 + kb.B1 * s.k.B1 * (-2.0 * S1);
+    const double bS2 = kb.E2 * two_over_sqrtpi * s.e2 + kb.B2 * s.k.B2 * (-2.0 * S2);
+    but += bS1 * s.sb;
+    bun += bS2 * s.sb;
+    const double bsb = bS1 * ut + bS2 * un;
+    const double bbk = 0.5 * bsb * s.rsb - (kb.B1 * s.k.B1 + kb.B2 * s.k.B2) * s.tm;  // 0.5 / beta = tm
+    const double irho = 1.0 / s.rho;
+    // 0.5 / p = beta / rho, p / rho^2 = tm / rho, beta / p = 2 beta^2 / rho
+    const double bP0 = kb.rho + bbk * s.beta * irho - kb.pbr * s.tm * irho;
+    const double bP3 = -bbk * 2.0 * s.beta * s.beta * irho + kb.pbr * irho;
+    const double bP1 = but * ny + bun * nx;
+    const double bP2 = -but * nx + bun * ny;
+    bnx += -but * s.u2 + bun * s.u1;
+    bny += but * s.u1 + bun * s.u2;
+    // q~ -> prim: rho = exp(q0 + beta |u|^2 - log(beta) / (gamma - 1)), u = q~(1:2) tm, p = rho tm
+    const double brho = bP0 + bP3 * s.tm;
+    const double bT1 = brho * s.rho;
+    const double bu1 = bP1 + bT1 * 2.0 * s.beta * s.u1;
+    const double bu2 = bP2 + bT1 * 2.0 * s.beta * s.u2;
+    const double bt = bP3 * s.rho + bu1 * s.qt1 + bu2 * s.qt2;
+    // 1 / beta = 2 tm, 0.5 / beta^2 = 2 tm^2
+    const double bbeta = bT1 * (s.u1 * s.u1 + s.u2 * s.u2) - bT1 * inv_gm1 * 2.0 * s.tm - bt * 2.0 * s.tm * s.tm;
+    const double bqt[4] = {bT1, bu1 * s.tm, bu2 * s.tm, -0.5 * bbeta};
+    // the limited reconstruction q~ = q - phi g / 2, phi = num / den of
+    // dn = (q - g / 2) - q and dp = qmax - q (dn > 0) or qmin - q
+    for (int r = 0; r < 4; r++) {
+        const double dn = s.dn[r], dp = s.dp[r], t = s.t[r];
+        const bool lim = fabs(dn) > 10e-6 && t < 1.0;
+        double bg = -0.5 * (lim ? t : 1.0) * bqt[r];
+        double bdp = 0.0;
+        if (lim) {
+            const double bphi = -0.5 * s.g[r] * bqt[r];
+            const double bnum = bphi * s.rden[r], bden = -bphi * t * s.rden[r];
+            const double bdn = bnum * (dp * dp + s.eps2 + 4.0 * dn * dp) +
+                               bden * ((dp * dp + 2.0 * dn * dn + dn * dp + s.eps2) + dn * (4.0 * dn + dp));
+            bdp = bnum * (2.0 * dp * dn + 2.0 * dn * dn) + bden * (dn * (2.0 * dp + dn));
+            bg += -0.5 * bdn;
+            if (dn > 0.0) bmx[r] += bdp;
+            else bmn[r] += bdp;
+        }
+        // q enters q~ directly and through dp (dn - its own rounding aside - is -g / 2)
+        bq[r] += bqt[r] - bdp;
+        bdx[r] += bg * delx;
+        bdy[r] += bg * dely;
+        bdelx += bg * dx[r];
+        bdely += bg * dy[r];
+    }
+}
+
 // primitive_to_conserved (state_update_mod.h:18-33)
 template <typename R>
 QLSKUM_HD void p2c_vjp(const R P[4], R nx, R ny, const R bU[4], R bP[4], R &bnx, R &bny)

@@ -102,6 +102,58 @@ void qlskum_dbg_edge_end_vjp(const double *in, double e2, double delx, double de
                       out + 16, out[20], out[21]);
 }
 
+// One edge end as the FP64 solver evaluates it: the limited reconstruction,
+// q~ -> prim and the flux of half-range D of a class-f point in the frame of
+// (nx, ny).  in: [q4 dx4 dy4 mx4 mn4] (20), e2, delx, dely -> G (4)
+void qlskum_dbg_end_flux(int f, int D, const double *in, double e2, double delx, double dely, double nx, double ny,
+                         double *G)
+{
+    double qt[4], P[4];
+    qlskum_dbg_edge_end(in, e2, delx, dely, qt);
+    qtilde_to_prim<double>(qt, P[1], P[2], P[0], P[3]);
+    qlskum_dbg_dir_flux(f, D, nx, ny, P, G);
+}
+
+namespace {
+adj::End64 end64_of(const double *in, double e2, double delx, double dely, double nx, double ny)
+{
+    adj::End64 s;
+    adj::end64(nx, ny, delx, dely, in, in + 4, in + 8, in + 12, in + 16, e2, s);
+    return s;
+}
+}  // namespace
+
+// The same flux from the FP64 reverse's kept edge-end state (adj::end64).
+void qlskum_dbg_end64_flux(int f, int D, const double *in, double e2, double delx, double dely, double nx, double ny,
+                           double *G)
+{
+    const adj::End64 s = end64_of(in, e2, delx, dely, nx, ny);
+    switch (D) {
+    case 0: dir_flux<double, 0>(f, s.k, G); break;
+    case 1: dir_flux<double, 1>(f, s.k, G); break;
+    case 2: dir_flux<double, 2>(f, s.k, G); break;
+    default: dir_flux<double, 3>(f, s.k, G); break;
+    }
+}
+
+// Reverse of qlskum_dbg_end_flux by end64 / end64_vjp.  out: bars of the 20
+// inputs, then bdelx, bdely, bnx, bny
+void qlskum_dbg_end64_flux_vjp(int f, int D, const double *in, double e2, double delx, double dely, double nx,
+                               double ny, const double *bG, double *out)
+{
+    const adj::End64 s = end64_of(in, e2, delx, dely, nx, ny);
+    adj::KinBar kb;
+    switch (D) {
+    case 0: adj::dir_flux_vjp<0>(f, s.k, bG, kb); break;
+    case 1: adj::dir_flux_vjp<1>(f, s.k, bG, kb); break;
+    case 2: adj::dir_flux_vjp<2>(f, s.k, bG, kb); break;
+    default: adj::dir_flux_vjp<3>(f, s.k, bG, kb); break;
+    }
+    for (int r = 0; r < 24; r++) out[r] = 0;
+    adj::end64_vjp(s, nx, ny, delx, dely, in + 4, in + 8, kb, out, out + 4, out + 8, out + 12, out + 16, out[20],
+                   out[21], out[22], out[23]);
+}
+
 void qlskum_dbg_stage_update(int f, double nx, double ny, const double *Pin, const double *Pold, const double *F,
                              int rk, double mach, double aoa, double *Pout)
 {

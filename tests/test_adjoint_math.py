@@ -162,6 +162,47 @@ def test_edge_end_reconstruction(L):
         check(f, vj, x, 4, rng, h=1e-8)
 
 
+@pytest.mark.parametrize("f,D", [(1, 0), (1, 1), (1, 2), (1, 3), (0, 0), (0, 1), (0, 3), (2, 0), (2, 1), (2, 2)])
+def test_fp64_edge_end_reverse(L, f, D):
+    """The FP64 flux reverse's unit (adj::end64 + end64_vjp): limited
+    reconstruction, q~ -> prim and the half-range flux of one edge end,
+    w.r.t. q, dq, qm, the edge vector and the normal, against central
+    differences of the solver's own forward functions; its kept forward
+    state gives the solver's flux to rounding."""
+    sig = [C.c_int, C.c_int, dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]
+    L.qlskum_dbg_end_flux.argtypes = sig + [dp]
+    L.qlskum_dbg_end64_flux.argtypes = sig + [dp]
+    L.qlskum_dbg_end64_flux_vjp.argtypes = sig + [dp, dp]
+    for fn in ("qlskum_dbg_end_flux", "qlskum_dbg_end64_flux", "qlskum_dbg_end64_flux_vjp"):
+        getattr(L, fn).restype = None
+    rng = np.random.default_rng(50 + 10 * f + D)
+    e2 = 1e-7
+    n_lim = 0
+    for _ in range(8):
+        q = np.zeros(4)
+        L.qlskum_dbg_prim_to_q(P(state(rng)), P(q))
+        scale = np.abs(q) + 0.1
+        dq = rng.uniform(-2, 2, 8) * np.tile(scale, 2)
+        th = rng.uniform(0, 2 * np.pi)
+        x = np.concatenate([q, dq, q + rng.uniform(1e-4, 0.02, 4) * scale, q - rng.uniform(1e-4, 0.02, 4) * scale,
+                            rng.uniform(-0.01, 0.01, 2), [np.cos(th), np.sin(th)]])
+        g = x[20] * x[4:8] + x[21] * x[8:12]
+        n_lim += sum(L.qlskum_dbg_venkat(q[r] - 0.5 * g[r], q[r], x[12 + r], x[16 + r], e2) < 1.0 for r in range(4))
+
+        def fwd(z, fn=L.qlskum_dbg_end_flux):
+            o = np.zeros(4)
+            fn(f, D, P(z[:20]), e2, z[20], z[21], z[22], z[23], P(o))
+            return o
+
+        def vj(z, w):
+            o = np.zeros(24)
+            L.qlskum_dbg_end64_flux_vjp(f, D, P(z[:20]), e2, z[20], z[21], z[22], z[23], P(w), P(o))
+            return o
+        check(fwd, vj, x, 4, rng, h=1e-8, rtol=2e-6)
+        np.testing.assert_allclose(fwd(x, L.qlskum_dbg_end64_flux), fwd(x), rtol=1e-13, atol=1e-15)
+    assert n_lim >= 4   # the limiter's phi < 1 branch is exercised
+
+
 @pytest.mark.parametrize("flag", [0, 1, 2])
 @pytest.mark.parametrize("rk", [1, 3])
 def test_stage_update(L, flag, rk):
