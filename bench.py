@@ -357,6 +357,50 @@ def run_adjoint_check(args):
     print(json.dumps(line), flush=True)
 
 
+def run_long(args):
+    """The mixed and FP64 forms on the same cloud for --long-iters iterations
+    from the free stream (the 1.02 M-point transonic recipe runs 5000):
+    Cl, Cd, the residual norm and the total entropy of both every
+    --long-every iterations, the primitive state's difference at the end.
+    Stops at the first non-finite state of either form and says which."""
+    import qlskum
+    qlskum.load()
+    cloud = make_cloud(args.workload)
+    kw = WORKLOADS[args.workload]["solver"]
+    forms = {"mixed": qlskum.Solver(cloud, precision=qlskum.MIXED, **kw),
+             "fp64": qlskum.Solver(cloud, precision=qlskum.FP64, **kw)}
+    seconds = {k: 0.0 for k in forms}
+    rows, done, failed = [], 0, None
+    while done < args.long_iters and failed is None:
+        k = min(args.long_every, args.long_iters - done)
+        for name, s in forms.items():
+            t0 = time.perf_counter()
+            try:
+                s.q_lskum(k)
+                s.synchronize()
+            except qlskum.QlskumError as e:
+                failed = {"form": name, "before_iteration": done + k, "error": str(e)}
+                break
+            seconds[name] += time.perf_counter() - t0
+        if failed:
+            break
+        done += k
+        obj = {n: s.objective() for n, s in forms.items()}
+        res = {n: float(s.residual_history()[-1][0]) for n, s in forms.items()}
+        row = {"iteration": done, "cl": obj["fp64"][0], "cd": obj["fp64"][1], "res_fp64": res["fp64"],
+               "res_mixed": res["mixed"], "abs_dcl": abs(obj["mixed"][0] - obj["fp64"][0]),
+               "abs_dcd": abs(obj["mixed"][1] - obj["fp64"][1]),
+               "rel_dentropy": abs(obj["mixed"][3] - obj["fp64"][3]) / abs(obj["fp64"][3])}
+        rows.append(row)
+        log(json.dumps(row))
+    out = {"workload": WORKLOADS[args.workload].get("name", args.workload), "points": cloud.n,
+           "iterations": done, "failed": failed, "seconds": seconds, "history": rows}
+    if failed is None:
+        pm, pd = forms["mixed"].prim, forms["fp64"].prim
+        out["prim_rel_err"] = float((np.abs(pm - pd) / np.abs(pd).max(axis=0)).max())
+    print(json.dumps(out), flush=True)
+
+
 def run_batch(args):
     """Batched launch: 64 flight conditions over 32 uneven clouds, mixed precision."""
     import torch
@@ -511,6 +555,10 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--adjoint-iters", type=int, default=3,
                     help="iterations differentiated by the adjoint timings (FP64 and mixed handles; 0: skip)")
+    ap.add_argument("--long-iters", type=int, default=0,
+                    help="instead of the benchmark: the mixed and FP64 forms side by side for this many "
+                         "iterations (Cl, Cd, residual, entropy every --long-every)")
+    ap.add_argument("--long-every", type=int, default=500)
     ap.add_argument("--launch", default="auto",
                     help="mixed launch shape 'flux_variant,point_block,staged' (e.g. 6,64,0) instead of autotuning")
     args = ap.parse_args()
@@ -526,6 +574,10 @@ def main():
     if args.workload == "adjoint":
         if rank == 0:
             run_adjoint_check(args)
+        return
+    if args.long_iters:
+        if rank == 0:
+            run_long(args)
         return
 
     import torch

@@ -31,9 +31,17 @@ Layout of a generated cloud
   spacing, "nearest" being measured in the local (tangential, normal) spacing
   units so that anisotropic near-wall rings still give every directional
   sub-stencil points on both sides.  Points whose sub-stencils (split the way
-  generate_connectivity_mod.h:5-219 splits them) are empty or nearly
-  collinear get further candidates, up to 20 neighbours.  This is the job of
-  the empty `check_condition_number` stub at generate_connectivity_mod.h:84-89.
+  generate_connectivity_mod.h:5-219 splits them) are empty, nearly
+  collinear, or whose least-squares derivative weights are too large or
+  not upwind (`_sub_stats`: weight sum times the nearest-neighbour distance
+  above `max_weight`, downwind-signed weight above `max_wrong`) get further
+  candidates, up to 20 neighbours.  This is the job of the empty
+  `check_condition_number` stub at generate_connectivity_mod.h:84-89.  The
+  weight bounds matter on the O-grid's wake line behind the trailing edge,
+  where the rings are sheared: without them some stencils there are
+  one-sided, and the unlimited update (small perturbations pass the
+  limiter's 1e-5 cut) grows at those points by a fixed factor per
+  iteration, in FP64 as in the mixed form.
 """
 from __future__ import annotations
 
@@ -241,28 +249,78 @@ def _classify_masks(dels: np.ndarray, deln: np.ndarray, flag: np.ndarray):
     return xpos, xneg, ypos, yneg
 
 
-def _stencil_ok(dels, deln, valid, flag, min_count=2, min_rcond=1e-3):
+def _sub_stats(dels, deln, w, along_s, dmin, sign=0.0):
+    """Per row, for the sub-stencil mask w: member count, reciprocal condition
+    number of its 2x2 least-squares matrix, its weight bound and its
+    wrong-sign weight.
+
+    The weights are those of the least-squares derivative (along s for the x
+    sub-stencils, along n for the y ones), in units of one over the row's
+    nearest-neighbour distance.  The explicit update moves a point by about
+    delta times their sum times the wave speed, and delta is CFL times the
+    nearest-neighbour distance over the wave speed (func_delta), so the
+    bound (the sum of their magnitudes) is the point's effective CFL number
+    per unit CFL.  A half-range stencil (sign -1: members with d <= 0, +1:
+    d >= 0) is upwind when every weight has that sign; the wrong-sign weight
+    is the sum of the magnitudes of those that do not.  Skewed, one-sided
+    stencils (on a generated cloud: the O-grid's wake line behind the
+    trailing edge) reach a bound of 10 and a wrong-sign weight of several
+    units where a well-shaped stencil has about 1 and 0.01; the unlimited
+    update (the limiter's |dq| <= 1e-5 cut) then grows there by a fixed
+    factor per iteration, in FP64 as in the mixed form."""
+    cnt = w.sum(1)
+    sxx = np.where(w, dels * dels, 0.0).sum(1)
+    syy = np.where(w, deln * deln, 0.0).sum(1)
+    sxy = np.where(w, dels * deln, 0.0).sum(1)
+    tr = sxx + syy
+    det = sxx * syy - sxy * sxy
+    disc = np.sqrt(np.maximum(tr * tr * 0.25 - det, 0.0))
+    lmax = tr * 0.5 + disc
+    lmin = tr * 0.5 - disc
+    rc = np.where(lmax > 0, lmin / np.where(lmax > 0, lmax, 1.0), 0.0)
+    pos = det > 0
+    inv = np.where(pos, 1.0 / np.where(pos, det, 1.0), 0.0)
+    if along_s:
+        cw = (syy[:, None] * dels - sxy[:, None] * deln) * inv[:, None]
+    else:
+        cw = (sxx[:, None] * deln - sxy[:, None] * dels) * inv[:, None]
+    bound = np.where(pos, np.where(w, np.abs(cw), 0.0).sum(1) * dmin, np.inf)
+    wrong = np.where(pos, np.where(w, np.maximum(-sign * cw, 0.0), 0.0).sum(1) * dmin, np.inf)
+    return cnt, rc, bound, wrong
+
+
+def _nearest(dels, deln, valid):
+    return np.where(valid, np.sqrt(dels * dels + deln * deln), np.inf).min(1)
+
+
+# sign of the half-range of the sub-stencils xpos, xneg, ypos, yneg of an
+# interior point (members with dels <= 0, dels >= 0, deln <= 0, deln >= 0)
+_HALF_SIGN = (-1.0, 1.0, -1.0, 1.0)
+
+
+def _half_sign(d, flag):
+    """Per row: the half-range sign of sub-stencil d, 0 where the class takes
+    the whole stencil (the wall's yneg, the outer boundary's ypos)."""
+    if d < 2:
+        return np.full(flag.shape, _HALF_SIGN[d])
+    return np.where(flag == 1, _HALF_SIGN[d], 0.0)
+
+
+def _stencil_ok(dels, deln, valid, flag, min_count=2, min_rcond=1e-3, max_weight=np.inf, max_wrong=np.inf):
     """Per point: every sub-stencil the point's class uses is well posed.
 
-    A sub-stencil passes when it has >= min_count members and the reciprocal
-    condition number of its 2x2 least-squares matrix is >= min_rcond.
+    A sub-stencil passes when it has >= min_count members, the reciprocal
+    condition number of its 2x2 least-squares matrix is >= min_rcond, its
+    weight bound is <= max_weight and its wrong-sign weight <= max_wrong
+    (`_sub_stats`).
     """
     masks = _classify_masks(dels, deln, flag)
     need = [np.ones_like(flag, bool), np.ones_like(flag, bool), flag != 0, flag != 2]
+    dmin = _nearest(dels, deln, valid)
     ok = np.ones(flag.shape[0], bool)
-    for mk, nd in zip(masks, need):
-        w = mk & valid
-        cnt = w.sum(1)
-        sxx = np.where(w, dels * dels, 0.0).sum(1)
-        syy = np.where(w, deln * deln, 0.0).sum(1)
-        sxy = np.where(w, dels * deln, 0.0).sum(1)
-        tr = sxx + syy
-        det = sxx * syy - sxy * sxy
-        disc = np.sqrt(np.maximum(tr * tr * 0.25 - det, 0.0))
-        lmax = tr * 0.5 + disc
-        lmin = tr * 0.5 - disc
-        rc = np.where(lmax > 0, lmin / np.where(lmax > 0, lmax, 1.0), 0.0)
-        good = (cnt >= min_count) & (rc >= min_rcond)
+    for d, (mk, nd) in enumerate(zip(masks, need)):
+        cnt, rc, bound, wrong = _sub_stats(dels, deln, mk & valid, d < 2, dmin, _half_sign(d, flag)[:, None])
+        good = (cnt >= min_count) & (rc >= min_rcond) & (bound <= max_weight) & (wrong <= max_wrong)
         ok &= np.where(nd, good, True)
     return ok
 
@@ -322,7 +380,7 @@ def _visible(x, y, nx, ny, flag, rows, idx, dx, dy, dist, wall, cache=None):
 
 
 def build_connectivity(x, y, nx, ny, flag, ht, hn, tx_, ty_, n_nbrs=10, nbr_radius=2.5,
-                       n_cand=32, min_rcond=1e-3, wall=None, chunk=1 << 20):
+                       n_cand=32, min_rcond=1e-3, wall=None, chunk=1 << 20, max_weight=np.inf, max_wrong=np.inf):
     """conn [N, 20] (0-based, -1 padded) and counts.
 
     Candidates come from a k-d tree; they are ranked by distance in the local
@@ -370,7 +428,8 @@ def build_connectivity(x, y, nx, ny, flag, ht, hn, tx_, ty_, n_nbrs=10, nbr_radi
         kk = np.arange(idx.shape[1])[None, :]
         valid = (kk < take[:, None]) & finite
         fl = flag[rows]
-        ok = _stencil_ok(dels_all, deln_all, valid, fl, min_rcond=min_rcond)
+        ok = _stencil_ok(dels_all, deln_all, valid, fl, min_rcond=min_rcond, max_weight=max_weight,
+                         max_wrong=max_wrong)
         bad = np.nonzero(~ok)[0]
         # grow failing stencils one candidate at a time, up to MAX_NBHS
         for extra in range(MAX_NBHS - n_nbrs):
@@ -378,7 +437,8 @@ def build_connectivity(x, y, nx, ny, flag, ht, hn, tx_, ty_, n_nbrs=10, nbr_radi
                 break
             take[bad] = np.minimum(take[bad] + 1, np.minimum(MAX_NBHS, finite[bad].sum(1)))
             vb = (kk < take[bad][:, None]) & finite[bad]
-            okb = _stencil_ok(dels_all[bad], deln_all[bad], vb, fl[bad], min_rcond=min_rcond)
+            okb = _stencil_ok(dels_all[bad], deln_all[bad], vb, fl[bad], min_rcond=min_rcond,
+                              max_weight=max_weight, max_wrong=max_wrong)
             bad = bad[~okb]
         valid = (kk < take[:, None]) & finite
         conn[rows] = np.where(valid, idx, -1)[:, :MAX_NBHS]
@@ -386,7 +446,8 @@ def build_connectivity(x, y, nx, ny, flag, ht, hn, tx_, ty_, n_nbrs=10, nbr_radi
         bad_all.append(rows[bad])
     bad = np.concatenate(bad_all) if bad_all else np.zeros(0, np.int64)
     if bad.size:
-        conn, cnt, bad = _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, wall, vis_cache)
+        conn, cnt, bad = _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, wall, vis_cache,
+                                 max_weight, max_wrong)
     return conn, cnt, bad
 
 
@@ -402,13 +463,30 @@ def _rcond(dels, deln):
     return (tr * 0.5 - disc) / lmax if lmax > 0 else 0.0
 
 
-def _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, wall=None, vis_cache=None):
+def _score(rc, bound, wrong, min_rcond, max_weight, max_wrong):
+    return np.maximum(np.maximum(np.where(rc > 0, min_rcond / np.where(rc > 0, rc, 1.0), np.inf), bound / max_weight),
+                      wrong / max_wrong)
+
+
+def _badness(dels, deln, along_s, dmin, sign, min_rcond, max_weight, max_wrong):
+    """> 1 when one sub-stencil fails: fewer than 2 members, reciprocal
+    condition number below min_rcond, weight bound above max_weight or
+    wrong-sign weight above max_wrong."""
+    if dels.size < 2:
+        return np.inf
+    _, rc, bound, wrong = _sub_stats(dels[None, :], deln[None, :], np.ones((1, dels.size), bool), along_s,
+                                     np.array([dmin]), sign)
+    return float(_score(rc, bound, wrong, min_rcond, max_weight, max_wrong)[0])
+
+
+def _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, wall=None, vis_cache=None,
+            max_weight=np.inf, max_wrong=np.inf):
     """Fix the few stencils the ranked selection leaves ill-posed.
 
     For each such point: restart from its n_nbrs nearest (Euclidean) points
-    and, while some sub-stencil its class uses is ill-posed, add the point in
-    that sub-stencil's half-plane (among the 256 nearest) that raises the
-    sub-stencil's reciprocal condition number the most.
+    and, while some sub-stencil its class uses fails (`_badness`), add the
+    point in that sub-stencil's half-plane (among the 256 nearest) that leaves
+    the sub-stencil the least bad.
     """
     still = []
     for i in bad:
@@ -420,6 +498,7 @@ def _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, w
             vis = _visible(x, y, nx, ny, flag, i, cand[None, :], dx[None, :], dy[None, :],
                            np.sqrt(dx * dx + dy * dy)[None, :], wall, vis_cache)[0]
             cand, dx, dy = cand[vis], dx[vis], dy[vis]
+        dist = np.sqrt(dx * dx + dy * dy)
         dels = dx * ny[i] - dy * nx[i]
         deln = dx * nx[i] + dy * ny[i]
         allm = np.ones(len(cand), bool)
@@ -428,31 +507,34 @@ def _repair(conn, cnt, bad, x, y, nx, ny, flag, hmax, tree, n_nbrs, min_rcond, w
                 (deln >= 0.0) if flag[i] == 1 else (allm if flag[i] == 0 else None)]
         sel = np.zeros(len(cand), bool)
         sel[:n_nbrs] = True
+
+        sgn = [(_HALF_SIGN[d] if (d < 2 or flag[i] == 1) else 0.0) for d in range(4)]
+
+        def failing(d, dmin, strict=True):
+            w = sel & want[d]
+            return _badness(dels[w], deln[w], d < 2, dmin, sgn[d], min_rcond, max_weight if strict else np.inf,
+                            max_wrong if strict else np.inf) > 1.0
+
         while sel.sum() < MAX_NBHS:
-            worst = None
-            for d in range(4):
-                if want[d] is None:
-                    continue
-                w = sel & want[d]
-                if w.sum() < 2 or _rcond(dels[w], deln[w]) < min_rcond:
-                    worst = d
-                    break
+            dmin = dist[sel].min()
+            worst = next((d for d in range(4) if want[d] is not None and failing(d, dmin)), None)
             if worst is None:
                 break
-            best, best_rc = None, -1.0
-            for c in np.nonzero(want[worst] & ~sel)[0]:
-                w = sel & want[worst]
-                w[c] = True
-                rc = _rcond(dels[w], deln[w]) if w.sum() >= 2 else 0.0
-                if rc > best_rc + 1e-12:
-                    best, best_rc = c, rc
-            if best is None:
+            cands = np.nonzero(want[worst] & ~sel)[0]
+            if cands.size == 0:
                 break
-            sel[best] = True
+            m = np.nonzero(sel & want[worst])[0]
+            ds = np.concatenate([np.broadcast_to(dels[m], (cands.size, m.size)), dels[cands][:, None]], 1)
+            dn = np.concatenate([np.broadcast_to(deln[m], (cands.size, m.size)), deln[cands][:, None]], 1)
+            cnt_c, rc_c, bound_c, wrong_c = _sub_stats(ds, dn, np.ones(ds.shape, bool), worst < 2,
+                                                       np.minimum(dmin, dist[cands]), sgn[worst])
+            score = np.where(cnt_c >= 2, _score(rc_c, bound_c, wrong_c, min_rcond, max_weight, max_wrong), np.inf)
+            sel[cands[int(np.argmin(score))]] = True
         chosen = np.nonzero(sel)[0]
-        ok = all(want[d] is None or ((sel & want[d]).sum() >= 2 and _rcond(dels[sel & want[d]], deln[sel & want[d]]) >= min_rcond)
-                 for d in range(4))
-        if not ok:
+        # degenerate stencils are errors; a weight bound that 20 neighbours
+        # cannot meet is left at the best stencil found
+        dmin = dist[sel].min()
+        if any(want[d] is not None and failing(d, dmin, strict=False) for d in range(4)):
             still.append(i)
         conn[i, :] = -1
         conn[i, :len(chosen)] = cand[chosen]
@@ -464,7 +546,8 @@ def make_cloud(n_wall: int = 160, n_layers: int = 60, first_spacing: float = 2e-
                radius: float = 20.0, seed: int = 0, jitter: float = 0.1,
                n_nbrs: int = 10, nbr_radius: float = 2.5,
                m: float = 0.0, p: float = 0.4, t: float = 0.12,
-               min_rcond: float = 1e-3, smooth: int = 30) -> Cloud:
+               min_rcond: float = 1e-3, smooth: int = 30, max_weight: float = 2.5,
+               max_wrong: float = 0.3) -> Cloud:
     """Generate a seeded NACA 4-digit O-type point cloud (see module docstring).
 
     Point order: wall ring (flag_1 0, flag_2 1), interior rings (flag_1 1),
@@ -528,7 +611,8 @@ def make_cloud(n_wall: int = 160, n_layers: int = 60, first_spacing: float = 2e-
 
     conn0, cnt, bad = build_connectivity(
         x, y, nx, ny, flag, ht.reshape(-1), hn.reshape(-1), tx.reshape(-1), ty.reshape(-1),
-        n_nbrs=n_nbrs, nbr_radius=nbr_radius, min_rcond=min_rcond, wall=[np.arange(W)])
+        n_nbrs=n_nbrs, nbr_radius=nbr_radius, min_rcond=min_rcond, wall=[np.arange(W)], max_weight=max_weight,
+        max_wrong=max_wrong)
     if bad.size:
         raise RuntimeError(f"{bad.size} points have degenerate sub-stencils even with {MAX_NBHS} neighbours")
     conn = np.zeros((n, MAX_NBHS), np.int32)
@@ -619,7 +703,8 @@ def two_element_cloud(n_main: int = 4096, n_flap: int = 1024, flap_chord: float 
                       gap: float = 0.015, overlap: float = 0.01, n_layers: int = 12, first_spacing: float = 1e-4,
                       h0: float = 1.5e-4, growth: float = 0.0033, radius: float = 20.0, seed: int = 5,
                       jitter: float = 0.1, n_nbrs: int = 10, nbr_radius: float = 2.5,
-                      min_rcond: float = 1e-3, smooth: int = 30) -> Cloud:
+                      min_rcond: float = 1e-3, smooth: int = 30, max_weight: float = 2.5,
+               max_wrong: float = 0.3) -> Cloud:
     """Seeded two-element cloud: NACA 0012 main element (chord 1, leading edge
     at the origin) and a NACA 0012 flap of chord `flap_chord` turned by
     `deflect` degrees whose leading edge sits `overlap` ahead of the main
@@ -767,7 +852,8 @@ def two_element_cloud(n_main: int = 4096, n_flap: int = 1024, flap_chord: float 
         ny[sl] = nyy / d
     conn0, cnt, bad = build_connectivity(x, y, nx, ny, flag, ht, hn, tx_, ty_, n_nbrs=n_nbrs,
                                          nbr_radius=nbr_radius, min_rcond=min_rcond,
-                                         wall=[np.arange(Wm), Wm + np.arange(Wf)])
+                                         wall=[np.arange(Wm), Wm + np.arange(Wf)], max_weight=max_weight,
+                                         max_wrong=max_wrong)
     if bad.size:
         raise RuntimeError(f"{bad.size} points have degenerate sub-stencils even with {MAX_NBHS} neighbours")
     conn = np.zeros((n, MAX_NBHS), np.int32)

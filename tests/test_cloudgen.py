@@ -72,6 +72,48 @@ def test_seeded_and_deterministic():
     assert not np.array_equal(a.x, c.x)
 
 
+def _weight_bounds(cloudgen, oracle_mod, c):
+    """Per sub-stencil d: (count, rcond, weight bound, wrong-sign weight, used)
+    of every point, split as the reference splits it (the oracle's normals)."""
+    o = oracle_mod.Oracle(c, threads=2)
+    nrm = o.normals
+    valid = np.arange(20)[None, :] < c.nbhs[:, None]
+    idx = np.where(valid, c.conn - 1, 0)
+    dx = np.where(valid, c.x[idx] - c.x[:, None], 0.0)
+    dy = np.where(valid, c.y[idx] - c.y[:, None], 0.0)
+    nx, ny = nrm[:, :1], nrm[:, 1:]
+    dels, deln = dx * ny - dy * nx, dx * nx + dy * ny
+    dmin = cloudgen._nearest(dels, deln, valid)
+    masks = cloudgen._classify_masks(dels, deln, c.flag_1)
+    used = [np.ones(c.n, bool), np.ones(c.n, bool), c.flag_1 != 0, c.flag_1 != 2]
+    return [cloudgen._sub_stats(dels, deln, masks[d] & valid, d < 2, dmin, cloudgen._half_sign(d, c.flag_1)[:, None])
+            + (used[d],) for d in range(4)]
+
+
+def test_substencils_upwind_and_bounded(oracle_mod):
+    """Every sub-stencil of a generated cloud, split as the reference splits it,
+    meets the generator's bounds on its least-squares derivative weights:
+    their magnitude sum times the nearest-neighbour distance <= 2.5 and the
+    weight of the wrong (downwind) sign <= 0.3 (points at the 20-neighbour
+    cap, where the repair stops, excepted).  The same cloud without the
+    bounds has wake-line stencils outside them: on the 1.02 M-point cloud
+    those reached 18 and 9, and the unlimited update grew there by 1.4x per
+    iteration."""
+    from qlskum import cloudgen
+    kw = dict(n_wall=256, n_layers=120, first_spacing=2e-3, radius=20.0, seed=3)
+    c = small_cloud(**kw)
+    capped = c.nbhs >= 20
+    assert capped.sum() < 0.01 * c.n
+    for cnt, rc, bound, wrong, used in _weight_bounds(cloudgen, oracle_mod, c):
+        chk = used & ~capped
+        assert (cnt[chk] >= 2).all() and (rc[chk] >= 1e-3).all()
+        assert bound[chk].max() <= 2.5 + 1e-9, bound[chk].max()
+        assert wrong[chk].max() <= 0.3 + 1e-9, wrong[chk].max()
+    u = cloudgen.make_cloud(**kw, max_weight=np.inf, max_wrong=np.inf)
+    worst = max(float(np.max(np.where(used, wrong, 0.0))) for _, _, _, wrong, used in _weight_bounds(cloudgen, oracle_mod, u))
+    assert worst > 0.3, worst
+
+
 def test_substencils_well_posed(oracle_mod):
     """Every sub-stencil a point's class uses has >= 2 members (the generator's
     check_condition_number job, generate_connectivity_mod.h:84-89)."""
