@@ -42,7 +42,10 @@ for _p in (os.path.join(REPO, "c-_serial_gb300"), os.path.join(REPO, "oracle")):
 import numpy as np  # noqa: E402
 
 WORKLOADS = {
-    "transonic": dict(cloud=dict(n_wall=1024, n_layers=1000, first_spacing=2e-3, radius=20.0, seed=2),
+    # te_spread: the cosine law's trailing-edge wall spacing of the 160-point
+    # ring (3.9e-4 chord) instead of 1e-5 (cloudgen.naca4_surface)
+    "transonic": dict(cloud=dict(n_wall=1024, n_layers=1000, first_spacing=2e-3, radius=20.0, seed=2,
+                                 te_spread=0.064),
                       solver=dict(mach=0.85, aoa=1.0, cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=3)),
     "subsonic": dict(cloud=dict(n_wall=160, n_layers=60, first_spacing=2e-3, radius=20.0, seed=1),
                      solver=dict(mach=0.63, aoa=2.0, cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=0)),

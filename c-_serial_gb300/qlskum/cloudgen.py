@@ -139,15 +139,22 @@ def read_partgrid(path: str) -> Cloud:
 # Geometry
 # ---------------------------------------------------------------------------
 
-def naca4_surface(theta: np.ndarray, m: float = 0.0, p: float = 0.4, t: float = 0.12):
+def naca4_surface(theta: np.ndarray, m: float = 0.0, p: float = 0.4, t: float = 0.12, te_spread: float = 0.0):
     """NACA 4-digit surface at parameter theta in [0, 2 pi).
 
     x_c = (1 + cos theta)/2; theta in [0, pi] is the upper surface (trailing
     edge to leading edge), (pi, 2 pi) the lower one.  Closed trailing edge
     (-0.1036 x^4 coefficient).  m = max camber, p = its chord position,
     t = thickness, all as fractions of the chord.
+
+    te_spread = w > 0 moves x_c away from the trailing edge by
+    w |sin theta| (1 + cos theta) / 2: the cosine law's spacing at the
+    trailing edge, which shrinks as 1 / n^2 with the number of wall points,
+    becomes w times the parameter step there, while the leading edge keeps
+    the cosine law (the added term vanishes to third order at theta = pi);
+    the map stays monotone for w < 0.8.
     """
-    xc = 0.5 * (1.0 + np.cos(theta))
+    xc = 0.5 * (1.0 + np.cos(theta)) - te_spread * np.abs(np.sin(theta)) * 0.5 * (1.0 + np.cos(theta))
     yt = 5.0 * t * (0.2969 * np.sqrt(xc) - 0.1260 * xc - 0.3516 * xc**2 + 0.2843 * xc**3 - 0.1036 * xc**4)
     if m > 0.0:
         fore = xc < p
@@ -195,10 +202,10 @@ def solve_growth(first: float, steps: int, total: float) -> float:
 
 def make_layers(n_wall: int, n_layers: int, first_spacing: float, radius: float,
                 m: float = 0.0, p: float = 0.4, t: float = 0.12,
-                center=(0.5, 0.0), blend_len: float = 1.0, smooth: int = 0):
+                center=(0.5, 0.0), blend_len: float = 1.0, smooth: int = 0, te_spread: float = 0.0):
     """Ring points [n_layers, n_wall] (x, y) and the ring offsets d_j."""
     theta = 2.0 * np.pi * np.arange(n_wall) / n_wall
-    wx, wy = naca4_surface(theta, m, p, t)
+    wx, wy = naca4_surface(theta, m, p, t, te_spread)
     nx, ny = _rot_normals(wx, wy)
     # Spread the ray fan at the sharp trailing edge: smooth the ray directions
     # along the ring so that the wake behind the edge is not left empty.
@@ -547,14 +554,14 @@ def make_cloud(n_wall: int = 160, n_layers: int = 60, first_spacing: float = 2e-
                n_nbrs: int = 10, nbr_radius: float = 2.5,
                m: float = 0.0, p: float = 0.4, t: float = 0.12,
                min_rcond: float = 1e-3, smooth: int = 30, max_weight: float = 2.5,
-               max_wrong: float = 0.3) -> Cloud:
+               max_wrong: float = 0.3, te_spread: float = 0.0) -> Cloud:
     """Generate a seeded NACA 4-digit O-type point cloud (see module docstring).
 
     Point order: wall ring (flag_1 0, flag_2 1), interior rings (flag_1 1),
     far-field ring (flag_1 2); inside a ring, counter-clockwise from the
     trailing edge.
     """
-    X, Y, _ = make_layers(n_wall, n_layers, first_spacing, radius, m, p, t, smooth=smooth)
+    X, Y, _ = make_layers(n_wall, n_layers, first_spacing, radius, m, p, t, smooth=smooth, te_spread=te_spread)
     L, W = X.shape
     # local spacing: half the central difference along / across rings
     Xp, Xm = np.roll(X, -1, 1), np.roll(X, 1, 1)
@@ -630,8 +637,9 @@ def config1_cloud(seed: int = 1) -> Cloud:
 
 
 def config2_cloud(seed: int = 2) -> Cloud:
-    """NACA 0012, 1024 wall points x 1000 rings = 1,024,000 points."""
-    return make_cloud(n_wall=1024, n_layers=1000, first_spacing=2e-3, radius=20.0, seed=seed)
+    """NACA 0012, 1024 wall points x 1000 rings = 1,024,000 points, the
+    trailing-edge wall spacing spread to the 160-point ring's (te_spread)."""
+    return make_cloud(n_wall=1024, n_layers=1000, first_spacing=2e-3, radius=20.0, seed=seed, te_spread=0.064)
 
 
 # ---------------------------------------------------------------------------

@@ -173,7 +173,7 @@ def test_mixed_vs_fp64_full_size_transonic(qlskum):
     largest magnitude per component; the residual norm (res_new) of every
     iteration within 1e-3 relative."""
     from qlskum import cloudgen
-    c = cloudgen.make_cloud(n_wall=1024, n_layers=1000, first_spacing=2e-3, radius=20.0, seed=2)
+    c = cloudgen.config2_cloud()
     kw = dict(mach=0.85, aoa=1.0, cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=3)
     m = qlskum.Solver(c, precision=qlskum.MIXED, **kw)
     d = qlskum.Solver(c, precision=qlskum.FP64, **kw)
