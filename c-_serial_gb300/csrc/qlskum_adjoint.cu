@@ -157,41 +157,46 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
     double bFi[4];
     ld4(bF[i], bFi);
     const double dl = delta[i];
-    // bars of the directional sums
-    double bsx[4][4], bsy[4][4];
+    // bars of the directional sums: the solve is linear in them, so the bar
+    // of sum x (y) of half-range d, component r, is bG[r] ax[d] (bG[r] ay[d])
+    // with bG = scale delta F-bar
+    double bG4[4], ax[4], ay[4];
+    for (int r = 0; r < 4; r++) bG4[r] = scale * dl * bFi[r];
     double bdl = 0.0;
     for (int d = 0; d < 4; d++) {
         const double4_32a m = c.fgeo[4 * i + d];
+        ax[d] = ay[d] = 0.0;
+        if (!used[d]) continue;
+        if (d < 2) {
+            ax[d] = m.y * m.w;
+            ay[d] = -m.z * m.w;
+        } else {
+            ax[d] = -m.z * m.w;
+            ay[d] = m.x * m.w;
+        }
+        if (!GEO) continue;
         double bm[4] = {0, 0, 0, 0};
         for (int r = 0; r < 4; r++) {
-            bsx[d][r] = bsy[d][r] = 0.0;
-            if (!used[d]) continue;
-            const double bG = scale * dl * bFi[r];
+            const double bG = bG4[r];
             if (d < 2) {
                 const double G = (sx[d][r] * m.y - sy[d][r] * m.z) * m.w;
-                if (GEO) bdl += scale * bFi[r] * G;
-                bsx[d][r] = bG * m.y * m.w;
-                bsy[d][r] = -bG * m.z * m.w;
+                bdl += scale * bFi[r] * G;
                 bm[1] += bG * sx[d][r] * m.w;
                 bm[2] -= bG * sy[d][r] * m.w;
                 bm[3] += bG * (sx[d][r] * m.y - sy[d][r] * m.z);
             } else {
                 const double G = (sy[d][r] * m.x - sx[d][r] * m.z) * m.w;
-                if (GEO) bdl += scale * bFi[r] * G;
-                bsy[d][r] = bG * m.x * m.w;
-                bsx[d][r] = -bG * m.z * m.w;
+                bdl += scale * bFi[r] * G;
                 bm[0] += bG * sy[d][r] * m.w;
                 bm[2] -= bG * sx[d][r] * m.w;
                 bm[3] += bG * (sy[d][r] * m.x - sx[d][r] * m.z);
             }
         }
-        if (GEO) {
-            double4_32a &acc = a.bfmom[4 * i + d];
-            acc.x += bm[0];
-            acc.y += bm[1];
-            acc.z += bm[2];
-            acc.w += bm[3];
-        }
+        double4_32a &acc = a.bfmom[4 * i + d];
+        acc.x += bm[0];
+        acc.y += bm[1];
+        acc.z += bm[2];
+        acc.w += bm[3];
     }
     if (!GEO) {
         double F[4];
@@ -212,19 +217,19 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
         const double2 sw = c.e_sn[e];
         const unsigned dir = c.e_dir[e];
         double bdelx = 0.0, bdely = 0.0, bsw_x = 0.0, bsw_y = 0.0;
-        // the bar of G_k on half-range D is bsx sw.x + bsy sw.y, that of G_i its negative
+        // the bar of G_k on half-range D is bG (ax sw.x + ay sw.y), that of G_i its negative
 #define QLSKUM_REV(D, SGN, KIN, KB)                                                  \
         if (dir & (1u << D)) {                                                       \
+            const double fw = SGN * (ax[D] * sw.x + ay[D] * sw.y);                   \
             double bG[4];                                                            \
-            for (int r = 0; r < 4; r++) bG[r] = SGN * (bsx[D][r] * sw.x + bsy[D][r] * sw.y); \
+            for (int r = 0; r < 4; r++) bG[r] = fw * bG4[r];                         \
             adj::dir_flux_vjp<D>(f, KIN, bG, KB);                                    \
             if (GEO) {                                                               \
                 double G[4];                                                         \
                 dir_flux<double, D>(f, KIN, G);                                      \
-                for (int r = 0; r < 4; r++) {                                        \
-                    bsw_x += SGN * bsx[D][r] * G[r];                                 \
-                    bsw_y += SGN * bsy[D][r] * G[r];                                 \
-                }                                                                    \
+                const double gb = bG4[0] * G[0] + bG4[1] * G[1] + bG4[2] * G[2] + bG4[3] * G[3]; \
+                bsw_x += SGN * ax[D] * gb;                                           \
+                bsw_y += SGN * ay[D] * gb;                                           \
             }                                                                        \
         }
         {
