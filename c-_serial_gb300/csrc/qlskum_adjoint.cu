@@ -85,7 +85,8 @@ template <bool GEO>
 __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__restrict__ q,
                                                const double4_32a *__restrict__ dq, const double4_32a *__restrict__ qm,
                                                const double *__restrict__ delta, const double4_32a *__restrict__ flux,
-                                               const double *__restrict__ sums, const double4_32a *__restrict__ bF,
+                                               const double *__restrict__ sums, const double *__restrict__ ends,
+                                               long long ns, const double4_32a *__restrict__ bF,
                                                double4_32a *__restrict__ bq, double4_32a *__restrict__ bdq,
                                                double4_32a *__restrict__ bqm, double *__restrict__ bdelta)
 {
@@ -240,7 +241,10 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
             ld4(qm[2 * k], mxk);
             ld4(qm[2 * k + 1], mnk);
             adj::End64 s;
-            adj::end64(nx, ny, g.x, g.y, qk, dxk, dyk, mxk, mnk, c.eps2[k], s);
+            double kept[6];
+            if (ends)
+                for (int w = 0; w < 6; w++) kept[w] = ends[(6 + w) * ns + e];
+            adj::end64(nx, ny, g.x, g.y, qk, dxk, dyk, mxk, mnk, c.eps2[k], s, ends ? kept : nullptr);
             KinBar kb;
             QLSKUM_REV(0, 1.0, s.k, kb)
             QLSKUM_REV(1, 1.0, s.k, kb)
@@ -257,7 +261,10 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
         }
         {
             adj::End64 s;
-            adj::end64(nx, ny, g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, s);
+            double kept[6];
+            if (ends)
+                for (int w = 0; w < 6; w++) kept[w] = ends[w * ns + e];
+            adj::end64(nx, ny, g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, s, ends ? kept : nullptr);
             KinBar kb;
             QLSKUM_REV(0, -1.0, s.k, kb)
             QLSKUM_REV(1, -1.0, s.k, kb)
@@ -1084,15 +1091,15 @@ void update(const Launch &L, const AdjView &a, const CaseConst &K, const double4
 }
 
 void flux(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
-          const double *delta, const double4_32a *flux, const double *sums, const double4_32a *bF, double4_32a *bq,
-          double4_32a *bdq, double4_32a *bqm, double *bdelta)
+          const double *delta, const double4_32a *flux, const double *sums, const double *ends, long long ns,
+          const double4_32a *bF, double4_32a *bq, double4_32a *bdq, double4_32a *bqm, double *bdelta)
 {
     if (a.bedge)
-        adjk::k_flux<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, sums, bF, bq,
-                                                                             bdq, bqm, bdelta);
+        adjk::k_flux<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, sums, ends, ns,
+                                                                             bF, bq, bdq, bqm, bdelta);
     else
-        adjk::k_flux<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, nullptr, bF,
-                                                                              bq, bdq, bqm, bdelta);
+        adjk::k_flux<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, nullptr, ends,
+                                                                              ns, bF, bq, bdq, bqm, bdelta);
 }
 
 void inner(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq_in,

@@ -230,8 +230,13 @@ struct End64 {
     Kin<double> k;
 };
 
+// kept (or NULL): the forward flux kernel's {rho, sqrt(beta), exp(-S1^2),
+// exp(-S2^2), erf(S1), erf(S2)} of this end (fp64::flux_residual's ends),
+// taken instead of recomputing the log, the exps, the square root and the
+// erfs.
 QLSKUM_HD void end64(double nx, double ny, double delx, double dely, const double q[4], const double dx[4],
-                     const double dy[4], const double mx[4], const double mn[4], double e2, End64 &s)
+                     const double dy[4], const double mx[4], const double mn[4], double e2, End64 &s,
+                     const double *kept = nullptr)
 {
     constexpr double inv_gm1 = 1.0 / (1.4 - 1.0);
     double qt[4];
@@ -259,20 +264,29 @@ QLSKUM_HD void end64(double nx, double ny, double delx, double dely, const doubl
     s.tm = 0.5 / s.beta;
     s.u1 = qt[1] * s.tm;
     s.u2 = qt[2] * s.tm;
-    s.rho = M<double>::ex(qt[0] + s.beta * (s.u1 * s.u1 + s.u2 * s.u2) - M<double>::lg(s.beta) * inv_gm1);
-    s.k.rho = s.rho;
     s.k.ut = s.u1 * ny - s.u2 * nx;
     s.k.un = s.u1 * nx + s.u2 * ny;
-    s.sb = M<double>::sq(s.beta);
+    if (kept) {
+        s.rho = kept[0];
+        s.sb = kept[1];
+        s.e1 = kept[2];
+        s.e2 = kept[3];
+        s.k.E1 = kept[4];
+        s.k.E2 = kept[5];
+    } else {
+        s.rho = M<double>::ex(qt[0] + s.beta * (s.u1 * s.u1 + s.u2 * s.u2) - M<double>::lg(s.beta) * inv_gm1);
+        s.sb = M<double>::sq(s.beta);
+        const double S1 = s.k.ut * s.sb, S2 = s.k.un * s.sb;
+        s.e1 = M<double>::ex(-S1 * S1);
+        s.e2 = M<double>::ex(-S2 * S2);
+        s.k.E1 = erf_e<double>(S1, s.e1);
+        s.k.E2 = erf_e<double>(S2, s.e2);
+    }
+    s.k.rho = s.rho;
     s.rsb = 1.0 / s.sb;
-    const double S1 = s.k.ut * s.sb, S2 = s.k.un * s.sb;
-    s.e1 = M<double>::ex(-S1 * S1);
-    s.e2 = M<double>::ex(-S2 * S2);
     const double half_rpi = 0.28209479177387814;  // 1 / (2 sqrt(pi))
     s.k.B1 = half_rpi * s.e1 * s.rsb;
     s.k.B2 = half_rpi * s.e2 * s.rsb;
-    s.k.E1 = erf_e<double>(S1, s.e1);
-    s.k.E2 = erf_e<double>(S2, s.e2);
     s.k.pbr = s.tm;
     s.k.usq = s.k.ut * s.k.ut + s.k.un * s.k.un;
 }

@@ -169,7 +169,8 @@ __global__ void k_func_delta(DevCloud c, const double4_32a *__restrict__ prim, d
 __device__ __forceinline__ void point_flux(const DevCloud &c, int i, int f, double nx, double ny,
                                            const double4_32a *__restrict__ q, const double4_32a *__restrict__ dq,
                                            const double4_32a *__restrict__ qm, double G[4][4],
-                                           double *__restrict__ sums = nullptr)
+                                           double *__restrict__ sums = nullptr, double *__restrict__ ends = nullptr,
+                                           long long ns = 0)
 {
     double qi[4], dxi[4], dyi[4], mxi[4], mni[4];
     ld4(q[i], qi);
@@ -201,8 +202,16 @@ __device__ __forceinline__ void point_flux(const DevCloud &c, int i, int f, doub
         double Pi[4], Pk[4];
         edge_states<double>(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, c.eps2[k], Pi, Pk);
         Kin<double> ki, kk;
-        kin_prep<double>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki);
-        kin_prep<double>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk);
+        double keep_i[3], keep_k[3];
+        kin_prep<double>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki, ends ? keep_i : nullptr);
+        kin_prep<double>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk, ends ? keep_k : nullptr);
+        if (ends) {
+            // planes [12][ns]: per end rho, sqrt(beta), exp(-S1^2), exp(-S2^2), erf(S1), erf(S2)
+            const double v[12] = {ki.rho, keep_i[0], keep_i[1], keep_i[2], ki.E1, ki.E2,
+                                  kk.rho, keep_k[0], keep_k[1], keep_k[2], kk.E1, kk.E2};
+#pragma unroll
+            for (int w = 0; w < 12; w++) ends[w * ns + e] = v[w];
+        }
 #define QLSKUM_ACC(D)                                                         \
         if (dir & (1u << D)) {                                                \
             double Gi[4], Gk[4];                                              \
@@ -253,14 +262,14 @@ __device__ __forceinline__ void combine(int f, double delta, const double G[4][4
 __global__ void __launch_bounds__(128) k_flux_residual(DevCloud c, const double4_32a *__restrict__ q,
                                                        const double4_32a *__restrict__ dq, const double4_32a *__restrict__ qm,
                                                        const double *__restrict__ delta, double4_32a *__restrict__ flux_res,
-                                                       double *__restrict__ sums)
+                                                       double *__restrict__ sums, double *__restrict__ ends, long long ns)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     const int f = c.flag[i];
     const double2 nn = c.nrm[i];
     double G[4][4], F[4];
-    point_flux(c, i, f, nn.x, nn.y, q, dq, qm, G, sums);
+    point_flux(c, i, f, nn.x, nn.y, q, dq, qm, G, sums, ends, ns);
     combine(f, delta[i], G, F);
     flux_res[i] = mk4(F);
 }
@@ -579,9 +588,9 @@ void func_delta(const Launch &L, const DevCloud &c, const double4_32a *prim, dou
 }
 
 void flux_residual(const Launch &L, const DevCloud &c, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
-                   const double *delta, double4_32a *flux_res, double *sums)
+                   const double *delta, double4_32a *flux_res, double *sums, double *ends, long long ns)
 {
-    k_flux_residual<<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq, qm, delta, flux_res, sums);
+    k_flux_residual<<<grid_for(c.n, 128), 128, 0, L.stream>>>(c, q, dq, qm, delta, flux_res, sums, ends, ns);
     QLSKUM_LAUNCHED(L);
 }
 

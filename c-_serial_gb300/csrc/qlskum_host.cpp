@@ -1994,6 +1994,7 @@ struct Set64 {
     double *delta = nullptr;
     double4_32a *flux[4] = {};         // each stage's flux residual
     double *sums[4] = {};              // each stage's directional sums (wall gradients only), [n][32]
+    double *ends[4] = {};              // each stage's edge-end transcendentals, [12][ne] (fp64::flux_residual)
 };
 
 struct AdjBuf {
@@ -2185,10 +2186,11 @@ void alloc_set32(DeviceArena &A, size_t np, int ni, Set32 &st)
 
 // The FP64 arrays of one stage-data set (its states are assigned by the
 // caller); geo: also the directional sums of the wall-gradient reverse.
-void alloc_set64(DeviceArena &A, size_t np, int ni, Set64 &st, bool geo)
+void alloc_set64(DeviceArena &A, size_t np, size_t ne, int ni, Set64 &st, bool geo)
 {
     if (geo)
         for (auto &p : st.sums) p = A.alloc<double>(32 * np);
+    for (auto &p : st.ends) p = A.alloc<double>(12 * ne);
     for (auto &p : st.q) p = A.alloc<double4_32a>(np);
     for (auto &p : st.qm) p = A.alloc<double4_32a>(2 * np);
     st.dq.resize(4 * (size_t)(ni + 1));
@@ -2197,10 +2199,11 @@ void alloc_set64(DeviceArena &A, size_t np, int ni, Set64 &st, bool geo)
     for (auto &p : st.flux) p = A.alloc<double4_32a>(np);
 }
 
-size_t set64_bytes(size_t np, int ni, bool geo)
+size_t set64_bytes(size_t np, size_t ne, int ni, bool geo)
 {
     return np * (5 * sizeof(double4_32a) + 4 * 32 + 4 * 64 + 4 * (size_t)(ni + 1) * 64 + 8 + 4 * 32 +
-                 (geo ? 4 * 32 * sizeof(double) : 0));
+                 (geo ? 4 * 32 * sizeof(double) : 0)) +
+           4 * 12 * ne * sizeof(double);
 }
 
 // Bytes of one set with its own states.
@@ -2232,8 +2235,9 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
     for (auto &p : a->P) p = A.alloc<double4_32a>(np);
     for (auto *p : {&a->bP, &a->bPacc, &a->bF, &a->lam, &a->lam_prev, &a->seed}) *p = A.alloc<double4_32a>(np);
     a->buinf = A.alloc<double>(4);  // free-stream velocity bars, then the initial-state sums
+    slice_bases(h, &a->ne);
     if (need64) {
-        alloc_set64(A, np, a->ni, a->set64, geo);
+        alloc_set64(A, np, a->ne, a->ni, a->set64, geo);
         for (int k = 0; k < 5; k++) a->set64.P[k] = a->P[k];
         a->bq = A.alloc<double4_32a>(np);
         for (auto *p : {&a->bdqA, &a->bdqB, &a->bqm}) *p = A.alloc<double4_32a>(2 * np);
@@ -2250,7 +2254,6 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
         a->bdelta32 = A.alloc<float>(np);
         a->bcs32 = A.alloc<float>(np);
     }
-    slice_bases(h, &a->ne);
     if (geo) {
         a->bedge = A.alloc<double4_32a>(a->ne);
         a->bdist = A.alloc<double>(a->ne);
@@ -2316,7 +2319,8 @@ void adj_stage_forward(qlskum_handle *h, Set64 &st, int s)
     fp64::q_variables(h->L, c, st.P[s], st.q[s]);
     fp64::q_derivatives(h->L, c, st.q[s], adj_dq(st, ni, s, 0), st.qm[s], nullptr, nullptr, 0.0);
     for (int j = 1; j <= ni; j++) fp64::q_inner(h->L, c, st.q[s], adj_dq(st, ni, s, j - 1), adj_dq(st, ni, s, j));
-    fp64::flux_residual(h->L, c, st.q[s], adj_dq(st, ni, s, ni), st.qm[s], st.delta, st.flux[s], st.sums[s]);
+    fp64::flux_residual(h->L, c, st.q[s], adj_dq(st, ni, s, ni), st.qm[s], st.delta, st.flux[s], st.sums[s],
+                        st.ends[s], (long long)h->adj->ne);
 }
 
 // The four stage states of one iteration from st.P[0] (fpi_solver_mod.h:14-40)
@@ -2348,7 +2352,8 @@ void adj_stage_reverse(qlskum_handle *h, const Set64 &st, int s, const AdjView &
     zero(h, a->bq, sizeof(double4_32a) * np);
     zero(h, a->bdqA, sizeof(double4_32a) * 2 * np);
     zero(h, a->bqm, sizeof(double4_32a) * 2 * np);
-    adjl::flux(h->L, v, st.q[s], adj_dq(st, ni, s, ni), st.qm[s], st.delta, st.flux[s], st.sums[s], a->bF, a->bq,
+    adjl::flux(h->L, v, st.q[s], adj_dq(st, ni, s, ni), st.qm[s], st.delta, st.flux[s], st.sums[s], st.ends[s],
+               (long long)a->ne, a->bF, a->bq,
                a->bdqA, a->bqm, a->bdelta);
     for (int j = ni; j >= 1; j--) {
         zero(h, a->bdqB, sizeof(double4_32a) * 2 * np);
@@ -2396,13 +2401,13 @@ bool adj_sets(qlskum_handle *h, int count, bool f64)
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
     // keep a quarter of the free memory for everything else
-    const size_t each = f64 ? set64_bytes(h->np, a->ni, geo) : set32_bytes(h->np, a->ni);
+    const size_t each = f64 ? set64_bytes(h->np, a->ne, a->ni, geo) : set32_bytes(h->np, a->ni);
     if ((double)each * count > 0.75 * (double)free_b) return false;
     std::vector<double4_32a *> p0;
     if (f64) {
         a->sets64.resize(count);
         for (auto &st : a->sets64) {
-            alloc_set64(a->set_arena, h->np, a->ni, st, geo);
+            alloc_set64(a->set_arena, h->np, a->ne, a->ni, st, geo);
             for (auto &p : st.P) p = a->set_arena.alloc<double4_32a>(h->np);
             p0.push_back(st.P[0]);
         }

@@ -185,10 +185,11 @@ void update(const Launch &L, const AdjView &a, const CaseConst &K, const double4
             const double4_32a *Pout, int rk, double4_32a *bP, double4_32a *bPold, double4_32a *bF, double *buinf);
 // flux: the stage's flux residual (the bar of delta without geometry bars);
 // sums: its directional sums (fp64::flux_residual) for the geometry bars, or
-// NULL (recomputed)
+// NULL (recomputed); ends: the edge ends' kept transcendentals
+// (fp64::flux_residual's ends, ns slots), or NULL (recomputed)
 void flux(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
-          const double *delta, const double4_32a *flux, const double *sums, const double4_32a *bF, double4_32a *bq,
-          double4_32a *bdq, double4_32a *bqm, double *bdelta);
+          const double *delta, const double4_32a *flux, const double *sums, const double *ends, long long ns,
+          const double4_32a *bF, double4_32a *bq, double4_32a *bdq, double4_32a *bqm, double *bdelta);
 void inner(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq_in,
            const double4_32a *bdq_out, double4_32a *bq, double4_32a *bdq_in);
 void grad(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *bdq, const double4_32a *bqm,
@@ -258,9 +259,13 @@ void q_derivatives(const Launch &L, const DevCloud &c, const double4_32a *q, dou
                    const double *cspeed, double *delta, double cfl);
 void q_inner(const Launch &L, const DevCloud &c, const double4_32a *q, const double4_32a *dq_in, double4_32a *dq_out);
 void func_delta(const Launch &L, const DevCloud &c, const double4_32a *prim, double *delta, double cfl);
-// sums (or NULL): each point's directional sums {sx[d][r], sy[d][r]}, [n][32] doubles
+// sums (or NULL): each point's directional sums {sx[d][r], sy[d][r]}, [n][32] doubles.
+// ends (or NULL): per edge slot of the ns slots, the owner's and the
+// neighbour's end's rho, sqrt(beta), exp(-S1^2), exp(-S2^2), erf(S1),
+// erf(S2), as 12 planes of ns doubles (read back by the flux reverse).
 void flux_residual(const Launch &L, const DevCloud &c, const double4_32a *q, const double4_32a *dq, const double4_32a *qm,
-                   const double *delta, double4_32a *flux_res, double *sums = nullptr);
+                   const double *delta, double4_32a *flux_res, double *sums = nullptr, double *ends = nullptr,
+                   long long ns = 0);
 void state_update(const Launch &L, const DevCloud &c, const CaseConst &k, double4_32a *prim, const double4_32a *prim_old,
                   const double4_32a *flux_res, int rk, const Reduce &R);
 void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const double4_32a *q, const double4_32a *dq,

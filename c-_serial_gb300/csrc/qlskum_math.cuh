@@ -136,8 +136,10 @@ template <typename R> struct Kin {
     R rho, ut, un, pbr, usq, B1, B2, E1, E2;
 };
 
+// keep != nullptr: also {sqrt(beta), exp(-S1^2), exp(-S2^2)}, which the
+// FP64 reverse reads back instead of recomputing them.
 template <typename R>
-QLSKUM_HD void kin_prep(R nx, R ny, R u1, R u2, R rho, R pr, Kin<R> &k)
+QLSKUM_HD void kin_prep(R nx, R ny, R u1, R u2, R rho, R pr, Kin<R> &k, R *keep = nullptr)
 {
     R tx = ny, ty = -nx;
     k.ut = u1 * tx + u2 * ty;
@@ -147,6 +149,11 @@ QLSKUM_HD void kin_prep(R nx, R ny, R u1, R u2, R rho, R pr, Kin<R> &k)
     R S1 = k.ut * sb;
     R S2 = k.un * sb;
     const R e1 = M<R>::ex(-S1 * S1), e2 = M<R>::ex(-S2 * S2);
+    if (keep) {
+        keep[0] = sb;
+        keep[1] = e1;
+        keep[2] = e2;
+    }
     k.B1 = M<R>::rdsq(R(0.5) * e1, R(QLSKUM_PI) * beta);
     k.B2 = M<R>::rdsq(R(0.5) * e2, R(QLSKUM_PI) * beta);
     k.E1 = erf_e<R>(S1, e1);

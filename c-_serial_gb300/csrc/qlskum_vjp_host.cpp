@@ -154,6 +154,32 @@ void qlskum_dbg_end64_flux_vjp(int f, int D, const double *in, double e2, double
                    out[21], out[22], out[23]);
 }
 
+// The same reverse with the transcendentals taken from the forward's own
+// evaluation (edge_end, qtilde_to_prim, kin_prep with keep), as the FP64
+// flux reverse reads them from the recording forward.
+void qlskum_dbg_end64_flux_vjp_kept(int f, int D, const double *in, double e2, double delx, double dely, double nx,
+                                    double ny, const double *bG, double *out)
+{
+    double qt[4], P[4], keep[3];
+    qlskum_dbg_edge_end(in, e2, delx, dely, qt);
+    qtilde_to_prim<double>(qt, P[1], P[2], P[0], P[3]);
+    Kin<double> k;
+    kin_prep<double>(nx, ny, P[1], P[2], P[0], P[3], k, keep);
+    const double kept[6] = {k.rho, keep[0], keep[1], keep[2], k.E1, k.E2};
+    adj::End64 s;
+    adj::end64(nx, ny, delx, dely, in, in + 4, in + 8, in + 12, in + 16, e2, s, kept);
+    adj::KinBar kb;
+    switch (D) {
+    case 0: adj::dir_flux_vjp<0>(f, s.k, bG, kb); break;
+    case 1: adj::dir_flux_vjp<1>(f, s.k, bG, kb); break;
+    case 2: adj::dir_flux_vjp<2>(f, s.k, bG, kb); break;
+    default: adj::dir_flux_vjp<3>(f, s.k, bG, kb); break;
+    }
+    for (int r = 0; r < 24; r++) out[r] = 0;
+    adj::end64_vjp(s, nx, ny, delx, dely, in + 4, in + 8, kb, out, out + 4, out + 8, out + 12, out + 16, out[20],
+                   out[21], out[22], out[23]);
+}
+
 void qlskum_dbg_stage_update(int f, double nx, double ny, const double *Pin, const double *Pold, const double *F,
                              int rk, double mach, double aoa, double *Pout)
 {

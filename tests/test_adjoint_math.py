@@ -168,12 +168,15 @@ def test_fp64_edge_end_reverse(L, f, D):
     reconstruction, q~ -> prim and the half-range flux of one edge end,
     w.r.t. q, dq, qm, the edge vector and the normal, against central
     differences of the solver's own forward functions; its kept forward
-    state gives the solver's flux to rounding."""
+    state gives the solver's flux to rounding, and the reverse from the
+    forward's kept transcendentals equals it to rounding."""
     sig = [C.c_int, C.c_int, dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]
     L.qlskum_dbg_end_flux.argtypes = sig + [dp]
     L.qlskum_dbg_end64_flux.argtypes = sig + [dp]
     L.qlskum_dbg_end64_flux_vjp.argtypes = sig + [dp, dp]
-    for fn in ("qlskum_dbg_end_flux", "qlskum_dbg_end64_flux", "qlskum_dbg_end64_flux_vjp"):
+    L.qlskum_dbg_end64_flux_vjp_kept.argtypes = sig + [dp, dp]
+    for fn in ("qlskum_dbg_end_flux", "qlskum_dbg_end64_flux", "qlskum_dbg_end64_flux_vjp",
+               "qlskum_dbg_end64_flux_vjp_kept"):
         getattr(L, fn).restype = None
     rng = np.random.default_rng(50 + 10 * f + D)
     e2 = 1e-7
@@ -200,6 +203,11 @@ def test_fp64_edge_end_reverse(L, f, D):
             return o
         check(fwd, vj, x, 4, rng, h=1e-8, rtol=2e-6)
         np.testing.assert_allclose(fwd(x, L.qlskum_dbg_end64_flux), fwd(x), rtol=1e-13, atol=1e-15)
+        # with the transcendentals the forward kept (the recording forward's path)
+        w = rng.standard_normal(4)
+        kept = np.zeros(24)
+        L.qlskum_dbg_end64_flux_vjp_kept(f, D, P(x[:20]), e2, x[20], x[21], x[22], x[23], P(w), P(kept))
+        np.testing.assert_allclose(kept, vj(x, w), rtol=1e-10, atol=1e-12 * np.abs(vj(x, w)).max())
     assert n_lim >= 4   # the limiter's phi < 1 branch is exercised
 
 
