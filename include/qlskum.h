@@ -322,8 +322,10 @@ qlskum_status qlskum_residual_vjp_full(qlskum_handle *h, const double *prim, con
  * the derivative w.r.t. the initial state.  Device memory: 32 bytes per
  * point per kept state (every stride-th iteration, qlskum_set_adjoint_stride).
  * Each iteration's stage data is also kept where it fits in three quarters
- * of the free device memory (FP64 handles about 1.7 KB, MIXED handles without
- * dJ_dwall about 1 KB per point per iteration at 3 inner steps): with stride 1
+ * of the free device memory (FP64 handles about 1.7 KB per point plus 384
+ * bytes per edge slot for the edge ends' kept transcendentals, about 5.5 KB
+ * per point at 10 neighbours; MIXED handles without dJ_dwall about 1 KB per
+ * point; per iteration at 3 inner steps): with stride 1
  * for all `iters` iterations (the primal then runs as the recording
  * iteration, with the same state, prim_old and residual history as
  * qlskum_q_lskum, and the reverse recomputes nothing), with a larger stride
