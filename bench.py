@@ -396,7 +396,7 @@ def run_long(args):
                "rel_dentropy": abs(obj["mixed"][3] - obj["fp64"][3]) / abs(obj["fp64"][3])}
         rows.append(row)
         log(json.dumps(row))
-    out = {"workload": WORKLOADS[args.workload].get("name", args.workload), "points": cloud.n,
+    out = {"workload": args.workload, "points": cloud.n,
            "iterations": done, "failed": failed, "seconds": seconds, "history": rows}
     if failed is None:
         pm, pd = forms["mixed"].prim, forms["fp64"].prim
