@@ -17,7 +17,13 @@
 //     library holds it until the process exits.
 //   * The first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, with that device current); make
-//     that first call before any stream capture.
+//     that first call before any stream capture.  The address is kept for
+//     the life of the process: a cudaDeviceReset (or anything else that
+//     destroys the device's primary context) makes it stale, and later calls
+//     on that device are then invalid.
+//   * Errors of the launches are reported with cudaPeekAtLastError, which
+//     leaves the error state as it was: an error that the caller's own work
+//     left pending is reported too, and stays visible to the caller.
 //   * All calls share the one array and it keeps the previous call's
 //     contents.  Each call writes every partial it later reads, so nothing has
 //     to start at zero, but calls that overlap on the GPU (two streams, two
@@ -119,11 +125,14 @@ extern "C" qlskum_status qlskum_state_update_noalloc(int n, int rk, double mach,
     if (n < 1 || (long long)n > noalloc::kNoallocMaxPoints) return QLSKUM_ERR_INVALID;
     if (rk < 1 || rk > 4) return QLSKUM_ERR_INVALID;
     if (!flag_1 || !normals || !prim || !prim_old || !flux_res || !residual_out) return QLSKUM_ERR_INVALID;
-    // double4_32a / double2 loads need 32- and 16-byte aligned rows
+    // double4_32a / double2 loads need 32- and 16-byte aligned rows; the
+    // residual is two doubles, the classes int32
     if ((reinterpret_cast<uintptr_t>(prim) | reinterpret_cast<uintptr_t>(prim_old) |
          reinterpret_cast<uintptr_t>(flux_res)) & 31u)
         return QLSKUM_ERR_INVALID;
     if (reinterpret_cast<uintptr_t>(normals) & 15u) return QLSKUM_ERR_INVALID;
+    if (reinterpret_cast<uintptr_t>(residual_out) & 7u) return QLSKUM_ERR_INVALID;
+    if (reinterpret_cast<uintptr_t>(flag_1) & 3u) return QLSKUM_ERR_INVALID;
     double *scratch = nullptr;
     if (noalloc::scratch_for_current_device(&scratch) != cudaSuccess) return QLSKUM_ERR_CUDA;
     CaseConst K{};
@@ -141,6 +150,7 @@ extern "C" qlskum_status qlskum_state_update_noalloc(int n, int rk, double mach,
     noalloc::k_update<<<blocks, noalloc::kBlock, 0, s>>>(
         n, K, flag_1, reinterpret_cast<const double2 *>(normals), reinterpret_cast<double4_32a *>(prim),
         reinterpret_cast<const double4_32a *>(prim_old), reinterpret_cast<const double4_32a *>(flux_res), rk, scratch);
+    if (cudaPeekAtLastError() != cudaSuccess) return QLSKUM_ERR_CUDA;
     noalloc::k_finish<<<1, noalloc::kBlock, 0, s>>>(blocks, scratch, residual_out);
-    return cudaGetLastError() == cudaSuccess ? QLSKUM_OK : QLSKUM_ERR_CUDA;
+    return cudaPeekAtLastError() == cudaSuccess ? QLSKUM_OK : QLSKUM_ERR_CUDA;
 }

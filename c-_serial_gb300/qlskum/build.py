@@ -1,6 +1,6 @@
 """Build recipe of the in-tree CUDA library (libqlskum.so) for sm_103a.
 
-Seven translation units compiled in parallel and linked into one shared
+Six translation units compiled in parallel and linked into one shared
 library with a C ABI (include/qlskum.h):
 
 * csrc/qlskum_fp64.cu  -- FP64 drop-in kernels, -fmad=false (no FMA
@@ -12,9 +12,12 @@ library with a C ABI (include/qlskum.h):
 * csrc/qlskum_host.cpp -- host layer, g++ -ffp-contract=off (bit-exact
   sub-stencil classification on x86-64 and aarch64 alike);
 * csrc/qlskum_io.cpp -- partGrid file I/O and the sub-stencil quality check
-  (host only, no GPU needed);
-* csrc/qlskum_vjp_host.cpp -- the per-point arithmetic and its reverse mode
-  compiled for the host, for derivative checks without a GPU.
+  (host only, no GPU needed).
+
+`build_vjp_host()` compiles a separate, test-only library
+(tests/vjp_host/qlskum_vjp_host.cpp -> tests/_build/libqlskum_vjp_host.so):
+the per-point arithmetic and its reverse mode compiled for the host, for
+derivative checks without a GPU.  It is not part of libqlskum.so.
 
 Output: c-_serial_gb300/_build/libqlskum.so (git-ignored; rebuilt on the GPU
 machine because binaries do not travel between architectures).
@@ -56,7 +59,6 @@ def sources():
         "qlskum_adjoint.cu": [],
         "qlskum_host.cpp": [],
         "qlskum_io.cpp": [],
-        "qlskum_vjp_host.cpp": [],
     }
 
 
@@ -114,6 +116,27 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         raise RuntimeError("linking libqlskum failed:\n" + " ".join(link) + "\n" + r.stdout)
     os.replace(tmp, LIB)
     return LIB
+
+
+VJP_SRC = os.path.join(REPO, "tests", "vjp_host", "qlskum_vjp_host.cpp")
+VJP_LIB = os.path.join(REPO, "tests", "_build", "libqlskum_vjp_host.so")
+
+
+def build_vjp_host() -> str:
+    """Compile the test-only host build of the per-point reverse arithmetic
+    (g++, no GPU needed) if missing or stale; return its path."""
+    deps = [VJP_SRC] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    if os.path.exists(VJP_LIB) and all(os.path.getmtime(p) <= os.path.getmtime(VJP_LIB) for p in deps):
+        return VJP_LIB
+    os.makedirs(os.path.dirname(VJP_LIB), exist_ok=True)
+    tmp = VJP_LIB + f".tmp{os.getpid()}"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
+           "-I", INCLUDE, "-I", CSRC, "-I", _cuda_include(_nvcc()), VJP_SRC, "-o", tmp]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("building the host VJP test library failed:\n" + " ".join(cmd) + "\n" + r.stdout)
+    os.replace(tmp, VJP_LIB)
+    return VJP_LIB
 
 
 if __name__ == "__main__":

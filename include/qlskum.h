@@ -361,11 +361,15 @@ qlskum_status qlskum_adjoint_fixed_point(qlskum_handle *h, int objective, int ad
  *   sum and the maximum of res_sqr over wall and interior points
  *   (state_update_mod.h:157-165).  stream: a cudaStream_t or NULL.
  * At most QLSKUM_NOALLOC_MAX_POINTS points; larger n returns
- * QLSKUM_ERR_INVALID.  The per-block partial sums live in one 128 KiB static
+ * QLSKUM_ERR_INVALID, as are misaligned buffers (residual_out 8 bytes,
+ * flag_1 4 bytes).  The per-block partial sums live in one 128 KiB static
  * device array that every GPU loading the library keeps until the process
  * exits.  The first call on a device looks up that array's address; make it
- * before any stream capture.  Every call reuses the array: calls that overlap
- * on the GPU race and must be serialised by the caller. */
+ * before any stream capture.  The address is kept for the process's life: a
+ * cudaDeviceReset makes later calls on that device invalid.  Every call
+ * reuses the array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  Launch errors are read with
+ * cudaPeekAtLastError (the error state is left as it was). */
 #define QLSKUM_NOALLOC_MAX_POINTS 2097152
 qlskum_status qlskum_state_update_noalloc(int n, int rk, double mach, double aoa, const int *flag_1,
                                           const double *normals, double *prim, const double *prim_old,

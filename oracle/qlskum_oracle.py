@@ -43,6 +43,15 @@ def build_reference() -> str | None:
     return REF_BIN if os.path.exists(REF_BIN) else None
 
 
+def reference_dir() -> str | None:
+    """The reference source directory oracle/build_ref.sh last built from, or None."""
+    p = os.path.join(os.path.dirname(REF_BIN), "source_dir")
+    if not (os.path.exists(REF_BIN) and os.path.exists(p)):
+        return None
+    d = open(p).read().strip()
+    return d if os.path.isdir(d) else None
+
+
 class _Cloud(C.Structure):
     _fields_ = [("n", C.c_int),
                 ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),

@@ -69,9 +69,9 @@ def run_ref(binary, mode, grid, **kw):
 
 def main():
     ref = qlskum_oracle.build_reference()
-    if ref is None:
+    refdir = qlskum_oracle.reference_dir()
+    if ref is None or refdir is None:
         sys.exit("reference sources not found (set QLSKUM_REFERENCE_DIR)")
-    refdir = os.environ.get("QLSKUM_REFERENCE_DIR", "/root/reference")
 
     # flux KAT on data.dat rows
     rows = np.loadtxt(os.path.join(refdir, "data.dat"))[:400]

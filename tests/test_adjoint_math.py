@@ -13,8 +13,9 @@ dp = C.POINTER(C.c_double)
 
 @pytest.fixture(scope="module")
 def L():
-    import qlskum
-    lib = qlskum.load()
+    """The test-only host build of the per-point arithmetic (not part of libqlskum.so)."""
+    from qlskum import build
+    lib = C.CDLL(build.build_vjp_host())
     sig = {
         "qlskum_dbg_prim_to_q": [dp, dp], "qlskum_dbg_prim_to_q_vjp": [dp, dp, dp],
         "qlskum_dbg_qtilde_to_prim": [dp, dp], "qlskum_dbg_qtilde_to_prim_vjp": [dp, dp, dp],

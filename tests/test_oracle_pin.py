@@ -109,13 +109,12 @@ def test_threads_do_not_change_results(oracle_mod):
     assert np.array_equal(a.prim, b.prim)
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(os.environ.get("QLSKUM_REFERENCE_DIR", "/root/reference"),
-                                                    "q_lskum_mod.h")),
-                    reason="reference sources not present")
 def test_against_reference_build(oracle_mod):
     """Oracle vs the reference compiled here, on a cloud and knobs no fixture uses."""
     from qlskum import cloudgen
     ref = oracle_mod.build_reference()
+    if ref is None:
+        pytest.skip("reference sources not present (oracle/build_ref.sh built nothing)")
     c = cloudgen.make_cloud(n_wall=48, n_layers=24, first_spacing=5e-3, radius=3.0, seed=23, m=0.02, p=0.4, t=0.1)
     tmp = tempfile.mkdtemp()
     grid = os.path.join(tmp, "g")
