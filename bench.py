@@ -171,16 +171,61 @@ def flux_update_bytes(cloud, precision: str, unit_weights: bool = True) -> float
     return n * per_pt + e * per_edge
 
 
-def measured_traffic(workload, precision, kernel):
-    """DRAM bytes per launch of `kernel` (dram__bytes_read.sum + dram__bytes_write.sum)
-    from the committed ncu summary of this workload, or None when none was captured.
-    The summaries carry lines 'traffic <precision> <kernel> <bytes>'."""
+def point_pass_bytes(cloud, precision: str, unit_weights: bool = True) -> dict:
+    """Compulsory bytes of one launch of each per-stage kernel, counted like
+    flux_update_bytes (each per-point array once per launch that needs it,
+    neighbour gathers served from cache, the streamed per-edge data once).
+
+    Mixed form (q, dq, qm FP32):
+    * gradient + max / min: own q 16, dq0 32 and qm 32 written, nbhs 4, slice
+      base 8/32; per edge neighbour index 4, folded gradient weights 8; the
+      first stage of four also the time step (wave speed 4 per point, delta 4
+      written, edge length 4 per edge), averaged over the stages;
+    * inner step: dq0 32, own dq 32, dq out 32, nbhs and slice base; per edge
+      index 4, edge vector 8 (16 with weights), folded weights 8;
+    * flux + update: flux_update_bytes.
+    FP64 form: the same arrays at 8-byte widths (moments 32 B per point, edge
+    vector and weights 32 B per edge in the gradient and inner kernels)."""
+    n = cloud.n
+    e = int(cloud.nbhs.sum())
+    if precision == "mixed":
+        grad = n * (16 + 32 + 32 + 4 + 8 / 32 + (4 + 4) / 4) + e * (4 + 8 + 4 / 4)
+        inner = n * (32 + 32 + 32 + 4 + 8 / 32) + e * (4 + (8 if unit_weights else 16) + 8)
+    else:
+        grad = n * (32 + 64 + 64 + 32 + 4 + 8 / 32 + (8 + 8) / 4) + e * (4 + 32 + 8 / 4)
+        inner = n * (32 + 64 + 64 + 32 + 4 + 8 / 32) + e * (4 + 32)
+    return {"gradient": grad, "inner": inner, "flux_update": flux_update_bytes(cloud, precision, unit_weights)}
+
+
+def bytes_per_point_iteration(cloud, precision: str, inner: int, unit_weights: bool = True) -> dict:
+    """Algorithmic bytes per point-iteration: 4 stages x (gradient + inner x
+    inner step + flux + update), from point_pass_bytes, divided by the points.
+    FP64 also by the survey's formula 4 (252 + 404 + 220 inner) + 100 (the
+    reference's arrays at 10 neighbours)."""
+    pb = point_pass_bytes(cloud, precision, unit_weights)
+    per = 4 * (pb["gradient"] + inner * pb["inner"] + pb["flux_update"]) / cloud.n
+    k = float(cloud.nbhs.mean())
+    out = {"bytes": per, "neighbours_per_point": k}
+    if precision == "mixed":
+        out["formula"] = ("4*((86.25+13K) + inner*(100.25+20K) + (198.25+21K)) with K neighbours per point "
+                          "(unit weights; FP32 q/dq/qm, FP64 prim, FP32 folded weights)")
+    else:
+        out["formula"] = "4*(252 + 404 + 220*inner) + 100 (FP64 arrays, K = 10)"
+        out["survey_bytes"] = 4 * (252 + 404 + 220 * inner) + 100
+    return out
+
+
+def measured_profile(workload, precision, kernel, key="traffic"):
+    """A per-launch figure of `kernel` from the committed ncu summary of this
+    workload, or (None, None): 'traffic' = dram__bytes_read.sum +
+    dram__bytes_write.sum, 'inst' = smsp__inst_executed.sum (warp
+    instructions).  The summaries carry lines '<key> <precision> <kernel> <value>'."""
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"k_flux_update_{workload}_1M.md")
     family = None
     try:
         for line in open(path):
             f = line.strip().strip("`").split()
-            if len(f) == 4 and f[0] == "traffic" and f[1] == precision:
+            if len(f) == 4 and f[0] == key and f[1] == precision:
                 if f[2] == kernel:
                     return float(f[3]), f[2]
                 if f[2].split("<")[0] == kernel.split("<")[0]:
@@ -188,6 +233,10 @@ def measured_traffic(workload, precision, kernel):
     except OSError:
         pass
     return family if family else (None, None)
+
+
+def measured_traffic(workload, precision, kernel):
+    return measured_profile(workload, precision, kernel, "traffic")
 
 
 def time_solver(qlskum, torch, solver, steps):
@@ -243,7 +292,7 @@ def cpu_baseline(workload, cloud, threads, iters):
     return cloud.n * iters / dt, dt
 
 
-def batch_workload(seed=3, n_clouds=32, n_cases=64):
+def batch_workload(seed=3, n_clouds=32, n_cases=64, size_range=(20_000, 500_000)):
     """Seeded NACA 4-digit clouds (thickness 8-16%, camber 0-4%, camber
     position 0.3-0.5) of 20k-500k points, and flight conditions M 0.5-0.85,
     AoA -2..4 deg; case j solves cloud j mod n_clouds."""
@@ -251,7 +300,7 @@ def batch_workload(seed=3, n_clouds=32, n_cases=64):
     rng = np.random.default_rng(seed)
     clouds = []
     for k in range(n_clouds):
-        size = int(rng.uniform(20_000, 500_000))
+        size = int(rng.uniform(*size_range))
         n_wall = max(64, int(round(np.sqrt(size) / 8)) * 8)
         n_layers = max(12, size // n_wall)
         t = rng.uniform(0.08, 0.16)
@@ -453,6 +502,38 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def batch_leg(torch, qlskum, warmup=3, steps=10):
+    """The batched launch on a reduced config-3 workload for the default
+    line: 8 seeded NACA 4-digit clouds of 20k-100k points, 16 flight
+    conditions (M 0.5-0.85, AoA -2..4 deg), mixed precision, 3 inner
+    iterations, autotuned; aggregate point-iter/s over all cases (CUDA
+    events on the batch's stream)."""
+    t0 = time.perf_counter()
+    clouds, cases = batch_workload(seed=4, n_clouds=8, n_cases=16, size_range=(20_000, 100_000))
+    t_gen = time.perf_counter() - t0
+    kw = dict(cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=3)
+    b = qlskum.Batch(clouds, cases, **kw)
+    b.run(warmup)
+    stream = torch.cuda.ExternalStream(b.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    l0 = b.launches
+    e0.record(stream)
+    b.run(steps)
+    e1.record(stream)
+    e1.synchronize()
+    dt = e0.elapsed_time(e1) / 1e3
+    cl, cd, _, _ = b.objective()
+    out = {"workload": "batch_16_conditions_8_clouds_20k_100k", "value": b.total_points * steps / dt,
+           "unit": "point-iter/s", "steps": steps, "warmup": warmup, "ms_per_step": dt / steps * 1e3,
+           "cases": len(cases), "points": b.total_points, "cloud_sizes": [c.n for c in clouds],
+           "gpu_launches": b.launches - l0, "tuning": b.tuning(), "finite": bool(np.isfinite(cl).all()),
+           "cloud_generation_s": t_gen, **kw}
+    b.close()
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -555,7 +636,11 @@ def main():
     ap.add_argument("--adjoint-stride", type=int, default=1,
                     help="adjoint checkpoint stride in iterations (2 = every 8 SSPRK steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--cpu-iters", type=int, default=3,
+                    help="iterations of the CPU baseline (one core and all cores)")
+    ap.add_argument("--no-batch-leg", dest="batch_leg", action="store_false",
+                    help="skip the reduced batched-launch leg of the default line")
     ap.add_argument("--adjoint-iters", type=int, default=3,
                     help="iterations differentiated by the adjoint timings (FP64 and mixed handles; 0: skip)")
     ap.add_argument("--long-iters", type=int, default=0,
@@ -624,16 +709,46 @@ def main():
     fl_ms, fl_n = kt["flux_update"]
     total_ms = sum(v[0] for v in kt.values())
     peak, peak_kind = measured_peaks()
-    nbytes = flux_update_bytes(cloud, args.precision, kw["power"] == 0.0)
+    unit_w = kw["power"] == 0.0
+    pbytes = point_pass_bytes(cloud, args.precision, unit_w)
+    nbytes = pbytes["flux_update"]
     achieved = nbytes / (fl_ms / fl_n / 1e3) / 1e9
     lc = solver.launch_config()
     kname = (f"k_flux_update{'_st' if lc['flux_variant'] >= 4 else ''}<{lc['flux_block']},{lc['flux_min_blocks']}>"
              if prec == qlskum.MIXED else "k_flux_update<128>")
     traffic, traffic_kernel = measured_traffic(args.workload, args.precision, kname)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+    # every per-stage kernel against HBM (event-timed launches, compulsory bytes)
+    kernels = {}
+    for kk in ("gradient", "inner", "flux_update"):
+        ms, nl = kt[kk]
+        if nl:
+            a = pbytes[kk] / (ms / nl / 1e3) / 1e9
+            kernels[kk] = {"algorithmic_bytes_per_launch": pbytes[kk], "avg_launch_ms": ms / nl, "launches": nl,
+                           "achieved_gbs": a, "frac": a / peak, "share": ms / total_ms}
+    # the flux kernel's instruction-issue roofline: its warp instructions
+    # per launch (ncu, committed summary) over 152 SMs x 4 schedulers x the
+    # SM clock sampled in the timed region
+    inst, inst_kernel = measured_profile(args.workload, args.precision, kname, "inst")
+    sm_mhz = clocks.summary().get("sm_mhz") or 2070.0
+    issue = None
+    bound = "hbm"
+    if inst:
+        n_sm = torch.cuda.get_device_properties(0).multi_processor_count
+        t_issue = inst / (n_sm * 4 * sm_mhz * 1e6)
+        issue = {"warp_instructions_per_launch": inst, "captured_on": inst_kernel, "sms": n_sm,
+                 "sm_mhz": sm_mhz, "issue_limited_ms": t_issue * 1e3,
+                 "frac": t_issue / (fl_ms / fl_n / 1e3),
+                 "note": "1.0 = one warp instruction per scheduler per cycle for the whole launch"}
+        bound = "issue" if issue["frac"] > achieved / peak else "hbm"
+    roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "traffic_captured_on": traffic_kernel, "kernel": f"{kname} ({args.precision})",
                 "algorithmic_bytes_per_launch": nbytes, "avg_launch_ms": fl_ms / fl_n,
-                "kernel_share": fl_ms / total_ms, "peak_source": f"{peak_kind} hbm_gbs"}
+                "kernel_share": fl_ms / total_ms, "peak_source": f"{peak_kind} hbm_gbs", "issue": issue,
+                "kernels": kernels}
+    bpi = bytes_per_point_iteration(cloud, args.precision, kw["inner_iterations"], unit_w)
+    whole = bpi["bytes"] * cloud.n / (dt / args.steps) / 1e9
+    roofline["iteration"] = dict(bpi, achieved_gbs=whole, frac=whole / peak,
+                                 note="bytes per point-iteration x points / ms_per_step")
 
     # the other form on the same cloud and iteration count, for the ratio and the Cl / Cd gap
     other = qlskum.FP64 if prec == qlskum.MIXED else qlskum.MIXED
@@ -645,10 +760,18 @@ def main():
     s2.q_lskum(args.steps - n2) if args.steps > n2 else None
     cl2, cd2, cm2, ent2 = s2.objective()
     fp64_value, mixed_value = (v2, value) if other == qlskum.FP64 else (value, v2)
+    r1 = float(solver.residual_history()[-1][0])
+    r2 = float(s2.residual_history()[-1][0])
+    ent64 = ent2 if other == qlskum.FP64 else ent
     compare = {"fp64_point_iter_s": fp64_value, "mixed_point_iter_s": mixed_value,
-               "mixed_over_fp64": mixed_value / fp64_value,
+               "mixed_over_fp64": mixed_value / fp64_value, "fp64_timed_iterations": n2,
                "after_iterations": args.warmup + args.steps,
-               "cl": cl, "cd": cd, "abs_dcl": abs(cl - cl2), "abs_dcd": abs(cd - cd2)}
+               "cl": cl, "cd": cd, "abs_dcl": abs(cl - cl2), "abs_dcd": abs(cd - cd2),
+               "total_entropy_fp64": ent64, "abs_dentropy": abs(ent - ent2),
+               "rel_dentropy": abs(ent - ent2) / max(abs(ent64), 1e-300),
+               "res_new_mixed": r1 if prec == qlskum.MIXED else r2,
+               "res_new_fp64": r2 if prec == qlskum.MIXED else r1,
+               "rel_dres": abs(r1 - r2) / max(abs(r2 if prec == qlskum.MIXED else r1), 1e-300)}
 
     # discrete adjoint: dCl/dMach, dCl/dAoA through K iterations from the
     # free stream (checkpointed primal + reverse sweep), against the same K
@@ -670,17 +793,23 @@ def main():
     e2e_v, h2d, d2h = e2e_rate(qlskum, solver, cloud.n, e2e_steps)
     e2e_v *= world
 
+    batch = None
+    if rank == 0 and world == 1 and args.batch_leg and args.workload == "transonic":
+        batch = batch_leg(torch, qlskum)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # the reference's serial path on one host core (the benchmark spec's
         # baseline), and the same code on every host core beside it
-        cv, cdt = cpu_baseline(args.workload, cloud, 1, 1)
+        ci = args.cpu_iters
+        cv, cdt = cpu_baseline(args.workload, cloud, 1, ci)
         thr = os.cpu_count() or 1
-        cv_all, cdt_all = cpu_baseline(args.workload, cloud, thr, 1)
+        cv_all, cdt_all = cpu_baseline(args.workload, cloud, thr, ci)
         cpu = {"value": cv, "unit": "point-iter/s", "cores": 1, "kind": "port",
-               "sample": f"1 iteration of the same {cloud.n}-point cloud ({cdt:.1f}s), C restatement of the "
-                         f"reference's serial FP64 path (bit-identical to it on x86-64), one core",
-               "all_cores": {"value": cv_all, "cores": thr, "seconds": cdt_all}}
+               "sample": f"{ci} iterations of the same {cloud.n}-point cloud from the free stream ({cdt:.1f}s), "
+                         f"C restatement of the reference's serial FP64 path (bit-identical to it on x86-64), "
+                         f"one core",
+               "all_cores": {"value": cv_all, "cores": thr, "seconds": cdt_all, "iterations": ci}}
 
     if rank == 0:
         line = {
@@ -694,7 +823,7 @@ def main():
             "e2e": {"value": e2e_v, "unit": "point-iter/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "roofline": roofline, "cpu_baseline": cpu, "fp64_vs_mixed": compare, "adjoint": adjoint,
-            "adjoint_mixed": adjoint_mixed,
+            "adjoint_mixed": adjoint_mixed, "batch": batch,
             "kernel_ms_per_iteration": {k: v[0] / max(1, 2) for k, v in kt.items()},
             "launch_config": solver.launch_config(),
         }

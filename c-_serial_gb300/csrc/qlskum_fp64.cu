@@ -746,4 +746,43 @@ void objective(const Launch &L, const DevCloud &c, const double4_32a *prim, cons
 }
 
 }  // namespace fp64
+
+namespace halo {
+
+// One thread per (ghost, 16-byte word) of the element.
+__global__ void k_pull16(int n, int w, const int *__restrict__ idx, const float4 *__restrict__ src,
+                         float4 *__restrict__ dst)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * w) return;
+    const int g = (int)(t / w), j = (int)(t - (long long)g * w);
+    dst[t] = src[(long long)idx[g] * w + j];
+}
+
+template <typename T>
+__global__ void k_pull(int n, const int *__restrict__ idx, const T *__restrict__ src, T *__restrict__ dst)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < n) dst[g] = src[idx[g]];
+}
+
+void pull(const Launch &L, int n, const int *idx, const void *src, void *dst, int bytes)
+{
+    if (n <= 0) return;
+    if (bytes == 4) {
+        k_pull<float><<<fp64::grid_for(n, 256), 256, 0, L.stream>>>(n, idx, static_cast<const float *>(src),
+                                                             static_cast<float *>(dst));
+    } else if (bytes == 8) {
+        k_pull<double><<<fp64::grid_for(n, 256), 256, 0, L.stream>>>(n, idx, static_cast<const double *>(src),
+                                                              static_cast<double *>(dst));
+    } else {
+        const int w = bytes / 16;
+        const long long items = (long long)n * w;
+        k_pull16<<<(int)((items + 255) / 256), 256, 0, L.stream>>>(n, w, idx, static_cast<const float4 *>(src),
+                                                                    static_cast<float4 *>(dst));
+    }
+    if (L.launches) ++*L.launches;
+}
+
+}  // namespace halo
 }  // namespace qlskum

@@ -339,19 +339,23 @@ qlskum_status precompute(const qlskum_cloud *c, const qlskum_params *p, Precomp 
     return QLSKUM_OK;
 }
 
-void set_case(qlskum_handle *h)
+// parameter_mod.h:4-30: the free stream of a case
+CaseConst case_of(const qlskum_params &p)
 {
-    CaseConst &K = h->K;
+    CaseConst K{};
     K.pi = 4 * std::atan(1.0);
     K.rho_inf = 1.0;
     K.pr_inf = 1.0 / 1.4;
     K.gamma = 1.4;
-    K.mach = h->prm.mach;
-    K.theta = h->prm.aoa * K.pi / 180;
-    K.u1_inf = h->prm.mach * std::cos(K.theta);
-    K.u2_inf = h->prm.mach * std::sin(K.theta);
-    K.cfl = h->prm.cfl;
+    K.mach = p.mach;
+    K.theta = p.aoa * K.pi / 180;
+    K.u1_inf = p.mach * std::cos(K.theta);
+    K.u2_inf = p.mach * std::sin(K.theta);
+    K.cfl = p.cfl;
+    return K;
 }
+
+void set_case(qlskum_handle *h) { h->K = case_of(h->prm); }
 
 qlskum_status ensure_hist(qlskum_handle *h, int needed)
 {
@@ -606,24 +610,50 @@ struct Geometry {
     double4_32a *d_wall_geo = nullptr;
 };
 
+// One partition of a cloud in the reference's distributed layout
+// (data_structure_mod.h:4-8 local_points / ghost_points / pghost,
+// point_preprocessing_mod.h:124-132): the points it owns, in device order,
+// then the ghost points its own points read, appended after them (slot
+// n_local + g).  slot[i]: the partition's slot of global point i, -1 when it
+// neither owns nor mirrors it.
+struct PartSpec {
+    std::vector<int> local;   // device position -> global index
+    std::vector<int> ghost;   // ghost g -> global index
+    std::vector<int> slot;    // global index -> slot, or -1
+};
+
 namespace {
 
 // The device geometry of one cloud: point order (class, then Morton code),
 // sliced-ELL edge arrays and every per-point / per-edge quantity the kernels
-// read, uploaded on `stream` into `A`.  G.pc must already hold precompute()'s
-// result (done first, on the host only, so malformed clouds are reported
-// before any device work).  need_fp64 / need_mixed select the arrays of the
+// read, uploaded on `stream` into `A`.  G.pc (or `pc`) must already hold
+// precompute()'s result (done first, on the host only, so malformed clouds
+// are reported before any device work).  need_fp64 / need_mixed select the arrays of the
 // FP64 and the mixed kernels.  Synchronises the stream.
+//
+// With a partition `ps`, the device arrays are those of the partition: its
+// own points (ps->local, already in device order) are the kernels' points,
+// their edges address the partition's slots (ps->slot), the per-point
+// arrays also hold the ghost slots (of which the kernels read only the
+// limiter's eps^2, the rest is state), and the wall list holds the
+// partition's own shape points.  Every per-point and per-edge value is the
+// one the whole cloud's geometry has, so a partitioned solve repeats the
+// single-domain arithmetic point for point.
 qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int sp, bool need_fp64, bool need_mixed,
-                             DeviceArena &A, cudaStream_t stream, Geometry &G)
+                             DeviceArena &A, cudaStream_t stream, Geometry &G, const PartSpec *ps = nullptr,
+                             const Precomp *pc = nullptr)
 {
-    G.n = c->n;
+    const int NB = QLSKUM_MAX_NBHS;
+    const int n = ps ? (int)ps->local.size() : c->n;       // the kernels' points
+    const int nslot = ps ? n + (int)ps->ghost.size() : n;  // with the ghost slots
+    G.n = n;
     G.shape_points = sp;
-    const int n = c->n, NB = QLSKUM_MAX_NBHS;
     // ---- point order: class (wall, outer, interior), then Morton code
     G.iperm.resize(n);
     std::iota(G.iperm.begin(), G.iperm.end(), 0);
-    if (p->reorder) {
+    if (ps) {
+        G.iperm = ps->local;
+    } else if (p->reorder) {
         double x0 = c->x[0], x1 = c->x[0], y0 = c->y[0], y1 = c->y[0];
         for (int i = 0; i < n; i++) {
             x0 = std::min(x0, c->x[i]); x1 = std::max(x1, c->x[i]);
@@ -639,12 +669,14 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
         }
         std::stable_sort(G.iperm.begin(), G.iperm.end(), [&](int a, int b) { return key[a] < key[b]; });
     }
-    G.perm.resize(n);
+    G.perm.assign(c->n, -1);
     for (int p2 = 0; p2 < n; p2++) G.perm[G.iperm[p2]] = p2;
+    // neighbour index -> the slot the kernels address
+    const std::vector<int> &slot_of = ps ? ps->slot : G.perm;
 
-    // ---- sliced ELL
-    G.np = (n + 31) / 32 * 32;
-    G.nslices = G.np / 32;
+    // ---- sliced ELL over the kernels' points; per-point arrays also cover the ghost slots
+    G.np = (nslot + 31) / 32 * 32;
+    G.nslices = (n + 31) / 32;
     std::vector<long long> sbase(G.nslices);
     long long tot = 0;
     for (int s = 0; s < G.nslices; s++) {
@@ -676,7 +708,7 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
     std::vector<float2> e_xy32(ne, make_float2(0, 0)), e_gw32(ne, make_float2(0, 0));
     const bool unit_w = p->power == 0.0;
     std::vector<float> e_dist32(ne, 1.0f);
-    const Precomp &P = G.pc;
+    const Precomp &P = pc ? *pc : G.pc;
     for (int pp = 0; pp < n; pp++) {
         const int i = G.iperm[pp];
         flag[pp] = (int8_t)c->flag_1[i];
@@ -710,7 +742,7 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
         for (int r = 0; r < c->nbhs[i]; r++) {
             const size_t e = (size_t)(sbase[pp >> 5] + 32LL * r + (pp & 31));
             const size_t src = (size_t)i * NB + r;
-            e_nbr[e] = G.perm[c->conn[src] - 1];
+            e_nbr[e] = slot_of[c->conn[src] - 1];
             e_geo[e] = make_double4_32a(P.geo[4 * src], P.geo[4 * src + 1], P.geo[4 * src + 2], P.geo[4 * src + 3]);
             e_sn[e] = make_double2(P.sn[2 * src], P.sn[2 * src + 1]);
             e_dist[e] = P.dist[src];
@@ -738,6 +770,13 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
             }
         }
     }
+
+    // ghost slots: the owner's limiter eps^2 (read for the neighbour end of an edge)
+    if (ps)
+        for (size_t g = 0; g < ps->ghost.size(); g++) {
+            eps2[n + g] = P.eps2[ps->ghost[g]];
+            eps2_32[n + g] = (float)P.eps2[ps->ghost[g]];
+        }
 
     // ---- device
     // Host vectors must outlive the asynchronous uploads: keep them until the
@@ -787,15 +826,22 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
     dc.e_dist32 = d_edist32; dc.e_w32 = d_ew32; dc.e_w32b = d_ew32b; dc.unit_w = unit_w ? 1 : 0; dc.e_xy32 = d_exy32;
     dc.e_gw32 = d_egw32;
     dc.max_nb = 0;
-    for (int i = 0; i < n; i++) dc.max_nb = std::max(dc.max_nb, c->nbhs[i]);
+    for (int pp = 0; pp < n; pp++) dc.max_nb = std::max(dc.max_nb, c->nbhs[G.iperm[pp]]);
 
-    G.d_wall_perm = A.alloc<int>(std::max(sp, 1));
-    G.d_wall_geo = A.alloc<double4_32a>(std::max(sp, 1));
+    // compute_force_coeffs_mod.h:37-59 geometry of the first shape_points
+    // points (of a partition: those it owns)
+    std::vector<int> wall;
+    for (int m = 0; m < sp; m++)
+        if (G.perm[m] >= 0) wall.push_back(m);
+    const int nw = (int)wall.size();
+    G.shape_points = nw;
+    G.d_wall_perm = A.alloc<int>(std::max(nw, 1));
+    G.d_wall_geo = A.alloc<double4_32a>(std::max(nw, 1));
     if (A.err != cudaSuccess) return fail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(A.err)));
-    // compute_force_coeffs_mod.h:37-59 geometry of the first shape_points points
-    std::vector<int> wperm(std::max(sp, 1), 0);
-    std::vector<double4_32a> wgeo(std::max(sp, 1), make_double4_32a(0, 0, 0, 0));
-    for (int m = 0; m < sp; m++) {
+    std::vector<int> wperm(std::max(nw, 1), 0);
+    std::vector<double4_32a> wgeo(std::max(nw, 1), make_double4_32a(0, 0, 0, 0));
+    for (int t = 0; t < nw; t++) {
+        const int m = wall[t];
         int r = c->right[m] - 1, l = c->left[m] - 1;
         double lx = c->x[l], ly = c->y[l], mx = c->x[m], my = c->y[m], rx = c->x[r], ry = c->y[r];
         double ds1 = std::pow((mx - lx), 2) + std::pow((my - ly), 2);
@@ -803,8 +849,8 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
         double ds2 = std::pow((rx - mx), 2) + std::pow((ry - my), 2);
         ds2 = std::sqrt(ds2);
         double ds = 0.5 * (ds1 + ds2);
-        wperm[m] = G.perm[m];
-        wgeo[m] = make_double4_32a(ds, mx - 0.25, my, 0.0);
+        wperm[t] = G.perm[m];
+        wgeo[t] = make_double4_32a(ds, mx - 0.25, my, 0.0);
     }
     up(G.d_wall_perm, wperm);
     up(G.d_wall_geo, wgeo);
@@ -1787,6 +1833,684 @@ qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_ti
 
 }  // extern "C"
 
+
+// ============================================================ partitions (halo exchange)
+//
+// The reference's distributed layout (data_structure_mod.h:4-8: local_points,
+// ghost_points and pghost, the global numbers of the ghost points;
+// point_preprocessing_mod.h:124-132 reads them per partition): the cloud is
+// cut into partitions, each holds the points it owns followed by copies of
+// the points its own points read (the ghosts), and the ghosts are refreshed
+// from their owners whenever the owners' values change.  Here the partitions
+// share one GPU, each with its own stream, geometry and state.  An exchange
+// is an event barrier between the partitions that share ghosts followed by
+// one gather launch per (partition, owner) pair and field that reads the
+// owner's array (across GPUs the same lists become peer reads or NCCL send /
+// receive pairs).  The residual norm and the objectives are sums over the
+// partitions: the all-reduce of a distributed run.
+
+struct PartPull {
+    int owner = 0;           // the partition owning these ghosts
+    int first = 0, count = 0;  // ghost range [first, first + count) of the receiving partition
+    int *d_src = nullptr;    // their positions in the owner [count]
+};
+
+struct PartDev {
+    PartSpec spec;
+    Geometry G;
+    DeviceArena A;
+    Launch L;
+    State64 s64;
+    State32 s32;
+    cudaEvent_t ev = nullptr;
+    std::vector<PartPull> pulls;
+    std::vector<int> peers;            // partitions it pulls from or that pull from it
+    int red_off = 0, red_blocks = 0;   // its residual partials in the shared arrays
+    double *d_obj = nullptr, *d_obj_partial = nullptr, *d_entropy = nullptr;
+};
+
+struct qlskum_partition {
+    qlskum_params prm{};
+    int n = 0, nparts = 0;
+    CaseConst K{};
+    std::vector<PartDev *> parts;
+    std::vector<int> part_of, pos_of;  // global point -> partition, position in it
+    DeviceArena A;                     // the shared residual arrays
+    cudaStream_t host_stream = nullptr;
+    Reduce R;
+    int pcur = 0;
+    bool derived_valid = false;
+    int it = 0;
+    int flux_variant = 5;              // mixed: the fused kernel's launch shape
+    int point_block = 128, staged = 0; // mixed: gradient / inner-loop launch shape
+    long long launches = 0;
+    long long halo_bytes = 0;          // bytes the exchanges of one iteration move
+    std::string err;
+};
+
+namespace {
+
+qlskum_status pfail(qlskum_partition *P, qlskum_status s, const std::string &msg)
+{
+    if (P) P->err = msg;
+    else g_create_error = msg;
+    return s;
+}
+
+#define PCK(P, call)                                                                          \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) return pfail(P, QLSKUM_ERR_CUDA, fmt("%s: %s", #call, cudaGetErrorString(e_))); \
+    } while (0)
+
+// Partition plan: the points sorted by the Morton code of their coordinates
+// and cut into n_parts contiguous ranges of (nearly) equal size, so each
+// partition is a compact region and its ghost layer a thin band; inside a
+// partition its points run in the single-domain device order (class, then
+// Morton code); each partition's ghosts are the points outside it that its
+// own points have as neighbours, grouped by owner and in the owner's order.
+void plan_partitions(const qlskum_cloud *c, int nparts, std::vector<int> &part_of, std::vector<int> &pos_of,
+                     std::vector<PartSpec> &specs)
+{
+    const int n = c->n, NB = QLSKUM_MAX_NBHS;
+    double x0 = c->x[0], x1 = c->x[0], y0 = c->y[0], y1 = c->y[0];
+    for (int i = 0; i < n; i++) {
+        x0 = std::min(x0, c->x[i]); x1 = std::max(x1, c->x[i]);
+        y0 = std::min(y0, c->y[i]); y1 = std::max(y1, c->y[i]);
+    }
+    const double span = std::max(x1 - x0, y1 - y0) + 1e-300;
+    std::vector<uint64_t> key(n);
+    for (int i = 0; i < n; i++) {
+        uint32_t qx = (uint32_t)std::min(2097151.0, std::floor((c->x[i] - x0) / span * 2097151.0));
+        uint32_t qy = (uint32_t)std::min(2097151.0, std::floor((c->y[i] - y0) / span * 2097151.0));
+        key[i] = morton2(qx, qy);
+    }
+    std::vector<int> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+    part_of.assign(n, 0);
+    for (int r = 0; r < n; r++) part_of[order[r]] = (int)((long long)r * nparts / n);
+    specs.assign(nparts, PartSpec());
+    static const int rank[3] = {0, 2, 1};
+    for (int i : order) specs[part_of[i]].local.push_back(i);
+    pos_of.assign(n, 0);
+    for (auto &sp : specs) {
+        std::stable_sort(sp.local.begin(), sp.local.end(), [&](int a, int b) {
+            const int ra = rank[c->flag_1[a]], rb = rank[c->flag_1[b]];
+            return ra != rb ? ra < rb : key[a] < key[b];
+        });
+        for (size_t t = 0; t < sp.local.size(); t++) pos_of[sp.local[t]] = (int)t;
+    }
+    for (int p = 0; p < nparts; p++) {
+        PartSpec &sp = specs[p];
+        std::vector<int> g;
+        for (int i : sp.local)
+            for (int r = 0; r < c->nbhs[i]; r++) {
+                const int k = c->conn[(size_t)i * NB + r] - 1;
+                if (part_of[k] != p) g.push_back(k);
+            }
+        std::sort(g.begin(), g.end(), [&](int a, int b) {
+            return part_of[a] != part_of[b] ? part_of[a] < part_of[b] : pos_of[a] < pos_of[b];
+        });
+        g.erase(std::unique(g.begin(), g.end()), g.end());
+        sp.ghost = std::move(g);
+        sp.slot.assign(n, -1);
+        for (size_t t = 0; t < sp.local.size(); t++) sp.slot[sp.local[t]] = (int)t;
+        for (size_t t = 0; t < sp.ghost.size(); t++) sp.slot[sp.ghost[t]] = (int)(sp.local.size() + t);
+    }
+}
+
+struct FieldRef {
+    void *base;
+    int bytes;   // per point
+};
+
+// One exchange: every partition waits for the partitions it shares ghosts
+// with to reach this point, then pulls the `nf` fields field(d, j) of its
+// ghosts from their owners.
+template <typename F> void part_exchange(qlskum_partition *P, int nf, F &&field)
+{
+    for (PartDev *d : P->parts) cudaEventRecord(d->ev, d->L.stream);
+    for (PartDev *d : P->parts)
+        for (int o : d->peers) cudaStreamWaitEvent(d->L.stream, P->parts[o]->ev, 0);
+    for (PartDev *d : P->parts)
+        for (const PartPull &pl : d->pulls)
+            for (int j = 0; j < nf; j++) {
+                const FieldRef src = field(*P->parts[pl.owner], j), dst = field(*d, j);
+                halo::pull(d->L, pl.count, pl.d_src, src.base,
+                           static_cast<char *>(dst.base) + (size_t)(d->G.n + pl.first) * dst.bytes, dst.bytes);
+            }
+}
+
+// Every partition's stream waits for partition `from`'s stream.
+void part_join(qlskum_partition *P, int from)
+{
+    PartDev *s = P->parts[from];
+    cudaEventRecord(s->ev, s->L.stream);
+    for (PartDev *d : P->parts)
+        if (d != s) cudaStreamWaitEvent(d->L.stream, s->ev, 0);
+}
+
+// Partition 0's stream waits for every other partition's.
+void part_gather(qlskum_partition *P)
+{
+    PartDev *z = P->parts[0];
+    for (PartDev *d : P->parts)
+        if (d != z) {
+            cudaEventRecord(d->ev, d->L.stream);
+            cudaStreamWaitEvent(z->L.stream, d->ev, 0);
+        }
+}
+
+// The residual partials of each partition's fused kernel, packed back to back.
+void part_reduce_layout(qlskum_partition *P)
+{
+    const bool mx = P->prm.precision == QLSKUM_MIXED;
+    const int fb = mx ? mixed::flux_block(P->flux_variant) : 128;
+    int off = 0;
+    for (PartDev *d : P->parts) {
+        d->red_off = off;
+        d->red_blocks = (d->G.n + fb - 1) / fb;
+        off += d->red_blocks;
+    }
+    P->R.blocks = off;
+}
+
+// One iteration over all partitions (the fused path of enqueue_iteration,
+// stage by stage, with the ghosts refreshed before every kernel that reads
+// a neighbour's value: q and, in the first stage, the wave speed before the
+// gradient; dq and qm after it; dq after each inner step).
+void part_iteration(qlskum_partition *P, int o)
+{
+    const int x = (o + 1) % 3, y = (o + 2) % 3;
+    const int dst[4] = {x, y, x, y}, src[4] = {o, x, y, x};
+    const int ni = P->prm.inner_iterations;
+    const bool mx = P->prm.precision == QLSKUM_MIXED;
+    const float cfl32 = (float)P->K.cfl;
+    for (int rk = 1; rk <= 4; rk++) {
+        const int qa = (rk - 1) & 1, qb = rk & 1;
+        if (mx)
+            part_exchange(P, rk == 1 ? 2 : 1, [&](PartDev &d, int j) {
+                return j == 0 ? FieldRef{d.s32.q[qa], 16} : FieldRef{d.s32.cspeed, 4};
+            });
+        else
+            part_exchange(P, rk == 1 ? 2 : 1, [&](PartDev &d, int j) {
+                return j == 0 ? FieldRef{d.s64.q[qa], 32} : FieldRef{d.s64.cspeed, 8};
+            });
+        for (PartDev *d : P->parts) {
+            if (mx)
+                mixed::q_derivatives(d->L, d->G.dc, d->s32.q[qa], d->s32.dq[0], d->s32.qm, d->s32.cspeed,
+                                     rk == 1 ? d->s32.delta : nullptr, cfl32);
+            else
+                fp64::q_derivatives(d->L, d->G.dc, d->s64.q[qa], d->s64.dq[0], d->s64.qm, d->s64.cspeed,
+                                    rk == 1 ? d->s64.delta : nullptr, P->K.cfl);
+        }
+        if (mx)
+            part_exchange(P, 2, [&](PartDev &d, int j) {
+                return j == 0 ? FieldRef{d.s32.dq[0], 32} : FieldRef{d.s32.qm, 32};
+            });
+        else
+            part_exchange(P, 2, [&](PartDev &d, int j) {
+                return j == 0 ? FieldRef{d.s64.dq[0], 64} : FieldRef{d.s64.qm, 64};
+            });
+        for (int j = 0; j < ni; j++) {
+            for (PartDev *d : P->parts) {
+                if (mx)
+                    mixed::q_inner(d->L, d->G.dc, d->s32.dq[0], d->s32.dq[mixed_dq_in(j)],
+                                   d->s32.dq[mixed_dq_out(j)]);
+                else
+                    fp64::q_inner(d->L, d->G.dc, d->s64.q[qa], d->s64.dq[j & 1], d->s64.dq[(j + 1) & 1]);
+            }
+            if (mx)
+                part_exchange(P, 1, [&](PartDev &d, int) { return FieldRef{d.s32.dq[mixed_dq_out(j)], 32}; });
+            else
+                part_exchange(P, 1, [&](PartDev &d, int) { return FieldRef{d.s64.dq[(j + 1) & 1], 64}; });
+        }
+        for (PartDev *d : P->parts) {
+            // only the last stage's residual is reported (fpi_solver_mod.h:138)
+            Reduce Rk = P->R;
+            if (rk == 4) {
+                Rk.partial_sum += d->red_off;
+                Rk.partial_max += d->red_off;
+            } else {
+                Rk.partial_sum = Rk.partial_max = nullptr;
+            }
+            double4_32a *const *prim = d->s64.prim;
+            if (mx)
+                mixed::flux_update(d->L, d->G.dc, P->K, d->s32.q[qa], d->s32.dq[mixed_dq_final(ni)], d->s32.qm,
+                                   d->s32.delta, prim[src[rk - 1]], prim[o], prim[dst[rk - 1]], d->s32.q[qb],
+                                   rk == 4 ? d->s32.cspeed : nullptr, rk, Rk, P->flux_variant);
+            else
+                fp64::flux_update(d->L, d->G.dc, P->K, d->s64.q[qa], d->s64.dq[ni & 1], d->s64.qm, d->s64.delta,
+                                  prim[src[rk - 1]], prim[o], prim[dst[rk - 1]], d->s64.q[qb],
+                                  rk == 4 ? d->s64.cspeed : nullptr, rk, Rk);
+        }
+    }
+    // the residual norm over all partitions (fpi_solver_mod.h:138-150)
+    part_gather(P);
+    fp64::reduce_residual(P->parts[0]->L, P->R, P->n, 0);
+    part_join(P, 0);
+}
+
+// Bytes the ghost exchanges of one iteration move.
+long long part_halo_bytes(const qlskum_partition *P)
+{
+    long long g = 0;
+    for (const PartDev *d : P->parts) g += (long long)d->spec.ghost.size();
+    const bool mx = P->prm.precision == QLSKUM_MIXED;
+    const int ni = P->prm.inner_iterations;
+    // per stage: q (+ the wave speed in stage 1), dq0 + qm, ni x dq
+    const long long q = mx ? 16 : 32, dq = mx ? 32 : 64, cs = mx ? 4 : 8;
+    return g * (4 * (q + 2 * dq + ni * dq) + cs);
+}
+
+qlskum_status part_derived(qlskum_partition *P)
+{
+    if (P->derived_valid) return QLSKUM_OK;
+    for (PartDev *d : P->parts) {
+        // over the ghost slots too: their state was written with the owners'
+        DevCloud all = d->G.dc;
+        all.n = d->G.n + (int)d->spec.ghost.size();
+        if (P->prm.precision == QLSKUM_MIXED)
+            mixed::derived(d->L, all, d->s64.prim[P->pcur], d->s32.q[0], d->s32.cspeed);
+        else
+            fp64::derived(d->L, all, d->s64.prim[P->pcur], d->s64.q[0], d->s64.cspeed);
+    }
+    P->derived_valid = true;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pfail(P, QLSKUM_ERR_CUDA, fmt("derived: %s", cudaGetErrorString(e)));
+    return QLSKUM_OK;
+}
+
+qlskum_status part_sync(qlskum_partition *P)
+{
+    for (PartDev *d : P->parts) PCK(P, cudaStreamSynchronize(d->L.stream));
+    return QLSKUM_OK;
+}
+
+qlskum_status part_ensure_hist(qlskum_partition *P, int needed)
+{
+    if (needed <= P->R.capacity) return QLSKUM_OK;
+    int cap = std::max(1024, P->R.capacity);
+    while (cap < needed) cap *= 2;
+    qlskum_status st = part_sync(P);
+    if (st) return st;
+    double *nh = nullptr;
+    PCK(P, cudaMalloc(&nh, sizeof(double) * 3 * (size_t)cap));
+    PCK(P, cudaMemset(nh, 0, sizeof(double) * 3 * (size_t)cap));
+    if (P->R.hist) {
+        PCK(P, cudaMemcpy(nh, P->R.hist, sizeof(double) * 3 * (size_t)P->R.capacity, cudaMemcpyDeviceToDevice));
+        cudaFree(P->R.hist);
+    }
+    // the copies above run on the legacy stream, unordered with the partitions' streams
+    PCK(P, cudaDeviceSynchronize());
+    P->R.hist = nh;
+    P->R.capacity = cap;
+    return QLSKUM_OK;
+}
+
+void part_free(qlskum_partition *P)
+{
+    if (!P) return;
+    for (PartDev *d : P->parts) {
+        if (d->L.stream) cudaStreamSynchronize(d->L.stream);
+        d->A.release();
+        if (d->ev) cudaEventDestroy(d->ev);
+        if (d->L.stream) cudaStreamDestroy(d->L.stream);
+        delete d;
+    }
+    P->parts.clear();
+    if (P->R.hist) cudaFree(P->R.hist);
+    P->R.hist = nullptr;
+    P->A.release();
+    delete P;
+}
+
+}  // namespace
+
+extern "C" {
+
+qlskum_status qlskum_partition_plan(const qlskum_cloud *c, int n_parts, int *part_of, int *n_local, int *n_ghost)
+{
+    qlskum_params p;
+    qlskum_default_params(&p);
+    int sp = 0;
+    qlskum_status st = validate(c, &p, &sp);
+    if (st) return st;
+    if (n_parts < 1 || n_parts > c->n) return fail(nullptr, QLSKUM_ERR_INVALID, "n_parts must be in 1..n");
+    std::vector<int> po, pos;
+    std::vector<PartSpec> specs;
+    plan_partitions(c, n_parts, po, pos, specs);
+    if (part_of) std::copy(po.begin(), po.end(), part_of);
+    for (int q = 0; q < n_parts; q++) {
+        if (n_local) n_local[q] = (int)specs[q].local.size();
+        if (n_ghost) n_ghost[q] = (int)specs[q].ghost.size();
+    }
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_partition_plan_lists(const qlskum_cloud *c, int n_parts, int part, int *local_ids,
+                                          int *ghost_ids)
+{
+    qlskum_params p;
+    qlskum_default_params(&p);
+    int sp = 0;
+    qlskum_status st = validate(c, &p, &sp);
+    if (st) return st;
+    if (n_parts < 1 || n_parts > c->n || part < 0 || part >= n_parts)
+        return fail(nullptr, QLSKUM_ERR_INVALID, "n_parts must be in 1..n and part in 0..n_parts-1");
+    std::vector<int> po, pos;
+    std::vector<PartSpec> specs;
+    plan_partitions(c, n_parts, po, pos, specs);
+    if (local_ids)
+        for (size_t t = 0; t < specs[part].local.size(); t++) local_ids[t] = specs[part].local[t] + 1;
+    if (ghost_ids)
+        for (size_t t = 0; t < specs[part].ghost.size(); t++) ghost_ids[t] = specs[part].ghost[t] + 1;
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_partition_create(const qlskum_cloud *c, const qlskum_params *p, int n_parts,
+                                      qlskum_partition **out)
+{
+    if (!out) return fail(nullptr, QLSKUM_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    int sp = 0;
+    qlskum_status st = validate(c, p, &sp);
+    if (st) return st;
+    if (n_parts < 1 || n_parts > c->n) return fail(nullptr, QLSKUM_ERR_INVALID, "n_parts must be in 1..n");
+    Precomp pc;
+    st = precompute(c, p, pc);
+    if (st) return st;
+    qlskum_partition *P = new qlskum_partition();
+    P->prm = *p;
+    P->n = c->n;
+    P->nparts = n_parts;
+    P->K = case_of(*p);
+    if (p->block_size) P->point_block = p->block_size;
+    std::vector<PartSpec> specs;
+    plan_partitions(c, n_parts, P->part_of, P->pos_of, specs);
+    for (int q = 0; q < n_parts; q++)
+        if (specs[q].local.empty()) {
+            part_free(P);
+            return fail(nullptr, QLSKUM_ERR_INVALID, fmt("partition %d has no points", q));
+        }
+    const bool mx = p->precision == QLSKUM_MIXED;
+    const std::vector<double4_32a> free_stream(1, make_double4_32a(P->K.rho_inf, P->K.u1_inf, P->K.u2_inf,
+                                                                  P->K.pr_inf));
+    for (int q = 0; q < n_parts; q++) {
+        PartDev *d = new PartDev();
+        P->parts.push_back(d);
+        d->spec = std::move(specs[q]);
+        cudaError_t ce = cudaStreamCreateWithFlags(&d->L.stream, cudaStreamNonBlocking);
+        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&d->ev, cudaEventDisableTiming);
+        if (ce != cudaSuccess) {
+            part_free(P);
+            return fail(nullptr, QLSKUM_ERR_CUDA, fmt("stream / event: %s", cudaGetErrorString(ce)));
+        }
+        d->L.block = P->point_block;
+        d->L.staged = P->staged;
+        d->L.launches = &P->launches;
+        st = build_geometry(c, p, sp, true, mx, d->A, d->L.stream, d->G, &d->spec, &pc);
+        if (st) {
+            part_free(P);
+            return st;
+        }
+        DeviceArena &A = d->A;
+        const size_t np = d->G.np;
+        for (int b = 0; b < 3; b++) d->s64.prim[b] = A.alloc<double4_32a>(np);
+        for (int b = 0; b < 2; b++) {
+            d->s64.q[b] = A.alloc<double4_32a>(np);
+            d->s64.dq[b] = A.alloc<double4_32a>(np * 2);
+        }
+        d->s64.qm = A.alloc<double4_32a>(np * 2);
+        d->s64.flux_res = A.alloc<double4_32a>(np);
+        d->s64.delta = A.alloc<double>(np);
+        d->s64.cspeed = A.alloc<double>(np);
+        if (mx) {
+            for (int b = 0; b < 2; b++) d->s32.q[b] = A.alloc<float4>(np);
+            for (int b = 0; b < 3; b++) d->s32.dq[b] = A.alloc<float4>(np * 2);
+            d->s32.qm = A.alloc<float4>(np * 2);
+            d->s32.delta = A.alloc<float>(np);
+            d->s32.cspeed = A.alloc<float>(np);
+        }
+        const int nl = d->G.n;
+        d->d_obj = A.alloc<double>(8);
+        d->d_obj_partial = A.alloc<double>(4 * (size_t)((std::max(nl, d->G.shape_points) + 255) / 256));
+        d->d_entropy = A.alloc<double>(np);
+        if (A.err != cudaSuccess) {
+            part_free(P);
+            return fail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(A.err)));
+        }
+        // initial_conditions_mod.h:23-37 on every slot (ghosts included)
+        std::vector<double4_32a> prim0(np, free_stream[0]);
+        for (int b = 0; b < 3; b++)
+            cudaMemcpyAsync(d->s64.prim[b], prim0.data(), np * sizeof(double4_32a), cudaMemcpyHostToDevice,
+                            d->L.stream);
+        cudaMemsetAsync(d->s64.dq[0], 0, sizeof(double4_32a) * 2 * np, d->L.stream);
+        cudaMemsetAsync(d->s64.dq[1], 0, sizeof(double4_32a) * 2 * np, d->L.stream);
+        cudaMemsetAsync(d->s64.qm, 0, sizeof(double4_32a) * 2 * np, d->L.stream);
+        ce = cudaStreamSynchronize(d->L.stream);
+        if (ce != cudaSuccess) {
+            part_free(P);
+            return fail(nullptr, QLSKUM_ERR_CUDA, fmt("upload: %s", cudaGetErrorString(ce)));
+        }
+    }
+    // the pull lists (one per owner, ghosts grouped by owner) and the peers
+    std::vector<std::vector<char>> peer(n_parts, std::vector<char>(n_parts, 0));
+    for (int q = 0; q < n_parts; q++) {
+        PartDev *d = P->parts[q];
+        const std::vector<int> &g = d->spec.ghost;
+        size_t a = 0;
+        while (a < g.size()) {
+            const int o = P->part_of[g[a]];
+            size_t b = a;
+            std::vector<int> src;
+            while (b < g.size() && P->part_of[g[b]] == o) src.push_back(P->pos_of[g[b++]]);
+            PartPull pl;
+            pl.owner = o;
+            pl.first = (int)a;
+            pl.count = (int)(b - a);
+            pl.d_src = d->A.alloc<int>(src.size());
+            if (d->A.err != cudaSuccess) {
+                part_free(P);
+                return fail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(d->A.err)));
+            }
+            cudaMemcpy(pl.d_src, src.data(), src.size() * sizeof(int), cudaMemcpyHostToDevice);
+            d->pulls.push_back(pl);
+            peer[q][o] = peer[o][q] = 1;
+            a = b;
+        }
+    }
+    for (int q = 0; q < n_parts; q++)
+        for (int o = 0; o < n_parts; o++)
+            if (peer[q][o] && o != q) P->parts[q]->peers.push_back(o);
+    // the shared residual arrays: a partial per 32 points of each partition is enough for any launch shape
+    int maxp = 0;
+    for (PartDev *d : P->parts) maxp += (d->G.n + 31) / 32;
+    P->R.max_blocks = maxp;
+    P->R.partial_sum = P->A.alloc<double>(maxp);
+    P->R.partial_max = P->A.alloc<double>(maxp);
+    P->R.res_old = P->A.alloc<double>(1);
+    P->R.iter = P->A.alloc<int>(1);
+    P->R.status = P->A.alloc<int>(1);
+    if (P->A.err != cudaSuccess) {
+        part_free(P);
+        return fail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(P->A.err)));
+    }
+    cudaMemset(P->R.res_old, 0, sizeof(double));
+    cudaMemset(P->R.iter, 0, sizeof(int));
+    cudaMemset(P->R.status, 0, sizeof(int));
+    part_reduce_layout(P);
+    P->halo_bytes = part_halo_bytes(P);
+    st = part_ensure_hist(P, 1024);
+    if (st) {
+        const std::string m = P->err;
+        part_free(P);
+        return fail(nullptr, st, m);
+    }
+    cudaError_t ce = cudaDeviceSynchronize();
+    if (ce != cudaSuccess) {
+        part_free(P);
+        return fail(nullptr, QLSKUM_ERR_CUDA, fmt("partition set-up: %s", cudaGetErrorString(ce)));
+    }
+    *out = P;
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_partition_destroy(qlskum_partition *P)
+{
+    part_free(P);
+    return QLSKUM_OK;
+}
+
+const char *qlskum_partition_last_error(const qlskum_partition *P)
+{
+    return P ? P->err.c_str() : g_create_error.c_str();
+}
+
+qlskum_status qlskum_partition_layout(const qlskum_partition *P, int part, int *n_local, int *n_ghost, int *local_ids,
+                                      int *ghost_ids)
+{
+    if (!P || part < 0 || part >= P->nparts) return QLSKUM_ERR_INVALID;
+    const PartSpec &sp = P->parts[part]->spec;
+    if (n_local) *n_local = (int)sp.local.size();
+    if (n_ghost) *n_ghost = (int)sp.ghost.size();
+    if (local_ids)
+        for (size_t t = 0; t < sp.local.size(); t++) local_ids[t] = sp.local[t] + 1;
+    if (ghost_ids)
+        for (size_t t = 0; t < sp.ghost.size(); t++) ghost_ids[t] = sp.ghost[t] + 1;
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_partition_set_launch_config(qlskum_partition *P, int flux_variant, int point_block, int staged)
+{
+    if (!P) return QLSKUM_ERR_INVALID;
+    if (flux_variant < 0 || flux_variant >= mixed::flux_variants())
+        return pfail(P, QLSKUM_ERR_INVALID, "flux_variant out of range");
+    if (point_block != 64 && point_block != 128 && point_block != 256 && point_block != 512)
+        return pfail(P, QLSKUM_ERR_INVALID, "point_block must be 64, 128, 256 or 512");
+    if (staged < 0 || staged > 4) return pfail(P, QLSKUM_ERR_INVALID, "staged must be in 0..4");
+    if (staged > 0 && P->prm.precision == QLSKUM_MIXED)
+        for (PartDev *d : P->parts)
+            if (mixed::staged_variants(d->G.dc) < staged)
+                return pfail(P, QLSKUM_ERR_UNSUPPORTED, "staged variant does not fit this cloud");
+    qlskum_status st = part_sync(P);
+    if (st) return st;
+    P->flux_variant = flux_variant;
+    P->point_block = point_block;
+    P->staged = staged;
+    for (PartDev *d : P->parts) {
+        d->L.block = point_block;
+        d->L.staged = staged;
+    }
+    part_reduce_layout(P);
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_partition_q_lskum(qlskum_partition *P, int iters)
+{
+    if (!P) return fail(nullptr, QLSKUM_ERR_INVALID, "null partition");
+    if (iters < 0) return pfail(P, QLSKUM_ERR_INVALID, "iters < 0");
+    qlskum_status st = part_ensure_hist(P, P->it + iters);
+    if (st) return st;
+    st = part_derived(P);
+    if (st) return st;
+    // the device iteration counter continues from the host's
+    PartDev *z = P->parts[0];
+    PCK(P, cudaMemcpyAsync(P->R.iter, &P->it, sizeof(int), cudaMemcpyHostToDevice, z->L.stream));
+    PCK(P, cudaStreamSynchronize(z->L.stream));
+    for (int t = 0; t < iters; t++) {
+        const int o = P->pcur;
+        part_iteration(P, o);
+        P->pcur = (o + 2) % 3;
+        P->it += 1;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pfail(P, QLSKUM_ERR_CUDA, fmt("partition iteration: %s", cudaGetErrorString(e)));
+    st = part_sync(P);
+    if (st) return st;
+    int bad = 0;
+    PCK(P, cudaMemcpy(&bad, P->R.status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (bad) return pfail(P, QLSKUM_ERR_NONFINITE, "residual became non-finite (NaN/Inf in the state)");
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_partition_get_prim(qlskum_partition *P, double *out)
+{
+    if (!P || !out) return QLSKUM_ERR_INVALID;
+    qlskum_status st = part_sync(P);
+    if (st) return st;
+    for (PartDev *d : P->parts) {
+        const int nl = d->G.n;
+        std::vector<double4_32a> h(nl);
+        PCK(P, cudaMemcpy(h.data(), d->s64.prim[P->pcur], nl * sizeof(double4_32a), cudaMemcpyDeviceToHost));
+        for (int t = 0; t < nl; t++) {
+            double *o4 = out + 4 * (size_t)d->spec.local[t];
+            o4[0] = h[t].x; o4[1] = h[t].y; o4[2] = h[t].z; o4[3] = h[t].w;
+        }
+    }
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_partition_set_prim(qlskum_partition *P, const double *prim)
+{
+    if (!P || !prim) return QLSKUM_ERR_INVALID;
+    qlskum_status st = part_sync(P);
+    if (st) return st;
+    for (PartDev *d : P->parts) {
+        const size_t ns = d->spec.local.size() + d->spec.ghost.size();
+        std::vector<double4_32a> h(ns);
+        for (size_t t = 0; t < ns; t++) {
+            const int g = t < d->spec.local.size() ? d->spec.local[t] : d->spec.ghost[t - d->spec.local.size()];
+            const double *p4 = prim + 4 * (size_t)g;
+            h[t] = make_double4_32a(p4[0], p4[1], p4[2], p4[3]);
+        }
+        PCK(P, cudaMemcpy(d->s64.prim[P->pcur], h.data(), ns * sizeof(double4_32a), cudaMemcpyHostToDevice));
+    }
+    P->derived_valid = false;
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_partition_residual_history(qlskum_partition *P, double *out, int max_rows, int *rows)
+{
+    if (!P) return QLSKUM_ERR_INVALID;
+    qlskum_status st = part_sync(P);
+    if (st) return st;
+    const int k = std::min(P->it, std::max(0, max_rows));
+    if (rows) *rows = P->it;
+    if (out && k > 0) PCK(P, cudaMemcpy(out, P->R.hist, sizeof(double) * 3 * (size_t)k, cudaMemcpyDeviceToHost));
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_partition_objective(qlskum_partition *P, double *cl, double *cd, double *cm,
+                                         double *total_entropy)
+{
+    if (!P) return QLSKUM_ERR_INVALID;
+    const double cp_scale = 0.5 * P->K.rho_inf * P->K.mach * P->K.mach;
+    double sum[4] = {0, 0, 0, 0};
+    for (PartDev *d : P->parts)
+        fp64::objective(d->L, d->G.dc, d->s64.prim[P->pcur], d->G.d_wall_perm, d->G.d_wall_geo, d->G.shape_points,
+                        cp_scale, P->K.pr_inf, P->K.gamma, d->d_entropy, d->d_obj, d->d_obj_partial);
+    // the all-reduce: the partitions' sums added in partition order
+    for (PartDev *d : P->parts) {
+        double o[4];
+        PCK(P, cudaMemcpyAsync(o, d->d_obj, sizeof o, cudaMemcpyDeviceToHost, d->L.stream));
+        PCK(P, cudaStreamSynchronize(d->L.stream));
+        for (int j = 0; j < 4; j++) sum[j] += o[j];
+    }
+    const double H = sum[0], V = sum[1];
+    if (cl) *cl = V * std::cos(P->K.theta) - H * std::sin(P->K.theta);
+    if (cd) *cd = H * std::cos(P->K.theta) + V * std::sin(P->K.theta);
+    if (cm) *cm = sum[2];
+    if (total_entropy) *total_entropy = sum[3];
+    return QLSKUM_OK;
+}
+
+long long qlskum_partition_halo_bytes(const qlskum_partition *P) { return P ? P->halo_bytes : 0; }
+
+long long qlskum_partition_launch_count(const qlskum_partition *P) { return P ? P->launches : 0; }
+
+}  // extern "C"
 
 // ============================================================ diagnostics and files
 

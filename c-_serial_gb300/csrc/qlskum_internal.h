@@ -164,6 +164,9 @@ struct Launch {
     // v > 0 = staged variant v (edge list in shared memory, neighbour data
     // streamed with cp.async a few edges ahead); picked by the autotuner
     int staged = 0;
+    // mixed gradient / inner-loop kernels of the per-edge gather form: lanes
+    // per point (1, 2 or 4: a point's edges split over that many lanes)
+    int lanes = 1;
 };
 
 // ---------------------------------------------------------- adjoint (qlskum_adjoint.cu)
@@ -296,6 +299,14 @@ void objective(const Launch &L, const DevCloud &c, const double4_32a *prim, cons
                int n_wall, double cp_scale, double pr_inf, double gamma, double *entropy, double *out4, double *scratch);
 }  // namespace fp64
 
+// ---------------------------------------------------------- halo exchange (qlskum_fp64.cu)
+namespace halo {
+// Ghost slots of a partition from their owner's arrays: dst[g] = src[idx[g]]
+// for g < n, elements of `bytes` bytes (4, 8 or a multiple of 16; src, dst
+// aligned to the element, 16 bytes for the multiples of 16).
+void pull(const Launch &L, int n, const int *idx, const void *src, void *dst, int bytes);
+}  // namespace halo
+
 // ---------------------------------------------------------- mixed kernels (qlskum_mixed.cu)
 namespace mixed {
 void derived(const Launch &L, const DevCloud &c, const double4_32a *prim, float4 *q, float *cspeed);
@@ -314,14 +325,23 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
                  double4_32a *prim_next, float4 *q_next, float *cspeed_next, int rk, const Reduce &R, int variant,
                  float4 *acc_out = nullptr);  // acc_out: the point's flux accumulator (F / delta) when non-null
 int flux_variants();
-int flux_block(int variant);
+int flux_block(int variant);        // threads per block
 int flux_min_blocks(int variant);
-// batched (persistent) forms
+int flux_lanes(int variant);        // lanes per point
+// blocks (residual partials) of one launch of `variant` over n points
+int flux_grid_blocks(int variant, int n);
+// batched (persistent) forms; tile = points per tile, L.lanes lanes per point
 void batch_derived(const Launch &L, const BatchView &B, int tile, const double4_32a *prim, float4 *q, float *cs);
 void batch_q_derivatives(const Launch &L, const BatchView &B, int tile, const float4 *q, float4 *dq, float4 *qm,
                          const float *cs, float *delta, float cfl);
 void batch_q_inner(const Launch &L, const BatchView &B, int tile, const float4 *dq0, const float4 *dq_in,
                    float4 *dq_out);
+// batched flux variants: 0..3 one lane per point (points per tile x min blocks
+// 128x4, 128x5, 64x8, 256x2), 4: 64-point tiles with 2 lanes per point, 5: with 4
+int batch_flux_variants();
+int batch_flux_tile(int variant);   // points per tile
+int batch_flux_min_blocks(int variant);
+int batch_flux_lanes(int variant);
 void batch_flux_update(const Launch &L, const BatchView &B, int variant, const float4 *q, const float4 *dq,
                        const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
                        double4_32a *prim_next, float4 *q_next, float *cs_next, int rk, double *psum, double *pmax);

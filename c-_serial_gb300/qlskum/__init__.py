@@ -129,6 +129,20 @@ def load(build_if_needed: bool = True):
         "qlskum_partgrid_write": (i, [C.c_char_p, C.POINTER(CloudStruct)]),
         "qlskum_io_last_error": (C.c_char_p, []),
         "qlskum_check_stencils": (i, [C.POINTER(CloudStruct), C.c_double, C.c_double, dp, ip]),
+        "qlskum_partition_plan": (i, [C.POINTER(CloudStruct), i, ip, ip, ip]),
+        "qlskum_partition_plan_lists": (i, [C.POINTER(CloudStruct), i, i, ip, ip]),
+        "qlskum_partition_create": (i, [C.POINTER(CloudStruct), C.POINTER(ParamsStruct), i, C.POINTER(H)]),
+        "qlskum_partition_destroy": (i, [H]),
+        "qlskum_partition_last_error": (C.c_char_p, [H]),
+        "qlskum_partition_layout": (i, [H, i, ip, ip, ip, ip]),
+        "qlskum_partition_set_launch_config": (i, [H, i, i, i]),
+        "qlskum_partition_q_lskum": (i, [H, i]),
+        "qlskum_partition_get_prim": (i, [H, dp]),
+        "qlskum_partition_set_prim": (i, [H, dp]),
+        "qlskum_partition_residual_history": (i, [H, dp, i, ip]),
+        "qlskum_partition_objective": (i, [H, dp, dp, dp, dp]),
+        "qlskum_partition_halo_bytes": (C.c_longlong, [H]),
+        "qlskum_partition_launch_count": (C.c_longlong, [H]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -503,3 +517,107 @@ class Batch:
         self._ck(self._L.qlskum_batch_tuning(self._h, *[C.byref(t) for t in v]))
         return {"tile": v[0].value, "flux_tile": v[1].value, "flux_min_blocks": v[2].value,
                 "points_per_warp": v[3].value}
+
+
+def partition_plan(cloud, n_parts):
+    """The partition plan without a GPU: (part_of [n], per partition
+    (local ids, ghost ids), 1-based global point numbers as pghost holds them)."""
+    L = load()
+    s, keep = cloud_struct(cloud)
+    part_of = np.empty(cloud.n, np.int32)
+    nl = np.empty(n_parts, np.int32)
+    ng = np.empty(n_parts, np.int32)
+    st = L.qlskum_partition_plan(C.byref(s), int(n_parts), _ip(part_of), _ip(nl), _ip(ng))
+    if st != 0:
+        raise QlskumError(st, L.qlskum_last_error(None).decode())
+    lists = []
+    for p in range(n_parts):
+        loc = np.empty(max(1, nl[p]), np.int32)
+        gh = np.empty(max(1, ng[p]), np.int32)
+        st = L.qlskum_partition_plan_lists(C.byref(s), int(n_parts), p, _ip(loc), _ip(gh))
+        if st != 0:
+            raise QlskumError(st, L.qlskum_last_error(None).decode())
+        lists.append((loc[:nl[p]].copy(), gh[:ng[p]].copy()))
+    return part_of, lists
+
+
+class Partition:
+    """The solve split into n_parts partitions with ghost points refreshed
+    from their owners before every kernel that reads them (the reference's
+    local / ghost point layout), all on the current GPU."""
+
+    def __init__(self, cloud, n_parts, mach=0.63, aoa=2.0, cfl=0.1, vl_const=150.0, power=0.0, inner_iterations=3,
+                 precision=FP64, block_size=0):
+        L = load()
+        self._L = L
+        s, self._keep = cloud_struct(cloud)
+        p = ParamsStruct(mach, aoa, cfl, vl_const, power, inner_iterations, precision, block_size, 1, 0)
+        h = C.c_void_p()
+        st = L.qlskum_partition_create(C.byref(s), C.byref(p), int(n_parts), C.byref(h))
+        if st != 0:
+            raise QlskumError(st, L.qlskum_partition_last_error(None).decode())
+        self._h = h
+        self.n = cloud.n
+        self.n_parts = n_parts
+
+    def _ck(self, st):
+        if st != 0:
+            raise QlskumError(st, self._L.qlskum_partition_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.qlskum_partition_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def layout(self, part):
+        """(local ids, ghost ids) of one partition, 1-based global point numbers."""
+        nl, ng = C.c_int(), C.c_int()
+        self._ck(self._L.qlskum_partition_layout(self._h, int(part), C.byref(nl), C.byref(ng), None, None))
+        loc = np.empty(max(1, nl.value), np.int32)
+        gh = np.empty(max(1, ng.value), np.int32)
+        self._ck(self._L.qlskum_partition_layout(self._h, int(part), None, None, _ip(loc), _ip(gh)))
+        return loc[:nl.value].copy(), gh[:ng.value].copy()
+
+    def set_launch_config(self, flux_variant, point_block, staged):
+        self._ck(self._L.qlskum_partition_set_launch_config(self._h, int(flux_variant), int(point_block),
+                                                            int(staged)))
+
+    def q_lskum(self, iters):
+        self._ck(self._L.qlskum_partition_q_lskum(self._h, int(iters)))
+
+    @property
+    def prim(self):
+        out = np.empty((self.n, 4))
+        self._ck(self._L.qlskum_partition_get_prim(self._h, _dp(out)))
+        return out
+
+    def set_prim(self, prim):
+        a = np.ascontiguousarray(prim, np.float64)
+        self._ck(self._L.qlskum_partition_set_prim(self._h, _dp(a)))
+
+    def residual_history(self):
+        rows = C.c_int()
+        self._ck(self._L.qlskum_partition_residual_history(self._h, None, 0, C.byref(rows)))
+        out = np.empty((rows.value, 3))
+        if rows.value:
+            self._ck(self._L.qlskum_partition_residual_history(self._h, _dp(out), rows.value, C.byref(rows)))
+        return out
+
+    def objective(self):
+        v = [C.c_double() for _ in range(4)]
+        self._ck(self._L.qlskum_partition_objective(self._h, *[C.byref(t) for t in v]))
+        return tuple(t.value for t in v)
+
+    @property
+    def halo_bytes(self) -> int:
+        return int(self._L.qlskum_partition_halo_bytes(self._h))
+
+    @property
+    def launches(self) -> int:
+        return int(self._L.qlskum_partition_launch_count(self._h))

@@ -45,7 +45,11 @@ typedef enum {
 
 typedef enum {
     QLSKUM_FP64 = 0,             /* FP64 end to end: the drop-in form */
-    QLSKUM_MIXED = 1             /* FP32 q / limiter / split fluxes, FP64 solve + accumulate + update */
+    QLSKUM_MIXED = 1             /* FP32: q, dq, qm storage, limiter, reconstruction, split fluxes and
+                                    the per-point weighted sums over the edges; FP64: the 2x2
+                                    least-squares solves (folded once per cloud into per-edge FP32
+                                    weights), the time-step scaling of the residual, the SSPRK
+                                    update, prim and the residual norm */
 } qlskum_precision;
 
 /* The grid file's columns (main.cpp:32-36), host memory, 1-based indices. */
@@ -223,6 +227,60 @@ void *qlskum_batch_stream(qlskum_batch *b);
  * kernel, points per warp (one thread per point: 32). */
 qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_tile, int *flux_min_blocks,
                                   int *points_per_warp);
+
+/* ------------------------------------------- partitions with a ghost-point halo */
+
+/* The solve split into partitions in the reference's distributed layout
+ * (data_structure_mod.h:4-8: local_points, ghost_points and pghost, the
+ * global numbers of a partition's ghost points; point_preprocessing_mod.h:
+ * 124-132 reads them per partition): each partition owns a compact range of
+ * the points (the cloud sorted by the Morton code of its coordinates and cut
+ * into n_parts ranges of nearly equal size) and keeps copies of the points
+ * outside it that its own points read (its ghosts: 1-based global numbers,
+ * grouped by owning partition, in the owner's order).  Every kernel that
+ * reads a neighbour's value is preceded by an exchange that refreshes the
+ * ghosts from their owners: per stage q (and the wave speed of the time
+ * step in the first stage), dq and qm after the gradient, dq after each
+ * inner step.  The residual norm and the objectives are sums over the
+ * partitions.  All partitions run on the current GPU, each on its own
+ * stream; the point arithmetic is the single-domain solve's, so the state
+ * equals qlskum_q_lskum's on the whole cloud (bit for bit in FP64, and in
+ * the mixed form with the same launch shape), and only the order of the
+ * residual and objective sums differs.  No counterpart in the serial
+ * reference, whose ghost arrays are never filled. */
+typedef struct qlskum_partition qlskum_partition;
+/* The plan without a GPU: part_of [n] (0-based partition of each point),
+ * n_local / n_ghost [n_parts]; any pointer may be NULL. */
+qlskum_status qlskum_partition_plan(const qlskum_cloud *cloud, int n_parts, int *part_of, int *n_local,
+                                    int *n_ghost);
+/* One partition's points (1-based, in its device order) and ghosts (1-based,
+ * as pghost holds them), without a GPU; either pointer may be NULL. */
+qlskum_status qlskum_partition_plan_lists(const qlskum_cloud *cloud, int n_parts, int part, int *local_ids,
+                                          int *ghost_ids);
+qlskum_status qlskum_partition_create(const qlskum_cloud *cloud, const qlskum_params *params, int n_parts,
+                                      qlskum_partition **out);
+qlskum_status qlskum_partition_destroy(qlskum_partition *p);
+const char *qlskum_partition_last_error(const qlskum_partition *p);
+/* Sizes and point lists of partition `part` (as qlskum_partition_plan_lists). */
+qlskum_status qlskum_partition_layout(const qlskum_partition *p, int part, int *n_local, int *n_ghost,
+                                      int *local_ids, int *ghost_ids);
+/* Mixed form: the launch shape (numbered as qlskum_set_launch_config;
+ * default flux_variant 5, point_block 128 or params.block_size, staged 0). */
+qlskum_status qlskum_partition_set_launch_config(qlskum_partition *p, int flux_variant, int point_block, int staged);
+/* `iters` iterations (q_lskum_mod.h:13-38) of the partitioned solve. */
+qlskum_status qlskum_partition_q_lskum(qlskum_partition *p, int iters);
+/* The state [n][4] in the cloud's point order, gathered from the owners /
+ * written to owners and ghosts alike. */
+qlskum_status qlskum_partition_get_prim(qlskum_partition *p, double *out);
+qlskum_status qlskum_partition_set_prim(qlskum_partition *p, const double *prim);
+/* As qlskum_get_residual_history. */
+qlskum_status qlskum_partition_residual_history(qlskum_partition *p, double *out, int max_rows, int *rows);
+/* As qlskum_objective, the partitions' sums added in partition order. */
+qlskum_status qlskum_partition_objective(qlskum_partition *p, double *cl, double *cd, double *cm,
+                                         double *total_entropy);
+/* Bytes the ghost exchanges of one iteration move, and the kernel launches so far. */
+long long qlskum_partition_halo_bytes(const qlskum_partition *p);
+long long qlskum_partition_launch_count(const qlskum_partition *p);
 
 /* ------------------------------------------------- diagnostics and state files */
 
