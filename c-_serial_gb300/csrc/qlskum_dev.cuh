@@ -84,9 +84,11 @@ __device__ __forceinline__ void mixed_end(float nx, float ny, float delx, float 
                                           const float dx[4], const float dy[4], const float mx[4],
                                           const float mn[4], float e2, MixedEnd &s)
 {
+    // -(delx dqx + dely dqy) / 2 with the halving on the edge vector (exact: a power of two)
+    const float hx = -0.5f * delx, hy = -0.5f * dely;
 #pragma unroll
     for (int r = 0; r < 4; r++) {
-        const float dn = -0.5f * fmaf(delx, dx[r], dely * dy[r]);
+        const float dn = fmaf(hx, dx[r], hy * dy[r]);
         const float dp = DQM ? ((dn > 0.f) ? mx[r] : mn[r]) : ((dn > 0.f) ? mx[r] : mn[r]) - q[r];
         const float base = fmaf(dp, dp, e2);
         const float num = fmaf(2.0f * dn, dp, base);

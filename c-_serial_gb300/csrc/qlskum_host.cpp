@@ -474,22 +474,26 @@ qlskum_status tune(qlskum_handle *h)
     static const int blocks[4] = {64, 128, 256, 512};
     float best = 1e30f;
     Launch best_L = h->L;
-    for (int bs : blocks) {
-        Launch L = h->L;
-        L.block = bs;
-        L.staged = 0;
-        const float ms = point_kernels(L);
-        if (ms < best) { best = ms; best_L = L; }
-    }
+    for (int bs : blocks)
+        for (int ln : {1, 2, 4}) {
+            Launch L = h->L;
+            L.block = bs;
+            L.staged = 0;
+            L.lanes = ln;
+            const float ms = point_kernels(L);
+            if (ms < best) { best = ms; best_L = L; }
+        }
     const int nst = mixed::staged_variants(c);
     for (int v = 1; v <= nst; v++) {
         Launch L = best_L;
         L.staged = v;
+        L.lanes = 1;
         const float ms = point_kernels(L);
         if (ms < best) { best = ms; best_L = L; }
     }
     h->L.block = best_L.block;
     h->L.staged = best_L.staged;
+    h->L.lanes = best_L.lanes;
     mixed::q_derivatives(h->L, c, S.q[0], S.dq[0], S.qm, S.cspeed, S.delta, (float)h->K.cfl);
     best = 1e30f;
     Reduce none = h->R;  // stage 1 writes no residual partials
@@ -555,8 +559,8 @@ void enqueue_iteration(qlskum_handle *h, int o, int it_arg)
         }
     }
     Reduce R = h->R;
-    R.blocks = (h->n + (h->prm.precision == QLSKUM_MIXED ? mixed::flux_block(h->flux_variant) : 128) - 1) /
-               (h->prm.precision == QLSKUM_MIXED ? mixed::flux_block(h->flux_variant) : 128);
+    R.blocks = h->prm.precision == QLSKUM_MIXED ? mixed::flux_grid_blocks(h->flux_variant, h->n)
+                                                 : (h->n + 127) / 128;
     timed(h, QLSKUM_KERNEL_REDUCE, [&] { fp64::reduce_residual(L, R, h->n, it_arg); });
 }
 
@@ -1386,6 +1390,7 @@ qlskum_status qlskum_set_launch_config(qlskum_handle *h, int flux_variant, int p
     h->flux_variant = flux_variant;
     h->L.block = point_block;
     h->L.staged = h->prm.precision == QLSKUM_MIXED ? staged : 0;
+    h->L.lanes = 1;
     h->tuned = true;
     // captured iterations hold the old shapes
     for (auto &g : h->graph)
@@ -1393,6 +1398,30 @@ qlskum_status qlskum_set_launch_config(qlskum_handle *h, int flux_variant, int p
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_set_point_lanes(qlskum_handle *h, int lanes)
+{
+    NEED(h);
+    if (lanes != 1 && lanes != 2 && lanes != 4) return fail(h, QLSKUM_ERR_INVALID, "lanes must be 1, 2 or 4");
+    if (lanes > 1 && h->L.staged) return fail(h, QLSKUM_ERR_UNSUPPORTED, "the staged gather form has one lane per point");
+    h->L.lanes = h->prm.precision == QLSKUM_MIXED ? lanes : 1;
+    h->tuned = true;
+    for (auto &g : h->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_get_lanes(const qlskum_handle *h, int *point_lanes, int *flux_lanes)
+{
+    if (!h) return QLSKUM_ERR_INVALID;
+    const bool mx = h->prm.precision == QLSKUM_MIXED;
+    if (point_lanes) *point_lanes = mx ? h->L.lanes : 1;
+    if (flux_lanes) *flux_lanes = mx ? mixed::flux_lanes(h->flux_variant) : 1;
     return QLSKUM_OK;
 }
 
@@ -1468,8 +1497,6 @@ qlskum_status bfail(qlskum_batch *b, qlskum_status s, const std::string &msg)
         if (e_ != cudaSuccess) return bfail(b, QLSKUM_ERR_CUDA, fmt("%s: %s", #call, cudaGetErrorString(e_))); \
     } while (0)
 
-static const int kFluxTile[4] = {128, 128, 64, 256};
-static const int kFluxMinB[4] = {4, 5, 8, 2};
 
 void batch_enqueue_iteration(qlskum_batch *b, int o)
 {
@@ -1488,7 +1515,7 @@ void batch_enqueue_iteration(qlskum_batch *b, int o)
                                  rk == 4 ? b->cspeed : nullptr, rk, rk == 4 ? b->psum : nullptr,
                                  rk == 4 ? b->pmax : nullptr);
     }
-    mixed::batch_reduce(b->L, b->view, kFluxTile[b->flux_variant], b->psum, b->pmax, b->d_iter, b->res_old,
+    mixed::batch_reduce(b->L, b->view, mixed::batch_flux_tile(b->flux_variant), b->psum, b->pmax, b->d_iter, b->res_old,
                         b->res_new, b->hist, b->capacity, b->d_status);
 }
 
@@ -1541,15 +1568,24 @@ qlskum_status batch_tune(qlskum_batch *b)
         return ms;
     };
     const long long l0 = b->launches;
+    // gradient / inner-loop kernels: points per tile x lanes per point, timed
+    // as an iteration weighs them (one gradient and inner_iterations inner steps)
     float best = 1e30f;
-    for (int t : {64, 128, 256}) {
-        float ms = time3([&] { mixed::batch_q_inner(b->L, b->view, t, b->dq[0], b->dq[0], b->dq[1]); });
-        if (ms < best) { best = ms; b->tile = t; }
-    }
+    const int ni = std::max(1, b->prm.inner_iterations);
+    for (int t : {64, 128, 256})
+        for (int ln : {1, 2, 4}) {
+            Launch L = b->L;
+            L.lanes = ln;
+            const float ms =
+                ni * time3([&] { mixed::batch_q_inner(L, b->view, t, b->dq[0], b->dq[0], b->dq[1]); }) +
+                time3([&] { mixed::batch_q_derivatives(L, b->view, t, b->q[0], b->dq[0], b->qm, b->cspeed, nullptr,
+                                                       b->cfl); });
+            if (ms < best) { best = ms; b->tile = t; b->L.lanes = ln; }
+        }
     const int o = b->pcur, x = (o + 1) % 3;
     mixed::batch_q_derivatives(b->L, b->view, b->tile, b->q[0], b->dq[0], b->qm, b->cspeed, b->delta, b->cfl);
     best = 1e30f;
-    for (int v = 0; v < 4; v++) {
+    for (int v = 0; v < mixed::batch_flux_variants(); v++) {
         float ms = time3([&] {
             mixed::batch_flux_update(b->L, b->view, v, b->q[0], b->dq[0], b->qm, b->delta, b->prim[o], b->prim[o],
                                      b->prim[x], b->q[1], nullptr, 1, nullptr, nullptr);
@@ -1818,6 +1854,34 @@ long long qlskum_batch_total_points(const qlskum_batch *b)
 
 long long qlskum_batch_launch_count(const qlskum_batch *b) { return b ? b->launches : 0; }
 
+qlskum_status qlskum_batch_lanes(const qlskum_batch *b, int *point_lanes, int *flux_lanes)
+{
+    if (!b) return QLSKUM_ERR_INVALID;
+    if (point_lanes) *point_lanes = b->L.lanes;
+    if (flux_lanes) *flux_lanes = mixed::batch_flux_lanes(b->flux_variant);
+    return QLSKUM_OK;
+}
+
+qlskum_status qlskum_batch_set_launch_config(qlskum_batch *b, int tile, int point_lanes, int flux_variant)
+{
+    if (!b) return QLSKUM_ERR_INVALID;
+    if (tile != 64 && tile != 128 && tile != 256) return bfail(b, QLSKUM_ERR_INVALID, "tile must be 64, 128 or 256");
+    if (point_lanes != 1 && point_lanes != 2 && point_lanes != 4)
+        return bfail(b, QLSKUM_ERR_INVALID, "point_lanes must be 1, 2 or 4");
+    if (flux_variant < 0 || flux_variant >= mixed::batch_flux_variants())
+        return bfail(b, QLSKUM_ERR_INVALID, fmt("flux_variant not in 0..%d", mixed::batch_flux_variants() - 1));
+    b->tile = tile;
+    b->L.lanes = point_lanes;
+    b->flux_variant = flux_variant;
+    b->tuned = true;
+    for (auto &g : b->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    return QLSKUM_OK;
+}
+
 void *qlskum_batch_stream(qlskum_batch *b) { return b ? (void *)b->L.stream : nullptr; }
 
 qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_tile, int *flux_min_blocks,
@@ -1825,9 +1889,9 @@ qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_ti
 {
     if (!b) return QLSKUM_ERR_INVALID;
     if (tile) *tile = b->tile;
-    if (flux_tile) *flux_tile = kFluxTile[b->flux_variant];
-    if (flux_min_blocks) *flux_min_blocks = kFluxMinB[b->flux_variant];
-    if (points_per_warp) *points_per_warp = 32;
+    if (flux_tile) *flux_tile = mixed::batch_flux_tile(b->flux_variant);
+    if (flux_min_blocks) *flux_min_blocks = mixed::batch_flux_min_blocks(b->flux_variant);
+    if (points_per_warp) *points_per_warp = 32 / mixed::batch_flux_lanes(b->flux_variant);
     return QLSKUM_OK;
 }
 
@@ -2006,11 +2070,10 @@ void part_gather(qlskum_partition *P)
 void part_reduce_layout(qlskum_partition *P)
 {
     const bool mx = P->prm.precision == QLSKUM_MIXED;
-    const int fb = mx ? mixed::flux_block(P->flux_variant) : 128;
     int off = 0;
     for (PartDev *d : P->parts) {
         d->red_off = off;
-        d->red_blocks = (d->G.n + fb - 1) / fb;
+        d->red_blocks = mx ? mixed::flux_grid_blocks(P->flux_variant, d->G.n) : (d->G.n + 127) / 128;
         off += d->red_blocks;
     }
     P->R.blocks = off;
@@ -3180,7 +3243,7 @@ void adj_iteration_forward32(qlskum_handle *h, Set32 &st, int it_rec = 0)
     }
     if (it_rec > 0) {
         Reduce R = h->R;
-        R.blocks = (h->n + mixed::flux_block(h->flux_variant) - 1) / mixed::flux_block(h->flux_variant);
+        R.blocks = mixed::flux_grid_blocks(h->flux_variant, h->n);
         fp64::reduce_residual(h->L, R, h->n, it_rec);
     }
 }
@@ -3434,6 +3497,75 @@ qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const do
     adjl::delta(h->L, v, a->P[0], a->bdelta, h->K.cfl, a->bc, a->bP);
     if ((st = check_launch(h, "residual_vjp"))) return st;
     return download_points(h, a->bP, bar_prim);
+}
+
+// The forward / VJP pair on device buffers in the cloud's point order, ordered
+// after the caller's stream (an event it records, which the handle's stream
+// waits for) and before the caller's later work (the reverse).
+namespace {
+
+qlskum_status dev_args(qlskum_handle *h, std::initializer_list<const void *> ptrs)
+{
+    for (const void *p : ptrs) {
+        if (!p) return fail(h, QLSKUM_ERR_INVALID, "null device buffer");
+        if (reinterpret_cast<uintptr_t>(p) & 31u) return fail(h, QLSKUM_ERR_INVALID, "device buffers must be 32-byte aligned");
+    }
+    return ensure_stage(h);
+}
+
+void wait_on(qlskum_handle *h, cudaStream_t waiter, cudaStream_t on)
+{
+    cudaEvent_t e = take_event(h);
+    cudaEventRecord(e, on);
+    cudaStreamWaitEvent(waiter, e, 0);
+    h->ev_pool.push_back(e);
+}
+
+}  // namespace
+
+qlskum_status qlskum_residual_forward_device(qlskum_handle *h, const double *prim, double *flux_res, void *stream)
+{
+    NEED(h);
+    qlskum_status st = dev_args(h, {prim, flux_res});
+    if (st) return st;
+    if ((st = adj_alloc(h, false, true, false))) return st;
+    AdjBuf *a = h->adj;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    wait_on(h, h->L.stream, cs);
+    fp64::fill_prim(h->L, h->np, make_double4_32a(1.0, 0, 0, 1.0), a->P[0]);
+    fp64::permute_in(h->L, h->n, h->d_perm, reinterpret_cast<const double4_32a *>(prim), a->P[0]);
+    fp64::func_delta(h->L, h->dc, a->P[0], a->set64.delta, h->K.cfl);
+    adj_stage_forward(h, a->set64, 0);
+    fp64::permute_out(h->L, h->n, h->d_perm, a->set64.flux[0], reinterpret_cast<double4_32a *>(flux_res));
+    wait_on(h, cs, h->L.stream);
+    return check_launch(h, "residual_forward_device");
+}
+
+qlskum_status qlskum_residual_vjp_device(qlskum_handle *h, const double *prim, const double *bar_flux_res,
+                                         double *bar_prim, void *stream)
+{
+    NEED(h);
+    qlskum_status st = dev_args(h, {prim, bar_flux_res, bar_prim});
+    if (st) return st;
+    if ((st = adj_alloc(h, false, true, false))) return st;
+    AdjBuf *a = h->adj;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    wait_on(h, h->L.stream, cs);
+    fp64::fill_prim(h->L, h->np, make_double4_32a(1.0, 0, 0, 1.0), a->P[0]);
+    fp64::permute_in(h->L, h->n, h->d_perm, reinterpret_cast<const double4_32a *>(prim), a->P[0]);
+    zero(h, a->bF, sizeof(double4_32a) * h->np);
+    fp64::permute_in(h->L, h->n, h->d_perm, reinterpret_cast<const double4_32a *>(bar_flux_res), a->bF);
+    fp64::func_delta(h->L, h->dc, a->P[0], a->set64.delta, h->K.cfl);
+    adj_stage_forward(h, a->set64, 0);
+    const AdjView v = adj_view(h, false);
+    zero(h, a->bP, sizeof(double4_32a) * h->np);
+    zero(h, a->bdelta, sizeof(double) * h->np);
+    adj_stage_reverse(h, a->set64, 0, v);
+    zero(h, a->bc, sizeof(double) * h->np);
+    adjl::delta(h->L, v, a->P[0], a->bdelta, h->K.cfl, a->bc, a->bP);
+    fp64::permute_out(h->L, h->n, h->d_perm, a->bP, reinterpret_cast<double4_32a *>(bar_prim));
+    wait_on(h, cs, h->L.stream);
+    return check_launch(h, "residual_vjp_device");
 }
 
 qlskum_status qlskum_residual_vjp_full(qlskum_handle *h, const double *prim, const double *bar_flux_res,

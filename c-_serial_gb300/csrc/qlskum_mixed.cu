@@ -23,6 +23,40 @@ namespace mixed {
 
 static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
 
+// ----------------------------------------------------- lanes per point
+// A point's edges can be split over L = 1, 2 or 4 adjacent lanes of a warp
+// (lane s takes edges s, s + L, ...); the lanes' partial sums, maxima and
+// minima are then combined with butterfly shuffles inside the aligned group
+// of L lanes, and the group's first lane finishes the point.  The groups of
+// a warp are independent (a group whose point is past the end skips the
+// shuffles as a whole), so the shuffle mask names the group's lanes only.
+template <int L> __device__ __forceinline__ unsigned group_mask()
+{
+    const unsigned lane = threadIdx.x & 31u;
+    return L >= 32 ? 0xffffffffu : (((1u << L) - 1u) << (lane & ~(unsigned)(L - 1)));
+}
+
+template <int L> __device__ __forceinline__ float group_sum(float v, unsigned m)
+{
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) v += __shfl_xor_sync(m, v, o);
+    return v;
+}
+
+template <int L> __device__ __forceinline__ float group_max(float v, unsigned m)
+{
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(m, v, o));
+    return v;
+}
+
+template <int L> __device__ __forceinline__ float group_min(float v, unsigned m)
+{
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(m, v, o));
+    return v;
+}
+
 __device__ __forceinline__ void q_of(const double P[4], float Q[4])
 {
     prim_to_q<float>(d2f(P[0]), d2f(P[1]), d2f(P[2]), d2f(P[3]), Q);
@@ -121,10 +155,11 @@ __device__ __forceinline__ float4 edge_w(const DevCloud &c, long long e)
 // q_variables_mod.h:36-118: FP32 differences, weighted by the FP64-folded
 // per-edge solve weights (DevCloud::e_gw32); with DT (the first stage) also
 // the local time step (state_update_mod.h:448-496) in FP32.
-template <bool DT>
+template <bool DT, int L = 1>
 __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float4 *__restrict__ q,
                                            float4 *__restrict__ dq, float4 *__restrict__ qm,
-                                           const float *__restrict__ cs, float *__restrict__ delta, float cfl)
+                                           const float *__restrict__ cs, float *__restrict__ delta, float cfl,
+                                           int sub = 0)
 {
     float qi[4], qmax[4], qmin[4], dx[4] = {0, 0, 0, 0}, dy[4] = {0, 0, 0, 0};
     ld4(q[i], qi);
@@ -133,7 +168,7 @@ __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float
     float min_dt = 1.0f;
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
-    for (int j = 0; j < nb; j++) {
+    for (int j = sub; j < nb; j += L) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         const float2 gw = c.e_gw32[e];
@@ -148,6 +183,18 @@ __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float
             dy[r] = fmaf(gw.y, d, dy[r]);
         }
         if (DT) min_dt = fminf(min_dt, cfl * __fdividef(c.e_dist32[e], cs[k]));
+    }
+    if (L > 1) {
+        const unsigned m = group_mask<L>();
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            dx[r] = group_sum<L>(dx[r], m);
+            dy[r] = group_sum<L>(dy[r], m);
+            qmax[r] = group_max<L>(qmax[r], m);
+            qmin[r] = group_min<L>(qmin[r], m);
+        }
+        if (DT) min_dt = group_min<L>(min_dt, m);
+        if (sub != 0) return;
     }
     dq[2 * i] = mk4(dx);
     dq[2 * i + 1] = mk4(dy);
@@ -181,14 +228,15 @@ __device__ __forceinline__ void inner_finish(const float ax[4], const float ay[4
     out[1] = mk4(ry);
 }
 
-template <bool UW>
+template <bool UW, int L = 1>
 __device__ __forceinline__ void inner_point(const DevCloud &c, int i, const float4 *__restrict__ dq0,
-                                            const float4 *__restrict__ dq_in, float4 *__restrict__ dq_out)
+                                            const float4 *__restrict__ dq_in, float4 *__restrict__ dq_out,
+                                            int sub = 0)
 {
     float dxi[4], dyi[4], ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0};
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
-    for (int j = 0; j < nb; j++) {
+    for (int j = sub; j < nb; j += L) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         const float4 g = edge_w<UW>(c, e);
@@ -202,6 +250,15 @@ __device__ __forceinline__ void inner_point(const DevCloud &c, int i, const floa
             ax[r] = fmaf(gw.x, u, ax[r]);
             ay[r] = fmaf(gw.y, u, ay[r]);
         }
+    }
+    if (L > 1) {
+        const unsigned m = group_mask<L>();
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            ax[r] = group_sum<L>(ax[r], m);
+            ay[r] = group_sum<L>(ay[r], m);
+        }
+        if (sub != 0) return;
     }
     // the point's own gradient only after the loop: fewer registers live across it
     ld4(dq_in[2 * i], dxi);
@@ -382,6 +439,30 @@ __device__ __forceinline__ void x_flux(int f, const Kin<float> &k, float s1, flo
     else flux_quad(k, s1, (f == kOuter) ? 1.0f : -1.0f, G);
 }
 
+// One interior edge end's weighted pair wx Gx(s1) + wy Gy(s2) (rho = 1),
+// scaled by sc and added to acc.  Both split fluxes are linear in their
+// half-range moments (split_fluxes_mod.h:14-84 and :86-164):
+//   Gx = A1 a + B1 b,  Gy = A2 c + B2 b,  A = (1 + s E) / 2,  B = s B,
+//   a = (ut, pbr + ut^2, ut un, ut (7 pbr + usq) / 2),
+//   c = (un, ut un, pbr + un^2, un (7 pbr + usq) / 2),
+//   b = (1, ut, un, (6 pbr + usq) / 2),
+// so the pair is three multiply-adds per component on top of the end's
+// vectors a, b, c.  hs1 / hs2 = s / 2; ws1 = wx s1, ws2 = wy s2.
+__device__ __forceinline__ void interior_pair(const Kin<float> &k, float hs1, float hs2, float wx, float wy,
+                                              float ws1, float ws2, float sc, float acc[4])
+{
+    const float A1 = fmaf(hs1, k.E1, 0.5f), A2 = fmaf(hs2, k.E2, 0.5f);
+    const float al = (sc * wx) * A1, ga = (sc * wy) * A2;
+    const float be = sc * fmaf(ws1, k.B1, ws2 * k.B2);
+    const float utun = k.ut * k.un;
+    const float h7 = 0.5f * fmaf(7.0f, k.pbr, k.usq), h6 = 0.5f * fmaf(6.0f, k.pbr, k.usq);
+    const float a[4] = {k.ut, fmaf(k.ut, k.ut, k.pbr), utun, k.ut * h7};
+    const float c[4] = {k.un, utun, fmaf(k.un, k.un, k.pbr), k.un * h7};
+    const float b[4] = {1.0f, k.ut, k.un, h6};
+#pragma unroll
+    for (int r = 0; r < 4; r++) acc[r] = fmaf(al, a[r], fmaf(ga, c[r], fmaf(be, b[r], acc[r])));
+}
+
 // Flux contribution of one edge (interior_fluxes_mod.h, wall_fluxes_mod.h,
 // outer_fluxes_mod.h), the owner's mxi / mni given as qmax - q / qmin - q:
 // reconstruction and limiter at both ends, then the
@@ -409,18 +490,24 @@ __device__ __forceinline__ void flux_edge(const DevCloud &c, long long e, int f,
     kk.rho = 1.0f;
     const float ri = si.k.rho, rk = sk.k.rho;
     float Gi[4], Gk[4];
-    // x: xpos (s1 = +1) when bit 1 is set, else xneg
+    // x: xpos (s1 = +1) when bit 1 is set, else xneg; y: ypos (s2 = +1) when bit 4 is set, else yneg
     const float s1 = (dir & kXpos) ? 1.0f : -1.0f;
-    x_flux(f, ki, s1, Gi);
-    x_flux(f, kk, s1, Gk);
-#pragma unroll
-    for (int r = 0; r < 4; r++) acc[r] = fmaf(w.x * rk, Gk[r], fmaf(-w.x * ri, Gi[r], acc[r]));
-    // y: ypos (s2 = +1) when bit 4 is set, else yneg
     const float s2 = (dir & kYpos) ? 1.0f : -1.0f;
-    flux_y(ki, s2, Gi);
-    flux_y(kk, s2, Gk);
+    if (f == kInterior) {
+        // warps are class-uniform: the interior points take the combined form
+        const float hs1 = 0.5f * s1, hs2 = 0.5f * s2, ws1 = w.x * s1, ws2 = w.y * s2;
+        interior_pair(ki, hs1, hs2, w.x, w.y, ws1, ws2, -ri, acc);
+        interior_pair(kk, hs1, hs2, w.x, w.y, ws1, ws2, rk, acc);
+    } else {
+        x_flux(f, ki, s1, Gi);
+        x_flux(f, kk, s1, Gk);
 #pragma unroll
-    for (int r = 0; r < 4; r++) acc[r] = fmaf(w.y * rk, Gk[r], fmaf(-w.y * ri, Gi[r], acc[r]));
+        for (int r = 0; r < 4; r++) acc[r] = fmaf(w.x * rk, Gk[r], fmaf(-w.x * ri, Gi[r], acc[r]));
+        flux_y(ki, s2, Gi);
+        flux_y(kk, s2, Gk);
+#pragma unroll
+        for (int r = 0; r < 4; r++) acc[r] = fmaf(w.y * rk, Gk[r], fmaf(-w.y * ri, Gi[r], acc[r]));
+    }
     const bool xb = (dir & (kXpos | kXneg)) == (kXpos | kXneg), yb = (dir & (kYpos | kYneg)) == (kYpos | kYneg);
     if (xb || yb) {
         const float2 w2 = c.e_w32b[e];
@@ -480,14 +567,15 @@ __device__ __forceinline__ double flux_tail(const CaseConst &K, int i, int f, do
 // Fused stage of one point: FP32 edge work with the FP64-folded solve
 // weights, FP64 residual scaling and update.
 // Returns the point's res_sqr.
-template <bool UW>
+template <bool UW, int L = 1>
 __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst &K, int i,
                                              const float4 *__restrict__ q, const float4 *__restrict__ dq,
                                              const float4 *__restrict__ qm, const float *__restrict__ delta,
                                              const double4_32a *__restrict__ prim,
                                              const double4_32a *__restrict__ prim_old,
                                              double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
-                                             float *__restrict__ cs_next, int rk, float4 *__restrict__ acc_out)
+                                             float *__restrict__ cs_next, int rk, float4 *__restrict__ acc_out,
+                                             int sub = 0)
 {
     const int f = c.flag[i];
     const double2 nn = c.nrm[i];
@@ -508,7 +596,7 @@ __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst 
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
-    for (int j = 0; j < nb; j++) {
+    for (int j = sub; j < nb; j += L) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         float4 g;
@@ -522,6 +610,12 @@ __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst 
         ld4(qm[2 * k], mxk);
         ld4(qm[2 * k + 1], mnk);
         flux_edge(c, e, f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, w, dir, qk, dxk, dyk, mxk, mnk, c.eps2_32[k], acc);
+    }
+    if (L > 1) {
+        const unsigned m = group_mask<L>();
+#pragma unroll
+        for (int r = 0; r < 4; r++) acc[r] = group_sum<L>(acc[r], m);
+        if (sub != 0) return 0.0;
     }
     return flux_tail(K, i, f, nn, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
 }
@@ -609,24 +703,27 @@ __device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseCon
 
 // ---------------------------------------------------- single-case kernels
 
-template <bool DT>
+template <bool DT, int L>
 __global__ void k_q_derivatives(DevCloud c, const float4 *__restrict__ q, float4 *__restrict__ dq,
                                 float4 *__restrict__ qm, const float *__restrict__ cs, float *__restrict__ delta,
                                 float cfl)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < c.n) grad_point<DT>(c, i, q, dq, qm, cs, delta, cfl);
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = g / L;
+    if (i < c.n) grad_point<DT, L>(c, i, q, dq, qm, cs, delta, cfl, g % L);
 }
 
-template <bool UW>
+template <bool UW, int L>
 __global__ void k_q_inner(DevCloud c, const float4 *__restrict__ dq0, const float4 *__restrict__ dq_in,
                           float4 *__restrict__ dq_out)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < c.n) inner_point<UW>(c, i, dq0, dq_in, dq_out);
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = g / L;
+    if (i < c.n) inner_point<UW, L>(c, i, dq0, dq_in, dq_out, g % L);
 }
 
-template <int BLOCK, int MINB, bool UW>
+// L lanes per point: BLOCK threads hold BLOCK / L points.
+template <int BLOCK, int MINB, bool UW, int L = 1>
 __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseConst K, const float4 *__restrict__ q,
                                                        const float4 *__restrict__ dq, const float4 *__restrict__ qm,
                                                        const float *__restrict__ delta,
@@ -637,10 +734,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseCon
                                                        double *__restrict__ psum, double *__restrict__ pmax,
                                                        float4 *__restrict__ acc_out)
 {
-    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    const int g = blockIdx.x * BLOCK + threadIdx.x;
+    const int i = g / L;
     double r2 = 0.0;
     if (i < c.n)
-        r2 = flux_point<UW>(c, K, i, q, dq, qm, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
+        r2 = flux_point<UW, L>(c, K, i, q, dq, qm, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out,
+                               g % L);
     if (psum) block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
 }
 
@@ -695,41 +794,44 @@ __global__ void __launch_bounds__(TILE) kb_derived(const BatchCase *__restrict__
     }
 }
 
-template <int TILE, bool DT>
-__global__ void __launch_bounds__(TILE) kb_q_derivatives(const DevCloud *__restrict__ clouds,
-                                                         const BatchCase *__restrict__ cases,
-                                                         const BatchTile *__restrict__ tiles, int ntiles,
-                                                         const float4 *__restrict__ q, float4 *__restrict__ dq,
-                                                         float4 *__restrict__ qm, const float *__restrict__ cs,
-                                                         float *__restrict__ delta, float cfl)
+// TILE points per tile, L lanes per point: TILE * L threads per block.
+template <int TILE, bool DT, int L = 1>
+__global__ void __launch_bounds__(TILE * L) kb_q_derivatives(const DevCloud *__restrict__ clouds,
+                                                             const BatchCase *__restrict__ cases,
+                                                             const BatchTile *__restrict__ tiles, int ntiles,
+                                                             const float4 *__restrict__ q, float4 *__restrict__ dq,
+                                                             float4 *__restrict__ qm, const float *__restrict__ cs,
+                                                             float *__restrict__ delta, float cfl)
 {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const BatchTile T = tiles[t];
         const BatchCase &C = cases[T.cas];
-        const int i = T.first + threadIdx.x;
+        const int i = T.first + (int)threadIdx.x / L;
         if (i < C.n)
-            grad_point<DT>(clouds[C.cloud], i, q + C.off, dq + 2 * C.off, qm + 2 * C.off, cs + C.off,
-                           DT ? delta + C.off : nullptr, cfl);
+            grad_point<DT, L>(clouds[C.cloud], i, q + C.off, dq + 2 * C.off, qm + 2 * C.off, cs + C.off,
+                              DT ? delta + C.off : nullptr, cfl, (int)threadIdx.x % L);
     }
 }
 
-template <int TILE, bool UW>
-__global__ void __launch_bounds__(TILE) kb_q_inner(const DevCloud *__restrict__ clouds,
-                                                   const BatchCase *__restrict__ cases,
-                                                   const BatchTile *__restrict__ tiles, int ntiles,
-                                                   const float4 *__restrict__ dq0, const float4 *__restrict__ dq_in,
-                                                   float4 *__restrict__ dq_out)
+template <int TILE, bool UW, int L = 1>
+__global__ void __launch_bounds__(TILE * L) kb_q_inner(const DevCloud *__restrict__ clouds,
+                                                       const BatchCase *__restrict__ cases,
+                                                       const BatchTile *__restrict__ tiles, int ntiles,
+                                                       const float4 *__restrict__ dq0,
+                                                       const float4 *__restrict__ dq_in, float4 *__restrict__ dq_out)
 {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const BatchTile T = tiles[t];
         const BatchCase &C = cases[T.cas];
-        const int i = T.first + threadIdx.x;
-        if (i < C.n) inner_point<UW>(clouds[C.cloud], i, dq0 + 2 * C.off, dq_in + 2 * C.off, dq_out + 2 * C.off);
+        const int i = T.first + (int)threadIdx.x / L;
+        if (i < C.n)
+            inner_point<UW, L>(clouds[C.cloud], i, dq0 + 2 * C.off, dq_in + 2 * C.off, dq_out + 2 * C.off,
+                               (int)threadIdx.x % L);
     }
 }
 
-template <int TILE, int MINB, bool UW>
-__global__ void __launch_bounds__(TILE, MINB) kb_flux_update(const DevCloud *__restrict__ clouds,
+template <int TILE, int MINB, bool UW, int L = 1>
+__global__ void __launch_bounds__(TILE * L, MINB) kb_flux_update(const DevCloud *__restrict__ clouds,
                                                              const BatchCase *__restrict__ cases,
                                                              const BatchTile *__restrict__ tiles, int ntiles,
                                                              const float4 *__restrict__ q,
@@ -746,15 +848,15 @@ __global__ void __launch_bounds__(TILE, MINB) kb_flux_update(const DevCloud *__r
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const BatchTile T = tiles[t];
         const BatchCase &C = cases[T.cas];
-        const int i = T.first + threadIdx.x;
+        const int i = T.first + (int)threadIdx.x / L;
         double r2 = 0.0;
         if (i < C.n) {
             const long long o = C.off;
-            r2 = flux_point<UW>(clouds[C.cloud], C.K, i, q + o, dq + 2 * o, qm + 2 * o, delta + o, prim + o,
-                                prim_old + o, prim_next + o, q_next + o, cs_next ? cs_next + o : nullptr, rk,
-                                nullptr);
+            r2 = flux_point<UW, L>(clouds[C.cloud], C.K, i, q + o, dq + 2 * o, qm + 2 * o, delta + o, prim + o,
+                                   prim_old + o, prim_next + o, q_next + o, cs_next ? cs_next + o : nullptr, rk,
+                                   nullptr, (int)threadIdx.x % L);
         }
-        if (psum) block_sum_max<TILE>(r2, r2, psum + t, pmax + t);
+        if (psum) block_sum_max<TILE * L>(r2, r2, psum + t, pmax + t);
     }
 }
 
@@ -859,10 +961,18 @@ void q_derivatives(const Launch &L, const DevCloud &c, const float4 *q, float4 *
             else
                 k_q_derivatives_st<B_, D_, false><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 2, c.max_nb, true),
                                                     L.stream>>>(c, q, dq, qm, cspeed, delta, cfl))
-    } else if (delta) {
-        k_q_derivatives<true><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
     } else {
-        k_q_derivatives<false><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, delta, cfl);
+#define QLSKUM_GRAD(LN)                                                                                         \
+    if (delta)                                                                                                  \
+        k_q_derivatives<true, LN><<<grid_for(c.n * LN, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed,  \
+                                                                                        delta, cfl);           \
+    else                                                                                                        \
+        k_q_derivatives<false, LN><<<grid_for(c.n * LN, L.block), L.block, 0, L.stream>>>(c, q, dq, qm, cspeed, \
+                                                                                         delta, cfl)
+        if (L.lanes == 4) { QLSKUM_GRAD(4); }
+        else if (L.lanes == 2) { QLSKUM_GRAD(2); }
+        else { QLSKUM_GRAD(1); }
+#undef QLSKUM_GRAD
     }
     QLSKUM_LAUNCHED(L);
 }
@@ -877,41 +987,50 @@ void q_inner(const Launch &L, const DevCloud &c, const float4 *dq0, const float4
             else
                 k_q_inner_st<B_, D_, false><<<grid_for(c.n, B_), B_, staged_bytes(B_, D_, 2, c.max_nb, false),
                                               L.stream>>>(c, dq0, dq_in, dq_out))
-    } else if (c.unit_w) {
-        k_q_inner<true><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, dq0, dq_in, dq_out);
     } else {
-        k_q_inner<false><<<grid_for(c.n, L.block), L.block, 0, L.stream>>>(c, dq0, dq_in, dq_out);
+#define QLSKUM_INNER(LN)                                                                                        \
+    if (c.unit_w)                                                                                               \
+        k_q_inner<true, LN><<<grid_for(c.n * LN, L.block), L.block, 0, L.stream>>>(c, dq0, dq_in, dq_out);      \
+    else                                                                                                        \
+        k_q_inner<false, LN><<<grid_for(c.n * LN, L.block), L.block, 0, L.stream>>>(c, dq0, dq_in, dq_out)
+        if (L.lanes == 4) { QLSKUM_INNER(4); }
+        else if (L.lanes == 2) { QLSKUM_INNER(2); }
+        else { QLSKUM_INNER(1); }
+#undef QLSKUM_INNER
     }
     QLSKUM_LAUNCHED(L);
 }
 
 // Launch-shape variants of the fused kernel (threads per block, minimum
-// resident blocks per SM -> register cap; 4..7 the staged-gather form),
-// picked by the host's autotuner.
-const int kFluxVariants = 8;
-static const int kFluxBlock[kFluxVariants] = {128, 128, 64, 256, 128, 128, 64, 256};
-static const int kFluxMinBlocks[kFluxVariants] = {4, 5, 8, 2, 4, 5, 8, 2};
+// resident blocks per SM -> register cap; 4..7 the staged-gather form; 8, 9
+// the per-edge gather form with 2 / 4 lanes per point), picked by the host's
+// autotuner.
+const int kFluxVariants = 10;
+static const int kFluxBlock[kFluxVariants] = {128, 128, 64, 256, 128, 128, 64, 256, 128, 256};
+static const int kFluxMinBlocks[kFluxVariants] = {4, 5, 8, 2, 4, 5, 8, 2, 4, 2};
+static const int kFluxLanes[kFluxVariants] = {1, 1, 1, 1, 1, 1, 1, 1, 2, 4};
 
 int flux_variants() { return kFluxVariants; }
 int flux_block(int v) { return kFluxBlock[v]; }
 int flux_min_blocks(int v) { return kFluxMinBlocks[v]; }
+int flux_lanes(int v) { return kFluxLanes[v]; }
+int flux_grid_blocks(int v, int n) { return grid_for(n * kFluxLanes[v], kFluxBlock[v]); }
 
 void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const float4 *q, const float4 *dq,
                  const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
                  double4_32a *prim_next, float4 *q_next, float *cspeed_next, int rk, const Reduce &R, int variant,
                  float4 *acc_out)
 {
-#define QLSKUM_FLUX(B, MB)                                                                                  \
+#define QLSKUM_FLUX_L(B, MB, LN)                                                                            \
     if (c.unit_w)                                                                                           \
-        k_flux_update<B, MB, true><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,      \
-                                                                      prim_old, prim_next, q_next,         \
-                                                                      cspeed_next, rk, R.partial_sum,      \
-                                                                      R.partial_max, acc_out);             \
+        k_flux_update<B, MB, true, LN><<<grid_for(c.n * LN, B), B, 0, L.stream>>>(                          \
+            c, k, q, dq, qm, delta, prim, prim_old, prim_next, q_next, cspeed_next, rk, R.partial_sum,      \
+            R.partial_max, acc_out);                                                                        \
     else                                                                                                    \
-        k_flux_update<B, MB, false><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,     \
-                                                                       prim_old, prim_next, q_next,        \
-                                                                       cspeed_next, rk, R.partial_sum,     \
-                                                                       R.partial_max, acc_out)
+        k_flux_update<B, MB, false, LN><<<grid_for(c.n * LN, B), B, 0, L.stream>>>(                         \
+            c, k, q, dq, qm, delta, prim, prim_old, prim_next, q_next, cspeed_next, rk, R.partial_sum,      \
+            R.partial_max, acc_out)
+#define QLSKUM_FLUX(B, MB) QLSKUM_FLUX_L(B, MB, 1)
 #define QLSKUM_FLUX_ST(B, MB)                                                                               \
     if (c.unit_w)                                                                                           \
         k_flux_update_st<B, MB, true><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,   \
@@ -931,9 +1050,12 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
     case 5: QLSKUM_FLUX_ST(128, 5); break;
     case 6: QLSKUM_FLUX_ST(64, 8); break;
     case 7: QLSKUM_FLUX_ST(256, 2); break;
+    case 8: QLSKUM_FLUX_L(128, 4, 2); break;
+    case 9: QLSKUM_FLUX_L(256, 2, 4); break;
     default: QLSKUM_FLUX(128, 4); break;
     }
 #undef QLSKUM_FLUX
+#undef QLSKUM_FLUX_L
 #undef QLSKUM_FLUX_ST
     QLSKUM_LAUNCHED(L);
 }
@@ -966,66 +1088,87 @@ void batch_derived(const Launch &L, const BatchView &B, int tile, const double4_
     QLSKUM_LAUNCHED(L);
 }
 
+#define QLSKUM_LANES_SWITCH(LN, ...)                                                            \
+    switch (LN) {                                                                              \
+    case 4: { constexpr int L_ = 4; __VA_ARGS__; } break;                                      \
+    case 2: { constexpr int L_ = 2; __VA_ARGS__; } break;                                      \
+    default: { constexpr int L_ = 1; __VA_ARGS__; } break;                                     \
+    }
+
 void batch_q_derivatives(const Launch &L, const BatchView &B, int tile, const float4 *q, float4 *dq, float4 *qm,
                          const float *cs, float *delta, float cfl)
 {
-    QLSKUM_TILE_SWITCH(tile, {
+    QLSKUM_TILE_SWITCH(tile, QLSKUM_LANES_SWITCH(L.lanes, {
         const int ti = tile_index(T_);
         if (delta) {
-            const int g = persistent_grid(kb_q_derivatives<T_, true>, T_, B.ntiles[ti]);
-            kb_q_derivatives<T_, true><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq, qm,
-                                                               cs, delta, cfl);
+            const int g = persistent_grid(kb_q_derivatives<T_, true, L_>, T_ * L_, B.ntiles[ti]);
+            kb_q_derivatives<T_, true, L_><<<g, T_ * L_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti],
+                                                                        q, dq, qm, cs, delta, cfl);
         } else {
-            const int g = persistent_grid(kb_q_derivatives<T_, false>, T_, B.ntiles[ti]);
-            kb_q_derivatives<T_, false><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq,
-                                                                qm, cs, delta, cfl);
+            const int g = persistent_grid(kb_q_derivatives<T_, false, L_>, T_ * L_, B.ntiles[ti]);
+            kb_q_derivatives<T_, false, L_><<<g, T_ * L_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti],
+                                                                         B.ntiles[ti], q, dq, qm, cs, delta, cfl);
         }
-    })
+    }))
     QLSKUM_LAUNCHED(L);
 }
 
 void batch_q_inner(const Launch &L, const BatchView &B, int tile, const float4 *dq0, const float4 *dq_in,
                    float4 *dq_out)
 {
-    QLSKUM_TILE_SWITCH(tile, {
+    QLSKUM_TILE_SWITCH(tile, QLSKUM_LANES_SWITCH(L.lanes, {
         const int ti = tile_index(T_);
         if (B.unit_w) {
-            const int g = persistent_grid(kb_q_inner<T_, true>, T_, B.ntiles[ti]);
-            kb_q_inner<T_, true><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], dq0, dq_in, dq_out);
+            const int g = persistent_grid(kb_q_inner<T_, true, L_>, T_ * L_, B.ntiles[ti]);
+            kb_q_inner<T_, true, L_><<<g, T_ * L_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], dq0,
+                                                                  dq_in, dq_out);
         } else {
-            const int g = persistent_grid(kb_q_inner<T_, false>, T_, B.ntiles[ti]);
-            kb_q_inner<T_, false><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], dq0, dq_in,
-                                                          dq_out);
+            const int g = persistent_grid(kb_q_inner<T_, false, L_>, T_ * L_, B.ntiles[ti]);
+            kb_q_inner<T_, false, L_><<<g, T_ * L_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti],
+                                                                   dq0, dq_in, dq_out);
         }
-    })
+    }))
     QLSKUM_LAUNCHED(L);
 }
 
-// flux variants as for the single case: (tile, min blocks) = (128,4) (128,5) (64,8) (256,2)
+// flux variants: (points per tile, min blocks, lanes per point) = (128,4,1) (128,5,1) (64,8,1) (256,2,1)
+// (64,4,2) (64,2,4); threads per block = points x lanes
+const int kBatchFluxVariants = 6;
+static const int kBatchFluxTile[kBatchFluxVariants] = {128, 128, 64, 256, 64, 64};
+static const int kBatchFluxMinB[kBatchFluxVariants] = {4, 5, 8, 2, 4, 2};
+static const int kBatchFluxLanes[kBatchFluxVariants] = {1, 1, 1, 1, 2, 4};
+
+int batch_flux_variants() { return kBatchFluxVariants; }
+int batch_flux_tile(int v) { return kBatchFluxTile[v]; }
+int batch_flux_min_blocks(int v) { return kBatchFluxMinB[v]; }
+int batch_flux_lanes(int v) { return kBatchFluxLanes[v]; }
+
 void batch_flux_update(const Launch &L, const BatchView &B, int variant, const float4 *q, const float4 *dq,
                        const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
                        double4_32a *prim_next, float4 *q_next, float *cs_next, int rk, double *psum, double *pmax)
 {
-#define QLSKUM_BFLUX(T_, MB)                                                                                     \
+#define QLSKUM_BFLUX(T_, MB, LN)                                                                                 \
     {                                                                                                            \
         const int ti = tile_index(T_);                                                                           \
         if (B.unit_w) {                                                                                          \
-            const int g = persistent_grid(kb_flux_update<T_, MB, true>, T_, B.ntiles[ti]);                      \
-            kb_flux_update<T_, MB, true><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, \
-                                                                 dq, qm, delta, prim, prim_old, prim_next,        \
-                                                                 q_next, cs_next, rk, psum, pmax);                \
+            const int g = persistent_grid(kb_flux_update<T_, MB, true, LN>, T_ * LN, B.ntiles[ti]);             \
+            kb_flux_update<T_, MB, true, LN><<<g, T_ * LN, 0, L.stream>>>(                                       \
+                B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq, qm, delta, prim, prim_old, prim_next,       \
+                q_next, cs_next, rk, psum, pmax);                                                                \
         } else {                                                                                                 \
-            const int g = persistent_grid(kb_flux_update<T_, MB, false>, T_, B.ntiles[ti]);                     \
-            kb_flux_update<T_, MB, false><<<g, T_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti],  \
-                                                                  q, dq, qm, delta, prim, prim_old, prim_next,    \
-                                                                  q_next, cs_next, rk, psum, pmax);               \
+            const int g = persistent_grid(kb_flux_update<T_, MB, false, LN>, T_ * LN, B.ntiles[ti]);            \
+            kb_flux_update<T_, MB, false, LN><<<g, T_ * LN, 0, L.stream>>>(                                      \
+                B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq, qm, delta, prim, prim_old, prim_next,       \
+                q_next, cs_next, rk, psum, pmax);                                                                \
         }                                                                                                        \
     }
     switch (variant) {
-    case 1: QLSKUM_BFLUX(128, 5); break;
-    case 2: QLSKUM_BFLUX(64, 8); break;
-    case 3: QLSKUM_BFLUX(256, 2); break;
-    default: QLSKUM_BFLUX(128, 4); break;
+    case 1: QLSKUM_BFLUX(128, 5, 1); break;
+    case 2: QLSKUM_BFLUX(64, 8, 1); break;
+    case 3: QLSKUM_BFLUX(256, 2, 1); break;
+    case 4: QLSKUM_BFLUX(64, 4, 2); break;
+    case 5: QLSKUM_BFLUX(64, 2, 4); break;
+    default: QLSKUM_BFLUX(128, 4, 1); break;
     }
 #undef QLSKUM_BFLUX
     QLSKUM_LAUNCHED(L);

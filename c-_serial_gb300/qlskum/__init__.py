@@ -129,6 +129,12 @@ def load(build_if_needed: bool = True):
         "qlskum_partgrid_write": (i, [C.c_char_p, C.POINTER(CloudStruct)]),
         "qlskum_io_last_error": (C.c_char_p, []),
         "qlskum_check_stencils": (i, [C.POINTER(CloudStruct), C.c_double, C.c_double, dp, ip]),
+        "qlskum_residual_forward_device": (i, [H, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "qlskum_residual_vjp_device": (i, [H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "qlskum_set_point_lanes": (i, [H, i]),
+        "qlskum_get_lanes": (i, [H, ip, ip]),
+        "qlskum_batch_lanes": (i, [H, ip, ip]),
+        "qlskum_batch_set_launch_config": (i, [H, i, i, i]),
         "qlskum_partition_plan": (i, [C.POINTER(CloudStruct), i, ip, ip, ip]),
         "qlskum_partition_plan_lists": (i, [C.POINTER(CloudStruct), i, i, ip, ip]),
         "qlskum_partition_create": (i, [C.POINTER(CloudStruct), C.POINTER(ParamsStruct), i, C.POINTER(H)]),
@@ -322,12 +328,17 @@ class Solver:
     def launch_config(self) -> dict:
         v = [C.c_int() for _ in range(4)]
         self._ck(self._L.qlskum_get_launch_config(self._h, *[C.byref(t) for t in v]))
+        ln = [C.c_int() for _ in range(2)]
+        self._ck(self._L.qlskum_get_lanes(self._h, C.byref(ln[0]), C.byref(ln[1])))
         return {"flux_block": v[0].value, "flux_min_blocks": v[1].value, "point_block": v[2].value,
-                "gather_depth": v[3].value, "flux_variant": int(self._L.qlskum_get_flux_variant(self._h))}
+                "gather_depth": v[3].value, "flux_variant": int(self._L.qlskum_get_flux_variant(self._h)),
+                "point_lanes": ln[0].value, "flux_lanes": ln[1].value}
 
-    def set_launch_config(self, flux_variant=0, point_block=128, staged=0):
+    def set_launch_config(self, flux_variant=0, point_block=128, staged=0, point_lanes=1):
         """Pin the mixed form's launch shape (no autotuning)."""
         self._ck(self._L.qlskum_set_launch_config(self._h, int(flux_variant), int(point_block), int(staged)))
+        if point_lanes != 1:
+            self._ck(self._L.qlskum_set_point_lanes(self._h, int(point_lanes)))
 
     KERNELS = ("gradient", "inner", "flux_update", "reduce")
 
@@ -386,6 +397,14 @@ class Solver:
         out = np.empty((self.n, 4))
         self._ck(self._L.qlskum_residual_forward(self._h, _dp(a), _dp(out)))
         return out
+
+    def residual_device(self, prim_ptr: int, out_ptr: int, stream: int = 0):
+        """R(prim) on device buffers (double [n, 4], cloud order), ordered on `stream`."""
+        self._ck(self._L.qlskum_residual_forward_device(self._h, prim_ptr, out_ptr, stream or None))
+
+    def residual_vjp_device(self, prim_ptr: int, bar_ptr: int, out_ptr: int, stream: int = 0):
+        """(dR/dprim)^T bar on device buffers (double [n, 4], cloud order), ordered on `stream`."""
+        self._ck(self._L.qlskum_residual_vjp_device(self._h, prim_ptr, bar_ptr, out_ptr, stream or None))
 
     def residual_vjp(self, prim, bar_res, wall=False):
         """(dR/dprim)^T bar_res at prim; with wall=True also
@@ -515,8 +534,13 @@ class Batch:
     def tuning(self) -> dict:
         v = [C.c_int() for _ in range(4)]
         self._ck(self._L.qlskum_batch_tuning(self._h, *[C.byref(t) for t in v]))
+        ln = [C.c_int() for _ in range(2)]
+        self._ck(self._L.qlskum_batch_lanes(self._h, C.byref(ln[0]), C.byref(ln[1])))
         return {"tile": v[0].value, "flux_tile": v[1].value, "flux_min_blocks": v[2].value,
-                "points_per_warp": v[3].value}
+                "points_per_warp": v[3].value, "point_lanes": ln[0].value, "flux_lanes": ln[1].value}
+
+    def set_launch_config(self, tile, point_lanes, flux_variant):
+        self._ck(self._L.qlskum_batch_set_launch_config(self._h, int(tile), int(point_lanes), int(flux_variant)))
 
 
 def partition_plan(cloud, n_parts):

@@ -173,14 +173,24 @@ long long qlskum_launch_count(const qlskum_handle *h);
 qlskum_status qlskum_get_launch_config(qlskum_handle *h, int *flux_block, int *flux_min_blocks, int *point_block,
                                        int *gather_depth);
 /* Pin the mixed form's launch shape instead of autotuning it: flux_variant in
- * 0 .. 7 (threads x min blocks 128x4, 128x5, 64x8, 256x2 with one gather per
+ * 0 .. 9 (threads x min blocks 128x4, 128x5, 64x8, 256x2 with one gather per
  * edge in turn; 128x4, 128x5, 64x8, 256x2 with the next edge's neighbour data
- * in flight by cp.async), point_block one of
+ * in flight by cp.async; 128x4 with 2 lanes per point, 256x2 with 4 lanes per
+ * point, a point's edges split over its lanes and their sums combined by
+ * warp shuffles), point_block one of
  * 64 / 128 / 256 / 512 for the per-edge gather form, staged 0 (that form) or
  * 1 .. 4 (staged gathers: 128 threads depth 2, 128 / 4, 256 / 3, 64 / 4).
+ * The gradient / inner-loop kernels go back to one lane per point.
  * QLSKUM_ERR_UNSUPPORTED if a staged variant does not fit the device's
  * shared memory for this cloud's neighbour count. */
 qlskum_status qlskum_set_launch_config(qlskum_handle *h, int flux_variant, int point_block, int staged);
+/* Lanes per point (1, 2 or 4) of the mixed gradient / inner-loop kernels in
+ * the per-edge gather form (staged 0): a point's edges split over adjacent
+ * lanes, their sums, maxima and minima combined with warp shuffles.  The
+ * autotuner picks it together with point_block unless it is set. */
+qlskum_status qlskum_set_point_lanes(qlskum_handle *h, int lanes);
+/* Lanes per point in use: gradient / inner-loop kernels and the fused flux kernel. */
+qlskum_status qlskum_get_lanes(const qlskum_handle *h, int *point_lanes, int *flux_lanes);
 /* The flux_variant in use (as qlskum_set_launch_config numbers them; 0 for FP64 handles). */
 int qlskum_get_flux_variant(const qlskum_handle *h);
 
@@ -224,9 +234,16 @@ long long qlskum_batch_launch_count(const qlskum_batch *b);
 void *qlskum_batch_stream(qlskum_batch *b);
 /* The autotuned launch shape: points per tile of the gradient / inner-loop
  * kernels, points per tile and minimum resident blocks per SM of the flux
- * kernel, points per warp (one thread per point: 32). */
+ * kernel, points per warp of the flux kernel (32 / its lanes per point). */
 qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_tile, int *flux_min_blocks,
                                   int *points_per_warp);
+/* Lanes per point (1, 2 or 4) of the gradient / inner-loop kernels and of the flux kernel. */
+qlskum_status qlskum_batch_lanes(const qlskum_batch *b, int *point_lanes, int *flux_lanes);
+/* Pin the batch's launch shape instead of autotuning it: tile (64, 128, 256
+ * points) and lanes per point of the gradient / inner-loop kernels, and the
+ * flux variant 0 .. 5 (points per tile x min blocks x lanes: 128x4x1,
+ * 128x5x1, 64x8x1, 256x2x1, 64x4x2, 64x2x4). */
+qlskum_status qlskum_batch_set_launch_config(qlskum_batch *b, int tile, int point_lanes, int flux_variant);
 
 /* ------------------------------------------- partitions with a ghost-point halo */
 
@@ -355,6 +372,14 @@ qlskum_status qlskum_residual_forward(qlskum_handle *h, const double *prim, doub
  * of qlskum_residual_forward, for an autograd.Function's backward. */
 qlskum_status qlskum_residual_vjp(qlskum_handle *h, const double *prim, const double *bar_flux_res,
                                   double *bar_prim);
+/* The same pair on device buffers (double [n][4] in the cloud's point order,
+ * 32-byte aligned), for callers whose state already lives on the GPU (a
+ * PyTorch graph): the work is ordered after what `stream` (a cudaStream_t, or
+ * NULL for the legacy stream) has queued, and the results are ready for what
+ * `stream` queues next; no host copy, no host synchronisation. */
+qlskum_status qlskum_residual_forward_device(qlskum_handle *h, const double *prim, double *flux_res, void *stream);
+qlskum_status qlskum_residual_vjp_device(qlskum_handle *h, const double *prim, const double *bar_flux_res,
+                                         double *bar_prim, void *stream);
 /* The same VJP with the bars of the case parameters and of the geometry:
  * bar_params (double [2] or NULL) = d/dMach, d/dAoA of bar_flux_res . R,
  * which are zero (R reads no free-stream quantity; Mach and AoA enter the

@@ -130,6 +130,26 @@ def test_autograd_function_matches_vjp(qlskum):
     np.testing.assert_allclose(p.grad.numpy(), ref, rtol=0, atol=1e-13 * np.abs(ref).max())
 
 
+def test_autograd_function_on_cuda_tensors(qlskum):
+    """CUDA tensors take the device-buffer pair (no host copy, ordered on the
+    current torch stream) and give what the host-buffer pair gives."""
+    torch = pytest.importorskip("torch")
+    from qlskum.autograd import flux_residual
+    c = _cloud()
+    s = qlskum.Solver(c, mach=MACH, aoa=AOA, inner_iterations=1, **KW)
+    s.q_lskum(5)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        p = torch.tensor(s.prim, dtype=torch.float64, device="cuda", requires_grad=True)
+        w = torch.randn(c.n, 4, dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(0))
+        R = flux_residual(p, s)
+        (R * w).sum().backward()
+        got_R, got_g = R.detach().cpu().numpy(), p.grad.cpu().numpy()
+    np.testing.assert_array_equal(got_R, s.residual(s.prim))
+    ref = s.residual_vjp(s.prim, w.cpu().numpy())
+    np.testing.assert_allclose(got_g, ref, rtol=0, atol=1e-13 * np.abs(ref).max())
+
+
 @pytest.mark.parametrize("which", ["cl", "cd"])
 def test_adjoint_mach_aoa_vs_oracle_fd(qlskum, oracle_mod, which):
     c = _cloud()

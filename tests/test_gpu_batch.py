@@ -54,7 +54,8 @@ def test_batch_tuning_and_graph_replay(qlskum):
     b = qlskum.Batch(clouds, CASES[:3], **KW)
     b.run(2)
     t = b.tuning()
-    assert t["tile"] in (64, 128, 256) and t["flux_tile"] in (64, 128, 256) and t["points_per_warp"] == 32
+    assert t["tile"] in (64, 128, 256) and t["flux_tile"] in (64, 128, 256)
+    assert t["points_per_warp"] == 32 // t["flux_lanes"] and t["point_lanes"] in (1, 2, 4)
     l0 = b.launches
     b.run(3)
     # per iteration: 4 x (gradient + 1 inner + flux) + reduce + counter
@@ -83,3 +84,22 @@ def test_batch_rejects_fp64_and_bad_case(qlskum):
     assert L.qlskum_batch_create(arr, 1, qlskum._ip(cc), qlskum._dp(mm), qlskum._dp(aa), 1, C.byref(p),
                                  C.byref(h)) == 5
     _ = keep
+
+
+@pytest.mark.parametrize("tile,point_lanes,flux_variant", [(64, 2, 4), (128, 4, 5), (256, 2, 0), (64, 4, 1)])
+def test_batch_lanes_per_point_match_one_lane(qlskum, tile, point_lanes, flux_variant):
+    """Batched kernels with 2 or 4 lanes per point (gradient / inner loop and
+    flux) against the one-lane batch: the same state to FP32 rounding."""
+    clouds = _clouds()
+    a = qlskum.Batch(clouds, CASES[:3], **KW)
+    a.set_launch_config(128, 1, 0)
+    a.run(5)
+    b = qlskum.Batch(clouds, CASES[:3], **KW)
+    b.set_launch_config(tile, point_lanes, flux_variant)
+    b.run(5)
+    t = b.tuning()
+    assert t["point_lanes"] == point_lanes and t["tile"] == tile
+    assert t["points_per_warp"] == 32 // {4: 2, 5: 4}.get(flux_variant, 1)
+    for k in range(3):
+        assert _close(b.prim(k), a.prim(k), 1e-5), k
+    np.testing.assert_allclose(b.residual_history(), a.residual_history(), rtol=1e-3)

@@ -61,7 +61,8 @@ def test_autotuner_shape_and_result(qlskum):
     b = qlskum.Solver(c, block_size=128, **kw)
     b.q_lskum(3)
     assert b.launch_config() == {"flux_block": 128, "flux_min_blocks": 4, "point_block": 128, "gather_depth": 0,
-                                 "flux_variant": 0}
+                                 "flux_variant": 0, "point_lanes": 1, "flux_lanes": 1}
+    assert cfg["point_lanes"] in (1, 2, 4) and cfg["flux_lanes"] in (1, 2, 4)
     assert _close(a.prim, b.prim, 1e-5)
     np.testing.assert_allclose(a.residual_history(), b.residual_history(), rtol=1e-3)
     c2 = qlskum.Solver(c, block_size=128, **kw)
@@ -87,6 +88,29 @@ def test_staged_gathers_bit_identical(qlskum, flux_variant, staged):
         b.set_launch_config(flux_variant, 128, staged)
         b.q_lskum(4)
         assert (b.launch_config()["gather_depth"] > 0) == (staged > 0)
+        assert _close(b.prim, a.prim, 1e-5), power
+        np.testing.assert_allclose(a.residual_history(), b.residual_history(), rtol=1e-3)
+
+
+@pytest.mark.parametrize("flux_variant,point_lanes", [(8, 1), (9, 1), (0, 2), (0, 4), (8, 2), (9, 4)])
+def test_lanes_per_point_match_one_lane(qlskum, flux_variant, point_lanes):
+    """2 or 4 lanes per point (a point's edges split over adjacent lanes,
+    their sums, maxima and minima combined with warp shuffles) give the
+    one-lane state to FP32 rounding (the sums run in another order), in the
+    flux kernel (variants 8, 9) and in the gradient / inner-loop kernels,
+    with and without unit weights."""
+    c = golden_cloud("cloud_c1")
+    for power in (0.0, 1.0):
+        kw = dict(mach=0.63, aoa=2.0, cfl=0.2, vl_const=50.0, power=power, inner_iterations=2,
+                  precision=qlskum.MIXED)
+        a = qlskum.Solver(c, **kw)
+        a.set_launch_config(0, 128, 0)
+        a.q_lskum(4)
+        b = qlskum.Solver(c, **kw)
+        b.set_launch_config(flux_variant, 128, 0, point_lanes=point_lanes)
+        b.q_lskum(4)
+        cfg = b.launch_config()
+        assert cfg["point_lanes"] == point_lanes and cfg["flux_lanes"] == {8: 2, 9: 4}.get(flux_variant, 1)
         assert _close(b.prim, a.prim, 1e-5), power
         np.testing.assert_allclose(a.residual_history(), b.residual_history(), rtol=1e-3)
 
