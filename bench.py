@@ -235,6 +235,16 @@ def measured_profile(workload, precision, kernel, key="traffic"):
     return family if family else (None, None)
 
 
+def flux_kernel_form(variant: int) -> str:
+    """Kernel name of a mixed flux_variant (as qlskum_set_launch_config numbers
+    them): 4..7 staged gathers, 10..13 register prefetch, else per-edge gathers."""
+    if 4 <= variant <= 7:
+        return "k_flux_update_st"
+    if 10 <= variant <= 13:
+        return "k_flux_update_rp"
+    return "k_flux_update"
+
+
 def measured_traffic(workload, precision, kernel):
     return measured_profile(workload, precision, kernel, "traffic")
 
@@ -714,7 +724,7 @@ def main():
     nbytes = pbytes["flux_update"]
     achieved = nbytes / (fl_ms / fl_n / 1e3) / 1e9
     lc = solver.launch_config()
-    kname = (f"k_flux_update{'_st' if lc['flux_variant'] >= 4 else ''}<{lc['flux_block']},{lc['flux_min_blocks']}>"
+    kname = (f"{flux_kernel_form(lc['flux_variant'])}<{lc['flux_block']},{lc['flux_min_blocks']}>"
              if prec == qlskum.MIXED else "k_flux_update<128>")
     traffic, traffic_kernel = measured_traffic(args.workload, args.precision, kname)
     # every per-stage kernel against HBM (event-timed launches, compulsory bytes)

@@ -41,6 +41,16 @@ __device__ __forceinline__ float d2f(double x)
     return __uint_as_float(b);
 }
 
+// Two consecutive float4 (32 bytes) in one 256-bit load through the
+// read-only path (sm_100 and later); p must be 32-byte aligned and the data
+// must not be written while the kernel runs.
+__device__ __forceinline__ void ldg_2x4(const float4 *p, float4 &a, float4 &b)
+{
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void cp_async16(void *dst, const void *src)

@@ -1,20 +1,25 @@
 // Mixed-precision kernels: q variables, the Venkatakrishnan limiter, the
 // reconstruction and the kinetic split fluxes in FP32; the 2x2
-// least-squares solves (their determinants are near-singular on anisotropic
-// wall stencils: the gradient's on the device, the flux's folded into
-// per-edge weights on the host), the flux residual's time-step scaling, the
-// SSPRK update and the residual sum in FP64.  Same algorithm, edge order and data layout as the FP64 kernels
+// least-squares solves in FP64 (their determinants are near-singular on
+// anisotropic wall stencils), folded on the host into per-edge FP32 weights
+// for the gradient and for the four directional flux solves, so the
+// near-singular inverses never meet FP32 arithmetic; the state and its
+// accumulation over the SSPRK stages in FP64, and the residual norm summed
+// in FP64.  Same algorithm, edge order and data layout as the FP64 kernels
 // (qlskum_fp64.cu); q, dq and qm are stored in FP32, which halves the bytes
-// gathered per neighbour.  Built with FMA contraction on.
+// gathered per neighbour.  Built with FMA contraction and FP32
+// flush-to-zero on.
 //
 // On GB300 FP64 runs at about 1/64 of the FP32 rate, so the O(points) FP64
-// work is kept to a minimum: the four directional solves are linear in the
-// edge sums and are folded, in FP64 on the host, into one weight per edge and
-// half-range (DevCloud::e_w32), so the near-singular inverses never meet FP32
-// arithmetic and the kernel adds weighted flux differences; the
-// conserved-variable update has no FP64 division (one reciprocal from an FP32
-// seed and two Newton steps), and the local time step and its wave speed are
-// FP32 (they only set the pseudo-time step, not the steady state).
+// work is kept to a minimum: the kernels add weighted flux differences
+// (the folded solves); an interior point's stage change is formed in FP32
+// (every term a product of the state and a change, so FP32 keeps the
+// change to the relative precision F has) and added to the FP64 state; the
+// wall and outer points (a few thousand, in warps of their own class) take
+// the reference's conserved-variable update in FP64 with no FP64 division
+// (one reciprocal from an FP32 seed and two Newton steps); the local time
+// step and its wave speed are FP32 (they only set the pseudo-time step, not
+// the steady state).
 #include "qlskum_math.cuh"
 #include "qlskum_dev.cuh"
 
@@ -540,35 +545,145 @@ __device__ __forceinline__ void edge_geo(const DevCloud &c, long long e, float4 
     w = c.e_w32[e];
 }
 
+// The SSPRK stage of an interior point (state_update_mod.h:173-232) as an
+// FP32 increment added to the FP64 state.  The reference turns the state
+// into conserved variables in the point's (t, n) frame, subtracts F / 2
+// (stage 3: 2/3 U_old + 1/3 (U - F / 2)), turns back and divides out rho.
+// The same map, written for the change of the state:
+//   dU = -F / 2, or 2/3 (U_old - U) - F / 6 in stage 3, F turned back to
+//   (x, y) (the frame rotation is linear, so only F needs it);
+//   rho' = rho + dU0,  u' = u + (dU12 - u dU0) / rho',
+//   p' = p + 0.4 (dU3 - (dU0 |u'|^2 + rho (u' + u).(u' - u)) / 2),
+// with U_old - U from the FP64 differences of the primitive states:
+//   rho_o u_o - rho u = (rho_o - rho) u_o + rho (u_o - u),
+//   E_o - E = 2.5 (p_o - p) + ((rho_o - rho) |u_o|^2 + rho (u_o + u).(u_o - u)) / 2.
+// Every term is a product of a state value and a change, so FP32 carries
+// the change to FP32's relative precision (the precision F itself has);
+// the state accumulates in FP64 (prim + change), so changes far below the
+// state's own size are not lost.  Returns res_sqr = dU0^2.
+__device__ __forceinline__ float interior_stage(const float acc[4], float dl, float nx, float ny, const double P[4],
+                                                const double4_32a *__restrict__ prim_old_i, int rk, double Pn[4])
+{
+    const float F0 = dl * acc[0], Ft = dl * acc[1], Fn = dl * acc[2], F3 = dl * acc[3];
+    const float Fx = fmaf(Ft, ny, Fn * nx), Fy = fmaf(Fn, ny, -Ft * nx);
+    const float rho = d2f(P[0]), u1 = d2f(P[1]), u2 = d2f(P[2]);
+    float dU0, dU1, dU2, dU3;
+    if (rk != 3) {
+        dU0 = -0.5f * F0;
+        dU1 = -0.5f * Fx;
+        dU2 = -0.5f * Fy;
+        dU3 = -0.5f * F3;
+    } else {
+        double Po[4];
+        ld4(*prim_old_i, Po);
+        const float dr = d2f(Po[0] - P[0]), da = d2f(Po[1] - P[1]), db = d2f(Po[2] - P[2]),
+                    dp = d2f(Po[3] - P[3]);
+        const float uo1 = u1 + da, uo2 = u2 + db;
+        const float W1 = fmaf(dr, uo1, rho * da), W2 = fmaf(dr, uo2, rho * db);
+        const float W3 = fmaf(2.5f, dp, 0.5f * fmaf(dr, fmaf(uo1, uo1, uo2 * uo2),
+                                                    rho * fmaf(uo1 + u1, da, (uo2 + u2) * db)));
+        const float tt = 2.0f / 3.0f, s6 = -1.0f / 6.0f;
+        dU0 = fmaf(tt, dr, s6 * F0);
+        dU1 = fmaf(tt, W1, s6 * Fx);
+        dU2 = fmaf(tt, W2, s6 * Fy);
+        dU3 = fmaf(tt, W3, s6 * F3);
+    }
+    const float rn = rho + dU0;
+    const float ir = __fdividef(1.0f, rn);
+    const float du1 = fmaf(-u1, dU0, dU1) * ir, du2 = fmaf(-u2, dU0, dU2) * ir;
+    const float un1 = u1 + du1, un2 = u2 + du2;
+    const float kin = fmaf(dU0, fmaf(un1, un1, un2 * un2), rho * fmaf(u1 + un1, du1, (u2 + un2) * du2));
+    const float dpr = 0.4f * fmaf(-0.5f, kin, dU3);
+    Pn[0] = P[0] + f2d(dU0);
+    Pn[1] = P[1] + f2d(du1);
+    Pn[2] = P[2] + f2d(du2);
+    Pn[3] = P[3] + f2d(dpr);
+    return dU0 * dU0;
+}
+
 // F = delta * acc (the weighted sum of the folded solves, flux_residual_mod.h
-// with the wall's 2 delta) in FP64, then the SSPRK stage, q and the wave
-// speed of the new state.  Returns res_sqr.
-__device__ __forceinline__ double flux_tail(const CaseConst &K, int i, int f, double2 nn, const float acc[4],
-                                            const float *__restrict__ delta, const double4_32a *__restrict__ prim,
-                                            const double4_32a *__restrict__ prim_old,
-                                            double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
-                                            float *__restrict__ cs_next, int rk, float4 *__restrict__ acc_out)
+// with the wall's 2 delta), then the SSPRK stage, q and the wave speed of the
+// new state: interior points by the increment form above; wall and outer
+// points (a few thousand, in warps of their own class) in FP64 as the
+// reference writes it.  Returns res_sqr.
+__device__ __forceinline__ float flux_tail(const CaseConst &K, int i, int f, double2 nn, float nx, float ny,
+                                           const float acc[4], const float *__restrict__ delta,
+                                           const double4_32a *__restrict__ prim,
+                                           const double4_32a *__restrict__ prim_old,
+                                           double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
+                                           float *__restrict__ cs_next, int rk, float4 *__restrict__ acc_out)
 {
     if (acc_out) acc_out[i] = mk4(acc);
-    const double dl = f2d(delta[i]);
-    double F[4], P[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) F[r] = dl * f2d(acc[r]);
+    double P[4];
     ld4(prim[i], P);
-    const double r2 = stage_update_fast(K, f, nn.x, nn.y, P, prim_old + i, F, rk);
-    prim_next[i] = mk4(P);
-    float Q[4];
-    q_of(P, Q);
+    float Q[4], cs, r2;
+    // q and the wave speed come from the stored FP64 state, as k_derived
+    // forms them, so that a run restarted from a stored state continues
+    // bit for bit
+    if (f == kInterior) {
+        double Pn[4];
+        r2 = interior_stage(acc, delta[i], nx, ny, P, prim_old + i, rk, Pn);
+        prim_next[i] = mk4(Pn);
+        q_of(Pn, Q);
+        cs = wave_speed32(Pn);
+    } else {
+        const double dl = f2d(delta[i]);
+        double F[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) F[r] = dl * f2d(acc[r]);
+        r2 = d2f(stage_update_fast(K, f, nn.x, nn.y, P, prim_old + i, F, rk));
+        prim_next[i] = mk4(P);
+        q_of(P, Q);
+        cs = wave_speed32(P);
+    }
     q_next[i] = mk4(Q);
-    if (cs_next) cs_next[i] = wave_speed32(P);
+    if (cs_next) cs_next[i] = cs;
     return r2;
 }
 
+// Deterministic block reduction (sum and max) of the points' res_sqr, given
+// in FP32: the sum in FP64 (each value widened exactly, the warp's 32 by
+// butterfly shuffles, the warps' partial sums in a fixed order by the
+// block's first thread), the maximum in FP32.  Every thread of the block
+// calls it.
+template <int BLOCK>
+__device__ __forceinline__ void block_sum_max32(float v, double *out_sum, double *out_max)
+{
+    __shared__ double ss[BLOCK / 32];
+    __shared__ float sm[BLOCK / 32];
+    double s = f2d(v);
+    float m = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        ss[w] = s;
+        sm[w] = m;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = ss[0];
+        float mm = sm[0];
+#pragma unroll
+        for (int k = 1; k < BLOCK / 32; k++) {
+            t += ss[k];
+            mm = fmaxf(mm, sm[k]);
+        }
+        *out_sum = t;
+        *out_max = f2d(mm);
+    }
+    // a persistent block's next tile writes ss / sm again
+    __syncthreads();
+}
+
 // Fused stage of one point: FP32 edge work with the FP64-folded solve
-// weights, FP64 residual scaling and update.
+// weights, then the stage update (flux_tail).
 // Returns the point's res_sqr.
 template <bool UW, int L = 1>
-__device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst &K, int i,
+__device__ __forceinline__ float flux_point(const DevCloud &c, const CaseConst &K, int i,
                                              const float4 *__restrict__ q, const float4 *__restrict__ dq,
                                              const float4 *__restrict__ qm, const float *__restrict__ delta,
                                              const double4_32a *__restrict__ prim,
@@ -615,9 +730,9 @@ __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst 
         const unsigned m = group_mask<L>();
 #pragma unroll
         for (int r = 0; r < 4; r++) acc[r] = group_sum<L>(acc[r], m);
-        if (sub != 0) return 0.0;
+        if (sub != 0) return 0.0f;
     }
-    return flux_tail(K, i, f, nn, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
+    return flux_tail(K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
 }
 
 // The same with the next edge's gathers in flight during the current edge's
@@ -627,7 +742,7 @@ __device__ __forceinline__ double flux_point(const DevCloud &c, const CaseConst 
 // loaded one edge earlier still, and its streamed edge data one edge ahead
 // into registers.  Same arithmetic in the same edge order as flux_point.
 template <int B, bool UW>
-__device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseConst &K, int i, int t,
+__device__ __forceinline__ float flux_point_st(const DevCloud &c, const CaseConst &K, int i, int t,
                                                 float4 *ring, float *reps, const float4 *__restrict__ q,
                                                 const float4 *__restrict__ dq, const float4 *__restrict__ qm,
                                                 const float *__restrict__ delta,
@@ -698,7 +813,94 @@ __device__ __forceinline__ double flux_point_st(const DevCloud &c, const CaseCon
         const float e2k = reps[(j & 1) * B + t];
         flux_edge(c, e, f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, w, dir, qk, dxk, dyk, mxk, mnk, e2k, acc);
     }
-    return flux_tail(K, i, f, nn, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
+    return flux_tail(K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
+}
+
+// Neighbour data of one edge end: q, the gradient (x, y) and the neighbour
+// max / min, each pair of float4 in one 32-byte load, and the limiter's eps^2.
+struct NbrData {
+    float4 q, dx, dy, mx, mn;
+    float e2;
+};
+
+__device__ __forceinline__ void load_nbr(const DevCloud &c, int k, const float4 *__restrict__ q,
+                                         const float4 *__restrict__ dq, const float4 *__restrict__ qm, NbrData &d)
+{
+    d.q = q[k];
+    ldg_2x4(dq + 2 * k, d.dx, d.dy);
+    ldg_2x4(qm + 2 * k, d.mx, d.mn);
+    d.e2 = c.eps2_32[k];
+}
+
+// The same edge walk with the next edge's gathers in registers: edge j + 1's
+// neighbour data (three loads: q, and the gradient and max / min as 32-byte
+// pairs) and streamed edge data are loaded while edge j is evaluated, the
+// neighbour index one edge earlier still.  No shared memory: the L1 data
+// path carries only the gathers themselves.  Same arithmetic in the same
+// edge order as flux_point.  dq and qm must be 32-byte aligned per point
+// (two float4 per point from an aligned base).
+template <bool UW>
+__device__ __forceinline__ float flux_point_rp(const DevCloud &c, const CaseConst &K, int i,
+                                               const float4 *__restrict__ q, const float4 *__restrict__ dq,
+                                               const float4 *__restrict__ qm, const float *__restrict__ delta,
+                                               const double4_32a *__restrict__ prim,
+                                               const double4_32a *__restrict__ prim_old,
+                                               double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
+                                               float *__restrict__ cs_next, int rk, float4 *__restrict__ acc_out)
+{
+    const int f = c.flag[i];
+    const double2 nn = c.nrm[i];
+    const float nx = d2f(nn.x), ny = d2f(nn.y);
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    NbrData nd;
+    float4 gn = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 wn = make_float2(0.f, 0.f);
+    unsigned dn = 0;
+    int kn = 0;
+    if (nb > 0) {
+        load_nbr(c, c.e_nbr[base], q, dq, qm, nd);
+        edge_geo<UW>(c, base, gn, wn);
+        dn = c.e_dir[base];
+    }
+    if (nb > 1) kn = c.e_nbr[base + 32];
+    NbrData me;
+    load_nbr(c, i, q, dq, qm, me);
+    float qi[4], dxi[4], dyi[4], mxi[4], mni[4];
+    ld4(me.q, qi);
+    ld4(me.dx, dxi);
+    ld4(me.dy, dyi);
+    ld4(me.mx, mxi);
+    ld4(me.mn, mni);
+    // the owner end's limiter reads qmax - q and qmin - q (flux_edge)
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        mxi[r] -= qi[r];
+        mni[r] -= qi[r];
+    }
+    const float e2i = me.e2;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const NbrData cur = nd;
+        const float4 g = gn;
+        const float2 w = wn;
+        const unsigned dir = dn;
+        if (j + 1 < nb) {
+            load_nbr(c, kn, q, dq, qm, nd);
+            edge_geo<UW>(c, e + 32, gn, wn);
+            dn = c.e_dir[e + 32];
+        }
+        if (j + 2 < nb) kn = c.e_nbr[e + 64];
+        float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
+        ld4(cur.q, qk);
+        ld4(cur.dx, dxk);
+        ld4(cur.dy, dyk);
+        ld4(cur.mx, mxk);
+        ld4(cur.mn, mnk);
+        flux_edge(c, e, f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, w, dir, qk, dxk, dyk, mxk, mnk, cur.e2, acc);
+    }
+    return flux_tail(K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
 }
 
 // ---------------------------------------------------- single-case kernels
@@ -736,11 +938,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update(DevCloud c, CaseCon
 {
     const int g = blockIdx.x * BLOCK + threadIdx.x;
     const int i = g / L;
-    double r2 = 0.0;
+    float r2 = 0.0f;
     if (i < c.n)
         r2 = flux_point<UW, L>(c, K, i, q, dq, qm, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out,
                                g % L);
-    if (psum) block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
+    if (psum) block_sum_max32<BLOCK>(r2, psum + blockIdx.x, pmax + blockIdx.x);
 }
 
 // Staged-gather form of k_flux_update; static shared ring of the block.
@@ -760,11 +962,31 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update_st(DevCloud c, Case
     __shared__ float reps[2 * BLOCK];
     const int t = threadIdx.x;
     const int i = blockIdx.x * BLOCK + t;
-    double r2 = 0.0;
+    float r2 = 0.0f;
     if (i < c.n)
         r2 = flux_point_st<BLOCK, UW>(c, K, i, t, ring, reps, q, dq, qm, delta, prim, prim_old, prim_next, q_next,
                                       cs_next, rk, acc_out);
-    if (psum) block_sum_max<BLOCK>(r2, r2, psum + blockIdx.x, pmax + blockIdx.x);
+    if (psum) block_sum_max32<BLOCK>(r2, psum + blockIdx.x, pmax + blockIdx.x);
+}
+
+// Register-prefetch form of k_flux_update (flux_point_rp).
+template <int BLOCK, int MINB, bool UW>
+__global__ void __launch_bounds__(BLOCK, MINB) k_flux_update_rp(DevCloud c, CaseConst K, const float4 *__restrict__ q,
+                                                          const float4 *__restrict__ dq,
+                                                          const float4 *__restrict__ qm,
+                                                          const float *__restrict__ delta,
+                                                          const double4_32a *__restrict__ prim,
+                                                          const double4_32a *__restrict__ prim_old,
+                                                          double4_32a *__restrict__ prim_next,
+                                                          float4 *__restrict__ q_next, float *__restrict__ cs_next,
+                                                          int rk, double *__restrict__ psum,
+                                                          double *__restrict__ pmax, float4 *__restrict__ acc_out)
+{
+    const int i = blockIdx.x * BLOCK + threadIdx.x;
+    float r2 = 0.0f;
+    if (i < c.n)
+        r2 = flux_point_rp<UW>(c, K, i, q, dq, qm, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
+    if (psum) block_sum_max32<BLOCK>(r2, psum + blockIdx.x, pmax + blockIdx.x);
 }
 
 // ------------------------------------------------------- batched kernels
@@ -849,14 +1071,14 @@ __global__ void __launch_bounds__(TILE * L, MINB) kb_flux_update(const DevCloud 
         const BatchTile T = tiles[t];
         const BatchCase &C = cases[T.cas];
         const int i = T.first + (int)threadIdx.x / L;
-        double r2 = 0.0;
+        float r2 = 0.0f;
         if (i < C.n) {
             const long long o = C.off;
             r2 = flux_point<UW, L>(clouds[C.cloud], C.K, i, q + o, dq + 2 * o, qm + 2 * o, delta + o, prim + o,
                                    prim_old + o, prim_next + o, q_next + o, cs_next ? cs_next + o : nullptr, rk,
                                    nullptr, (int)threadIdx.x % L);
         }
-        if (psum) block_sum_max<TILE * L>(r2, r2, psum + t, pmax + t);
+        if (psum) block_sum_max32<TILE * L>(r2, psum + t, pmax + t);
     }
 }
 
@@ -1003,12 +1225,12 @@ void q_inner(const Launch &L, const DevCloud &c, const float4 *dq0, const float4
 
 // Launch-shape variants of the fused kernel (threads per block, minimum
 // resident blocks per SM -> register cap; 4..7 the staged-gather form; 8, 9
-// the per-edge gather form with 2 / 4 lanes per point), picked by the host's
-// autotuner.
-const int kFluxVariants = 10;
-static const int kFluxBlock[kFluxVariants] = {128, 128, 64, 256, 128, 128, 64, 256, 128, 256};
-static const int kFluxMinBlocks[kFluxVariants] = {4, 5, 8, 2, 4, 5, 8, 2, 4, 2};
-static const int kFluxLanes[kFluxVariants] = {1, 1, 1, 1, 1, 1, 1, 1, 2, 4};
+// the per-edge gather form with 2 / 4 lanes per point; 10..13 the
+// register-prefetch form), picked by the host's autotuner.
+const int kFluxVariants = 14;
+static const int kFluxBlock[kFluxVariants] = {128, 128, 64, 256, 128, 128, 64, 256, 128, 256, 128, 128, 64, 256};
+static const int kFluxMinBlocks[kFluxVariants] = {4, 5, 8, 2, 4, 5, 8, 2, 4, 2, 4, 5, 6, 2};
+static const int kFluxLanes[kFluxVariants] = {1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 1, 1, 1, 1};
 
 int flux_variants() { return kFluxVariants; }
 int flux_block(int v) { return kFluxBlock[v]; }
@@ -1042,6 +1264,17 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
                                                                           prim_old, prim_next, q_next,     \
                                                                           cspeed_next, rk, R.partial_sum,  \
                                                                           R.partial_max, acc_out)
+#define QLSKUM_FLUX_RP(B, MB)                                                                               \
+    if (c.unit_w)                                                                                           \
+        k_flux_update_rp<B, MB, true><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,   \
+                                                                         prim_old, prim_next, q_next,      \
+                                                                         cspeed_next, rk, R.partial_sum,   \
+                                                                         R.partial_max, acc_out);          \
+    else                                                                                                    \
+        k_flux_update_rp<B, MB, false><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,  \
+                                                                          prim_old, prim_next, q_next,     \
+                                                                          cspeed_next, rk, R.partial_sum,  \
+                                                                          R.partial_max, acc_out)
     switch (variant) {
     case 1: QLSKUM_FLUX(128, 5); break;
     case 2: QLSKUM_FLUX(64, 8); break;
@@ -1052,11 +1285,16 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
     case 7: QLSKUM_FLUX_ST(256, 2); break;
     case 8: QLSKUM_FLUX_L(128, 4, 2); break;
     case 9: QLSKUM_FLUX_L(256, 2, 4); break;
+    case 10: QLSKUM_FLUX_RP(128, 4); break;
+    case 11: QLSKUM_FLUX_RP(128, 5); break;
+    case 12: QLSKUM_FLUX_RP(64, 6); break;
+    case 13: QLSKUM_FLUX_RP(256, 2); break;
     default: QLSKUM_FLUX(128, 4); break;
     }
 #undef QLSKUM_FLUX
 #undef QLSKUM_FLUX_L
 #undef QLSKUM_FLUX_ST
+#undef QLSKUM_FLUX_RP
     QLSKUM_LAUNCHED(L);
 }
 

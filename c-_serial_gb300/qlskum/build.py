@@ -54,7 +54,7 @@ def _cuda_include(nvcc: str) -> str:
 def sources():
     return {
         "qlskum_fp64.cu": ["-fmad=false"],
-        "qlskum_mixed.cu": ["-fmad=true"],
+        "qlskum_mixed.cu": ["-fmad=true", "-ftz=true"],
         "qlskum_noalloc.cu": ["-fmad=false"],
         "qlskum_adjoint.cu": [],
         "qlskum_host.cpp": [],
