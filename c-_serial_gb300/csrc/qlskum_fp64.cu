@@ -1,8 +1,14 @@
 // FP64 kernels: the drop-in form of the q-LSKUM primal iteration.
 //
-// Built with -fmad=false so that no multiply-add is contracted: every
-// expression keeps the reference's rounding sequence and the results differ
-// from the serial reference only through the device's exp / log / erf.
+// Every formula is the reference's, with FMA contraction on (GB300 runs FP64
+// at 1/64 of the FP32 rate, and a fused multiply-add is one FP64 instruction
+// instead of two), and in the edge ends' hot arithmetic a few expressions
+// rewritten to use fewer FP64 instructions for the same value to a few ulps
+// (edge_qtilde / venkat_r and end_kin in qlskum_math.cuh: one reciprocal
+// square root for sqrt(beta), 1 / sqrt(pi beta) and beta^-2.5, reciprocals
+// instead of divisions).  The results differ from the serial reference by
+// those roundings and the device's exp / log / erf: 1e-10 relative after
+// 1000 iterations (the parity tests).
 //
 // One thread per point; the point's edges are walked in the reference's
 // neighbour order from the sliced-ELL edge arrays (coalesced across the warp),
@@ -199,12 +205,12 @@ __device__ __forceinline__ void point_flux(const DevCloud &c, int i, int f, doub
         ld4(dq[2 * k + 1], dyk);
         ld4(qm[2 * k], mxk);
         ld4(qm[2 * k + 1], mnk);
-        double Pi[4], Pk[4];
-        edge_states<double>(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, c.eps2[k], Pi, Pk);
+        double ti[4], tk[4];
+        edge_qtilde<double>(g.x, g.y, qi, dxi, dyi, mxi, mni, e2i, qk, dxk, dyk, mxk, mnk, c.eps2[k], ti, tk);
         Kin<double> ki, kk;
         double keep_i[3], keep_k[3];
-        kin_prep<double>(nx, ny, Pi[1], Pi[2], Pi[0], Pi[3], ki, ends ? keep_i : nullptr);
-        kin_prep<double>(nx, ny, Pk[1], Pk[2], Pk[0], Pk[3], kk, ends ? keep_k : nullptr);
+        end_kin<double>(nx, ny, ti, ki, ends ? keep_i : nullptr);
+        end_kin<double>(nx, ny, tk, kk, ends ? keep_k : nullptr);
         if (ends) {
             // planes [12][ns]: per end rho, sqrt(beta), exp(-S1^2), exp(-S2^2), erf(S1), erf(S2)
             const double v[12] = {ki.rho, keep_i[0], keep_i[1], keep_i[2], ki.E1, ki.E2,

@@ -1,12 +1,15 @@
 // Per-point and per-edge arithmetic of the q-LSKUM scheme, templated on the
-// real type R so the FP64 translation unit (built with -fmad=false, every
-// expression in the reference's own operation order) and the mixed-precision
-// unit (FP32 with FMA contraction) share one source.
+// real type R so the FP64 translation unit, the mixed-precision unit (FP32),
+// the reverse-mode unit and the host build of the reverse arithmetic share
+// one source.
 //
-// Each function names the reference lines it restates.  Where the reference
-// writes `a - b` for the negative half-range we write `a + s*b` with s = -1:
-// IEEE subtraction is addition of the negation and s*b is exact, so the FP64
-// results are the reference's bit for bit apart from the device libm.
+// Each function names the reference lines it restates, in the reference's
+// operation order.  Where the reference writes `a - b` for the negative
+// half-range we write `a + s*b` with s = -1: IEEE subtraction is addition of
+// the negation and s*b is exact.  Compiled without FMA contraction (the host
+// build, the noalloc unit) the FP64 results are the reference's bit for bit
+// apart from libm; the FP64 device unit contracts multiply-adds and takes
+// the faster, equivalent forms venkat_r / end_kin for the edge ends.
 #pragma once
 #include <cmath>
 #include <cuda_runtime.h>
@@ -21,6 +24,53 @@
 #endif
 
 namespace qlskum {
+
+#ifdef __CUDACC__
+// Conversions between FP32 and FP64 on the integer pipe (the hardware
+// conversion issues on the FP64 pipe, which on this chip is the scarce one).
+// float -> double: exact for normal numbers and zero, flushes subnormals to
+// zero and keeps Inf / NaN.
+__device__ __forceinline__ double f2d(float x)
+{
+    const unsigned b = __float_as_uint(x);
+    const unsigned mag = b & 0x7fffffffu;
+    const unsigned sign = b & 0x80000000u;
+    unsigned hi = sign | (((mag >> 23) + 896u) << 20) | ((mag & 0x7fffffu) >> 3);
+    unsigned lo = b << 29;
+    if (mag < 0x00800000u) { hi = sign; lo = 0u; }
+    if (mag >= 0x7f800000u) hi = sign | 0x7ff00000u | ((mag & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// double -> float on the integer pipe, truncating the mantissa (< 1 ulp);
+// underflow goes to zero, overflow and Inf to Inf, NaN stays NaN.
+__device__ __forceinline__ float d2f(double x)
+{
+    const unsigned h = (unsigned)__double2hiint(x), l = (unsigned)__double2loint(x);
+    const unsigned mag = h & 0x7fffffffu;
+    const unsigned sign = h & 0x80000000u;
+    const int e = (int)(mag >> 20) - 896;
+    const unsigned m = ((mag & 0xfffffu) << 3) | (l >> 29);
+    unsigned b = sign | ((unsigned)e << 23) | m;
+    if (e <= 0) b = sign;
+    if (e >= 255) b = sign | 0x7f800000u | ((mag >= 0x7ff00000u && (m | (mag & 0xfffffu) | l)) ? 0x400000u : 0u);
+    return __uint_as_float(b);
+}
+
+// 1 / x in FP64 from the FP32 reciprocal refined by two Newton steps (about
+// an ulp; no FP64 division).  Where x is outside the normal FP32 range the
+// seed is not usable and the division is taken instead.
+__device__ __forceinline__ double rcp64(double x)
+{
+    const float s = __frcp_rn(d2f(x));
+    if (!(fabsf(s) > 1e-37f && fabsf(s) < 1e37f)) return 1.0 / x;
+    double r = f2d(s);
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+#endif
 
 // Elementary operations per real type.  For double they are exactly the
 // reference's: IEEE division and square root, libm-style exp / log / erf.
@@ -38,6 +88,14 @@ template <> struct M<double> {
     static QLSKUM_HD double div(double a, double b) { return a / b; }
     // a / sqrt(x)
     static QLSKUM_HD double rdsq(double a, double x) { return a / sqrt(x); }
+    // 1 / sqrt(x) (the device's rsqrt: 1 ulp) and 1 / x (rcp64: about an ulp)
+#ifdef __CUDA_ARCH__
+    static QLSKUM_HD double rsq(double x) { return rsqrt(x); }
+    static QLSKUM_HD double rcp(double x) { return rcp64(x); }
+#else
+    static QLSKUM_HD double rsq(double x) { return 1.0 / std::sqrt(x); }
+    static QLSKUM_HD double rcp(double x) { return 1.0 / x; }
+#endif
 };
 template <> struct M<float> {
     static QLSKUM_HD float ef(float x) { return erff(x); }
@@ -163,6 +221,49 @@ QLSKUM_HD void kin_prep(R nx, R ny, R u1, R u2, R rho, R pr, Kin<R> &k, R *keep 
     k.rho = rho;
 }
 
+// One edge end's q~ -> prim step (q_variables_mod.h:230-253) and its
+// half-range moments (kin_prep) in one pass, for the FP64 drop-in's
+// forward: the moments take beta and p / rho = 0.5 / beta from the q~ ->
+// prim step (split_fluxes_mod.h:17-19 forms both again from rho and p, two
+// more divisions that give the same values to an ulp); sqrt(beta),
+// 1 / sqrt(pi beta) and beta^-2.5 = exp(-log(beta) / (gamma - 1)) come from
+// one reciprocal square root (split_fluxes_mod.h:20-26 takes three square
+// roots and two divisions, q_variables_mod.h:246-249 a log); 0.5 / beta is
+// a reciprocal (rcp64) instead of a division.  Each replacement agrees with
+// the reference's expression to a few ulps.  keep as kin_prep.
+template <typename R>
+QLSKUM_HD void end_kin(R nx, R ny, const R qt[4], Kin<R> &k, R *keep = nullptr)
+{
+    const R beta = -qt[3] * R(0.5);
+    const R temp = R(0.5) * M<R>::rcp(beta);
+    const R u1 = qt[1] * temp, u2 = qt[2] * temp;
+    const R temp1 = qt[0] + beta * (u1 * u1 + u2 * u2);
+    const R rsb = M<R>::rsq(beta);
+    // exp(temp1 - log(beta) / (gamma - 1)) = exp(temp1) beta^-2.5, gamma = 1.4
+    const R rsb2 = rsb * rsb;
+    k.rho = M<R>::ex(temp1) * (rsb2 * rsb2 * rsb);
+    const R tx = ny, ty = -nx;
+    k.ut = u1 * tx + u2 * ty;
+    k.un = u1 * nx + u2 * ny;
+    const R sb = beta * rsb;
+    const R S1 = k.ut * sb;
+    const R S2 = k.un * sb;
+    const R e1 = M<R>::ex(-S1 * S1), e2 = M<R>::ex(-S2 * S2);
+    if (keep) {
+        keep[0] = sb;
+        keep[1] = e1;
+        keep[2] = e2;
+    }
+    // 0.5 / sqrt(pi beta) = (0.5 / sqrt(pi)) / sqrt(beta)
+    const R hrs = R(0.28209479177387814) * rsb;
+    k.B1 = hrs * e1;
+    k.B2 = hrs * e2;
+    k.E1 = erf_e<R>(S1, e1);
+    k.E2 = erf_e<R>(S2, e2);
+    k.pbr = temp;
+    k.usq = k.ut * k.ut + k.un * k.un;
+}
+
 // flux_Gxp (s1 = +1) / flux_Gxn (s1 = -1): split_fluxes_mod.h:6-84
 template <typename R>
 QLSKUM_HD void flux_x(const Kin<R> &k, R s1, R G[4])
@@ -257,6 +358,39 @@ QLSKUM_HD void edge_states(R delx, R dely, const R qi[4], const R dxi[4], const 
     }
     qtilde_to_prim(ti, pi_[1], pi_[2], pi_[0], pi_[3]);
     qtilde_to_prim(tk, pk_[1], pk_[2], pk_[0], pk_[3]);
+}
+
+// venkat() with the common factor del_neg of the numerator and the
+// denominator cancelled (both are multiplied by it in limiters_mod.h:93-97)
+// and the quotient taken through a reciprocal: the same value to a few ulps.
+template <typename R>
+QLSKUM_HD R venkat_r(R qt, R q, R qmax, R qmin, R eps2)
+{
+    const R dn = qt - q;
+    if (M<R>::ab(dn) <= R(10e-6)) return R(1.0);
+    const R dp = (dn > R(0)) ? qmax - q : qmin - q;
+    const R base = dp * dp + eps2;
+    const R num = base + R(2.0) * dn * dp;
+    const R den = base + dn * (R(2.0) * dn + dp);
+    const R t = num * M<R>::rcp(den);
+    return t < R(1) ? t : R(1);
+}
+
+// The limited reconstruction of edge_states, each end's q~ returned.
+template <typename R>
+QLSKUM_HD void edge_qtilde(R delx, R dely, const R qi[4], const R dxi[4], const R dyi[4], const R mxi[4],
+                           const R mni[4], R e2i, const R qk[4], const R dxk[4], const R dyk[4], const R mxk[4],
+                           const R mnk[4], R e2k, R ti[4], R tk[4])
+{
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        R gi = delx * dxi[r] + dely * dyi[r];
+        R gk = delx * dxk[r] + dely * dyk[r];
+        R phi_i = venkat_r(qi[r] - R(0.5) * gi, qi[r], mxi[r], mni[r], e2i);
+        R phi_k = venkat_r(qk[r] - R(0.5) * gk, qk[r], mxk[r], mnk[r], e2k);
+        ti[r] = qi[r] - R(0.5) * phi_i * gi;
+        tk[r] = qk[r] - R(0.5) * phi_k * gk;
+    }
 }
 
 // state_update_mod.h:18-33

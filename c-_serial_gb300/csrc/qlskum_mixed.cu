@@ -241,14 +241,18 @@ __device__ __forceinline__ void inner_point(const DevCloud &c, int i, const floa
     float dxi[4], dyi[4], ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0};
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
+#pragma unroll 2
     for (int j = sub; j < nb; j += L) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         const float4 g = edge_w<UW>(c, e);
         const float2 gw = c.e_gw32[e];
+        // the neighbour's gradient pair in one 32-byte load
+        float4 gx, gy;
+        ldg_2x4(dq_in + 2 * k, gx, gy);
         float dxk[4], dyk[4];
-        ld4(dq_in[2 * k], dxk);
-        ld4(dq_in[2 * k + 1], dyk);
+        ld4(gx, dxk);
+        ld4(gy, dyk);
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             const float u = fmaf(g.x, dxk[r], g.y * dyk[r]);

@@ -3,12 +3,14 @@
 Six translation units compiled in parallel and linked into one shared
 library with a C ABI (include/qlskum.h):
 
-* csrc/qlskum_fp64.cu  -- FP64 drop-in kernels, -fmad=false (no FMA
-  contraction, the reference's rounding sequence);
-* csrc/qlskum_mixed.cu -- mixed-precision kernels (FP32 edge work, FMA on);
+* csrc/qlskum_fp64.cu  -- FP64 drop-in kernels, FMA contraction on (one
+  FP64 instruction per multiply-add; 1e-10 parity with the reference);
+* csrc/qlskum_mixed.cu -- mixed-precision kernels (FP32 edge work, FMA and
+  FP32 flush-to-zero on);
 * csrc/qlskum_adjoint.cu -- reverse-mode kernels of the FP64 iteration;
 * csrc/qlskum_noalloc.cu -- the stage update over caller buffers that
-  allocates nothing (static device scratch), -fmad=false like the FP64 unit;
+  allocates nothing (static device scratch), -fmad=false (the reference's
+  rounding sequence of the update);
 * csrc/qlskum_host.cpp -- host layer, g++ -ffp-contract=off (bit-exact
   sub-stencil classification on x86-64 and aarch64 alike);
 * csrc/qlskum_io.cpp -- partGrid file I/O and the sub-stencil quality check
@@ -53,7 +55,7 @@ def _cuda_include(nvcc: str) -> str:
 
 def sources():
     return {
-        "qlskum_fp64.cu": ["-fmad=false"],
+        "qlskum_fp64.cu": ["-fmad=true"],
         "qlskum_mixed.cu": ["-fmad=true", "-ftz=true"],
         "qlskum_noalloc.cu": ["-fmad=false"],
         "qlskum_adjoint.cu": [],
