@@ -907,6 +907,85 @@ __device__ __forceinline__ float flux_point_rp(const DevCloud &c, const CaseCons
     return flux_tail(K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
 }
 
+// A float4 from shared memory, read again at every use (volatile: not
+// hoisted out of the loop into registers).
+__device__ __forceinline__ void lds_v4(const float4 *p, float o[4])
+{
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(o[0]), "=f"(o[1]), "=f"(o[2]), "=f"(o[3])
+                 : "r"(smem_addr(p)));
+}
+
+// flux_point_rp with the owner's own data (q, gradient, qmax - q, qmin - q:
+// five float4) in the thread's slots of shared memory ([5][B], thread-minor,
+// conflict-free), read back at every edge instead of held in 20 registers
+// across the edge loop: fewer registers, so more resident warps.
+template <int B, bool UW>
+__device__ __forceinline__ float flux_point_rps(const DevCloud &c, const CaseConst &K, int i, int t, float4 *sown,
+                                                const float4 *__restrict__ q, const float4 *__restrict__ dq,
+                                                const float4 *__restrict__ qm, const float *__restrict__ delta,
+                                                const double4_32a *__restrict__ prim,
+                                                const double4_32a *__restrict__ prim_old,
+                                                double4_32a *__restrict__ prim_next, float4 *__restrict__ q_next,
+                                                float *__restrict__ cs_next, int rk, float4 *__restrict__ acc_out)
+{
+    const int f = c.flag[i];
+    const double2 nn = c.nrm[i];
+    const float nx = d2f(nn.x), ny = d2f(nn.y);
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    NbrData nd;
+    float4 gn = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 wn = make_float2(0.f, 0.f);
+    unsigned dn = 0;
+    int kn = 0;
+    if (nb > 0) {
+        load_nbr(c, c.e_nbr[base], q, dq, qm, nd);
+        edge_geo<UW>(c, base, gn, wn);
+        dn = c.e_dir[base];
+    }
+    if (nb > 1) kn = c.e_nbr[base + 32];
+    {
+        NbrData me;
+        load_nbr(c, i, q, dq, qm, me);
+        // the owner end's limiter reads qmax - q and qmin - q (flux_edge)
+        sown[t] = me.q;
+        sown[B + t] = me.dx;
+        sown[2 * B + t] = me.dy;
+        sown[3 * B + t] = make_float4(me.mx.x - me.q.x, me.mx.y - me.q.y, me.mx.z - me.q.z, me.mx.w - me.q.w);
+        sown[4 * B + t] = make_float4(me.mn.x - me.q.x, me.mn.y - me.q.y, me.mn.z - me.q.z, me.mn.w - me.q.w);
+    }
+    const float e2i = c.eps2_32[i];
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int j = 0; j < nb; j++) {
+        const long long e = base + 32LL * j;
+        const NbrData cur = nd;
+        const float4 g = gn;
+        const float2 w = wn;
+        const unsigned dir = dn;
+        if (j + 1 < nb) {
+            load_nbr(c, kn, q, dq, qm, nd);
+            edge_geo<UW>(c, e + 32, gn, wn);
+            dn = c.e_dir[e + 32];
+        }
+        if (j + 2 < nb) kn = c.e_nbr[e + 64];
+        float qi[4], dxi[4], dyi[4], mxi[4], mni[4];
+        lds_v4(sown + t, qi);
+        lds_v4(sown + B + t, dxi);
+        lds_v4(sown + 2 * B + t, dyi);
+        lds_v4(sown + 3 * B + t, mxi);
+        lds_v4(sown + 4 * B + t, mni);
+        float qk[4], dxk[4], dyk[4], mxk[4], mnk[4];
+        ld4(cur.q, qk);
+        ld4(cur.dx, dxk);
+        ld4(cur.dy, dyk);
+        ld4(cur.mx, mxk);
+        ld4(cur.mn, mnk);
+        flux_edge(c, e, f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, w, dir, qk, dxk, dyk, mxk, mnk, cur.e2, acc);
+    }
+    return flux_tail(K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
+}
+
 // ---------------------------------------------------- single-case kernels
 
 template <bool DT, int L>
@@ -990,6 +1069,29 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update_rp(DevCloud c, Case
     float r2 = 0.0f;
     if (i < c.n)
         r2 = flux_point_rp<UW>(c, K, i, q, dq, qm, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
+    if (psum) block_sum_max32<BLOCK>(r2, psum + blockIdx.x, pmax + blockIdx.x);
+}
+
+// Register-prefetch form with the owner's data in shared memory (flux_point_rps).
+template <int BLOCK, int MINB, bool UW>
+__global__ void __launch_bounds__(BLOCK, MINB) k_flux_update_rps(DevCloud c, CaseConst K, const float4 *__restrict__ q,
+                                                           const float4 *__restrict__ dq,
+                                                           const float4 *__restrict__ qm,
+                                                           const float *__restrict__ delta,
+                                                           const double4_32a *__restrict__ prim,
+                                                           const double4_32a *__restrict__ prim_old,
+                                                           double4_32a *__restrict__ prim_next,
+                                                           float4 *__restrict__ q_next, float *__restrict__ cs_next,
+                                                           int rk, double *__restrict__ psum,
+                                                           double *__restrict__ pmax, float4 *__restrict__ acc_out)
+{
+    __shared__ float4 sown[5 * BLOCK];
+    const int t = threadIdx.x;
+    const int i = blockIdx.x * BLOCK + t;
+    float r2 = 0.0f;
+    if (i < c.n)
+        r2 = flux_point_rps<BLOCK, UW>(c, K, i, t, sown, q, dq, qm, delta, prim, prim_old, prim_next, q_next,
+                                       cs_next, rk, acc_out);
     if (psum) block_sum_max32<BLOCK>(r2, psum + blockIdx.x, pmax + blockIdx.x);
 }
 
@@ -1230,11 +1332,12 @@ void q_inner(const Launch &L, const DevCloud &c, const float4 *dq0, const float4
 // Launch-shape variants of the fused kernel (threads per block, minimum
 // resident blocks per SM -> register cap; 4..7 the staged-gather form; 8, 9
 // the per-edge gather form with 2 / 4 lanes per point; 10..13 the
-// register-prefetch form), picked by the host's autotuner.
-const int kFluxVariants = 14;
-static const int kFluxBlock[kFluxVariants] = {128, 128, 64, 256, 128, 128, 64, 256, 128, 256, 128, 128, 64, 256};
-static const int kFluxMinBlocks[kFluxVariants] = {4, 5, 8, 2, 4, 5, 8, 2, 4, 2, 4, 5, 6, 2};
-static const int kFluxLanes[kFluxVariants] = {1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 1, 1, 1, 1};
+// register-prefetch form; 14, 15 the same with the owner's data in shared
+// memory), picked by the host's autotuner.
+const int kFluxVariants = 16;
+static const int kFluxBlock[kFluxVariants] = {128, 128, 64, 256, 128, 128, 64, 256, 128, 256, 128, 128, 64, 256, 128, 128};
+static const int kFluxMinBlocks[kFluxVariants] = {4, 5, 8, 2, 4, 5, 8, 2, 4, 2, 4, 5, 6, 2, 5, 6};
+static const int kFluxLanes[kFluxVariants] = {1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 1, 1, 1, 1, 1, 1};
 
 int flux_variants() { return kFluxVariants; }
 int flux_block(int v) { return kFluxBlock[v]; }
@@ -1279,6 +1382,17 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
                                                                           prim_old, prim_next, q_next,     \
                                                                           cspeed_next, rk, R.partial_sum,  \
                                                                           R.partial_max, acc_out)
+#define QLSKUM_FLUX_RPS(B, MB)                                                                              \
+    if (c.unit_w)                                                                                           \
+        k_flux_update_rps<B, MB, true><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,  \
+                                                                          prim_old, prim_next, q_next,     \
+                                                                          cspeed_next, rk, R.partial_sum,  \
+                                                                          R.partial_max, acc_out);         \
+    else                                                                                                    \
+        k_flux_update_rps<B, MB, false><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim, \
+                                                                           prim_old, prim_next, q_next,    \
+                                                                           cspeed_next, rk, R.partial_sum, \
+                                                                           R.partial_max, acc_out)
     switch (variant) {
     case 1: QLSKUM_FLUX(128, 5); break;
     case 2: QLSKUM_FLUX(64, 8); break;
@@ -1293,12 +1407,15 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
     case 11: QLSKUM_FLUX_RP(128, 5); break;
     case 12: QLSKUM_FLUX_RP(64, 6); break;
     case 13: QLSKUM_FLUX_RP(256, 2); break;
+    case 14: QLSKUM_FLUX_RPS(128, 5); break;
+    case 15: QLSKUM_FLUX_RPS(128, 6); break;
     default: QLSKUM_FLUX(128, 4); break;
     }
 #undef QLSKUM_FLUX
 #undef QLSKUM_FLUX_L
 #undef QLSKUM_FLUX_ST
 #undef QLSKUM_FLUX_RP
+#undef QLSKUM_FLUX_RPS
     QLSKUM_LAUNCHED(L);
 }
 

@@ -7,7 +7,8 @@ library with a C ABI (include/qlskum.h):
   FP64 instruction per multiply-add; 1e-10 parity with the reference);
 * csrc/qlskum_mixed.cu -- mixed-precision kernels (FP32 edge work, FMA and
   FP32 flush-to-zero on);
-* csrc/qlskum_adjoint.cu -- reverse-mode kernels of the FP64 iteration;
+* csrc/qlskum_adjoint.cu -- reverse-mode kernels of the FP64 and the mixed
+  iterations (FP32 flush-to-zero on, as in the mixed forward);
 * csrc/qlskum_noalloc.cu -- the stage update over caller buffers that
   allocates nothing (static device scratch), -fmad=false (the reference's
   rounding sequence of the update);
@@ -58,7 +59,7 @@ def sources():
         "qlskum_fp64.cu": ["-fmad=true"],
         "qlskum_mixed.cu": ["-fmad=true", "-ftz=true"],
         "qlskum_noalloc.cu": ["-fmad=false"],
-        "qlskum_adjoint.cu": [],
+        "qlskum_adjoint.cu": ["-ftz=true"],
         "qlskum_host.cpp": [],
         "qlskum_io.cpp": [],
     }
