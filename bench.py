@@ -237,11 +237,14 @@ def measured_profile(workload, precision, kernel, key="traffic"):
 
 def flux_kernel_form(variant: int) -> str:
     """Kernel name of a mixed flux_variant (as qlskum_set_launch_config numbers
-    them): 4..7 staged gathers, 10..13 register prefetch, else per-edge gathers."""
+    them): 4..7 staged gathers, 10..13 register prefetch, 14..18 register
+    prefetch with the owner's data in shared memory, else per-edge gathers."""
     if 4 <= variant <= 7:
         return "k_flux_update_st"
     if 10 <= variant <= 13:
         return "k_flux_update_rp"
+    if 14 <= variant <= 18:
+        return "k_flux_update_rps"
     return "k_flux_update"
 
 

@@ -920,7 +920,9 @@ __device__ __forceinline__ void lds_v4(const float4 *p, float o[4])
 // five float4) in the thread's slots of shared memory ([5][B], thread-minor,
 // conflict-free), read back at every edge instead of held in 20 registers
 // across the edge loop: fewer registers, so more resident warps.
-template <int B, bool UW>
+// PF false: the neighbour data is loaded at its edge, only the index and the
+// streamed edge data one edge ahead (fewer registers again).
+template <int B, bool UW, bool PF = true>
 __device__ __forceinline__ float flux_point_rps(const DevCloud &c, const CaseConst &K, int i, int t, float4 *sown,
                                                 const float4 *__restrict__ q, const float4 *__restrict__ dq,
                                                 const float4 *__restrict__ qm, const float *__restrict__ delta,
@@ -939,8 +941,10 @@ __device__ __forceinline__ float flux_point_rps(const DevCloud &c, const CaseCon
     float2 wn = make_float2(0.f, 0.f);
     unsigned dn = 0;
     int kn = 0;
+    int kc = 0;
     if (nb > 0) {
-        load_nbr(c, c.e_nbr[base], q, dq, qm, nd);
+        kc = c.e_nbr[base];
+        if (PF) load_nbr(c, kc, q, dq, qm, nd);
         edge_geo<UW>(c, base, gn, wn);
         dn = c.e_dir[base];
     }
@@ -959,12 +963,15 @@ __device__ __forceinline__ float flux_point_rps(const DevCloud &c, const CaseCon
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
-        const NbrData cur = nd;
+        NbrData cur;
+        if (PF) cur = nd;
+        else load_nbr(c, kc, q, dq, qm, cur);
         const float4 g = gn;
         const float2 w = wn;
         const unsigned dir = dn;
         if (j + 1 < nb) {
-            load_nbr(c, kn, q, dq, qm, nd);
+            if (PF) load_nbr(c, kn, q, dq, qm, nd);
+            else kc = kn;
             edge_geo<UW>(c, e + 32, gn, wn);
             dn = c.e_dir[e + 32];
         }
@@ -1073,7 +1080,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update_rp(DevCloud c, Case
 }
 
 // Register-prefetch form with the owner's data in shared memory (flux_point_rps).
-template <int BLOCK, int MINB, bool UW>
+template <int BLOCK, int MINB, bool UW, bool PF = true>
 __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update_rps(DevCloud c, CaseConst K, const float4 *__restrict__ q,
                                                            const float4 *__restrict__ dq,
                                                            const float4 *__restrict__ qm,
@@ -1090,8 +1097,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update_rps(DevCloud c, Cas
     const int i = blockIdx.x * BLOCK + t;
     float r2 = 0.0f;
     if (i < c.n)
-        r2 = flux_point_rps<BLOCK, UW>(c, K, i, t, sown, q, dq, qm, delta, prim, prim_old, prim_next, q_next,
-                                       cs_next, rk, acc_out);
+        r2 = flux_point_rps<BLOCK, UW, PF>(c, K, i, t, sown, q, dq, qm, delta, prim, prim_old, prim_next, q_next,
+                                           cs_next, rk, acc_out);
     if (psum) block_sum_max32<BLOCK>(r2, psum + blockIdx.x, pmax + blockIdx.x);
 }
 
@@ -1185,6 +1192,41 @@ __global__ void __launch_bounds__(TILE * L, MINB) kb_flux_update(const DevCloud 
                                    nullptr, (int)threadIdx.x % L);
         }
         if (psum) block_sum_max32<TILE * L>(r2, psum + t, pmax + t);
+    }
+}
+
+// kb_flux_update in the register-prefetch form with the owner's data in
+// shared memory (flux_point_rps; one thread per point).
+template <int TILE, int MINB, bool UW, bool PF>
+__global__ void __launch_bounds__(TILE, MINB) kb_flux_update_rps(const DevCloud *__restrict__ clouds,
+                                                                 const BatchCase *__restrict__ cases,
+                                                                 const BatchTile *__restrict__ tiles, int ntiles,
+                                                                 const float4 *__restrict__ q,
+                                                                 const float4 *__restrict__ dq,
+                                                                 const float4 *__restrict__ qm,
+                                                                 const float *__restrict__ delta,
+                                                                 const double4_32a *__restrict__ prim,
+                                                                 const double4_32a *__restrict__ prim_old,
+                                                                 double4_32a *__restrict__ prim_next,
+                                                                 float4 *__restrict__ q_next,
+                                                                 float *__restrict__ cs_next, int rk,
+                                                                 double *__restrict__ psum, double *__restrict__ pmax)
+{
+    __shared__ float4 sown[5 * TILE];
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BatchTile T = tiles[t];
+        const BatchCase &C = cases[T.cas];
+        const int i = T.first + (int)threadIdx.x;
+        float r2 = 0.0f;
+        if (i < C.n) {
+            const long long o = C.off;
+            r2 = flux_point_rps<TILE, UW, PF>(clouds[C.cloud], C.K, i, threadIdx.x, sown, q + o, dq + 2 * o,
+                                              qm + 2 * o, delta + o, prim + o, prim_old + o, prim_next + o,
+                                              q_next + o, cs_next ? cs_next + o : nullptr, rk, nullptr);
+        }
+        // (each thread reads and writes only its own shared slots, so the
+        // next tile needs no barrier before reusing them)
+        if (psum) block_sum_max32<TILE>(r2, psum + t, pmax + t);
     }
 }
 
@@ -1333,11 +1375,13 @@ void q_inner(const Launch &L, const DevCloud &c, const float4 *dq0, const float4
 // resident blocks per SM -> register cap; 4..7 the staged-gather form; 8, 9
 // the per-edge gather form with 2 / 4 lanes per point; 10..13 the
 // register-prefetch form; 14, 15 the same with the owner's data in shared
-// memory), picked by the host's autotuner.
-const int kFluxVariants = 16;
-static const int kFluxBlock[kFluxVariants] = {128, 128, 64, 256, 128, 128, 64, 256, 128, 256, 128, 128, 64, 256, 128, 128};
-static const int kFluxMinBlocks[kFluxVariants] = {4, 5, 8, 2, 4, 5, 8, 2, 4, 2, 4, 5, 6, 2, 5, 6};
-static const int kFluxLanes[kFluxVariants] = {1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 1, 1, 1, 1, 1, 1};
+// memory; 16..18 that form with only the edge index and data prefetched),
+// picked by the host's autotuner.
+const int kFluxVariants = 19;
+static const int kFluxBlock[kFluxVariants] = {128, 128, 64, 256, 128, 128, 64, 256, 128, 256,
+                                              128, 128, 64, 256, 128, 128, 128, 128, 128};
+static const int kFluxMinBlocks[kFluxVariants] = {4, 5, 8, 2, 4, 5, 8, 2, 4, 2, 4, 5, 6, 2, 5, 6, 6, 7, 8};
+static const int kFluxLanes[kFluxVariants] = {1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 1, 1, 1, 1, 1, 1, 1, 1, 1};
 
 int flux_variants() { return kFluxVariants; }
 int flux_block(int v) { return kFluxBlock[v]; }
@@ -1382,17 +1426,19 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
                                                                           prim_old, prim_next, q_next,     \
                                                                           cspeed_next, rk, R.partial_sum,  \
                                                                           R.partial_max, acc_out)
-#define QLSKUM_FLUX_RPS(B, MB)                                                                              \
+#define QLSKUM_FLUX_RPS(B, MB, PF)                                                                          \
     if (c.unit_w)                                                                                           \
-        k_flux_update_rps<B, MB, true><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim,  \
-                                                                          prim_old, prim_next, q_next,     \
-                                                                          cspeed_next, rk, R.partial_sum,  \
-                                                                          R.partial_max, acc_out);         \
+        k_flux_update_rps<B, MB, true, PF><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta,     \
+                                                                              prim, prim_old, prim_next,   \
+                                                                              q_next, cspeed_next, rk,     \
+                                                                              R.partial_sum, R.partial_max, \
+                                                                              acc_out);                    \
     else                                                                                                    \
-        k_flux_update_rps<B, MB, false><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta, prim, \
-                                                                           prim_old, prim_next, q_next,    \
-                                                                           cspeed_next, rk, R.partial_sum, \
-                                                                           R.partial_max, acc_out)
+        k_flux_update_rps<B, MB, false, PF><<<grid_for(c.n, B), B, 0, L.stream>>>(c, k, q, dq, qm, delta,    \
+                                                                               prim, prim_old, prim_next,  \
+                                                                               q_next, cspeed_next, rk,    \
+                                                                               R.partial_sum,              \
+                                                                               R.partial_max, acc_out)
     switch (variant) {
     case 1: QLSKUM_FLUX(128, 5); break;
     case 2: QLSKUM_FLUX(64, 8); break;
@@ -1407,8 +1453,11 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
     case 11: QLSKUM_FLUX_RP(128, 5); break;
     case 12: QLSKUM_FLUX_RP(64, 6); break;
     case 13: QLSKUM_FLUX_RP(256, 2); break;
-    case 14: QLSKUM_FLUX_RPS(128, 5); break;
-    case 15: QLSKUM_FLUX_RPS(128, 6); break;
+    case 14: QLSKUM_FLUX_RPS(128, 5, true); break;
+    case 15: QLSKUM_FLUX_RPS(128, 6, true); break;
+    case 16: QLSKUM_FLUX_RPS(128, 6, false); break;
+    case 17: QLSKUM_FLUX_RPS(128, 7, false); break;
+    case 18: QLSKUM_FLUX_RPS(128, 8, false); break;
     default: QLSKUM_FLUX(128, 4); break;
     }
 #undef QLSKUM_FLUX
@@ -1492,10 +1541,13 @@ void batch_q_inner(const Launch &L, const BatchView &B, int tile, const float4 *
 
 // flux variants: (points per tile, min blocks, lanes per point) = (128,4,1) (128,5,1) (64,8,1) (256,2,1)
 // (64,4,2) (64,2,4); threads per block = points x lanes
-const int kBatchFluxVariants = 6;
-static const int kBatchFluxTile[kBatchFluxVariants] = {128, 128, 64, 256, 64, 64};
-static const int kBatchFluxMinB[kBatchFluxVariants] = {4, 5, 8, 2, 4, 2};
-static const int kBatchFluxLanes[kBatchFluxVariants] = {1, 1, 1, 1, 2, 4};
+// Batched flux variants: tile, minimum resident blocks, lanes per point;
+// 6..8 the register-prefetch form with the owner's data in shared memory
+// (6 with the neighbour data prefetched, 7 and 8 the edge index and data only).
+const int kBatchFluxVariants = 9;
+static const int kBatchFluxTile[kBatchFluxVariants] = {128, 128, 64, 256, 64, 64, 128, 128, 128};
+static const int kBatchFluxMinB[kBatchFluxVariants] = {4, 5, 8, 2, 4, 2, 5, 6, 7};
+static const int kBatchFluxLanes[kBatchFluxVariants] = {1, 1, 1, 1, 2, 4, 1, 1, 1};
 
 int batch_flux_variants() { return kBatchFluxVariants; }
 int batch_flux_tile(int v) { return kBatchFluxTile[v]; }
@@ -1521,15 +1573,34 @@ void batch_flux_update(const Launch &L, const BatchView &B, int variant, const f
                 q_next, cs_next, rk, psum, pmax);                                                                \
         }                                                                                                        \
     }
+#define QLSKUM_BFLUX_RPS(T_, MB, PF)                                                                            \
+    {                                                                                                            \
+        const int ti = tile_index(T_);                                                                           \
+        if (B.unit_w) {                                                                                          \
+            const int g = persistent_grid(kb_flux_update_rps<T_, MB, true, PF>, T_, B.ntiles[ti]);              \
+            kb_flux_update_rps<T_, MB, true, PF><<<g, T_, 0, L.stream>>>(                                        \
+                B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq, qm, delta, prim, prim_old, prim_next,       \
+                q_next, cs_next, rk, psum, pmax);                                                                \
+        } else {                                                                                                 \
+            const int g = persistent_grid(kb_flux_update_rps<T_, MB, false, PF>, T_, B.ntiles[ti]);             \
+            kb_flux_update_rps<T_, MB, false, PF><<<g, T_, 0, L.stream>>>(                                       \
+                B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq, qm, delta, prim, prim_old, prim_next,       \
+                q_next, cs_next, rk, psum, pmax);                                                                \
+        }                                                                                                        \
+    }
     switch (variant) {
     case 1: QLSKUM_BFLUX(128, 5, 1); break;
     case 2: QLSKUM_BFLUX(64, 8, 1); break;
     case 3: QLSKUM_BFLUX(256, 2, 1); break;
     case 4: QLSKUM_BFLUX(64, 4, 2); break;
     case 5: QLSKUM_BFLUX(64, 2, 4); break;
+    case 6: QLSKUM_BFLUX_RPS(128, 5, true); break;
+    case 7: QLSKUM_BFLUX_RPS(128, 6, false); break;
+    case 8: QLSKUM_BFLUX_RPS(128, 7, false); break;
     default: QLSKUM_BFLUX(128, 4, 1); break;
     }
 #undef QLSKUM_BFLUX
+#undef QLSKUM_BFLUX_RPS
     QLSKUM_LAUNCHED(L);
 }
 
