@@ -547,6 +547,44 @@ def batch_leg(torch, qlskum, warmup=3, steps=10):
     return out
 
 
+def two_element_leg(torch, qlskum, warmup=3, steps=10, fp64_steps=3, adjoint_iters=4, adjoint_stride=2):
+    """Config 5 at a reduced size for the default line: the two-element cloud
+    (NACA 0012 main element + 30%-chord flap at 20 deg, 1.5%-chord slot,
+    4096 + 1024 wall points) with a coarser background (h0 4e-4, growth
+    0.04: ~450k points instead of ~16M), M 0.2, AoA 8, inner 0.  Mixed
+    point-iter/s (CUDA events on the library's stream), the FP64 form on the
+    same cloud and iteration count for the ratio and the Cl / Cd gap, and
+    the mixed adjoint of Cl with a checkpoint every 2 iterations (8 SSPRK
+    stages) against the same primal iterations."""
+    t0 = time.perf_counter()
+    cloud = cloudgen_mod().two_element_cloud(h0=4e-4, growth=0.04)
+    t_gen = time.perf_counter() - t0
+    kw = WORKLOADS["two_element"]["solver"]
+    s = qlskum.Solver(cloud, precision=qlskum.MIXED, **kw)
+    s.q_lskum(warmup)
+    dt, launches = time_solver(qlskum, torch, s, steps)
+    cl, cd, _, _ = s.objective()
+    f = qlskum.Solver(cloud, precision=qlskum.FP64, **kw)
+    f.q_lskum(warmup)
+    dt64, _ = time_solver(qlskum, torch, f, fp64_steps)
+    f.q_lskum(steps - fp64_steps)
+    cl64, cd64, _, _ = f.objective()
+    f.close()
+    adj = measure_adjoint(s, "mixed", adjoint_iters, adjoint_stride, cloud.n)
+    s.close()
+    return {"workload": "two_element_450k", "points": cloud.n, "value": cloud.n * steps / dt,
+            "unit": "point-iter/s", "steps": steps, "warmup": warmup, "ms_per_step": dt / steps * 1e3,
+            "gpu_launches": launches, "fp64_point_iter_s": cloud.n * fp64_steps / dt64,
+            "after_iterations": warmup + steps, "cl": cl, "cd": cd, "abs_dcl": abs(cl - cl64),
+            "abs_dcd": abs(cd - cd64), "adjoint_mixed": adj, "cloud_generation_s": t_gen,
+            "cloud": {"h0": 4e-4, "growth": 0.04, "n_main": 4096, "n_flap": 1024}, **kw}
+
+
+def cloudgen_mod():
+    from qlskum import cloudgen
+    return cloudgen
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -653,7 +691,7 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=3,
                     help="iterations of the CPU baseline (one core and all cores)")
     ap.add_argument("--no-batch-leg", dest="batch_leg", action="store_false",
-                    help="skip the reduced batched-launch leg of the default line")
+                    help="skip the reduced batched-launch and two-element legs of the default line")
     ap.add_argument("--adjoint-iters", type=int, default=3,
                     help="iterations differentiated by the adjoint timings (FP64 and mixed handles; 0: skip)")
     ap.add_argument("--long-iters", type=int, default=0,
@@ -806,9 +844,10 @@ def main():
     e2e_v, h2d, d2h = e2e_rate(qlskum, solver, cloud.n, e2e_steps)
     e2e_v *= world
 
-    batch = None
+    batch = two_el = None
     if rank == 0 and world == 1 and args.batch_leg and args.workload == "transonic":
         batch = batch_leg(torch, qlskum)
+        two_el = two_element_leg(torch, qlskum)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -836,7 +875,7 @@ def main():
             "e2e": {"value": e2e_v, "unit": "point-iter/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "roofline": roofline, "cpu_baseline": cpu, "fp64_vs_mixed": compare, "adjoint": adjoint,
-            "adjoint_mixed": adjoint_mixed, "batch": batch,
+            "adjoint_mixed": adjoint_mixed, "batch": batch, "two_element": two_el,
             "kernel_ms_per_iteration": {k: v[0] / max(1, 2) for k, v in kt.items()},
             "launch_config": solver.launch_config(),
         }

@@ -141,14 +141,18 @@ __global__ void k_derived(int n, const double4_32a *__restrict__ prim, float4 *_
 }
 
 // Edge vector and least-squares weights of edge e: {delx, dely, w delx, w dely}.
+// The gradient and inner-step kernels stream their edge arrays once per
+// launch: those loads are marked evict-first (__ldcs), so that L1 and L2
+// keep the gathered neighbour data instead (inner step 0.059 -> 0.055 ms on
+// the 1.02 M cloud).
 template <bool UW>
 __device__ __forceinline__ float4 edge_w(const DevCloud &c, long long e)
 {
     if (UW) {
-        const float2 d = c.e_xy32[e];
+        const float2 d = __ldcs(c.e_xy32 + e);
         return make_float4(d.x, d.y, d.x, d.y);
     }
-    return c.e_geo32[e];
+    return __ldcs(c.e_geo32 + e);
 }
 
 // ----------------------------------------------------------- point bodies
@@ -175,8 +179,8 @@ __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float
     const long long base = c.slice_base[i >> 5] + (i & 31);
     for (int j = sub; j < nb; j += L) {
         const long long e = base + 32LL * j;
-        const int k = c.e_nbr[e];
-        const float2 gw = c.e_gw32[e];
+        const int k = __ldcs(c.e_nbr + e);
+        const float2 gw = __ldcs(c.e_gw32 + e);
         float qk[4];
         ld4(q[k], qk);
 #pragma unroll
@@ -244,9 +248,9 @@ __device__ __forceinline__ void inner_point(const DevCloud &c, int i, const floa
 #pragma unroll 2
     for (int j = sub; j < nb; j += L) {
         const long long e = base + 32LL * j;
-        const int k = c.e_nbr[e];
+        const int k = __ldcs(c.e_nbr + e);
         const float4 g = edge_w<UW>(c, e);
-        const float2 gw = c.e_gw32[e];
+        const float2 gw = __ldcs(c.e_gw32 + e);
         // the neighbour's gradient pair in one 32-byte load
         float4 gx, gy;
         ldg_2x4(dq_in + 2 * k, gx, gy);

@@ -45,11 +45,12 @@ typedef enum {
 
 typedef enum {
     QLSKUM_FP64 = 0,             /* FP64 end to end: the drop-in form */
-    QLSKUM_MIXED = 1             /* FP32: q, dq, qm storage, limiter, reconstruction, split fluxes and
-                                    the per-point weighted sums over the edges; FP64: the 2x2
-                                    least-squares solves (folded once per cloud into per-edge FP32
-                                    weights), the time-step scaling of the residual, the SSPRK
-                                    update, prim and the residual norm */
+    QLSKUM_MIXED = 1             /* FP32: q, dq, qm storage, limiter, reconstruction, split fluxes,
+                                    the per-point weighted sums over the edges and an interior
+                                    point's stage change; FP64: the 2x2 least-squares solves (folded
+                                    once per cloud into per-edge FP32 weights), prim and its
+                                    accumulation over the stages (prim + change), the wall and outer
+                                    points' SSPRK update, the residual norm's sum over the points */
 } qlskum_precision;
 
 /* The grid file's columns (main.cpp:32-36), host memory, 1-based indices. */

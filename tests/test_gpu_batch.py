@@ -86,10 +86,13 @@ def test_batch_rejects_fp64_and_bad_case(qlskum):
     _ = keep
 
 
-@pytest.mark.parametrize("tile,point_lanes,flux_variant", [(64, 2, 4), (128, 4, 5), (256, 2, 0), (64, 4, 1)])
+@pytest.mark.parametrize("tile,point_lanes,flux_variant", [(64, 2, 4), (128, 4, 5), (256, 2, 0), (64, 4, 1),
+                                                          (128, 1, 6), (128, 2, 7), (64, 1, 8)])
 def test_batch_lanes_per_point_match_one_lane(qlskum, tile, point_lanes, flux_variant):
     """Batched kernels with 2 or 4 lanes per point (gradient / inner loop and
-    flux) against the one-lane batch: the same state to FP32 rounding."""
+    flux), and the batched flux forms with the owner's data in shared memory
+    (flux variants 6..8), against the one-lane batch: the same state to FP32
+    rounding."""
     clouds = _clouds()
     a = qlskum.Batch(clouds, CASES[:3], **KW)
     a.set_launch_config(128, 1, 0)

@@ -115,6 +115,28 @@ def test_lanes_per_point_match_one_lane(qlskum, flux_variant, point_lanes):
         np.testing.assert_allclose(a.residual_history(), b.residual_history(), rtol=1e-3)
 
 
+@pytest.mark.parametrize("flux_variant", [10, 13, 14, 16, 17, 18])
+def test_flux_forms_match_per_edge_form(qlskum, flux_variant):
+    """The register-prefetch forms of the flux kernel (10..13: the next
+    edge's neighbour data in registers, 256-bit gathers; 14..18: the owner's
+    data in shared memory, with or without the neighbour data prefetched)
+    give the per-edge form's state to FP32 rounding, with and without unit
+    weights."""
+    c = golden_cloud("cloud_c1")
+    for power in (0.0, 1.0):
+        kw = dict(mach=0.63, aoa=2.0, cfl=0.2, vl_const=50.0, power=power, inner_iterations=2,
+                  precision=qlskum.MIXED)
+        a = qlskum.Solver(c, **kw)
+        a.set_launch_config(0, 128, 0)
+        a.q_lskum(4)
+        b = qlskum.Solver(c, **kw)
+        b.set_launch_config(flux_variant, 128, 0)
+        b.q_lskum(4)
+        assert b.launch_config()["flux_variant"] == flux_variant
+        assert _close(b.prim, a.prim, 1e-5), power
+        np.testing.assert_allclose(a.residual_history(), b.residual_history(), rtol=1e-3)
+
+
 def test_objective_matches_host_sum(qlskum, oracle_mod):
     """Cl / Cd / Cm / entropy of the same state from the device reduction and
     from the oracle (compute_force_coeffs_mod.h, compute_entropy_mod.h)."""
