@@ -893,13 +893,18 @@ __global__ void k_inner(DevCloud c, AdjT T, const float4 *__restrict__ bdq_out, 
     float ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0};
     const int nb = T.nb[i];
     const long long base = T.sbase[i >> 5] + (i & 31);
+    // the transposed list is streamed once (evict-first), the owners' bars
+    // gathered as 32-byte pairs (the forward inner step's access pattern)
+#pragma unroll 2
     for (int j = 0; j < nb; j++) {
         const long long t = base + 32LL * j;
-        const int src = T.src[t];
-        const float2 d = T.xy[t], gw = T.gw[t];
+        const int src = __ldcs(T.src + t);
+        const float2 d = __ldcs(T.xy + t), gw = __ldcs(T.gw + t);
+        float4 b0, b1;
+        ldg_2x4(bdq_out + 2 * src, b0, b1);
         float bx[4], by[4];
-        ldf4(bdq_out[2 * src], bx);
-        ldf4(bdq_out[2 * src + 1], by);
+        ldf4(b0, bx);
+        ldf4(b1, by);
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             const float bu = fmaf(gw.x, bx[r], gw.y * by[r]);
@@ -965,8 +970,8 @@ __global__ void k_grad(DevCloud c, const float4 *__restrict__ q, const float4 *_
     const long long base = c.slice_base[i >> 5] + (i & 31);
     for (int j = 0; j < nb; j++) {
         const long long e = base + 32LL * j;
-        const int k = c.e_nbr[e];
-        const float2 gw = c.e_gw32[e];
+        const int k = __ldcs(c.e_nbr + e);
+        const float2 gw = __ldcs(c.e_gw32 + e);
         float qk[4], bqk[4];
         ldf4(q[k], qk);
 #pragma unroll
