@@ -107,6 +107,8 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
     const long long base = c.slice_base[i >> 5] + (i & 31);
     const double scale = (f == kWall) ? 2.0 : 1.0;
     const bool used[4] = {true, true, f != kWall, f != kOuter};
+    // geometry bars only where the geometry depends on a wall point (AdjView::geo_pt)
+    const bool geo = GEO && a.geo_pt[i];
 
     // forward: the directional sums, for the bars of the moments (GEO only:
     // the forward kernel's stored sums, or recomputed; without them the bar of
@@ -115,7 +117,7 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
     double sx[4][4], sy[4][4];
     for (int d = 0; d < 4; d++)
         for (int r = 0; r < 4; r++) sx[d][r] = sy[d][r] = 0.0;
-    if (GEO && sums) {
+    if (geo && sums) {
         const double *o = sums + 32 * (size_t)i;
         for (int d = 0; d < 4; d++)
             for (int r = 0; r < 4; r++) {
@@ -123,7 +125,7 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
                 sy[d][r] = o[8 * d + 4 + r];
             }
     }
-    for (int j = 0; GEO && !sums && j < nb; j++) {
+    for (int j = 0; geo && !sums && j < nb; j++) {
         const long long e = base + 32LL * j;
         const int k = c.e_nbr[e];
         const double4_32a g = c.e_geo[e];
@@ -175,7 +177,7 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
             ax[d] = -m.z * m.w;
             ay[d] = m.x * m.w;
         }
-        if (!GEO) continue;
+        if (!geo) continue;
         double bm[4] = {0, 0, 0, 0};
         for (int r = 0; r < 4; r++) {
             const double bG = bG4[r];
@@ -199,7 +201,7 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
         acc.z += bm[2];
         acc.w += bm[3];
     }
-    if (!GEO) {
+    if (!geo) {
         double F[4];
         ld4(flux[i], F);
         bdl = (bFi[0] * F[0] + bFi[1] * F[1] + bFi[2] * F[2] + bFi[3] * F[3]) / dl;
@@ -225,7 +227,7 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
             double bG[4];                                                            \
             for (int r = 0; r < 4; r++) bG[r] = fw * bG4[r];                         \
             adj::dir_flux_vjp<D>(f, KIN, bG, KB);                                    \
-            if (GEO) {                                                               \
+            if (geo) {                                                               \
                 double G[4];                                                         \
                 dir_flux<double, D>(f, KIN, G);                                      \
                 const double gb = bG4[0] * G[0] + bG4[1] * G[1] + bG4[2] * G[2] + bG4[3] * G[3]; \
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
             adj::end64_vjp(s, nx, ny, g.x, g.y, dxi, dyi, kb, bqi, bdxi, bdyi, bmxi, bmni, bdelx, bdely, bnx, bny);
         }
 #undef QLSKUM_REV
-        if (GEO) {
+        if (geo) {
             double4_32a &ge = a.bedge[e];
             ge.x += bdelx;
             ge.y += bdely;
@@ -286,7 +288,7 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
     atomic_add4(bdq + 2 * i + 1, bdyi);
     atomic_add4(bqm + 2 * i, bmxi);
     atomic_add4(bqm + 2 * i + 1, bmni);
-    if (GEO && a.bnrm) {
+    if (geo && a.bnrm) {
         a.bnrm[i].x += bnx;
         a.bnrm[i].y += bny;
     }
@@ -302,6 +304,7 @@ __global__ void k_inner(AdjView a, const double4_32a *__restrict__ q, const doub
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.c.n) return;
     const DevCloud &c = a.c;
+    const bool geo = GEO && a.geo_pt[i];
     const double4_32a m = c.ggeo[i];
     double bx[4], by[4];
     ld4(bdq_out[2 * i], bx);
@@ -341,7 +344,7 @@ __global__ void k_inner(AdjView a, const double4_32a *__restrict__ q, const doub
             bqi[r] -= bt;
             bdxi[r] += 0.5 * g.x * bt;
             bdyi[r] += 0.5 * g.y * bt;
-            if (GEO) {
+            if (geo) {
                 bwx += bsdx[r] * (t2 - t1);
                 bwy += bsdy[r] * (t2 - t1);
                 bgx += -0.5 * bt * (dxk[r] - dxi[r]);
@@ -351,7 +354,7 @@ __global__ void k_inner(AdjView a, const double4_32a *__restrict__ q, const doub
         atomic_add4(bq + k, bqk);
         atomic_add4(bdq_in + 2 * k, bdxk);
         atomic_add4(bdq_in + 2 * k + 1, bdyk);
-        if (GEO) {
+        if (geo) {
             // unit weights: w delx == delx
             double4_32a &ge = a.bedge[e];
             ge.x += bgx + bwx;
@@ -361,7 +364,7 @@ __global__ void k_inner(AdjView a, const double4_32a *__restrict__ q, const doub
     atomic_add4(bq + i, bqi);
     atomic_add4(bdq_in + 2 * i, bdxi);
     atomic_add4(bdq_in + 2 * i + 1, bdyi);
-    if (GEO) {
+    if (geo) {
         double bm[4] = {0, 0, 0, 0};
         for (int r = 0; r < 4; r++) {
             // dx = ood (Sx syy - Sy sxy), dy = ood (Sy sxx - Sx sxy)
@@ -387,6 +390,7 @@ __global__ void k_grad(AdjView a, const double4_32a *__restrict__ q, const doubl
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.c.n) return;
     const DevCloud &c = a.c;
+    const bool geo = GEO && a.geo_pt[i];
     const double4_32a m = c.ggeo[i];
     double bx[4], by[4], bmax[4], bmin[4];
     ld4(bdq[2 * i], bx);
@@ -425,13 +429,13 @@ __global__ void k_grad(AdjView a, const double4_32a *__restrict__ q, const doubl
             const double bt = g.z * bsdx[r] + g.w * bsdy[r];
             bqk[r] = bt;
             bqi[r] -= bt;
-            if (GEO) {
+            if (geo) {
                 bwx += bsdx[r] * (qk[r] - qi[r]);
                 bwy += bsdy[r] * (qk[r] - qi[r]);
             }
         }
         atomic_add4(bq + k, bqk);
-        if (GEO) {
+        if (geo) {
             double4_32a &ge = a.bedge[e];
             ge.x += bwx;
             ge.y += bwy;
@@ -443,7 +447,7 @@ __global__ void k_grad(AdjView a, const double4_32a *__restrict__ q, const doubl
         if (bmax[r] != 0.0) atomicAdd(bqd + 4 * (size_t)amax[r] + r, bmax[r]);
         if (bmin[r] != 0.0) atomicAdd(bqd + 4 * (size_t)amin[r] + r, bmin[r]);
     }
-    if (GEO) {
+    if (geo) {
         double bm[4] = {0, 0, 0, 0};
         for (int r = 0; r < 4; r++) {
             bm[1] += m.w * bx[r] * sdx[r];
@@ -505,7 +509,7 @@ __global__ void k_delta(AdjView a, const double4_32a *__restrict__ P, const doub
     }
     if (arg >= 0 && bdelta[i] != 0.0) {
         atomicAdd(bc + arg, -bdelta[i] * cfl * c.e_dist[earg] / (carg * carg));
-        if (GEO) a.bdist[earg] += bdelta[i] * cfl / carg;
+        if (GEO && a.geo_pt[i]) a.bdist[earg] += bdelta[i] * cfl / carg;
     }
 }
 
@@ -562,6 +566,18 @@ __global__ void k_objective_J(int n, const double4_32a *__restrict__ P, double g
     bP[i] = b;
 }
 
+// AdjView::geo_pt: 1 for a wall point and for a point with a wall neighbour.
+__global__ void k_mark_geo(DevCloud c, uint8_t *__restrict__ geo_pt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    bool g = c.flag[i] == kWall;
+    const int nb = c.nbhs[i];
+    const long long base = c.slice_base[i >> 5] + (i & 31);
+    for (int j = 0; j < nb && !g; j++) g = c.flag[c.e_nbr[base + 32LL * j]] == kWall;
+    geo_pt[i] = g ? 1 : 0;
+}
+
 // The geometry bars the reverse kernels accumulated (per edge: vector,
 // rotated vector, length; per point: normal, gradient and directional LSQ
 // moments) pulled back to the point coordinates, unit weights: each point's
@@ -573,6 +589,12 @@ __global__ void k_geom_pullback(AdjView a, double *__restrict__ bx, double *__re
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.c.n) return;
+    // a point whose geometry does not depend on a wall point accumulated no
+    // geometry bars (AdjView::geo_pt): nothing to pull back
+    if (!a.geo_pt[i]) {
+        bn[i] = a.bnrm[i];
+        return;
+    }
     const DevCloud &c = a.c;
     const double2 nn = c.nrm[i];
     const double nx = nn.x, ny = nn.y;
@@ -1174,6 +1196,11 @@ void objective(const Launch &L, const AdjView &a, const int *wall_perm, const do
     if (n_wall > 0)
         adjk::k_objective<<<adjk::grid_for(n_wall, 128), 128, 0, L.stream>>>(a, wall_perm, wall_geo, n_wall, cp_scale,
                                                                             theta, which, bP);
+}
+
+void mark_geo_points(const Launch &L, const DevCloud &c, uint8_t *geo_pt)
+{
+    adjk::k_mark_geo<<<adjk::grid_for(c.n, 128), 128, 0, L.stream>>>(c, geo_pt);
 }
 
 void geom_pullback(const Launch &L, const AdjView &a, double *bx, double *by, double2 *bn)

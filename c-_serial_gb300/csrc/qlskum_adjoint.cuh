@@ -217,8 +217,9 @@ template <typename R> QLSKUM_HD void edge_end_vjp(R delx, R dely, const R q[4], 
 // q~ -> prim (q_variables_mod.h:230-253) and the half-range moments
 // (split_fluxes_mod.h:14-26), keeping what end64_vjp reads.  The functions
 // above recompute each quantity they need (an edge end then costs 33 FP64
-// divisions, 6 exps and 2 logs); here one end costs 7 divisions, 3 exps and
-// 1 log.  The forward values are those of edge_states / kin_prep up to
+// divisions, 6 exps and 2 logs); here one end costs 7 reciprocals (rcp64 on
+// the device: an FP32 seed and two Newton steps, no FP64 division), 3 exps
+// and 1 log.  The forward values are those of edge_states / kin_prep up to
 // last-bit roundings: the limiter's ratio is num * (1 / den), whose
 // reciprocal the VJP reads too; kin_prep's beta = rho / (2 p) and
 // p / rho are the q~ -> prim step's beta and 1 / (2 beta); 1 / (gamma - 1)
@@ -247,7 +248,7 @@ QLSKUM_HD void end64(double nx, double ny, double delx, double dely, const doubl
         const double num = (dp * dp + e2) * dn + 2.0 * dn * dn * dp;
         const double den = ((dp * dp + 2.0 * dn * dn) + dn * dp + e2) * dn;
         const bool cut = fabs(dn) <= 10e-6;
-        const double rden = 1.0 / (cut ? 1.0 : den);
+        const double rden = M<double>::rcp(cut ? 1.0 : den);
         const double t = num * rden;
         const double phi = (cut || !(t < 1.0)) ? 1.0 : t;
         s.g[r] = g;
@@ -261,7 +262,7 @@ QLSKUM_HD void end64(double nx, double ny, double delx, double dely, const doubl
     s.qt1 = qt[1];
     s.qt2 = qt[2];
     s.beta = -qt[3] * 0.5;
-    s.tm = 0.5 / s.beta;
+    s.tm = 0.5 * M<double>::rcp(s.beta);
     s.u1 = qt[1] * s.tm;
     s.u2 = qt[2] * s.tm;
     s.k.ut = s.u1 * ny - s.u2 * nx;
@@ -283,7 +284,7 @@ QLSKUM_HD void end64(double nx, double ny, double delx, double dely, const doubl
         s.k.E2 = erf_e<double>(S2, s.e2);
     }
     s.k.rho = s.rho;
-    s.rsb = 1.0 / s.sb;
+    s.rsb = M<double>::rcp(s.sb);
     const double half_rpi = 0.28209479177387814;  // 1 / (2 sqrt(pi))
     s.k.B1 = half_rpi * s.e1 * s.rsb;
     s.k.B2 = half_rpi * s.e2 * s.rsb;
@@ -312,7 +313,7 @@ QLSKUM_HD void end64_vjp(const End64 &s, double nx, double ny, double delx, doub
     bun += bS2 * s.sb;
     const double bsb = bS1 * ut + bS2 * un;
     const double bbk = 0.5 * bsb * s.rsb - (kb.B1 * s.k.B1 + kb.B2 * s.k.B2) * s.tm;  // 0.5 / beta = tm
-    const double irho = 1.0 / s.rho;
+    const double irho = M<double>::rcp(s.rho);
     // 0.5 / p = beta / rho, p / rho^2 = tm / rho, beta / p = 2 beta^2 / rho
     const double bP0 = kb.rho + bbk * s.beta * irho - kb.pbr * s.tm * irho;
     const double bP3 = -bbk * 2.0 * s.beta * s.beta * irho + kb.pbr * irho;

@@ -2800,6 +2800,7 @@ struct AdjBuf {
     double *bdist = nullptr;
     double2 *bnrm = nullptr;
     double4_32a *bgmom = nullptr, *bfmom = nullptr;
+    uint8_t *geo_pt = nullptr;              // AdjView::geo_pt
     double *gbx = nullptr, *gby = nullptr;  // coordinate bars (geom_pullback)
     double2 *gbn = nullptr;                 // normal bars (geom_pullback)
     // the checkpointed primal: the state of every stride-th iteration, and
@@ -3050,6 +3051,7 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
         a->gby = A.alloc<double>(np);
         a->gbn = A.alloc<double2>(np);
         a->bfmom = A.alloc<double4_32a>(4 * np);
+        a->geo_pt = A.alloc<uint8_t>(np);
     }
     if (A.err != cudaSuccess) {
         qlskum_status st = fail(h, QLSKUM_ERR_CUDA, fmt("adjoint cudaMalloc: %s", cudaGetErrorString(A.err)));
@@ -3058,6 +3060,7 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
     }
     // padding rows stay zero (and finite) in every buffer
     for (auto *p : a->P) zero(h, p, sizeof(double4_32a) * np);
+    if (geo) adjl::mark_geo_points(h->L, h->dc, a->geo_pt);
     if (need32) {
         qlskum_status st = adj_transpose(h);
         if (st) adj_free(h);
@@ -3072,6 +3075,7 @@ AdjView adj_view(qlskum_handle *h, bool geo)
     v.c = h->dc;
     AdjBuf *a = h->adj;
     if (geo && a->geo) {
+        v.geo_pt = a->geo_pt;
         v.bedge = a->bedge;
         v.bdist = a->bdist;
         v.bnrm = a->bnrm;

@@ -176,6 +176,11 @@ struct Launch {
 // gradient moments and the four directional moment sets.
 struct AdjView {
     DevCloud c;
+    // with the geometry accumulators: 1 for the points whose geometry (edge
+    // vectors, moments, normal) depends on a wall point's coordinates (the
+    // wall points and the points with a wall neighbour), 0 elsewhere; the
+    // kernels accumulate geometry bars only there
+    const uint8_t *geo_pt = nullptr;
     double4_32a *bedge = nullptr;
     double *bdist = nullptr;
     double2 *bnrm = nullptr;
@@ -207,6 +212,8 @@ void objective_J(const Launch &L, int n, const double4_32a *P, double gamma, dou
 // the geometry bars of a reverse sweep pulled back to the point coordinates
 // (bx, by zeroed first; bn: each point's normal bar), unit weights
 void geom_pullback(const Launch &L, const AdjView &a, double *bx, double *by, double2 *bn);
+// AdjView::geo_pt of the cloud (1: a wall point or a point with a wall neighbour)
+void mark_geo_points(const Launch &L, const DevCloud &c, uint8_t *geo_pt);
 }  // namespace adjl
 
 // Reverse of the mixed iteration (qlskum_adjoint.cu, FP32 edge work): bars of
