@@ -340,7 +340,7 @@ def run_adjoint_check(args):
     kw = dict(WORKLOADS["transonic"]["solver"], mach=0.63, aoa=2.0)
     k, stride = max(1, args.adjoint_iters), args.adjoint_stride
     s = qlskum.Solver(cloud, precision=qlskum.FP64, **kw)
-    s.adjoint_gradient("cl", iters=1, wall=True)                      # allocation
+    s.adjoint_gradient("cl", iters=k, wall=True, stride=stride)       # allocation of the K stage sets
     grads, t_adj = {}, {}
     for obj in ("cl", "cd"):
         t0 = time.perf_counter()
