@@ -335,20 +335,37 @@ __global__ void __launch_bounds__(BLOCK) k_flux_update(DevCloud c, CaseConst K, 
 
 // fpi_solver_mod.h:138-147: res_new = sqrt(sum)/n, residue against res_old
 // latched at iterations 1 and 2; one block, fixed summation order.
-__global__ void k_reduce_residual(int nblocks, const double *__restrict__ psum, const double *__restrict__ pmax,
-                                  int n, int it_arg, double *hist, int capacity, double *res_old, int *iter,
-                                  int *status, int latch)
+// One block of RB threads: each thread sums a strided share of the block
+// partials with four independent accumulators (its loads in flight together
+// instead of one dependent chain), then a tree over the block; the order is
+// fixed, so the result is the same on every run.
+constexpr int RB = 1024;
+__global__ void __launch_bounds__(RB) k_reduce_residual(int nblocks, const double *__restrict__ psum,
+                                                       const double *__restrict__ pmax, int n, int it_arg,
+                                                       double *hist, int capacity, double *res_old, int *iter,
+                                                       int *status, int latch)
 {
-    __shared__ double ss[256], sm[256];
-    double v = 0.0, m = 0.0;
-    for (int b = threadIdx.x; b < nblocks; b += 256) {
-        v += psum[b];
-        m = pmax[b] > m ? pmax[b] : m;
+    __shared__ double ss[RB], sm[RB];
+    double v[4] = {0.0, 0.0, 0.0, 0.0}, mm[4] = {0.0, 0.0, 0.0, 0.0};
+    int b = threadIdx.x;
+    for (; b + 3 * RB < nblocks; b += 4 * RB) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            v[u] += psum[b + u * RB];
+            const double x = pmax[b + u * RB];
+            mm[u] = x > mm[u] ? x : mm[u];
+        }
     }
-    ss[threadIdx.x] = v;
+    for (; b < nblocks; b += RB) {
+        v[0] += psum[b];
+        mm[0] = pmax[b] > mm[0] ? pmax[b] : mm[0];
+    }
+    double m = mm[0];
+    for (int u = 1; u < 4; u++) m = mm[u] > m ? mm[u] : m;
+    ss[threadIdx.x] = (v[0] + v[1]) + (v[2] + v[3]);
     sm[threadIdx.x] = m;
     __syncthreads();
-    for (int s = 128; s > 0; s >>= 1) {
+    for (int s = RB / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) {
             ss[threadIdx.x] += ss[threadIdx.x + s];
             sm[threadIdx.x] = sm[threadIdx.x + s] > sm[threadIdx.x] ? sm[threadIdx.x + s] : sm[threadIdx.x];
@@ -620,8 +637,8 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const d
 
 void reduce_residual(const Launch &L, const Reduce &R, int n, int it)
 {
-    k_reduce_residual<<<1, 256, 0, L.stream>>>(R.blocks, R.partial_sum, R.partial_max, n, it, R.hist, R.capacity,
-                                               R.res_old, R.iter, R.status, R.latch);
+    k_reduce_residual<<<1, RB, 0, L.stream>>>(R.blocks, R.partial_sum, R.partial_max, n, it, R.hist, R.capacity,
+                                              R.res_old, R.iter, R.status, R.latch);
     QLSKUM_LAUNCHED(L);
 }
 

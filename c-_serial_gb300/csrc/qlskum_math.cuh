@@ -57,6 +57,15 @@ __device__ __forceinline__ float d2f(double x)
     return __uint_as_float(b);
 }
 
+// double -> float rounded to nearest (ties away from zero) on the integer
+// pipe: half an FP32 ulp (bit 28 of the FP64 pattern) added to the
+// magnitude, then d2f's truncation; a carry out of the mantissa moves into
+// the exponent as it should.  (An infinity comes out as NaN.)
+__device__ __forceinline__ float d2f_rn(double x)
+{
+    return d2f(__longlong_as_double(__double_as_longlong(x) + (1LL << 28)));
+}
+
 // 1 / x in FP64 from the FP32 reciprocal refined by two Newton steps (about
 // an ulp; no FP64 division).  Where x is outside the normal FP32 range the
 // seed is not usable and the division is taken instead.

@@ -574,7 +574,9 @@ __device__ __forceinline__ float interior_stage(const float acc[4], float dl, fl
 {
     const float F0 = dl * acc[0], Ft = dl * acc[1], Fn = dl * acc[2], F3 = dl * acc[3];
     const float Fx = fmaf(Ft, ny, Fn * nx), Fy = fmaf(Fn, ny, -Ft * nx);
-    const float rho = d2f(P[0]), u1 = d2f(P[1]), u2 = d2f(P[2]);
+    // the state's FP32 values and the stage-3 differences rounded to nearest
+    // (a truncating conversion would bias every change the same way)
+    const float rho = d2f_rn(P[0]), u1 = d2f_rn(P[1]), u2 = d2f_rn(P[2]);
     float dU0, dU1, dU2, dU3;
     if (rk != 3) {
         dU0 = -0.5f * F0;
@@ -584,8 +586,8 @@ __device__ __forceinline__ float interior_stage(const float acc[4], float dl, fl
     } else {
         double Po[4];
         ld4(*prim_old_i, Po);
-        const float dr = d2f(Po[0] - P[0]), da = d2f(Po[1] - P[1]), db = d2f(Po[2] - P[2]),
-                    dp = d2f(Po[3] - P[3]);
+        const float dr = d2f_rn(Po[0] - P[0]), da = d2f_rn(Po[1] - P[1]), db = d2f_rn(Po[2] - P[2]),
+                    dp = d2f_rn(Po[3] - P[3]);
         const float uo1 = u1 + da, uo2 = u2 + db;
         const float W1 = fmaf(dr, uo1, rho * da), W2 = fmaf(dr, uo2, rho * db);
         const float W3 = fmaf(2.5f, dp, 0.5f * fmaf(dr, fmaf(uo1, uo1, uo2 * uo2),
