@@ -191,7 +191,7 @@ __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float
             dx[r] = fmaf(gw.x, d, dx[r]);
             dy[r] = fmaf(gw.y, d, dy[r]);
         }
-        if (DT) min_dt = fminf(min_dt, cfl * __fdividef(c.e_dist32[e], cs[k]));
+        if (DT) min_dt = fminf(min_dt, cfl * __fdividef(__ldcs(c.e_dist32 + e), cs[k]));
     }
     if (L > 1) {
         const unsigned m = group_mask<L>();
