@@ -220,18 +220,20 @@ def measured_profile(workload, precision, kernel, key="traffic"):
     workload, or (None, None): 'traffic' = dram__bytes_read.sum +
     dram__bytes_write.sum, 'inst' = smsp__inst_executed.sum (warp
     instructions).  The summaries carry lines '<key> <precision> <kernel> <value>'."""
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"k_flux_update_{workload}_1M.md")
+    import glob
     family = None
-    try:
-        for line in open(path):
-            f = line.strip().strip("`").split()
-            if len(f) == 4 and f[0] == key and f[1] == precision:
-                if f[2] == kernel:
-                    return float(f[3]), f[2]
-                if f[2].split("<")[0] == kernel.split("<")[0]:
-                    family = (float(f[3]), f[2])   # same code and data, another launch shape
-    except OSError:
-        pass
+    for path in sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                                              f"*_{workload}_1M.md"))):
+        try:
+            for line in open(path):
+                f = line.strip().strip("`").split()
+                if len(f) == 4 and f[0] == key and f[1] == precision:
+                    if f[2] == kernel:
+                        return float(f[3]), f[2]
+                    if f[2].split("<")[0] == kernel.split("<")[0]:
+                        family = (float(f[3]), f[2])   # same code and data, another launch shape
+        except OSError:
+            pass
     return family if family else (None, None)
 
 
@@ -768,14 +770,18 @@ def main():
     kname = (f"{flux_kernel_form(lc['flux_variant'])}<{lc['flux_block']},{lc['flux_min_blocks']}>"
              if prec == qlskum.MIXED else "k_flux_update<128>")
     traffic, traffic_kernel = measured_traffic(args.workload, args.precision, kname)
-    # every per-stage kernel against HBM (event-timed launches, compulsory bytes)
+    # every per-stage kernel against HBM (event-timed launches, compulsory
+    # bytes), with its ncu DRAM traffic per launch where a committed summary has it
+    names = {"gradient": "k_q_derivatives", "inner": "k_q_inner", "flux_update": kname}
     kernels = {}
     for kk in ("gradient", "inner", "flux_update"):
         ms, nl = kt[kk]
         if nl:
             a = pbytes[kk] / (ms / nl / 1e3) / 1e9
-            kernels[kk] = {"algorithmic_bytes_per_launch": pbytes[kk], "avg_launch_ms": ms / nl, "launches": nl,
-                           "achieved_gbs": a, "frac": a / peak, "share": ms / total_ms}
+            tr, tr_k = measured_traffic(args.workload, args.precision, names[kk])
+            kernels[kk] = {"kernel": names[kk], "algorithmic_bytes_per_launch": pbytes[kk],
+                           "avg_launch_ms": ms / nl, "launches": nl, "achieved_gbs": a, "frac": a / peak,
+                           "share": ms / total_ms, "traffic": tr, "traffic_captured_on": tr_k}
     # the flux kernel's instruction-issue roofline: its warp instructions
     # per launch (ncu, committed summary) over 152 SMs x 4 schedulers x the
     # SM clock sampled in the timed region
@@ -791,11 +797,26 @@ def main():
                  "frac": t_issue / (fl_ms / fl_n / 1e3),
                  "note": "1.0 = one warp instruction per scheduler per cycle for the whole launch"}
         bound = "issue" if issue["frac"] > achieved / peak else "hbm"
-    roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "traffic_captured_on": traffic_kernel, "kernel": f"{kname} ({args.precision})",
-                "algorithmic_bytes_per_launch": nbytes, "avg_launch_ms": fl_ms / fl_n,
-                "kernel_share": fl_ms / total_ms, "peak_source": f"{peak_kind} hbm_gbs", "issue": issue,
-                "kernels": kernels}
+    if "flux_update" in kernels:
+        kernels["flux_update"].update(bound=bound, issue=issue)
+    # the line's roofline is the dominant kernel's: the largest share of the
+    # iteration's device time (all three stay in `kernels`)
+    dom = max(kernels, key=lambda k: kernels[k]["share"]) if kernels else "flux_update"
+    if dom == "flux_update" or dom not in kernels:
+        roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                    "traffic": traffic, "traffic_captured_on": traffic_kernel,
+                    "kernel": f"{kname} ({args.precision})", "algorithmic_bytes_per_launch": nbytes,
+                    "avg_launch_ms": fl_ms / fl_n, "kernel_share": fl_ms / total_ms}
+    else:
+        kd = kernels[dom]
+        roofline = {"bound": "hbm", "achieved": kd["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                    "frac": kd["frac"], "traffic": kd["traffic"], "traffic_captured_on": kd["traffic_captured_on"],
+                    "kernel": f"{kd['kernel']} ({args.precision})",
+                    "algorithmic_bytes_per_launch": kd["algorithmic_bytes_per_launch"],
+                    "avg_launch_ms": kd["avg_launch_ms"], "kernel_share": kd["share"]}
+    roofline.update({"peak_source": f"{peak_kind} hbm_gbs", "dominant": dom, "issue": issue, "kernels": kernels,
+                     "note": "achieved = algorithmic bytes per launch / event-timed launch; the dominant kernel "
+                             "has the largest share of the iteration; issue = the flux kernel's issue roofline"})
     bpi = bytes_per_point_iteration(cloud, args.precision, kw["inner_iterations"], unit_w)
     whole = bpi["bytes"] * cloud.n / (dt / args.steps) / 1e9
     roofline["iteration"] = dict(bpi, achieved_gbs=whole, frac=whole / peak,
