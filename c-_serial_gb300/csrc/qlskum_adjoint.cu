@@ -81,7 +81,7 @@ __global__ void k_update(AdjView a, CaseConst K, const double4_32a *__restrict__
 // Reverse of the flux residual of every point: F_i = s delta_i sum_d G_d.
 // Adds the bars of q, dq, qm (own and neighbours'), of delta, and (GEO) of the
 // edge geometry, the normal and the directional moments.
-template <bool GEO>
+template <int MODE>
 __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__restrict__ q,
                                                const double4_32a *__restrict__ dq, const double4_32a *__restrict__ qm,
                                                const double *__restrict__ delta, const double4_32a *__restrict__ flux,
@@ -90,8 +90,13 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
                                                double4_32a *__restrict__ bq, double4_32a *__restrict__ bdq,
                                                double4_32a *__restrict__ bqm, double *__restrict__ bdelta)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.c.n) return;
+    // MODE 0: the state bars at every point; 2: only the geometry bars, at
+    // the points AdjView::geo_list names (the geometry's instantiation needs
+    // far more registers, so it runs on those few points alone)
+    constexpr bool GEO = MODE != 0, STATE = MODE != 2;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (MODE == 2 ? a.n_geo : a.c.n)) return;
+    const int i = MODE == 2 ? a.geo_list[t] : t;
     const DevCloud &c = a.c;
     const int f = c.flag[i];
     const double2 nn = c.nrm[i];
@@ -107,8 +112,7 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
     const long long base = c.slice_base[i >> 5] + (i & 31);
     const double scale = (f == kWall) ? 2.0 : 1.0;
     const bool used[4] = {true, true, f != kWall, f != kOuter};
-    // geometry bars only where the geometry depends on a wall point (AdjView::geo_pt)
-    const bool geo = GEO && a.geo_pt[i];
+    const bool geo = GEO;
 
     // forward: the directional sums, for the bars of the moments (GEO only:
     // the forward kernel's stored sums, or recomputed; without them the bar of
@@ -206,7 +210,7 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
         ld4(flux[i], F);
         bdl = (bFi[0] * F[0] + bFi[1] * F[1] + bFi[2] * F[2] + bFi[3] * F[3]) / dl;
     }
-    bdelta[i] += bdl;
+    if (STATE) bdelta[i] += bdl;
 
     // reverse over the edges, one end at a time (end64 / end64_vjp): the
     // neighbour's end first, its bars scattered, then the owner's
@@ -255,11 +259,13 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
             double bqk[4] = {0, 0, 0, 0}, bdxk[4] = {0, 0, 0, 0}, bdyk[4] = {0, 0, 0, 0}, bmxk[4] = {0, 0, 0, 0},
                    bmnk[4] = {0, 0, 0, 0};
             adj::end64_vjp(s, nx, ny, g.x, g.y, dxk, dyk, kb, bqk, bdxk, bdyk, bmxk, bmnk, bdelx, bdely, bnx, bny);
-            atomic_add4(bq + k, bqk);
-            atomic_add4(bdq + 2 * k, bdxk);
-            atomic_add4(bdq + 2 * k + 1, bdyk);
-            atomic_add4(bqm + 2 * k, bmxk);
-            atomic_add4(bqm + 2 * k + 1, bmnk);
+            if (STATE) {
+                atomic_add4(bq + k, bqk);
+                atomic_add4(bdq + 2 * k, bdxk);
+                atomic_add4(bdq + 2 * k + 1, bdyk);
+                atomic_add4(bqm + 2 * k, bmxk);
+                atomic_add4(bqm + 2 * k + 1, bmnk);
+            }
         }
         {
             adj::End64 s;
@@ -283,11 +289,13 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
             ge.w += bsw_y;
         }
     }
-    atomic_add4(bq + i, bqi);
-    atomic_add4(bdq + 2 * i, bdxi);
-    atomic_add4(bdq + 2 * i + 1, bdyi);
-    atomic_add4(bqm + 2 * i, bmxi);
-    atomic_add4(bqm + 2 * i + 1, bmni);
+    if (STATE) {
+        atomic_add4(bq + i, bqi);
+        atomic_add4(bdq + 2 * i, bdxi);
+        atomic_add4(bdq + 2 * i + 1, bdyi);
+        atomic_add4(bqm + 2 * i, bmxi);
+        atomic_add4(bqm + 2 * i + 1, bmni);
+    }
     if (geo && a.bnrm) {
         a.bnrm[i].x += bnx;
         a.bnrm[i].y += bny;
@@ -296,15 +304,18 @@ __global__ void __launch_bounds__(128) k_flux(AdjView a, const double4_32a *__re
 
 // Reverse of one inner iteration (q_variables_mod.h:120-213): bdq_out is the
 // bar of its output; adds bars of q and of its input dq.
-template <bool GEO>
+template <int MODE>
 __global__ void k_inner(AdjView a, const double4_32a *__restrict__ q, const double4_32a *__restrict__ dq_in,
                         const double4_32a *__restrict__ bdq_out, double4_32a *__restrict__ bq,
                         double4_32a *__restrict__ bdq_in)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.c.n) return;
+    // MODE 0: state bars everywhere; 2: geometry bars only, at AdjView::geo_list
+    constexpr bool STATE = MODE != 2;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (MODE == 2 ? a.n_geo : a.c.n)) return;
+    const int i = MODE == 2 ? a.geo_list[t] : t;
     const DevCloud &c = a.c;
-    const bool geo = GEO && a.geo_pt[i];
+    const bool geo = MODE != 0;
     const double4_32a m = c.ggeo[i];
     double bx[4], by[4];
     ld4(bdq_out[2 * i], bx);
@@ -351,9 +362,11 @@ __global__ void k_inner(AdjView a, const double4_32a *__restrict__ q, const doub
                 bgy += -0.5 * bt * (dyk[r] - dyi[r]);
             }
         }
-        atomic_add4(bq + k, bqk);
-        atomic_add4(bdq_in + 2 * k, bdxk);
-        atomic_add4(bdq_in + 2 * k + 1, bdyk);
+        if (STATE) {
+            atomic_add4(bq + k, bqk);
+            atomic_add4(bdq_in + 2 * k, bdxk);
+            atomic_add4(bdq_in + 2 * k + 1, bdyk);
+        }
         if (geo) {
             // unit weights: w delx == delx
             double4_32a &ge = a.bedge[e];
@@ -361,9 +374,11 @@ __global__ void k_inner(AdjView a, const double4_32a *__restrict__ q, const doub
             ge.y += bgy + bwy;
         }
     }
-    atomic_add4(bq + i, bqi);
-    atomic_add4(bdq_in + 2 * i, bdxi);
-    atomic_add4(bdq_in + 2 * i + 1, bdyi);
+    if (STATE) {
+        atomic_add4(bq + i, bqi);
+        atomic_add4(bdq_in + 2 * i, bdxi);
+        atomic_add4(bdq_in + 2 * i + 1, bdyi);
+    }
     if (geo) {
         double bm[4] = {0, 0, 0, 0};
         for (int r = 0; r < 4; r++) {
@@ -383,14 +398,17 @@ __global__ void k_inner(AdjView a, const double4_32a *__restrict__ q, const doub
 
 // Reverse of the least-squares gradient and of the neighbour max / min
 // (q_variables_mod.h:36-118).
-template <bool GEO>
+template <int MODE>
 __global__ void k_grad(AdjView a, const double4_32a *__restrict__ q, const double4_32a *__restrict__ bdq,
                        const double4_32a *__restrict__ bqm, double4_32a *__restrict__ bq)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.c.n) return;
+    // MODE 0: state bars everywhere; 2: geometry bars only, at AdjView::geo_list
+    constexpr bool STATE = MODE != 2;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (MODE == 2 ? a.n_geo : a.c.n)) return;
+    const int i = MODE == 2 ? a.geo_list[t] : t;
     const DevCloud &c = a.c;
-    const bool geo = GEO && a.geo_pt[i];
+    const bool geo = MODE != 0;
     const double4_32a m = c.ggeo[i];
     double bx[4], by[4], bmax[4], bmin[4];
     ld4(bdq[2 * i], bx);
@@ -434,18 +452,20 @@ __global__ void k_grad(AdjView a, const double4_32a *__restrict__ q, const doubl
                 bwy += bsdy[r] * (qk[r] - qi[r]);
             }
         }
-        atomic_add4(bq + k, bqk);
+        if (STATE) atomic_add4(bq + k, bqk);
         if (geo) {
             double4_32a &ge = a.bedge[e];
             ge.x += bwx;
             ge.y += bwy;
         }
     }
-    atomic_add4(bq + i, bqi);
-    double *bqd = reinterpret_cast<double *>(bq);
-    for (int r = 0; r < 4; r++) {
-        if (bmax[r] != 0.0) atomicAdd(bqd + 4 * (size_t)amax[r] + r, bmax[r]);
-        if (bmin[r] != 0.0) atomicAdd(bqd + 4 * (size_t)amin[r] + r, bmin[r]);
+    if (STATE) {
+        atomic_add4(bq + i, bqi);
+        double *bqd = reinterpret_cast<double *>(bq);
+        for (int r = 0; r < 4; r++) {
+            if (bmax[r] != 0.0) atomicAdd(bqd + 4 * (size_t)amax[r] + r, bmax[r]);
+            if (bmin[r] != 0.0) atomicAdd(bqd + 4 * (size_t)amin[r] + r, bmin[r]);
+        }
     }
     if (geo) {
         double bm[4] = {0, 0, 0, 0};
@@ -1144,30 +1164,27 @@ void flux(const Launch &L, const AdjView &a, const double4_32a *q, const double4
           const double *delta, const double4_32a *flux, const double *sums, const double *ends, long long ns,
           const double4_32a *bF, double4_32a *bq, double4_32a *bdq, double4_32a *bqm, double *bdelta)
 {
-    if (a.bedge)
-        adjk::k_flux<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, sums, ends, ns,
-                                                                             bF, bq, bdq, bqm, bdelta);
-    else
-        adjk::k_flux<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, nullptr, ends,
-                                                                              ns, bF, bq, bdq, bqm, bdelta);
+    adjk::k_flux<0><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, nullptr, ends, ns,
+                                                                       bF, bq, bdq, bqm, bdelta);
+    if (a.bedge && a.n_geo > 0)
+        adjk::k_flux<2><<<adjk::grid_for(a.n_geo, 128), 128, 0, L.stream>>>(a, q, dq, qm, delta, flux, sums, ends, ns,
+                                                                            bF, bq, bdq, bqm, bdelta);
 }
 
 void inner(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *dq_in,
            const double4_32a *bdq_out, double4_32a *bq, double4_32a *bdq_in)
 {
-    if (a.bedge)
-        adjk::k_inner<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq_in, bdq_out, bq, bdq_in);
-    else
-        adjk::k_inner<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq_in, bdq_out, bq, bdq_in);
+    adjk::k_inner<0><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, dq_in, bdq_out, bq, bdq_in);
+    if (a.bedge && a.n_geo > 0)
+        adjk::k_inner<2><<<adjk::grid_for(a.n_geo, 128), 128, 0, L.stream>>>(a, q, dq_in, bdq_out, bq, bdq_in);
 }
 
 void grad(const Launch &L, const AdjView &a, const double4_32a *q, const double4_32a *bdq, const double4_32a *bqm,
           double4_32a *bq)
 {
-    if (a.bedge)
-        adjk::k_grad<true><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, bdq, bqm, bq);
-    else
-        adjk::k_grad<false><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, bdq, bqm, bq);
+    adjk::k_grad<0><<<adjk::grid_for(a.c.n, 128), 128, 0, L.stream>>>(a, q, bdq, bqm, bq);
+    if (a.bedge && a.n_geo > 0)
+        adjk::k_grad<2><<<adjk::grid_for(a.n_geo, 128), 128, 0, L.stream>>>(a, q, bdq, bqm, bq);
 }
 
 void qvars(const Launch &L, int n, const double4_32a *P, const double4_32a *bq, double4_32a *bP)

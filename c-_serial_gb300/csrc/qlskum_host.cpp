@@ -2801,6 +2801,8 @@ struct AdjBuf {
     double2 *bnrm = nullptr;
     double4_32a *bgmom = nullptr, *bfmom = nullptr;
     uint8_t *geo_pt = nullptr;              // AdjView::geo_pt
+    int *geo_list = nullptr;                // AdjView::geo_list
+    int n_geo = 0;
     double *gbx = nullptr, *gby = nullptr;  // coordinate bars (geom_pullback)
     double2 *gbn = nullptr;                 // normal bars (geom_pullback)
     // the checkpointed primal: the state of every stride-th iteration, and
@@ -3060,7 +3062,28 @@ qlskum_status adj_alloc(qlskum_handle *h, bool geo, bool need64, bool need32)
     }
     // padding rows stay zero (and finite) in every buffer
     for (auto *p : a->P) zero(h, p, sizeof(double4_32a) * np);
-    if (geo) adjl::mark_geo_points(h->L, h->dc, a->geo_pt);
+    if (geo) {
+        // the points whose geometry depends on a wall point, marked on the
+        // device and listed on the host
+        adjl::mark_geo_points(h->L, h->dc, a->geo_pt);
+        std::vector<uint8_t> mark(h->n);
+        CK(h, cudaMemcpyAsync(mark.data(), a->geo_pt, h->n, cudaMemcpyDeviceToHost, h->L.stream));
+        CK(h, cudaStreamSynchronize(h->L.stream));
+        std::vector<int> list;
+        for (int i = 0; i < h->n; i++)
+            if (mark[i]) list.push_back(i);
+        a->n_geo = (int)list.size();
+        a->geo_list = a->arena.alloc<int>(std::max<size_t>(list.size(), 1));
+        if (a->arena.err != cudaSuccess) {
+            qlskum_status st = fail(h, QLSKUM_ERR_CUDA, fmt("adjoint cudaMalloc: %s", cudaGetErrorString(a->arena.err)));
+            adj_free(h);
+            return st;
+        }
+        if (!list.empty())
+            CK(h, cudaMemcpyAsync(a->geo_list, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice,
+                                  h->L.stream));
+        CK(h, cudaStreamSynchronize(h->L.stream));
+    }
     if (need32) {
         qlskum_status st = adj_transpose(h);
         if (st) adj_free(h);
@@ -3076,6 +3099,8 @@ AdjView adj_view(qlskum_handle *h, bool geo)
     AdjBuf *a = h->adj;
     if (geo && a->geo) {
         v.geo_pt = a->geo_pt;
+        v.geo_list = a->geo_list;
+        v.n_geo = a->n_geo;
         v.bedge = a->bedge;
         v.bdist = a->bdist;
         v.bnrm = a->bnrm;

@@ -181,6 +181,10 @@ struct AdjView {
     // wall points and the points with a wall neighbour), 0 elsewhere; the
     // kernels accumulate geometry bars only there
     const uint8_t *geo_pt = nullptr;
+    // the same points as a list (device order indices), for the kernels
+    // that accumulate geometry bars over those points alone
+    const int *geo_list = nullptr;
+    int n_geo = 0;
     double4_32a *bedge = nullptr;
     double *bdist = nullptr;
     double2 *bnrm = nullptr;
