@@ -177,6 +177,8 @@ __device__ __forceinline__ void grad_point(const DevCloud &c, int i, const float
     float min_dt = 1.0f;
     const int nb = c.nbhs[i];
     const long long base = c.slice_base[i >> 5] + (i & 31);
+    // two edges per trip: their index loads and gathers are issued together
+#pragma unroll 2
     for (int j = sub; j < nb; j += L) {
         const long long e = base + 32LL * j;
         const int k = __ldcs(c.e_nbr + e);
