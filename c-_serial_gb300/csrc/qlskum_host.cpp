@@ -607,6 +607,7 @@ qlskum_status check_status(qlskum_handle *h)
 
 struct Geometry {
     int n = 0, np = 0, nslices = 0, shape_points = 0;
+    size_t ne = 0;                             // edge slots of the sliced-ELL arrays
     std::vector<int> perm, iperm;
     Precomp pc;
     DevCloud dc;
@@ -693,6 +694,7 @@ qlskum_status build_geometry(const qlskum_cloud *c, const qlskum_params *p, int 
         tot += 32LL * w;
     }
     const size_t ne = (size_t)std::max(tot, 32LL);
+    G.ne = ne;
     std::vector<int> e_nbr(ne, 0);
     std::vector<double4_32a> e_geo(ne, make_double4_32a(0, 0, 0, 0));
     std::vector<double2> e_sn(ne, make_double2(0, 0));
@@ -1457,8 +1459,8 @@ struct qlskum_batch {
     qlskum_params prm{};
     std::vector<Geometry> geo;                 // per cloud
     std::vector<BatchCase> cases;
-    std::vector<BatchTile> tiles[3];
     DeviceArena arena;
+    DevCloud sc;                               // the cases' concatenated cloud
     BatchView view;
     Launch L;
     long long launches = 0;
@@ -1468,13 +1470,13 @@ struct qlskum_batch {
     float4 *dq[3] = {nullptr, nullptr, nullptr};  // as State32::dq
     float4 *qm = nullptr;
     float *delta = nullptr, *cspeed = nullptr;
-    double *psum = nullptr, *pmax = nullptr;   // per flux tile
+    double *psum = nullptr, *pmax = nullptr;   // per flux block
     int *d_iter = nullptr, *d_status = nullptr;
     double *res_old = nullptr, *res_new = nullptr, *hist = nullptr;
     int capacity = 0;
     double *d_obj = nullptr, *d_obj_scratch = nullptr, *d_entropy = nullptr;
     int pcur = 0;
-    int tile = 128, flux_variant = 0;
+    int flux_variant = 0;                      // the single-cloud flux variants (mixed::flux_update)
     bool tuned = false, derived_valid = false;
     int it = 0;
     float cfl = 0.f;
@@ -1498,24 +1500,27 @@ qlskum_status bfail(qlskum_batch *b, qlskum_status s, const std::string &msg)
     } while (0)
 
 
+// Points of each flux block of a variant (its threads over its lanes per point).
+int batch_flux_points(int v) { return mixed::flux_block(v) / mixed::flux_lanes(v); }
+
 void batch_enqueue_iteration(qlskum_batch *b, int o)
 {
     const int x = (o + 1) % 3, y = (o + 2) % 3;
     const int dst[4] = {x, y, x, y};
     const int src[4] = {o, x, y, x};
     const int ni = b->prm.inner_iterations;
+    const Reduce R{b->psum, b->pmax};
+    const Reduce none{nullptr, nullptr};
     for (int rk = 1; rk <= 4; rk++) {
         const int qa = (rk - 1) & 1, qb = rk & 1;
-        mixed::batch_q_derivatives(b->L, b->view, b->tile, b->q[qa], b->dq[0], b->qm, b->cspeed,
-                                   rk == 1 ? b->delta : nullptr, b->cfl);
+        mixed::q_derivatives(b->L, b->sc, b->q[qa], b->dq[0], b->qm, b->cspeed, rk == 1 ? b->delta : nullptr, b->cfl);
         for (int j = 0; j < ni; j++)
-            mixed::batch_q_inner(b->L, b->view, b->tile, b->dq[0], b->dq[mixed_dq_in(j)], b->dq[mixed_dq_out(j)]);
-        mixed::batch_flux_update(b->L, b->view, b->flux_variant, b->q[qa], b->dq[mixed_dq_final(ni)], b->qm, b->delta,
-                                 b->prim[src[rk - 1]], b->prim[o], b->prim[dst[rk - 1]], b->q[qb],
-                                 rk == 4 ? b->cspeed : nullptr, rk, rk == 4 ? b->psum : nullptr,
-                                 rk == 4 ? b->pmax : nullptr);
+            mixed::q_inner(b->L, b->sc, b->dq[0], b->dq[mixed_dq_in(j)], b->dq[mixed_dq_out(j)]);
+        mixed::flux_update(b->L, b->sc, b->cases[0].K, b->q[qa], b->dq[mixed_dq_final(ni)], b->qm, b->delta,
+                           b->prim[src[rk - 1]], b->prim[o], b->prim[dst[rk - 1]], b->q[qb],
+                           rk == 4 ? b->cspeed : nullptr, rk, rk == 4 ? R : none, b->flux_variant);
     }
-    mixed::batch_reduce(b->L, b->view, mixed::batch_flux_tile(b->flux_variant), b->psum, b->pmax, b->d_iter, b->res_old,
+    mixed::batch_reduce(b->L, b->view, batch_flux_points(b->flux_variant), b->psum, b->pmax, b->d_iter, b->res_old,
                         b->res_new, b->hist, b->capacity, b->d_status);
 }
 
@@ -1544,14 +1549,15 @@ qlskum_status batch_ensure_hist(qlskum_batch *b, int needed)
     return QLSKUM_OK;
 }
 
-// Batch autotuner: points per tile of the gradient / inner-loop kernels and
-// the shape of the flux kernel, each timed over three launches on the batch.
+// Batch autotuner: threads per block and lanes per point of the gradient /
+// inner-loop kernels and the shape of the flux kernel (the single-cloud
+// variants), each timed over three launches on the concatenated cloud.
 qlskum_status batch_tune(qlskum_batch *b)
 {
     if (b->tuned) return QLSKUM_OK;
     b->tuned = true;
     if (b->prm.block_size != 0) {
-        b->tile = b->prm.block_size == 64 || b->prm.block_size == 256 ? b->prm.block_size : 128;
+        b->L.block = b->prm.block_size == 64 || b->prm.block_size == 256 ? b->prm.block_size : 128;
         return QLSKUM_OK;
     }
     cudaEvent_t e0, e1;
@@ -1568,27 +1574,29 @@ qlskum_status batch_tune(qlskum_batch *b)
         return ms;
     };
     const long long l0 = b->launches;
-    // gradient / inner-loop kernels: points per tile x lanes per point, timed
+    // gradient / inner-loop kernels: threads per block x lanes per point, timed
     // as an iteration weighs them (one gradient and inner_iterations inner steps)
     float best = 1e30f;
     const int ni = std::max(1, b->prm.inner_iterations);
     for (int t : {64, 128, 256})
         for (int ln : {1, 2, 4}) {
             Launch L = b->L;
+            L.block = t;
             L.lanes = ln;
+            L.staged = 0;
             const float ms =
-                ni * time3([&] { mixed::batch_q_inner(L, b->view, t, b->dq[0], b->dq[0], b->dq[1]); }) +
-                time3([&] { mixed::batch_q_derivatives(L, b->view, t, b->q[0], b->dq[0], b->qm, b->cspeed, nullptr,
-                                                       b->cfl); });
-            if (ms < best) { best = ms; b->tile = t; b->L.lanes = ln; }
+                ni * time3([&] { mixed::q_inner(L, b->sc, b->dq[0], b->dq[0], b->dq[1]); }) +
+                time3([&] { mixed::q_derivatives(L, b->sc, b->q[0], b->dq[0], b->qm, b->cspeed, nullptr, b->cfl); });
+            if (ms < best) { best = ms; b->L.block = t; b->L.lanes = ln; }
         }
     const int o = b->pcur, x = (o + 1) % 3;
-    mixed::batch_q_derivatives(b->L, b->view, b->tile, b->q[0], b->dq[0], b->qm, b->cspeed, b->delta, b->cfl);
+    mixed::q_derivatives(b->L, b->sc, b->q[0], b->dq[0], b->qm, b->cspeed, b->delta, b->cfl);
     best = 1e30f;
-    for (int v = 0; v < mixed::batch_flux_variants(); v++) {
+    const Reduce none{nullptr, nullptr};
+    for (int v = 0; v < mixed::flux_variants(); v++) {
         float ms = time3([&] {
-            mixed::batch_flux_update(b->L, b->view, v, b->q[0], b->dq[0], b->qm, b->delta, b->prim[o], b->prim[o],
-                                     b->prim[x], b->q[1], nullptr, 1, nullptr, nullptr);
+            mixed::flux_update(b->L, b->sc, b->cases[0].K, b->q[0], b->dq[0], b->qm, b->delta, b->prim[o],
+                               b->prim[o], b->prim[x], b->q[1], nullptr, 1, none, v);
         });
         if (ms < best) { best = ms; b->flux_variant = v; }
     }
@@ -1648,7 +1656,8 @@ qlskum_status qlskum_batch_create(const qlskum_cloud *clouds, int n_clouds, cons
         b->geo[k].pc = Precomp();
         std::vector<int>().swap(b->geo[k].perm);
     }
-    // cases, state offsets and the tile tables of the three tile sizes
+    // cases and their offsets in the concatenated cloud (multiples of
+    // kBatchAlign), the flux blocks of each case per block size
     long long off = 0;
     b->cases.resize(n_cases);
     for (int c = 0; c < n_cases; c++) {
@@ -1656,7 +1665,12 @@ qlskum_status qlskum_batch_create(const qlskum_cloud *clouds, int n_clouds, cons
         C.cloud = case_cloud[c];
         C.n = clouds[C.cloud].n;
         C.off = off;
-        off += (C.n + 31) / 32 * 32;
+        off += (C.n + kBatchAlign - 1) / kBatchAlign * kBatchAlign;
+        const int bsz[3] = {64, 128, 256};
+        for (int t = 0; t < 3; t++) {
+            C.blk0[t] = (int)(C.off / bsz[t]);
+            C.nblk[t] = (C.n + bsz[t] - 1) / bsz[t];
+        }
         CaseConst &K = C.K;
         K.pi = 4 * std::atan(1.0);
         K.rho_inf = 1.0;
@@ -1669,21 +1683,104 @@ qlskum_status qlskum_batch_create(const qlskum_cloud *clouds, int n_clouds, cons
         K.cfl = params->cfl;
     }
     b->total = off;
-    const int tsz[3] = {64, 128, 256};
-    for (int ti = 0; ti < 3; ti++) {
-        for (int c = 0; c < n_cases; c++) {
-            BatchCase &C = b->cases[c];
-            C.tile0[ti] = (int)b->tiles[ti].size();
-            for (int f = 0; f < C.n; f += tsz[ti]) b->tiles[ti].push_back(BatchTile{c, f});
-            C.ntl[ti] = (int)b->tiles[ti].size() - C.tile0[ti];
-        }
+    if (off > 0x7fffffffLL / 4)
+        return cleanup(QLSKUM_ERR_INVALID, fmt("batch of %lld points: more than the 32-bit point index allows", off));
+    const bool unit_w = params->power == 0.0;
+    // the concatenated cloud: per point (padding: interior, no neighbours)
+    const long long T_pts = off, nsl = off / 32;
+    long long ne_tot = 0;
+    std::vector<long long> e_off(n_cases);
+    for (int c = 0; c < n_cases; c++) {
+        e_off[c] = ne_tot;
+        ne_tot += (long long)b->geo[b->cases[c].cloud].ne;
     }
-    std::vector<DevCloud> dcs(n_clouds);
-    for (int k = 0; k < n_clouds; k++) dcs[k] = b->geo[k].dc;
-    DevCloud *d_clouds = A.alloc<DevCloud>(n_clouds);
+    int8_t *s_flag = A.alloc<int8_t>(T_pts);
+    int *s_nb = A.alloc<int>(T_pts);
+    double2 *s_nrm = A.alloc<double2>(T_pts);
+    float *s_eps = A.alloc<float>(T_pts);
+    long long *s_sb = A.alloc<long long>(nsl);
+    int *s_case = A.alloc<int>(nsl);
+    CaseConst *s_k = A.alloc<CaseConst>(n_cases);
+    int *s_enbr = A.alloc<int>(ne_tot);
+    uint8_t *s_edir = A.alloc<uint8_t>(ne_tot);
+    float2 *s_exy = unit_w ? A.alloc<float2>(ne_tot) : nullptr;
+    float4 *s_egeo = unit_w ? nullptr : A.alloc<float4>(ne_tot);
+    float *s_edist = A.alloc<float>(ne_tot);
+    float2 *s_ew = A.alloc<float2>(ne_tot), *s_ewb = A.alloc<float2>(ne_tot), *s_egw = A.alloc<float2>(ne_tot);
+    if (A.err != cudaSuccess) return cleanup(QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(A.err)));
+    {
+        cudaStream_t s = b->L.stream;
+        std::vector<long long> sb(nsl);
+        std::vector<int> sc(nsl);
+        int max_nb = 0;
+        for (int c = 0; c < n_cases; c++) {
+            const BatchCase &C = b->cases[c];
+            const Geometry &G = b->geo[C.cloud];
+            const DevCloud &d = G.dc;
+            max_nb = std::max(max_nb, d.max_nb);
+            std::vector<long long> csb(G.nslices);
+            cudaMemcpy(csb.data(), d.slice_base, sizeof(long long) * G.nslices, cudaMemcpyDeviceToHost);
+            const long long s0 = C.off / 32, s1 = (C.off + (C.n + kBatchAlign - 1) / kBatchAlign * kBatchAlign) / 32;
+            for (long long t = s0; t < s1; t++) {
+                sb[t] = e_off[c] + (t - s0 < G.nslices ? csb[t - s0] : 0);
+                sc[t] = c;
+            }
+        }
+        cudaMemsetAsync(s_flag, kInterior, sizeof(int8_t) * T_pts, s);
+        cudaMemsetAsync(s_nb, 0, sizeof(int) * T_pts, s);
+        cudaMemsetAsync(s_eps, 0, sizeof(float) * T_pts, s);
+        mixed::batch_fill_normals(b->L, s_nrm, T_pts);
+        for (int c = 0; c < n_cases; c++) {
+            const BatchCase &C = b->cases[c];
+            const Geometry &G = b->geo[C.cloud];
+            const DevCloud &d = G.dc;
+            const size_t np = (size_t)G.n, ne = G.ne, e0 = (size_t)e_off[c], p0 = (size_t)C.off;
+            auto cp = [&](auto *dst, const auto *src, size_t cnt) {
+                cudaMemcpyAsync(dst, src, sizeof(*src) * cnt, cudaMemcpyDeviceToDevice, s);
+            };
+            cp(s_flag + p0, d.flag, np);
+            cp(s_nb + p0, d.nbhs, np);
+            cp(s_nrm + p0, d.nrm, np);
+            cp(s_eps + p0, d.eps2_32, np);
+            mixed::batch_offset_nbr(b->L, d.e_nbr, s_enbr + e0, (long long)ne, (int)C.off);
+            cp(s_edir + e0, d.e_dir, ne);
+            if (unit_w) cp(s_exy + e0, d.e_xy32, ne);
+            else cp(s_egeo + e0, d.e_geo32, ne);
+            cp(s_edist + e0, d.e_dist32, ne);
+            cp(s_ew + e0, d.e_w32, ne);
+            cp(s_ewb + e0, d.e_w32b, ne);
+            cp(s_egw + e0, d.e_gw32, ne);
+        }
+        std::vector<CaseConst> ks(n_cases);
+        for (int c = 0; c < n_cases; c++) ks[c] = b->cases[c].K;
+        cudaMemcpyAsync(s_sb, sb.data(), sizeof(long long) * nsl, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(s_case, sc.data(), sizeof(int) * nsl, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(s_k, ks.data(), sizeof(CaseConst) * n_cases, cudaMemcpyHostToDevice, s);
+        ce = cudaStreamSynchronize(s);
+        if (ce == cudaSuccess) ce = cudaGetLastError();
+        if (ce != cudaSuccess) return cleanup(QLSKUM_ERR_CUDA, fmt("batch cloud: %s", cudaGetErrorString(ce)));
+        DevCloud &S = b->sc;
+        S.n = (int)T_pts;
+        S.np = (int)T_pts;
+        S.flag = s_flag;
+        S.nbhs = s_nb;
+        S.slice_base = s_sb;
+        S.e_nbr = s_enbr;
+        S.e_dir = s_edir;
+        S.nrm = s_nrm;
+        S.eps2_32 = s_eps;
+        S.e_xy32 = s_exy;
+        S.e_geo32 = s_egeo;
+        S.e_dist32 = s_edist;
+        S.e_w32 = s_ew;
+        S.e_w32b = s_ewb;
+        S.e_gw32 = s_egw;
+        S.unit_w = unit_w ? 1 : 0;
+        S.max_nb = max_nb;
+        S.case_k = s_k;
+        S.slice_case = s_case;
+    }
     BatchCase *d_cases = A.alloc<BatchCase>(n_cases);
-    BatchTile *d_tiles[3];
-    for (int ti = 0; ti < 3; ti++) d_tiles[ti] = A.alloc<BatchTile>(b->tiles[ti].size());
     const size_t T = (size_t)b->total;
     for (int k = 0; k < 3; k++) b->prim[k] = A.alloc<double4_32a>(T);
     for (int k = 0; k < 2; k++) b->q[k] = A.alloc<float4>(T);
@@ -1691,8 +1788,8 @@ qlskum_status qlskum_batch_create(const qlskum_cloud *clouds, int n_clouds, cons
     b->qm = A.alloc<float4>(2 * T);
     b->delta = A.alloc<float>(T);
     b->cspeed = A.alloc<float>(T);
-    b->psum = A.alloc<double>(b->tiles[0].size());
-    b->pmax = A.alloc<double>(b->tiles[0].size());
+    b->psum = A.alloc<double>(T / 64);
+    b->pmax = A.alloc<double>(T / 64);
     b->d_iter = A.alloc<int>(1);
     b->d_status = A.alloc<int>(1);
     b->res_old = A.alloc<double>(n_cases);
@@ -1704,11 +1801,7 @@ qlskum_status qlskum_batch_create(const qlskum_cloud *clouds, int n_clouds, cons
     b->d_entropy = A.alloc<double>(T);
     if (A.err != cudaSuccess) return cleanup(QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(A.err)));
     cudaStream_t s = b->L.stream;
-    cudaMemcpyAsync(d_clouds, dcs.data(), sizeof(DevCloud) * n_clouds, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(d_cases, b->cases.data(), sizeof(BatchCase) * n_cases, cudaMemcpyHostToDevice, s);
-    for (int ti = 0; ti < 3; ti++)
-        cudaMemcpyAsync(d_tiles[ti], b->tiles[ti].data(), sizeof(BatchTile) * b->tiles[ti].size(),
-                        cudaMemcpyHostToDevice, s);
     // initial_conditions_mod.h:23-37 per case
     std::vector<double4_32a> prim0(T, make_double4_32a(1.0, 0.0, 0.0, 1.0 / 1.4));
     for (const BatchCase &C : b->cases)
@@ -1724,14 +1817,8 @@ qlskum_status qlskum_batch_create(const qlskum_cloud *clouds, int n_clouds, cons
     ce = cudaStreamSynchronize(s);
     if (ce == cudaSuccess) ce = cudaGetLastError();
     if (ce != cudaSuccess) return cleanup(QLSKUM_ERR_CUDA, fmt("batch upload: %s", cudaGetErrorString(ce)));
-    b->view.clouds = d_clouds;
     b->view.cases = d_cases;
     b->view.ncases = n_cases;
-    for (int ti = 0; ti < 3; ti++) {
-        b->view.tiles[ti] = d_tiles[ti];
-        b->view.ntiles[ti] = (int)b->tiles[ti].size();
-    }
-    b->view.unit_w = params->power == 0.0 ? 1 : 0;
     if (batch_ensure_hist(b, 256) != QLSKUM_OK) return cleanup(QLSKUM_ERR_CUDA, b->err);
     *out = b;
     return QLSKUM_OK;
@@ -1759,7 +1846,7 @@ qlskum_status qlskum_batch_run(qlskum_batch *b, int iters)
     qlskum_status st = batch_ensure_hist(b, b->it + iters);
     if (st) return st;
     if (!b->derived_valid) {
-        mixed::batch_derived(b->L, b->view, 128, b->prim[b->pcur], b->q[0], b->cspeed);
+        mixed::derived(b->L, b->sc, b->prim[b->pcur], b->q[0], b->cspeed);
         b->derived_valid = true;
         st = batch_tune(b);
         if (st) return st;
@@ -1858,7 +1945,7 @@ qlskum_status qlskum_batch_lanes(const qlskum_batch *b, int *point_lanes, int *f
 {
     if (!b) return QLSKUM_ERR_INVALID;
     if (point_lanes) *point_lanes = b->L.lanes;
-    if (flux_lanes) *flux_lanes = mixed::batch_flux_lanes(b->flux_variant);
+    if (flux_lanes) *flux_lanes = mixed::flux_lanes(b->flux_variant);
     return QLSKUM_OK;
 }
 
@@ -1868,9 +1955,10 @@ qlskum_status qlskum_batch_set_launch_config(qlskum_batch *b, int tile, int poin
     if (tile != 64 && tile != 128 && tile != 256) return bfail(b, QLSKUM_ERR_INVALID, "tile must be 64, 128 or 256");
     if (point_lanes != 1 && point_lanes != 2 && point_lanes != 4)
         return bfail(b, QLSKUM_ERR_INVALID, "point_lanes must be 1, 2 or 4");
-    if (flux_variant < 0 || flux_variant >= mixed::batch_flux_variants())
-        return bfail(b, QLSKUM_ERR_INVALID, fmt("flux_variant not in 0..%d", mixed::batch_flux_variants() - 1));
-    b->tile = tile;
+    if (flux_variant < 0 || flux_variant >= mixed::flux_variants())
+        return bfail(b, QLSKUM_ERR_INVALID, fmt("flux_variant not in 0..%d", mixed::flux_variants() - 1));
+    b->L.block = tile;
+    b->L.staged = 0;
     b->L.lanes = point_lanes;
     b->flux_variant = flux_variant;
     b->tuned = true;
@@ -1888,10 +1976,10 @@ qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_ti
                                   int *points_per_warp)
 {
     if (!b) return QLSKUM_ERR_INVALID;
-    if (tile) *tile = b->tile;
-    if (flux_tile) *flux_tile = mixed::batch_flux_tile(b->flux_variant);
-    if (flux_min_blocks) *flux_min_blocks = mixed::batch_flux_min_blocks(b->flux_variant);
-    if (points_per_warp) *points_per_warp = 32 / mixed::batch_flux_lanes(b->flux_variant);
+    if (tile) *tile = b->L.block;
+    if (flux_tile) *flux_tile = batch_flux_points(b->flux_variant);
+    if (flux_min_blocks) *flux_min_blocks = mixed::flux_min_blocks(b->flux_variant);
+    if (points_per_warp) *points_per_warp = 32 / mixed::flux_lanes(b->flux_variant);
     return QLSKUM_OK;
 }
 

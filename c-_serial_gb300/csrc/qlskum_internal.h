@@ -25,6 +25,8 @@ namespace qlskum {
 enum : int { kWall = 0, kInterior = 1, kOuter = 2 };
 enum : unsigned { kXpos = 1u, kXneg = 2u, kYpos = 4u, kYneg = 8u };
 
+struct CaseConst;
+
 struct DevCloud {
     int n = 0;
     int np = 0;
@@ -72,6 +74,12 @@ struct DevCloud {
     const float2 *e_xy32 = nullptr;
     // largest neighbour count of the cloud (sizes the staged kernels' shared memory)
     int max_nb = 0;
+    // A batch's concatenated cloud (several cases, each its own flight
+    // condition): the free-stream constants of the case that owns slice s
+    // are case_k[slice_case[s]], read by the outer points' far-field state;
+    // NULL for a single case, whose constants come with the launch.
+    const CaseConst *case_k = nullptr;
+    const int *slice_case = nullptr;
 };
 
 // Free-stream constants of one case (parameter_mod.h:4-30).
@@ -82,32 +90,28 @@ struct CaseConst {
 };
 
 // ----------------------------------------------------------------- batches
-// A batch runs many cases (a cloud and a flight condition each) through the
-// same kernels: the state of case c occupies points [off, off + n) of the
-// batch arrays; its geometry is its cloud's DevCloud.  Work is cut into tiles
-// of 64, 128 or 256 points of one case (one thread per point).
-constexpr int tile_index(int tile) { return tile == 64 ? 0 : (tile == 256 ? 2 : 1); }
+// A batch runs many cases (a cloud and a flight condition each) as one
+// concatenated cloud: case c owns points [off, off + n) of it, off a
+// multiple of kBatchAlign, and the points up to the next case are padding
+// (no neighbours, a finite state).  Its per-point and per-edge geometry is
+// its cloud's, with the neighbour indices moved by off, so the single-cloud
+// kernels run every case in one launch each.  Because off is a multiple of
+// every flux block's point count, a block of the flux kernel never spans two
+// cases and case c's residual partials are blocks [blk0, blk0 + nblk).
+constexpr int kBatchAlign = 256;
+constexpr int block_index(int points) { return points == 64 ? 0 : (points == 256 ? 2 : 1); }
 
 struct BatchCase {
     int cloud;
     int n;
     long long off;
-    int tile0[3], ntl[3];                    // first tile and tile count per tile size
+    int blk0[3], nblk[3];                    // first flux block and block count per block size (64, 128, 256 points)
     CaseConst K;
 };
 
-struct BatchTile {
-    int cas;
-    int first;                               // first cloud-local point (a multiple of 32)
-};
-
 struct BatchView {
-    const DevCloud *clouds = nullptr;        // device array [n_clouds]
     const BatchCase *cases = nullptr;        // device array [ncases]
     int ncases = 0;
-    const BatchTile *tiles[3] = {nullptr, nullptr, nullptr};
-    int ntiles[3] = {0, 0, 0};
-    int unit_w = 0;
 };
 
 // FP64 state buffers of one handle.
@@ -341,22 +345,13 @@ int flux_min_blocks(int variant);
 int flux_lanes(int variant);        // lanes per point
 // blocks (residual partials) of one launch of `variant` over n points
 int flux_grid_blocks(int variant, int n);
-// batched (persistent) forms; tile = points per tile, L.lanes lanes per point
-void batch_derived(const Launch &L, const BatchView &B, int tile, const double4_32a *prim, float4 *q, float *cs);
-void batch_q_derivatives(const Launch &L, const BatchView &B, int tile, const float4 *q, float4 *dq, float4 *qm,
-                         const float *cs, float *delta, float cfl);
-void batch_q_inner(const Launch &L, const BatchView &B, int tile, const float4 *dq0, const float4 *dq_in,
-                   float4 *dq_out);
-// batched flux variants: 0..3 one lane per point (points per tile x min blocks
-// 128x4, 128x5, 64x8, 256x2), 4: 64-point tiles with 2 lanes per point, 5: with 4
-int batch_flux_variants();
-int batch_flux_tile(int variant);   // points per tile
-int batch_flux_min_blocks(int variant);
-int batch_flux_lanes(int variant);
-void batch_flux_update(const Launch &L, const BatchView &B, int variant, const float4 *q, const float4 *dq,
-                       const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
-                       double4_32a *prim_next, float4 *q_next, float *cs_next, int rk, double *psum, double *pmax);
-void batch_reduce(const Launch &L, const BatchView &B, int flux_tile, const double *psum, const double *pmax,
+// batches: the concatenated cloud's neighbour lists (dst[j] = src[j] + off
+// for j < ne) and the padding points' normals ((0, 1) for the n points)
+void batch_offset_nbr(const Launch &L, const int *src, int *dst, long long ne, int off);
+void batch_fill_normals(const Launch &L, double2 *nrm, long long n);
+// per case: res_new from the flux kernel's block partials (`points` points per block), the residual
+// history row, the non-finite flag; then the device iteration counter
+void batch_reduce(const Launch &L, const BatchView &B, int points, const double *psum, const double *pmax,
                   int *iter, double *res_old, double *res_new, double *hist, int capacity, int *status);
 }  // namespace mixed
 

@@ -156,10 +156,10 @@ __device__ __forceinline__ float4 edge_w(const DevCloud &c, long long e)
 }
 
 // ----------------------------------------------------------- point bodies
-// One point's work, shared by the single-case kernels and the batched
-// persistent kernels.  Geometry (c) is indexed by the cloud-local point i;
-// the state pointers are already offset to the case's first point, so
-// neighbour indices from the edge list address them directly.
+// One point's work.  Geometry (c) and state are indexed by the point i, and
+// neighbour indices from the edge list address the state directly (a
+// batch's concatenated cloud carries each case's indices moved by its
+// offset).
 
 // q_variables_mod.h:36-118: FP32 differences, weighted by the FP64-folded
 // per-edge solve weights (DevCloud::e_gw32); with DT (the first stage) also
@@ -617,8 +617,10 @@ __device__ __forceinline__ float interior_stage(const float acc[4], float dl, fl
 // with the wall's 2 delta), then the SSPRK stage, q and the wave speed of the
 // new state: interior points by the increment form above; wall and outer
 // points (a few thousand, in warps of their own class) in FP64 as the
-// reference writes it.  Returns res_sqr.
-__device__ __forceinline__ float flux_tail(const CaseConst &K, int i, int f, double2 nn, float nx, float ny,
+// reference writes it, an outer point of a batch with its own case's
+// free-stream constants.  Returns res_sqr.
+__device__ __forceinline__ float flux_tail(const DevCloud &c, const CaseConst &K, int i, int f, double2 nn,
+                                           float nx, float ny,
                                            const float acc[4], const float *__restrict__ delta,
                                            const double4_32a *__restrict__ prim,
                                            const double4_32a *__restrict__ prim_old,
@@ -643,7 +645,10 @@ __device__ __forceinline__ float flux_tail(const CaseConst &K, int i, int f, dou
         double F[4];
 #pragma unroll
         for (int r = 0; r < 4; r++) F[r] = dl * f2d(acc[r]);
-        r2 = d2f(stage_update_fast(K, f, nn.x, nn.y, P, prim_old + i, F, rk));
+        // (two calls, not a reference to either: a pointer to the launch's
+        // constants would copy them to the stack)
+        if (c.case_k) r2 = d2f(stage_update_fast(c.case_k[c.slice_case[i >> 5]], f, nn.x, nn.y, P, prim_old + i, F, rk));
+        else r2 = d2f(stage_update_fast(K, f, nn.x, nn.y, P, prim_old + i, F, rk));
         prim_next[i] = mk4(P);
         q_of(P, Q);
         cs = wave_speed32(P);
@@ -687,8 +692,6 @@ __device__ __forceinline__ void block_sum_max32(float v, double *out_sum, double
         *out_sum = t;
         *out_max = f2d(mm);
     }
-    // a persistent block's next tile writes ss / sm again
-    __syncthreads();
 }
 
 // Fused stage of one point: FP32 edge work with the FP64-folded solve
@@ -744,7 +747,7 @@ __device__ __forceinline__ float flux_point(const DevCloud &c, const CaseConst &
         for (int r = 0; r < 4; r++) acc[r] = group_sum<L>(acc[r], m);
         if (sub != 0) return 0.0f;
     }
-    return flux_tail(K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
+    return flux_tail(c, K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
 }
 
 // The same with the next edge's gathers in flight during the current edge's
@@ -825,7 +828,7 @@ __device__ __forceinline__ float flux_point_st(const DevCloud &c, const CaseCons
         const float e2k = reps[(j & 1) * B + t];
         flux_edge(c, e, f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, w, dir, qk, dxk, dyk, mxk, mnk, e2k, acc);
     }
-    return flux_tail(K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
+    return flux_tail(c, K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
 }
 
 // Neighbour data of one edge end: q, the gradient (x, y) and the neighbour
@@ -912,7 +915,7 @@ __device__ __forceinline__ float flux_point_rp(const DevCloud &c, const CaseCons
         ld4(cur.mn, mnk);
         flux_edge(c, e, f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, w, dir, qk, dxk, dyk, mxk, mnk, cur.e2, acc);
     }
-    return flux_tail(K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
+    return flux_tail(c, K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
 }
 
 // A float4 from shared memory, read again at every use (volatile: not
@@ -998,7 +1001,7 @@ __device__ __forceinline__ float flux_point_rps(const DevCloud &c, const CaseCon
         ld4(cur.mn, mnk);
         flux_edge(c, e, f, nx, ny, qi, dxi, dyi, mxi, mni, e2i, g, w, dir, qk, dxk, dyk, mxk, mnk, cur.e2, acc);
     }
-    return flux_tail(K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
+    return flux_tail(c, K, i, f, nn, nx, ny, acc, delta, prim, prim_old, prim_next, q_next, cs_next, rk, acc_out);
 }
 
 // ---------------------------------------------------- single-case kernels
@@ -1111,134 +1114,23 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_flux_update_rps(DevCloud c, Cas
 }
 
 // ------------------------------------------------------- batched kernels
-// Persistent grids: block b walks tiles b, b + gridDim.x, ...; a tile is
-// TILE consecutive points of one case (one thread per point), so every case
-// of every cloud runs in the same launch.
+// A batch is one concatenated cloud (its cases' points at offsets that are
+// multiples of kBatchAlign), run by the kernels above; these build its edge
+// lists and reduce its residual per case.
 
-template <int TILE>
-__global__ void __launch_bounds__(TILE) kb_derived(const BatchCase *__restrict__ cases,
-                                                   const BatchTile *__restrict__ tiles, int ntiles,
-                                                   const double4_32a *__restrict__ prim, float4 *__restrict__ q,
-                                                   float *__restrict__ cs)
+__global__ void k_batch_offset_nbr(const int *__restrict__ src, int *__restrict__ dst, long long ne, int off)
 {
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const BatchTile T = tiles[t];
-        const BatchCase &C = cases[T.cas];
-        const int i = T.first + threadIdx.x;
-        if (i < C.n) {
-            const long long g = C.off + i;
-            double P[4];
-            float Q[4];
-            ld4(prim[g], P);
-            q_of(P, Q);
-            q[g] = mk4(Q);
-            cs[g] = wave_speed32(P);
-        }
-    }
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < ne) dst[j] = src[j] + off;
 }
 
-// TILE points per tile, L lanes per point: TILE * L threads per block.
-template <int TILE, bool DT, int L = 1>
-__global__ void __launch_bounds__(TILE * L) kb_q_derivatives(const DevCloud *__restrict__ clouds,
-                                                             const BatchCase *__restrict__ cases,
-                                                             const BatchTile *__restrict__ tiles, int ntiles,
-                                                             const float4 *__restrict__ q, float4 *__restrict__ dq,
-                                                             float4 *__restrict__ qm, const float *__restrict__ cs,
-                                                             float *__restrict__ delta, float cfl)
+__global__ void k_batch_fill_normals(double2 *__restrict__ nrm, long long n)
 {
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const BatchTile T = tiles[t];
-        const BatchCase &C = cases[T.cas];
-        const int i = T.first + (int)threadIdx.x / L;
-        if (i < C.n)
-            grad_point<DT, L>(clouds[C.cloud], i, q + C.off, dq + 2 * C.off, qm + 2 * C.off, cs + C.off,
-                              DT ? delta + C.off : nullptr, cfl, (int)threadIdx.x % L);
-    }
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) nrm[i] = make_double2(0.0, 1.0);
 }
 
-template <int TILE, bool UW, int L = 1>
-__global__ void __launch_bounds__(TILE * L) kb_q_inner(const DevCloud *__restrict__ clouds,
-                                                       const BatchCase *__restrict__ cases,
-                                                       const BatchTile *__restrict__ tiles, int ntiles,
-                                                       const float4 *__restrict__ dq0,
-                                                       const float4 *__restrict__ dq_in, float4 *__restrict__ dq_out)
-{
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const BatchTile T = tiles[t];
-        const BatchCase &C = cases[T.cas];
-        const int i = T.first + (int)threadIdx.x / L;
-        if (i < C.n)
-            inner_point<UW, L>(clouds[C.cloud], i, dq0 + 2 * C.off, dq_in + 2 * C.off, dq_out + 2 * C.off,
-                               (int)threadIdx.x % L);
-    }
-}
-
-template <int TILE, int MINB, bool UW, int L = 1>
-__global__ void __launch_bounds__(TILE * L, MINB) kb_flux_update(const DevCloud *__restrict__ clouds,
-                                                             const BatchCase *__restrict__ cases,
-                                                             const BatchTile *__restrict__ tiles, int ntiles,
-                                                             const float4 *__restrict__ q,
-                                                             const float4 *__restrict__ dq,
-                                                             const float4 *__restrict__ qm,
-                                                             const float *__restrict__ delta,
-                                                             const double4_32a *__restrict__ prim,
-                                                             const double4_32a *__restrict__ prim_old,
-                                                             double4_32a *__restrict__ prim_next,
-                                                             float4 *__restrict__ q_next, float *__restrict__ cs_next,
-                                                             int rk, double *__restrict__ psum,
-                                                             double *__restrict__ pmax)
-{
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const BatchTile T = tiles[t];
-        const BatchCase &C = cases[T.cas];
-        const int i = T.first + (int)threadIdx.x / L;
-        float r2 = 0.0f;
-        if (i < C.n) {
-            const long long o = C.off;
-            r2 = flux_point<UW, L>(clouds[C.cloud], C.K, i, q + o, dq + 2 * o, qm + 2 * o, delta + o, prim + o,
-                                   prim_old + o, prim_next + o, q_next + o, cs_next ? cs_next + o : nullptr, rk,
-                                   nullptr, (int)threadIdx.x % L);
-        }
-        if (psum) block_sum_max32<TILE * L>(r2, psum + t, pmax + t);
-    }
-}
-
-// kb_flux_update in the register-prefetch form with the owner's data in
-// shared memory (flux_point_rps; one thread per point).
-template <int TILE, int MINB, bool UW, bool PF>
-__global__ void __launch_bounds__(TILE, MINB) kb_flux_update_rps(const DevCloud *__restrict__ clouds,
-                                                                 const BatchCase *__restrict__ cases,
-                                                                 const BatchTile *__restrict__ tiles, int ntiles,
-                                                                 const float4 *__restrict__ q,
-                                                                 const float4 *__restrict__ dq,
-                                                                 const float4 *__restrict__ qm,
-                                                                 const float *__restrict__ delta,
-                                                                 const double4_32a *__restrict__ prim,
-                                                                 const double4_32a *__restrict__ prim_old,
-                                                                 double4_32a *__restrict__ prim_next,
-                                                                 float4 *__restrict__ q_next,
-                                                                 float *__restrict__ cs_next, int rk,
-                                                                 double *__restrict__ psum, double *__restrict__ pmax)
-{
-    __shared__ float4 sown[5 * TILE];
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const BatchTile T = tiles[t];
-        const BatchCase &C = cases[T.cas];
-        const int i = T.first + (int)threadIdx.x;
-        float r2 = 0.0f;
-        if (i < C.n) {
-            const long long o = C.off;
-            r2 = flux_point_rps<TILE, UW, PF>(clouds[C.cloud], C.K, i, threadIdx.x, sown, q + o, dq + 2 * o,
-                                              qm + 2 * o, delta + o, prim + o, prim_old + o, prim_next + o,
-                                              q_next + o, cs_next ? cs_next + o : nullptr, rk, nullptr);
-        }
-        // (each thread reads and writes only its own shared slots, so the
-        // next tile needs no barrier before reusing them)
-        if (psum) block_sum_max32<TILE>(r2, psum + t, pmax + t);
-    }
-}
-
-// Per case: res_new = sqrt(sum of its tiles' partials) / n, residue against
+// Per case: res_new = sqrt(sum of its flux blocks' partials) / n, residue against
 // res_old latched at iterations 1 and 2 (fpi_solver_mod.h:138-147).
 __global__ void kb_reduce(const BatchCase *__restrict__ cases, int ncases, int ti, const double *__restrict__ psum,
                           const double *__restrict__ pmax, int *iter, double *res_old, double *res_new,
@@ -1249,7 +1141,7 @@ __global__ void kb_reduce(const BatchCase *__restrict__ cases, int ncases, int t
     if (c >= ncases) return;
     const BatchCase &C = cases[c];
     double v = 0.0;
-    for (int t = threadIdx.x; t < C.ntl[ti]; t += 256) v += psum[C.tile0[ti] + t];
+    for (int t = threadIdx.x; t < C.nblk[ti]; t += 256) v += psum[C.blk0[ti] + t];
     ss[threadIdx.x] = v;
     __syncthreads();
     for (int s = 128; s > 0; s >>= 1) {
@@ -1478,144 +1370,24 @@ void flux_update(const Launch &L, const DevCloud &c, const CaseConst &k, const f
 
 // ---------------------------------------------------- batched launchers
 
-template <typename K> static int persistent_grid(K kernel, int block, int ntiles)
+void batch_offset_nbr(const Launch &L, const int *src, int *dst, long long ne, int off)
 {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
-    const int g = sms * (per_sm > 0 ? per_sm : 1);
-    return g < ntiles ? g : (ntiles > 0 ? ntiles : 1);
-}
-
-#define QLSKUM_TILE_SWITCH(TS, ...)                                                            \
-    switch (TS) {                                                                              \
-    case 64: { constexpr int T_ = 64; __VA_ARGS__; } break;                                    \
-    case 256: { constexpr int T_ = 256; __VA_ARGS__; } break;                                  \
-    default: { constexpr int T_ = 128; __VA_ARGS__; } break;                                   \
-    }
-
-void batch_derived(const Launch &L, const BatchView &B, int tile, const double4_32a *prim, float4 *q, float *cs)
-{
-    QLSKUM_TILE_SWITCH(tile, {
-        const int g = persistent_grid(kb_derived<T_>, T_, B.ntiles[tile_index(T_)]);
-        kb_derived<T_><<<g, T_, 0, L.stream>>>(B.cases, B.tiles[tile_index(T_)], B.ntiles[tile_index(T_)], prim, q, cs);
-    })
+    if (ne <= 0) return;
+    k_batch_offset_nbr<<<(unsigned)((ne + 255) / 256), 256, 0, L.stream>>>(src, dst, ne, off);
     QLSKUM_LAUNCHED(L);
 }
 
-#define QLSKUM_LANES_SWITCH(LN, ...)                                                            \
-    switch (LN) {                                                                              \
-    case 4: { constexpr int L_ = 4; __VA_ARGS__; } break;                                      \
-    case 2: { constexpr int L_ = 2; __VA_ARGS__; } break;                                      \
-    default: { constexpr int L_ = 1; __VA_ARGS__; } break;                                     \
-    }
-
-void batch_q_derivatives(const Launch &L, const BatchView &B, int tile, const float4 *q, float4 *dq, float4 *qm,
-                         const float *cs, float *delta, float cfl)
+void batch_fill_normals(const Launch &L, double2 *nrm, long long n)
 {
-    QLSKUM_TILE_SWITCH(tile, QLSKUM_LANES_SWITCH(L.lanes, {
-        const int ti = tile_index(T_);
-        if (delta) {
-            const int g = persistent_grid(kb_q_derivatives<T_, true, L_>, T_ * L_, B.ntiles[ti]);
-            kb_q_derivatives<T_, true, L_><<<g, T_ * L_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti],
-                                                                        q, dq, qm, cs, delta, cfl);
-        } else {
-            const int g = persistent_grid(kb_q_derivatives<T_, false, L_>, T_ * L_, B.ntiles[ti]);
-            kb_q_derivatives<T_, false, L_><<<g, T_ * L_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti],
-                                                                         B.ntiles[ti], q, dq, qm, cs, delta, cfl);
-        }
-    }))
+    if (n <= 0) return;
+    k_batch_fill_normals<<<(unsigned)((n + 255) / 256), 256, 0, L.stream>>>(nrm, n);
     QLSKUM_LAUNCHED(L);
 }
 
-void batch_q_inner(const Launch &L, const BatchView &B, int tile, const float4 *dq0, const float4 *dq_in,
-                   float4 *dq_out)
-{
-    QLSKUM_TILE_SWITCH(tile, QLSKUM_LANES_SWITCH(L.lanes, {
-        const int ti = tile_index(T_);
-        if (B.unit_w) {
-            const int g = persistent_grid(kb_q_inner<T_, true, L_>, T_ * L_, B.ntiles[ti]);
-            kb_q_inner<T_, true, L_><<<g, T_ * L_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], dq0,
-                                                                  dq_in, dq_out);
-        } else {
-            const int g = persistent_grid(kb_q_inner<T_, false, L_>, T_ * L_, B.ntiles[ti]);
-            kb_q_inner<T_, false, L_><<<g, T_ * L_, 0, L.stream>>>(B.clouds, B.cases, B.tiles[ti], B.ntiles[ti],
-                                                                   dq0, dq_in, dq_out);
-        }
-    }))
-    QLSKUM_LAUNCHED(L);
-}
-
-// flux variants: (points per tile, min blocks, lanes per point) = (128,4,1) (128,5,1) (64,8,1) (256,2,1)
-// (64,4,2) (64,2,4); threads per block = points x lanes
-// Batched flux variants: tile, minimum resident blocks, lanes per point;
-// 6..8 the register-prefetch form with the owner's data in shared memory
-// (6 with the neighbour data prefetched, 7 and 8 the edge index and data only).
-const int kBatchFluxVariants = 9;
-static const int kBatchFluxTile[kBatchFluxVariants] = {128, 128, 64, 256, 64, 64, 128, 128, 128};
-static const int kBatchFluxMinB[kBatchFluxVariants] = {4, 5, 8, 2, 4, 2, 5, 6, 7};
-static const int kBatchFluxLanes[kBatchFluxVariants] = {1, 1, 1, 1, 2, 4, 1, 1, 1};
-
-int batch_flux_variants() { return kBatchFluxVariants; }
-int batch_flux_tile(int v) { return kBatchFluxTile[v]; }
-int batch_flux_min_blocks(int v) { return kBatchFluxMinB[v]; }
-int batch_flux_lanes(int v) { return kBatchFluxLanes[v]; }
-
-void batch_flux_update(const Launch &L, const BatchView &B, int variant, const float4 *q, const float4 *dq,
-                       const float4 *qm, const float *delta, const double4_32a *prim, const double4_32a *prim_old,
-                       double4_32a *prim_next, float4 *q_next, float *cs_next, int rk, double *psum, double *pmax)
-{
-#define QLSKUM_BFLUX(T_, MB, LN)                                                                                 \
-    {                                                                                                            \
-        const int ti = tile_index(T_);                                                                           \
-        if (B.unit_w) {                                                                                          \
-            const int g = persistent_grid(kb_flux_update<T_, MB, true, LN>, T_ * LN, B.ntiles[ti]);             \
-            kb_flux_update<T_, MB, true, LN><<<g, T_ * LN, 0, L.stream>>>(                                       \
-                B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq, qm, delta, prim, prim_old, prim_next,       \
-                q_next, cs_next, rk, psum, pmax);                                                                \
-        } else {                                                                                                 \
-            const int g = persistent_grid(kb_flux_update<T_, MB, false, LN>, T_ * LN, B.ntiles[ti]);            \
-            kb_flux_update<T_, MB, false, LN><<<g, T_ * LN, 0, L.stream>>>(                                      \
-                B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq, qm, delta, prim, prim_old, prim_next,       \
-                q_next, cs_next, rk, psum, pmax);                                                                \
-        }                                                                                                        \
-    }
-#define QLSKUM_BFLUX_RPS(T_, MB, PF)                                                                            \
-    {                                                                                                            \
-        const int ti = tile_index(T_);                                                                           \
-        if (B.unit_w) {                                                                                          \
-            const int g = persistent_grid(kb_flux_update_rps<T_, MB, true, PF>, T_, B.ntiles[ti]);              \
-            kb_flux_update_rps<T_, MB, true, PF><<<g, T_, 0, L.stream>>>(                                        \
-                B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq, qm, delta, prim, prim_old, prim_next,       \
-                q_next, cs_next, rk, psum, pmax);                                                                \
-        } else {                                                                                                 \
-            const int g = persistent_grid(kb_flux_update_rps<T_, MB, false, PF>, T_, B.ntiles[ti]);             \
-            kb_flux_update_rps<T_, MB, false, PF><<<g, T_, 0, L.stream>>>(                                       \
-                B.clouds, B.cases, B.tiles[ti], B.ntiles[ti], q, dq, qm, delta, prim, prim_old, prim_next,       \
-                q_next, cs_next, rk, psum, pmax);                                                                \
-        }                                                                                                        \
-    }
-    switch (variant) {
-    case 1: QLSKUM_BFLUX(128, 5, 1); break;
-    case 2: QLSKUM_BFLUX(64, 8, 1); break;
-    case 3: QLSKUM_BFLUX(256, 2, 1); break;
-    case 4: QLSKUM_BFLUX(64, 4, 2); break;
-    case 5: QLSKUM_BFLUX(64, 2, 4); break;
-    case 6: QLSKUM_BFLUX_RPS(128, 5, true); break;
-    case 7: QLSKUM_BFLUX_RPS(128, 6, false); break;
-    case 8: QLSKUM_BFLUX_RPS(128, 7, false); break;
-    default: QLSKUM_BFLUX(128, 4, 1); break;
-    }
-#undef QLSKUM_BFLUX
-#undef QLSKUM_BFLUX_RPS
-    QLSKUM_LAUNCHED(L);
-}
-
-void batch_reduce(const Launch &L, const BatchView &B, int flux_tile, const double *psum, const double *pmax,
+void batch_reduce(const Launch &L, const BatchView &B, int points, const double *psum, const double *pmax,
                   int *iter, double *res_old, double *res_new, double *hist, int capacity, int *status)
 {
-    kb_reduce<<<B.ncases, 256, 0, L.stream>>>(B.cases, B.ncases, tile_index(flux_tile), psum, pmax, iter, res_old,
+    kb_reduce<<<B.ncases, 256, 0, L.stream>>>(B.cases, B.ncases, block_index(points), psum, pmax, iter, res_old,
                                               res_new, hist, capacity, status);
     kb_count<<<1, 1, 0, L.stream>>>(iter);
     if (L.launches) *L.launches += 2;

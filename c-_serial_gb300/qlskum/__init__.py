@@ -455,9 +455,9 @@ class Solver:
 
 
 class Batch:
-    """Many flight conditions over many clouds in one set of persistent,
-    graph-captured launches (mixed precision).  cases: list of
-    (cloud index, mach, aoa)."""
+    """Many flight conditions over many clouds as one concatenated cloud,
+    each kernel one launch over every case, graph-captured (mixed
+    precision).  cases: list of (cloud index, mach, aoa)."""
 
     def __init__(self, clouds, cases, cfl=0.2, vl_const=50.0, power=0.0, inner_iterations=3, block_size=0):
         L = load()
@@ -540,6 +540,9 @@ class Batch:
                 "points_per_warp": v[3].value, "point_lanes": ln[0].value, "flux_lanes": ln[1].value}
 
     def set_launch_config(self, tile, point_lanes, flux_variant):
+        """Pin the launch shape: threads per block (64, 128, 256) and lanes
+        per point of the gradient / inner-loop kernels, and the flux variant
+        (Solver.set_launch_config's numbering)."""
         self._ck(self._L.qlskum_batch_set_launch_config(self._h, int(tile), int(point_lanes), int(flux_variant)))
 
 

@@ -207,11 +207,14 @@ qlskum_status qlskum_get_kernel_timing(qlskum_handle *h, int kernel, double *ms_
 /* ------------------------------------------------------- batched launches */
 
 /* Many flight conditions over many clouds of uneven size, solved together:
- * every kernel of an iteration is one persistent launch over all cases
- * (tiles of one case, walked by a grid sized to the GPU), each iteration's
+ * the cases form one concatenated cloud (each case's points from a multiple
+ * of 256 on, its neighbour lists moved by that offset, its free-stream
+ * constants looked up by its outer points), so every kernel of an iteration
+ * is one launch of the single-cloud kernel over all cases; each iteration's
  * four SSPRK stages are captured once per buffer phase as a CUDA graph and
- * replayed, and the tile size and the register / occupancy shape of the flux
- * kernel are picked by timing the candidates on the batch (autotuner).  The
+ * replayed, and the block size of the gradient / inner-loop kernels and the
+ * flux kernel's variant are picked by timing the candidates on the batch
+ * (autotuner).  The
  * q-LSKUM iteration per case is fpi_solver_mod.h:14-151 in the mixed
  * precision form (params->precision must be QLSKUM_MIXED).
  * Case c solves cloud case_cloud[c] at Mach case_mach[c], AoA case_aoa[c]
@@ -233,17 +236,16 @@ qlskum_status qlskum_batch_residual_history(qlskum_batch *b, double *out, int ma
 long long qlskum_batch_total_points(const qlskum_batch *b);
 long long qlskum_batch_launch_count(const qlskum_batch *b);
 void *qlskum_batch_stream(qlskum_batch *b);
-/* The autotuned launch shape: points per tile of the gradient / inner-loop
- * kernels, points per tile and minimum resident blocks per SM of the flux
+/* The autotuned launch shape: threads per block of the gradient / inner-loop
+ * kernels, points per block and minimum resident blocks per SM of the flux
  * kernel, points per warp of the flux kernel (32 / its lanes per point). */
 qlskum_status qlskum_batch_tuning(const qlskum_batch *b, int *tile, int *flux_tile, int *flux_min_blocks,
                                   int *points_per_warp);
 /* Lanes per point (1, 2 or 4) of the gradient / inner-loop kernels and of the flux kernel. */
 qlskum_status qlskum_batch_lanes(const qlskum_batch *b, int *point_lanes, int *flux_lanes);
-/* Pin the batch's launch shape instead of autotuning it: tile (64, 128, 256
- * points) and lanes per point of the gradient / inner-loop kernels, and the
- * flux variant 0 .. 5 (points per tile x min blocks x lanes: 128x4x1,
- * 128x5x1, 64x8x1, 256x2x1, 64x4x2, 64x2x4). */
+/* Pin the batch's launch shape instead of autotuning it: threads per block
+ * (64, 128, 256) and lanes per point of the gradient / inner-loop kernels,
+ * and the flux variant (0 .. 18, the numbering of qlskum_set_launch_config). */
 qlskum_status qlskum_batch_set_launch_config(qlskum_batch *b, int tile, int point_lanes, int flux_variant);
 
 /* ------------------------------------------- partitions with a ghost-point halo */

@@ -1,9 +1,10 @@
 """Batched launches: several flight conditions over clouds of different size
-in one set of persistent, graph-captured kernels.  Each case must give what a
-single-case mixed-precision solve of the same cloud and condition gives: the
-per-point arithmetic is the same source, so the state agrees to FP32
-rounding (the compiler may fuse a multiply and an add differently in the
-batched kernels); the residual sums run in another order."""
+run as one concatenated cloud by the single-cloud kernels, graph-captured.
+Each case must give what a single-case mixed-precision solve of the same
+cloud and condition gives: with the same launch shape bit for bit (the same
+kernels on the same per-point data, and each case starts on a flux block
+boundary); with the shapes each autotuner picks, to FP32 rounding.  The
+per-case residual sums the same block partials in another order."""
 import numpy as np
 import pytest
 
@@ -86,13 +87,30 @@ def test_batch_rejects_fp64_and_bad_case(qlskum):
     _ = keep
 
 
-@pytest.mark.parametrize("tile,point_lanes,flux_variant", [(64, 2, 4), (128, 4, 5), (256, 2, 0), (64, 4, 1),
-                                                          (128, 1, 6), (128, 2, 7), (64, 1, 8)])
+@pytest.mark.parametrize("variant", [17, 8, 4])
+def test_batch_is_the_single_cloud_iteration(qlskum, variant):
+    """With the same launch shape (the owner-in-shared-memory flux form, the
+    2-lanes-per-point form, the staged form) every case's state after 6
+    iterations equals the single-case solve's bit for bit."""
+    clouds = _clouds()
+    b = qlskum.Batch(clouds, CASES, **KW)
+    b.set_launch_config(128, 1, variant)
+    b.run(6)
+    for k, (ci, mach, aoa) in enumerate(CASES):
+        s = qlskum.Solver(clouds[ci], mach=mach, aoa=aoa, precision=qlskum.MIXED, **KW)
+        s.set_launch_config(variant, 128, 0)
+        s.q_lskum(6)
+        assert np.array_equal(b.prim(k), s.prim), (variant, k)
+        np.testing.assert_allclose(b.residual_history()[:, k], s.residual_history()[:, 0], rtol=1e-12)
+
+
+@pytest.mark.parametrize("tile,point_lanes,flux_variant", [(64, 2, 8), (128, 4, 9), (256, 2, 0), (64, 4, 1),
+                                                          (128, 1, 5), (128, 2, 11), (64, 1, 17), (256, 1, 14)])
 def test_batch_lanes_per_point_match_one_lane(qlskum, tile, point_lanes, flux_variant):
-    """Batched kernels with 2 or 4 lanes per point (gradient / inner loop and
-    flux), and the batched flux forms with the owner's data in shared memory
-    (flux variants 6..8), against the one-lane batch: the same state to FP32
-    rounding."""
+    """Gradient / inner-loop kernels with 2 or 4 lanes per point, and the flux
+    variants (2 and 4 lanes per point, the staged, register-prefetch and
+    owner-in-shared-memory forms), against the one-lane batch: the same
+    state to FP32 rounding."""
     clouds = _clouds()
     a = qlskum.Batch(clouds, CASES[:3], **KW)
     a.set_launch_config(128, 1, 0)
@@ -102,7 +120,7 @@ def test_batch_lanes_per_point_match_one_lane(qlskum, tile, point_lanes, flux_va
     b.run(5)
     t = b.tuning()
     assert t["point_lanes"] == point_lanes and t["tile"] == tile
-    assert t["points_per_warp"] == 32 // {4: 2, 5: 4}.get(flux_variant, 1)
+    assert t["points_per_warp"] == 32 // {8: 2, 9: 4}.get(flux_variant, 1)
     for k in range(3):
         assert _close(b.prim(k), a.prim(k), 1e-5), k
     np.testing.assert_allclose(b.residual_history(), a.residual_history(), rtol=1e-3)
