@@ -104,6 +104,22 @@ def test_batch_is_the_single_cloud_iteration(qlskum, variant):
         np.testing.assert_allclose(b.residual_history()[:, k], s.residual_history()[:, 0], rtol=1e-12)
 
 
+def test_batch_weighted_least_squares_is_the_single_cloud_iteration(qlskum):
+    """Distance-weighted least squares (power -2: the kernels read the
+    weighted edge vectors instead of rotating {delx, dely}), three inner
+    steps: every case equals its single-case solve bit for bit."""
+    clouds = _clouds()
+    kw = dict(KW, power=-2.0, inner_iterations=3)
+    b = qlskum.Batch(clouds, CASES[:3], **kw)
+    b.set_launch_config(128, 1, 17)
+    b.run(5)
+    for k, (ci, mach, aoa) in enumerate(CASES[:3]):
+        s = qlskum.Solver(clouds[ci], mach=mach, aoa=aoa, precision=qlskum.MIXED, **kw)
+        s.set_launch_config(17, 128, 0)
+        s.q_lskum(5)
+        assert np.array_equal(b.prim(k), s.prim), k
+
+
 @pytest.mark.parametrize("tile,point_lanes,flux_variant", [(64, 2, 8), (128, 4, 9), (256, 2, 0), (64, 4, 1),
                                                           (128, 1, 5), (128, 2, 11), (64, 1, 17), (256, 1, 14)])
 def test_batch_lanes_per_point_match_one_lane(qlskum, tile, point_lanes, flux_variant):
