@@ -1719,7 +1719,10 @@ qlskum_status qlskum_batch_create(const qlskum_cloud *clouds, int n_clouds, cons
             const DevCloud &d = G.dc;
             max_nb = std::max(max_nb, d.max_nb);
             std::vector<long long> csb(G.nslices);
-            cudaMemcpy(csb.data(), d.slice_base, sizeof(long long) * G.nslices, cudaMemcpyDeviceToHost);
+            ce = cudaMemcpy(csb.data(), d.slice_base, sizeof(long long) * G.nslices, cudaMemcpyDeviceToHost);
+            if (ce != cudaSuccess)
+                return cleanup(QLSKUM_ERR_CUDA, fmt("batch cloud: slice bases of cloud %d: %s", C.cloud,
+                                                    cudaGetErrorString(ce)));
             const long long s0 = C.off / 32, s1 = (C.off + (C.n + kBatchAlign - 1) / kBatchAlign * kBatchAlign) / 32;
             for (long long t = s0; t < s1; t++) {
                 sb[t] = e_off[c] + (t - s0 < G.nslices ? csb[t - s0] : 0);
