@@ -584,8 +584,8 @@ void unpermute(const qlskum_handle *h, const std::vector<T> &dev, T *out, int wi
 
 qlskum_status print_iters(qlskum_handle *h, int from, int to)
 {
-    std::vector<double> hist((size_t)3 * (to - from));
     if (to <= from) return QLSKUM_OK;
+    std::vector<double> hist((size_t)3 * (size_t)(to - from));
     CK(h, cudaMemcpyAsync(hist.data(), h->R.hist + 3 * (size_t)from, sizeof(double) * hist.size(),
                           cudaMemcpyDeviceToHost, h->L.stream));
     CK(h, cudaStreamSynchronize(h->L.stream));
@@ -2469,7 +2469,12 @@ qlskum_status qlskum_partition_create(const qlskum_cloud *c, const qlskum_params
                 part_free(P);
                 return fail(nullptr, QLSKUM_ERR_CUDA, fmt("cudaMalloc: %s", cudaGetErrorString(d->A.err)));
             }
-            cudaMemcpy(pl.d_src, src.data(), src.size() * sizeof(int), cudaMemcpyHostToDevice);
+            const cudaError_t ce = cudaMemcpy(pl.d_src, src.data(), src.size() * sizeof(int),
+                                              cudaMemcpyHostToDevice);
+            if (ce != cudaSuccess) {
+                part_free(P);
+                return fail(nullptr, QLSKUM_ERR_CUDA, fmt("ghost list upload: %s", cudaGetErrorString(ce)));
+            }
             d->pulls.push_back(pl);
             peer[q][o] = peer[o][q] = 1;
             a = b;
